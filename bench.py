@@ -1,0 +1,428 @@
+#!/usr/bin/env python
+"""Benchmark: texel*view render+adjoint+Adam updates/s, fused batched vs plain, on GB300.
+
+Workload (the uneven batched per-pixel optimisation): 64 seeded synthetic materials,
+resolution drawn from {256, 512, 1024}, 5-16 co-located flash views within +-8 cm at
+25-35 cm, log(1+x) L2 loss, Adam lr 0.01. One *step* is one replay of a CUDA graph of
+100 iterations, each iteration one persistent launch of the fused batched kernel over
+every material. Metric unit: texel*view updates per second = sum(H*W*V) * iterations / s.
+
+Lines printed (rank 0, one JSON line):
+* ``value``: device-resident inputs, CUDA events around K graph replays;
+* ``e2e``: the same job through the public API from pinned host buffers: each step copies
+  the initial maps and the targets host->device, restarts the optimiser, runs the 100
+  iterations and copies the optimised maps and the loss history back;
+* ``roofline``: the batched kernel's algorithmic bytes per launch (params+moments read and
+  written, targets read: sum H*W*(216+12V)) over its average launch time, against the
+  measured HBM copy bandwidth;
+* ``plain`` / ``fused_single``: the unfused single-material GPU form (forward kernel +
+  torch loss + adjoint kernel via autograd + torch.optim.Adam) and the fused single-material
+  kernel, both on the 1024^2, 9-view scene;
+* ``cpu_baseline``: the reference's PyTorch CPU loop (the oracle restatement, same op
+  sequence) on a bounded sample of the workload, all host threads.
+
+``--impl reference`` times only that CPU implementation (rank 0), one step = one
+iteration over the sample.
+
+The inputs are larger than L2 (several GB of targets and state), so no L2 flush is done.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+HERE = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE))
+
+import torch  # noqa: E402
+
+PKG = importlib.import_module("svbrdf-diff-renderer_gb300")
+METRIC = "texel*view render+adjoint+Adam updates/s, fused batched vs plain, 1 GB300"
+UNIT = "texel*view updates/s"
+WORKLOAD = "batched 64 materials, res {256,512,1024}, V 5-16, 100 iterations per graph replay, log1p L2, Adam lr 0.01"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--materials", type=int, default=64)
+    ap.add_argument("--iters", type=int, default=100, help="iterations per step (graph replay)")
+    ap.add_argument("--no-extras", action="store_true", help="skip the plain/single/cpu comparison legs")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline budget")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def shard(costs, world):
+    """Greedy (largest first) assignment of materials to ranks; returns a list per rank."""
+    order = sorted(range(len(costs)), key=lambda i: -costs[i])
+    load = [0.0] * world
+    out = [[] for _ in range(world)]
+    for i in order:
+        r = min(range(world), key=lambda k: (load[k], k))
+        out[r].append(i)
+        load[r] += costs[i]
+    return [sorted(x) for x in out]
+
+
+def workload_specs(n, scene_seed=0):
+    """Resolutions and view counts of the batch, without generating maps."""
+    g = torch.Generator().manual_seed(scene_seed)
+    specs = []
+    for _ in range(n):
+        res = (256, 512, 1024)[int(torch.randint(3, (1,), generator=g))]
+        v = int(torch.randint(5, 17, (1,), generator=g))
+        torch.rand(v, 2, generator=g)  # keep the draw order of scenes.batched_scenes
+        torch.rand(v, 1, generator=g)
+        specs.append((res, v))
+    return specs
+
+
+def gpu_render_fn(dev):
+    def fn(tex, cam, lit, lp, size):
+        r = PKG.Microfacet(tex.shape[-1], cam.shape[0], size, [cam.to(dev), lit.to(dev), lp.to(dev)], dev)
+        with torch.no_grad():
+            return r.eval(tex.to(dev))
+    return fn
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, dev_index=0):
+        self.proc = None
+        self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        sel = []
+        try:
+            uuid = str(torch.cuda.get_device_properties(dev_index).uuid)
+            sel = ["-i", uuid if uuid.startswith("GPU-") else "GPU-" + uuid]
+        except Exception:
+            sel = []
+        self.cmd = ["nvidia-smi", *sel, f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200"]
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(self.cmd, stdout=self.file, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        self.file.flush()
+        self.file.seek(0)
+        rows = [l.strip().split(",") for l in self.file.read().splitlines() if l.strip()]
+        try:
+            os.unlink(self.file.name)
+        except OSError:
+            pass
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            if len(r) < 8:
+                continue
+            try:
+                sm.append(float(r[0]))
+                mx.append(float(r[1]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, r[4:8]):
+                if val.strip().lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    p = HERE / "MEASURED_PEAKS.json"
+    try:
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------- CPU reference (oracle port)
+def cpu_reference_sample(specs_idx, specs, budget_texel_views):
+    """Materials of the workload (in order) up to a texel*view budget, generated on CPU."""
+    from oracle import microfacet_ref as R
+
+    chosen = []
+    tot = 0
+    for i in specs_idx:
+        res, v = specs[i]
+        # 1024^2 materials are left out of the CPU sample: the reference's autograd graph
+        # holds ~60 [V,3,H,W] temporaries, several GB per material at that size
+        if res > 512 or (chosen and tot + res * res * v > budget_texel_views):
+            continue
+        chosen.append(i)
+        tot += res * res * v
+        if tot >= budget_texel_views:
+            break
+    all_sc = PKG.scenes.batched_scenes(n=max(chosen) + 1, render_fn=None)
+    mats = []
+    for i in chosen:
+        sc = all_sc[i]
+        PKG.scenes.add_targets(sc, lambda *a: R.render(*a, dtype=torch.float32))
+        mats.append(sc)
+    return mats, tot
+
+
+class CpuReferenceLoop:
+    """The reference's loop (src/svbrdf.py:48-71) through the oracle's restatement of
+    Microfacet.eval, one torch.optim.Adam per material, on the host cores."""
+
+    def __init__(self, mats, lr=0.01):
+        from oracle import microfacet_ref as R
+
+        self.R = R
+        self.mats = mats
+        self.tex = [m.init.clone().requires_grad_(True) for m in mats]
+        self.opts = [torch.optim.Adam([t], lr=lr, betas=(0.9, 0.999)) for t in self.tex]
+
+    def step(self):
+        for m, t, o in zip(self.mats, self.tex, self.opts):
+            out = self.R.render(t.clamp(-1, 1), m.camera_pos, m.light_pos, m.light_pow, m.size, torch.float32)
+            loss = self.R.image_loss(out, m.targets, "log1p")
+            o.zero_grad()
+            loss.backward()
+            o.step()
+
+
+def run_cpu_baseline(specs, seconds, threads):
+    torch.set_num_threads(threads)
+    mats, tv = cpu_reference_sample(range(len(specs)), specs, budget_texel_views=6e6)
+    loop = CpuReferenceLoop(mats)
+    loop.step()  # warm
+    n, t0 = 0, time.perf_counter()
+    while True:
+        loop.step()
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= seconds or n >= 50:
+            break
+    return {"value": tv * n / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{len(mats)} materials (res <= 512) of the batch ({tv} texel*views), {n} Adam iterations, "
+                      f"reference loop restated in torch (oracle), {threads} threads"}
+
+
+def impl_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    torch.set_num_threads(threads)
+    specs = workload_specs(args.materials)
+    mats, tv = cpu_reference_sample(range(len(specs)), specs, budget_texel_views=1.2e7)
+    loop = CpuReferenceLoop(mats)
+    for _ in range(args.warmup):
+        loop.step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        loop.step()
+    el = time.perf_counter() - t0
+    value = tv * args.steps / el
+    sample = (f"{len(mats)} materials (res <= 512) of the batched workload ({tv} texel*views per step), one Adam iteration per "
+              f"step, reference loop restated in torch (oracle), {threads} threads")
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "sample": sample},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------- GPU legs
+def time_single(dev, fused, iters, res=1024):
+    """Single material 1024^2, 9 views: plain (unfused) or fused kernel, texel*view/s."""
+    sc = PKG.scenes.single_scene(res=res, device=dev, render_fn=gpu_render_fn(dev))
+    r = PKG.Microfacet(res, 9, sc.size, sc.cl, dev)
+    o = PKG.SvbrdfOptim(dev, r, loss="log1p", fused=fused, graph=fused)
+    o.load_targets(sc.targets)
+    o.init_from_tex(sc.init)
+    o.optim(3, 0.01, None, False)  # warm
+    o.init_from_tex(sc.init)
+    o.exp_avg = None
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    o.optim(iters, 0.01, None, False)
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    return {"value": res * res * 9 * iters / el, "unit": UNIT,
+            "workload": f"1 material {res}^2, 9 views, {iters} Adam iterations, log1p L2"
+                        + (", fused kernel in one CUDA graph" if fused else
+                           ", forward kernel + torch loss + adjoint kernel (autograd) + torch.optim.Adam")}
+
+
+def impl_ours(args):
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+    specs = workload_specs(args.materials)
+    costs = [r * r * (v + 3) for r, v in specs]
+    mine = shard(costs, world)[rank]
+    all_sc = PKG.scenes.batched_scenes(n=args.materials, device=dev, render_fn=None)
+    mats = []
+    for i in mine:
+        PKG.scenes.add_targets(all_sc[i], gpu_render_fn(dev))
+        mats.append(all_sc[i])
+    del all_sc
+    opt = PKG.BatchedOptim(mats, lr=0.01, loss="log1p", device=dev, hist_len=args.iters)
+    tv = opt.texel_views()
+    abytes = opt.algorithmic_bytes()
+    opt.capture(args.iters)
+    for _ in range(args.warmup):
+        opt.run(args.iters)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+
+    stream = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        barrier()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            opt.run(args.iters)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+    ms = e0.elapsed_time(e1)
+    clocks = clk.summary()
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t)
+        tvt = torch.tensor([float(tv)], device=dev)
+        dist.all_reduce(tvt)
+        tv_all = float(tvt)
+    else:
+        tv_all = float(tv)
+    value = tv_all * args.iters * args.steps / (ms / 1e3)
+    launch_ms = ms / (args.steps * args.iters)
+    peak, peak_kind = peaks()
+    achieved = abytes / (launch_ms / 1e3) / 1e9
+    traffic = None
+    tfile = HERE / "profiles" / "batched_step_kernel_traffic.json"
+    if tfile.exists():
+        try:
+            tr = json.loads(tfile.read_text())
+            traffic = float(tr["dram_bytes_per_texel_iter_at_mean_v"]) * sum(H * W for H, W, _, _ in opt.meta)
+        except Exception:
+            traffic = None
+
+    # ---- end to end through the public API, host buffers ----
+    h_init = [m.init.detach().cpu().pin_memory() for m in mats]
+    h_tgt = [m.targets.detach().cpu().pin_memory() for m in mats]
+    h_out = [torch.empty(t.shape, dtype=t.dtype).pin_memory() for t in opt.tex]
+    h_loss = torch.empty(opt.loss_hist.shape, dtype=torch.float32).pin_memory()
+    h2d = sum(t.numel() * 4 for t in h_init) + sum(t.numel() * 4 for t in h_tgt)
+    d2h = sum(t.numel() * 4 for t in h_out) + h_loss.numel() * 4
+
+    def e2e_step():
+        opt.reset(inits=h_init, targets=h_tgt)
+        opt.run(args.iters)
+        for i, t in enumerate(opt.tex):
+            h_out[i].copy_(t, non_blocking=True)
+        h_loss.copy_(opt.loss_hist, non_blocking=True)
+
+    e2e_step()
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t)
+    e2e_value = tv_all * args.iters * args.steps / e2e_s
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded materials and flash views)",
+            "config": {"workload": WORKLOAD, "materials": args.materials, "materials_this_rank": len(mats),
+                       "texel_views_per_iteration": tv_all, "iterations_per_step": args.iters,
+                       "batch_config": opt.config.__dict__, "ctas": opt.n_ctas(),
+                       "l2": "inputs larger than L2 (no flush)", "parallelism": f"materials sharded over {world} GPU(s)"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                         "kernel": "batched_step_kernel", "algorithmic_bytes_per_launch": abytes,
+                         "launch_ms": launch_ms},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": args.steps * args.iters,
+            "clocks": clocks}
+    if rank == 0 and not args.no_extras:
+        del opt
+        torch.cuda.empty_cache()
+        line["plain"] = time_single(dev, fused=False, iters=20)
+        line["fused_single"] = time_single(dev, fused=True, iters=200)
+        line["fused_vs_plain"] = value / line["plain"]["value"]
+        if world == 1:
+            line["cpu_baseline"] = run_cpu_baseline(specs, args.cpu_seconds, os.cpu_count() or 1)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return impl_reference(args)
+    return impl_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,148 @@
+/*
+ * svbrdf_gb300.h - C ABI of the GB300 (sm_103a) differentiable SVBRDF renderer.
+ *
+ * Drop-in kernels for the per-pixel hot path of tflsguoyu/svbrdf-diff-renderer:
+ * the flash-lit GGX/Cook-Torrance renderer Microfacet.eval (src/microfacet.py:84-120),
+ * its autograd backward, and the per-pixel Adam loop SvbrdfOptim.optim
+ * (src/svbrdf.py:44-83). The reference is pure Python and has no FFI; these entry
+ * points are what its Python classes call through ctypes.
+ *
+ * Conventions shared by every entry point:
+ *  - All tensor pointers are DEVICE pointers to contiguous FP32 data unless marked HOST.
+ *    textures are planar [9][H][W] (channels 0:3 diffuse, 3:5 normal xy, 5 roughness,
+ *    6:9 specular; the reference's [1,9,H,W], src/microfacet.py:72-77); renders, targets
+ *    and render gradients are planar [V][3][H][W]; camera_pos/light_pos are [V][3] in cm;
+ *    light_pow is [3].
+ *  - `stream` is a cudaStream_t (NULL = the legacy default stream). Every call is
+ *    asynchronous and stream-ordered; no call synchronises the device or allocates memory.
+ *  - Scratch memory ("workspace") is caller-owned. It must be zero-filled once before
+ *    its first use; the library leaves it ready for the next call. Calls that share one
+ *    workspace must be ordered on the same stream.
+ *  - Return value: SVBRDF_OK (0) or a negative SVBRDF_ERR_* code; svbrdf_last_error()
+ *    then returns a message for the calling host thread. The reference instead asserts
+ *    (src/microfacet.py:85-86) or prints and exits (src/svbrdf.py:91-92).
+ */
+#ifndef SVBRDF_GB300_H
+#define SVBRDF_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SVBRDF_ABI_VERSION 1
+
+enum {
+  SVBRDF_OK = 0,
+  SVBRDF_ERR_INVALID = -1,     /* null pointer, bad size, bad enum value */
+  SVBRDF_ERR_UNSUPPORTED = -2, /* e.g. more views than svbrdf_max_views() */
+  SVBRDF_ERR_CUDA = -3,        /* a CUDA runtime call or kernel launch failed */
+  SVBRDF_ERR_WORKSPACE = -4    /* workspace missing or too small */
+};
+
+/* Image loss. MSE is the reference's nn.MSELoss on the gamma-encoded renders
+ * (src/optimization.py:14,28-29). LOG1P is mean((log1p(render)-log1p(target))^2);
+ * LOG1P_PRE is the same with the targets already passed as log1p(target). */
+enum {
+  SVBRDF_LOSS_NONE = -1,
+  SVBRDF_LOSS_MSE = 0,
+  SVBRDF_LOSS_LOG1P = 1,
+  SVBRDF_LOSS_LOG1P_PRE = 2
+};
+
+/* Message for the last failed call on this host thread ("" if none). */
+const char* svbrdf_last_error(void);
+int svbrdf_abi_version(void);
+/* Largest view count a single material may have. */
+int svbrdf_max_views(void);
+/* Workspace bytes for svbrdf_render_fwd / svbrdf_render_bwd / svbrdf_fused_step. */
+size_t svbrdf_workspace_bytes(void);
+
+/* Forward render: out = Microfacet(res, V, size, cl).eval(textures).
+ * Replaces Microfacet.eval, src/microfacet.py:84-120 (construction :10-26 folds into the
+ * arguments). `out` may be NULL when only the loss is wanted. With loss_kind != NONE,
+ * `targets` [V][3][H][W] and `loss_out` (one device float) are required and the mean loss
+ * is written to *loss_out (src/optimization.py:28-29). */
+int svbrdf_render_fwd(const float* textures, const float* camera_pos, const float* light_pos,
+                      const float* light_pow, int n_views, int height, int width, float size,
+                      float* out, const float* targets, int loss_kind, float* loss_out,
+                      void* workspace, size_t workspace_bytes, void* stream);
+
+/* Adjoint of svbrdf_render_fwd: given dL/d(render) `grad_out` [V][3][H][W], writes
+ * dL/d(textures) to `grad_textures` [9][H][W] (overwritten) and, when `grad_light_pow`
+ * is not NULL, dL/d(light_pow) [3] (overwritten). Replaces the autograd graph of
+ * Microfacet.eval (src/microfacet.py:84-120, backward through src/svbrdf.py:70). The
+ * forward terms are recomputed, nothing is saved between the two calls. */
+int svbrdf_render_bwd(const float* textures, const float* camera_pos, const float* light_pos,
+                      const float* light_pow, int n_views, int height, int width, float size,
+                      const float* grad_out, float* grad_textures, float* grad_light_pow,
+                      void* workspace, size_t workspace_bytes, void* stream);
+
+/* One fused iteration of SvbrdfOptim.optim (src/svbrdf.py:56-71): render of
+ * clamp(textures, -1, 1), image loss, adjoint and torch.optim.Adam update
+ * (betas beta1/beta2, eps, no weight decay, 1-based `step` after this update), in one
+ * pass over the texels. textures, exp_avg and exp_avg_sq are updated in place; the mean
+ * loss of the pre-update textures goes to *loss_out. With `light_adam_state` non-NULL the
+ * light power is learnable (src/svbrdf.py:48-50, 58-59): light_pow [3] is then updated in
+ * place by Adam with state light_adam_state [6] = {exp_avg[3], exp_avg_sq[3]}. */
+int svbrdf_fused_step(float* textures, float* exp_avg, float* exp_avg_sq, const float* targets,
+                      const float* camera_pos, const float* light_pos, float* light_pow,
+                      float* light_adam_state, int n_views, int height, int width, float size,
+                      int loss_kind, int step, float lr, float beta1, float beta2, float eps,
+                      float* loss_out, void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---- batched: many materials of uneven resolution and view count in one launch ---- */
+
+/* One material of a batch. Device pointers except camera_pos/light_pos (HOST, read by the
+ * planner only). Each material is what one SvbrdfOptim instance owns. */
+typedef struct svbrdf_material {
+  float* textures;         /* [9][H][W], updated in place */
+  float* exp_avg;          /* [9][H][W] Adam first moment */
+  float* exp_avg_sq;       /* [9][H][W] Adam second moment */
+  const float* targets;    /* [V][3][H][W] */
+  const float* light_pow;  /* [3] */
+  const float* camera_pos; /* HOST [V][3] */
+  const float* light_pos;  /* HOST [V][3] */
+  int n_views;
+  int height;
+  int width;
+  float size;
+} svbrdf_material;
+
+/* Launch shape of the persistent batched kernel (chosen by the autotuner).
+ * threads: 128, 256 or 512. tile_texels: texels per work item, a multiple of threads.
+ * ctas: persistent CTAs (0 = SM count x resident CTAs per SM). */
+typedef struct svbrdf_batch_config {
+  int threads;
+  int tile_texels;
+  int ctas;
+  int reserved;
+} svbrdf_batch_config;
+
+/* Bytes of the plan for this batch (0 on error). */
+size_t svbrdf_batched_plan_bytes(const svbrdf_material* materials, int n_materials,
+                                 const svbrdf_batch_config* config);
+/* Build the plan (material table, views, work list balanced across CTAs) into a HOST
+ * buffer. The caller copies it verbatim into a device buffer of the same size. */
+int svbrdf_batched_plan(const svbrdf_material* materials, int n_materials,
+                        const svbrdf_batch_config* config, void* host_plan, size_t plan_bytes);
+/* Workspace bytes for svbrdf_batched_step with this plan. */
+size_t svbrdf_batched_workspace_bytes(const void* host_plan);
+/* One fused render+adjoint+Adam iteration for every material of the plan, in one
+ * persistent launch (the loop body of src/svbrdf.py:56-71 for each material). All
+ * materials share the Adam hyper-parameters. The step count lives on the device:
+ * `step_counter` (one int, 0 before the first iteration) is read by the launch, which
+ * uses step = *step_counter + 1 and stores it back when done, so a CUDA graph of these
+ * launches can be replayed any number of times. The mean loss of material m for that
+ * step goes to loss_hist[((step - 1) % hist_len) * n_materials + m]. */
+int svbrdf_batched_step(const void* device_plan, const void* host_plan, int loss_kind, int* step_counter,
+                        float lr, float beta1, float beta2, float eps, float* loss_hist, int hist_len,
+                        void* workspace, size_t workspace_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SVBRDF_GB300_H */

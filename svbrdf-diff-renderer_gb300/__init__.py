@@ -1,0 +1,22 @@
+"""GB300-native (sm_103a) differentiable SVBRDF renderer and per-pixel optimiser.
+
+Drop-ins for the hot path of tflsguoyu/svbrdf-diff-renderer:
+
+* ``Microfacet`` - the flash-lit GGX/Cook-Torrance renderer (src/microfacet.py), with a
+  hand-written adjoint behind torch.autograd;
+* ``SvbrdfOptim`` - the per-pixel Adam loop (src/svbrdf.py:15-83) as one fused
+  render+adjoint+Adam kernel per iteration;
+* ``BatchedOptim`` - many materials of uneven size in one persistent launch per iteration.
+
+The package directory name contains hyphens; import it with
+``importlib.import_module("svbrdf-diff-renderer_gb300")``.
+"""
+from . import _native
+from ._native import SvbrdfError, build
+from .batched import BatchConfig, BatchedOptim, autotune
+from .microfacet import Microfacet
+from .svbrdf import SvbrdfOptim
+from . import scenes
+
+__all__ = ["Microfacet", "SvbrdfOptim", "BatchedOptim", "BatchConfig", "autotune", "SvbrdfError", "build", "scenes",
+           "_native"]

@@ -1,0 +1,233 @@
+"""Many materials of uneven resolution and view count, optimised together.
+
+Each material is what one ``SvbrdfOptim`` owns in the reference (src/svbrdf.py:15-83):
+textures, Adam moments, targets and its own views. ``BatchedOptim`` advances all of them
+with one persistent launch of ``svbrdf_batched_step`` per iteration (fused render, loss,
+adjoint and Adam), and ``run(iters)`` captures ``iters`` launches into one CUDA graph.
+
+The launch shape (threads per CTA, texels per work tile, persistent CTA count) comes from
+``autotune``: it times each candidate on the real workload for a few iterations, on copies
+of the state, and caches the winner per workload signature.
+"""
+from __future__ import annotations
+
+import ctypes
+import hashlib
+import json
+import os
+import pathlib
+from dataclasses import dataclass
+from typing import List, Optional, Sequence
+
+import numpy as np
+import torch
+
+from . import _native as N
+
+LOSS_KINDS = {"mse": 0, "log1p": 1, "log1p_pre": 2}
+CANDIDATES = [(t, k) for t in (128, 256, 512) for k in (1, 2, 4, 8, 16)]
+CACHE_FILE = pathlib.Path(os.environ.get("SVBRDF_TUNE_CACHE", str(pathlib.Path.home() / ".cache" / "svbrdf_gb300_tune.json")))
+
+
+@dataclass
+class BatchConfig:
+    threads: int = 256
+    tile_texels: int = 1024
+    ctas: int = 0  # 0 = SM count x resident CTAs per SM
+
+    def as_c(self):
+        return N.svbrdf_batch_config(self.threads, self.tile_texels, self.ctas, 0)
+
+
+class BatchedOptim:
+    """Batched per-pixel optimisation. ``materials`` items need ``init`` ([1,9,H,W]),
+    ``targets`` ([V,3,H,W]), ``camera_pos``/``light_pos`` ([V,3]), ``light_pow`` ([3]) and
+    ``size`` (cm); e.g. ``scenes.Scene`` objects."""
+
+    def __init__(self, materials: Sequence, lr: float = 0.01, loss: str = "log1p", device="cuda",
+                 config: Optional[BatchConfig] = None, betas=(0.9, 0.999), eps: float = 1e-8,
+                 hist_len: int = 100):
+        self.L = N.lib()
+        self.device = torch.device(device)
+        self.lr, self.betas, self.eps = float(lr), betas, float(eps)
+        self.n = len(materials)
+        self.tex, self.m1, self.m2, self.tgt, self.lpow = [], [], [], [], []
+        self.cam_host, self.lit_host, self.meta = [], [], []
+        if loss not in ("mse", "log1p"):
+            raise ValueError("loss must be 'mse' or 'log1p'")
+        self.loss = loss
+        self.kind = LOSS_KINDS["mse"] if loss == "mse" else LOSS_KINDS["log1p_pre"]
+        for m in materials:
+            t = m.init.detach().to(self.device, torch.float32).contiguous().clone()
+            self.tex.append(t)
+            self.m1.append(torch.zeros_like(t))
+            self.m2.append(torch.zeros_like(t))
+            tg = m.targets.to(self.device, torch.float32).contiguous()
+            self.tgt.append(torch.log1p(tg) if loss == "log1p" else tg)
+            self.lpow.append(torch.as_tensor(m.light_pow, dtype=torch.float32).to(self.device).contiguous())
+            self.cam_host.append(np.ascontiguousarray(torch.as_tensor(m.camera_pos).cpu().numpy(), dtype=np.float32))
+            self.lit_host.append(np.ascontiguousarray(torch.as_tensor(m.light_pos).cpu().numpy(), dtype=np.float32))
+            _, _, H, W = t.shape
+            self.meta.append((H, W, int(self.cam_host[-1].shape[0]), float(m.size)))
+        self.hist_len = int(hist_len)
+        self.loss_hist = torch.zeros(self.hist_len, self.n, device=self.device, dtype=torch.float32)
+        self.step_dev = torch.zeros(1, device=self.device, dtype=torch.int32)
+        self.step_count = 0
+        self.graph = None
+        self.config = config or autotune(self)
+        self._build_plan(self.config)
+
+    # ---- work accounting ----
+    def texel_views(self) -> int:
+        return sum(H * W * V for H, W, V, _ in self.meta)
+
+    def algorithmic_bytes(self) -> int:
+        """HBM bytes one iteration must move: params+m+v read and written, targets read."""
+        return sum(H * W * (216 + 12 * V) for H, W, V, _ in self.meta)
+
+    def signature(self) -> str:
+        h = hashlib.sha1(json.dumps(sorted(self.meta)).encode()).hexdigest()[:16]
+        return f"{torch.cuda.get_device_name(self.device)}|{self.loss}|{h}"
+
+    # ---- plan ----
+    def _mat_array(self, tex=None, m1=None, m2=None):
+        tex = tex or self.tex
+        m1 = m1 or self.m1
+        m2 = m2 or self.m2
+        arr = (N.svbrdf_material * self.n)()
+        for i in range(self.n):
+            H, W, V, size = self.meta[i]
+            arr[i] = N.svbrdf_material(tex[i].data_ptr(), m1[i].data_ptr(), m2[i].data_ptr(), self.tgt[i].data_ptr(),
+                                       self.lpow[i].data_ptr(), self.cam_host[i].ctypes.data,
+                                       self.lit_host[i].ctypes.data, V, H, W, size)
+        return arr
+
+    def _make_plan(self, cfg: BatchConfig, tex=None, m1=None, m2=None):
+        arr = self._mat_array(tex, m1, m2)
+        c = cfg.as_c()
+        nbytes = self.L.svbrdf_batched_plan_bytes(arr, self.n, ctypes.byref(c))
+        if nbytes == 0:
+            N.check(-1)
+        host = np.zeros(nbytes, dtype=np.uint8)
+        N.check(self.L.svbrdf_batched_plan(arr, self.n, ctypes.byref(c), host.ctypes.data, nbytes))
+        dev = torch.from_numpy(host).to(self.device)
+        ws_bytes = self.L.svbrdf_batched_workspace_bytes(host.ctypes.data)
+        ws = torch.zeros(int(ws_bytes), dtype=torch.uint8, device=self.device)
+        return host, dev, ws
+
+    def _build_plan(self, cfg: BatchConfig):
+        self.plan_host, self.plan_dev, self.ws = self._make_plan(cfg)
+        self.graph = None
+
+    def n_ctas(self) -> int:
+        return int(np.frombuffer(self.plan_host[:16].tobytes(), dtype=np.int32)[3])
+
+    # ---- stepping ----
+    def _launch(self, plan_host, plan_dev, ws, step_dev, loss_hist):
+        b1, b2 = self.betas
+        N.check(self.L.svbrdf_batched_step(plan_dev.data_ptr(), plan_host.ctypes.data, self.kind,
+                                           step_dev.data_ptr(), self.lr, float(b1), float(b2), self.eps,
+                                           loss_hist.data_ptr(), int(loss_hist.shape[0]), ws.data_ptr(),
+                                           ws.numel(), N.stream_handle(self.device)))
+
+    def step(self):
+        """One iteration for every material (one eager launch). The step count is kept on
+        the device; the losses of this iteration land in ``loss_hist[(step-1) % len]``."""
+        self._launch(self.plan_host, self.plan_dev, self.ws, self.step_dev, self.loss_hist)
+        self.step_count += 1
+
+    @property
+    def loss_out(self) -> torch.Tensor:
+        """Per-material loss of the most recent iteration."""
+        return self.loss_hist[(self.step_count - 1) % self.loss_hist.shape[0]]
+
+    def capture(self, iters: int):
+        """Capture ``iters`` iterations into one CUDA graph. Each replay advances every
+        material by ``iters`` Adam steps (the step counter is device-resident)."""
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            for _ in range(iters):
+                self._launch(self.plan_host, self.plan_dev, self.ws, self.step_dev, self.loss_hist)
+        self.graph, self.graph_iters = g, iters
+        return g
+
+    def run(self, iters: int):
+        """Advance ``iters`` iterations through one CUDA-graph replay (captured on first use)."""
+        if self.graph is None or self.graph_iters != iters:
+            self.capture(iters)
+        self.graph.replay()
+        self.step_count += iters
+
+    def reset(self, inits=None, targets=None):
+        """Restart the optimisation (step 0, zero moments), optionally from new initial maps
+        and targets (host or device tensors; pinned host memory copies asynchronously)."""
+        for i in range(self.n):
+            if inits is not None:
+                self.tex[i].copy_(inits[i], non_blocking=True)
+            if targets is not None:
+                self.tgt[i].copy_(targets[i], non_blocking=True)
+                if self.loss == "log1p":
+                    self.tgt[i].log1p_()
+            self.m1[i].zero_()
+            self.m2[i].zero_()
+        self.step_dev.zero_()
+        self.loss_hist.zero_()
+        self.step_count = 0
+
+    def textures(self, i: int) -> torch.Tensor:
+        return self.tex[i]
+
+
+def _time_config(opt: BatchedOptim, cfg: BatchConfig, iters: int = 3) -> float:
+    tex = [t.clone() for t in opt.tex]
+    m1 = [torch.zeros_like(t) for t in tex]
+    m2 = [torch.zeros_like(t) for t in tex]
+    host, dev, ws = opt._make_plan(cfg, tex, m1, m2)
+    loss = torch.zeros(1, opt.n, device=opt.device)
+    step = torch.zeros(1, device=opt.device, dtype=torch.int32)
+    opt._launch(host, dev, ws, step, loss)  # warm
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(iters):
+        opt._launch(host, dev, ws, step, loss)
+    e.record()
+    e.synchronize()
+    return s.elapsed_time(e) / iters
+
+
+def _load_cache():
+    try:
+        return json.loads(CACHE_FILE.read_text())
+    except Exception:
+        return {}
+
+
+def autotune(opt: BatchedOptim, candidates=None, use_cache: bool = True) -> BatchConfig:
+    """Pick threads/tile_texels/ctas for ``opt``'s workload by timing every candidate."""
+    key = opt.signature()
+    cache = _load_cache() if use_cache else {}
+    if key in cache:
+        return BatchConfig(**cache[key])
+    best, best_ms = None, float("inf")
+    results = []
+    for threads, mult in (candidates or CANDIDATES):
+        for ctas_mult in (0,):
+            cfg = BatchConfig(threads=threads, tile_texels=threads * mult, ctas=ctas_mult)
+            try:
+                ms = _time_config(opt, cfg)
+            except N.SvbrdfError:
+                continue
+            results.append((ms, threads, mult))
+            if ms < best_ms:
+                best, best_ms = cfg, ms
+    opt.tune_results = sorted(results)
+    if best is None:
+        best = BatchConfig()
+    if use_cache:
+        cache[key] = best.__dict__
+        try:
+            CACHE_FILE.parent.mkdir(parents=True, exist_ok=True)
+            CACHE_FILE.write_text(json.dumps(cache, indent=1))
+        except OSError:
+            pass
+    return best

@@ -1,0 +1,323 @@
+// Per-texel forward render, loss, adjoint and Adam update of the flash-lit
+// GGX/Cook-Torrance SVBRDF model.
+//
+// The model is the one of Microfacet.eval (src/microfacet.py:84-120 in
+// tflsguoyu/svbrdf-diff-renderer). Rendered pixel (i, j) of every view depends only
+// on texel (i, j), so one thread owns one texel: it decodes the 9 parameters once,
+// loops over the views keeping every per-view term (v, l, h, D, F, G) in registers,
+// and accumulates the adjoint into a handful of per-texel sums. Nothing per-view is
+// ever written to memory except, in the forward-only kernel, the render itself.
+//
+// Texture layout is the reference's planar [9][H][W] FP32 (channels 0:3 diffuse,
+// 3:5 normal xy, 5 roughness, 6:9 specular; src/microfacet.py:72-77); targets and
+// renders are planar [V][3][H][W].
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace svb {
+
+constexpr float kEps = 1e-6f;                  // Microfacet.eps (src/microfacet.py:14)
+constexpr float kPi = 3.14159265358979323846f;  // np.pi as the FP32 scalar ATen uses
+constexpr float kInvGamma = 1.0f / 2.2f;        // output encode exponent (src/microfacet.py:120)
+constexpr int kMaxViews = 64;
+
+enum LossKind : int {
+  kLossMSE = 0,       // mean((render - target)^2)            (src/optimization.py:14,28-29)
+  kLossLog1p = 1,     // mean((log1p(render) - log1p(target))^2)
+  kLossLog1pPre = 2,  // as kLossLog1p, targets already hold log1p(target)
+};
+
+// One view: camera and light position in cm. `coloc` is 1 when the two are bitwise equal
+// (the reference's flash captures, src/capture.py:70-71); the co-located branch uses
+// l = v and h = v exactly, which is what FP64 evaluation of the reference formula gives.
+struct __align__(16) View {
+  float cx, cy, cz, coloc;
+  float lx, ly, lz, pad;
+};
+
+// ---- fast transcendental helpers (single PTX instructions) ----
+__device__ __forceinline__ float ex2_approx(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float lg2_approx(float x) {
+  float y;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float rcp_approx(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float rsqrt_approx(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float sqrt_approx(float x) {
+  float y;
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// Decoded maps of one texel (tex2map, src/microfacet.py:72-79) plus the factors the
+// adjoint needs to map map-space gradients back to the 9 parameters.
+struct Maps {
+  float d[3];     // diffuse  ((t+1)/2)^2.2
+  float s[3];     // specular ((t+1)/2)^2.2
+  float f1[3];    // d/pi * (1 - s)            (src/microfacet.py:102-103)
+  float r;        // roughness ((t+1)/2)^2.2
+  float alpha;    // r^2 (the reference passes roughness**2 to GGX and Smith)
+  float a2;       // alpha^2                   (src/microfacet.py:30)
+  float k;        // alpha*0.5 + eps            (src/microfacet.py:51)
+  float n[3];     // unit normal               (src/microfacet.py:64-70)
+};
+
+// x = ((t+1)/2)^2.2 and dx/dt = 1.1 * ((t+1)/2)^1.2. A base of 0 gives 0 for both
+// (lg2 -> -inf -> ex2 -> 0), matching pow's value and its ATen gradient at 0.
+__device__ __forceinline__ float decode22(float t, float* dxdt) {
+  const float base = (t + 1.0f) * 0.5f;
+  const float lb = lg2_approx(base);
+  if (dxdt) *dxdt = 1.1f * ex2_approx(1.2f * lb);
+  return ex2_approx(2.2f * lb);
+}
+
+__device__ __forceinline__ void decode(const float t[9], Maps& m) {
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    m.d[c] = decode22(t[c], nullptr);
+    m.s[c] = decode22(t[6 + c], nullptr);
+    m.f1[c] = m.d[c] / kPi * (1.0f - m.s[c]);
+  }
+  m.r = decode22(t[5], nullptr);
+  m.alpha = m.r * m.r;
+  m.a2 = m.alpha * m.alpha;
+  m.k = m.alpha * 0.5f + kEps;
+  // reconstruct_normal: clamp xy, z = sqrt(1 - clamp(x^2+y^2, 0, 1-eps)), normalise
+  const float nx = fminf(fmaxf(t[3], -1.0f), 1.0f);
+  const float ny = fminf(fmaxf(t[4], -1.0f), 1.0f);
+  const float sxy = fminf(fmaxf(nx * nx + ny * ny, 0.0f), 1.0f - kEps);
+  const float nz = sqrtf(1.0f - sxy);
+  const float inv = 1.0f / sqrtf(nx * nx + ny * ny + nz * nz);
+  m.n[0] = nx * inv;
+  m.n[1] = ny * inv;
+  m.n[2] = nz * inv;
+}
+
+// Per-texel adjoint sums over views (all unscaled by the loss normaliser).
+struct Adj {
+  float gf1[3];   // d/d f1_c
+  float gs[3];    // d/d s_c through F
+  float ga2;      // d/d alpha^2 through D
+  float gk;       // d/d k through G
+  float gn[3];    // d/d unit normal
+  float gp[3];    // d/d light power
+};
+
+__device__ __forceinline__ void adj_zero(Adj& a) {
+#pragma unroll
+  for (int c = 0; c < 3; ++c) { a.gf1[c] = 0.f; a.gs[c] = 0.f; a.gn[c] = 0.f; a.gp[c] = 0.f; }
+  a.ga2 = 0.f;
+  a.gk = 0.f;
+}
+
+// Texel position of src/microfacet.py:16-19 in FP32, same operation order.
+__device__ __forceinline__ void texel_pos(int i, int j, int res_w, int res_h, float size, float& px, float& py) {
+  px = (((float)j + 0.5f) / (float)res_w - 0.5f) * size;
+  py = -((((float)i + 0.5f) / (float)res_h - 0.5f) * size);
+}
+
+enum Mode : int { kModeFwd = 0, kModeBwd = 1, kModeFused = 2 };
+
+// One view of one texel. MODE:
+//   kModeFwd   : writes the 3 rendered channels to out[c]; optional loss vs tgt.
+//   kModeBwd   : reads dL/d render from gin[c] and accumulates the adjoint.
+//   kModeFused : reads the target, accumulates the loss, then the adjoint.
+// `io` holds 3 values: the target (fused), the incoming gradient (bwd) or the output (fwd).
+template <int MODE, int LOSS, bool GRAD_POW, bool COLOC>
+__device__ __forceinline__ void texel_view(const Maps& m, float px, float py, const View& vw,
+                                           const float P[3], float io[3], float& loss, Adj& a) {
+  // ---- geometry (get_dir, src/microfacet.py:60-62, 91-93) ----
+  const float vx0 = vw.cx - px, vy0 = vw.cy - py, vz0 = vw.cz;
+  const float qv = vx0 * vx0 + vy0 * vy0 + vz0 * vz0;
+  const float iv = rsqrt_approx(qv);
+  const float vx = vx0 * iv, vy = vy0 * iv, vz = vz0 * iv;
+  float lx, ly, lz, inv_d2, hx, hy, hz;
+  float nv_raw, nl_raw, nh_raw, vh;
+  nv_raw = m.n[0] * vx + m.n[1] * vy + m.n[2] * vz;
+  if (COLOC) {
+    // l == v, h == normalize(2v) == v, v.h == 1
+    lx = vx; ly = vy; lz = vz;
+    hx = vx; hy = vy; hz = vz;
+    inv_d2 = iv * iv;
+    nl_raw = nv_raw;
+    nh_raw = nv_raw;
+    vh = 1.0f;
+  } else {
+    const float lx0 = vw.lx - px, ly0 = vw.ly - py, lz0 = vw.lz;
+    const float d2 = lx0 * lx0 + ly0 * ly0 + lz0 * lz0;
+    const float il = rsqrt_approx(d2);
+    inv_d2 = il * il;
+    lx = lx0 * il; ly = ly0 * il; lz = lz0 * il;
+    const float hx0 = lx + vx, hy0 = ly + vy, hz0 = lz + vz;
+    const float ih = rsqrt_approx(hx0 * hx0 + hy0 * hy0 + hz0 * hz0);
+    hx = hx0 * ih; hy = hy0 * ih; hz = hz0 * ih;
+    nl_raw = m.n[0] * lx + m.n[1] * ly + m.n[2] * lz;
+    nh_raw = m.n[0] * hx + m.n[1] * hy + m.n[2] * hz;
+    vh = fmaxf(vx * hx + vy * hy + vz * hz, 0.0f);
+  }
+  const float nv = fmaxf(nv_raw, 0.0f);
+  const float nl = fmaxf(nl_raw, 0.0f);
+  const float nh = fmaxf(nh_raw, 0.0f);
+
+  // ---- GGX D (src/microfacet.py:28-32) ----
+  const float c2 = nh * nh;
+  const float den = c2 * m.a2 + (1.0f - c2);
+  const float E = kPi * (den * den) + kEps;
+  const float rE = rcp_approx(E);
+  const float D = m.a2 * rE;
+  // ---- Smith G (src/microfacet.py:47-52) ----
+  const float omk = 1.0f - m.k;
+  const float Bv = nv * omk + m.k;
+  const float rBv = rcp_approx(Bv);
+  const float G1v = nv * rBv;
+  float Bl, rBl, G1l;
+  if (COLOC) { Bl = Bv; rBl = rBv; G1l = G1v; }
+  else { Bl = nl * omk + m.k; rBl = rcp_approx(Bl); G1l = nl * rBl; }
+  const float G = G1v * G1l;
+  // ---- Fresnel, spherical-Gaussian Schlick (src/microfacet.py:43-45) ----
+  const float sphg = ex2_approx((-5.55473f * vh - 6.98316f) * vh);
+  // ---- f2 = D F G / (4 nv nl + eps), img = P f nl / d^2 (src/microfacet.py:109-117) ----
+  const float Q = 4.0f * nv * nl + kEps;
+  const float rQ = rcp_approx(Q);
+  const float DGQ = D * G * rQ;
+  const float W = nl * inv_d2;
+
+  float gDGQ = 0.f, gW = 0.f;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const float F = m.s[c] + (1.0f - m.s[c]) * sphg;
+    const float f = m.f1[c] + DGQ * F;
+    const float PW = P[c] * W;
+    const float img = f * PW;
+    const float x = fminf(fmaxf(img, kEps), 1.0f);             // clamp(eps, 1)
+    const float xp = ex2_approx(lg2_approx(x) * (kInvGamma - 1.0f));  // x^(1/2.2 - 1)
+    const float out = x * xp;                                   // x^(1/2.2)
+    float gout;
+    if (MODE == kModeFwd) {
+      if (LOSS >= 0) {
+        float e;
+        if (LOSS == kLossMSE) e = out - io[c];
+        else if (LOSS == kLossLog1p) e = log1pf(out) - log1pf(io[c]);
+        else e = log1pf(out) - io[c];
+        loss += e * e;
+      }
+      io[c] = out;
+      continue;
+    } else if (MODE == kModeBwd) {
+      gout = io[c];
+    } else {
+      float e;
+      if (LOSS == kLossMSE) { e = out - io[c]; gout = e; }
+      else {
+        const float lo = log1pf(out);
+        e = (LOSS == kLossLog1p) ? lo - log1pf(io[c]) : lo - io[c];
+        gout = e * rcp_approx(1.0f + out);
+      }
+      loss += e * e;
+    }
+    // d out / d img = (1/2.2) x^(1/2.2-1) inside [eps, 1] (clamp passes its bounds)
+    const float gimg = (img >= kEps && img <= 1.0f) ? gout * kInvGamma * xp : 0.0f;
+    const float gf = gimg * PW;
+    gW += gimg * (P[c] * f);
+    if (GRAD_POW) a.gp[c] += gimg * f * W;
+    a.gf1[c] += gf;
+    gDGQ += gf * F;
+    a.gs[c] += gf * DGQ * (1.0f - sphg);
+  }
+  if (MODE == kModeFwd) return;
+
+  // ---- adjoint of the shared terms ----
+  float gnl = gW * inv_d2;
+  const float gD = gDGQ * G * rQ;
+  const float gG = gDGQ * D * rQ;
+  const float gQ = -gDGQ * DGQ * rQ;
+  float gnv = gQ * 4.0f * nl;
+  gnl += gQ * 4.0f * nv;
+  const float gG1v = gG * G1l;
+  const float gG1l = gG * G1v;
+  gnv += gG1v * m.k * rBv * rBv;
+  gnl += gG1l * m.k * rBl * rBl;
+  a.gk -= gG1v * nv * (1.0f - nv) * rBv * rBv + gG1l * nl * (1.0f - nl) * rBl * rBl;
+  const float t2 = D * rE * (2.0f * kPi) * den;
+  a.ga2 += gD * (rE - t2 * c2);
+  float gnh = -gD * t2 * (m.a2 - 1.0f) * 2.0f * nh;
+  // clamp(min=0) of the dot products passes the gradient where the dot is >= 0
+  if (COLOC) {
+    const float gsum = (nv_raw >= 0.0f) ? (gnv + gnl + gnh) : 0.0f;
+    a.gn[0] += gsum * vx; a.gn[1] += gsum * vy; a.gn[2] += gsum * vz;
+  } else {
+    gnv = (nv_raw >= 0.0f) ? gnv : 0.0f;
+    gnl = (nl_raw >= 0.0f) ? gnl : 0.0f;
+    gnh = (nh_raw >= 0.0f) ? gnh : 0.0f;
+    a.gn[0] += gnv * vx + gnl * lx + gnh * hx;
+    a.gn[1] += gnv * vy + gnl * ly + gnh * hy;
+    a.gn[2] += gnv * vz + gnl * lz + gnh * hz;
+  }
+}
+
+// Map the per-texel adjoint sums back to the 9 texture parameters (tex2map and
+// reconstruct_normal reversed). `scale` is the loss normaliser's factor (2/N).
+__device__ __forceinline__ void adj_to_params(const float t[9], const Maps& m, const Adj& a, float scale,
+                                              float g[9]) {
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    float dd, ds;
+    decode22(t[c], &dd);
+    decode22(t[6 + c], &ds);
+    const float gd = a.gf1[c] * (1.0f - m.s[c]) / kPi;
+    const float gs = a.gs[c] - a.gf1[c] * m.d[c] / kPi;
+    g[c] = gd * dd * scale;
+    g[6 + c] = gs * ds * scale;
+  }
+  float dr;
+  decode22(t[5], &dr);
+  const float galpha = a.ga2 * 2.0f * m.alpha + a.gk * 0.5f;
+  g[5] = galpha * 2.0f * m.r * dr * scale;
+  // normal: n = mvec/|mvec|, mvec = (nx, ny, sqrt(1 - clamp(nx^2+ny^2, 0, 1-eps)))
+  const float nx = fminf(fmaxf(t[3], -1.0f), 1.0f);
+  const float ny = fminf(fmaxf(t[4], -1.0f), 1.0f);
+  const float s = nx * nx + ny * ny;
+  const float sxy = fminf(fmaxf(s, 0.0f), 1.0f - kEps);
+  const float nz = sqrtf(1.0f - sxy);
+  const float inv = 1.0f / sqrtf(nx * nx + ny * ny + nz * nz);
+  const float ndg = m.n[0] * a.gn[0] + m.n[1] * a.gn[1] + m.n[2] * a.gn[2];
+  const float gmx = (a.gn[0] - m.n[0] * ndg) * inv;
+  const float gmy = (a.gn[1] - m.n[1] * ndg) * inv;
+  const float gmz = (a.gn[2] - m.n[2] * ndg) * inv;
+  const float gsxy = (s >= 0.0f && s <= 1.0f - kEps) ? (-0.5f * gmz / nz) : 0.0f;
+  const float gnx = gmx + gsxy * 2.0f * nx;
+  const float gny = gmy + gsxy * 2.0f * ny;
+  g[3] = (t[3] >= -1.0f && t[3] <= 1.0f) ? gnx * scale : 0.0f;
+  g[4] = (t[4] >= -1.0f && t[4] <= 1.0f) ? gny * scale : 0.0f;
+}
+
+// torch.optim.Adam's update for one element (amsgrad off, no weight decay):
+//   m.lerp_(g, 1-b1); v.mul_(b2).addcmul_(g, g, 1-b2);
+//   p.addcdiv_(m, sqrt(v)/sqrt(bc2) + eps, -lr/bc1)
+struct AdamScalars {
+  float one_minus_b1, b2, one_minus_b2, inv_bc2_sqrt, eps, neg_step_size;
+};
+
+__device__ __forceinline__ void adam_update(float& p, float& mo, float& vo, float g, const AdamScalars& s) {
+  mo = mo + s.one_minus_b1 * (g - mo);
+  vo = vo * s.b2 + s.one_minus_b2 * (g * g);
+  const float denom = sqrt_approx(vo) * s.inv_bc2_sqrt + s.eps;
+  p = p + s.neg_step_size * __fdividef(mo, denom);
+}
+
+}  // namespace svb

@@ -1,0 +1,193 @@
+"""Drop-in per-pixel optimiser ``SvbrdfOptim`` (src/svbrdf.py:15-83) on the fused kernel.
+
+Same interface as the reference class: ``SvbrdfOptim(device, renderer_obj)``,
+``init_from_tex``, ``init_from_const``, ``init_from_randn``, ``load_targets`` and
+``optim(epochs, lr, svbrdf_obj, optim_light)``.
+
+``optim`` runs ``svbrdf_fused_step`` once per epoch: render of clamp(textures, -1, 1),
+image loss, hand-written adjoint and Adam(lr, betas=(0.9, 0.999)) in a single pass per
+texel (the loop body of src/svbrdf.py:56-71). The per-epoch losses stay on the device
+and are read once at the end (the reference reads them every epoch, src/svbrdf.py:64-66).
+With ``graph=True`` the whole epoch loop is captured once into a CUDA graph and replayed.
+
+Setting ``fused=False`` gives the plain, unfused GPU form instead: the reference's own loop
+(``eval`` -> loss -> ``backward`` -> ``torch.optim.Adam.step``) with the forward and
+adjoint kernels behind ``torch.autograd``.
+"""
+from __future__ import annotations
+
+import pathlib
+from datetime import datetime
+
+import torch
+
+from . import _native as N
+from .microfacet import Microfacet
+
+LOSS_KINDS = {"mse": 0, "log1p": 1, "log1p_pre": 2}
+
+
+class SvbrdfOptim:
+    def __init__(self, device, renderer_obj, loss="mse", fused=True, graph=False, save_process=False):
+        self.device = torch.device(device)
+        self.eps = 1e-4
+        self.renderer_obj = renderer_obj
+        self.res = renderer_obj.res
+        if loss not in ("mse", "log1p"):
+            raise ValueError("loss must be 'mse' or 'log1p'")
+        self.loss = loss
+        self.fused = fused
+        self.graph = graph
+        self.save_process = save_process
+        self.loss_image_list = []
+
+    # ---- init_from_* : src/svbrdf.py:20-39 ----
+    def _leaf(self, t):
+        return t.detach().to(self.device, torch.float32).contiguous().requires_grad_(True)
+
+    def init_from_tex(self, textures):
+        self.textures = self._leaf(textures)
+
+    def init_from_const(self, dif=0.5, spe=0.04, rgh=0.2):
+        r = self.res
+        normal = torch.zeros(1, 2, r, r, device=self.device)
+        diffuse = torch.ones(1, 3, r, r, device=self.device) * dif * 2 - 1
+        specular = torch.ones(1, 3, r, r, device=self.device) * spe * 2 - 1
+        roughness = torch.ones(1, 1, r, r, device=self.device) * rgh * 2 - 1
+        self.textures = self._leaf(torch.cat((diffuse, normal, roughness, specular), 1))
+
+    def init_from_randn(self, dif=0.5, spe=0.04, rgh=0.2):
+        r = self.res
+        normal = (torch.randn(1, 2, r, r, device=self.device) / 4).clamp(-1, 1)
+        diffuse = (torch.randn(1, 3, r, r, device=self.device) / 8 + dif).clamp(0, 1) * 2 - 1
+        specular = (torch.randn(1, 3, r, r, device=self.device) / 32 + spe).clamp(0, 1) * 2 - 1
+        roughness = (torch.randn(1, 1, r, r, device=self.device) / 16 + rgh).clamp(0, 1) * 2 - 1
+        self.textures = self._leaf(torch.cat((diffuse, normal, roughness, specular), 1))
+
+    def load_targets(self, targets):
+        self.targets = targets.to(self.device, torch.float32).contiguous()
+
+    def compute_image_loss(self, predicts):
+        """src/optimization.py:28-29 (MSE), or the log(1+x) L2 loss."""
+        if self.loss == "mse":
+            return torch.nn.functional.mse_loss(predicts, self.targets)
+        return torch.nn.functional.mse_loss(torch.log1p(predicts), torch.log1p(self.targets))
+
+    # ---- optim : src/svbrdf.py:44-83 ----
+    def optim(self, epochs, lr, svbrdf_obj=None, optim_light=False):
+        if self.fused:
+            return self._optim_fused(epochs, lr, svbrdf_obj, optim_light)
+        return self._optim_plain(epochs, lr, svbrdf_obj, optim_light)
+
+    def _light_tensor(self, svbrdf_obj):
+        if svbrdf_obj is not None and hasattr(svbrdf_obj, "cl"):
+            lp = svbrdf_obj.cl[2]
+        else:
+            lp = self.renderer_obj.light_pow
+        return lp
+
+    def _save_dir(self, svbrdf_obj):
+        if not self.save_process or svbrdf_obj is None or not hasattr(svbrdf_obj, "optimize_dir"):
+            return None
+        stamp = str(datetime.now()).replace(" ", "-").replace(":", "-").replace(".", "-")
+        d = pathlib.Path(svbrdf_obj.optimize_dir) / "tmp" / stamp
+        d.mkdir(parents=True, exist_ok=True)
+        return d
+
+    def _maybe_save(self, tmp_dir, epoch, epochs, svbrdf_obj):
+        # save points of src/svbrdf.py:74-83 (textures and re-renders; no loss plot)
+        if tmp_dir is None or not ((epoch + 1) % 100 == 0 or epoch == 0 or epoch == epochs - 1):
+            return
+        d = tmp_dir / f"{epoch + 1}"
+        d.mkdir(parents=True, exist_ok=True)
+        with torch.no_grad():
+            tex = self.textures.detach().clamp(-1, 1)
+            if hasattr(svbrdf_obj, "save_textures_th"):
+                svbrdf_obj.save_textures_th(tex, d)
+            if hasattr(svbrdf_obj, "save_images_th"):
+                svbrdf_obj.save_images_th(self.renderer_obj.eval(tex), d)
+
+    def _optim_plain(self, epochs, lr, svbrdf_obj, optim_light):
+        params = [self.textures]
+        if optim_light:
+            lp = self._light_tensor(svbrdf_obj)
+            lp = lp.detach().to(self.device, torch.float32).clone().requires_grad_(True)
+            if svbrdf_obj is not None and hasattr(svbrdf_obj, "cl"):
+                svbrdf_obj.cl[2] = lp
+            params.append(lp)
+        self.optimizer = torch.optim.Adam(params, lr=lr, betas=(0.9, 0.999))
+        tmp_dir = self._save_dir(svbrdf_obj)
+        losses = []
+        for epoch in range(epochs):
+            if optim_light:
+                self.renderer_obj.update_light(params[1])
+            rendereds = self.renderer_obj.eval(self.textures.clamp(-1, 1))
+            loss = self.compute_image_loss(rendereds)
+            losses.append(loss.detach())
+            self.optimizer.zero_grad()
+            loss.backward()
+            self.optimizer.step()
+            self._maybe_save(tmp_dir, epoch, epochs, svbrdf_obj)
+        self.loss_image_list = torch.stack(losses).tolist() if losses else []
+        st = self.optimizer.state[self.textures]
+        self.exp_avg, self.exp_avg_sq = st.get("exp_avg"), st.get("exp_avg_sq")
+
+    def _optim_fused(self, epochs, lr, svbrdf_obj, optim_light):
+        L = N.lib()
+        r = self.renderer_obj
+        tex = self.textures.detach()  # same storage: the kernel updates the leaf in place
+        if not hasattr(self, "exp_avg") or self.exp_avg is None or self.exp_avg.shape != tex.shape:
+            self.exp_avg = torch.zeros_like(tex)
+            self.exp_avg_sq = torch.zeros_like(tex)
+        self._step = 0
+        targets = self.targets
+        kind = LOSS_KINDS[self.loss]
+        if self.loss == "log1p":
+            targets = torch.log1p(self.targets)  # constant over the run: transform once
+            kind = LOSS_KINDS["log1p_pre"]
+        lp = self._light_tensor(svbrdf_obj)
+        lp_dev = lp.detach().to(self.device, torch.float32).contiguous().clone()
+        lstate = torch.zeros(6, device=self.device, dtype=torch.float32) if optim_light else None
+        ws = torch.zeros(int(L.svbrdf_workspace_bytes()), dtype=torch.uint8, device=self.device)
+        losses = torch.zeros(max(epochs, 1), device=self.device, dtype=torch.float32)
+        _, _, H, W = tex.shape
+        V = r.n_of_imgs
+        tmp_dir = self._save_dir(svbrdf_obj)
+
+        def launch(step, loss_slot):
+            N.check(L.svbrdf_fused_step(tex.data_ptr(), self.exp_avg.data_ptr(), self.exp_avg_sq.data_ptr(),
+                                        targets.data_ptr(), r._cam.data_ptr(), r._lit.data_ptr(),
+                                        lp_dev.data_ptr(), N.ptr(lstate), V, H, W, float(r.size), kind, step,
+                                        float(lr), 0.9, 0.999, 1e-8, losses.data_ptr() + 4 * loss_slot,
+                                        ws.data_ptr(), ws.numel(), N.stream_handle(self.device)))
+
+        if self.graph and tmp_dir is None and epochs > 1:
+            # Warm once outside capture (occupancy queries), then undo its effect by restarting
+            # from a snapshot so the captured run is the whole trajectory.
+            snap = [tex.clone(), self.exp_avg.clone(), self.exp_avg_sq.clone(), lp_dev.clone()]
+            if lstate is not None:
+                snap.append(lstate.clone())
+            launch(1, 0)
+            tex.copy_(snap[0]); self.exp_avg.copy_(snap[1]); self.exp_avg_sq.copy_(snap[2]); lp_dev.copy_(snap[3])
+            if lstate is not None:
+                lstate.copy_(snap[4])
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):
+                for e in range(epochs):
+                    launch(e + 1, e)
+            g.replay()
+            self._graph = g
+        else:
+            for e in range(epochs):
+                launch(e + 1, e)
+                if tmp_dir is not None:
+                    self._maybe_save(tmp_dir, e, epochs, svbrdf_obj)
+        self._step = epochs
+        self.loss_image_list = losses[:epochs].tolist()
+        if optim_light:
+            with torch.no_grad():
+                if svbrdf_obj is not None and hasattr(svbrdf_obj, "cl"):
+                    svbrdf_obj.cl[2] = lp_dev.clone().requires_grad_(True)
+                r.update_light(lp_dev.clone())
+            self.light_exp_avg, self.light_exp_avg_sq = lstate[:3].clone(), lstate[3:].clone()
+        self.light_pow = lp_dev

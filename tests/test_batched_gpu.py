@@ -1,0 +1,77 @@
+"""Batched persistent kernel: each material must follow exactly the trajectory the
+single-material fused kernel gives it (same per-texel arithmetic, so bit-identical
+parameters and moments), on an uneven batch."""
+import pytest
+import torch
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def _batch(svb, cuda, n=6):
+    from oracle import microfacet_ref as R
+    mats = svb.scenes.batched_scenes(n=n, resolutions=(16, 32, 48), vmin=3, vmax=12,
+                                     render_fn=lambda *a: R.render(*a, dtype=torch.float32))
+    mats[1].light_pos = mats[1].light_pos + torch.tensor([1.0, -2.0, 3.0])  # one non-co-located material
+    return mats
+
+
+@pytest.mark.parametrize("threads,tile", [(128, 128), (256, 512), (512, 2048)])
+def test_batched_equals_single(svb, cuda, threads, tile):
+    mats = _batch(svb, cuda)
+    cfg = svb.BatchConfig(threads=threads, tile_texels=tile, ctas=5)
+    b = svb.BatchedOptim(mats, lr=0.01, loss="log1p", device=cuda, config=cfg)
+    losses = []
+    for _ in range(7):
+        b.step()
+        losses.append(b.loss_out.clone())
+    for i, m in enumerate(mats):
+        r = svb.Microfacet(m.res, m.n_views, m.size, [t.to(cuda) for t in m.cl], cuda)
+        o = svb.SvbrdfOptim(cuda, r, loss="log1p")
+        o.load_targets(m.targets.to(cuda))
+        o.init_from_tex(m.init.to(cuda))
+        o.optim(7, 0.01, None, False)
+        assert torch.equal(b.tex[i], o.textures.detach())
+        assert torch.equal(b.m2[i], o.exp_avg_sq)
+        for k in range(7):
+            assert abs(float(losses[k][i]) - o.loss_image_list[k]) <= 1e-6 * o.loss_image_list[k]
+
+
+def test_batched_graph_matches_eager(svb, cuda):
+    mats = _batch(svb, cuda)
+    cfg = svb.BatchConfig(threads=256, tile_texels=1024, ctas=0)
+    a = svb.BatchedOptim(mats, device=cuda, config=cfg)
+    for _ in range(5):
+        a.step()
+    b = svb.BatchedOptim(mats, device=cuda, config=cfg)
+    b.run(2)
+    b.run(3)  # re-captured for 3 iterations, continuing at step 3
+    for i in range(len(mats)):
+        assert torch.equal(a.tex[i], b.tex[i])
+    assert torch.equal(a.loss_out, b.loss_out)
+    assert torch.equal(a.loss_hist[:5], b.loss_hist[:5])
+    # a replay of the same graph keeps advancing, identically to eager steps
+    b.run(3)
+    for _ in range(3):
+        a.step()
+    for i in range(len(mats)):
+        assert torch.equal(a.tex[i], b.tex[i])
+    # reset restarts from the initial state
+    b.reset(inits=[m.init for m in mats], targets=[m.targets for m in mats])
+    b.run(3)
+    c = svb.BatchedOptim(mats, device=cuda, config=cfg)
+    for _ in range(3):
+        c.step()
+    for i in range(len(mats)):
+        assert torch.equal(c.tex[i], b.tex[i])
+
+
+def test_autotune_picks_a_valid_config(svb, cuda, tmp_path, monkeypatch):
+    monkeypatch.setattr(svb.batched, "CACHE_FILE", tmp_path / "tune.json")
+    mats = _batch(svb, cuda, n=4)
+    b = svb.BatchedOptim(mats, device=cuda)
+    assert b.config.tile_texels % b.config.threads == 0
+    assert len(b.tune_results if hasattr(b, "tune_results") else [1]) >= 1
+    b.step()
+    assert torch.isfinite(b.loss_out).all()

@@ -1,0 +1,108 @@
+"""The C-ABI library builds for sm_103a, loads without a GPU, exports every symbol the
+header declares, and validates arguments on the host before touching the device."""
+import ctypes
+import re
+
+import numpy as np
+import pytest
+
+from conftest import REPO
+
+
+@pytest.fixture(scope="module")
+def lib(svb):
+    return svb._native.load()
+
+
+def test_exports_match_header(svb, lib):
+    hdr = (REPO / "include" / "svbrdf_gb300.h").read_text()
+    declared = set(re.findall(r"\b(svbrdf_[a-z_0-9]+)\s*\(", hdr))
+    assert declared == set(svb._native.EXPORTS)
+    for name in declared:
+        assert hasattr(lib, name), name
+
+
+def test_constants(lib):
+    assert lib.svbrdf_abi_version() == 1
+    assert lib.svbrdf_max_views() >= 16
+    assert lib.svbrdf_workspace_bytes() >= 16
+
+
+def test_invalid_arguments_rejected_on_host(svb, lib):
+    SV = svb._native
+    # null textures
+    rc = lib.svbrdf_render_fwd(None, None, None, None, 9, 8, 8, 17.0, None, None, -1, None, None, 0, None)
+    assert rc == -1 and b"null" in lib.svbrdf_last_error()
+    fake = ctypes.c_void_p(16)
+    # too many views
+    rc = lib.svbrdf_render_fwd(fake, fake, fake, fake, 10_000, 8, 8, 17.0, fake, None, -1, None, None, 0, None)
+    assert rc == -2
+    # bad loss kind
+    rc = lib.svbrdf_render_fwd(fake, fake, fake, fake, 9, 8, 8, 17.0, fake, None, 7, None, None, 0, None)
+    assert rc == -1
+    # loss without workspace
+    rc = lib.svbrdf_render_fwd(fake, fake, fake, fake, 9, 8, 8, 17.0, fake, fake, 0, fake, None, 0, None)
+    assert rc == -4
+    # fused step: step 0 and missing workspace
+    args = [fake] * 8 + [9, 8, 8, 17.0, 0, 0, 0.01, 0.9, 0.999, 1e-8, fake, fake, 1 << 20, None]
+    assert lib.svbrdf_fused_step(*args) == -1
+    args[13] = 1
+    args[20] = 0
+    assert lib.svbrdf_fused_step(*args) == -4
+    with pytest.raises(SV.SvbrdfError):
+        SV.check(-4)
+
+
+def _materials(SV, shapes):
+    arrs = (SV.svbrdf_material * len(shapes))()
+    keep = []
+    for i, (h, w, v) in enumerate(shapes):
+        cam = np.random.default_rng(i).uniform(-8, 8, (v, 3)).astype(np.float32)
+        cam[:, 2] = 30
+        keep.append(cam)
+        arrs[i] = SV.svbrdf_material(16, 16, 16, 16, 16, cam.ctypes.data, cam.ctypes.data, v, h, w, 17.0)
+    return arrs, keep
+
+
+def test_batched_plan_host_logic(svb, lib):
+    SV = svb._native
+    shapes = [(256, 256, 9), (64, 64, 5), (128, 128, 16), (256, 256, 7), (32, 32, 12)]
+    mats, keep = _materials(SV, shapes)
+    cfg = SV.svbrdf_batch_config(256, 1024, 7, 0)
+    nbytes = lib.svbrdf_batched_plan_bytes(mats, len(shapes), ctypes.byref(cfg))
+    assert nbytes > 0
+    buf = np.zeros(nbytes, np.uint8)
+    assert lib.svbrdf_batched_plan(mats, len(shapes), ctypes.byref(cfg), buf.ctypes.data, nbytes) == 0
+    hdr = np.frombuffer(buf[:48].tobytes(), np.int32)
+    magic, n_mat, n_tiles, n_ctas, threads, tile = hdr[:6]
+    off_mats, off_views, off_cta, off_order, off_tiles, off_mat_tiles = hdr[6:12]
+    assert n_mat == 5 and n_ctas == 7 and threads == 256 and tile == 1024
+    exp_tiles = sum(-(-h * w // 1024) for h, w, _ in shapes)
+    assert n_tiles == exp_tiles
+    cta = np.frombuffer(buf[off_cta:off_cta + 4 * (n_ctas + 1)].tobytes(), np.int32)
+    order = np.frombuffer(buf[off_order:off_order + 4 * n_tiles].tobytes(), np.int32)
+    tiles = np.frombuffer(buf[off_tiles:off_tiles + 8 * n_tiles].tobytes(), np.int32).reshape(-1, 2)
+    mt = np.frombuffer(buf[off_mat_tiles:off_mat_tiles + 4 * (n_mat + 1)].tobytes(), np.int32)
+    # every tile scheduled exactly once
+    assert cta[0] == 0 and cta[-1] == n_tiles
+    assert sorted(order.tolist()) == list(range(n_tiles))
+    # tiles cover each material's texels exactly, contiguous per material
+    for m, (h, w, v) in enumerate(shapes):
+        t = tiles[mt[m]:mt[m + 1]]
+        assert (t[:, 0] == m).all()
+        assert t[:, 1].tolist() == list(range(0, h * w, 1024))
+    # LPT balance: the heaviest CTA carries at most the mean plus one tile
+    cost = np.array([min(1024, shapes[m][0] * shapes[m][1] - x) * (shapes[m][2] + 3) for m, x in tiles], float)
+    loads = [cost[order[cta[c]:cta[c + 1]]].sum() for c in range(n_ctas)]
+    assert max(loads) <= cost.sum() / n_ctas + cost.max() + 1e-6
+    ws = lib.svbrdf_batched_workspace_bytes(buf.ctypes.data)
+    assert ws >= 4 * n_tiles
+
+
+def test_batched_plan_rejects_bad_config(svb, lib):
+    SV = svb._native
+    mats, keep = _materials(SV, [(64, 64, 9)])
+    for cfg in (SV.svbrdf_batch_config(100, 1000, 4, 0), SV.svbrdf_batch_config(256, 1000, 4, 0)):
+        assert lib.svbrdf_batched_plan_bytes(mats, 1, ctypes.byref(cfg)) == 0
+    mats[0].n_views = 1000
+    assert lib.svbrdf_batched_plan_bytes(mats, 1, ctypes.byref(SV.svbrdf_batch_config(256, 1024, 4, 0))) == 0

@@ -60,6 +60,7 @@ def parse():
     ap.add_argument("--iters", type=int, default=100, help="iterations per step (graph replay)")
     ap.add_argument("--no-extras", action="store_true", help="skip the plain/single/cpu comparison legs")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline budget")
+    ap.add_argument("--config", default=None, help="threads,tile_texels[,ctas] instead of autotuning")
     return ap.parse_args()
 
 
@@ -303,7 +304,11 @@ def impl_ours(args):
         PKG.scenes.add_targets(all_sc[i], gpu_render_fn(dev))
         mats.append(all_sc[i])
     del all_sc
-    opt = PKG.BatchedOptim(mats, lr=0.01, loss="log1p", device=dev, hist_len=args.iters)
+    cfg = None
+    if args.config:
+        parts = [int(x) for x in args.config.split(",")]
+        cfg = PKG.BatchConfig(parts[0], parts[1], parts[2] if len(parts) > 2 else 0)
+    opt = PKG.BatchedOptim(mats, lr=0.01, loss="log1p", device=dev, hist_len=args.iters, config=cfg)
     tv = opt.texel_views()
     abytes = opt.algorithmic_bytes()
     opt.capture(args.iters)
@@ -392,6 +397,7 @@ def impl_ours(args):
             "config": {"workload": WORKLOAD, "materials": args.materials, "materials_this_rank": len(mats),
                        "texel_views_per_iteration": tv_all, "iterations_per_step": args.iters,
                        "batch_config": opt.config.__dict__, "ctas": opt.n_ctas(),
+                       "autotune_ms": [list(r) for r in getattr(opt, "tune_results", [])[:6]],
                        "l2": "inputs larger than L2 (no flush)", "parallelism": f"materials sharded over {world} GPU(s)"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,

@@ -112,14 +112,25 @@ typedef struct svbrdf_material {
 } svbrdf_material;
 
 /* Launch shape of the persistent batched kernel (chosen by the autotuner).
- * threads: 128, 256 or 512. tile_texels: texels per work item, a multiple of threads.
+ * variant 0 (direct loads): threads 128, 256 or 512; tile_texels a multiple of threads.
+ * variant 1 (bulk-copy pipeline: one producer warp streams planes into a shared-memory
+ *   ring with cp.async.bulk, `threads` consumer threads compute from it): threads 256,
+ *   384 or 480, tile_texels == threads; every material needs H*W % 4 == 0 and 16-byte
+ *   aligned textures/exp_avg/exp_avg_sq/targets.
  * ctas: persistent CTAs (0 = SM count x resident CTAs per SM). */
 typedef struct svbrdf_batch_config {
   int threads;
   int tile_texels;
   int ctas;
-  int reserved;
+  int variant;
 } svbrdf_batch_config;
+
+/* Workspace of svbrdf_batched_step: the int32 at byte offset 4 is a device error word,
+ * 0 while healthy. A pipelined launch that waited too long for its copies or consumers
+ * stores a non-zero code there (1: copy never landed, 2: consumers stalled, 3: drain
+ * timeout), skips the rest of its work and returns; the caller reads the word after
+ * synchronising and treats non-zero as a failed step. */
+#define SVBRDF_WORKSPACE_ERROR_OFFSET 4
 
 /* Bytes of the plan for this batch (0 on error). */
 size_t svbrdf_batched_plan_bytes(const svbrdf_material* materials, int n_materials,

@@ -21,7 +21,8 @@ INCLUDE = REPO / "include"
 LIBDIR = PKG / "_lib"
 LIBNAME = "libsvbrdf_gb300.so"
 SOURCES = ["render.cu", "fused.cu"]
-HEADERS = ["svbrdf_math.cuh", "svbrdf_common.cuh"]
+HEADERS = ["svbrdf_math.cuh", "svbrdf_common.cuh", "svbrdf_plan.cuh"]
+WORKSPACE_ERROR_OFFSET = 4
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 
@@ -102,7 +103,7 @@ class svbrdf_material(ctypes.Structure):
 
 class svbrdf_batch_config(ctypes.Structure):
     _fields_ = [("threads", ctypes.c_int), ("tile_texels", ctypes.c_int), ("ctas", ctypes.c_int),
-                ("reserved", ctypes.c_int)]
+                ("variant", ctypes.c_int)]
 
 
 def _declare(L):

@@ -25,7 +25,9 @@ import torch
 from . import _native as N
 
 LOSS_KINDS = {"mse": 0, "log1p": 1, "log1p_pre": 2}
-CANDIDATES = [(t, k) for t in (128, 256, 512) for k in (1, 2, 4, 8, 16)]
+# (variant, threads, tiles-per-work-item multiplier)
+CANDIDATES = ([(1, t, 1) for t in (256, 384, 480)] +
+              [(0, t, k) for t in (128, 256, 512) for k in (1, 4, 16)])
 CACHE_FILE = pathlib.Path(os.environ.get("SVBRDF_TUNE_CACHE", str(pathlib.Path.home() / ".cache" / "svbrdf_gb300_tune.json")))
 
 
@@ -33,10 +35,11 @@ CACHE_FILE = pathlib.Path(os.environ.get("SVBRDF_TUNE_CACHE", str(pathlib.Path.h
 class BatchConfig:
     threads: int = 256
     tile_texels: int = 1024
-    ctas: int = 0  # 0 = SM count x resident CTAs per SM
+    ctas: int = 0     # 0 = SM count x resident CTAs per SM
+    variant: int = 0  # 0 direct loads, 1 bulk-copy (TMA) pipeline
 
     def as_c(self):
-        return N.svbrdf_batch_config(self.threads, self.tile_texels, self.ctas, 0)
+        return N.svbrdf_batch_config(self.threads, self.tile_texels, self.ctas, self.variant)
 
 
 class BatchedOptim:
@@ -177,6 +180,17 @@ class BatchedOptim:
     def textures(self, i: int) -> torch.Tensor:
         return self.tex[i]
 
+    def device_error(self) -> int:
+        """The workspace error word (0 = healthy); synchronises with the device."""
+        off = N.WORKSPACE_ERROR_OFFSET
+        return int(self.ws[off:off + 4].view(torch.int32).item())
+
+    def check(self):
+        """Raise if a pipelined launch gave up waiting (see svbrdf_gb300.h)."""
+        e = self.device_error()
+        if e:
+            raise N.SvbrdfError(-3, f"batched kernel reported device error {e}")
+
 
 def _time_config(opt: BatchedOptim, cfg: BatchConfig, iters: int = 3) -> float:
     tex = [t.clone() for t in opt.tex]
@@ -192,6 +206,9 @@ def _time_config(opt: BatchedOptim, cfg: BatchConfig, iters: int = 3) -> float:
         opt._launch(host, dev, ws, step, loss)
     e.record()
     e.synchronize()
+    off = N.WORKSPACE_ERROR_OFFSET
+    if int(ws[off:off + 4].view(torch.int32).item()):
+        raise N.SvbrdfError(-3, "device error during tuning")
     return s.elapsed_time(e) / iters
 
 
@@ -210,16 +227,15 @@ def autotune(opt: BatchedOptim, candidates=None, use_cache: bool = True) -> Batc
         return BatchConfig(**cache[key])
     best, best_ms = None, float("inf")
     results = []
-    for threads, mult in (candidates or CANDIDATES):
-        for ctas_mult in (0,):
-            cfg = BatchConfig(threads=threads, tile_texels=threads * mult, ctas=ctas_mult)
-            try:
-                ms = _time_config(opt, cfg)
-            except N.SvbrdfError:
-                continue
-            results.append((ms, threads, mult))
-            if ms < best_ms:
-                best, best_ms = cfg, ms
+    for variant, threads, mult in (candidates or CANDIDATES):
+        cfg = BatchConfig(threads=threads, tile_texels=threads * mult, ctas=0, variant=variant)
+        try:
+            ms = _time_config(opt, cfg)
+        except N.SvbrdfError:
+            continue
+        results.append((ms, variant, threads, mult))
+        if ms < best_ms:
+            best, best_ms = cfg, ms
     opt.tune_results = sorted(results)
     if best is None:
         best = BatchConfig()

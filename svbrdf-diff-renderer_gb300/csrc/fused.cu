@@ -3,10 +3,15 @@
 // Replaces the loop body of SvbrdfOptim.optim (src/svbrdf.py:56-71):
 //   rendereds = eval(textures.clamp(-1, 1)); loss = MSE(rendereds, targets);
 //   zero_grad(); loss.backward(); optimizer.step()
-// Each thread owns a texel: it reads the 9 parameters, the Adam moments and the V
-// targets once, recomputes every per-view term in registers, and writes the 9
-// parameters and the two moments back. Per-iteration HBM traffic is therefore
-// (36 + 36 + 36) read + (36 + 36 + 36) write + 12*V target bytes per texel.
+// Each texel's 9 parameters, its Adam moments and its V targets are read once, every
+// per-view term is recomputed in registers, and the parameters and moments are written
+// back. Per-iteration HBM traffic: 108 B read + 108 B written + 12*V B of targets per texel.
+//
+// Kernels:
+//   fused_step_kernel     one material, grid-stride, direct loads (drop-in SvbrdfOptim)
+//   batched_step_kernel   many materials, persistent, direct loads           (variant 0)
+//   batched_tma_kernel    many materials, persistent, warp-specialised bulk-copy
+//                         (TMA) pipeline through a shared-memory ring         (variant 1)
 #include <math.h>
 #include <string.h>
 
@@ -15,6 +20,7 @@
 #include <vector>
 
 #include "svbrdf_common.cuh"
+#include "svbrdf_plan.cuh"
 
 namespace svb {
 
@@ -23,8 +29,8 @@ int check_common(const float* tex, const float* cam, const float* lit, const flo
 int grid_for(long long T, int threads, int occupancy_blocks);
 
 AdamScalars make_adam(int step, float lr, float beta1, float beta2, float eps) {
-  // torch.optim.Adam (single-tensor and foreach paths) computes the bias corrections as
-  // Python floats and hands them to FP32 kernels.
+  // torch.optim.Adam computes the bias corrections as Python floats (double) and hands
+  // them to FP32 kernels.
   const double bc1 = 1.0 - pow((double)beta1, (double)step);
   const double bc2 = 1.0 - pow((double)beta2, (double)step);
   AdamScalars s;
@@ -37,52 +43,82 @@ AdamScalars make_adam(int step, float lr, float beta1, float beta2, float eps) {
   return s;
 }
 
-// One texel of one fused iteration. Returns the texel's summed squared error.
-template <int LOSS, bool GRAD_POW>
-__device__ __forceinline__ float fused_texel(float* __restrict__ tex, float* __restrict__ mom1,
-                                             float* __restrict__ mom2, const float* __restrict__ tgt,
-                                             long long T, long long idx, int W, int H, float size, int V,
-                                             const View* s_views, const float* s_pow, float scale,
-                                             const AdamScalars& adam, float gp[3]) {
-  float raw[9], t[9];
+__device__ __forceinline__ AdamScalars device_adam(const AdamHyper& h, int step) {
+  const double bc1 = 1.0 - pow((double)h.beta1, (double)step);
+  const double bc2 = 1.0 - pow((double)h.beta2, (double)step);
+  AdamScalars s;
+  s.one_minus_b1 = (float)(1.0 - (double)h.beta1);
+  s.b2 = h.beta2;
+  s.one_minus_b2 = (float)(1.0 - (double)h.beta2);
+  s.inv_bc2_sqrt = (float)(1.0 / sqrt(bc2));
+  s.eps = h.eps;
+  s.neg_step_size = (float)(-(double)h.lr / bc1);
+  return s;
+}
+
+// Render, loss and adjoint of one texel over its V views, from already-loaded inputs.
+// `raw` are the stored parameters (the optimiser clamps them to [-1, 1] before eval,
+// src/svbrdf.py:60); targets come from `tgt_at(v, c)`. Returns the summed squared error
+// and the parameter gradient scaled by `scale`, zero outside [-1, 1].
+template <int LOSS, bool GRAD_POW, typename TgtFn>
+__device__ __forceinline__ float texel_fused_grad(const float raw[9], float px, float py, int V, const View* s_views,
+                                                  const float* s_pow, float scale, TgtFn tgt_at, float g[9],
+                                                  float gp[3]) {
+  float t[9];
 #pragma unroll
-  for (int c = 0; c < 9; ++c) {
-    raw[c] = tex[c * T + idx];
-    t[c] = fminf(fmaxf(raw[c], -1.0f), 1.0f);  // textures.clamp(-1, 1), src/svbrdf.py:60
-  }
+  for (int c = 0; c < 9; ++c) t[c] = fminf(fmaxf(raw[c], -1.0f), 1.0f);
   Maps m;
   decode(t, m);
-  float px, py;
-  texel_pos((int)(idx / W), (int)(idx % W), W, H, size, px, py);
   Adj a;
   adj_zero(a);
   float loss = 0.f;
   for (int v = 0; v < V; ++v) {
     float io[3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) io[c] = __ldcs(tgt + (3LL * v + c) * T + idx);
+    tgt_at(v, io);
     if (s_views[v].coloc != 0.f)
       texel_view<kModeFused, LOSS, GRAD_POW, true>(m, px, py, s_views[v], s_pow, io, loss, a);
     else
       texel_view<kModeFused, LOSS, GRAD_POW, false>(m, px, py, s_views[v], s_pow, io, loss, a);
   }
-  float g[9];
   adj_to_params(t, m, a, scale, g);
 #pragma unroll
-  for (int c = 0; c < 9; ++c) {
-    const float gc = (raw[c] >= -1.0f && raw[c] <= 1.0f) ? g[c] : 0.0f;
-    float p = raw[c];
-    float m1 = mom1[c * T + idx];
-    float m2 = mom2[c * T + idx];
-    adam_update(p, m1, m2, gc, adam);
-    tex[c * T + idx] = p;
-    mom1[c * T + idx] = m1;
-    mom2[c * T + idx] = m2;
-  }
+  for (int c = 0; c < 9; ++c) g[c] = (raw[c] >= -1.0f && raw[c] <= 1.0f) ? g[c] : 0.0f;
   if (GRAD_POW) {
     gp[0] += a.gp[0] * scale;
     gp[1] += a.gp[1] * scale;
     gp[2] += a.gp[2] * scale;
+  }
+  return loss;
+}
+
+// One texel of one fused iteration with direct global loads. Returns the squared error.
+template <int LOSS, bool GRAD_POW>
+__device__ __forceinline__ float fused_texel(float* __restrict__ tex, float* __restrict__ mom1,
+                                             float* __restrict__ mom2, const float* __restrict__ tgt, int T,
+                                             int idx, float px, float py, int V, const View* s_views,
+                                             const float* s_pow, float scale, const AdamScalars& adam,
+                                             float gp[3]) {
+  float raw[9];
+#pragma unroll
+  for (int c = 0; c < 9; ++c) raw[c] = tex[(size_t)c * T + idx];
+  const float* tp = tgt + idx;
+  auto tgt_at = [&](int v, float io[3]) {
+    const float* p = tp + (size_t)(3 * v) * T;
+    io[0] = __ldcs(p);
+    io[1] = __ldcs(p + T);
+    io[2] = __ldcs(p + 2 * (size_t)T);
+  };
+  float g[9];
+  const float loss = texel_fused_grad<LOSS, GRAD_POW>(raw, px, py, V, s_views, s_pow, scale, tgt_at, g, gp);
+#pragma unroll
+  for (int c = 0; c < 9; ++c) {
+    float p = raw[c];
+    float m1 = mom1[(size_t)c * T + idx];
+    float m2 = mom2[(size_t)c * T + idx];
+    adam_update(p, m1, m2, g[c], adam);
+    tex[(size_t)c * T + idx] = p;
+    mom1[(size_t)c * T + idx] = m1;
+    mom2[(size_t)c * T + idx] = m2;
   }
   return loss;
 }
@@ -105,13 +141,14 @@ fused_step_kernel(float* __restrict__ tex, float* __restrict__ mom1, float* __re
   if (threadIdx.x < 3) s_pow[threadIdx.x] = lpow[threadIdx.x];
   __syncthreads();
 
-  const long long T = (long long)H * W;
+  const int T = H * W;
   float loss = 0.f;
   float gp[3] = {0.f, 0.f, 0.f};
-  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < T;
-       idx += (long long)gridDim.x * blockDim.x)
-    loss += fused_texel<LOSS, GRAD_POW>(tex, mom1, mom2, tgt, T, idx, W, H, size, V, s_views, s_pow, scale, adam,
-                                        gp);
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < T; idx += gridDim.x * blockDim.x) {
+    float px, py;
+    texel_pos(idx / W, idx % W, W, H, size, px, py);
+    loss += fused_texel<LOSS, GRAD_POW>(tex, mom1, mom2, tgt, T, idx, px, py, V, s_views, s_pow, scale, adam, gp);
+  }
 
   const float bl = block_sum<kFusedThreads>(loss, s_red);
   float b0 = 0.f, b1 = 0.f, b2 = 0.f;
@@ -143,78 +180,63 @@ fused_step_kernel(float* __restrict__ tex, float* __restrict__ mom1, float* __re
 }
 
 template <typename K>
-int occupancy_of(K kernel, int threads) {
+int occupancy_of(K kernel, int threads, size_t smem = 0) {
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, 0) != cudaSuccess) {
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, smem) != cudaSuccess) {
     cudaGetLastError();
     return 1;
   }
   return n;
 }
 
-// ============================================================== batched, persistent
-//
-// Plan (one contiguous buffer, identical on host and device):
-//   PlanHeader | MatDesc[n_mat] | View[total views] | int cta_off[n_ctas+1]
-//   | int2 tiles[n_tiles] (material, first texel) | int mat_tile_off[n_mat+1]
-// Tiles of one material are contiguous in tile-index order (mat_tile_off), so the
-// per-material loss is a fixed-order sum over a tile range. cta_off[c]..cta_off[c+1]
-// indexes `order`, a permutation of tile ids balanced across CTAs by the planner.
-
-struct PlanHeader {
-  int magic;
-  int n_mat;
-  int n_tiles;
-  int n_ctas;
-  int threads;
-  int tile_texels;
-  int off_mats;      // byte offsets from the plan base
-  int off_views;
-  int off_cta;
-  int off_order;
-  int off_tiles;
-  int off_mat_tiles;
-  long long total_bytes;
-  double total_cost;  // texel*views
-};
-
-struct __align__(16) MatDesc {
-  float* tex;
-  float* m1;
-  float* m2;
-  const float* tgt;
-  const float* lpow;
-  int H, W, V, view_off;
-  float size, scale;
-  double inv_n;
-};
-
-constexpr int kPlanMagic = 0x53564231;  // "SVB1"
-
-// Adam hyper-parameters of a batched launch; the step itself lives on the device so
-// one captured graph can be replayed indefinitely.
-struct AdamHyper {
-  float lr, beta1, beta2, eps;
-};
-
-__device__ __forceinline__ AdamScalars device_adam(const AdamHyper& h, int step) {
-  // same double-precision bias corrections as make_adam() / torch.optim.Adam
-  const double bc1 = 1.0 - pow((double)h.beta1, (double)step);
-  const double bc2 = 1.0 - pow((double)h.beta2, (double)step);
-  AdamScalars s;
-  s.one_minus_b1 = (float)(1.0 - (double)h.beta1);
-  s.b2 = h.beta2;
-  s.one_minus_b2 = (float)(1.0 - (double)h.beta2);
-  s.inv_bc2_sqrt = (float)(1.0 / sqrt(bc2));
-  s.eps = h.eps;
-  s.neg_step_size = (float)(-(double)h.lr / bc1);
-  return s;
+// ---- row/column of a texel index without integer division: exact for T < 2^24 ----
+__device__ __forceinline__ void texel_rc(int idx, const MatDesc& md, int& i, int& j) {
+  i = (int)((float)idx * md.inv_w);
+  j = idx - i * md.W;
+  if (j < 0) { --i; j += md.W; }
+  else if (j >= md.W) { ++i; j -= md.W; }
 }
 
+// Last CTA of a batched launch: per-material mean loss from the fixed-order partial sums
+// (`per_tile` partials per tile), step counter store, completion counter reset.
+template <int NT>
+__device__ __forceinline__ void batched_finish(const char* plan, const PlanHeader* hdr, const MatDesc* mats,
+                                               const float* partial, int per_tile, float* loss_hist, int hist_len,
+                                               int step, int* step_counter, unsigned* counter, int* s_flag,
+                                               int nwarps) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned prev = atomicAdd(counter, 1u);
+    *s_flag = (prev == gridDim.x - 1) ? 1 : 0;
+  }
+  __syncthreads();
+  if (!*s_flag) return;
+  __threadfence();
+  const int* mat_tiles = (const int*)(plan + hdr->off_mat_tiles);
+  float* loss_out = loss_hist + (size_t)((step - 1) % hist_len) * hdr->n_mat;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (w < nwarps) {
+    for (int mi = w; mi < hdr->n_mat; mi += nwarps) {
+      double acc = 0.0;
+      const int e0 = mat_tiles[mi] * per_tile, e1 = mat_tiles[mi + 1] * per_tile;
+      for (int t = e0 + lane; t < e1; t += 32) acc += (double)__ldcg(partial + t);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      if (lane == 0) loss_out[mi] = (float)(acc * mats[mi].inv_n);
+    }
+  }
+  if (threadIdx.x == 0) {
+    *step_counter = step;
+    *counter = 0u;
+  }
+}
+
+// ============================================================== variant 0: direct loads
 template <int LOSS, int NT>
 __global__ void __launch_bounds__(NT)
 batched_step_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restrict__ step_counter,
-                    float* __restrict__ loss_hist, int hist_len, float* __restrict__ tile_loss, unsigned* counter) {
+                    float* __restrict__ loss_hist, int hist_len, float* __restrict__ tile_loss, unsigned* ws) {
   __shared__ View s_views[kMaxViews];
   __shared__ float s_pow[3];
   __shared__ float s_red[NT / 32];
@@ -233,6 +255,7 @@ batched_step_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
   const int* cta_off = (const int*)(plan + hdr->off_cta);
   const int* order = (const int*)(plan + hdr->off_order);
   const int2* tiles = (const int2*)(plan + hdr->off_tiles);
+  const float* coords = (const float*)(plan + hdr->off_coords);
   const int tile_texels = hdr->tile_texels;
 
   int cur = -1;
@@ -250,59 +273,293 @@ batched_step_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
       if (threadIdx.x < 3) s_pow[threadIdx.x] = md.lpow[threadIdx.x];
       __syncthreads();
     }
-    const long long T = (long long)md.H * md.W;
-    const long long end = min((long long)tl.y + tile_texels, T);
+    const int T = md.H * md.W;
+    const int end = min(tl.y + tile_texels, T);
     float loss = 0.f;
-    for (long long idx = tl.y + threadIdx.x; idx < end; idx += NT)
-      loss += fused_texel<LOSS, false>(md.tex, md.m1, md.m2, md.tgt, T, idx, md.W, md.H, md.size, md.V, s_views,
-                                       s_pow, md.scale, adam, gp_unused);
+    for (int idx = tl.y + threadIdx.x; idx < end; idx += NT) {
+      int i, j;
+      texel_rc(idx, md, i, j);
+      const float px = __ldg(coords + md.coord_off + j), py = __ldg(coords + md.coord_off + md.W + i);
+      loss += fused_texel<LOSS, false>(md.tex, md.m1, md.m2, md.tgt, T, idx, px, py, md.V, s_views, s_pow, md.scale,
+                                       adam, gp_unused);
+    }
     const float bl = block_sum<NT>(loss, s_red);
     if (threadIdx.x == 0) tile_loss[tid] = bl;
   }
-
-  // last CTA: per-material loss, one warp per material, fixed order
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    const unsigned prev = atomicAdd(counter, 1u);
-    s_flag = (prev == gridDim.x - 1) ? 1 : 0;
-  }
-  __syncthreads();
-  if (!s_flag) return;
-  __threadfence();
-  const int* mat_tiles = (const int*)(plan + hdr->off_mat_tiles);
-  float* loss_out = loss_hist + (size_t)((s_step - 1) % hist_len) * hdr->n_mat;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int mi = w; mi < hdr->n_mat; mi += NT / 32) {
-    double acc = 0.0;
-    for (int t = mat_tiles[mi] + lane; t < mat_tiles[mi + 1]; t += 32) acc += (double)__ldcg(tile_loss + t);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane == 0) loss_out[mi] = (float)(acc * mats[mi].inv_n);
-  }
-  if (threadIdx.x == 0) {
-    *step_counter = s_step;
-    *counter = 0u;
-  }
+  __shared__ int s_last;
+  batched_finish<NT>(plan, hdr, mats, tile_loss, 1, loss_hist, hist_len, s_step, step_counter,
+                     ws + kWsCounter, &s_last, NT / 32);
 }
 
+// ============================================================== variant 1: TMA pipeline
+//
+// One producer warp streams, per tile of NT = 32*NCW texels, the chunks
+//   params planes {0-2, 3-5, 6-8}, targets of view 0..V-1 (3 planes each),
+//   exp_avg planes {0-2, 3-5, 6-8}, exp_avg_sq planes {0-2, 3-5, 6-8}
+// into a ring of shared-memory slots (3 planes x NT floats each) with cp.async.bulk
+// (the non-tensor TMA path), one mbarrier per slot signalling "full" (transaction
+// bytes) and one signalling "empty" (one arrival per consumer warp). The NCW consumer
+// warps own one texel per thread and read everything from shared memory; the bytes in
+// flight are bounded by the ring, not by registers. Updated parameters and moments go
+// back with coalesced stores. Every wait is bounded: on timeout the kernel records an
+// error in the workspace, stops issuing, drains its in-flight copies and returns.
+
+constexpr int kMaxRing = 64;
+constexpr uint32_t kSpinLimit = 1u << 22;
+constexpr size_t kRingBudget = 200 * 1024;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
+}
+__device__ __forceinline__ void named_sync(int id, int nthreads) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
+// Bounded wait on an mbarrier phase. Gives up (and records `code`) after kSpinLimit
+// polls, or early once another warp has recorded an error.
+__device__ __forceinline__ bool wait_phase(uint32_t bar, uint32_t parity, int* err, int code) {
+  uint32_t it = 0;
+  while (!mbar_try_wait(bar, parity)) {
+    if (++it >= kSpinLimit) {
+      atomicCAS(err, 0, code);
+      return false;
+    }
+    if ((it & 255u) == 0 && *(volatile int*)err != 0) return false;
+  }
+  return true;
+}
+
+template <int LOSS, int NCW>
+__global__ void __launch_bounds__((NCW + 1) * 32, 1)
+batched_tma_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restrict__ step_counter,
+                   float* __restrict__ loss_hist, int hist_len, float* __restrict__ warp_loss, unsigned* ws) {
+  constexpr int NT = NCW * 32;
+  constexpr int SLOT = 3 * NT;  // floats per ring slot
+  extern __shared__ __align__(128) float ring[];
+  __shared__ __align__(8) uint64_t full_bar[kMaxRing];
+  __shared__ __align__(8) uint64_t empty_bar[kMaxRing];
+  __shared__ View s_views[kMaxViews];
+  __shared__ float s_pow[3];
+  __shared__ AdamScalars s_adam;
+  __shared__ int s_step;
+  __shared__ int s_last;
+
+  const PlanHeader* hdr = (const PlanHeader*)plan;
+  const MatDesc* mats = (const MatDesc*)(plan + hdr->off_mats);
+  const View* views = (const View*)(plan + hdr->off_views);
+  const int* cta_off = (const int*)(plan + hdr->off_cta);
+  const int* order = (const int*)(plan + hdr->off_order);
+  const int2* tiles = (const int2*)(plan + hdr->off_tiles);
+  const float* coords = (const float*)(plan + hdr->off_coords);
+  const int R = hdr->ring_slots;
+  int* err = (int*)(ws + kWsError);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < R; ++s) {
+      mbar_init(smem_u32(&full_bar[s]), 1);
+      mbar_init(smem_u32(&empty_bar[s]), NCW);
+    }
+    fence_mbar_init();
+    s_step = *step_counter + 1;
+    s_adam = device_adam(hyper, s_step);
+  }
+  __syncthreads();
+  const int k0 = cta_off[blockIdx.x], k1 = cta_off[blockIdx.x + 1];
+  const uint32_t ring_base = smem_u32(ring);
+
+  if (warp == NCW) {
+    // ------------------------------------------------------------ producer
+    if (lane == 0) {
+      int slot = 0;
+      uint32_t phase = 0;
+      long long issued = 0;
+      bool ok = true;
+      for (int k = k0; k < k1 && ok; ++k) {
+        const int2 tl = tiles[order[k]];
+        const MatDesc& md = mats[tl.x];
+        const int T = md.H * md.W, V = md.V;
+        const uint32_t bytes = (uint32_t)min(NT, T - tl.y) * 4u;
+        const int nchunks = 9 + V;
+        for (int q = 0; q < nchunks; ++q) {
+          if (issued >= R && !wait_phase(smem_u32(&empty_bar[slot]), phase ^ 1u, err, kDevTimeoutEmpty)) {
+            ok = false;
+            break;
+          }
+          const float* base;
+          int plane0;
+          if (q < 3) { base = md.tex; plane0 = 3 * q; }
+          else if (q < 3 + V) { base = md.tgt; plane0 = 3 * (q - 3); }
+          else if (q < 6 + V) { base = md.m1; plane0 = 3 * (q - 3 - V); }
+          else { base = md.m2; plane0 = 3 * (q - 6 - V); }
+          const uint32_t fb = smem_u32(&full_bar[slot]);
+          mbar_arrive_expect_tx(fb, 3u * bytes);
+#pragma unroll
+          for (int p = 0; p < 3; ++p)
+            bulk_g2s(ring_base + (uint32_t)(slot * SLOT + p * NT) * 4u, base + (size_t)(plane0 + p) * T + tl.y,
+                     bytes, fb);
+          ++issued;
+          if (++slot == R) { slot = 0; phase ^= 1u; }
+        }
+      }
+      if (!ok) {
+        // drain: wait for the copies of the last min(R, issued) chunks to land
+        const long long n = issued < R ? issued : R;
+        int s = slot;
+        uint32_t ph = phase;
+        for (long long i = 0; i < n; ++i) {
+          if (--s < 0) { s = R - 1; ph ^= 1u; }
+          uint32_t it = 0;
+          while (!mbar_try_wait(smem_u32(&full_bar[s]), ph)) {
+            if (++it >= kSpinLimit) { atomicCAS(err, 0, kDevTimeoutDrain); break; }
+          }
+        }
+      }
+    }
+  } else {
+    // ------------------------------------------------------------ consumers
+    const int tid = threadIdx.x;
+    int slot = 0;
+    uint32_t phase = 0;
+    bool ok = true;
+    int cur = -1;
+    float loss_warp_unused = 0.f;
+    (void)loss_warp_unused;
+    // wait for the next chunk, run `use(const float* slot_floats)`, release the slot
+    auto take = [&](auto use) {
+      if (ok) ok = wait_phase(smem_u32(&full_bar[slot]), phase, err, kDevTimeoutFull);
+      if (ok) use(ring + slot * SLOT);
+      __syncwarp();
+      if (lane == 0 && ok) mbar_arrive(smem_u32(&empty_bar[slot]));
+      if (++slot == R) { slot = 0; phase ^= 1u; }
+    };
+    for (int k = k0; k < k1; ++k) {
+      const int tile = order[k];
+      const int2 tl = tiles[tile];
+      if (tl.x != cur) {  // uniform over the consumer warps
+        named_sync(1, NT);
+        cur = tl.x;
+        const MatDesc& m0 = mats[cur];
+        for (int v = tid; v < m0.V; v += NT) s_views[v] = views[m0.view_off + v];
+        if (tid < 3) s_pow[tid] = m0.lpow[tid];
+        named_sync(1, NT);
+      }
+      const MatDesc& md = mats[cur];
+      const int T = md.H * md.W, V = md.V;
+      const bool active = tid < T - tl.y;
+      const int idx = tl.y + tid;
+      float raw[9];
+#pragma unroll
+      for (int q = 0; q < 3; ++q)
+        take([&](const float* sl) {
+#pragma unroll
+          for (int p = 0; p < 3; ++p) raw[3 * q + p] = sl[p * NT + tid];
+        });
+      float px = 0.f, py = 0.f;
+      if (active) {
+        int i, j;
+        texel_rc(idx, md, i, j);
+        px = __ldg(coords + md.coord_off + j);
+        py = __ldg(coords + md.coord_off + md.W + i);
+      }
+      auto tgt_at = [&](int v, float io[3]) {
+        take([&](const float* sl) {
+          io[0] = sl[tid];
+          io[1] = sl[NT + tid];
+          io[2] = sl[2 * NT + tid];
+        });
+      };
+      float g[9], gp[3];
+      float loss = texel_fused_grad<LOSS, false>(raw, px, py, V, s_views, s_pow, md.scale, tgt_at, g, gp);
+      float m1[9], m2[9];
+#pragma unroll
+      for (int q = 0; q < 3; ++q)
+        take([&](const float* sl) {
+#pragma unroll
+          for (int p = 0; p < 3; ++p) m1[3 * q + p] = sl[p * NT + tid];
+        });
+#pragma unroll
+      for (int q = 0; q < 3; ++q)
+        take([&](const float* sl) {
+#pragma unroll
+          for (int p = 0; p < 3; ++p) m2[3 * q + p] = sl[p * NT + tid];
+        });
+      if (active && ok) {
+#pragma unroll
+        for (int c = 0; c < 9; ++c) {
+          float p = raw[c];
+          adam_update(p, m1[c], m2[c], g[c], s_adam);
+          md.tex[(size_t)c * T + idx] = p;
+          md.m1[(size_t)c * T + idx] = m1[c];
+          md.m2[(size_t)c * T + idx] = m2[c];
+        }
+      } else {
+        loss = 0.f;
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, o);
+      if (lane == 0) warp_loss[(size_t)tile * NCW + warp] = loss;
+    }
+  }
+  batched_finish<NT + 32>(plan, hdr, mats, warp_loss, NCW, loss_hist, hist_len, s_step, step_counter,
+                          ws + kWsCounter, &s_last, NCW);
+}
+
+// ============================================================== planner
 static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 struct PlanLayout {
-  size_t off_mats, off_views, off_cta, off_order, off_tiles, off_mat_tiles, total;
-  int n_tiles, n_ctas, total_views;
+  size_t off_mats, off_views, off_cta, off_order, off_tiles, off_mat_tiles, off_coords, total;
+  int n_tiles, n_ctas, total_views, ring;
+  long long coord_floats;
 };
 
-int resident_ctas(int threads);
+int resident_ctas(int variant, int threads);
+
+static int slot_bytes(int threads) { return 3 * threads * 4; }
 
 static int plan_layout(const svbrdf_material* mats, int n, const svbrdf_batch_config* cfg, PlanLayout& L) {
   if (!mats || n <= 0) return fail(SVBRDF_ERR_INVALID, "no materials");
   if (!cfg) return fail(SVBRDF_ERR_INVALID, "null config");
-  if (cfg->threads != 128 && cfg->threads != 256 && cfg->threads != 512)
-    return fail(SVBRDF_ERR_UNSUPPORTED, "threads must be 128, 256 or 512 (got %d)", cfg->threads);
-  if (cfg->tile_texels <= 0 || cfg->tile_texels % cfg->threads)
-    return fail(SVBRDF_ERR_INVALID, "tile_texels must be a positive multiple of threads");
-  long long tiles = 0;
+  const int variant = cfg->variant;
+  if (variant != 0 && variant != 1) return fail(SVBRDF_ERR_INVALID, "variant must be 0 or 1 (got %d)", variant);
+  if (variant == 0) {
+    if (cfg->threads != 128 && cfg->threads != 256 && cfg->threads != 512)
+      return fail(SVBRDF_ERR_UNSUPPORTED, "threads must be 128, 256 or 512 (got %d)", cfg->threads);
+    if (cfg->tile_texels <= 0 || cfg->tile_texels % cfg->threads)
+      return fail(SVBRDF_ERR_INVALID, "tile_texels must be a positive multiple of threads");
+  } else {
+    if (cfg->threads != 256 && cfg->threads != 384 && cfg->threads != 480)
+      return fail(SVBRDF_ERR_UNSUPPORTED, "pipelined variant: threads must be 256, 384 or 480 (got %d)", cfg->threads);
+    if (cfg->tile_texels != cfg->threads)
+      return fail(SVBRDF_ERR_INVALID, "pipelined variant: tile_texels must equal threads");
+  }
+  long long tiles = 0, coords = 0;
   int views = 0;
   for (int i = 0; i < n; ++i) {
     const svbrdf_material& m = mats[i];
@@ -312,17 +569,26 @@ static int plan_layout(const svbrdf_material* mats, int n, const svbrdf_batch_co
       return fail(SVBRDF_ERR_INVALID, "material %d has a bad shape", i);
     if (m.n_views > kMaxViews) return fail(SVBRDF_ERR_UNSUPPORTED, "material %d: too many views", i);
     const long long T = (long long)m.height * m.width;
-    if (T > (1LL << 30)) return fail(SVBRDF_ERR_UNSUPPORTED, "material %d too large", i);
+    if (T >= (1LL << 24)) return fail(SVBRDF_ERR_UNSUPPORTED, "material %d: more than 2^24 texels", i);
+    if (variant == 1) {
+      if (T % 4) return fail(SVBRDF_ERR_UNSUPPORTED, "pipelined variant: material %d H*W must be a multiple of 4", i);
+      const void* ptrs[4] = {m.textures, m.exp_avg, m.exp_avg_sq, m.targets};
+      for (const void* p : ptrs)
+        if ((uintptr_t)p % 16) return fail(SVBRDF_ERR_UNSUPPORTED, "pipelined variant: material %d not 16-byte aligned", i);
+    }
     tiles += (T + cfg->tile_texels - 1) / cfg->tile_texels;
     views += m.n_views;
+    coords += m.width + m.height;
   }
   if (tiles > (1LL << 30)) return fail(SVBRDF_ERR_UNSUPPORTED, "too many tiles");
-  int ctas = cfg->ctas > 0 ? cfg->ctas : resident_ctas(cfg->threads);
+  int ctas = cfg->ctas > 0 ? cfg->ctas : resident_ctas(variant, cfg->threads);
   if (ctas <= 0) return fail(SVBRDF_ERR_CUDA, "could not query the device");
   if (ctas > tiles) ctas = (int)tiles;
   L.n_tiles = (int)tiles;
   L.n_ctas = ctas;
   L.total_views = views;
+  L.coord_floats = coords;
+  L.ring = variant == 1 ? (int)std::min<size_t>(kMaxRing, kRingBudget / slot_bytes(cfg->threads)) : 0;
   size_t o = align_up(sizeof(PlanHeader), 16);
   L.off_mats = o; o += sizeof(MatDesc) * n; o = align_up(o, 16);
   L.off_views = o; o += sizeof(View) * views; o = align_up(o, 16);
@@ -330,7 +596,9 @@ static int plan_layout(const svbrdf_material* mats, int n, const svbrdf_batch_co
   L.off_order = o; o += sizeof(int) * tiles; o = align_up(o, 16);
   L.off_tiles = o; o += sizeof(int2) * tiles; o = align_up(o, 16);
   L.off_mat_tiles = o; o += sizeof(int) * (n + 1); o = align_up(o, 16);
+  L.off_coords = o; o += sizeof(float) * coords; o = align_up(o, 16);
   L.total = o;
+  if (L.total > (size_t)0x7fffffff) return fail(SVBRDF_ERR_UNSUPPORTED, "plan too large");
   return SVBRDF_OK;
 }
 
@@ -339,9 +607,31 @@ static int plan_layout(const svbrdf_material* mats, int n, const svbrdf_batch_co
 using namespace svb;
 
 namespace svb {
-int resident_ctas(int threads) {
+template <int NCW>
+static size_t tma_smem(int ring) {
+  return (size_t)ring * 3 * NCW * 32 * 4;
+}
+
+template <int LOSS, int NCW>
+static int tma_prepare(int ring) {
+  // once per instantiation: allow the ring's dynamic shared memory
+  static int done = 0;
+  static size_t have = 0;
+  const size_t need = tma_smem<NCW>(ring);
+  if (!done || need > have) {
+    if (cudaFuncSetAttribute(batched_tma_kernel<LOSS, NCW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need) !=
+        cudaSuccess)
+      return fail(SVBRDF_ERR_CUDA, "cudaFuncSetAttribute: %s", cudaGetErrorString(cudaGetLastError()));
+    done = 1;
+    have = need;
+  }
+  return SVBRDF_OK;
+}
+
+int resident_ctas(int variant, int threads) {
   const int sms = device_sm_count();
   if (sms <= 0) return 0;
+  if (variant == 1) return sms;  // one pipelined CTA per SM (its ring takes the shared memory)
   int occ = 1;
   switch (threads) {
     case 128: occ = occupancy_of(batched_step_kernel<0, 128>, 128); break;
@@ -426,6 +716,9 @@ int svbrdf_batched_plan(const svbrdf_material* materials, int n_materials, const
   h->off_order = (int)L.off_order;
   h->off_tiles = (int)L.off_tiles;
   h->off_mat_tiles = (int)L.off_mat_tiles;
+  h->off_coords = (int)L.off_coords;
+  h->variant = config->variant;
+  h->ring_slots = L.ring;
   h->total_bytes = (long long)L.total;
   MatDesc* md = (MatDesc*)(base + L.off_mats);
   View* vw = (View*)(base + L.off_views);
@@ -433,8 +726,10 @@ int svbrdf_batched_plan(const svbrdf_material* materials, int n_materials, const
   int* order = (int*)(base + L.off_order);
   int2* tiles = (int2*)(base + L.off_tiles);
   int* mat_tiles = (int*)(base + L.off_mat_tiles);
+  float* coords = (float*)(base + L.off_coords);
   std::vector<double> cost(L.n_tiles);
   int voff = 0, t = 0;
+  long long coff = 0;
   double total = 0;
   for (int i = 0; i < n_materials; ++i) {
     const svbrdf_material& m = materials[i];
@@ -451,7 +746,15 @@ int svbrdf_batched_plan(const svbrdf_material* materials, int n_materials, const
     md[i].view_off = voff;
     md[i].size = m.size;
     md[i].scale = (float)(2.0 / N);
+    md[i].inv_w = 1.0f / (float)m.width;
+    md[i].coord_off = (int)coff;
     md[i].inv_n = 1.0 / N;
+    // pixel-centre grid of src/microfacet.py:16-19, FP32 with IEEE division: x[j], -y[i]
+    for (int j = 0; j < m.width; ++j)
+      coords[coff + j] = (((float)j + 0.5f) / (float)m.width - 0.5f) * m.size;
+    for (int r = 0; r < m.height; ++r)
+      coords[coff + m.width + r] = -((((float)r + 0.5f) / (float)m.height - 0.5f) * m.size);
+    coff += m.width + m.height;
     for (int v = 0; v < m.n_views; ++v) {
       View& w = vw[voff + v];
       w.cx = m.camera_pos[3 * v]; w.cy = m.camera_pos[3 * v + 1]; w.cz = m.camera_pos[3 * v + 2];
@@ -476,9 +779,7 @@ int svbrdf_batched_plan(const svbrdf_material* materials, int n_materials, const
   std::vector<int> idx(L.n_tiles);
   std::iota(idx.begin(), idx.end(), 0);
   std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return cost[a] > cost[b]; });
-  std::vector<double> load(L.n_ctas, 0.0);
   std::vector<std::vector<int>> per(L.n_ctas);
-  // min-heap over (load, cta)
   std::vector<std::pair<double, int>> heap;
   heap.reserve(L.n_ctas);
   for (int c = 0; c < L.n_ctas; ++c) heap.push_back({0.0, c});
@@ -509,12 +810,13 @@ size_t svbrdf_batched_workspace_bytes(const void* host_plan) {
   if (!host_plan) return 0;
   const PlanHeader* h = (const PlanHeader*)host_plan;
   if (h->magic != kPlanMagic) return 0;
-  return 256 + sizeof(float) * (size_t)h->n_tiles;
+  const size_t per_tile = h->variant == 1 ? (size_t)(h->threads / 32) : 1;
+  return kWsLossOffset + sizeof(float) * (size_t)h->n_tiles * per_tile;
 }
 
-int svbrdf_batched_step(const void* device_plan, const void* host_plan, int loss_kind, int* step_counter,
-                        float lr, float beta1, float beta2, float eps, float* loss_hist, int hist_len,
-                        void* workspace, size_t workspace_bytes, void* stream) {
+int svbrdf_batched_step(const void* device_plan, const void* host_plan, int loss_kind, int* step_counter, float lr,
+                        float beta1, float beta2, float eps, float* loss_hist, int hist_len, void* workspace,
+                        size_t workspace_bytes, void* stream) {
   if (!device_plan || !host_plan || !loss_hist || !step_counter)
     return fail(SVBRDF_ERR_INVALID, "null plan/step_counter/loss_hist");
   const PlanHeader* h = (const PlanHeader*)host_plan;
@@ -524,8 +826,8 @@ int svbrdf_batched_step(const void* device_plan, const void* host_plan, int loss
   if (hist_len < 1) return fail(SVBRDF_ERR_INVALID, "hist_len must be >= 1");
   const size_t need = svbrdf_batched_workspace_bytes(host_plan);
   if (!workspace || workspace_bytes < need) return fail(SVBRDF_ERR_WORKSPACE, "workspace of %zu bytes needed", need);
-  unsigned* counter = (unsigned*)workspace;
-  float* tile_loss = (float*)((char*)workspace + 256);
+  unsigned* ws = (unsigned*)workspace;
+  float* part = (float*)((char*)workspace + kWsLossOffset);
   AdamHyper hyper;
   hyper.lr = lr;
   hyper.beta1 = beta1;
@@ -533,20 +835,43 @@ int svbrdf_batched_step(const void* device_plan, const void* host_plan, int loss
   hyper.eps = eps;
   cudaStream_t st = (cudaStream_t)stream;
   const char* plan = (const char*)device_plan;
+  if (h->variant == 0) {
 #define SVB_B(L, NT) \
-  batched_step_kernel<L, NT><<<h->n_ctas, NT, 0, st>>>(plan, hyper, step_counter, loss_hist, hist_len, tile_loss, counter)
-#define SVB_BL(NT)                                    \
-  if (loss_kind == SVBRDF_LOSS_MSE) SVB_B(0, NT);     \
+  batched_step_kernel<L, NT><<<h->n_ctas, NT, 0, st>>>(plan, hyper, step_counter, loss_hist, hist_len, part, ws)
+#define SVB_BL(NT)                                       \
+  if (loss_kind == SVBRDF_LOSS_MSE) SVB_B(0, NT);        \
   else if (loss_kind == SVBRDF_LOSS_LOG1P) SVB_B(1, NT); \
   else SVB_B(2, NT);
-  switch (h->threads) {
-    case 128: SVB_BL(128) break;
-    case 256: SVB_BL(256) break;
-    default: SVB_BL(512) break;
-  }
+    switch (h->threads) {
+      case 128: SVB_BL(128) break;
+      case 256: SVB_BL(256) break;
+      default: SVB_BL(512) break;
+    }
 #undef SVB_BL
 #undef SVB_B
-  return check_launch("batched_step_kernel");
+    return check_launch("batched_step_kernel");
+  }
+  const int ring = h->ring_slots;
+  if (ring < 2 || ring > kMaxRing) return fail(SVBRDF_ERR_INVALID, "bad ring depth %d", ring);
+#define SVB_T(L, NCW)                                                                                        \
+  {                                                                                                          \
+    int prc = tma_prepare<L, NCW>(ring);                                                                     \
+    if (prc) return prc;                                                                                     \
+    batched_tma_kernel<L, NCW><<<h->n_ctas, (NCW + 1) * 32, tma_smem<NCW>(ring), st>>>(                      \
+        plan, hyper, step_counter, loss_hist, hist_len, part, ws);                                           \
+  }
+#define SVB_TL(NCW)                                       \
+  if (loss_kind == SVBRDF_LOSS_MSE) SVB_T(0, NCW)         \
+  else if (loss_kind == SVBRDF_LOSS_LOG1P) SVB_T(1, NCW)  \
+  else SVB_T(2, NCW)
+  switch (h->threads) {
+    case 256: SVB_TL(8) break;
+    case 384: SVB_TL(12) break;
+    default: SVB_TL(15) break;
+  }
+#undef SVB_TL
+#undef SVB_T
+  return check_launch("batched_tma_kernel");
 }
 
 }  // extern "C"

@@ -63,6 +63,8 @@ __device__ __forceinline__ float sqrt_approx(float x) {
   asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
   return y;
 }
+// log1p(u) for u in [0, 1] (renders and targets): one lg2 of 1+u, about 1e-7 absolute.
+__device__ __forceinline__ float log1p_fast(float u) { return lg2_approx(1.0f + u) * 0.69314718055994531f; }
 
 // Decoded maps of one texel (tex2map, src/microfacet.py:72-79) plus the factors the
 // adjoint needs to map map-space gradients back to the 9 parameters.
@@ -175,8 +177,18 @@ __device__ __forceinline__ void texel_view(const Maps& m, float px, float py, co
   const float nh = fmaxf(nh_raw, 0.0f);
 
   // ---- GGX D (src/microfacet.py:28-32) ----
+  // den = c2*a2 + (1 - c2). For unit n and h, 1 - (n.h)^2 = |n x h|^2; the cross product
+  // has no cancellation near the highlight (n.h -> 1), where 1 - c2 in FP32 loses most
+  // of its digits. Where the reference clamps n.h to 0, 1 - c2 is exactly 1.
   const float c2 = nh * nh;
-  const float den = c2 * m.a2 + (1.0f - c2);
+  float s2 = 1.0f;
+  if (nh_raw > 0.0f) {
+    const float x0 = m.n[1] * hz - m.n[2] * hy;
+    const float x1 = m.n[2] * hx - m.n[0] * hz;
+    const float x2 = m.n[0] * hy - m.n[1] * hx;
+    s2 = x0 * x0 + x1 * x1 + x2 * x2;
+  }
+  const float den = c2 * m.a2 + s2;
   const float E = kPi * (den * den) + kEps;
   const float rE = rcp_approx(E);
   const float D = m.a2 * rE;
@@ -190,7 +202,8 @@ __device__ __forceinline__ void texel_view(const Maps& m, float px, float py, co
   else { Bl = nl * omk + m.k; rBl = rcp_approx(Bl); G1l = nl * rBl; }
   const float G = G1v * G1l;
   // ---- Fresnel, spherical-Gaussian Schlick (src/microfacet.py:43-45) ----
-  const float sphg = ex2_approx((-5.55473f * vh - 6.98316f) * vh);
+  // co-located: v.h = 1, so sphg = 2^(-5.55473 - 6.98316) is a constant
+  const float sphg = COLOC ? 1.6815858e-4f : ex2_approx((-5.55473f * vh - 6.98316f) * vh);
   // ---- f2 = D F G / (4 nv nl + eps), img = P f nl / d^2 (src/microfacet.py:109-117) ----
   const float Q = 4.0f * nv * nl + kEps;
   const float rQ = rcp_approx(Q);
@@ -224,8 +237,8 @@ __device__ __forceinline__ void texel_view(const Maps& m, float px, float py, co
       float e;
       if (LOSS == kLossMSE) { e = out - io[c]; gout = e; }
       else {
-        const float lo = log1pf(out);
-        e = (LOSS == kLossLog1p) ? lo - log1pf(io[c]) : lo - io[c];
+        const float lo = log1p_fast(out);
+        e = (LOSS == kLossLog1p) ? lo - log1p_fast(io[c]) : lo - io[c];
         gout = e * rcp_approx(1.0f + out);
       }
       loss += e * e;

@@ -1,6 +1,7 @@
-"""Batched persistent kernel: each material must follow exactly the trajectory the
-single-material fused kernel gives it (same per-texel arithmetic, so bit-identical
-parameters and moments), on an uneven batch."""
+"""Batched persistent kernel: each material must follow the trajectory the
+single-material fused kernel gives it, on an uneven batch. Both kernels inline the same
+per-texel code, but they are separate kernels (ptxas may contract and schedule them
+differently), so the comparison allows last-bit differences."""
 import pytest
 import torch
 
@@ -17,10 +18,11 @@ def _batch(svb, cuda, n=6):
     return mats
 
 
-@pytest.mark.parametrize("threads,tile", [(128, 128), (256, 512), (512, 2048)])
-def test_batched_equals_single(svb, cuda, threads, tile):
+@pytest.mark.parametrize("variant,threads,tile", [(0, 128, 128), (0, 256, 512), (0, 512, 2048),
+                                                  (1, 256, 256), (1, 384, 384), (1, 480, 480)])
+def test_batched_equals_single(svb, cuda, variant, threads, tile):
     mats = _batch(svb, cuda)
-    cfg = svb.BatchConfig(threads=threads, tile_texels=tile, ctas=5)
+    cfg = svb.BatchConfig(threads=threads, tile_texels=tile, ctas=5, variant=variant)
     b = svb.BatchedOptim(mats, lr=0.01, loss="log1p", device=cuda, config=cfg)
     losses = []
     for _ in range(7):
@@ -32,15 +34,18 @@ def test_batched_equals_single(svb, cuda, threads, tile):
         o.load_targets(m.targets.to(cuda))
         o.init_from_tex(m.init.to(cuda))
         o.optim(7, 0.01, None, False)
-        assert torch.equal(b.tex[i], o.textures.detach())
-        assert torch.equal(b.m2[i], o.exp_avg_sq)
+        assert rel_l2(b.tex[i], o.textures.detach()) <= 1e-6
+        assert rel_l2(b.m1[i], o.exp_avg) <= 1e-5
+        assert rel_l2(b.m2[i], o.exp_avg_sq) <= 1e-5
         for k in range(7):
             assert abs(float(losses[k][i]) - o.loss_image_list[k]) <= 1e-6 * o.loss_image_list[k]
+    assert b.device_error() == 0
 
 
-def test_batched_graph_matches_eager(svb, cuda):
+@pytest.mark.parametrize("variant,threads,tile", [(0, 256, 1024), (1, 384, 384)])
+def test_batched_graph_matches_eager(svb, cuda, variant, threads, tile):
     mats = _batch(svb, cuda)
-    cfg = svb.BatchConfig(threads=256, tile_texels=1024, ctas=0)
+    cfg = svb.BatchConfig(threads=threads, tile_texels=tile, ctas=0, variant=variant)
     a = svb.BatchedOptim(mats, device=cuda, config=cfg)
     for _ in range(5):
         a.step()

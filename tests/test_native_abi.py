@@ -106,3 +106,44 @@ def test_batched_plan_rejects_bad_config(svb, lib):
         assert lib.svbrdf_batched_plan_bytes(mats, 1, ctypes.byref(cfg)) == 0
     mats[0].n_views = 1000
     assert lib.svbrdf_batched_plan_bytes(mats, 1, ctypes.byref(SV.svbrdf_batch_config(256, 1024, 4, 0))) == 0
+
+
+def test_pipelined_plan_requirements(svb, lib):
+    SV = svb._native
+    ok_cfg = SV.svbrdf_batch_config(384, 384, 4, 1)
+    mats, keep = _materials(SV, [(64, 64, 9), (32, 32, 5)])
+    assert lib.svbrdf_batched_plan_bytes(mats, 2, ctypes.byref(ok_cfg)) > 0
+    # tile must equal the consumer thread count
+    assert lib.svbrdf_batched_plan_bytes(mats, 2, ctypes.byref(SV.svbrdf_batch_config(384, 768, 4, 1))) == 0
+    # unsupported width
+    assert lib.svbrdf_batched_plan_bytes(mats, 2, ctypes.byref(SV.svbrdf_batch_config(512, 512, 4, 1))) == 0
+    # H*W not a multiple of 4
+    odd, keep2 = _materials(SV, [(37, 37, 9)])
+    assert lib.svbrdf_batched_plan_bytes(odd, 1, ctypes.byref(ok_cfg)) == 0
+    assert b"multiple of 4" in lib.svbrdf_last_error()
+    # misaligned pointer
+    mats[0].textures = 20
+    assert lib.svbrdf_batched_plan_bytes(mats, 2, ctypes.byref(ok_cfg)) == 0
+    assert b"aligned" in lib.svbrdf_last_error()
+    # bad variant
+    assert lib.svbrdf_batched_plan_bytes(keep2 and odd, 1, ctypes.byref(SV.svbrdf_batch_config(256, 256, 4, 7))) == 0
+
+
+def test_pipelined_plan_ring_and_workspace(svb, lib):
+    SV = svb._native
+    mats, keep = _materials(SV, [(64, 64, 9), (32, 32, 5)])
+    cfg = SV.svbrdf_batch_config(480, 480, 3, 1)
+    n = lib.svbrdf_batched_plan_bytes(mats, 2, ctypes.byref(cfg))
+    buf = np.zeros(n, np.uint8)
+    assert lib.svbrdf_batched_plan(mats, 2, ctypes.byref(cfg), buf.ctypes.data, n) == 0
+    hdr = np.frombuffer(buf[:64].tobytes(), np.int32)
+    n_tiles, variant, ring = hdr[2], hdr[13], hdr[14]
+    assert variant == 1
+    assert 2 <= ring <= 64 and ring * 3 * 480 * 4 <= 200 * 1024
+    # one partial loss per (tile, consumer warp) after the 256-byte header
+    assert lib.svbrdf_batched_workspace_bytes(buf.ctypes.data) == 256 + 4 * n_tiles * (480 // 32)
+    # coordinate tables: the reference's pixel-centre grid (src/microfacet.py:16-19)
+    off_coords = hdr[12]
+    xs = np.frombuffer(buf[off_coords:off_coords + 4 * 64].tobytes(), np.float32)
+    ref = ((np.arange(64, dtype=np.float32) + np.float32(0.5)) / np.float32(64) - np.float32(0.5)) * np.float32(17.0)
+    assert np.array_equal(xs, ref)

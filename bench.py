@@ -60,7 +60,7 @@ def parse():
     ap.add_argument("--iters", type=int, default=100, help="iterations per step (graph replay)")
     ap.add_argument("--no-extras", action="store_true", help="skip the plain/single/cpu comparison legs")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline budget")
-    ap.add_argument("--config", default=None, help="threads,tile_texels[,ctas] instead of autotuning")
+    ap.add_argument("--config", default=None, help="threads,tile_texels[,ctas[,variant]] instead of autotuning")
     return ap.parse_args()
 
 
@@ -307,7 +307,7 @@ def impl_ours(args):
     cfg = None
     if args.config:
         parts = [int(x) for x in args.config.split(",")]
-        cfg = PKG.BatchConfig(parts[0], parts[1], parts[2] if len(parts) > 2 else 0)
+        cfg = PKG.BatchConfig(parts[0], parts[1], parts[2] if len(parts) > 2 else 0, parts[3] if len(parts) > 3 else 0)
     opt = PKG.BatchedOptim(mats, lr=0.01, loss="log1p", device=dev, hist_len=args.iters, config=cfg)
     tv = opt.texel_views()
     abytes = opt.algorithmic_bytes()
@@ -401,7 +401,8 @@ def impl_ours(args):
                        "l2": "inputs larger than L2 (no flush)", "parallelism": f"materials sharded over {world} GPU(s)"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
-                         "kernel": "batched_step_kernel", "algorithmic_bytes_per_launch": abytes,
+                         "kernel": "batched_tma_kernel" if opt.config.variant == 1 else "batched_step_kernel",
+                         "algorithmic_bytes_per_launch": abytes,
                          "launch_ms": launch_ms},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": args.steps * args.iters,

@@ -60,13 +60,19 @@ __device__ __forceinline__ AdamScalars device_adam(const AdamHyper& h, int step)
 // `raw` are the stored parameters (the optimiser clamps them to [-1, 1] before eval,
 // src/svbrdf.py:60); targets come from `tgt_at(v, c)`. Returns the summed squared error
 // and the parameter gradient scaled by `scale`, zero outside [-1, 1].
-template <int LOSS, bool GRAD_POW, typename TgtFn>
+template <int LOSS, bool GRAD_POW, bool ALL_COLOC, typename TgtFn>
 __device__ __forceinline__ float texel_fused_grad(const float raw[9], float px, float py, int V, const View* s_views,
                                                   const float* s_pow, float scale, TgtFn tgt_at, float g[9],
                                                   float gp[3]) {
   float t[9];
 #pragma unroll
   for (int c = 0; c < 9; ++c) t[c] = fminf(fmaxf(raw[c], -1.0f), 1.0f);
+  if (ALL_COLOC) {
+    const float loss = coloc_texel<LOSS, GRAD_POW>(t, px, py, V, s_views, s_pow, scale, tgt_at, g, gp);
+#pragma unroll
+    for (int c = 0; c < 9; ++c) g[c] = (raw[c] >= -1.0f && raw[c] <= 1.0f) ? g[c] : 0.0f;
+    return loss;
+  }
   Maps m;
   decode(t, m);
   Adj a;
@@ -92,7 +98,7 @@ __device__ __forceinline__ float texel_fused_grad(const float raw[9], float px, 
 }
 
 // One texel of one fused iteration with direct global loads. Returns the squared error.
-template <int LOSS, bool GRAD_POW>
+template <int LOSS, bool GRAD_POW, bool ALL_COLOC>
 __device__ __forceinline__ float fused_texel(float* __restrict__ tex, float* __restrict__ mom1,
                                              float* __restrict__ mom2, const float* __restrict__ tgt, int T,
                                              int idx, float px, float py, int V, const View* s_views,
@@ -109,7 +115,8 @@ __device__ __forceinline__ float fused_texel(float* __restrict__ tex, float* __r
     io[2] = __ldcs(p + 2 * (size_t)T);
   };
   float g[9];
-  const float loss = texel_fused_grad<LOSS, GRAD_POW>(raw, px, py, V, s_views, s_pow, scale, tgt_at, g, gp);
+  const float loss =
+      texel_fused_grad<LOSS, GRAD_POW, ALL_COLOC>(raw, px, py, V, s_views, s_pow, scale, tgt_at, g, gp);
 #pragma unroll
   for (int c = 0; c < 9; ++c) {
     float p = raw[c];
@@ -144,10 +151,22 @@ fused_step_kernel(float* __restrict__ tex, float* __restrict__ mom1, float* __re
   const int T = H * W;
   float loss = 0.f;
   float gp[3] = {0.f, 0.f, 0.f};
-  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < T; idx += gridDim.x * blockDim.x) {
-    float px, py;
-    texel_pos(idx / W, idx % W, W, H, size, px, py);
-    loss += fused_texel<LOSS, GRAD_POW>(tex, mom1, mom2, tgt, T, idx, px, py, V, s_views, s_pow, scale, adam, gp);
+  bool allc = true;
+  for (int v = 0; v < V; ++v) allc = allc && (s_views[v].coloc != 0.f);
+  if (allc) {
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < T; idx += gridDim.x * blockDim.x) {
+      float px, py;
+      texel_pos(idx / W, idx % W, W, H, size, px, py);
+      loss += fused_texel<LOSS, GRAD_POW, true>(tex, mom1, mom2, tgt, T, idx, px, py, V, s_views, s_pow, scale,
+                                                adam, gp);
+    }
+  } else {
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < T; idx += gridDim.x * blockDim.x) {
+      float px, py;
+      texel_pos(idx / W, idx % W, W, H, size, px, py);
+      loss += fused_texel<LOSS, GRAD_POW, false>(tex, mom1, mom2, tgt, T, idx, px, py, V, s_views, s_pow, scale,
+                                                 adam, gp);
+    }
   }
 
   const float bl = block_sum<kFusedThreads>(loss, s_red);
@@ -280,8 +299,12 @@ batched_step_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
       int i, j;
       texel_rc(idx, md, i, j);
       const float px = __ldg(coords + md.coord_off + j), py = __ldg(coords + md.coord_off + md.W + i);
-      loss += fused_texel<LOSS, false>(md.tex, md.m1, md.m2, md.tgt, T, idx, px, py, md.V, s_views, s_pow, md.scale,
-                                       adam, gp_unused);
+      if (md.all_coloc)
+        loss += fused_texel<LOSS, false, true>(md.tex, md.m1, md.m2, md.tgt, T, idx, px, py, md.V, s_views, s_pow,
+                                               md.scale, adam, gp_unused);
+      else
+        loss += fused_texel<LOSS, false, false>(md.tex, md.m1, md.m2, md.tgt, T, idx, px, py, md.V, s_views, s_pow,
+                                                md.scale, adam, gp_unused);
     }
     const float bl = block_sum<NT>(loss, s_red);
     if (threadIdx.x == 0) tile_loss[tid] = bl;
@@ -495,7 +518,9 @@ batched_tma_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restri
         });
       };
       float g[9], gp[3];
-      float loss = texel_fused_grad<LOSS, false>(raw, px, py, V, s_views, s_pow, md.scale, tgt_at, g, gp);
+      float loss = md.all_coloc
+                       ? texel_fused_grad<LOSS, false, true>(raw, px, py, V, s_views, s_pow, md.scale, tgt_at, g, gp)
+                       : texel_fused_grad<LOSS, false, false>(raw, px, py, V, s_views, s_pow, md.scale, tgt_at, g, gp);
       float m1[9], m2[9];
 #pragma unroll
       for (int q = 0; q < 3; ++q)
@@ -755,12 +780,15 @@ int svbrdf_batched_plan(const svbrdf_material* materials, int n_materials, const
     for (int r = 0; r < m.height; ++r)
       coords[coff + m.width + r] = -((((float)r + 0.5f) / (float)m.height - 0.5f) * m.size);
     coff += m.width + m.height;
+    int allc = 1;
     for (int v = 0; v < m.n_views; ++v) {
       View& w = vw[voff + v];
       w.cx = m.camera_pos[3 * v]; w.cy = m.camera_pos[3 * v + 1]; w.cz = m.camera_pos[3 * v + 2];
       w.lx = m.light_pos[3 * v]; w.ly = m.light_pos[3 * v + 1]; w.lz = m.light_pos[3 * v + 2];
       w.coloc = (w.cx == w.lx && w.cy == w.ly && w.cz == w.lz) ? 1.f : 0.f;
+      allc = allc && w.coloc != 0.f;
     }
+    md[i].all_coloc = allc;
     voff += m.n_views;
     mat_tiles[i] = t;
     for (long long x = 0; x < T; x += config->tile_texels) {

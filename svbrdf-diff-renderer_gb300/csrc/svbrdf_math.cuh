@@ -319,6 +319,172 @@ __device__ __forceinline__ void adj_to_params(const float t[9], const Maps& m, c
   g[4] = (t[4] >= -1.0f && t[4] <= 1.0f) ? gny * scale : 0.0f;
 }
 
+// ---------------------------------------------------------------- co-located fast path
+// Flash captures put the light at the camera (src/capture.py:70-71; data/random/render.json).
+// Then l = h = v, v.h = 1 and the Fresnel term F_c = s_c + (1 - s_c) 2^(-12.53789) no
+// longer depends on the view: the per-view work shrinks to one normalisation, D, G and the
+// per-channel encode/loss. Gradients below omit the output encode's 1/2.2 factor, which
+// the per-texel map-back applies once.
+constexpr float kSphgColoc = 1.6815858e-4f;  // 2^(-5.55473 - 6.98316)
+constexpr float kInvPi = 0.318309886183790671f;
+constexpr float kLn2 = 0.69314718055994531f;
+
+struct TexelC {
+  float n0, n1, n2;  // unit normal
+  float px, py;      // texel position (cm)
+  float a2, k, omk;  // alpha^2, Smith k, 1 - k
+  float f1[3];       // d/pi (1 - s)
+  float F[3];        // s + (1 - s) sphg
+};
+
+struct AccC {
+  float gf1[3];  // sum over views of dL/d f   (= dL/d f1)
+  float gfd[3];  // sum over views of dL/d f * D G / Q   (-> dL/d F)
+  float ga2, gk;
+  float gn0, gn1, gn2;  // dL/d n, accumulated against the unnormalised view vector
+  float gp[3];
+  float loss;
+};
+
+template <int LOSS, bool GRAD_POW>
+__device__ __forceinline__ void coloc_view(const TexelC& t, const View& vw, const float P[3], const float tg[3],
+                                           AccC& a) {
+  const float vx = vw.cx - t.px, vy = vw.cy - t.py, vz = vw.cz;
+  const float q = fmaf(vx, vx, fmaf(vy, vy, vz * vz));
+  const float iv = rsqrt_approx(q);
+  const float inv_d2 = iv * iv;
+  const float nv_raw = fmaf(t.n0, vx, fmaf(t.n1, vy, t.n2 * vz)) * iv;
+  const float nv = fmaxf(nv_raw, 0.0f);
+  // 1 - (n.v)^2 as |n x v|^2 (no cancellation at the highlight); 1 where n.v is clamped
+  const float x0 = fmaf(t.n1, vz, -t.n2 * vy);
+  const float x1 = fmaf(t.n2, vx, -t.n0 * vz);
+  const float x2 = fmaf(t.n0, vy, -t.n1 * vx);
+  const float s2 = nv_raw > 0.0f ? fmaf(x0, x0, fmaf(x1, x1, x2 * x2)) * inv_d2 : 1.0f;
+  const float c2 = nv * nv;
+  const float den = fmaf(c2, t.a2, s2);
+  const float rE = rcp_approx(fmaf(kPi, den * den, kEps));
+  const float D = t.a2 * rE;
+  const float rB = rcp_approx(fmaf(nv, t.omk, t.k));
+  const float G1 = nv * rB;
+  const float G = G1 * G1;
+  const float rQ = rcp_approx(fmaf(4.0f, c2, kEps));
+  const float DGQ = D * G * rQ;
+  const float W = nv * inv_d2;
+  float gDGQ = 0.f, gW = 0.f;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const float f = fmaf(DGQ, t.F[c], t.f1[c]);
+    const float PW = P[c] * W;
+    const float img = f * PW;
+    const float x = fminf(fmaxf(img, kEps), 1.0f);
+    const float xp = ex2_approx(lg2_approx(x) * (kInvGamma - 1.0f));  // x^(1/2.2 - 1)
+    const float out = x * xp;
+    float e, gout;
+    if (LOSS == kLossMSE) {
+      e = out - tg[c];
+      gout = e;
+    } else {
+      const float op1 = 1.0f + out;
+      const float lo = lg2_approx(op1) * kLn2;
+      e = lo - (LOSS == kLossLog1p ? log1p_fast(tg[c]) : tg[c]);
+      gout = e * rcp_approx(op1);
+    }
+    a.loss = fmaf(e, e, a.loss);
+    const float gimg = (x == img) ? gout * xp : 0.0f;  // clamp(eps, 1) passes its range
+    const float gf = gimg * PW;
+    gW = fmaf(gimg, P[c] * f, gW);
+    if (GRAD_POW) a.gp[c] = fmaf(gimg * f, W, a.gp[c]);
+    a.gf1[c] += gf;
+    gDGQ = fmaf(gf, t.F[c], gDGQ);
+    a.gfd[c] = fmaf(gf, DGQ, a.gfd[c]);
+  }
+  const float tq = gDGQ * rQ;
+  const float gD = tq * G;
+  const float gG1 = 2.0f * tq * D * G1;  // G = G1^2
+  const float rB2 = rB * rB;
+  float gnv = fmaf(gG1 * t.k, rB2, fmaf(-tq * DGQ * 8.0f, nv, gW * inv_d2));
+  a.gk = fmaf(-gG1 * nv * (1.0f - nv), rB2, a.gk);
+  const float t2 = D * rE * (2.0f * kPi) * den;
+  a.ga2 = fmaf(gD, fmaf(-t2, c2, rE), a.ga2);
+  gnv = fmaf(-gD * t2 * (t.a2 - 1.0f) * 2.0f, nv, gnv);
+  const float gs = nv_raw >= 0.0f ? gnv * iv : 0.0f;
+  a.gn0 = fmaf(gs, vx, a.gn0);
+  a.gn1 = fmaf(gs, vy, a.gn1);
+  a.gn2 = fmaf(gs, vz, a.gn2);
+}
+
+// x = ((t+1)/2)^2.2 and its derivative 1.1 ((t+1)/2)^1.2 = 1.1 x / base (0 at base 0).
+__device__ __forceinline__ float pow22(float base) { return ex2_approx(2.2f * lg2_approx(base)); }
+__device__ __forceinline__ float dpow22(float x, float base) { return base > 0.0f ? 1.1f * x * rcp_approx(base) : 0.0f; }
+
+// Render, loss and adjoint of one co-located texel (all views co-located). `t9` holds the
+// parameters already clamped to [-1, 1]. Returns the summed squared error; g[9] receives
+// dL/dt scaled by `scale` (the loss normaliser).
+template <int LOSS, bool GRAD_POW, typename TgtFn>
+__device__ __forceinline__ float coloc_texel(const float t9[9], float px, float py, int V, const View* views,
+                                             const float P[3], float scale, TgtFn tgt_at, float g[9], float gp[3]) {
+  TexelC t;
+  float bd[3], bs[3], d[3], sp[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    bd[c] = (t9[c] + 1.0f) * 0.5f;
+    bs[c] = (t9[6 + c] + 1.0f) * 0.5f;
+    d[c] = pow22(bd[c]);
+    sp[c] = pow22(bs[c]);
+    const float oms = 1.0f - sp[c];
+    t.f1[c] = d[c] * kInvPi * oms;
+    t.F[c] = fmaf(oms, kSphgColoc, sp[c]);
+  }
+  const float br = (t9[5] + 1.0f) * 0.5f;
+  const float r = pow22(br);
+  const float alpha = r * r;
+  t.a2 = alpha * alpha;
+  t.k = fmaf(alpha, 0.5f, kEps);
+  t.omk = 1.0f - t.k;
+  const float nx = t9[3], ny = t9[4];  // already within [-1, 1]
+  const float sxy_raw = fmaf(nx, nx, ny * ny);
+  const float sxy = fminf(sxy_raw, 1.0f - kEps);
+  const float nz = sqrt_approx(1.0f - sxy);
+  const float inv = rsqrt_approx(fmaf(nx, nx, fmaf(ny, ny, nz * nz)));
+  t.n0 = nx * inv;
+  t.n1 = ny * inv;
+  t.n2 = nz * inv;
+  t.px = px;
+  t.py = py;
+  AccC a;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) { a.gf1[c] = 0.f; a.gfd[c] = 0.f; a.gp[c] = 0.f; }
+  a.ga2 = a.gk = a.gn0 = a.gn1 = a.gn2 = a.loss = 0.f;
+  for (int v = 0; v < V; ++v) {
+    float tg[3];
+    tgt_at(v, tg);
+    coloc_view<LOSS, GRAD_POW>(t, views[v], P, tg, a);
+  }
+  const float sc = scale * kInvGamma;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const float oms = 1.0f - sp[c];
+    g[c] = a.gf1[c] * oms * kInvPi * dpow22(d[c], bd[c]) * sc;
+    g[6 + c] = fmaf(a.gfd[c], 1.0f - kSphgColoc, -a.gf1[c] * d[c] * kInvPi) * dpow22(sp[c], bs[c]) * sc;
+  }
+  const float galpha = fmaf(a.ga2, 2.0f * alpha, a.gk * 0.5f);
+  g[5] = galpha * 2.0f * r * dpow22(r, br) * sc;
+  // normal: n = m/|m|, m = (nx, ny, sqrt(1 - min(nx^2+ny^2, 1-eps)))
+  const float ndg = t.n0 * a.gn0 + t.n1 * a.gn1 + t.n2 * a.gn2;
+  const float gmx = (a.gn0 - t.n0 * ndg) * inv;
+  const float gmy = (a.gn1 - t.n1 * ndg) * inv;
+  const float gmz = (a.gn2 - t.n2 * ndg) * inv;
+  const float gsxy = (sxy_raw <= 1.0f - kEps) ? (-0.5f * gmz * rcp_approx(nz)) : 0.0f;
+  g[3] = fmaf(gsxy * 2.0f, nx, gmx) * sc;
+  g[4] = fmaf(gsxy * 2.0f, ny, gmy) * sc;
+  if (GRAD_POW) {
+    gp[0] += a.gp[0] * sc;
+    gp[1] += a.gp[1] * sc;
+    gp[2] += a.gp[2] * sc;
+  }
+  return a.loss;
+}
+
 // torch.optim.Adam's update for one element (amsgrad off, no weight decay):
 //   m.lerp_(g, 1-b1); v.mul_(b2).addcmul_(g, g, 1-b2);
 //   p.addcdiv_(m, sqrt(v)/sqrt(bc2) + eps, -lr/bc1)

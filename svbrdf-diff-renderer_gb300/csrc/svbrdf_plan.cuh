@@ -44,6 +44,8 @@ struct __align__(16) MatDesc {
   float size, scale;  // scale = 2 / (3 V H W), the loss-gradient normaliser
   float inv_w;        // 1 / W for the row/column split of a texel index
   int coord_off;      // float index of this material's x table (y follows at +W)
+  int all_coloc;      // 1 when every view has the light at the camera
+  int pad;
   double inv_n;       // 1 / (3 V H W)
 };
 

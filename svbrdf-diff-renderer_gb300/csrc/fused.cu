@@ -317,17 +317,19 @@ batched_step_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
 // ============================================================== variant 1: TMA pipeline
 //
 // One producer warp streams, per tile of NT = 32*NCW texels, the chunks
-//   params planes {0-2, 3-5, 6-8}, targets of view 0..V-1 (3 planes each),
-//   exp_avg planes {0-2, 3-5, 6-8}, exp_avg_sq planes {0-2, 3-5, 6-8}
-// into a ring of shared-memory slots (3 planes x NT floats each) with cp.async.bulk
-// (the non-tensor TMA path), one mbarrier per slot signalling "full" (transaction
-// bytes) and one signalling "empty" (one arrival per consumer warp). The NCW consumer
-// warps own one texel per thread and read everything from shared memory; the bytes in
-// flight are bounded by the ring, not by registers. Updated parameters and moments go
-// back with coalesced stores. Every wait is bounded: on timeout the kernel records an
-// error in the workspace, stops issuing, drains its in-flight copies and returns.
+//   P  = the 9 parameter planes,
+//   Tc = target planes of views 3c .. 3c+2 (3 planes per view),  c = 0 .. ceil(V/3)-1,
+//   M  = the 9 exp_avg planes,  S = the 9 exp_avg_sq planes
+// into a ring of shared-memory slots of 9 planes x NT floats with cp.async.bulk (the
+// non-tensor TMA path). Each slot has an mbarrier signalling "full" (transaction bytes)
+// and one signalling "empty" (one arrival per consumer warp). The NCW consumer warps own
+// one texel per thread and read everything from shared memory, so the bytes in flight
+// are bounded by the ring, not by registers. Updated parameters and moments go back with
+// coalesced stores. Every wait is bounded: on timeout the kernel records an error in the
+// workspace, stops issuing, drains its in-flight copies and returns.
 
 constexpr int kMaxRing = 64;
+constexpr int kSlotPlanes = 9;
 constexpr uint32_t kSpinLimit = 1u << 22;
 constexpr size_t kRingBudget = 200 * 1024;
 
@@ -377,16 +379,36 @@ __device__ __forceinline__ bool wait_phase(uint32_t bar, uint32_t parity, int* e
   return true;
 }
 
+// Consumer-side ring cursor.
+struct RingCursor {
+  int slot;
+  uint32_t phase;
+  bool ok;
+};
+
+template <int NT>
+__device__ __forceinline__ const float* ring_acquire(RingCursor& rc, const float* ring, uint64_t* full_bar, int* err) {
+  if (rc.ok) rc.ok = __all_sync(0xffffffffu, wait_phase(smem_u32(&full_bar[rc.slot]), rc.phase, err, kDevTimeoutFull));
+  return ring + (size_t)rc.slot * (kSlotPlanes * NT);
+}
+
+__device__ __forceinline__ void ring_release(RingCursor& rc, uint64_t* empty_bar, int R) {
+  __syncwarp();
+  if ((threadIdx.x & 31) == 0 && rc.ok) mbar_arrive(smem_u32(&empty_bar[rc.slot]));
+  if (++rc.slot == R) { rc.slot = 0; rc.phase ^= 1u; }
+}
+
 template <int LOSS, int NCW>
 __global__ void __launch_bounds__((NCW + 1) * 32, 1)
 batched_tma_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restrict__ step_counter,
                    float* __restrict__ loss_hist, int hist_len, float* __restrict__ warp_loss, unsigned* ws) {
   constexpr int NT = NCW * 32;
-  constexpr int SLOT = 3 * NT;  // floats per ring slot
+  constexpr int SLOT = kSlotPlanes * NT;  // floats per ring slot
   extern __shared__ __align__(128) float ring[];
   __shared__ __align__(8) uint64_t full_bar[kMaxRing];
   __shared__ __align__(8) uint64_t empty_bar[kMaxRing];
   __shared__ View s_views[kMaxViews];
+  __shared__ MatDesc s_md;
   __shared__ float s_pow[3];
   __shared__ AdamScalars s_adam;
   __shared__ int s_step;
@@ -425,27 +447,26 @@ batched_tma_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restri
       bool ok = true;
       for (int k = k0; k < k1 && ok; ++k) {
         const int2 tl = tiles[order[k]];
-        const MatDesc& md = mats[tl.x];
+        const MatDesc md = mats[tl.x];
         const int T = md.H * md.W, V = md.V;
         const uint32_t bytes = (uint32_t)min(NT, T - tl.y) * 4u;
-        const int nchunks = 9 + V;
-        for (int q = 0; q < nchunks; ++q) {
+        const int nt = (V + 2) / 3;
+        for (int q = 0; q < nt + 3; ++q) {
           if (issued >= R && !wait_phase(smem_u32(&empty_bar[slot]), phase ^ 1u, err, kDevTimeoutEmpty)) {
             ok = false;
             break;
           }
           const float* base;
-          int plane0;
-          if (q < 3) { base = md.tex; plane0 = 3 * q; }
-          else if (q < 3 + V) { base = md.tgt; plane0 = 3 * (q - 3); }
-          else if (q < 6 + V) { base = md.m1; plane0 = 3 * (q - 3 - V); }
-          else { base = md.m2; plane0 = 3 * (q - 6 - V); }
+          int plane0, nplanes;
+          if (q == 0) { base = md.tex; plane0 = 0; nplanes = 9; }
+          else if (q <= nt) { base = md.tgt; plane0 = 9 * (q - 1); nplanes = min(9, 3 * V - plane0); }
+          else if (q == nt + 1) { base = md.m1; plane0 = 0; nplanes = 9; }
+          else { base = md.m2; plane0 = 0; nplanes = 9; }
           const uint32_t fb = smem_u32(&full_bar[slot]);
-          mbar_arrive_expect_tx(fb, 3u * bytes);
-#pragma unroll
-          for (int p = 0; p < 3; ++p)
-            bulk_g2s(ring_base + (uint32_t)(slot * SLOT + p * NT) * 4u, base + (size_t)(plane0 + p) * T + tl.y,
-                     bytes, fb);
+          mbar_arrive_expect_tx(fb, (uint32_t)nplanes * bytes);
+          const float* src = base + (size_t)plane0 * T + tl.y;
+          for (int p = 0; p < nplanes; ++p)
+            bulk_g2s(ring_base + (uint32_t)(slot * SLOT + p * NT) * 4u, src + (size_t)p * T, bytes, fb);
           ++issued;
           if (++slot == R) { slot = 0; phase ^= 1u; }
         }
@@ -467,81 +488,118 @@ batched_tma_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restri
   } else {
     // ------------------------------------------------------------ consumers
     const int tid = threadIdx.x;
-    int slot = 0;
-    uint32_t phase = 0;
-    bool ok = true;
+    RingCursor rc{0, 0u, true};
     int cur = -1;
-    float loss_warp_unused = 0.f;
-    (void)loss_warp_unused;
-    // wait for the next chunk, run `use(const float* slot_floats)`, release the slot
-    auto take = [&](auto use) {
-      if (ok) ok = wait_phase(smem_u32(&full_bar[slot]), phase, err, kDevTimeoutFull);
-      if (ok) use(ring + slot * SLOT);
-      __syncwarp();
-      if (lane == 0 && ok) mbar_arrive(smem_u32(&empty_bar[slot]));
-      if (++slot == R) { slot = 0; phase ^= 1u; }
-    };
     for (int k = k0; k < k1; ++k) {
       const int tile = order[k];
       const int2 tl = tiles[tile];
       if (tl.x != cur) {  // uniform over the consumer warps
         named_sync(1, NT);
         cur = tl.x;
-        const MatDesc& m0 = mats[cur];
-        for (int v = tid; v < m0.V; v += NT) s_views[v] = views[m0.view_off + v];
-        if (tid < 3) s_pow[tid] = m0.lpow[tid];
+        if (tid == 0) s_md = mats[cur];
+        const int vo = mats[cur].view_off, nv = mats[cur].V;
+        for (int v = tid; v < nv; v += NT) s_views[v] = views[vo + v];
+        if (tid < 3) s_pow[tid] = mats[cur].lpow[tid];
         named_sync(1, NT);
       }
-      const MatDesc& md = mats[cur];
-      const int T = md.H * md.W, V = md.V;
+      const int T = s_md.H * s_md.W, V = s_md.V;
       const bool active = tid < T - tl.y;
       const int idx = tl.y + tid;
+      const float scale = s_md.scale;
+      // ---- parameters
       float raw[9];
+      {
+        const float* sl = ring_acquire<NT>(rc, ring, full_bar, err);
 #pragma unroll
-      for (int q = 0; q < 3; ++q)
-        take([&](const float* sl) {
-#pragma unroll
-          for (int p = 0; p < 3; ++p) raw[3 * q + p] = sl[p * NT + tid];
-        });
+        for (int p = 0; p < 9; ++p) raw[p] = sl[p * NT + tid];
+        ring_release(rc, empty_bar, R);
+      }
       float px = 0.f, py = 0.f;
       if (active) {
         int i, j;
-        texel_rc(idx, md, i, j);
-        px = __ldg(coords + md.coord_off + j);
-        py = __ldg(coords + md.coord_off + md.W + i);
+        texel_rc(idx, s_md, i, j);
+        px = __ldg(coords + s_md.coord_off + j);
+        py = __ldg(coords + s_md.coord_off + s_md.W + i);
       }
-      auto tgt_at = [&](int v, float io[3]) {
-        take([&](const float* sl) {
-          io[0] = sl[tid];
-          io[1] = sl[NT + tid];
-          io[2] = sl[2 * NT + tid];
-        });
-      };
+      float t9[9];
+#pragma unroll
+      for (int c = 0; c < 9; ++c) t9[c] = fminf(fmaxf(raw[c], -1.0f), 1.0f);
       float g[9], gp[3];
-      float loss = md.all_coloc
-                       ? texel_fused_grad<LOSS, false, true>(raw, px, py, V, s_views, s_pow, md.scale, tgt_at, g, gp)
-                       : texel_fused_grad<LOSS, false, false>(raw, px, py, V, s_views, s_pow, md.scale, tgt_at, g, gp);
+      float loss;
+      if (s_md.all_coloc) {
+        TexelC tc;
+        coloc_prepare(t9, px, py, tc);
+        AccC a;
+        acc_zero(a);
+        const float P0 = s_pow[0], P1 = s_pow[1], P2 = s_pow[2];
+        for (int v0 = 0; v0 < V; v0 += 3) {
+          const float* sl = ring_acquire<NT>(rc, ring, full_bar, err);
+          const int nv = min(3, V - v0);
+#pragma unroll
+          for (int j = 0; j < 3; ++j) {
+            if (j < nv) {
+              float tg[3];
+              tg[0] = sl[(3 * j + 0) * NT + tid];
+              tg[1] = sl[(3 * j + 1) * NT + tid];
+              tg[2] = sl[(3 * j + 2) * NT + tid];
+              const float4 cam = *reinterpret_cast<const float4*>(&s_views[v0 + j]);
+              coloc_view<LOSS, false>(tc, cam, P0, P1, P2, tg, a);
+            }
+          }
+          ring_release(rc, empty_bar, R);
+        }
+        loss = coloc_finish<LOSS, false>(t9, tc, a, scale, g, gp);
+#pragma unroll
+        for (int c = 0; c < 9; ++c) g[c] = (raw[c] >= -1.0f && raw[c] <= 1.0f) ? g[c] : 0.0f;
+      } else {
+        Maps m;
+        decode(t9, m);
+        Adj a;
+        adj_zero(a);
+        loss = 0.f;
+        for (int v0 = 0; v0 < V; v0 += 3) {
+          const float* sl = ring_acquire<NT>(rc, ring, full_bar, err);
+          const int nv = min(3, V - v0);
+          for (int j = 0; j < nv; ++j) {
+            float io[3];
+            io[0] = sl[(3 * j + 0) * NT + tid];
+            io[1] = sl[(3 * j + 1) * NT + tid];
+            io[2] = sl[(3 * j + 2) * NT + tid];
+            const View& w = s_views[v0 + j];
+            if (w.coloc != 0.f) texel_view<kModeFused, LOSS, false, true>(m, px, py, w, s_pow, io, loss, a);
+            else texel_view<kModeFused, LOSS, false, false>(m, px, py, w, s_pow, io, loss, a);
+          }
+          ring_release(rc, empty_bar, R);
+        }
+        adj_to_params(t9, m, a, scale, g);
+#pragma unroll
+        for (int c = 0; c < 9; ++c) g[c] = (raw[c] >= -1.0f && raw[c] <= 1.0f) ? g[c] : 0.0f;
+      }
+      // ---- Adam moments, update, write back
       float m1[9], m2[9];
+      {
+        const float* sl = ring_acquire<NT>(rc, ring, full_bar, err);
 #pragma unroll
-      for (int q = 0; q < 3; ++q)
-        take([&](const float* sl) {
+        for (int p = 0; p < 9; ++p) m1[p] = sl[p * NT + tid];
+        ring_release(rc, empty_bar, R);
+      }
+      {
+        const float* sl = ring_acquire<NT>(rc, ring, full_bar, err);
 #pragma unroll
-          for (int p = 0; p < 3; ++p) m1[3 * q + p] = sl[p * NT + tid];
-        });
-#pragma unroll
-      for (int q = 0; q < 3; ++q)
-        take([&](const float* sl) {
-#pragma unroll
-          for (int p = 0; p < 3; ++p) m2[3 * q + p] = sl[p * NT + tid];
-        });
-      if (active && ok) {
+        for (int p = 0; p < 9; ++p) m2[p] = sl[p * NT + tid];
+        ring_release(rc, empty_bar, R);
+      }
+      if (active && rc.ok) {
+        float* tex = s_md.tex;
+        float* gm1 = s_md.m1;
+        float* gm2 = s_md.m2;
 #pragma unroll
         for (int c = 0; c < 9; ++c) {
           float p = raw[c];
           adam_update(p, m1[c], m2[c], g[c], s_adam);
-          md.tex[(size_t)c * T + idx] = p;
-          md.m1[(size_t)c * T + idx] = m1[c];
-          md.m2[(size_t)c * T + idx] = m2[c];
+          tex[(size_t)c * T + idx] = p;
+          gm1[(size_t)c * T + idx] = m1[c];
+          gm2[(size_t)c * T + idx] = m2[c];
         }
       } else {
         loss = 0.f;
@@ -566,7 +624,7 @@ struct PlanLayout {
 
 int resident_ctas(int variant, int threads);
 
-static int slot_bytes(int threads) { return 3 * threads * 4; }
+static int slot_bytes(int threads) { return kSlotPlanes * threads * 4; }
 
 static int plan_layout(const svbrdf_material* mats, int n, const svbrdf_batch_config* cfg, PlanLayout& L) {
   if (!mats || n <= 0) return fail(SVBRDF_ERR_INVALID, "no materials");
@@ -634,7 +692,7 @@ using namespace svb;
 namespace svb {
 template <int NCW>
 static size_t tma_smem(int ring) {
-  return (size_t)ring * 3 * NCW * 32 * 4;
+  return (size_t)ring * kSlotPlanes * NCW * 32 * 4;
 }
 
 template <int LOSS, int NCW>

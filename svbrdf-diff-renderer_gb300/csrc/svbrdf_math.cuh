@@ -346,10 +346,13 @@ struct AccC {
   float loss;
 };
 
+// One co-located view of one texel. `cam` = (cx, cy, cz, -); tg = targets of this view.
+// For the log1p losses the error is kept in log2 units (e = log2(1+out) - log2(1+target)):
+// the caller scales the loss by ln2^2 and the gradient by ln2.
 template <int LOSS, bool GRAD_POW>
-__device__ __forceinline__ void coloc_view(const TexelC& t, const View& vw, const float P[3], const float tg[3],
-                                           AccC& a) {
-  const float vx = vw.cx - t.px, vy = vw.cy - t.py, vz = vw.cz;
+__device__ __forceinline__ void coloc_view(const TexelC& t, float4 cam, float P0, float P1, float P2,
+                                           const float tg[3], AccC& a) {
+  const float vx = cam.x - t.px, vy = cam.y - t.py, vz = cam.z;
   const float q = fmaf(vx, vx, fmaf(vy, vy, vz * vz));
   const float iv = rsqrt_approx(q);
   const float inv_d2 = iv * iv;
@@ -359,7 +362,8 @@ __device__ __forceinline__ void coloc_view(const TexelC& t, const View& vw, cons
   const float x0 = fmaf(t.n1, vz, -t.n2 * vy);
   const float x1 = fmaf(t.n2, vx, -t.n0 * vz);
   const float x2 = fmaf(t.n0, vy, -t.n1 * vx);
-  const float s2 = nv_raw > 0.0f ? fmaf(x0, x0, fmaf(x1, x1, x2 * x2)) * inv_d2 : 1.0f;
+  const float s2c = fmaf(x0, x0, fmaf(x1, x1, x2 * x2)) * inv_d2;
+  const float s2 = nv_raw > 0.0f ? s2c : 1.0f;
   const float c2 = nv * nv;
   const float den = fmaf(c2, t.a2, s2);
   const float rE = rcp_approx(fmaf(kPi, den * den, kEps));
@@ -370,6 +374,7 @@ __device__ __forceinline__ void coloc_view(const TexelC& t, const View& vw, cons
   const float rQ = rcp_approx(fmaf(4.0f, c2, kEps));
   const float DGQ = D * G * rQ;
   const float W = nv * inv_d2;
+  const float P[3] = {P0, P1, P2};
   float gDGQ = 0.f, gW = 0.f;
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
@@ -385,8 +390,8 @@ __device__ __forceinline__ void coloc_view(const TexelC& t, const View& vw, cons
       gout = e;
     } else {
       const float op1 = 1.0f + out;
-      const float lo = lg2_approx(op1) * kLn2;
-      e = lo - (LOSS == kLossLog1p ? log1p_fast(tg[c]) : tg[c]);
+      e = (LOSS == kLossLog1p) ? lg2_approx(op1) - lg2_approx(1.0f + tg[c])
+                               : fmaf(-tg[c], 1.44269504088896341f, lg2_approx(op1));
       gout = e * rcp_approx(op1);
     }
     a.loss = fmaf(e, e, a.loss);
@@ -417,33 +422,23 @@ __device__ __forceinline__ void coloc_view(const TexelC& t, const View& vw, cons
 __device__ __forceinline__ float pow22(float base) { return ex2_approx(2.2f * lg2_approx(base)); }
 __device__ __forceinline__ float dpow22(float x, float base) { return base > 0.0f ? 1.1f * x * rcp_approx(base) : 0.0f; }
 
-// Render, loss and adjoint of one co-located texel (all views co-located). `t9` holds the
-// parameters already clamped to [-1, 1]. Returns the summed squared error; g[9] receives
-// dL/dt scaled by `scale` (the loss normaliser).
-template <int LOSS, bool GRAD_POW, typename TgtFn>
-__device__ __forceinline__ float coloc_texel(const float t9[9], float px, float py, int V, const View* views,
-                                             const float P[3], float scale, TgtFn tgt_at, float g[9], float gp[3]) {
-  TexelC t;
-  float bd[3], bs[3], d[3], sp[3];
+// Per-texel constants of the co-located loop from parameters clamped to [-1, 1].
+__device__ __forceinline__ void coloc_prepare(const float t9[9], float px, float py, TexelC& t) {
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    bd[c] = (t9[c] + 1.0f) * 0.5f;
-    bs[c] = (t9[6 + c] + 1.0f) * 0.5f;
-    d[c] = pow22(bd[c]);
-    sp[c] = pow22(bs[c]);
-    const float oms = 1.0f - sp[c];
-    t.f1[c] = d[c] * kInvPi * oms;
-    t.F[c] = fmaf(oms, kSphgColoc, sp[c]);
+    const float d = pow22((t9[c] + 1.0f) * 0.5f);
+    const float sp = pow22((t9[6 + c] + 1.0f) * 0.5f);
+    const float oms = 1.0f - sp;
+    t.f1[c] = d * kInvPi * oms;
+    t.F[c] = fmaf(oms, kSphgColoc, sp);
   }
-  const float br = (t9[5] + 1.0f) * 0.5f;
-  const float r = pow22(br);
+  const float r = pow22((t9[5] + 1.0f) * 0.5f);
   const float alpha = r * r;
   t.a2 = alpha * alpha;
   t.k = fmaf(alpha, 0.5f, kEps);
   t.omk = 1.0f - t.k;
-  const float nx = t9[3], ny = t9[4];  // already within [-1, 1]
-  const float sxy_raw = fmaf(nx, nx, ny * ny);
-  const float sxy = fminf(sxy_raw, 1.0f - kEps);
+  const float nx = t9[3], ny = t9[4];
+  const float sxy = fminf(fmaf(nx, nx, ny * ny), 1.0f - kEps);
   const float nz = sqrt_approx(1.0f - sxy);
   const float inv = rsqrt_approx(fmaf(nx, nx, fmaf(ny, ny, nz * nz)));
   t.n0 = nx * inv;
@@ -451,25 +446,39 @@ __device__ __forceinline__ float coloc_texel(const float t9[9], float px, float 
   t.n2 = nz * inv;
   t.px = px;
   t.py = py;
-  AccC a;
+}
+
+__device__ __forceinline__ void acc_zero(AccC& a) {
 #pragma unroll
   for (int c = 0; c < 3; ++c) { a.gf1[c] = 0.f; a.gfd[c] = 0.f; a.gp[c] = 0.f; }
   a.ga2 = a.gk = a.gn0 = a.gn1 = a.gn2 = a.loss = 0.f;
-  for (int v = 0; v < V; ++v) {
-    float tg[3];
-    tgt_at(v, tg);
-    coloc_view<LOSS, GRAD_POW>(t, views[v], P, tg, a);
-  }
-  const float sc = scale * kInvGamma;
+}
+
+// Map the co-located sums back to dL/dt (scaled by `scale`, the loss normaliser) and
+// return the texel's squared error. The maps are re-derived from t9 rather than kept live
+// through the view loop.
+template <int LOSS, bool GRAD_POW>
+__device__ __forceinline__ float coloc_finish(const float t9[9], const TexelC& t, const AccC& a, float scale,
+                                              float g[9], float gp[3]) {
+  const float unit = (LOSS == kLossMSE) ? 1.0f : kLn2;  // log1p errors were kept in log2 units
+  const float sc = scale * kInvGamma * unit;
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    const float oms = 1.0f - sp[c];
-    g[c] = a.gf1[c] * oms * kInvPi * dpow22(d[c], bd[c]) * sc;
-    g[6 + c] = fmaf(a.gfd[c], 1.0f - kSphgColoc, -a.gf1[c] * d[c] * kInvPi) * dpow22(sp[c], bs[c]) * sc;
+    const float bd = (t9[c] + 1.0f) * 0.5f, bs = (t9[6 + c] + 1.0f) * 0.5f;
+    const float d = pow22(bd), sp = pow22(bs);
+    g[c] = a.gf1[c] * (1.0f - sp) * kInvPi * dpow22(d, bd) * sc;
+    g[6 + c] = fmaf(a.gfd[c], 1.0f - kSphgColoc, -a.gf1[c] * d * kInvPi) * dpow22(sp, bs) * sc;
   }
+  const float br = (t9[5] + 1.0f) * 0.5f;
+  const float r = pow22(br);
+  const float alpha = r * r;
   const float galpha = fmaf(a.ga2, 2.0f * alpha, a.gk * 0.5f);
   g[5] = galpha * 2.0f * r * dpow22(r, br) * sc;
   // normal: n = m/|m|, m = (nx, ny, sqrt(1 - min(nx^2+ny^2, 1-eps)))
+  const float nx = t9[3], ny = t9[4];
+  const float sxy_raw = fmaf(nx, nx, ny * ny);
+  const float nz = sqrt_approx(1.0f - fminf(sxy_raw, 1.0f - kEps));
+  const float inv = rsqrt_approx(fmaf(nx, nx, fmaf(ny, ny, nz * nz)));
   const float ndg = t.n0 * a.gn0 + t.n1 * a.gn1 + t.n2 * a.gn2;
   const float gmx = (a.gn0 - t.n0 * ndg) * inv;
   const float gmy = (a.gn1 - t.n1 * ndg) * inv;
@@ -482,7 +491,26 @@ __device__ __forceinline__ float coloc_texel(const float t9[9], float px, float 
     gp[1] += a.gp[1] * sc;
     gp[2] += a.gp[2] * sc;
   }
-  return a.loss;
+  return (LOSS == kLossMSE) ? a.loss : a.loss * (kLn2 * kLn2);
+}
+
+// Render, loss and adjoint of one texel whose views are all co-located. `t9` holds the
+// parameters already clamped to [-1, 1]; targets come from tgt_at(v, tg[3]).
+template <int LOSS, bool GRAD_POW, typename TgtFn>
+__device__ __forceinline__ float coloc_texel(const float t9[9], float px, float py, int V, const View* views,
+                                             const float P[3], float scale, TgtFn tgt_at, float g[9], float gp[3]) {
+  TexelC t;
+  coloc_prepare(t9, px, py, t);
+  AccC a;
+  acc_zero(a);
+  const float P0 = P[0], P1 = P[1], P2 = P[2];
+  for (int v = 0; v < V; ++v) {
+    float tg[3];
+    tgt_at(v, tg);
+    const View& w = views[v];
+    coloc_view<LOSS, GRAD_POW>(t, make_float4(w.cx, w.cy, w.cz, 0.f), P0, P1, P2, tg, a);
+  }
+  return coloc_finish<LOSS, GRAD_POW>(t9, t, a, scale, g, gp);
 }
 
 // torch.optim.Adam's update for one element (amsgrad off, no weight decay):

@@ -93,6 +93,26 @@ int svbrdf_fused_step(float* textures, float* exp_avg, float* exp_avg_sq, const 
                       int loss_kind, int step, float lr, float beta1, float beta2, float eps,
                       float* loss_out, void* workspace, size_t workspace_bytes, void* stream);
 
+/* svbrdf_fused_step without a workspace argument. This entry point has no counterpart in
+ * the reference; it exists for callers that cannot allocate device memory at the point
+ * where they step the optimiser: for example a host application that hands this library
+ * only the tensors it already owns from its own memory pool, or that calls it from code
+ * where cudaMalloc is not allowed. Arguments and results are those of svbrdf_fused_step.
+ * The scratch it needs (a completion counter and one 16-byte partial sum per CTA) lives in
+ * a static device array of 16 + 2048*16 bytes inside the library, so a step may use at
+ * most 2048 CTAs (a GB300 uses about 300); a call that would need more returns
+ * SVBRDF_ERR_UNSUPPORTED. The call itself allocates nothing: no cudaMalloc, no cudaFree.
+ * The first call on each device looks the array up with cudaGetSymbolAddress, with that
+ * device current; make that first call before any stream capture. Every call clears the
+ * counter with cudaMemsetAsync on `stream` before its launch. All calls share the one
+ * array, so calls whose kernels overlap on the GPU (different streams, no ordering between
+ * them) race on it and give wrong losses; order them on one stream. */
+int svbrdf_fused_step_noalloc(float* textures, float* exp_avg, float* exp_avg_sq, const float* targets,
+                              const float* camera_pos, const float* light_pos, float* light_pow,
+                              float* light_adam_state, int n_views, int height, int width, float size,
+                              int loss_kind, int step, float lr, float beta1, float beta2, float eps,
+                              float* loss_out, void* stream);
+
 /* ---- batched: many materials of uneven resolution and view count in one launch ---- */
 
 /* One material of a batch. Device pointers except camera_pos/light_pos (HOST, read by the

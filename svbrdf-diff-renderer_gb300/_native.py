@@ -119,6 +119,8 @@ def _declare(L):
     L.svbrdf_render_bwd.argtypes = [P, P, P, P, I, I, I, F, P, P, P, P, S, P]
     L.svbrdf_fused_step.restype = I
     L.svbrdf_fused_step.argtypes = [P, P, P, P, P, P, P, P, I, I, I, F, I, I, F, F, F, F, P, P, S, P]
+    L.svbrdf_fused_step_noalloc.restype = I
+    L.svbrdf_fused_step_noalloc.argtypes = [P, P, P, P, P, P, P, P, I, I, I, F, I, I, F, F, F, F, P, P]
     L.svbrdf_batched_plan_bytes.restype = S
     L.svbrdf_batched_plan_bytes.argtypes = [ctypes.POINTER(svbrdf_material), I, ctypes.POINTER(svbrdf_batch_config)]
     L.svbrdf_batched_plan.restype = I
@@ -133,7 +135,8 @@ def _declare(L):
 # Every symbol include/svbrdf_gb300.h declares.
 EXPORTS = [
     "svbrdf_last_error", "svbrdf_abi_version", "svbrdf_max_views", "svbrdf_workspace_bytes",
-    "svbrdf_render_fwd", "svbrdf_render_bwd", "svbrdf_fused_step", "svbrdf_batched_plan_bytes",
+    "svbrdf_render_fwd", "svbrdf_render_bwd", "svbrdf_fused_step", "svbrdf_fused_step_noalloc",
+    "svbrdf_batched_plan_bytes",
     "svbrdf_batched_plan", "svbrdf_batched_workspace_bytes", "svbrdf_batched_step",
 ]
 

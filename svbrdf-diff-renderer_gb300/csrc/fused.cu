@@ -16,6 +16,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <mutex>
 #include <numeric>
 #include <vector>
 
@@ -769,6 +770,96 @@ int svbrdf_fused_step(float* textures, float* exp_avg, float* exp_avg_sq, const 
   }
 #undef SVB_FUSED
   return check_launch("fused_step_kernel");
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- no-allocation variant
+// svbrdf_fused_step_noalloc runs the same fused_step_kernel as svbrdf_fused_step, but its
+// scratch (the completion counter and one float4 of partial sums per CTA) lives in this
+// file-scope device array instead of a caller workspace. Every GPU that loads the library
+// holds these 32 KB until the process exits.
+namespace svb {
+constexpr int kNoAllocMaxBlocks = 2048;
+constexpr size_t kNoAllocScratchBytes = 16 + (size_t)kNoAllocMaxBlocks * sizeof(float4);
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+// Device address of g_noalloc_scratch on the current device. Host code cannot use the
+// symbol's name as a pointer, so it is resolved once per device (with that device
+// current) through cudaGetSymbolAddress and cached.
+static int noalloc_scratch(void** out) {
+  static std::mutex mu;
+  static void* cache[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return fail(SVBRDF_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
+  if (dev < 0 || dev >= 64) return fail(SVBRDF_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
+  std::lock_guard<std::mutex> lock(mu);
+  if (!cache[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+      cudaGetLastError();
+      return fail(SVBRDF_ERR_CUDA, "cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(e));
+    }
+    cache[dev] = p;
+  }
+  *out = cache[dev];
+  return SVBRDF_OK;
+}
+}  // namespace svb
+
+extern "C" {
+
+int svbrdf_fused_step_noalloc(float* textures, float* exp_avg, float* exp_avg_sq, const float* targets,
+                              const float* camera_pos, const float* light_pos, float* light_pow,
+                              float* light_adam_state, int n_views, int height, int width, float size,
+                              int loss_kind, int step, float lr, float beta1, float beta2, float eps,
+                              float* loss_out, void* stream) {
+  int rc = check_common(textures, camera_pos, light_pos, light_pow, n_views, height, width, size);
+  if (rc) return rc;
+  if (!exp_avg || !exp_avg_sq || !targets || !loss_out)
+    return fail(SVBRDF_ERR_INVALID, "null exp_avg/exp_avg_sq/targets/loss_out");
+  if (loss_kind < SVBRDF_LOSS_MSE || loss_kind > SVBRDF_LOSS_LOG1P_PRE)
+    return fail(SVBRDF_ERR_INVALID, "bad loss_kind %d", loss_kind);
+  if (step < 1) return fail(SVBRDF_ERR_INVALID, "step must be >= 1");
+  void* scratch = nullptr;
+  rc = noalloc_scratch(&scratch);
+  if (rc) return rc;
+  const long long T = (long long)height * width;
+  const double N = 3.0 * n_views * (double)T;
+  const float scale = (float)(2.0 / N);
+  const AdamScalars adam = make_adam(step, lr, beta1, beta2, eps);
+  unsigned* counter = (unsigned*)scratch;
+  float4* partials = (float4*)((char*)scratch + 16);
+  cudaStream_t st = (cudaStream_t)stream;
+  const bool gp = light_adam_state != nullptr;
+  // the counter must start at zero; the array keeps whatever the previous call left
+  cudaError_t e = cudaMemsetAsync(counter, 0, 16, st);
+  if (e != cudaSuccess) return fail(SVBRDF_ERR_CUDA, "cudaMemsetAsync(scratch counter): %s", cudaGetErrorString(e));
+#define SVB_FUSED_NA(L, G)                                                                                       \
+  {                                                                                                              \
+    static int occ = occupancy_of(fused_step_kernel<L, G>, kFusedThreads);                                       \
+    const int grid = grid_for(T, kFusedThreads, occ);                                                            \
+    if (grid > kNoAllocMaxBlocks)                                                                                \
+      return fail(SVBRDF_ERR_UNSUPPORTED, "no-allocation step needs %d CTAs of scratch; the static array holds %d", \
+                  grid, kNoAllocMaxBlocks);                                                                      \
+    fused_step_kernel<L, G><<<grid, kFusedThreads, 0, st>>>(textures, exp_avg, exp_avg_sq, targets, camera_pos,   \
+                                                            light_pos, light_pow, light_adam_state, n_views,      \
+                                                            height, width, size, scale, 1.0 / N, adam,            \
+                                                            loss_out, partials, counter);                         \
+  }
+  if (gp) {
+    if (loss_kind == SVBRDF_LOSS_MSE) SVB_FUSED_NA(0, true)
+    else if (loss_kind == SVBRDF_LOSS_LOG1P) SVB_FUSED_NA(1, true)
+    else SVB_FUSED_NA(2, true)
+  } else {
+    if (loss_kind == SVBRDF_LOSS_MSE) SVB_FUSED_NA(0, false)
+    else if (loss_kind == SVBRDF_LOSS_LOG1P) SVB_FUSED_NA(1, false)
+    else SVB_FUSED_NA(2, false)
+  }
+#undef SVB_FUSED_NA
+  return check_launch("fused_step_kernel (no-allocation)");
 }
 
 size_t svbrdf_batched_plan_bytes(const svbrdf_material* materials, int n_materials,

@@ -15,8 +15,9 @@ from . import _native
 from ._native import SvbrdfError, build
 from .batched import BatchConfig, BatchedOptim, autotune
 from .microfacet import Microfacet
-from .svbrdf import SvbrdfOptim
-from . import scenes
+from .svbrdf import SvbrdfIO, SvbrdfOptim
+from .scripts import optim_perpixel, render
+from . import imageio, scenes
 
-__all__ = ["Microfacet", "SvbrdfOptim", "BatchedOptim", "BatchConfig", "autotune", "SvbrdfError", "build", "scenes",
-           "_native"]
+__all__ = ["Microfacet", "SvbrdfOptim", "SvbrdfIO", "optim_perpixel", "render", "BatchedOptim", "BatchConfig",
+           "autotune", "SvbrdfError", "build", "scenes", "imageio", "_native"]

@@ -319,9 +319,9 @@ batched_step_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
 //
 // One producer warp streams, per tile of NT = 32*NCW texels, the chunks
 //   P  = the 9 parameter planes,
-//   Tc = target planes of views 3c .. 3c+2 (3 planes per view),  c = 0 .. ceil(V/3)-1,
+//   Tc = target planes of views 4c .. 4c+3 (3 planes per view),  c = 0 .. ceil(V/4)-1,
 //   M  = the 9 exp_avg planes,  S = the 9 exp_avg_sq planes
-// into a ring of shared-memory slots of 9 planes x NT floats with cp.async.bulk (the
+// into a ring of shared-memory slots of 12 planes x NT floats with cp.async.bulk (the
 // non-tensor TMA path). Each slot has an mbarrier signalling "full" (transaction bytes)
 // and one signalling "empty" (one arrival per consumer warp). The NCW consumer warps own
 // one texel per thread and read everything from shared memory, so the bytes in flight
@@ -330,7 +330,7 @@ batched_step_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
 // workspace, stops issuing, drains its in-flight copies and returns.
 
 constexpr int kMaxRing = 64;
-constexpr int kSlotPlanes = 9;
+constexpr int kSlotPlanes = 12;  // 9 parameter/moment planes, or 4 views x 3 target planes
 constexpr uint32_t kSpinLimit = 1u << 22;
 constexpr size_t kRingBudget = 200 * 1024;
 
@@ -409,6 +409,7 @@ batched_tma_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restri
   __shared__ __align__(8) uint64_t full_bar[kMaxRing];
   __shared__ __align__(8) uint64_t empty_bar[kMaxRing];
   __shared__ View s_views[kMaxViews];
+  __shared__ __align__(8) float s_cx[kMaxViews + 2], s_cy[kMaxViews + 2], s_cz[kMaxViews + 2];
   __shared__ MatDesc s_md;
   __shared__ float s_pow[3];
   __shared__ AdamScalars s_adam;
@@ -451,7 +452,7 @@ batched_tma_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restri
         const MatDesc md = mats[tl.x];
         const int T = md.H * md.W, V = md.V;
         const uint32_t bytes = (uint32_t)min(NT, T - tl.y) * 4u;
-        const int nt = (V + 2) / 3;
+        const int nt = (V + 3) / 4;
         for (int q = 0; q < nt + 3; ++q) {
           if (issued >= R && !wait_phase(smem_u32(&empty_bar[slot]), phase ^ 1u, err, kDevTimeoutEmpty)) {
             ok = false;
@@ -460,7 +461,7 @@ batched_tma_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restri
           const float* base;
           int plane0, nplanes;
           if (q == 0) { base = md.tex; plane0 = 0; nplanes = 9; }
-          else if (q <= nt) { base = md.tgt; plane0 = 9 * (q - 1); nplanes = min(9, 3 * V - plane0); }
+          else if (q <= nt) { base = md.tgt; plane0 = 12 * (q - 1); nplanes = min(12, 3 * V - plane0); }
           else if (q == nt + 1) { base = md.m1; plane0 = 0; nplanes = 9; }
           else { base = md.m2; plane0 = 0; nplanes = 9; }
           const uint32_t fb = smem_u32(&full_bar[slot]);
@@ -499,7 +500,13 @@ batched_tma_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restri
         cur = tl.x;
         if (tid == 0) s_md = mats[cur];
         const int vo = mats[cur].view_off, nv = mats[cur].V;
-        for (int v = tid; v < nv; v += NT) s_views[v] = views[vo + v];
+        for (int v = tid; v < nv; v += NT) {
+          const View w = views[vo + v];
+          s_views[v] = w;
+          s_cx[v] = w.cx;
+          s_cy[v] = w.cy;
+          s_cz[v] = w.cz;
+        }
         if (tid < 3) s_pow[tid] = mats[cur].lpow[tid];
         named_sync(1, NT);
       }
@@ -528,27 +535,51 @@ batched_tma_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restri
       float g[9], gp[3];
       float loss;
       if (s_md.all_coloc) {
-        TexelC tc;
-        coloc_prepare(t9, px, py, tc);
+        TexelC2 tp;
+        {
+          TexelC tc;
+          coloc_prepare(t9, px, py, tc);
+          pack_texel(tc, tp);
+        }
+        AccC2 ap;
+        acc2_zero(ap);
         AccC a;
         acc_zero(a);
-        const float P0 = s_pow[0], P1 = s_pow[1], P2 = s_pow[2];
-        for (int v0 = 0; v0 < V; v0 += 3) {
+        const float2 PP[3] = {bc2(s_pow[0]), bc2(s_pow[1]), bc2(s_pow[2])};
+        for (int v0 = 0; v0 < V; v0 += 4) {
           const float* sl = ring_acquire<NT>(rc, ring, full_bar, err);
-          const int nv = min(3, V - v0);
+          const int nv = min(4, V - v0);
 #pragma unroll
-          for (int j = 0; j < 3; ++j) {
-            if (j < nv) {
-              float tg[3];
-              tg[0] = sl[(3 * j + 0) * NT + tid];
-              tg[1] = sl[(3 * j + 1) * NT + tid];
-              tg[2] = sl[(3 * j + 2) * NT + tid];
-              const float4 cam = *reinterpret_cast<const float4*>(&s_views[v0 + j]);
-              coloc_view<LOSS, false>(tc, cam, P0, P1, P2, tg, a);
+          for (int j = 0; j < 4; j += 2) {
+            if (j + 1 < nv) {
+              float2 tg[3];
+#pragma unroll
+              for (int c = 0; c < 3; ++c) tg[c] = make_float2(sl[(3 * j + c) * NT + tid], sl[(3 * j + 3 + c) * NT + tid]);
+              const float2 cx = *reinterpret_cast<const float2*>(&s_cx[v0 + j]);
+              const float2 cy = *reinterpret_cast<const float2*>(&s_cy[v0 + j]);
+              const float2 cz = *reinterpret_cast<const float2*>(&s_cz[v0 + j]);
+              coloc_view2<LOSS>(tp, cx, cy, cz, PP, tg, ap);
             }
+          }
+          if (nv & 1) {  // odd last view of the material
+            const int j = nv - 1;
+            float tg[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) tg[c] = sl[(3 * j + c) * NT + tid];
+            TexelC tc;
+            tc.n0 = tp.n0.x; tc.n1 = tp.n1.x; tc.n2 = tp.n2.x;
+            tc.px = -tp.mpx.x; tc.py = -tp.mpy.x;
+            tc.a2 = tp.a2.x; tc.k = tp.k.x; tc.omk = tp.omk.x;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) { tc.f1[c] = tp.f1[c].x; tc.F[c] = tp.F[c].x; }
+            coloc_view<LOSS, false>(tc, make_float4(s_cx[v0 + j], s_cy[v0 + j], s_cz[v0 + j], 0.f), s_pow[0],
+                                    s_pow[1], s_pow[2], tg, a);
           }
           ring_release(rc, empty_bar, R);
         }
+        acc2_fold(ap, a);
+        TexelC tc;
+        tc.n0 = tp.n0.x; tc.n1 = tp.n1.x; tc.n2 = tp.n2.x;
         loss = coloc_finish<LOSS, false>(t9, tc, a, scale, g, gp);
 #pragma unroll
         for (int c = 0; c < 9; ++c) g[c] = (raw[c] >= -1.0f && raw[c] <= 1.0f) ? g[c] : 0.0f;
@@ -558,9 +589,9 @@ batched_tma_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restri
         Adj a;
         adj_zero(a);
         loss = 0.f;
-        for (int v0 = 0; v0 < V; v0 += 3) {
+        for (int v0 = 0; v0 < V; v0 += 4) {
           const float* sl = ring_acquire<NT>(rc, ring, full_bar, err);
-          const int nv = min(3, V - v0);
+          const int nv = min(4, V - v0);
           for (int j = 0; j < nv; ++j) {
             float io[3];
             io[0] = sl[(3 * j + 0) * NT + tid];

@@ -513,6 +513,130 @@ __device__ __forceinline__ float coloc_texel(const float t9[9], float px, float 
   return coloc_finish<LOSS, GRAD_POW>(t9, t, a, scale, g, gp);
 }
 
+// ---------------------------------------------------------------- packed two-view path
+// Blackwell issues FP32x2 (FFMA2/FMUL2/FADD2): one instruction does the same FP32 work
+// on two lanes. The co-located loop runs two views per step, lane x = view v and lane
+// y = view v+1, with the texel constants broadcast into both lanes; MUFU, min/max and
+// select stay per lane.
+__device__ __forceinline__ float2 bc2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 rcp2(float2 a) { return make_float2(rcp_approx(a.x), rcp_approx(a.y)); }
+__device__ __forceinline__ float2 rsqrt2(float2 a) { return make_float2(rsqrt_approx(a.x), rsqrt_approx(a.y)); }
+__device__ __forceinline__ float2 lg22(float2 a) { return make_float2(lg2_approx(a.x), lg2_approx(a.y)); }
+__device__ __forceinline__ float2 ex22(float2 a) { return make_float2(ex2_approx(a.x), ex2_approx(a.y)); }
+
+struct TexelC2 {
+  float2 n0, n1, n2, mn0, mn1, mn2;  // unit normal and its negation
+  float2 mpx, mpy;                   // -position
+  float2 a2, k, omk, ma2m1x2;        // alpha^2, k, 1-k, -2(alpha^2 - 1)
+  float2 f1[3], F[3];
+};
+
+struct AccC2 {
+  float2 gf1[3], gfd[3];
+  float2 ga2, gk, gn0, gn1, gn2, loss;
+};
+
+__device__ __forceinline__ void pack_texel(const TexelC& t, TexelC2& u) {
+  u.n0 = bc2(t.n0); u.n1 = bc2(t.n1); u.n2 = bc2(t.n2);
+  u.mn0 = bc2(-t.n0); u.mn1 = bc2(-t.n1); u.mn2 = bc2(-t.n2);
+  u.mpx = bc2(-t.px); u.mpy = bc2(-t.py);
+  u.a2 = bc2(t.a2); u.k = bc2(t.k); u.omk = bc2(t.omk); u.ma2m1x2 = bc2(-2.0f * (t.a2 - 1.0f));
+#pragma unroll
+  for (int c = 0; c < 3; ++c) { u.f1[c] = bc2(t.f1[c]); u.F[c] = bc2(t.F[c]); }
+}
+
+__device__ __forceinline__ void acc2_zero(AccC2& a) {
+  const float2 z = make_float2(0.f, 0.f);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) { a.gf1[c] = z; a.gfd[c] = z; }
+  a.ga2 = a.gk = a.gn0 = a.gn1 = a.gn2 = a.loss = z;
+}
+
+// Fold the two lanes into the scalar accumulator.
+__device__ __forceinline__ void acc2_fold(const AccC2& p, AccC& a) {
+#pragma unroll
+  for (int c = 0; c < 3; ++c) { a.gf1[c] += p.gf1[c].x + p.gf1[c].y; a.gfd[c] += p.gfd[c].x + p.gfd[c].y; }
+  a.ga2 += p.ga2.x + p.ga2.y;
+  a.gk += p.gk.x + p.gk.y;
+  a.gn0 += p.gn0.x + p.gn0.y;
+  a.gn1 += p.gn1.x + p.gn1.y;
+  a.gn2 += p.gn2.x + p.gn2.y;
+  a.loss += p.loss.x + p.loss.y;
+}
+
+// Views v (lane x) and v+1 (lane y) of one co-located texel: the arithmetic of coloc_view.
+// cx/cy/cz are the two cameras, PP the light power broadcast, tg[c] the two targets.
+template <int LOSS>
+__device__ __forceinline__ void coloc_view2(const TexelC2& t, float2 cx, float2 cy, float2 cz, const float2 PP[3],
+                                            const float2 tg[3], AccC2& a) {
+  const float2 vx = add2(cx, t.mpx), vy = add2(cy, t.mpy), vz = cz;
+  const float2 q = fma2(vx, vx, fma2(vy, vy, mul2(vz, vz)));
+  const float2 iv = rsqrt2(q);
+  const float2 inv_d2 = mul2(iv, iv);
+  const float2 nvr = mul2(fma2(t.n0, vx, fma2(t.n1, vy, mul2(t.n2, vz))), iv);
+  const float2 nv = make_float2(fmaxf(nvr.x, 0.0f), fmaxf(nvr.y, 0.0f));
+  const float2 x0 = fma2(t.n1, vz, mul2(t.mn2, vy));
+  const float2 x1 = fma2(t.n2, vx, mul2(t.mn0, vz));
+  const float2 x2 = fma2(t.n0, vy, mul2(t.mn1, vx));
+  const float2 s2c = mul2(fma2(x0, x0, fma2(x1, x1, mul2(x2, x2))), inv_d2);
+  const float2 s2 = make_float2(nvr.x > 0.0f ? s2c.x : 1.0f, nvr.y > 0.0f ? s2c.y : 1.0f);
+  const float2 c2 = mul2(nv, nv);
+  const float2 den = fma2(c2, t.a2, s2);
+  const float2 rE = rcp2(fma2(bc2(kPi), mul2(den, den), bc2(kEps)));
+  const float2 D = mul2(t.a2, rE);
+  const float2 rB = rcp2(fma2(nv, t.omk, t.k));
+  const float2 G1 = mul2(nv, rB);
+  const float2 rQ = rcp2(fma2(bc2(4.0f), c2, bc2(kEps)));
+  const float2 DGQ = mul2(mul2(D, mul2(G1, G1)), rQ);
+  const float2 W = mul2(nv, inv_d2);
+  float2 gDGQ = make_float2(0.f, 0.f), gW = make_float2(0.f, 0.f);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const float2 f = fma2(DGQ, t.F[c], t.f1[c]);
+    const float2 PW = mul2(PP[c], W);
+    const float2 img = mul2(f, PW);
+    const float2 x = make_float2(fminf(fmaxf(img.x, kEps), 1.0f), fminf(fmaxf(img.y, kEps), 1.0f));
+    const float2 xp = ex22(mul2(lg22(x), bc2(kInvGamma - 1.0f)));
+    const float2 out = mul2(x, xp);
+    float2 e, gout;
+    if (LOSS == kLossMSE) {
+      e = add2(out, make_float2(-tg[c].x, -tg[c].y));
+      gout = e;
+    } else {
+      const float2 op1 = add2(out, bc2(1.0f));
+      const float2 lo = lg22(op1);
+      e = (LOSS == kLossLog1p) ? add2(lo, make_float2(-lg2_approx(1.0f + tg[c].x), -lg2_approx(1.0f + tg[c].y)))
+                               : fma2(tg[c], bc2(-1.44269504088896341f), lo);
+      gout = mul2(e, rcp2(op1));
+    }
+    a.loss = fma2(e, e, a.loss);
+    const float2 gm = mul2(gout, xp);
+    const float2 gimg = make_float2(x.x == img.x ? gm.x : 0.0f, x.y == img.y ? gm.y : 0.0f);
+    const float2 gf = mul2(gimg, PW);
+    gW = fma2(gimg, mul2(PP[c], f), gW);
+    a.gf1[c] = add2(a.gf1[c], gf);
+    gDGQ = fma2(gf, t.F[c], gDGQ);
+    a.gfd[c] = fma2(gf, DGQ, a.gfd[c]);
+  }
+  const float2 tq = mul2(gDGQ, rQ);
+  const float2 gD = mul2(tq, mul2(G1, G1));
+  const float2 gG1 = mul2(mul2(tq, D), add2(G1, G1));
+  const float2 rB2 = mul2(rB, rB);
+  float2 gnv = fma2(mul2(gG1, t.k), rB2, fma2(mul2(tq, mul2(DGQ, bc2(-8.0f))), nv, mul2(gW, inv_d2)));
+  a.gk = fma2(mul2(mul2(gG1, nv), fma2(nv, bc2(1.0f), bc2(-1.0f))), rB2, a.gk);  // -gG1 nv (1-nv) rB^2
+  const float2 t2 = mul2(mul2(D, rE), mul2(bc2(2.0f * kPi), den));
+  a.ga2 = fma2(gD, fma2(mul2(t2, bc2(-1.0f)), c2, rE), a.ga2);
+  gnv = fma2(mul2(mul2(gD, t2), t.ma2m1x2), nv, gnv);
+  const float2 gsv = mul2(gnv, iv);
+  const float2 gs = make_float2(nvr.x >= 0.0f ? gsv.x : 0.0f, nvr.y >= 0.0f ? gsv.y : 0.0f);
+  a.gn0 = fma2(gs, vx, a.gn0);
+  a.gn1 = fma2(gs, vy, a.gn1);
+  a.gn2 = fma2(gs, vz, a.gn2);
+}
+
 // torch.optim.Adam's update for one element (amsgrad off, no weight decay):
 //   m.lerp_(g, 1-b1); v.mul_(b2).addcmul_(g, g, 1-b2);
 //   p.addcdiv_(m, sqrt(v)/sqrt(bc2) + eps, -lr/bc1)

@@ -1,0 +1,58 @@
+"""Pipeline drop-ins: ``render`` and ``optim_perpixel`` (src/scripts.py:31-41, 67-97).
+
+Same arguments and file layout as the reference: a scene JSON read by ``SvbrdfIO``,
+target photos ``{idx:02d}.png`` in ``target_dir``, maps ``nom/dif/spe/rgh.png`` in
+``reference_dir`` / ``optimize_dir``, re-renders in ``rerender_dir``. The optimisation runs
+on the fused sm_103a kernel (``SvbrdfOptim``); there is no CPU path.
+"""
+from __future__ import annotations
+
+import pathlib
+
+import torch
+
+from .microfacet import Microfacet
+from .svbrdf import SvbrdfIO, SvbrdfOptim
+
+
+def render(json_dir, res, device="cuda:0"):
+    """Render the reference maps of the scene to ``target_dir`` (src/scripts.py:31-41)."""
+    io = SvbrdfIO(pathlib.Path(json_dir), device)
+    textures = io.load_textures_th(io.reference_dir, res)
+    r = Microfacet(res, io.n_of_imgs, io.im_size, io.cl, device)
+    with torch.no_grad():
+        out = r.eval(textures)
+    io.save_images_th(out, io.target_dir)
+    return out
+
+
+def optim_perpixel(json_dir, res, lr, epochs, tex_init, optim_light=False, device="cuda:0", loss="mse",
+                   graph=True, seed=None):
+    """Per-pixel SVBRDF fit (src/scripts.py:67-97): targets -> fused optimisation -> maps.
+
+    ``tex_init`` is "random", "const" or "textures" (the maps in ``reference_dir``). Returns
+    the ``SvbrdfOptim`` (its ``textures``, ``loss_image_list``, Adam moments).
+    """
+    io = SvbrdfIO(pathlib.Path(json_dir), device)
+    targets = io.load_images_th(io.target_dir, res)
+    renderer = Microfacet(res, io.n_of_imgs, io.im_size, io.cl, device)
+    opt = SvbrdfOptim(device, renderer, loss=loss, graph=graph and not optim_light)
+    opt.load_targets(targets)
+    if tex_init == "random":
+        if seed is not None:
+            torch.manual_seed(seed)
+        opt.init_from_randn()
+    elif tex_init == "const":
+        opt.init_from_const()
+    elif tex_init == "textures":
+        opt.init_from_tex(io.load_textures_th(io.reference_dir, res))
+    else:
+        raise ValueError(f"tex_init must be 'random', 'const' or 'textures', not {tex_init!r}")
+    opt.optim(epochs, lr, io, optim_light)
+    io.save_textures_th(opt.textures.detach().clamp(-1, 1), io.optimize_dir)
+    if optim_light:
+        renderer.update_light(io.cl[2].detach())
+    with torch.no_grad():
+        out = renderer.eval(opt.textures.detach().clamp(-1, 1))
+    io.save_images_th(out, io.rerender_dir)
+    return opt

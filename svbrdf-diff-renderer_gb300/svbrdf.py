@@ -191,3 +191,102 @@ class SvbrdfOptim:
                 r.update_light(lp_dev.clone())
             self.light_exp_avg, self.light_exp_avg_sq = lstate[:3].clone(), lstate[3:].clone()
         self.light_pow = lp_dev
+
+
+class SvbrdfIO:
+    """Scene and map I/O of the reference (src/svbrdf.py:86-221), on the package's own PNG codec.
+
+    JSON keys (all optional, paths relative to the JSON file): reference_dir, target_dir,
+    optimize_dir, rerender_dir, im_size (cm), idx (view ids), camera_pos, light_pos,
+    light_pow. ``cl = [camera_pos[idx], light_pos[idx], light_pow]`` as FP32 tensors on
+    ``device`` (src/svbrdf.py:134-146). Errors raise instead of printing and exiting.
+    """
+
+    def __init__(self, json_dir, device):
+        import json
+
+        self.device = torch.device(device)
+        json_dir = pathlib.Path(json_dir)
+        if not json_dir.exists():
+            raise FileNotFoundError(f"{json_dir} does not exist")
+        data = json.loads(json_dir.read_text())
+        for key in ("reference_dir", "target_dir", "optimize_dir", "rerender_dir"):
+            if key in data:
+                setattr(self, key, json_dir.parent / data[key])
+        if "im_size" in data:
+            self.im_size = data["im_size"]
+        if "idx" in data:
+            self.idx = list(data["idx"])
+            self.n_of_imgs = len(self.idx)
+        for key in ("camera_pos", "light_pos"):
+            if key in data:
+                setattr(self, key, data[key])
+        if "light_pow" in data:
+            self.light_pow = data["light_pow"]
+            self.load_calibration_th()
+
+    def load_calibration_th(self):
+        import numpy as np
+
+        cam = np.asarray(self.camera_pos, dtype=np.float32)[self.idx, :]
+        lit = np.asarray(self.light_pos, dtype=np.float32)[self.idx, :]
+        pw = np.asarray(self.light_pow, dtype=np.float32)
+        self.cl = [torch.from_numpy(cam).to(self.device), torch.from_numpy(lit).to(self.device),
+                   torch.from_numpy(pw).to(self.device)]
+
+    def load_textures_th(self, textures_dir, res):
+        """[1, 9, res, res] in [-1, 1] from nom/dif/spe/rgh.png (src/svbrdf.py:150-166)."""
+        from .imageio import imread
+
+        d = pathlib.Path(textures_dir)
+        normal = imread(d / "nom.png", "normal", (res, res))
+        diffuse = imread(d / "dif.png", "srgb", (res, res))
+        specular = imread(d / "spe.png", "srgb", (res, res))
+        roughness = imread(d / "rgh.png", "rough", (res, res))
+        t = lambda a: torch.from_numpy(a).to(self.device)
+        return torch.cat((t(diffuse * 2 - 1).permute(2, 0, 1).unsqueeze(0),
+                          t(normal).permute(2, 0, 1).unsqueeze(0)[:, :2],
+                          t(roughness * 2 - 1).unsqueeze(0).unsqueeze(0),
+                          t(specular * 2 - 1).permute(2, 0, 1).unsqueeze(0)), 1)
+
+    @staticmethod
+    def _normal3(t2):
+        nx = t2[:, 0].clamp(-1, 1)
+        ny = t2[:, 1].clamp(-1, 1)
+        nz = (1 - (nx ** 2 + ny ** 2).clamp(0, 1)).sqrt()
+        n = torch.stack((nx, ny, nz), 1)
+        return n / n.norm(2.0, 1, keepdim=True)
+
+    def save_textures_th(self, textures_th, textures_dir):
+        """nom/dif/spe/rgh.png from [1, 9, H, W] (src/svbrdf.py:168-189, without the mosaic)."""
+        from .imageio import imwrite
+
+        d = pathlib.Path(textures_dir)
+        d.mkdir(parents=True, exist_ok=True)
+        t = textures_th.detach()
+        np_ = lambda x: x.squeeze(0).permute(1, 2, 0).cpu().numpy()
+        imwrite(np_(self._normal3(t[:, 3:5])), d / "nom.png", "normal")
+        imwrite(np_((t[:, 0:3] + 1) / 2), d / "dif.png", "srgb")
+        imwrite(np_((t[:, 6:9] + 1) / 2), d / "spe.png", "srgb")
+        imwrite(((t[0, 5] + 1) / 2).cpu().numpy(), d / "rgh.png", "rough")
+
+    def load_images_th(self, images_dir, res=256):
+        """[n, 3, res, res] from {idx:02d}.png (src/svbrdf.py:191-204)."""
+        from .imageio import imread
+
+        d = pathlib.Path(images_dir)
+        out = torch.zeros(self.n_of_imgs, 3, res, res, device=self.device)
+        for i, idx in enumerate(self.idx):
+            out[i] = torch.from_numpy(imread(d / f"{idx:02d}.png", "srgb", (res, res))).permute(2, 0, 1)
+        return out
+
+    def save_images_th(self, images_th, images_dir):
+        """{idx:02d}.png per view (src/svbrdf.py:206-221, without the 3x3 mosaic)."""
+        from .imageio import imwrite
+
+        d = pathlib.Path(images_dir)
+        d.mkdir(parents=True, exist_ok=True)
+        if images_th.shape[0] != self.n_of_imgs:
+            raise ValueError(f"expected {self.n_of_imgs} images, got {images_th.shape[0]}")
+        for i, idx in enumerate(self.idx):
+            imwrite(images_th[i].detach().permute(1, 2, 0).cpu().numpy(), d / f"{idx:02d}.png", "srgb")

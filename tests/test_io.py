@@ -1,0 +1,121 @@
+"""PNG codec, imread/imwrite flags (src/imageio.py:11-76 semantics), Lanczos resize and
+SvbrdfIO (src/svbrdf.py:86-221) on the host."""
+import json
+import struct
+import zlib
+
+import numpy as np
+import pytest
+import torch
+
+
+def _encode_filtered(arr, filters):
+    """Reference PNG encoder that applies the given filter type per row."""
+    h, w, ch = arr.shape
+    bpp = ch
+    rows = arr.reshape(h, w * ch).astype(np.int32)
+    out = []
+    prev = np.zeros(w * ch, np.int32)
+    for y in range(h):
+        ft = filters[y % len(filters)]
+        cur = rows[y]
+        a = np.concatenate([np.zeros(bpp, np.int32), cur[:-bpp]])
+        c = np.concatenate([np.zeros(bpp, np.int32), prev[:-bpp]])
+        b = prev
+        if ft == 0:
+            f = cur
+        elif ft == 1:
+            f = cur - a
+        elif ft == 2:
+            f = cur - b
+        elif ft == 3:
+            f = cur - ((a + b) >> 1)
+        else:
+            p = a + b - c
+            pa, pb, pc = np.abs(p - a), np.abs(p - b), np.abs(p - c)
+            f = cur - np.where((pa <= pb) & (pa <= pc), a, np.where(pb <= pc, b, c))
+        out.append(bytes([ft]) + (f & 0xFF).astype(np.uint8).tobytes())
+        prev = cur
+    raw = b"".join(out)
+
+    def chunk(kind, body):
+        return struct.pack(">I", len(body)) + kind + body + struct.pack(">I", zlib.crc32(kind + body) & 0xFFFFFFFF)
+
+    ctype = {1: 0, 3: 2, 4: 6}[ch]
+    return (b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, ctype, 0, 0, 0))
+            + chunk(b"IDAT", zlib.compress(raw)) + chunk(b"IEND", b""))
+
+
+@pytest.mark.parametrize("ch", [1, 3, 4])
+def test_png_decoder_all_filters(svb, tmp_path, ch):
+    rng = np.random.default_rng(ch)
+    arr = rng.integers(0, 256, (13, 17, ch), dtype=np.uint8)
+    p = tmp_path / "f.png"
+    p.write_bytes(_encode_filtered(arr, [0, 1, 2, 3, 4]))
+    got = svb.imageio.png_read(p)
+    assert np.array_equal(got.reshape(arr.shape), arr)
+
+
+@pytest.mark.parametrize("dtype", [np.uint8, np.uint16])
+def test_png_roundtrip(svb, tmp_path, dtype):
+    rng = np.random.default_rng(1)
+    arr = rng.integers(0, np.iinfo(dtype).max, (7, 9, 3)).astype(dtype)
+    svb.imageio.png_write(tmp_path / "a.png", arr)
+    assert np.array_equal(svb.imageio.png_read(tmp_path / "a.png"), arr)
+
+
+def test_imread_flags(svb, tmp_path):
+    io = svb.imageio
+    rng = np.random.default_rng(2)
+    rgb = rng.integers(0, 256, (8, 8, 3), dtype=np.uint8)
+    io.png_write(tmp_path / "c.png", rgb)
+    s = io.imread(tmp_path / "c.png", "srgb")
+    assert s.dtype == np.float32 and np.allclose(s, rgb / 255.0)
+    r = io.imread(tmp_path / "c.png", "rough")
+    assert r.shape == (8, 8) and np.allclose(r, (rgb / 255.0).mean(2), atol=1e-6)
+    n = io.imread(tmp_path / "c.png", "normal")
+    assert np.allclose(np.linalg.norm(n, axis=2), 1.0, atol=1e-5)
+    # imwrite normal maps [-1, 1] to 8 bits and back
+    nn = np.zeros((4, 4, 3), np.float32)
+    nn[..., 2] = 1.0
+    io.imwrite(nn, tmp_path / "n.png", "normal")
+    back = io.imread(tmp_path / "n.png", "normal")
+    assert np.allclose(back[..., 2], 1.0, atol=1e-2)
+
+
+def test_lanczos_properties(svb):
+    io = svb.imageio
+    const = np.full((16, 16, 3), 0.25, np.float32)
+    up = io.imresize(const, (32, 32))
+    assert up.shape == (32, 32, 3) and np.allclose(up, 0.25, atol=1e-6)
+    ramp = np.tile(np.linspace(0, 1, 32, dtype=np.float32), (32, 1))
+    down = io.imresize(ramp, (16, 16))
+    # a linear ramp stays (nearly) linear and keeps its mean
+    assert abs(down.mean() - ramp.mean()) < 1e-3
+    assert np.all(np.diff(down[8]) > 0)
+    assert io.imresize(ramp, (32, 32)) is ramp
+
+
+def test_svbrdfio_roundtrip(svb, tmp_path):
+    cams = [[-3, 3, 16], [0, 3, 16], [3, 3, 16], [-3, 0, 16]]
+    cfg = {"reference_dir": "ref", "target_dir": "tgt", "optimize_dir": "opt", "rerender_dir": "rr",
+           "im_size": 6.5, "idx": [0, 2, 3], "camera_pos": cams, "light_pos": cams, "light_pow": [1400, 1500, 1600]}
+    j = tmp_path / "scene.json"
+    j.write_text(json.dumps(cfg))
+    io = svb.SvbrdfIO(j, "cpu")
+    assert io.n_of_imgs == 3 and io.im_size == 6.5
+    assert torch.equal(io.cl[0], torch.tensor([cams[0], cams[2], cams[3]], dtype=torch.float32))
+    assert torch.equal(io.cl[2], torch.tensor([1400.0, 1500.0, 1600.0]))
+    tex = svb.scenes.make_material(16, 1000)
+    io.save_textures_th(tex, io.reference_dir)
+    back = io.load_textures_th(io.reference_dir, 16)
+    assert back.shape == (1, 9, 16, 16)
+    # 8-bit quantisation of [-1, 1] maps: within 2/255 (+ normal renormalisation)
+    assert (back[:, [0, 1, 2, 5, 6, 7, 8]] - tex[:, [0, 1, 2, 5, 6, 7, 8]]).abs().max() < 2.5 / 255
+    assert (back[:, 3:5] - tex[:, 3:5]).abs().max() < 0.02
+    imgs = torch.rand(3, 3, 16, 16)
+    io.save_images_th(imgs, io.target_dir)
+    got = io.load_images_th(io.target_dir, 16)
+    assert (got - imgs).abs().max() <= 1.0 / 255 + 1e-6
+    with pytest.raises(FileNotFoundError):
+        svb.SvbrdfIO(tmp_path / "missing.json", "cpu")

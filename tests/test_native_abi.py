@@ -139,7 +139,7 @@ def test_pipelined_plan_ring_and_workspace(svb, lib):
     hdr = np.frombuffer(buf[:64].tobytes(), np.int32)
     n_tiles, variant, ring = hdr[2], hdr[13], hdr[14]
     assert variant == 1
-    assert 2 <= ring <= 64 and ring * 9 * 480 * 4 <= 200 * 1024
+    assert 2 <= ring <= 64 and ring * 12 * 480 * 4 <= 200 * 1024
     # one partial loss per (tile, consumer warp) after the 256-byte header
     assert lib.svbrdf_batched_workspace_bytes(buf.ctypes.data) == 256 + 4 * n_tiles * (480 // 32)
     # coordinate tables: the reference's pixel-centre grid (src/microfacet.py:16-19)

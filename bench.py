@@ -350,12 +350,13 @@ def impl_ours(args):
     launch_ms = ms / (args.steps * args.iters)
     peak, peak_kind = peaks()
     achieved = abytes / (launch_ms / 1e3) / 1e9
+    # DRAM bytes per launch: an ncu capture of a smaller case of the same kernel, scaled to
+    # this launch by the algorithmic bytes (traffic is proportional to texels x views)
     traffic = None
-    tfile = HERE / "profiles" / "batched_step_kernel_traffic.json"
-    if tfile.exists():
+    tfile = HERE / "profiles" / "batched_tma_kernel_traffic.json"
+    if tfile.exists() and opt.config.variant == 1:
         try:
-            tr = json.loads(tfile.read_text())
-            traffic = float(tr["dram_bytes_per_texel_iter_at_mean_v"]) * sum(H * W for H, W, _, _ in opt.meta)
+            traffic = float(json.loads(tfile.read_text())["dram_bytes_per_algorithmic_byte"]) * abytes
         except Exception:
             traffic = None
 

@@ -172,6 +172,20 @@ int svbrdf_batched_step(const void* device_plan, const void* host_plan, int loss
                         float lr, float beta1, float beta2, float eps, float* loss_hist, int hist_len,
                         void* workspace, size_t workspace_bytes, void* stream);
 
+/* ---- descriptor loss: BF16 3x3 convolutions on the tensor cores ---- */
+
+/* y = epilogue(conv3x3(x, weight)), stride 1, zero padding 1, for the VGG-feature loss of
+ * VGGLoss (src/descriptor.py:7-79; the reference runs torchvision's VGG19, :13, 43).
+ * x: BF16 NHWC [n][h][w][cin]; weight: BF16 [cout][9][cin] (tap = 3*ky + kx); y: BF16 NHWC
+ * [n][h][w][cout]. h % 8 == 0, w % 16 == 0, cin and cout multiples of 64; 16-byte aligned.
+ * epilogue 0: none; 1: bias [cout] (FP32) then ReLU; 2: multiply by (mask > 0), mask BF16
+ * NHWC like y (a ReLU mask for the backward pass). The data gradient dL/dx of a convolution
+ * is this call on dL/d(pre-activation) with weight'[cin][8 - tap][cout] = weight[cout][tap][cin].
+ * FP32 accumulation in tensor memory. `err` (one device int, zeroed by the caller) receives a
+ * non-zero code if a launch gave up waiting on its pipeline. */
+int svbrdf_conv3x3_bf16(const void* x, const void* weight, const float* bias, const void* mask, void* y, int n,
+                        int h, int w, int cin, int cout, int epilogue, int* err, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

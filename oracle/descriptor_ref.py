@@ -1,0 +1,66 @@
+"""FP64 CPU oracle of the descriptor loss.
+
+TEST INFRASTRUCTURE ONLY (tests and bench's CPU legs). Restates the VGG-feature loss of
+src/descriptor.py:7-79 with the stack the GPU module uses: 2x2 box downsample, ImageNet
+normalisation with the reference's std (0.229, 0.224, 0.255; src/descriptor.py:65-75),
+conv1_1..conv4_1 (3x3, padding 1, ReLU, 2x2 max-pool), hooks at relu1_1, relu1_2, relu3_2,
+relu4_1, and the weighted feature-L2 (src/descriptor.py:39-60, 77-79) and Gram (:50-56)
+terms. Runs in FP64 on the exact weights the BF16 kernels use, so the difference to the GPU
+measures the BF16 activations and FP32 tensor-core accumulation alone.
+"""
+from __future__ import annotations
+
+import torch
+
+MEAN = (0.485, 0.456, 0.406)
+STD = (0.229, 0.224, 0.255)
+LAYERS = [("conv1_1", 3, 64), ("conv1_2", 64, 64), "pool", ("conv2_1", 64, 128), ("conv2_2", 128, 128), "pool",
+          ("conv3_1", 128, 256), ("conv3_2", 256, 256), ("conv3_3", 256, 256), ("conv3_4", 256, 256), "pool",
+          ("conv4_1", 256, 512)]
+HOOKS = ("conv1_1", "conv1_2", "conv3_2", "conv4_1")
+
+
+def features(renders, weights, downsample=True):
+    x = renders.double()
+    if downsample:
+        x = torch.nn.functional.avg_pool2d(x, 2)
+    mean = torch.tensor(MEAN, dtype=torch.float64).view(1, 3, 1, 1)
+    std = torch.tensor(STD, dtype=torch.float64).view(1, 3, 1, 1)
+    x = (x - mean) / std
+    out = []
+    for item in LAYERS:
+        if item == "pool":
+            x = torch.nn.functional.max_pool2d(x, 2)
+            continue
+        name = item[0]
+        w, b = weights[name]
+        x = torch.relu(torch.nn.functional.conv2d(x, w.double(), b.double(), padding=1))
+        if name in HOOKS:
+            out.append(x)
+    return out
+
+
+def gram(f):
+    v, c, h, w = f.shape
+    ff = f.reshape(v, c, h * w)
+    return torch.bmm(ff, ff.transpose(1, 2)) / (h * w)
+
+
+def loss_terms(renders, targets, weights, hook_weights=(0.25, 0.25, 0.25, 0.25), downsample=True):
+    """(feature_loss, gram_loss, d(feature+gram)/d renders) in FP64."""
+    r = renders.detach().double().clone().requires_grad_(True)
+    with torch.no_grad():
+        tf = features(targets, weights, downsample)
+        tg = [gram(f) for f in tf]
+    feats = features(r, weights, downsample)
+    fl, gl, nf, ng = 0.0, 0.0, 0, 0
+    for w, f, t, g_t in zip(hook_weights, feats, tf, tg):
+        fl = fl + (w * w) * ((f - t) ** 2).sum()
+        nf += f.numel()
+        g = gram(f)
+        gl = gl + (w * w) * ((g - g_t) ** 2).sum()
+        ng += g.numel()
+    fl = fl / nf
+    gl = gl / ng
+    (fl + gl).backward()
+    return float(fl), float(gl), r.grad.detach()

@@ -17,7 +17,7 @@ from .batched import BatchConfig, BatchedOptim, autotune
 from .microfacet import Microfacet
 from .svbrdf import SvbrdfIO, SvbrdfOptim
 from .scripts import optim_perpixel, render
-from . import imageio, scenes
+from . import descriptor, imageio, scenes
 
 __all__ = ["Microfacet", "SvbrdfOptim", "SvbrdfIO", "optim_perpixel", "render", "BatchedOptim", "BatchConfig",
-           "autotune", "SvbrdfError", "build", "scenes", "imageio", "_native"]
+           "autotune", "SvbrdfError", "build", "scenes", "imageio", "descriptor", "_native"]

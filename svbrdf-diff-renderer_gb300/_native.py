@@ -20,7 +20,7 @@ CSRC = PKG / "csrc"
 INCLUDE = REPO / "include"
 LIBDIR = PKG / "_lib"
 LIBNAME = "libsvbrdf_gb300.so"
-SOURCES = ["render.cu", "fused.cu"]
+SOURCES = ["render.cu", "fused.cu", "conv_tc.cu"]
 HEADERS = ["svbrdf_math.cuh", "svbrdf_common.cuh", "svbrdf_plan.cuh"]
 WORKSPACE_ERROR_OFFSET = 4
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -121,6 +121,8 @@ def _declare(L):
     L.svbrdf_fused_step.argtypes = [P, P, P, P, P, P, P, P, I, I, I, F, I, I, F, F, F, F, P, P, S, P]
     L.svbrdf_fused_step_noalloc.restype = I
     L.svbrdf_fused_step_noalloc.argtypes = [P, P, P, P, P, P, P, P, I, I, I, F, I, I, F, F, F, F, P, P]
+    L.svbrdf_conv3x3_bf16.restype = I
+    L.svbrdf_conv3x3_bf16.argtypes = [P, P, P, P, P, I, I, I, I, I, I, P, P]
     L.svbrdf_batched_plan_bytes.restype = S
     L.svbrdf_batched_plan_bytes.argtypes = [ctypes.POINTER(svbrdf_material), I, ctypes.POINTER(svbrdf_batch_config)]
     L.svbrdf_batched_plan.restype = I
@@ -137,7 +139,7 @@ EXPORTS = [
     "svbrdf_last_error", "svbrdf_abi_version", "svbrdf_max_views", "svbrdf_workspace_bytes",
     "svbrdf_render_fwd", "svbrdf_render_bwd", "svbrdf_fused_step", "svbrdf_fused_step_noalloc",
     "svbrdf_batched_plan_bytes",
-    "svbrdf_batched_plan", "svbrdf_batched_workspace_bytes", "svbrdf_batched_step",
+    "svbrdf_batched_plan", "svbrdf_batched_workspace_bytes", "svbrdf_batched_step", "svbrdf_conv3x3_bf16",
 ]
 
 

@@ -1,0 +1,90 @@
+"""BF16 tensor-core 3x3 convolution and the descriptor loss.
+
+The convolution is checked against torch's FP32 conv2d on the same BF16 inputs (relative
+L2 <= 1e-2: the output is rounded to BF16, 2^-8 relative). The descriptor loss is checked
+per term against the FP64 CPU oracle on the same weights: feature and Gram losses within
+3e-2 relative, gradient w.r.t. the renders within 5e-2 relative L2 (BF16 activations
+through 9 convolutions)."""
+import pytest
+import torch
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def _ref_conv(x_nhwc, w_cout_tap_cin, bias=None):
+    cout, _, cin = w_cout_tap_cin.shape
+    w = w_cout_tap_cin.float().reshape(cout, 3, 3, cin).permute(0, 3, 1, 2)
+    y = torch.nn.functional.conv2d(x_nhwc.float().permute(0, 3, 1, 2), w, bias, padding=1)
+    return y.permute(0, 2, 3, 1)
+
+
+@pytest.mark.parametrize("n,h,w,cin,cout", [(1, 8, 16, 64, 64), (2, 16, 32, 64, 128), (1, 24, 48, 128, 256),
+                                            (2, 32, 32, 256, 512), (1, 8, 16, 192, 64)])
+def test_conv3x3_tc_matches_torch(svb, cuda, n, h, w, cin, cout):
+    D = svb.descriptor
+    g = torch.Generator().manual_seed(n * 1000 + cin)
+    x = torch.randn(n, h, w, cin, generator=g).to(cuda, torch.bfloat16)
+    wt = (torch.randn(cout, 9, cin, generator=g) * (2.0 / (9 * cin)) ** 0.5).to(cuda, torch.bfloat16)
+    b = (torch.randn(cout, generator=g) * 0.1).to(cuda)
+    err = torch.zeros(1, dtype=torch.int32, device=cuda)
+    y0 = D.conv3x3_bf16(x, wt, None, D.EPI_NONE, err)
+    y1 = D.conv3x3_bf16(x, wt, b, D.EPI_BIAS_RELU, err)
+    mask = torch.randn(n, h, w, cout, generator=g).to(cuda, torch.bfloat16)
+    y2 = D.conv3x3_bf16(x, wt, None, D.EPI_MASK, err, mask=mask)
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    ref = _ref_conv(x, wt)
+    assert rel_l2(y0.float(), ref) <= 1e-2
+    assert rel_l2(y1.float(), torch.relu(ref + b)) <= 1e-2
+    assert rel_l2(y2.float(), ref * (mask.float() > 0)) <= 1e-2
+
+
+def test_conv3x3_tc_data_gradient(svb, cuda):
+    D = svb.descriptor
+    g = torch.Generator().manual_seed(7)
+    n, h, w, cin, cout = 2, 16, 32, 64, 128
+    wt = torch.randn(cout, cin, 3, 3, generator=g) * 0.05
+    wb = wt.to(torch.bfloat16)
+    w_dg = wb.flip(2, 3).permute(1, 2, 3, 0).reshape(cin, 9, cout).contiguous().to(cuda)
+    gy = torch.randn(n, h, w, cout, generator=g).to(cuda, torch.bfloat16)
+    err = torch.zeros(1, dtype=torch.int32, device=cuda)
+    gx = D.conv3x3_bf16(gy, w_dg, None, D.EPI_NONE, err)
+    ref = torch.nn.grad.conv2d_input((n, cin, h, w), wb.float().to(cuda), gy.float().permute(0, 3, 1, 2), padding=1)
+    assert rel_l2(gx.float(), ref.permute(0, 2, 3, 1)) <= 1e-2
+
+
+def test_conv3x3_rejects_bad_shapes(svb, cuda):
+    D = svb.descriptor
+    err = torch.zeros(1, dtype=torch.int32, device=cuda)
+    x = torch.zeros(1, 8, 20, 64, device=cuda, dtype=torch.bfloat16)  # W not a multiple of 16
+    wt = torch.zeros(64, 9, 64, device=cuda, dtype=torch.bfloat16)
+    with pytest.raises(svb.SvbrdfError):
+        D.conv3x3_bf16(x, wt, None, D.EPI_NONE, err)
+    x = torch.zeros(1, 8, 16, 32, device=cuda, dtype=torch.bfloat16)  # Cin not a multiple of 64
+    with pytest.raises(svb.SvbrdfError):
+        D.conv3x3_bf16(x, torch.zeros(64, 9, 32, device=cuda, dtype=torch.bfloat16), None, D.EPI_NONE, err)
+
+
+def test_descriptor_loss_vs_fp64_oracle(svb, cuda):
+    from oracle import descriptor_ref as DR
+    from oracle import microfacet_ref as R
+
+    sc = svb.scenes.single_scene(res=64, seed=1008)
+    tgt = R.render(sc.gt, sc.camera_pos, sc.light_pos, sc.light_pow, sc.size, torch.float32)[:3]
+    cur = R.render((0.5 * sc.gt + 0.5 * sc.init), sc.camera_pos, sc.light_pos, sc.light_pow, sc.size,
+                   torch.float32)[:3]
+    d = svb.descriptor.VGGDescriptor(cuda, seed=3)
+    d.load(tgt.to(cuda))
+    r = cur.to(cuda).requires_grad_(True)
+    fl, gl = d.loss(r)
+    (fl + gl).backward()
+    torch.cuda.synchronize()
+    assert d.device_error() == 0
+    rfl, rgl, rgrad = DR.loss_terms(cur, tgt, d.bf16_weights())
+    e_f = abs(float(fl) - rfl) / rfl
+    e_g = abs(float(gl) - rgl) / rgl
+    e_d = rel_l2(r.grad, rgrad)
+    print(f"descriptor vs FP64: feature {e_f:.2e}, gram {e_g:.2e}, d/drender {e_d:.2e}")
+    assert e_f <= 3e-2 and e_g <= 3e-2 and e_d <= 5e-2

@@ -287,6 +287,49 @@ def time_single(dev, fused, iters, res=1024):
                            ", forward kernel + torch loss + adjoint kernel (autograd) + torch.optim.Adam")}
 
 
+def time_descriptor(dev, iters=10, views=9, res=512):
+    """Descriptor loss forward + backward over `views` renders of res^2 (2x2-downsampled to
+    (res/2)^2), VGG19-shaped conv1_1..conv4_1. Reports the tcgen05 convolutions' FLOP rate."""
+    d = PKG.descriptor.VGGDescriptor(dev, seed=0)
+    sc = PKG.scenes.single_scene(res=res, device=dev, render_fn=gpu_render_fn(dev))
+    cam, lit = sc.camera_pos[:views], sc.light_pos[:views]
+    r0 = gpu_render_fn(dev)(sc.init, cam, lit, sc.light_pow, sc.size)
+    d.load(sc.targets[:views])
+    h = res // 2
+    flops = 0.0
+    for item in PKG.descriptor.VGG19_TO_CONV4_1:
+        if item == "pool":
+            h //= 2
+            continue
+        _, cin, cout = item
+        if cin >= 64:  # the tensor-core convolutions: forward and data gradient
+            flops += 2 * 2.0 * h * h * cin * cout * 9 * views
+    for _ in range(2):
+        r = r0.clone().requires_grad_(True)
+        fl, gl = d.loss(r)
+        (fl + gl).backward()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(iters):
+        r = r0.clone().requires_grad_(True)
+        fl, gl = d.loss(r)
+        (fl + gl).backward()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / iters
+    tf = flops / (ms / 1e3) / 1e12
+    peak = 1910.1
+    try:
+        peak = float(json.loads((HERE / "MEASURED_PEAKS.json").read_text())["bf16_tflops"])
+    except Exception:
+        pass
+    return {"workload": f"{views} renders {res}^2 -> {res // 2}^2, conv1_1..conv4_1 forward + data gradient, "
+                        "feature + Gram loss", "ms_per_iteration": ms, "tc_conv_tflops": tf,
+            "tc_conv_gflop_per_iteration": flops / 1e9, "bf16_peak_tflops": peak, "frac_of_bf16_peak": tf / peak,
+            "device_error": d.device_error()}
+
+
 def impl_ours(args):
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
@@ -414,6 +457,7 @@ def impl_ours(args):
         line["plain"] = time_single(dev, fused=False, iters=20)
         line["fused_single"] = time_single(dev, fused=True, iters=200)
         line["fused_vs_plain"] = value / line["plain"]["value"]
+        line["descriptor"] = time_descriptor(dev)
         if world == 1:
             line["cpu_baseline"] = run_cpu_baseline(specs, args.cpu_seconds, os.cpu_count() or 1)
     if rank == 0:

@@ -28,8 +28,16 @@ LOSS_KINDS = {"mse": 0, "log1p": 1, "log1p_pre": 2}
 
 
 class SvbrdfOptim:
-    def __init__(self, device, renderer_obj, loss="mse", fused=True, graph=False, save_process=False):
+    def __init__(self, device, renderer_obj, loss="mse", fused=True, graph=False, save_process=False,
+                 descriptor=None, descriptor_weight=0.1):
         self.device = torch.device(device)
+        # optional descriptor (VGG-feature) term, e.g. descriptor.VGGDescriptor; like the
+        # reference's loss + 0.1 * VGG loss (src/materialgan.py:139-146) it needs the renders,
+        # so it runs the unfused form
+        self.descriptor = descriptor
+        self.descriptor_weight = float(descriptor_weight)
+        if descriptor is not None:
+            fused = False
         self.eps = 1e-4
         self.renderer_obj = renderer_obj
         self.res = renderer_obj.res
@@ -66,6 +74,8 @@ class SvbrdfOptim:
 
     def load_targets(self, targets):
         self.targets = targets.to(self.device, torch.float32).contiguous()
+        if self.descriptor is not None:
+            self.descriptor.load(self.targets)
 
     def compute_image_loss(self, predicts):
         """src/optimization.py:28-29 (MSE), or the log(1+x) L2 loss."""
@@ -124,6 +134,9 @@ class SvbrdfOptim:
             rendereds = self.renderer_obj.eval(self.textures.clamp(-1, 1))
             loss = self.compute_image_loss(rendereds)
             losses.append(loss.detach())
+            if self.descriptor is not None:
+                fl, gl = self.descriptor.loss(rendereds)
+                loss = loss + self.descriptor_weight * (fl + gl)
             self.optimizer.zero_grad()
             loss.backward()
             self.optimizer.step()

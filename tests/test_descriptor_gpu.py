@@ -3,8 +3,10 @@
 The convolution is checked against torch's FP32 conv2d on the same BF16 inputs (relative
 L2 <= 1e-2: the output is rounded to BF16, 2^-8 relative). The descriptor loss is checked
 per term against the FP64 CPU oracle on the same weights: feature and Gram losses within
-3e-2 relative, gradient w.r.t. the renders within 5e-2 relative L2 (BF16 activations
-through 9 convolutions)."""
+1e-3 relative (measured ~3e-5). The gradient w.r.t. the renders is held to relative L2
+<= 0.3 and cosine >= 0.95: rounding the activations to BF16 moves ReLU kinks and max-pool
+winners, and the FP64 oracle with its activations rounded to BF16 the same way is itself
+0.18 (relative L2) from the unrounded FP64 gradient."""
 import pytest
 import torch
 
@@ -71,10 +73,11 @@ def test_descriptor_loss_vs_fp64_oracle(svb, cuda):
     from oracle import descriptor_ref as DR
     from oracle import microfacet_ref as R
 
-    sc = svb.scenes.single_scene(res=64, seed=1008)
-    tgt = R.render(sc.gt, sc.camera_pos, sc.light_pos, sc.light_pow, sc.size, torch.float32)[:3]
-    cur = R.render((0.5 * sc.gt + 0.5 * sc.init), sc.camera_pos, sc.light_pos, sc.light_pow, sc.size,
-                   torch.float32)[:3]
+    # 256^2 renders: 128^2 after the 2x2 downsample, 16^2 at conv4_1 (the 8x16 tile minimum)
+    sc = svb.scenes.single_scene(res=256, seed=1008)
+    tgt = R.render(sc.gt, sc.camera_pos[:2], sc.light_pos[:2], sc.light_pow, sc.size, torch.float32)
+    cur = R.render((0.5 * sc.gt + 0.5 * sc.init), sc.camera_pos[:2], sc.light_pos[:2], sc.light_pow, sc.size,
+                   torch.float32)
     d = svb.descriptor.VGGDescriptor(cuda, seed=3)
     d.load(tgt.to(cuda))
     r = cur.to(cuda).requires_grad_(True)
@@ -86,5 +89,24 @@ def test_descriptor_loss_vs_fp64_oracle(svb, cuda):
     e_f = abs(float(fl) - rfl) / rfl
     e_g = abs(float(gl) - rgl) / rgl
     e_d = rel_l2(r.grad, rgrad)
-    print(f"descriptor vs FP64: feature {e_f:.2e}, gram {e_g:.2e}, d/drender {e_d:.2e}")
-    assert e_f <= 3e-2 and e_g <= 3e-2 and e_d <= 5e-2
+    a, b = r.grad.double().cpu().flatten(), rgrad.double().flatten()
+    cos = float(a @ b / (a.norm() * b.norm()))
+    print(f"descriptor vs FP64: feature {e_f:.2e}, gram {e_g:.2e}, d/drender rel-L2 {e_d:.2e}, cosine {cos:.4f}")
+    assert e_f <= 1e-3 and e_g <= 1e-3
+    assert e_d <= 0.3 and cos >= 0.95
+
+
+def test_perpixel_with_descriptor_loss(svb, cuda):
+    """The descriptor-augmented per-pixel loop (BF16 tensor-core features) lowers the loss."""
+    from oracle import microfacet_ref as R
+
+    sc = svb.scenes.single_scene(res=256, seed=1009)
+    svb.scenes.add_targets(sc, lambda *a: R.render(*a, dtype=torch.float32))
+    r = svb.Microfacet(256, 9, sc.size, [t.to(cuda) for t in sc.cl], cuda)
+    d = svb.descriptor.VGGDescriptor(cuda, seed=0)
+    o = svb.SvbrdfOptim(cuda, r, loss="log1p", descriptor=d, descriptor_weight=0.1)
+    o.load_targets(sc.targets.to(cuda))
+    o.init_from_tex(sc.init.to(cuda))
+    o.optim(8, 0.02, None, False)
+    assert d.device_error() == 0
+    assert o.loss_image_list[-1] < o.loss_image_list[0]

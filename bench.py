@@ -61,6 +61,7 @@ def parse():
     ap.add_argument("--no-extras", action="store_true", help="skip the plain/single/cpu comparison legs")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline budget")
     ap.add_argument("--config", default=None, help="threads,tile_texels[,ctas[,variant]] instead of autotuning")
+    ap.add_argument("--only", default=None, choices=["descriptor"], help="run one comparison leg alone")
     return ap.parse_args()
 
 
@@ -471,6 +472,10 @@ def impl_ours(args):
 
 def main():
     args = parse()
+    if args.only == "descriptor":
+        dev = torch.device("cuda", dist_env()[2])
+        print(json.dumps({"descriptor": time_descriptor(dev, iters=max(args.steps, 1))}), flush=True)
+        return 0
     if args.impl == "reference":
         return impl_reference(args)
     return impl_ours(args)

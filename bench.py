@@ -306,16 +306,12 @@ def time_descriptor(dev, iters=10, views=9, res=512):
         if cin >= 64:  # the tensor-core convolutions: forward and data gradient
             flops += 2 * 2.0 * h * h * cin * cout * 9 * views
     for _ in range(2):
-        r = r0.clone().requires_grad_(True)
-        fl, gl = d.loss(r)
-        (fl + gl).backward()
+        d.loss_and_grad(r0)  # captures the forward + backward graph on first use
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     for _ in range(iters):
-        r = r0.clone().requires_grad_(True)
-        fl, gl = d.loss(r)
-        (fl + gl).backward()
+        d.loss_and_grad(r0)
     e1.record()
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / iters
@@ -326,7 +322,7 @@ def time_descriptor(dev, iters=10, views=9, res=512):
     except Exception:
         pass
     return {"workload": f"{views} renders {res}^2 -> {res // 2}^2, conv1_1..conv4_1 forward + data gradient, "
-                        "feature + Gram loss", "ms_per_iteration": ms, "tc_conv_tflops": tf,
+                        "feature + Gram loss, one CUDA-graph replay per iteration", "ms_per_iteration": ms, "tc_conv_tflops": tf,
             "tc_conv_gflop_per_iteration": flops / 1e9, "bf16_peak_tflops": peak, "frac_of_bf16_peak": tf / peak,
             "device_error": d.device_error()}
 

@@ -128,7 +128,7 @@ struct Shape {
 };
 
 template <int BN, int STAGES, int EPI>
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(kThreads, 2)
 conv3x3_tc_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_constant__ CUtensorMap tmap_w,
                   const float* __restrict__ bias, const __nv_bfloat16* __restrict__ mask,
                   __nv_bfloat16* __restrict__ y, int H, int W, int Cin, int Cout, int* err) {
@@ -299,7 +299,9 @@ static int launch(const CUtensorMap& mx, const CUtensorMap& mw, const float* bia
 template <int BN>
 static int dispatch_epi(int epi, const CUtensorMap& mx, const CUtensorMap& mw, const float* bias, const void* mask,
                         void* y, int n, int h, int w, int cin, int cout, int* err, cudaStream_t st) {
-  constexpr int STAGES = BN == 256 ? 4 : (BN == 128 ? 6 : 8);
+  // 96 KB of stages per CTA: two CTAs share an SM (and its 512 TMEM columns), so one
+  // CTA's epilogue overlaps the other's main loop
+  constexpr int STAGES = BN == 256 ? 2 : (BN == 128 ? 3 : 4);
   switch (epi) {
     case kEpiNone: return launch<BN, STAGES, kEpiNone>(mx, mw, bias, mask, y, n, h, w, cin, cout, err, st);
     case kEpiBiasRelu: return launch<BN, STAGES, kEpiBiasRelu>(mx, mw, bias, mask, y, n, h, w, cin, cout, err, st);

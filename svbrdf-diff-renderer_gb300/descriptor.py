@@ -151,6 +151,7 @@ class VGGDescriptor:
         return torch.bmm(ff.transpose(1, 2), ff) / (h * w)
 
     def load(self, targets: torch.Tensor):
+        self._graph = None  # a captured graph holds the previous targets' features
         with torch.no_grad():
             feats = self.features(targets)
             self.target = ([f.float() for f in feats], [self._gram(f) for f in feats])
@@ -171,3 +172,54 @@ class VGGDescriptor:
 
     def device_error(self) -> int:
         return int(self.err.item())
+
+    # ---- CUDA-graph replay of forward + backward -------------------------------------
+    # One eager pass issues a few hundred small kernels; replaying them as one graph removes
+    # the host dispatch cost, which otherwise exceeds the GPU time of the whole stack.
+    def _capture(self, shape):
+        static_r = torch.zeros(shape, device=self.device, requires_grad=True)
+        side = torch.cuda.Stream(self.device)
+        side.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(side):
+            for _ in range(2):
+                static_r.grad = None
+                fl, gl = self.loss(static_r)
+                (fl + gl).backward()
+        torch.cuda.current_stream(self.device).wait_stream(side)
+        static_r.grad = None
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            fl, gl = self.loss(static_r)
+            (fl + gl).backward()
+        self._graph = (tuple(shape), graph, static_r, fl, gl)
+
+    def loss_and_grad(self, renders: torch.Tensor):
+        """(feature_loss, gram_loss, d(feature + gram)/d renders) by one graph replay. The
+        returned tensors are reused by the next call."""
+        if getattr(self, "_graph", None) is None or self._graph[0] != tuple(renders.shape):
+            self._capture(renders.shape)
+        _, graph, static_r, fl, gl = self._graph
+        with torch.no_grad():
+            static_r.copy_(renders)
+        graph.replay()
+        return fl, gl, static_r.grad
+
+
+class _DescriptorTerm(torch.autograd.Function):
+    """feature + Gram loss of ``renders`` with its gradient from one graph replay."""
+
+    @staticmethod
+    def forward(ctx, renders, desc):
+        fl, gl, g = desc.loss_and_grad(renders.detach())
+        ctx.save_for_backward(g.clone())
+        return (fl + gl).detach().clone()
+
+    @staticmethod
+    def backward(ctx, gout):
+        (g,) = ctx.saved_tensors
+        return gout * g, None
+
+
+def descriptor_term(renders: torch.Tensor, desc: VGGDescriptor) -> torch.Tensor:
+    """Differentiable feature + Gram descriptor loss of ``renders`` (graph-replayed)."""
+    return _DescriptorTerm.apply(renders, desc)

@@ -135,8 +135,9 @@ class SvbrdfOptim:
             loss = self.compute_image_loss(rendereds)
             losses.append(loss.detach())
             if self.descriptor is not None:
-                fl, gl = self.descriptor.loss(rendereds)
-                loss = loss + self.descriptor_weight * (fl + gl)
+                from .descriptor import descriptor_term
+
+                loss = loss + self.descriptor_weight * descriptor_term(rendereds, self.descriptor)
             self.optimizer.zero_grad()
             loss.backward()
             self.optimizer.step()

@@ -110,3 +110,22 @@ def test_perpixel_with_descriptor_loss(svb, cuda):
     o.optim(8, 0.02, None, False)
     assert d.device_error() == 0
     assert o.loss_image_list[-1] < o.loss_image_list[0]
+
+
+def test_graph_replay_matches_eager(svb, cuda):
+    from oracle import microfacet_ref as R
+
+    sc = svb.scenes.single_scene(res=256, seed=1010)
+    tgt = R.render(sc.gt, sc.camera_pos[:3], sc.light_pos[:3], sc.light_pow, sc.size, torch.float32).to(cuda)
+    cur = R.render(sc.init, sc.camera_pos[:3], sc.light_pos[:3], sc.light_pow, sc.size, torch.float32).to(cuda)
+    d = svb.descriptor.VGGDescriptor(cuda, seed=1)
+    d.load(tgt)
+    r = cur.clone().requires_grad_(True)
+    fl, gl = d.loss(r)
+    (fl + gl).backward()
+    for _ in range(2):  # capture, then a second replay
+        gfl, ggl, gg = d.loss_and_grad(cur)
+    torch.cuda.synchronize()
+    assert abs(float(gfl) - float(fl)) <= 1e-6 * float(fl)
+    assert abs(float(ggl) - float(gl)) <= 1e-6 * float(gl)
+    assert rel_l2(gg, r.grad) <= 1e-6

@@ -176,6 +176,7 @@ class VGGDescriptor:
     # ---- CUDA-graph replay of forward + backward -------------------------------------
     # One eager pass issues a few hundred small kernels; replaying them as one graph removes
     # the host dispatch cost, which otherwise exceeds the GPU time of the whole stack.
+    @torch.enable_grad()
     def _capture(self, shape):
         static_r = torch.zeros(shape, device=self.device, requires_grad=True)
         side = torch.cuda.Stream(self.device)

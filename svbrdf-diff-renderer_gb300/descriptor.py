@@ -19,8 +19,8 @@ conv4_1), weights [1, 1, 1, 1] / 4 (the reference's default).
 Every 3x3 convolution with 64 or more input channels runs as a tcgen05 implicit GEMM
 (``svbrdf_conv3x3_bf16``: BF16 operands, FP32 accumulation in TMEM, bias + ReLU fused).
 Its data gradient is the same kernel on the transposed, flipped weights. conv1_1 (3 input
-channels, under 1% of the FLOPs), the pools, the normalisation and the Gram products (plain
-GEMMs) use torch.
+channels, under 1% of the FLOPs), the pools and the normalisation use torch; the Gram
+products are plain batched BF16 GEMMs (cuBLAS tensor cores, FP32 accumulation).
 """
 from __future__ import annotations
 
@@ -70,6 +70,43 @@ class _ConvReLU(torch.autograd.Function):
         gz = (gy.to(torch.bfloat16) * (y > 0)).contiguous()
         gx = conv3x3_bf16(gz, w_dgrad, None, EPI_NONE, err)
         return gx, None, None, None, None
+
+
+_BMM_F32_OUT = {}
+
+
+def _bmm_f32out(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
+    """Batched BF16 x BF16 product on the tensor cores, FP32 accumulation, FP32 result when
+    torch exposes bmm's out_dtype (checked once per device), else a BF16 result widened."""
+    key = a.device
+    if key not in _BMM_F32_OUT:
+        try:
+            z = torch.zeros(1, 2, 2, device=a.device, dtype=torch.bfloat16)
+            _BMM_F32_OUT[key] = torch.bmm(z, z, out_dtype=torch.float32).dtype == torch.float32
+        except (TypeError, RuntimeError):
+            _BMM_F32_OUT[key] = False
+    if _BMM_F32_OUT[key]:
+        return torch.bmm(a, b, out_dtype=torch.float32)
+    return torch.bmm(a, b).float()
+
+
+class _Gram(torch.autograd.Function):
+    """G = F^T F / S for NHWC features F [V, H, W, C] (BF16); gradient F (dG + dG^T) / S."""
+
+    @staticmethod
+    def forward(ctx, f):
+        v, h, w, c = f.shape
+        ff = f.reshape(v, h * w, c).to(torch.bfloat16)
+        ctx.save_for_backward(ff)
+        ctx.shape = f.shape
+        return _bmm_f32out(ff.transpose(1, 2), ff) / (h * w)
+
+    @staticmethod
+    def backward(ctx, g):
+        (ff,) = ctx.saved_tensors
+        v, h, w, c = ctx.shape
+        gs = ((g + g.transpose(1, 2)) / (h * w)).to(torch.bfloat16)
+        return torch.bmm(ff, gs).reshape(v, h, w, c)
 
 
 def he_normal_weights(seed: int, layers=VGG19_TO_CONV4_1):
@@ -146,9 +183,7 @@ class VGGDescriptor:
 
     @staticmethod
     def _gram(f: torch.Tensor) -> torch.Tensor:
-        v, h, w, c = f.shape
-        ff = f.reshape(v, h * w, c).float()
-        return torch.bmm(ff.transpose(1, 2), ff) / (h * w)
+        return _Gram.apply(f)
 
     def load(self, targets: torch.Tensor):
         self._graph = None  # a captured graph holds the previous targets' features
@@ -163,10 +198,10 @@ class VGGDescriptor:
         tf, tg = self.target
         fl, gl, nf, ng = 0.0, 0.0, 0, 0
         for w, f, t, gt in zip(self.hook_weights, feats, tf, tg):
-            fl = fl + (w * w) * ((f.float() - t) ** 2).sum()
+            fl = fl + (w * w) * torch.nn.functional.mse_loss(f.float(), t, reduction="sum")
             nf += f.numel()
             g = self._gram(f)
-            gl = gl + (w * w) * ((g - gt) ** 2).sum()
+            gl = gl + (w * w) * torch.nn.functional.mse_loss(g, gt, reduction="sum")
             ng += g.numel()
         return fl / nf, gl / ng
 

@@ -61,7 +61,7 @@ def parse():
     ap.add_argument("--no-extras", action="store_true", help="skip the plain/single/cpu comparison legs")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline budget")
     ap.add_argument("--config", default=None, help="threads,tile_texels[,ctas[,variant]] instead of autotuning")
-    ap.add_argument("--only", default=None, choices=["descriptor"], help="run one comparison leg alone")
+    ap.add_argument("--only", default=None, choices=["descriptor", "latent"], help="run one comparison leg alone")
     return ap.parse_args()
 
 
@@ -327,6 +327,62 @@ def time_descriptor(dev, iters=10, views=9, res=512):
             "device_error": d.device_error()}
 
 
+def time_latent(dev, batch=16, iters=10, refine_iters=20):
+    """Latent-space optimisation of a batch of materials (StyleGAN2-shaped generator, seeded
+    weights, W+ [batch, 14, 512]) through the renderer adjoint at 256^2, then per-pixel
+    refinement of the Lanczos-upsampled maps at 512^2 and 1024^2 with the batched fused kernel."""
+    MG = PKG.materialgan
+    rf = gpu_render_fn(dev)
+    gen = MG.StyleGAN2Generator(256, seed=0)
+    cam = PKG.scenes.grid_views().to(dev)
+    lp = torch.full((3,), PKG.scenes.LIGHT_POW, device=dev)
+    gts = [PKG.scenes.make_material(1024, 2000 + i, dev) for i in range(batch)]
+
+    def targets_at(res):
+        out = []
+        for gt in gts:
+            g = torch.nn.functional.interpolate(gt, size=(res, res), mode="area") if res != 1024 else gt
+            out.append(rf(g, cam, cam, lp, PKG.scenes.GRID_SIZE_CM))
+        return out
+
+    t256 = torch.cat(targets_at(256))
+    r = PKG.Microfacet(256, 9, PKG.scenes.GRID_SIZE_CM, [cam, cam, lp], dev)
+    o = MG.MaterialGANOptim(dev, r, gen)
+    o.load_targets(t256)
+    o.init_from(batch=batch, seed=1)
+    o.optim([2, 10, 10], 0.02)  # warm
+    o.loss_image_list = []
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    tex = o.optim([iters, 10, 10], 0.02)
+    torch.cuda.synchronize()
+    lat_s = (time.perf_counter() - t0) / iters
+    out = {"workload": f"{batch} materials, W+ [{batch},14,512], generator 256^2 (seeded weights), 9 views, Adam lr 0.02",
+           "latent_ms_per_iteration": lat_s * 1e3,
+           "latent_texel_views_per_s": batch * 256 * 256 * 9 / lat_s,
+           "latent_loss_first_last": [o.loss_image_list[0], o.loss_image_list[-1]]}
+    for res in (512, 1024):
+        tex = MG.upsample_textures(tex, res)
+        tg = targets_at(res)
+        mats = []
+        for i in range(batch):
+            sc = PKG.scenes.Scene(res=res, size=PKG.scenes.GRID_SIZE_CM, camera_pos=cam, light_pos=cam, light_pow=lp,
+                                  gt=gts[i], targets=tg[i], init=tex[i:i + 1])
+            mats.append(sc)
+        b = PKG.BatchedOptim(mats, lr=0.01, loss="mse", device=dev, hist_len=refine_iters)
+        b.capture(refine_iters)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        b.run(refine_iters)
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        out[f"refine_{res}_ms"] = el * 1e3
+        out[f"refine_{res}_texel_views_per_s"] = batch * res * res * 9 * refine_iters / el
+        tex = torch.cat([t.clamp(-1, 1) for t in b.tex])
+        del b, mats
+    return out
+
+
 def impl_ours(args):
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
@@ -455,6 +511,7 @@ def impl_ours(args):
         line["fused_single"] = time_single(dev, fused=True, iters=200)
         line["fused_vs_plain"] = value / line["plain"]["value"]
         line["descriptor"] = time_descriptor(dev)
+        line["latent"] = time_latent(dev, iters=5)
         if world == 1:
             line["cpu_baseline"] = run_cpu_baseline(specs, args.cpu_seconds, os.cpu_count() or 1)
     if rank == 0:
@@ -471,6 +528,10 @@ def main():
     if args.only == "descriptor":
         dev = torch.device("cuda", dist_env()[2])
         print(json.dumps({"descriptor": time_descriptor(dev, iters=max(args.steps, 1))}), flush=True)
+        return 0
+    if args.only == "latent":
+        dev = torch.device("cuda", dist_env()[2])
+        print(json.dumps({"latent": time_latent(dev, iters=max(args.steps, 1))}), flush=True)
         return 0
     if args.impl == "reference":
         return impl_reference(args)

@@ -17,7 +17,7 @@ from .batched import BatchConfig, BatchedOptim, autotune
 from .microfacet import Microfacet
 from .svbrdf import SvbrdfIO, SvbrdfOptim
 from .scripts import optim_perpixel, render
-from . import descriptor, imageio, scenes
+from . import descriptor, imageio, materialgan, scenes
 
 __all__ = ["Microfacet", "SvbrdfOptim", "SvbrdfIO", "optim_perpixel", "render", "BatchedOptim", "BatchConfig",
-           "autotune", "SvbrdfError", "build", "scenes", "imageio", "descriptor", "_native"]
+           "autotune", "SvbrdfError", "build", "scenes", "imageio", "descriptor", "materialgan", "_native"]

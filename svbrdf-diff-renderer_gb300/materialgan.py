@@ -1,0 +1,276 @@
+"""Latent-space SVBRDF optimisation through the GPU renderer (the MaterialGAN path).
+
+The reference optimises a StyleGAN2 W+ latent (and its noise maps) so that the generated
+maps, rendered by ``Microfacet``, match the photos (src/materialgan.py:21-206, generator in
+src/higan_models/). Its trained checkpoint is downloaded at run time and is not available
+here, so ``StyleGAN2Generator`` is a StyleGAN2 ("config F", skip architecture) generator of
+the same shape with seeded random weights:
+
+* mapping: 8 equalised-learning-rate dense layers (lr multiplier 0.01), leaky ReLU, z -> w;
+* synthesis at 256^2: learned 4x4 constant, one modulated 3x3 conv at 4^2, then per
+  resolution 8 .. 256 an up-sampling modulated conv and a modulated conv (weight
+  demodulation, per-layer noise with learned strength, bias, leaky ReLU x sqrt 2), and a
+  modulated 1x1 toRGB whose output is up-sampled with a [1, 3, 3, 1] FIR filter and added
+  (skip connections); channels 512 up to 32^2, then 512, 256, 128;
+* W+ = 14 x 512 (2 log2(256) - 2); 13 noise maps (4^2, 8^2 x 2, ..., 256^2 x 2);
+* output: 9 texture channels (the repository's layout: diffuse 3, normal xy 2, roughness 1,
+  specular 3), clamped like ``latent_to_textures`` (src/materialgan.py:91-100).
+
+``MaterialGANOptim`` keeps the reference's loop (src/materialgan.py:102-173): alternating
+latent and noise phases of ``[total, l, n]`` epochs, Adam re-created every iteration (as the
+reference does, so its moments never accumulate), loss = image MSE (+ 0.1 x descriptor loss
+when a descriptor is given). Renders go through the drop-in ``Microfacet``, so the texture
+gradient is the hand-written adjoint kernel. A batch of materials is one generator batch,
+each material rendered under its own copy of the view set.
+"""
+from __future__ import annotations
+
+import math
+from typing import List, Optional
+
+import torch
+import torch.nn.functional as Fn
+
+LRELU_GAIN = math.sqrt(2.0)
+
+
+def _nf(res: int, fmap_base: int = 16384, fmap_max: int = 512) -> int:
+    """Channels of the block producing res^2: fmap_base / 2^(log2(res) - 1), capped."""
+    return min(int(fmap_base * 2 / res), fmap_max)
+
+
+class _Dense(torch.nn.Module):
+    """Equalised learning-rate dense layer: N(0, 1/lr_mul^2) weights scaled at run time."""
+
+    def __init__(self, cin, cout, g, lr_mul=1.0, bias_init=0.0, act=False):
+        super().__init__()
+        self.weight = torch.nn.Parameter(torch.randn(cout, cin, generator=g) / lr_mul)
+        self.bias = torch.nn.Parameter(torch.full((cout,), float(bias_init)))
+        self.scale = lr_mul / math.sqrt(cin)
+        self.lr_mul = lr_mul
+        self.act = act
+
+    def forward(self, x):
+        y = Fn.linear(x, self.weight * self.scale, self.bias * self.lr_mul)
+        return Fn.leaky_relu(y, 0.2) * LRELU_GAIN if self.act else y
+
+
+def _fir_kernel(device=None, dtype=torch.float32):
+    k = torch.tensor([1.0, 3.0, 3.0, 1.0], device=device, dtype=dtype)
+    k2 = torch.outer(k, k)
+    return k2 / k2.sum()
+
+
+def _blur(x, pad):
+    """Depthwise [1,3,3,1] x [1,3,3,1] FIR with (pad0, pad1) padding on both axes."""
+    c = x.shape[1]
+    k = _fir_kernel(x.device, x.dtype).view(1, 1, 4, 4).repeat(c, 1, 1, 1)
+    x = Fn.pad(x, (pad[0], pad[1], pad[0], pad[1]))
+    return Fn.conv2d(x, k, groups=c)
+
+
+def _upsample2(x):
+    """2x up-sampling: zero insertion + FIR (gain 4 keeps the mean)."""
+    b, c, h, w = x.shape
+    up = torch.zeros(b, c, h * 2, w * 2, device=x.device, dtype=x.dtype)
+    up[:, :, ::2, ::2] = x * 4.0
+    return _blur(up, (2, 1))
+
+
+class _ModConv(torch.nn.Module):
+    """Modulated (and optionally demodulated) conv, optionally 2x up-sampling first."""
+
+    def __init__(self, cin, cout, k, w_dim, g, demod=True, up=False):
+        super().__init__()
+        self.weight = torch.nn.Parameter(torch.randn(cout, cin, k, k, generator=g))
+        self.affine = _Dense(w_dim, cin, g, bias_init=1.0)
+        self.scale = 1.0 / math.sqrt(cin * k * k)
+        self.demod, self.up, self.k = demod, up, k
+
+    def forward(self, x, w):
+        b, cin, h, wd = x.shape
+        s = self.affine(w)  # [B, cin]
+        wt = self.weight[None] * self.scale * s[:, None, :, None, None]  # [B, cout, cin, k, k]
+        if self.demod:
+            wt = wt * torch.rsqrt(wt.pow(2).sum(dim=(2, 3, 4), keepdim=True) + 1e-8)
+        cout = wt.shape[1]
+        if self.up:
+            x = _upsample2(x)
+            h, wd = h * 2, wd * 2
+        xg = x.reshape(1, b * cin, h, wd)
+        y = Fn.conv2d(xg, wt.reshape(b * cout, cin, self.k, self.k), padding=self.k // 2, groups=b)
+        return y.reshape(b, cout, h, wd)
+
+
+class _StyleLayer(torch.nn.Module):
+    def __init__(self, cin, cout, w_dim, g, up=False):
+        super().__init__()
+        self.conv = _ModConv(cin, cout, 3, w_dim, g, up=up)
+        self.noise_strength = torch.nn.Parameter(torch.zeros(()))
+        self.bias = torch.nn.Parameter(torch.zeros(cout))
+
+    def forward(self, x, w, noise):
+        y = self.conv(x, w)
+        if noise is not None:
+            y = y + self.noise_strength * noise
+        return Fn.leaky_relu(y + self.bias.view(1, -1, 1, 1), 0.2) * LRELU_GAIN
+
+
+class _ToRGB(torch.nn.Module):
+    def __init__(self, cin, cout, w_dim, g):
+        super().__init__()
+        self.conv = _ModConv(cin, cout, 1, w_dim, g, demod=False)
+        self.bias = torch.nn.Parameter(torch.zeros(cout))
+
+    def forward(self, x, w, skip):
+        y = self.conv(x, w) + self.bias.view(1, -1, 1, 1)
+        return y if skip is None else y + _upsample2(skip)
+
+
+class StyleGAN2Generator(torch.nn.Module):
+    """StyleGAN2-shaped generator (seeded random weights) producing [B, 9, res, res] textures."""
+
+    def __init__(self, resolution: int = 256, w_dim: int = 512, out_channels: int = 9, seed: int = 0,
+                 fmap_base: int = 16384, fmap_max: int = 512, mapping_layers: int = 8):
+        super().__init__()
+        g = torch.Generator().manual_seed(seed)
+        self.resolution, self.w_dim = resolution, w_dim
+        log2 = int(round(math.log2(resolution)))
+        assert 2 ** log2 == resolution and resolution >= 8
+        self.num_ws = 2 * log2 - 2
+        nf = lambda r: _nf(r, fmap_base, fmap_max)
+        self.mapping = torch.nn.ModuleList([_Dense(w_dim, w_dim, g, lr_mul=0.01, act=True)
+                                            for _ in range(mapping_layers)])
+        self.register_buffer("w_avg", torch.zeros(w_dim))
+        self.const = torch.nn.Parameter(torch.randn(1, nf(4), 4, 4, generator=g))
+        self.conv4 = _StyleLayer(nf(4), nf(4), w_dim, g)
+        self.rgb4 = _ToRGB(nf(4), out_channels, w_dim, g)
+        self.ups, self.convs, self.rgbs = torch.nn.ModuleList(), torch.nn.ModuleList(), torch.nn.ModuleList()
+        self.noise_res = [4]
+        for l in range(3, log2 + 1):
+            r = 2 ** l
+            self.ups.append(_StyleLayer(nf(r // 2), nf(r), w_dim, g, up=True))
+            self.convs.append(_StyleLayer(nf(r), nf(r), w_dim, g))
+            self.rgbs.append(_ToRGB(nf(r), out_channels, w_dim, g))
+            self.noise_res += [r, r]
+        with torch.no_grad():  # average w of the random mapping (truncation centre)
+            z = torch.randn(4096, w_dim, generator=g)
+            self.w_avg.copy_(self.map(z).mean(0))
+
+    def map(self, z: torch.Tensor) -> torch.Tensor:
+        x = z * torch.rsqrt(z.pow(2).mean(dim=1, keepdim=True) + 1e-8)
+        for layer in self.mapping:
+            x = layer(x)
+        return x
+
+    def truncate(self, w: torch.Tensor, psi: float = 0.7) -> torch.Tensor:
+        return self.w_avg + psi * (w - self.w_avg)
+
+    def make_noises(self, mode: str = "zero", batch: int = 1, device=None, seed: int = 0) -> List[torch.Tensor]:
+        """One noise map per style layer ([batch, 1, r, r]); 'zero' like the reference's "avg"."""
+        g = torch.Generator().manual_seed(seed)
+        out = []
+        for r in self.noise_res:
+            n = torch.zeros(batch, 1, r, r) if mode == "zero" else torch.randn(batch, 1, r, r, generator=g)
+            out.append(n.to(device))
+        return out
+
+    def synthesis(self, wp: torch.Tensor, noises: Optional[List[torch.Tensor]] = None) -> torch.Tensor:
+        """W+ [B, num_ws, w_dim] -> [B, out_channels, res, res]."""
+        b = wp.shape[0]
+        noises = noises if noises is not None else [None] * len(self.noise_res)
+        x = self.const.expand(b, -1, -1, -1)
+        x = self.conv4(x, wp[:, 0], noises[0])
+        img = self.rgb4(x, wp[:, 1], None)
+        for i, (up, conv, rgb) in enumerate(zip(self.ups, self.convs, self.rgbs)):
+            x = up(x, wp[:, 1 + 2 * i], noises[1 + 2 * i])
+            x = conv(x, wp[:, 2 + 2 * i], noises[2 + 2 * i])
+            img = rgb(x, wp[:, 3 + 2 * i], img)
+        return img
+
+
+def latent_to_textures(gen: StyleGAN2Generator, latent: torch.Tensor, noises=None) -> torch.Tensor:
+    """synthesis + the reference's per-group clamps (src/materialgan.py:91-100)."""
+    t = gen.synthesis(latent, noises)
+    return torch.cat((t[:, 0:5].clamp(-1, 1), t[:, 5:6].clamp(-0.5, 0.5), t[:, 6:9].clamp(-1, 1)), 1)
+
+
+class MaterialGANOptim:
+    """Latent (W+) and noise optimisation through the renderer (src/materialgan.py:21-206)."""
+
+    def __init__(self, device, renderer_obj, generator: StyleGAN2Generator, descriptor=None,
+                 descriptor_weight: float = 0.1):
+        self.device = torch.device(device)
+        self.renderer_obj = renderer_obj
+        self.net = generator.to(self.device).eval()
+        for p in self.net.parameters():
+            p.requires_grad_(False)
+        self.descriptor = descriptor
+        self.descriptor_weight = descriptor_weight
+        self.loss_image_list, self.loss_feature_list = [], []
+
+    def init_from(self, latent: Optional[torch.Tensor] = None, batch: int = 1, seed: int = 0, noise: str = "zero"):
+        """W+ from a given latent, else the truncated mapping of seeded z (src/materialgan.py:58-75)."""
+        if latent is None:
+            g = torch.Generator().manual_seed(seed)
+            z = torch.randn(batch, self.net.w_dim, generator=g).to(self.device)
+            with torch.no_grad():
+                w = self.net.truncate(self.net.map(z))
+            latent = w[:, None, :].repeat(1, self.net.num_ws, 1)
+        self.latent = latent.detach().to(self.device, torch.float32).clone().requires_grad_(True)
+        self.noises = [n.requires_grad_(True) for n in
+                       self.net.make_noises(noise, self.latent.shape[0], self.device, seed)]
+
+    def load_targets(self, targets: torch.Tensor):
+        """targets [B*V, 3, H, W] (materials major)."""
+        self.targets = targets.to(self.device, torch.float32).contiguous()
+        if self.descriptor is not None:
+            self.descriptor.load(self.targets)
+
+    def latent_to_textures(self, latent=None):
+        return latent_to_textures(self.net, self.latent if latent is None else latent, self.noises)
+
+    def optim(self, epochs, lr, svbrdf_obj=None, optim_light=False, reset_adam_each_iter=True):
+        """``epochs = [total, l, n]``: alternate l latent epochs and n noise epochs."""
+        total, l_ep, n_ep = epochs
+        cycle = l_ep + n_ep
+        opt = None
+        for epoch in range(total):
+            phase_latent = (epoch % cycle) < l_ep
+            params = [self.latent] if phase_latent else self.noises
+            if opt is None or reset_adam_each_iter or getattr(self, "_phase", None) != phase_latent:
+                opt = torch.optim.Adam(params, lr=lr, betas=(0.9, 0.999))
+            self._phase = phase_latent
+            textures = self.latent_to_textures()
+            rendered = self.renderer_obj.eval(textures)
+            loss = torch.nn.functional.mse_loss(rendered, self.targets)
+            self.loss_image_list.append(loss.detach())
+            if self.descriptor is not None:
+                from .descriptor import descriptor_term
+
+                fl = descriptor_term(rendered, self.descriptor) * self.descriptor_weight
+                self.loss_feature_list.append(fl.detach())
+                loss = loss + fl
+            opt.zero_grad()
+            loss.backward()
+            opt.step()
+        self.textures = self.latent_to_textures().detach()
+        self.loss_image_list = [float(x) for x in torch.stack(self.loss_image_list).tolist()]
+        self.loss_feature_list = [float(x) for x in torch.stack(self.loss_feature_list).tolist()] \
+            if self.loss_feature_list else []
+        return self.textures
+
+
+def upsample_textures(textures: torch.Tensor, res: int) -> torch.Tensor:
+    """Lanczos up-sampling of [B, 9, r, r] maps to res (the reference resizes the saved PNG maps,
+    src/svbrdf.py:155-158, src/imageio.py:75-76), normal xy renormalised with z >= 0."""
+    from .imageio import imresize
+
+    b, c, r, _ = textures.shape
+    x = textures.permute(0, 2, 3, 1)  # [B, r, r, 9]
+    out = torch.stack([imresize(x[i], (res, res)) for i in range(b)])
+    out = out.permute(0, 3, 1, 2).contiguous().clamp(-1, 1)
+    nxy = out[:, 3:5]
+    norm = nxy.pow(2).sum(1, keepdim=True).clamp_min(1.0).sqrt()
+    out[:, 3:5] = nxy / norm
+    return out

@@ -135,7 +135,7 @@ typedef struct svbrdf_material {
  * variant 0 (direct loads): threads 128, 256 or 512; tile_texels a multiple of threads.
  * variant 1 (bulk-copy pipeline: one producer warp streams planes into a shared-memory
  *   ring with cp.async.bulk, `threads` consumer threads compute from it): threads 256,
- *   384 or 480, tile_texels == threads; every material needs H*W % 4 == 0 and 16-byte
+ *   384, 480 or 608, tile_texels == threads; every material needs H*W % 4 == 0 and 16-byte
  *   aligned textures/exp_avg/exp_avg_sq/targets.
  * ctas: persistent CTAs (0 = SM count x resident CTAs per SM). */
 typedef struct svbrdf_batch_config {

@@ -399,6 +399,18 @@ __device__ __forceinline__ void ring_release(RingCursor& rc, uint64_t* empty_bar
   if (++rc.slot == R) { rc.slot = 0; rc.phase ^= 1u; }
 }
 
+// Step past the current slot without freeing it (released later with ring_release_slot).
+__device__ __forceinline__ int ring_hold(RingCursor& rc, int R) {
+  const int held = rc.slot;
+  if (++rc.slot == R) { rc.slot = 0; rc.phase ^= 1u; }
+  return held;
+}
+
+__device__ __forceinline__ void ring_release_slot(const RingCursor& rc, int slot, uint64_t* empty_bar) {
+  __syncwarp();
+  if ((threadIdx.x & 31) == 0 && rc.ok) mbar_arrive(smem_u32(&empty_bar[slot]));
+}
+
 template <int LOSS, int NCW>
 __global__ void __launch_bounds__((NCW + 1) * 32, 1)
 batched_tma_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restrict__ step_counter,
@@ -514,14 +526,6 @@ batched_tma_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restri
       const bool active = tid < T - tl.y;
       const int idx = tl.y + tid;
       const float scale = s_md.scale;
-      // ---- parameters
-      float raw[9];
-      {
-        const float* sl = ring_acquire<NT>(rc, ring, full_bar, err);
-#pragma unroll
-        for (int p = 0; p < 9; ++p) raw[p] = sl[p * NT + tid];
-        ring_release(rc, empty_bar, R);
-      }
       float px = 0.f, py = 0.f;
       if (active) {
         int i, j;
@@ -529,22 +533,24 @@ batched_tma_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restri
         px = __ldg(coords + s_md.coord_off + j);
         py = __ldg(coords + s_md.coord_off + s_md.W + i);
       }
-      float t9[9];
-#pragma unroll
-      for (int c = 0; c < 9; ++c) t9[c] = fminf(fmaxf(raw[c], -1.0f), 1.0f);
+      // ---- parameters: the slot stays held until the update, so the 9 values are read
+      // again there instead of being kept in registers through the view loop
+      const float* psl = ring_acquire<NT>(rc, ring, full_bar, err);
+      const int pslot = ring_hold(rc, R);
       float g[9], gp[3];
       float loss;
       if (s_md.all_coloc) {
         TexelC2 tp;
         {
+          float t9[9];
+#pragma unroll
+          for (int c = 0; c < 9; ++c) t9[c] = fminf(fmaxf(psl[c * NT + tid], -1.0f), 1.0f);
           TexelC tc;
           coloc_prepare(t9, px, py, tc);
           pack_texel(tc, tp);
         }
         AccC2 ap;
         acc2_zero(ap);
-        AccC a;
-        acc_zero(a);
         const float2 PP[3] = {bc2(s_pow[0]), bc2(s_pow[1]), bc2(s_pow[2])};
         for (int v0 = 0; v0 < V; v0 += 4) {
           const float* sl = ring_acquire<NT>(rc, ring, full_bar, err);
@@ -561,29 +567,31 @@ batched_tma_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restri
               coloc_view2<LOSS>(tp, cx, cy, cz, PP, tg, ap);
             }
           }
-          if (nv & 1) {  // odd last view of the material
+          if (nv & 1) {  // odd last view of the material: lane x only
             const int j = nv - 1;
-            float tg[3];
+            float2 tg[3];
 #pragma unroll
-            for (int c = 0; c < 3; ++c) tg[c] = sl[(3 * j + c) * NT + tid];
-            TexelC tc;
-            tc.n0 = tp.n0.x; tc.n1 = tp.n1.x; tc.n2 = tp.n2.x;
-            tc.px = -tp.mpx.x; tc.py = -tp.mpy.x;
-            tc.a2 = tp.a2.x; tc.k = tp.k.x; tc.omk = tp.omk.x;
-#pragma unroll
-            for (int c = 0; c < 3; ++c) { tc.f1[c] = tp.f1[c].x; tc.F[c] = tp.F[c].x; }
-            coloc_view<LOSS, false>(tc, make_float4(s_cx[v0 + j], s_cy[v0 + j], s_cz[v0 + j], 0.f), s_pow[0],
-                                    s_pow[1], s_pow[2], tg, a);
+            for (int c = 0; c < 3; ++c) {
+              const float t = sl[(3 * j + c) * NT + tid];
+              tg[c] = make_float2(t, t);
+            }
+            coloc_view2<LOSS, true>(tp, bc2(s_cx[v0 + j]), bc2(s_cy[v0 + j]), bc2(s_cz[v0 + j]), PP, tg, ap);
           }
           ring_release(rc, empty_bar, R);
         }
+        AccC a;
+        acc_zero(a);
         acc2_fold(ap, a);
         TexelC tc;
         tc.n0 = tp.n0.x; tc.n1 = tp.n1.x; tc.n2 = tp.n2.x;
-        loss = coloc_finish<LOSS, false>(t9, tc, a, scale, g, gp);
+        float t9[9];
 #pragma unroll
-        for (int c = 0; c < 9; ++c) g[c] = (raw[c] >= -1.0f && raw[c] <= 1.0f) ? g[c] : 0.0f;
+        for (int c = 0; c < 9; ++c) t9[c] = fminf(fmaxf(psl[c * NT + tid], -1.0f), 1.0f);
+        loss = coloc_finish<LOSS, false>(t9, tc, a, scale, g, gp);
       } else {
+        float t9[9];
+#pragma unroll
+        for (int c = 0; c < 9; ++c) t9[c] = fminf(fmaxf(psl[c * NT + tid], -1.0f), 1.0f);
         Maps m;
         decode(t9, m);
         Adj a;
@@ -604,8 +612,6 @@ batched_tma_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restri
           ring_release(rc, empty_bar, R);
         }
         adj_to_params(t9, m, a, scale, g);
-#pragma unroll
-        for (int c = 0; c < 9; ++c) g[c] = (raw[c] >= -1.0f && raw[c] <= 1.0f) ? g[c] : 0.0f;
       }
       // ---- Adam moments, update, write back
       float m1[9], m2[9];
@@ -627,8 +633,9 @@ batched_tma_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restri
         float* gm2 = s_md.m2;
 #pragma unroll
         for (int c = 0; c < 9; ++c) {
-          float p = raw[c];
-          adam_update(p, m1[c], m2[c], g[c], s_adam);
+          float p = psl[c * NT + tid];
+          const float gc = (p >= -1.0f && p <= 1.0f) ? g[c] : 0.0f;  // textures.clamp(-1, 1)
+          adam_update(p, m1[c], m2[c], gc, s_adam);
           tex[(size_t)c * T + idx] = p;
           gm1[(size_t)c * T + idx] = m1[c];
           gm2[(size_t)c * T + idx] = m2[c];
@@ -636,6 +643,7 @@ batched_tma_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restri
       } else {
         loss = 0.f;
       }
+      ring_release_slot(rc, pslot, empty_bar);
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, o);
       if (lane == 0) warp_loss[(size_t)tile * NCW + warp] = loss;
@@ -669,8 +677,9 @@ static int plan_layout(const svbrdf_material* mats, int n, const svbrdf_batch_co
     if (cfg->tile_texels <= 0 || cfg->tile_texels % cfg->threads)
       return fail(SVBRDF_ERR_INVALID, "tile_texels must be a positive multiple of threads");
   } else {
-    if (cfg->threads != 256 && cfg->threads != 384 && cfg->threads != 480)
-      return fail(SVBRDF_ERR_UNSUPPORTED, "pipelined variant: threads must be 256, 384 or 480 (got %d)", cfg->threads);
+    if (cfg->threads != 256 && cfg->threads != 384 && cfg->threads != 480 && cfg->threads != 608)
+      return fail(SVBRDF_ERR_UNSUPPORTED, "pipelined variant: threads must be 256, 384, 480 or 608 (got %d)",
+                  cfg->threads);
     if (cfg->tile_texels != cfg->threads)
       return fail(SVBRDF_ERR_INVALID, "pipelined variant: tile_texels must equal threads");
   }
@@ -1075,7 +1084,8 @@ int svbrdf_batched_step(const void* device_plan, const void* host_plan, int loss
   switch (h->threads) {
     case 256: SVB_TL(8) break;
     case 384: SVB_TL(12) break;
-    default: SVB_TL(15) break;
+    case 480: SVB_TL(15) break;
+    default: SVB_TL(19) break;
   }
 #undef SVB_TL
 #undef SVB_T

@@ -568,8 +568,10 @@ __device__ __forceinline__ void acc2_fold(const AccC2& p, AccC& a) {
 }
 
 // Views v (lane x) and v+1 (lane y) of one co-located texel: the arithmetic of coloc_view.
-// cx/cy/cz are the two cameras, PP the light power broadcast, tg[c] the two targets.
-template <int LOSS>
+// cx/cy/cz are the two cameras, PP the light power broadcast, tg[c] the two targets. With
+// LANE_X_ONLY the y lane is a placeholder (an odd view count's last view): its error is
+// zeroed, so it adds nothing to the loss or the gradients.
+template <int LOSS, bool LANE_X_ONLY = false>
 __device__ __forceinline__ void coloc_view2(const TexelC2& t, float2 cx, float2 cy, float2 cz, const float2 PP[3],
                                             const float2 tg[3], AccC2& a) {
   const float2 vx = add2(cx, t.mpx), vy = add2(cy, t.mpy), vz = cz;
@@ -611,6 +613,10 @@ __device__ __forceinline__ void coloc_view2(const TexelC2& t, float2 cx, float2 
       e = (LOSS == kLossLog1p) ? add2(lo, make_float2(-lg2_approx(1.0f + tg[c].x), -lg2_approx(1.0f + tg[c].y)))
                                : fma2(tg[c], bc2(-1.44269504088896341f), lo);
       gout = mul2(e, rcp2(op1));
+    }
+    if (LANE_X_ONLY) {
+      e.y = 0.0f;
+      gout.y = 0.0f;
     }
     a.loss = fma2(e, e, a.loss);
     const float2 gm = mul2(gout, xp);

@@ -19,7 +19,7 @@ def _batch(svb, cuda, n=6):
 
 
 @pytest.mark.parametrize("variant,threads,tile", [(0, 128, 128), (0, 256, 512), (0, 512, 2048),
-                                                  (1, 256, 256), (1, 384, 384), (1, 480, 480)])
+                                                  (1, 256, 256), (1, 384, 384), (1, 480, 480), (1, 608, 608)])
 def test_batched_equals_single(svb, cuda, variant, threads, tile):
     mats = _batch(svb, cuda)
     cfg = svb.BatchConfig(threads=threads, tile_texels=tile, ctas=5, variant=variant)

@@ -47,6 +47,7 @@ import torch  # noqa: E402
 PKG = importlib.import_module("svbrdf-diff-renderer_gb300")
 METRIC = "texel*view render+adjoint+Adam updates/s, fused batched vs plain, 1 GB300"
 UNIT = "texel*view updates/s"
+KERNEL_NAMES = {0: "batched_step_kernel", 1: "batched_tma_kernel", 2: "batched_pair_kernel"}
 WORKLOAD = "batched 64 materials, res {256,512,1024}, V 5-16, 100 iterations per graph replay, log1p L2, Adam lr 0.01"
 
 
@@ -449,8 +450,9 @@ def impl_ours(args):
     # DRAM bytes per launch: an ncu capture of a smaller case of the same kernel, scaled to
     # this launch by the algorithmic bytes (traffic is proportional to texels x views)
     traffic = None
-    tfile = HERE / "profiles" / "batched_tma_kernel_traffic.json"
-    if tfile.exists() and opt.config.variant == 1:
+    kernel = KERNEL_NAMES[opt.config.variant]
+    tfile = HERE / "profiles" / f"{kernel}_traffic.json"
+    if tfile.exists():
         try:
             traffic = float(json.loads(tfile.read_text())["dram_bytes_per_algorithmic_byte"]) * abytes
         except Exception:
@@ -498,7 +500,7 @@ def impl_ours(args):
                        "l2": "inputs larger than L2 (no flush)", "parallelism": f"materials sharded over {world} GPU(s)"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
-                         "kernel": "batched_tma_kernel" if opt.config.variant == 1 else "batched_step_kernel",
+                         "kernel": kernel,
                          "algorithmic_bytes_per_launch": abytes,
                          "launch_ms": launch_ms},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},

@@ -25,8 +25,9 @@ import torch
 from . import _native as N
 
 LOSS_KINDS = {"mse": 0, "log1p": 1, "log1p_pre": 2}
-# (variant, threads, tiles-per-work-item multiplier)
-CANDIDATES = ([(1, t, 1) for t in (256, 384, 480, 608)] +
+# (variant, threads, tile_texels / threads)
+CANDIDATES = ([(2, t, 2) for t in (256, 384, 480)] +
+              [(1, t, 1) for t in (256, 384, 480, 608)] +
               [(0, t, k) for t in (128, 256, 512) for k in (1, 4, 16)])
 CACHE_FILE = pathlib.Path(os.environ.get("SVBRDF_TUNE_CACHE", str(pathlib.Path.home() / ".cache" / "svbrdf_gb300_tune.json")))
 
@@ -36,7 +37,7 @@ class BatchConfig:
     threads: int = 256
     tile_texels: int = 1024
     ctas: int = 0     # 0 = SM count x resident CTAs per SM
-    variant: int = 0  # 0 direct loads, 1 bulk-copy (TMA) pipeline
+    variant: int = 0  # 0 direct loads, 1 bulk-copy (TMA) pipeline, 2 the pipeline on texel pairs
 
     def as_c(self):
         return N.svbrdf_batch_config(self.threads, self.tile_texels, self.ctas, self.variant)

@@ -260,7 +260,6 @@ batched_step_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
   __shared__ View s_views[kMaxViews];
   __shared__ float s_pow[3];
   __shared__ float s_red[NT / 32];
-  __shared__ int s_flag;
   __shared__ AdamScalars s_adam;
   __shared__ int s_step;
   if (threadIdx.x == 0) {
@@ -628,22 +627,332 @@ batched_tma_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restri
         ring_release(rc, empty_bar, R);
       }
       if (active && rc.ok) {
-        float* tex = s_md.tex;
-        float* gm1 = s_md.m1;
-        float* gm2 = s_md.m2;
+        float* tex = s_md.tex + idx;
+        float* gm1 = s_md.m1 + idx;
+        float* gm2 = s_md.m2 + idx;
+        const AdamScalars ad = s_adam;
+        float pv[9];
 #pragma unroll
         for (int c = 0; c < 9; ++c) {
-          float p = psl[c * NT + tid];
-          const float gc = (p >= -1.0f && p <= 1.0f) ? g[c] : 0.0f;  // textures.clamp(-1, 1)
-          adam_update(p, m1[c], m2[c], gc, s_adam);
-          tex[(size_t)c * T + idx] = p;
-          gm1[(size_t)c * T + idx] = m1[c];
-          gm2[(size_t)c * T + idx] = m2[c];
+          pv[c] = psl[c * NT + tid];
+          g[c] = (pv[c] >= -1.0f && pv[c] <= 1.0f) ? g[c] : 0.0f;  // textures.clamp(-1, 1)
+        }
+#pragma unroll
+        for (int c = 0; c < 8; c += 2) {
+          float2 p2 = make_float2(pv[c], pv[c + 1]), a2 = make_float2(m1[c], m1[c + 1]);
+          float2 b2 = make_float2(m2[c], m2[c + 1]);
+          adam_update2(p2, a2, b2, make_float2(g[c], g[c + 1]), ad);
+          pv[c] = p2.x; pv[c + 1] = p2.y; m1[c] = a2.x; m1[c + 1] = a2.y; m2[c] = b2.x; m2[c + 1] = b2.y;
+        }
+        adam_update(pv[8], m1[8], m2[8], g[8], ad);
+#pragma unroll
+        for (int c = 0; c < 9; ++c) {
+          const int off = c * T;
+          tex[off] = pv[c];
+          gm1[off] = m1[c];
+          gm2[off] = m2[c];
         }
       } else {
         loss = 0.f;
       }
       ring_release_slot(rc, pslot, empty_bar);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, o);
+      if (lane == 0) warp_loss[(size_t)tile * NCW + warp] = loss;
+    }
+  }
+  batched_finish<NT + 32>(plan, hdr, mats, warp_loss, NCW, loss_hist, hist_len, s_step, step_counter,
+                          ws + kWsCounter, &s_last, NCW);
+}
+
+// ============================================================== variant 2: texel pairs
+//
+// The pipeline of variant 1 with two adjacent texels per consumer thread, so a tile is
+// TT = 2 x 32 x NCW texels. Lane x of every FP32x2 value is texel 2i of the tile, lane y
+// texel 2i+1: the per-texel set-up, the map-back to the parameters and Adam run packed,
+// shared and global accesses are 64-bit, and the co-located view loop steps one view at
+// a time for both texels (no odd-view tail). Slots hold 9 planes of TT floats; per tile
+// the producer streams
+//   P = the 9 parameter planes, Tc = targets of views 3c .. 3c+2, P again, M = exp_avg,
+//   S = exp_avg_sq.
+// The second copy of P (an L2 hit: the tile's parameters were read a few chunks earlier)
+// feeds the map-back and the update, so every slot is released as soon as it has been
+// read and the ring never deadlocks, whatever the view count and ring depth.
+// Waits, error recording and draining follow variant 1. GEN instantiations also carry the
+// general (light off the camera) path; plans whose views are all co-located launch the
+// instantiation without it, which keeps its registers for the co-located loop.
+constexpr int kPairSlotPlanes = 9;
+constexpr int kPairChunkViews = 3;
+constexpr size_t kPairRingBudget = 216 * 1024;
+
+// Wait (bounded, warp-uniform) for the cursor's slot and return it as float2 pairs.
+template <int SLOT>
+__device__ __forceinline__ const float2* pair_acquire(RingCursor& rc, const float* ring, uint64_t* full_bar, int* err) {
+  if (rc.ok) rc.ok = __all_sync(0xffffffffu, wait_phase(smem_u32(&full_bar[rc.slot]), rc.phase, err, kDevTimeoutFull));
+  return reinterpret_cast<const float2*>(ring + (size_t)rc.slot * SLOT);
+}
+
+template <int LOSS, int NCW, bool GEN>
+__global__ void __launch_bounds__((NCW + 1) * 32, 1)
+batched_pair_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restrict__ step_counter,
+                    float* __restrict__ loss_hist, int hist_len, float* __restrict__ warp_loss, unsigned* ws) {
+  constexpr int NT = NCW * 32;
+  constexpr int TT = 2 * NT;                  // texels per tile
+  constexpr int SLOT = kPairSlotPlanes * TT;  // floats per ring slot
+  extern __shared__ __align__(128) float ring[];
+  __shared__ __align__(8) uint64_t full_bar[kMaxRing];
+  __shared__ __align__(8) uint64_t empty_bar[kMaxRing];
+  __shared__ View s_views[kMaxViews];
+  __shared__ float4 s_cxy[kMaxViews];  // (cx, cx, cy, cy): the camera broadcast into both lanes
+  __shared__ float2 s_cz[kMaxViews];   // (cz, cz)
+  __shared__ MatDesc s_md;
+  __shared__ float s_pow[3];
+  __shared__ AdamScalars s_adam;
+  __shared__ int s_step;
+  __shared__ int s_last;
+
+  const PlanHeader* hdr = (const PlanHeader*)plan;
+  const MatDesc* mats = (const MatDesc*)(plan + hdr->off_mats);
+  const View* views = (const View*)(plan + hdr->off_views);
+  const int* cta_off = (const int*)(plan + hdr->off_cta);
+  const int* order = (const int*)(plan + hdr->off_order);
+  const int2* tiles = (const int2*)(plan + hdr->off_tiles);
+  const float* coords = (const float*)(plan + hdr->off_coords);
+  const int R = hdr->ring_slots;
+  int* err = (int*)(ws + kWsError);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < R; ++s) {
+      mbar_init(smem_u32(&full_bar[s]), 1);
+      mbar_init(smem_u32(&empty_bar[s]), NCW);
+    }
+    fence_mbar_init();
+    s_step = *step_counter + 1;
+    s_adam = device_adam(hyper, s_step);
+  }
+  __syncthreads();
+  const int k0 = cta_off[blockIdx.x], k1 = cta_off[blockIdx.x + 1];
+  const uint32_t ring_base = smem_u32(ring);
+
+  if (warp == NCW) {
+    // ------------------------------------------------------------ producer
+    if (lane == 0) {
+      int slot = 0;
+      uint32_t phase = 0;
+      long long issued = 0;
+      bool ok = true;
+      for (int k = k0; k < k1 && ok; ++k) {
+        const int2 tl = tiles[order[k]];
+        const MatDesc md = mats[tl.x];
+        const int T = md.H * md.W, V = md.V;
+        const uint32_t bytes = (uint32_t)min(TT, T - tl.y) * 4u;
+        const int nt = (V + kPairChunkViews - 1) / kPairChunkViews;
+        for (int q = 0; q < nt + 4; ++q) {
+          if (issued >= R && !wait_phase(smem_u32(&empty_bar[slot]), phase ^ 1u, err, kDevTimeoutEmpty)) {
+            ok = false;
+            break;
+          }
+          const float* base;
+          int plane0, nplanes;
+          if (q == 0 || q == nt + 1) { base = md.tex; plane0 = 0; nplanes = 9; }
+          else if (q <= nt) {
+            base = md.tgt;
+            plane0 = 3 * kPairChunkViews * (q - 1);
+            nplanes = min(3 * kPairChunkViews, 3 * V - plane0);
+          }
+          else if (q == nt + 2) { base = md.m1; plane0 = 0; nplanes = 9; }
+          else { base = md.m2; plane0 = 0; nplanes = 9; }
+          const uint32_t fb = smem_u32(&full_bar[slot]);
+          mbar_arrive_expect_tx(fb, (uint32_t)nplanes * bytes);
+          const float* src = base + (size_t)plane0 * T + tl.y;
+          for (int p = 0; p < nplanes; ++p)
+            bulk_g2s(ring_base + (uint32_t)(slot * SLOT + p * TT) * 4u, src + (size_t)p * T, bytes, fb);
+          ++issued;
+          if (++slot == R) { slot = 0; phase ^= 1u; }
+        }
+      }
+      if (!ok) {
+        // drain: wait for the copies of the last min(R, issued) chunks to land
+        const long long n = issued < R ? issued : R;
+        int s = slot;
+        uint32_t ph = phase;
+        for (long long i = 0; i < n; ++i) {
+          if (--s < 0) { s = R - 1; ph ^= 1u; }
+          uint32_t it = 0;
+          while (!mbar_try_wait(smem_u32(&full_bar[s]), ph)) {
+            if (++it >= kSpinLimit) { atomicCAS(err, 0, kDevTimeoutDrain); break; }
+          }
+        }
+      }
+    }
+  } else {
+    // ------------------------------------------------------------ consumers
+    const int tid = threadIdx.x;
+    RingCursor rc{0, 0u, true};
+    int cur = -1;
+    for (int k = k0; k < k1; ++k) {
+      const int tile = order[k];
+      const int2 tl = tiles[tile];
+      if (tl.x != cur) {  // uniform over the consumer warps
+        named_sync(1, NT);
+        cur = tl.x;
+        if (tid == 0) s_md = mats[cur];
+        const int vo = mats[cur].view_off, nv = mats[cur].V;
+        for (int v = tid; v < nv; v += NT) {
+          const View w = views[vo + v];
+          s_views[v] = w;
+          s_cxy[v] = make_float4(w.cx, w.cx, w.cy, w.cy);
+          s_cz[v] = make_float2(w.cz, w.cz);
+        }
+        if (tid < 3) s_pow[tid] = mats[cur].lpow[tid];
+        named_sync(1, NT);
+      }
+      const int T = s_md.H * s_md.W, V = s_md.V;
+      // T is a multiple of 4 and tiles start at multiples of TT: both texels of a pair
+      // are in range or neither is
+      const bool active = 2 * tid < T - tl.y;
+      const int idx = tl.y + 2 * tid;
+      const float scale = s_md.scale;
+      float2 px = make_float2(0.f, 0.f), py = make_float2(0.f, 0.f);
+      if (active) {
+        int i, j;
+        texel_rc(idx, s_md, i, j);
+        int i1 = i, j1 = j + 1;
+        if (j1 == s_md.W) { j1 = 0; ++i1; }
+        const float* cx = coords + s_md.coord_off;
+        px = make_float2(__ldg(cx + j), __ldg(cx + j1));
+        py = make_float2(__ldg(cx + s_md.W + i), __ldg(cx + s_md.W + i1));
+      }
+      float2 g[9];
+      float2 pv[9];  // raw parameters of the second P copy
+      float2 loss2;
+      if (!GEN || s_md.all_coloc) {
+        TexelC2 u;
+        {
+          const float2* pp = pair_acquire<SLOT>(rc, ring, full_bar, err) + tid;
+          float2 t9[9];
+#pragma unroll
+          for (int c = 0; c < 9; ++c) t9[c] = clamp2(pp[c * NT]);
+          ring_release(rc, empty_bar, R);
+          coloc_prepare_pair(t9, px, py, u);
+        }
+        AccC2 a;
+        acc2_zero(a);
+        const float2 PP[3] = {bc2(s_pow[0]), bc2(s_pow[1]), bc2(s_pow[2])};
+        for (int v0 = 0; v0 < V; v0 += kPairChunkViews) {
+          const float2* tp = pair_acquire<SLOT>(rc, ring, full_bar, err) + tid;
+          const int nv = min(kPairChunkViews, V - v0);
+#pragma unroll
+          for (int j = 0; j < kPairChunkViews; ++j) {
+            if (j < nv) {
+              const float2 tg[3] = {tp[(3 * j) * NT], tp[(3 * j + 1) * NT], tp[(3 * j + 2) * NT]};
+              const float4 cxy = s_cxy[v0 + j];
+              coloc_view2<LOSS>(u, make_float2(cxy.x, cxy.y), make_float2(cxy.z, cxy.w), s_cz[v0 + j], PP, tg, a);
+            }
+          }
+          ring_release(rc, empty_bar, R);
+        }
+        {
+          const float2* pp = pair_acquire<SLOT>(rc, ring, full_bar, err) + tid;
+#pragma unroll
+          for (int c = 0; c < 9; ++c) pv[c] = pp[c * NT];
+          ring_release(rc, empty_bar, R);
+        }
+        float2 t9[9];
+#pragma unroll
+        for (int c = 0; c < 9; ++c) t9[c] = clamp2(pv[c]);
+        loss2 = coloc_finish_pair<LOSS>(t9, u, a, scale, g);
+      } else {
+        // general views: the two texels one after the other through each chunk
+        Maps ma, mb;
+        Adj aa, ab;
+        {
+          const float2* pp = pair_acquire<SLOT>(rc, ring, full_bar, err) + tid;
+          float ta[9], tb[9];
+#pragma unroll
+          for (int c = 0; c < 9; ++c) {
+            const float2 t = clamp2(pp[c * NT]);
+            ta[c] = t.x;
+            tb[c] = t.y;
+          }
+          ring_release(rc, empty_bar, R);
+          decode(ta, ma);
+          decode(tb, mb);
+        }
+        adj_zero(aa);
+        adj_zero(ab);
+        float la = 0.f, lb = 0.f;
+        for (int v0 = 0; v0 < V; v0 += kPairChunkViews) {
+          const float2* tp = pair_acquire<SLOT>(rc, ring, full_bar, err) + tid;
+          const int nv = min(kPairChunkViews, V - v0);
+          for (int j = 0; j < nv; ++j) {
+            const float2 t0 = tp[(3 * j) * NT], t1 = tp[(3 * j + 1) * NT], t2 = tp[(3 * j + 2) * NT];
+            const View& w = s_views[v0 + j];
+            float ia[3] = {t0.x, t1.x, t2.x}, ib[3] = {t0.y, t1.y, t2.y};
+            if (w.coloc != 0.f) {
+              texel_view<kModeFused, LOSS, false, true>(ma, px.x, py.x, w, s_pow, ia, la, aa);
+              texel_view<kModeFused, LOSS, false, true>(mb, px.y, py.y, w, s_pow, ib, lb, ab);
+            } else {
+              texel_view<kModeFused, LOSS, false, false>(ma, px.x, py.x, w, s_pow, ia, la, aa);
+              texel_view<kModeFused, LOSS, false, false>(mb, px.y, py.y, w, s_pow, ib, lb, ab);
+            }
+          }
+          ring_release(rc, empty_bar, R);
+        }
+        {
+          const float2* pp = pair_acquire<SLOT>(rc, ring, full_bar, err) + tid;
+#pragma unroll
+          for (int c = 0; c < 9; ++c) pv[c] = pp[c * NT];
+          ring_release(rc, empty_bar, R);
+        }
+        float ta[9], tb[9], ga[9], gb[9];
+#pragma unroll
+        for (int c = 0; c < 9; ++c) {
+          const float2 t = clamp2(pv[c]);
+          ta[c] = t.x;
+          tb[c] = t.y;
+        }
+        adj_to_params(ta, ma, aa, scale, ga);
+        adj_to_params(tb, mb, ab, scale, gb);
+#pragma unroll
+        for (int c = 0; c < 9; ++c) g[c] = make_float2(ga[c], gb[c]);
+        loss2 = make_float2(la, lb);
+      }
+      // ---- Adam moments, update, write back
+      float2 m1[9], m2[9];
+      {
+        const float2* sp = pair_acquire<SLOT>(rc, ring, full_bar, err) + tid;
+#pragma unroll
+        for (int p = 0; p < 9; ++p) m1[p] = sp[p * NT];
+        ring_release(rc, empty_bar, R);
+      }
+      {
+        const float2* sp = pair_acquire<SLOT>(rc, ring, full_bar, err) + tid;
+#pragma unroll
+        for (int p = 0; p < 9; ++p) m2[p] = sp[p * NT];
+        ring_release(rc, empty_bar, R);
+      }
+      float loss = 0.f;
+      if (active && rc.ok) {
+        const AdamScalars ad = s_adam;
+        float* tex = s_md.tex + idx;
+        float* gm1 = s_md.m1 + idx;
+        float* gm2 = s_md.m2 + idx;
+#pragma unroll
+        for (int c = 0; c < 9; ++c) {
+          float2 p = pv[c];
+          // textures.clamp(-1, 1): no gradient outside the range
+          const float2 gc = make_float2((p.x >= -1.0f && p.x <= 1.0f) ? g[c].x : 0.0f,
+                                        (p.y >= -1.0f && p.y <= 1.0f) ? g[c].y : 0.0f);
+          adam_update2(p, m1[c], m2[c], gc, ad);
+          const size_t off = (size_t)c * T;
+          *reinterpret_cast<float2*>(tex + off) = p;
+          *reinterpret_cast<float2*>(gm1 + off) = m1[c];
+          *reinterpret_cast<float2*>(gm2 + off) = m2[c];
+        }
+        loss = loss2.x + loss2.y;
+      }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, o);
       if (lane == 0) warp_loss[(size_t)tile * NCW + warp] = loss;
@@ -665,12 +974,13 @@ struct PlanLayout {
 int resident_ctas(int variant, int threads);
 
 static int slot_bytes(int threads) { return kSlotPlanes * threads * 4; }
+static int pair_slot_bytes(int threads) { return kPairSlotPlanes * 2 * threads * 4; }
 
 static int plan_layout(const svbrdf_material* mats, int n, const svbrdf_batch_config* cfg, PlanLayout& L) {
   if (!mats || n <= 0) return fail(SVBRDF_ERR_INVALID, "no materials");
   if (!cfg) return fail(SVBRDF_ERR_INVALID, "null config");
   const int variant = cfg->variant;
-  if (variant != 0 && variant != 1) return fail(SVBRDF_ERR_INVALID, "variant must be 0 or 1 (got %d)", variant);
+  if (variant < 0 || variant > 2) return fail(SVBRDF_ERR_INVALID, "variant must be 0, 1 or 2 (got %d)", variant);
   if (variant == 0) {
     if (cfg->threads != 128 && cfg->threads != 256 && cfg->threads != 512)
       return fail(SVBRDF_ERR_UNSUPPORTED, "threads must be 128, 256 or 512 (got %d)", cfg->threads);
@@ -680,11 +990,15 @@ static int plan_layout(const svbrdf_material* mats, int n, const svbrdf_batch_co
     if (cfg->threads != 256 && cfg->threads != 384 && cfg->threads != 480 && cfg->threads != 608)
       return fail(SVBRDF_ERR_UNSUPPORTED, "pipelined variant: threads must be 256, 384, 480 or 608 (got %d)",
                   cfg->threads);
-    if (cfg->tile_texels != cfg->threads)
+    if (variant == 1 && cfg->tile_texels != cfg->threads)
       return fail(SVBRDF_ERR_INVALID, "pipelined variant: tile_texels must equal threads");
+    if (variant == 2 && cfg->threads == 608)
+      return fail(SVBRDF_ERR_UNSUPPORTED, "texel-pair variant: threads must be 256, 384 or 480 (got 608)");
+    if (variant == 2 && cfg->tile_texels != 2 * cfg->threads)
+      return fail(SVBRDF_ERR_INVALID, "texel-pair variant: tile_texels must be twice threads");
   }
   long long tiles = 0, coords = 0;
-  int views = 0;
+  int views = 0, max_views = 0;
   for (int i = 0; i < n; ++i) {
     const svbrdf_material& m = mats[i];
     if (!m.textures || !m.exp_avg || !m.exp_avg_sq || !m.targets || !m.light_pow || !m.camera_pos || !m.light_pos)
@@ -694,7 +1008,7 @@ static int plan_layout(const svbrdf_material* mats, int n, const svbrdf_batch_co
     if (m.n_views > kMaxViews) return fail(SVBRDF_ERR_UNSUPPORTED, "material %d: too many views", i);
     const long long T = (long long)m.height * m.width;
     if (T >= (1LL << 24)) return fail(SVBRDF_ERR_UNSUPPORTED, "material %d: more than 2^24 texels", i);
-    if (variant == 1) {
+    if (variant >= 1) {
       if (T % 4) return fail(SVBRDF_ERR_UNSUPPORTED, "pipelined variant: material %d H*W must be a multiple of 4", i);
       const void* ptrs[4] = {m.textures, m.exp_avg, m.exp_avg_sq, m.targets};
       for (const void* p : ptrs)
@@ -702,6 +1016,7 @@ static int plan_layout(const svbrdf_material* mats, int n, const svbrdf_batch_co
     }
     tiles += (T + cfg->tile_texels - 1) / cfg->tile_texels;
     views += m.n_views;
+    max_views = std::max(max_views, m.n_views);
     coords += m.width + m.height;
   }
   if (tiles > (1LL << 30)) return fail(SVBRDF_ERR_UNSUPPORTED, "too many tiles");
@@ -712,7 +1027,14 @@ static int plan_layout(const svbrdf_material* mats, int n, const svbrdf_batch_co
   L.n_ctas = ctas;
   L.total_views = views;
   L.coord_floats = coords;
-  L.ring = variant == 1 ? (int)std::min<size_t>(kMaxRing, kRingBudget / slot_bytes(cfg->threads)) : 0;
+  L.ring = variant == 1   ? (int)std::min<size_t>(kMaxRing, kRingBudget / slot_bytes(cfg->threads))
+           : variant == 2 ? (int)std::min<size_t>(kMaxRing, kPairRingBudget / pair_slot_bytes(cfg->threads))
+                          : 0;
+  // variant 1 holds a tile's parameter slot until its last chunk (S) has been read, so
+  // all 3 + ceil(V/4) chunks of a tile must fit in the ring at once
+  if (variant == 1 && 3 + (max_views + 3) / 4 > L.ring)
+    return fail(SVBRDF_ERR_UNSUPPORTED, "pipelined variant: %d views need %d ring slots; %d threads leave room for %d",
+                max_views, 3 + (max_views + 3) / 4, cfg->threads, L.ring);
   size_t o = align_up(sizeof(PlanHeader), 16);
   L.off_mats = o; o += sizeof(MatDesc) * n; o = align_up(o, 16);
   L.off_views = o; o += sizeof(View) * views; o = align_up(o, 16);
@@ -736,15 +1058,16 @@ static size_t tma_smem(int ring) {
   return (size_t)ring * kSlotPlanes * NCW * 32 * 4;
 }
 
-template <int LOSS, int NCW>
-static int tma_prepare(int ring) {
-  // once per instantiation: allow the ring's dynamic shared memory
-  static int done = 0;
-  static size_t have = 0;
-  const size_t need = tma_smem<NCW>(ring);
+template <int NCW>
+static size_t pair_smem(int ring) {
+  return (size_t)ring * kPairSlotPlanes * 2 * NCW * 32 * 4;
+}
+
+// Once per kernel instantiation: allow the ring's dynamic shared memory.
+template <typename Kernel>
+static int allow_smem(Kernel kernel, size_t need, int& done, size_t& have) {
   if (!done || need > have) {
-    if (cudaFuncSetAttribute(batched_tma_kernel<LOSS, NCW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need) !=
-        cudaSuccess)
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need) != cudaSuccess)
       return fail(SVBRDF_ERR_CUDA, "cudaFuncSetAttribute: %s", cudaGetErrorString(cudaGetLastError()));
     done = 1;
     have = need;
@@ -752,10 +1075,24 @@ static int tma_prepare(int ring) {
   return SVBRDF_OK;
 }
 
+template <int LOSS, int NCW>
+static int tma_prepare(int ring) {
+  static int done = 0;
+  static size_t have = 0;
+  return allow_smem(batched_tma_kernel<LOSS, NCW>, tma_smem<NCW>(ring), done, have);
+}
+
+template <int LOSS, int NCW, bool GEN>
+static int pair_prepare(int ring) {
+  static int done = 0;
+  static size_t have = 0;
+  return allow_smem(batched_pair_kernel<LOSS, NCW, GEN>, pair_smem<NCW>(ring), done, have);
+}
+
 int resident_ctas(int variant, int threads) {
   const int sms = device_sm_count();
   if (sms <= 0) return 0;
-  if (variant == 1) return sms;  // one pipelined CTA per SM (its ring takes the shared memory)
+  if (variant >= 1) return sms;  // one pipelined CTA per SM (its ring takes the shared memory)
   int occ = 1;
   switch (threads) {
     case 128: occ = occupancy_of(batched_step_kernel<0, 128>, 128); break;
@@ -978,6 +1315,7 @@ int svbrdf_batched_plan(const svbrdf_material* materials, int n_materials, const
       allc = allc && w.coloc != 0.f;
     }
     md[i].all_coloc = allc;
+    if (!allc) h->general = 1;
     voff += m.n_views;
     mat_tiles[i] = t;
     for (long long x = 0; x < T; x += config->tile_texels) {
@@ -1027,7 +1365,7 @@ size_t svbrdf_batched_workspace_bytes(const void* host_plan) {
   if (!host_plan) return 0;
   const PlanHeader* h = (const PlanHeader*)host_plan;
   if (h->magic != kPlanMagic) return 0;
-  const size_t per_tile = h->variant == 1 ? (size_t)(h->threads / 32) : 1;
+  const size_t per_tile = h->variant >= 1 ? (size_t)(h->threads / 32) : 1;
   return kWsLossOffset + sizeof(float) * (size_t)h->n_tiles * per_tile;
 }
 
@@ -1070,6 +1408,31 @@ int svbrdf_batched_step(const void* device_plan, const void* host_plan, int loss
   }
   const int ring = h->ring_slots;
   if (ring < 2 || ring > kMaxRing) return fail(SVBRDF_ERR_INVALID, "bad ring depth %d", ring);
+  if (h->variant == 2) {
+#define SVB_P(L, NCW, G)                                                                                     \
+  {                                                                                                          \
+    int prc = pair_prepare<L, NCW, G>(ring);                                                                 \
+    if (prc) return prc;                                                                                     \
+    batched_pair_kernel<L, NCW, G><<<h->n_ctas, (NCW + 1) * 32, pair_smem<NCW>(ring), st>>>(                 \
+        plan, hyper, step_counter, loss_hist, hist_len, part, ws);                                           \
+  }
+#define SVB_PG(L, NCW)         \
+  if (h->general) SVB_P(L, NCW, true) \
+  else SVB_P(L, NCW, false)
+#define SVB_PL(NCW)                                       \
+  if (loss_kind == SVBRDF_LOSS_MSE) SVB_PG(0, NCW)        \
+  else if (loss_kind == SVBRDF_LOSS_LOG1P) SVB_PG(1, NCW) \
+  else SVB_PG(2, NCW)
+    switch (h->threads) {
+      case 256: SVB_PL(8) break;
+      case 384: SVB_PL(12) break;
+      default: SVB_PL(15) break;
+    }
+#undef SVB_PG
+#undef SVB_PL
+#undef SVB_P
+    return check_launch("batched_pair_kernel");
+  }
 #define SVB_T(L, NCW)                                                                                        \
   {                                                                                                          \
     int prc = tma_prepare<L, NCW>(ring);                                                                     \

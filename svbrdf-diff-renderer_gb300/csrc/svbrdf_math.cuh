@@ -643,12 +643,110 @@ __device__ __forceinline__ void coloc_view2(const TexelC2& t, float2 cx, float2 
   a.gn2 = fma2(gs, vz, a.gn2);
 }
 
+// ---------------------------------------------------------------- texel-pair path
+// Two adjacent texels per thread: lane x = texel i, lane y = texel i+1, one view at a time
+// with the camera broadcast into both lanes. coloc_view2 is lane-generic, so it serves
+// unchanged; the per-texel set-up and map-back below run on both texels at once, which
+// the view-pair form has to do in scalar code.
+__device__ __forceinline__ float2 clamp2(float2 t) {
+  return make_float2(fminf(fmaxf(t.x, -1.0f), 1.0f), fminf(fmaxf(t.y, -1.0f), 1.0f));
+}
+__device__ __forceinline__ float2 half_up2(float2 t) { return fma2(t, bc2(0.5f), bc2(0.5f)); }  // (t+1)/2
+__device__ __forceinline__ float2 one_minus2(float2 t) { return fma2(t, bc2(-1.0f), bc2(1.0f)); }
+__device__ __forceinline__ float2 neg2(float2 t) { return make_float2(-t.x, -t.y); }
+
+// pow22 of both lanes and, from the same lg2, d/dt = 1.1 base^1.2 (0 at base 0).
+__device__ __forceinline__ float2 pow22_2(float2 base) { return ex22(mul2(bc2(2.2f), lg22(base))); }
+__device__ __forceinline__ float2 pow22_2d(float2 base, float2& dxdt) {
+  const float2 lb = lg22(base);
+  dxdt = mul2(bc2(1.1f), ex22(mul2(bc2(1.2f), lb)));
+  return ex22(mul2(bc2(2.2f), lb));
+}
+
+// coloc_prepare for two texels. t9 = parameters already clamped to [-1, 1].
+__device__ __forceinline__ void coloc_prepare_pair(const float2 t9[9], float2 px, float2 py, TexelC2& u) {
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const float2 d = pow22_2(half_up2(t9[c]));
+    const float2 sp = pow22_2(half_up2(t9[6 + c]));
+    const float2 oms = one_minus2(sp);
+    u.f1[c] = mul2(mul2(d, bc2(kInvPi)), oms);
+    u.F[c] = fma2(oms, bc2(kSphgColoc), sp);
+  }
+  const float2 r = pow22_2(half_up2(t9[5]));
+  const float2 alpha = mul2(r, r);
+  u.a2 = mul2(alpha, alpha);
+  u.k = fma2(alpha, bc2(0.5f), bc2(kEps));
+  u.omk = one_minus2(u.k);
+  u.ma2m1x2 = mul2(bc2(-2.0f), add2(u.a2, bc2(-1.0f)));
+  const float2 nx = t9[3], ny = t9[4];
+  const float2 s = fma2(nx, nx, mul2(ny, ny));
+  const float2 sxy = make_float2(fminf(s.x, 1.0f - kEps), fminf(s.y, 1.0f - kEps));
+  const float2 oz = one_minus2(sxy);
+  const float2 nz = make_float2(sqrt_approx(oz.x), sqrt_approx(oz.y));
+  const float2 inv = rsqrt2(fma2(nx, nx, fma2(ny, ny, mul2(nz, nz))));
+  u.n0 = mul2(nx, inv);
+  u.n1 = mul2(ny, inv);
+  u.n2 = mul2(nz, inv);
+  u.mn0 = neg2(u.n0);
+  u.mn1 = neg2(u.n1);
+  u.mn2 = neg2(u.n2);
+  u.mpx = neg2(px);
+  u.mpy = neg2(py);
+}
+
+// coloc_finish for two texels: dL/dt of both (scaled by `scale`) and their squared errors.
+// The maps are re-derived from t9 (clamped parameters); the unit normal comes from u.
+template <int LOSS>
+__device__ __forceinline__ float2 coloc_finish_pair(const float2 t9[9], const TexelC2& u, const AccC2& a, float scale,
+                                                    float2 g[9]) {
+  const float unit = (LOSS == kLossMSE) ? 1.0f : kLn2;  // log1p errors were kept in log2 units
+  const float2 sc = bc2(scale * kInvGamma * unit);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    float2 dd, ds;
+    const float2 d = pow22_2d(half_up2(t9[c]), dd);
+    const float2 sp = pow22_2d(half_up2(t9[6 + c]), ds);
+    g[c] = mul2(mul2(mul2(a.gf1[c], mul2(one_minus2(sp), bc2(kInvPi))), dd), sc);
+    const float2 gsp = fma2(a.gfd[c], bc2(1.0f - kSphgColoc), mul2(a.gf1[c], mul2(d, bc2(-kInvPi))));
+    g[6 + c] = mul2(mul2(gsp, ds), sc);
+  }
+  float2 dr;
+  const float2 r = pow22_2d(half_up2(t9[5]), dr);
+  const float2 alpha = mul2(r, r);
+  const float2 galpha = fma2(a.ga2, add2(alpha, alpha), mul2(a.gk, bc2(0.5f)));
+  g[5] = mul2(mul2(mul2(galpha, add2(r, r)), dr), sc);
+  // normal: n = m/|m|, m = (nx, ny, sqrt(1 - min(nx^2+ny^2, 1-eps)))
+  const float2 nx = t9[3], ny = t9[4];
+  const float2 s = fma2(nx, nx, mul2(ny, ny));
+  const float2 oz = make_float2(1.0f - fminf(s.x, 1.0f - kEps), 1.0f - fminf(s.y, 1.0f - kEps));
+  const float2 nz = make_float2(sqrt_approx(oz.x), sqrt_approx(oz.y));
+  const float2 inv = rsqrt2(fma2(nx, nx, fma2(ny, ny, mul2(nz, nz))));
+  const float2 ndg = fma2(u.n0, a.gn0, fma2(u.n1, a.gn1, mul2(u.n2, a.gn2)));
+  const float2 gmx = mul2(fma2(u.mn0, ndg, a.gn0), inv);
+  const float2 gmy = mul2(fma2(u.mn1, ndg, a.gn1), inv);
+  const float2 gmz = mul2(fma2(u.mn2, ndg, a.gn2), inv);
+  const float2 hz = mul2(mul2(bc2(-1.0f), gmz), rcp2(nz));  // -gmz/nz = 2 dL/d sxy
+  const float2 gsxy2 = make_float2(s.x <= 1.0f - kEps ? hz.x : 0.0f, s.y <= 1.0f - kEps ? hz.y : 0.0f);
+  g[3] = mul2(fma2(gsxy2, nx, gmx), sc);
+  g[4] = mul2(fma2(gsxy2, ny, gmy), sc);
+  return (LOSS == kLossMSE) ? a.loss : mul2(a.loss, bc2(kLn2 * kLn2));
+}
+
 // torch.optim.Adam's update for one element (amsgrad off, no weight decay):
 //   m.lerp_(g, 1-b1); v.mul_(b2).addcmul_(g, g, 1-b2);
 //   p.addcdiv_(m, sqrt(v)/sqrt(bc2) + eps, -lr/bc1)
 struct AdamScalars {
   float one_minus_b1, b2, one_minus_b2, inv_bc2_sqrt, eps, neg_step_size;
 };
+
+// Two elements of the Adam update in FP32x2 (same arithmetic as adam_update per lane).
+__device__ __forceinline__ void adam_update2(float2& p, float2& mo, float2& vo, float2 g, const AdamScalars& s) {
+  mo = fma2(bc2(s.one_minus_b1), add2(g, make_float2(-mo.x, -mo.y)), mo);
+  vo = fma2(bc2(s.one_minus_b2), mul2(g, g), mul2(vo, bc2(s.b2)));
+  const float2 den = fma2(make_float2(sqrt_approx(vo.x), sqrt_approx(vo.y)), bc2(s.inv_bc2_sqrt), bc2(s.eps));
+  p = fma2(bc2(s.neg_step_size), mul2(mo, rcp2(den)), p);
+}
 
 __device__ __forceinline__ void adam_update(float& p, float& mo, float& vo, float g, const AdamScalars& s) {
   mo = mo + s.one_minus_b1 * (g - mo);

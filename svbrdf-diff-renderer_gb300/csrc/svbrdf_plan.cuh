@@ -27,9 +27,9 @@ struct PlanHeader {
   int off_tiles;
   int off_mat_tiles;
   int off_coords;
-  int variant;      // 0: direct loads, 1: bulk-copy (TMA) pipeline
-  int ring_slots;   // variant 1: shared-memory ring depth
-  int pad;
+  int variant;      // 0: direct loads, 1: bulk-copy (TMA) pipeline, 2: the pipeline on texel pairs
+  int ring_slots;   // variants 1 and 2: shared-memory ring depth
+  int general;      // 1 when some material has a view whose light is not at the camera
   long long total_bytes;
   double total_cost;
 };

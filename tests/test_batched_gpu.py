@@ -10,18 +10,25 @@ from conftest import rel_l2
 pytestmark = pytest.mark.gpu
 
 
-def _batch(svb, cuda, n=6):
+def _batch(svb, cuda, n=6, general=True):
     from oracle import microfacet_ref as R
     mats = svb.scenes.batched_scenes(n=n, resolutions=(16, 32, 48), vmin=3, vmax=12,
                                      render_fn=lambda *a: R.render(*a, dtype=torch.float32))
-    mats[1].light_pos = mats[1].light_pos + torch.tensor([1.0, -2.0, 3.0])  # one non-co-located material
+    if general:
+        mats[1].light_pos = mats[1].light_pos + torch.tensor([1.0, -2.0, 3.0])  # one non-co-located material
     return mats
 
 
-@pytest.mark.parametrize("variant,threads,tile", [(0, 128, 128), (0, 256, 512), (0, 512, 2048),
-                                                  (1, 256, 256), (1, 384, 384), (1, 480, 480), (1, 608, 608)])
-def test_batched_equals_single(svb, cuda, variant, threads, tile):
-    mats = _batch(svb, cuda)
+@pytest.mark.parametrize("variant,threads,tile,general", [
+    (0, 128, 128, True), (0, 256, 512, True), (0, 512, 2048, True),
+    (1, 256, 256, True), (1, 384, 384, True), (1, 480, 480, True), (1, 608, 608, True),
+    (2, 256, 512, True), (2, 384, 768, True), (2, 480, 960, True),
+    (2, 480, 960, False), (2, 256, 512, False)])
+def test_batched_equals_single(svb, cuda, variant, threads, tile, general):
+    """`general` puts one material's light off the camera; without it every view is
+    co-located and the texel-pair variant launches its instantiation without the general
+    path."""
+    mats = _batch(svb, cuda, general=general)
     cfg = svb.BatchConfig(threads=threads, tile_texels=tile, ctas=5, variant=variant)
     b = svb.BatchedOptim(mats, lr=0.01, loss="log1p", device=cuda, config=cfg)
     losses = []
@@ -42,7 +49,30 @@ def test_batched_equals_single(svb, cuda, variant, threads, tile):
     assert b.device_error() == 0
 
 
-@pytest.mark.parametrize("variant,threads,tile", [(0, 256, 1024), (1, 384, 384)])
+@pytest.mark.parametrize("general", [False, True])
+def test_pair_many_views_equals_single(svb, cuda, general):
+    """40 views: 14 target chunks per tile go through a 6-slot ring."""
+    from oracle import microfacet_ref as R
+    mats = svb.scenes.batched_scenes(n=2, resolutions=(32,), vmin=40, vmax=40,
+                                     render_fn=lambda *a: R.render(*a, dtype=torch.float32))
+    if general:
+        mats[0].light_pos = mats[0].light_pos + torch.tensor([0.5, 1.0, -2.0])
+    b = svb.BatchedOptim(mats, lr=0.01, loss="log1p", device=cuda,
+                         config=svb.BatchConfig(threads=480, tile_texels=960, ctas=2, variant=2))
+    for _ in range(4):
+        b.step()
+    assert b.device_error() == 0
+    for i, m in enumerate(mats):
+        r = svb.Microfacet(m.res, m.n_views, m.size, [t.to(cuda) for t in m.cl], cuda)
+        o = svb.SvbrdfOptim(cuda, r, loss="log1p")
+        o.load_targets(m.targets.to(cuda))
+        o.init_from_tex(m.init.to(cuda))
+        o.optim(4, 0.01, None, False)
+        assert rel_l2(b.tex[i], o.textures.detach()) <= 1e-6
+        assert rel_l2(b.m2[i], o.exp_avg_sq) <= 1e-5
+
+
+@pytest.mark.parametrize("variant,threads,tile", [(0, 256, 1024), (1, 384, 384), (2, 480, 960)])
 def test_batched_graph_matches_eager(svb, cuda, variant, threads, tile):
     mats = _batch(svb, cuda)
     cfg = svb.BatchConfig(threads=threads, tile_texels=tile, ctas=0, variant=variant)

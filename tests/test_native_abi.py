@@ -129,6 +129,39 @@ def test_pipelined_plan_requirements(svb, lib):
     assert lib.svbrdf_batched_plan_bytes(keep2 and odd, 1, ctypes.byref(SV.svbrdf_batch_config(256, 256, 4, 7))) == 0
 
 
+def test_pipelined_plan_rejects_views_beyond_ring(svb, lib):
+    """Variant 1 holds a tile's parameter slot through the tile: 3 + ceil(V/4) chunks must
+    fit in the ring. The texel-pair variant streams the parameters twice and takes any V."""
+    SV = svb._native
+    mats, keep = _materials(SV, [(32, 32, 40)])
+    assert lib.svbrdf_batched_plan_bytes(mats, 1, ctypes.byref(SV.svbrdf_batch_config(480, 480, 2, 1))) == 0
+    assert b"ring slots" in lib.svbrdf_last_error()
+    assert lib.svbrdf_batched_plan_bytes(mats, 1, ctypes.byref(SV.svbrdf_batch_config(480, 960, 2, 2))) > 0
+    few, keep2 = _materials(SV, [(32, 32, 16)])
+    assert lib.svbrdf_batched_plan_bytes(few, 1, ctypes.byref(SV.svbrdf_batch_config(608, 608, 2, 1))) > 0
+
+
+def test_pair_plan_requirements_and_ring(svb, lib):
+    SV = svb._native
+    mats, keep = _materials(SV, [(64, 64, 9), (32, 32, 5)])
+    cfg = SV.svbrdf_batch_config(480, 960, 3, 2)
+    n = lib.svbrdf_batched_plan_bytes(mats, 2, ctypes.byref(cfg))
+    assert n > 0
+    # tile must be twice the consumer thread count; 608 threads is not offered
+    assert lib.svbrdf_batched_plan_bytes(mats, 2, ctypes.byref(SV.svbrdf_batch_config(480, 480, 3, 2))) == 0
+    assert b"twice" in lib.svbrdf_last_error()
+    assert lib.svbrdf_batched_plan_bytes(mats, 2, ctypes.byref(SV.svbrdf_batch_config(608, 1216, 3, 2))) == 0
+    buf = np.zeros(n, np.uint8)
+    assert lib.svbrdf_batched_plan(mats, 2, ctypes.byref(cfg), buf.ctypes.data, n) == 0
+    hdr = np.frombuffer(buf[:64].tobytes(), np.int32)
+    n_tiles, variant, ring, general = hdr[2], hdr[13], hdr[14], hdr[15]
+    assert variant == 2 and general == 0  # _materials gives co-located views
+    assert n_tiles == -(-64 * 64 // 960) + -(-32 * 32 // 960)
+    # 9-plane slots of 960 floats within the 216 KB ring budget
+    assert 2 <= ring <= 64 and ring * 9 * 960 * 4 <= 216 * 1024 < (ring + 1) * 9 * 960 * 4
+    assert lib.svbrdf_batched_workspace_bytes(buf.ctypes.data) == 256 + 4 * n_tiles * (480 // 32)
+
+
 def test_pipelined_plan_ring_and_workspace(svb, lib):
     SV = svb._native
     mats, keep = _materials(SV, [(64, 64, 9), (32, 32, 5)])

@@ -138,8 +138,8 @@ typedef struct svbrdf_material {
  *   384, 480 or 608, tile_texels == threads; every material needs H*W % 4 == 0 and 16-byte
  *   aligned textures/exp_avg/exp_avg_sq/targets.
  * variant 2 (the variant 1 pipeline with two adjacent texels per consumer thread, every
- *   per-texel stage in FP32x2): threads 256, 384 or 480, tile_texels == 2 * threads,
- *   the material requirements of variant 1.
+ *   per-texel stage in FP32x2): threads 224, 256, 384 or 480, tile_texels == 2 * threads,
+ *   the material requirements of variant 1. threads 224 runs two CTAs per SM.
  * ctas: persistent CTAs (0 = SM count x resident CTAs per SM). */
 typedef struct svbrdf_batch_config {
   int threads;

@@ -26,7 +26,7 @@ from . import _native as N
 
 LOSS_KINDS = {"mse": 0, "log1p": 1, "log1p_pre": 2}
 # (variant, threads, tile_texels / threads)
-CANDIDATES = ([(2, t, 2) for t in (256, 384, 480)] +
+CANDIDATES = ([(2, t, 2) for t in (224, 256, 384, 480)] +
               [(1, t, 1) for t in (256, 384, 480, 608)] +
               [(0, t, k) for t in (128, 256, 512) for k in (1, 4, 16)])
 CACHE_FILE = pathlib.Path(os.environ.get("SVBRDF_TUNE_CACHE", str(pathlib.Path.home() / ".cache" / "svbrdf_gb300_tune.json")))

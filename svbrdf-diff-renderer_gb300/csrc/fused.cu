@@ -684,6 +684,17 @@ batched_tma_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restri
 constexpr int kPairSlotPlanes = 9;
 constexpr int kPairChunkViews = 3;
 constexpr size_t kPairRingBudget = 216 * 1024;
+// Shapes with at most this many consumer warps run two CTAs per SM, each with half the
+// shared memory: two independent pipelines whose phases (MUFU-heavy set-up and map-back,
+// FMA-heavy view loop, stores) drift apart and overlap.
+constexpr int kPairTwoCtaNcw = 7;
+constexpr size_t kPairRingBudgetTwoCta = 104 * 1024;
+
+// ((k + 0.5) / n - 0.5) * size, each operation IEEE round-to-nearest: the pixel-centre grid
+// of src/microfacet.py:16-19 exactly as the planner's FP32 coordinate table holds it.
+__device__ __forceinline__ float pixel_centre(int k, float n, float size) {
+  return __fmul_rn(__fsub_rn(__fdiv_rn(__fadd_rn((float)k, 0.5f), n), 0.5f), size);
+}
 
 // Wait (bounded, warp-uniform) for the cursor's slot and return it as float2 pairs.
 template <int SLOT>
@@ -693,7 +704,7 @@ __device__ __forceinline__ const float2* pair_acquire(RingCursor& rc, const floa
 }
 
 template <int LOSS, int NCW, bool GEN>
-__global__ void __launch_bounds__((NCW + 1) * 32, 1)
+__global__ void __launch_bounds__((NCW + 1) * 32, NCW <= kPairTwoCtaNcw ? 2 : 1)
 batched_pair_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restrict__ step_counter,
                     float* __restrict__ loss_hist, int hist_len, float* __restrict__ warp_loss, unsigned* ws) {
   constexpr int NT = NCW * 32;
@@ -705,7 +716,9 @@ batched_pair_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
   __shared__ View s_views[kMaxViews];
   __shared__ float4 s_cxy[kMaxViews];  // (cx, cx, cy, cy): the camera broadcast into both lanes
   __shared__ float2 s_cz[kMaxViews];   // (cz, cz)
+  __shared__ int4 s_slot_tile[kMaxRing];  // (tile id, material, first texel) of the P chunk in each slot
   __shared__ MatDesc s_md;
+  __shared__ MatDesc s_prod_md;  // the producer's copy of its current material
   __shared__ float s_pow[3];
   __shared__ AdamScalars s_adam;
   __shared__ int s_step;
@@ -715,9 +728,7 @@ batched_pair_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
   const MatDesc* mats = (const MatDesc*)(plan + hdr->off_mats);
   const View* views = (const View*)(plan + hdr->off_views);
   const int* cta_off = (const int*)(plan + hdr->off_cta);
-  const int* order = (const int*)(plan + hdr->off_order);
-  const int2* tiles = (const int2*)(plan + hdr->off_tiles);
-  const float* coords = (const float*)(plan + hdr->off_coords);
+  const int4* seq = (const int4*)(plan + hdr->off_seq);
   const int R = hdr->ring_slots;
   int* err = (int*)(ws + kWsError);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -736,64 +747,91 @@ batched_pair_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
   const uint32_t ring_base = smem_u32(ring);
 
   if (warp == NCW) {
-    // ------------------------------------------------------------ producer
-    if (lane == 0) {
-      int slot = 0;
-      uint32_t phase = 0;
-      long long issued = 0;
-      bool ok = true;
-      for (int k = k0; k < k1 && ok; ++k) {
-        const int2 tl = tiles[order[k]];
-        const MatDesc md = mats[tl.x];
-        const int T = md.H * md.W, V = md.V;
-        const uint32_t bytes = (uint32_t)min(TT, T - tl.y) * 4u;
-        const int nt = (V + kPairChunkViews - 1) / kPairChunkViews;
-        for (int q = 0; q < nt + 4; ++q) {
-          if (issued >= R && !wait_phase(smem_u32(&empty_bar[slot]), phase ^ 1u, err, kDevTimeoutEmpty)) {
-            ok = false;
-            break;
-          }
-          const float* base;
-          int plane0, nplanes;
-          if (q == 0 || q == nt + 1) { base = md.tex; plane0 = 0; nplanes = 9; }
-          else if (q <= nt) {
-            base = md.tgt;
-            plane0 = 3 * kPairChunkViews * (q - 1);
-            nplanes = min(3 * kPairChunkViews, 3 * V - plane0);
-          }
-          else if (q == nt + 2) { base = md.m1; plane0 = 0; nplanes = 9; }
-          else { base = md.m2; plane0 = 0; nplanes = 9; }
-          const uint32_t fb = smem_u32(&full_bar[slot]);
-          mbar_arrive_expect_tx(fb, (uint32_t)nplanes * bytes);
-          const float* src = base + (size_t)plane0 * T + tl.y;
-          for (int p = 0; p < nplanes; ++p)
-            bulk_g2s(ring_base + (uint32_t)(slot * SLOT + p * TT) * 4u, src + (size_t)p * T, bytes, fb);
-          ++issued;
-          if (++slot == R) { slot = 0; phase ^= 1u; }
-        }
+    // ------------------------------------------------------------ producer (the whole warp)
+    // Lane 0 records the tile of each P chunk in s_slot_tile and posts the chunk's bytes
+    // on its full barrier (a release); lanes 0 .. nplanes-1 then issue one plane copy each.
+    // The next tile's record is loaded one tile ahead and the material's fields only when
+    // the material changes, so no global load sits in front of a chunk's copies.
+    int slot = 0;
+    uint32_t phase = 0;
+    long long issued = 0;
+    bool ok = true;
+    int4 sq_next = k0 < k1 ? seq[k0] : make_int4(0, 0, 0, 0);
+    int cur = -1;
+    for (int k = k0; k < k1 && ok; ++k) {
+      const int4 sq = sq_next;
+      if (k + 1 < k1) sq_next = seq[k + 1];
+      if (sq.y != cur) {
+        cur = sq.y;
+        __syncwarp();
+        if (lane == 0) s_prod_md = mats[cur];
+        __syncwarp();
       }
-      if (!ok) {
-        // drain: wait for the copies of the last min(R, issued) chunks to land
-        const long long n = issued < R ? issued : R;
-        int s = slot;
-        uint32_t ph = phase;
-        for (long long i = 0; i < n; ++i) {
-          if (--s < 0) { s = R - 1; ph ^= 1u; }
-          uint32_t it = 0;
-          while (!mbar_try_wait(smem_u32(&full_bar[s]), ph)) {
-            if (++it >= kSpinLimit) { atomicCAS(err, 0, kDevTimeoutDrain); break; }
-          }
+      const MatDesc& md = s_prod_md;
+      const int T = md.H * md.W, V = md.V;
+      const int tile = sq.x;
+      const int2 tl = make_int2(sq.y, sq.z);
+      const uint32_t bytes = (uint32_t)min(TT, T - tl.y) * 4u;
+      const int nt = (V + kPairChunkViews - 1) / kPairChunkViews;
+      for (int q = 0; q < nt + 4; ++q) {
+        if (issued >= R) {
+          ok = __all_sync(0xffffffffu, wait_phase(smem_u32(&empty_bar[slot]), phase ^ 1u, err, kDevTimeoutEmpty));
+          if (!ok) break;
+        }
+        const float* base;
+        int plane0, nplanes;
+        if (q == 0 || q == nt + 1) { base = md.tex; plane0 = 0; nplanes = 9; }
+        else if (q <= nt) {
+          base = md.tgt;
+          plane0 = 3 * kPairChunkViews * (q - 1);
+          nplanes = min(3 * kPairChunkViews, 3 * V - plane0);
+        }
+        else if (q == nt + 2) { base = md.m1; plane0 = 0; nplanes = 9; }
+        else { base = md.m2; plane0 = 0; nplanes = 9; }
+        const uint32_t fb = smem_u32(&full_bar[slot]);
+        if (lane == 0) {
+          if (q == 0) s_slot_tile[slot] = make_int4(tile, tl.x, tl.y, 0);
+          mbar_arrive_expect_tx(fb, (uint32_t)nplanes * bytes);
+        }
+        __syncwarp();
+        if (lane < nplanes)
+          bulk_g2s(ring_base + (uint32_t)(slot * SLOT + lane * TT) * 4u, base + (size_t)(plane0 + lane) * T + tl.y,
+                   bytes, fb);
+        ++issued;
+        if (++slot == R) { slot = 0; phase ^= 1u; }
+      }
+    }
+    if (!ok && lane == 0) {
+      // drain: wait for the copies of the last min(R, issued) chunks to land
+      const long long n = issued < R ? issued : R;
+      int s = slot;
+      uint32_t ph = phase;
+      for (long long i = 0; i < n; ++i) {
+        if (--s < 0) { s = R - 1; ph ^= 1u; }
+        uint32_t it = 0;
+        while (!mbar_try_wait(smem_u32(&full_bar[s]), ph)) {
+          if (++it >= kSpinLimit) { atomicCAS(err, 0, kDevTimeoutDrain); break; }
         }
       }
     }
+    __syncwarp();
   } else {
     // ------------------------------------------------------------ consumers
     const int tid = threadIdx.x;
     RingCursor rc{0, 0u, true};
     int cur = -1;
     for (int k = k0; k < k1; ++k) {
-      const int tile = order[k];
-      const int2 tl = tiles[tile];
+      // the tile's P chunk; its slot record names the tile
+      const float2* pp = pair_acquire<SLOT>(rc, ring, full_bar, err) + tid;
+      int tile, mat, first;
+      if (rc.ok) {
+        const int4 sq = s_slot_tile[rc.slot];
+        tile = sq.x; mat = sq.y; first = sq.z;
+      } else {  // the producer gave up: walk the CTA's tiles without data
+        const int4 sq = ((const int4*)(plan + ((const PlanHeader*)plan)->off_seq))[k];
+        tile = sq.x; mat = sq.y; first = sq.z;
+      }
+      const int2 tl = make_int2(mat, first);
       if (tl.x != cur) {  // uniform over the consumer warps
         named_sync(1, NT);
         cur = tl.x;
@@ -820,55 +858,55 @@ batched_pair_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
         texel_rc(idx, s_md, i, j);
         int i1 = i, j1 = j + 1;
         if (j1 == s_md.W) { j1 = 0; ++i1; }
-        const float* cx = coords + s_md.coord_off;
-        px = make_float2(__ldg(cx + j), __ldg(cx + j1));
-        py = make_float2(__ldg(cx + s_md.W + i), __ldg(cx + s_md.W + i1));
+        // the planner's coordinate table, recomputed with the same IEEE operations
+        const float size = s_md.size, fw = (float)s_md.W, fh = (float)s_md.H;
+        px = make_float2(pixel_centre(j, fw, size), pixel_centre(j1, fw, size));
+        const float yi = -pixel_centre(i, fh, size);
+        py = make_float2(yi, i1 == i ? yi : -pixel_centre(i1, fh, size));
       }
       float2 g[9];
       float2 pv[9];  // raw parameters of the second P copy
       float2 loss2;
       if (!GEN || s_md.all_coloc) {
-        TexelC2 u;
+        const float P[3] = {s_pow[0], s_pow[1], s_pow[2]};
+        TexelPair u;
         {
-          const float2* pp = pair_acquire<SLOT>(rc, ring, full_bar, err) + tid;
           float2 t9[9];
 #pragma unroll
           for (int c = 0; c < 9; ++c) t9[c] = clamp2(pp[c * NT]);
           ring_release(rc, empty_bar, R);
-          coloc_prepare_pair(t9, px, py, u);
+          coloc_prepare_pair(t9, px, py, P, u);
         }
         AccC2 a;
         acc2_zero(a);
-        const float2 PP[3] = {bc2(s_pow[0]), bc2(s_pow[1]), bc2(s_pow[2])};
+        auto view = [&](const float2* tp, int v, int j) {
+          const float2 tg[3] = {tp[(3 * j) * NT], tp[(3 * j + 1) * NT], tp[(3 * j + 2) * NT]};
+          const float4 cxy = s_cxy[v];
+          coloc_view_pair<LOSS>(u, make_float2(cxy.x, cxy.y), make_float2(cxy.z, cxy.w), s_cz[v], tg, a);
+        };
         for (int v0 = 0; v0 < V; v0 += kPairChunkViews) {
           const float2* tp = pair_acquire<SLOT>(rc, ring, full_bar, err) + tid;
           const int nv = min(kPairChunkViews, V - v0);
 #pragma unroll
-          for (int j = 0; j < kPairChunkViews; ++j) {
-            if (j < nv) {
-              const float2 tg[3] = {tp[(3 * j) * NT], tp[(3 * j + 1) * NT], tp[(3 * j + 2) * NT]};
-              const float4 cxy = s_cxy[v0 + j];
-              coloc_view2<LOSS>(u, make_float2(cxy.x, cxy.y), make_float2(cxy.z, cxy.w), s_cz[v0 + j], PP, tg, a);
-            }
-          }
+          for (int j = 0; j < kPairChunkViews; ++j)
+            if (j < nv) view(tp, v0 + j, j);
           ring_release(rc, empty_bar, R);
         }
         {
-          const float2* pp = pair_acquire<SLOT>(rc, ring, full_bar, err) + tid;
+          const float2* pq = pair_acquire<SLOT>(rc, ring, full_bar, err) + tid;
 #pragma unroll
-          for (int c = 0; c < 9; ++c) pv[c] = pp[c * NT];
+          for (int c = 0; c < 9; ++c) pv[c] = pq[c * NT];
           ring_release(rc, empty_bar, R);
         }
         float2 t9[9];
 #pragma unroll
         for (int c = 0; c < 9; ++c) t9[c] = clamp2(pv[c]);
-        loss2 = coloc_finish_pair<LOSS>(t9, u, a, scale, g);
+        loss2 = coloc_finish_pair<LOSS>(t9, u, a, P, scale, g);
       } else {
         // general views: the two texels one after the other through each chunk
         Maps ma, mb;
         Adj aa, ab;
         {
-          const float2* pp = pair_acquire<SLOT>(rc, ring, full_bar, err) + tid;
           float ta[9], tb[9];
 #pragma unroll
           for (int c = 0; c < 9; ++c) {
@@ -901,9 +939,9 @@ batched_pair_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
           ring_release(rc, empty_bar, R);
         }
         {
-          const float2* pp = pair_acquire<SLOT>(rc, ring, full_bar, err) + tid;
+          const float2* pq = pair_acquire<SLOT>(rc, ring, full_bar, err) + tid;
 #pragma unroll
-          for (int c = 0; c < 9; ++c) pv[c] = pp[c * NT];
+          for (int c = 0; c < 9; ++c) pv[c] = pq[c * NT];
           ring_release(rc, empty_bar, R);
         }
         float ta[9], tb[9], ga[9], gb[9];
@@ -924,13 +962,13 @@ batched_pair_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
       {
         const float2* sp = pair_acquire<SLOT>(rc, ring, full_bar, err) + tid;
 #pragma unroll
-        for (int p = 0; p < 9; ++p) m1[p] = sp[p * NT];
+        for (int c = 0; c < 9; ++c) m1[c] = sp[c * NT];
         ring_release(rc, empty_bar, R);
       }
       {
         const float2* sp = pair_acquire<SLOT>(rc, ring, full_bar, err) + tid;
 #pragma unroll
-        for (int p = 0; p < 9; ++p) m2[p] = sp[p * NT];
+        for (int c = 0; c < 9; ++c) m2[c] = sp[c * NT];
         ring_release(rc, empty_bar, R);
       }
       float loss = 0.f;
@@ -942,9 +980,8 @@ batched_pair_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
 #pragma unroll
         for (int c = 0; c < 9; ++c) {
           float2 p = pv[c];
-          // textures.clamp(-1, 1): no gradient outside the range
-          const float2 gc = make_float2((p.x >= -1.0f && p.x <= 1.0f) ? g[c].x : 0.0f,
-                                        (p.y >= -1.0f && p.y <= 1.0f) ? g[c].y : 0.0f);
+          // textures.clamp(-1, 1): no gradient outside the range (nor for NaN)
+          const float2 gc = make_float2(fabsf(p.x) <= 1.0f ? g[c].x : 0.0f, fabsf(p.y) <= 1.0f ? g[c].y : 0.0f);
           adam_update2(p, m1[c], m2[c], gc, ad);
           const size_t off = (size_t)c * T;
           *reinterpret_cast<float2*>(tex + off) = p;
@@ -966,7 +1003,7 @@ batched_pair_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
 static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 struct PlanLayout {
-  size_t off_mats, off_views, off_cta, off_order, off_tiles, off_mat_tiles, off_coords, total;
+  size_t off_mats, off_views, off_cta, off_order, off_tiles, off_mat_tiles, off_coords, off_seq, total;
   int n_tiles, n_ctas, total_views, ring;
   long long coord_floats;
 };
@@ -975,6 +1012,9 @@ int resident_ctas(int variant, int threads);
 
 static int slot_bytes(int threads) { return kSlotPlanes * threads * 4; }
 static int pair_slot_bytes(int threads) { return kPairSlotPlanes * 2 * threads * 4; }
+static size_t pair_ring_budget(int threads) {
+  return threads / 32 <= kPairTwoCtaNcw ? kPairRingBudgetTwoCta : kPairRingBudget;
+}
 
 static int plan_layout(const svbrdf_material* mats, int n, const svbrdf_batch_config* cfg, PlanLayout& L) {
   if (!mats || n <= 0) return fail(SVBRDF_ERR_INVALID, "no materials");
@@ -987,13 +1027,15 @@ static int plan_layout(const svbrdf_material* mats, int n, const svbrdf_batch_co
     if (cfg->tile_texels <= 0 || cfg->tile_texels % cfg->threads)
       return fail(SVBRDF_ERR_INVALID, "tile_texels must be a positive multiple of threads");
   } else {
-    if (cfg->threads != 256 && cfg->threads != 384 && cfg->threads != 480 && cfg->threads != 608)
+    if (variant == 1 && cfg->threads != 256 && cfg->threads != 384 && cfg->threads != 480 && cfg->threads != 608)
       return fail(SVBRDF_ERR_UNSUPPORTED, "pipelined variant: threads must be 256, 384, 480 or 608 (got %d)",
                   cfg->threads);
     if (variant == 1 && cfg->tile_texels != cfg->threads)
       return fail(SVBRDF_ERR_INVALID, "pipelined variant: tile_texels must equal threads");
-    if (variant == 2 && cfg->threads == 608)
-      return fail(SVBRDF_ERR_UNSUPPORTED, "texel-pair variant: threads must be 256, 384 or 480 (got 608)");
+    if (variant == 2 && cfg->threads != 224 && cfg->threads != 256 && cfg->threads != 384 && cfg->threads != 480 &&
+        cfg->threads != 608)
+      return fail(SVBRDF_ERR_UNSUPPORTED, "texel-pair variant: threads must be 224, 256, 384, 480 or 608 (got %d)",
+                  cfg->threads);
     if (variant == 2 && cfg->tile_texels != 2 * cfg->threads)
       return fail(SVBRDF_ERR_INVALID, "texel-pair variant: tile_texels must be twice threads");
   }
@@ -1028,7 +1070,7 @@ static int plan_layout(const svbrdf_material* mats, int n, const svbrdf_batch_co
   L.total_views = views;
   L.coord_floats = coords;
   L.ring = variant == 1   ? (int)std::min<size_t>(kMaxRing, kRingBudget / slot_bytes(cfg->threads))
-           : variant == 2 ? (int)std::min<size_t>(kMaxRing, kPairRingBudget / pair_slot_bytes(cfg->threads))
+           : variant == 2 ? (int)std::min<size_t>(kMaxRing, pair_ring_budget(cfg->threads) / pair_slot_bytes(cfg->threads))
                           : 0;
   // variant 1 holds a tile's parameter slot until its last chunk (S) has been read, so
   // all 3 + ceil(V/4) chunks of a tile must fit in the ring at once
@@ -1043,6 +1085,7 @@ static int plan_layout(const svbrdf_material* mats, int n, const svbrdf_batch_co
   L.off_tiles = o; o += sizeof(int2) * tiles; o = align_up(o, 16);
   L.off_mat_tiles = o; o += sizeof(int) * (n + 1); o = align_up(o, 16);
   L.off_coords = o; o += sizeof(float) * coords; o = align_up(o, 16);
+  L.off_seq = o; o += sizeof(int4) * tiles; o = align_up(o, 16);
   L.total = o;
   if (L.total > (size_t)0x7fffffff) return fail(SVBRDF_ERR_UNSUPPORTED, "plan too large");
   return SVBRDF_OK;
@@ -1092,7 +1135,9 @@ static int pair_prepare(int ring) {
 int resident_ctas(int variant, int threads) {
   const int sms = device_sm_count();
   if (sms <= 0) return 0;
-  if (variant >= 1) return sms;  // one pipelined CTA per SM (its ring takes the shared memory)
+  // one pipelined CTA per SM (its ring takes the shared memory); two for the small texel-pair shape
+  if (variant == 2 && threads / 32 <= kPairTwoCtaNcw) return 2 * sms;
+  if (variant >= 1) return sms;
   int occ = 1;
   switch (threads) {
     case 128: occ = occupancy_of(batched_step_kernel<0, 128>, 128); break;
@@ -1268,6 +1313,7 @@ int svbrdf_batched_plan(const svbrdf_material* materials, int n_materials, const
   h->off_tiles = (int)L.off_tiles;
   h->off_mat_tiles = (int)L.off_mat_tiles;
   h->off_coords = (int)L.off_coords;
+  h->off_seq = (int)L.off_seq;
   h->variant = config->variant;
   h->ring_slots = L.ring;
   h->total_bytes = (long long)L.total;
@@ -1321,43 +1367,33 @@ int svbrdf_batched_plan(const svbrdf_material* materials, int n_materials, const
     for (long long x = 0; x < T; x += config->tile_texels) {
       tiles[t] = make_int2(i, (int)x);
       const long long cnt = std::min<long long>(config->tile_texels, T - x);
-      // cost model: per-texel fixed work (decode, adjoint map-back, Adam) ~ 3 views
-      cost[t] = (double)cnt * (m.n_views + 3.0);
+      // cost model: per-texel fixed work (set-up, map-back, Adam, parameter and moment
+      // traffic) ~ 5 views
+      cost[t] = (double)cnt * (m.n_views + 5.0);
       total += cost[t];
       ++t;
     }
   }
   mat_tiles[n_materials] = t;
   h->total_cost = total;
-  // Longest-processing-time-first assignment to CTAs, then each CTA's tiles sorted by
-  // id so consecutive tiles share a material (fewer view re-stages).
-  std::vector<int> idx(L.n_tiles);
-  std::iota(idx.begin(), idx.end(), 0);
-  std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return cost[a] > cost[b]; });
-  std::vector<std::vector<int>> per(L.n_ctas);
-  std::vector<std::pair<double, int>> heap;
-  heap.reserve(L.n_ctas);
-  for (int c = 0; c < L.n_ctas; ++c) heap.push_back({0.0, c});
-  auto cmp = [](const std::pair<double, int>& a, const std::pair<double, int>& b) {
-    return a.first > b.first || (a.first == b.first && a.second > b.second);
-  };
-  std::make_heap(heap.begin(), heap.end(), cmp);
-  for (int ti : idx) {
-    std::pop_heap(heap.begin(), heap.end(), cmp);
-    auto top = heap.back();
-    heap.pop_back();
-    per[top.second].push_back(ti);
-    top.first += cost[ti];
-    heap.push_back(top);
-    std::push_heap(heap.begin(), heap.end(), cmp);
-  }
-  int k = 0;
+  // Contiguous split: CTA c takes the run of tiles (in material order) whose cost midpoints
+  // fall in its share [c, c+1) * total / n_ctas. Every CTA's load is within one tile of the
+  // mean, and a CTA crosses few material boundaries, so its consumers rarely re-stage a
+  // material's views and its producer rarely reloads a material.
+  int kk = 0;
+  double acc = 0.0;
   for (int c = 0; c < L.n_ctas; ++c) {
-    cta_off[c] = k;
-    std::sort(per[c].begin(), per[c].end());
-    for (int ti : per[c]) order[k++] = ti;
+    cta_off[c] = kk;
+    const double target = total * (double)(c + 1) / (double)L.n_ctas;
+    while (kk < L.n_tiles && (c == L.n_ctas - 1 || acc + 0.5 * cost[kk] <= target)) {
+      acc += cost[kk];
+      order[kk] = kk;
+      ++kk;
+    }
   }
-  cta_off[L.n_ctas] = k;
+  cta_off[L.n_ctas] = L.n_tiles;
+  int4* seq = (int4*)(base + L.off_seq);
+  for (int k = 0; k < L.n_tiles; ++k) seq[k] = make_int4(order[k], tiles[order[k]].x, tiles[order[k]].y, 0);
   return SVBRDF_OK;
 }
 
@@ -1424,9 +1460,11 @@ int svbrdf_batched_step(const void* device_plan, const void* host_plan, int loss
   else if (loss_kind == SVBRDF_LOSS_LOG1P) SVB_PG(1, NCW) \
   else SVB_PG(2, NCW)
     switch (h->threads) {
+      case 224: SVB_PL(7) break;
       case 256: SVB_PL(8) break;
       case 384: SVB_PL(12) break;
-      default: SVB_PL(15) break;
+      case 480: SVB_PL(15) break;
+      default: SVB_PL(19) break;
     }
 #undef SVB_PG
 #undef SVB_PL

@@ -663,22 +663,31 @@ __device__ __forceinline__ float2 pow22_2d(float2 base, float2& dxdt) {
   return ex22(mul2(bc2(2.2f), lb));
 }
 
-// coloc_prepare for two texels. t9 = parameters already clamped to [-1, 1].
-__device__ __forceinline__ void coloc_prepare_pair(const float2 t9[9], float2 px, float2 py, TexelC2& u) {
+// Per-texel constants of two texels. The light power is folded in: Pf1[c] = P_c f1_c and
+// PF[c] = P_c F_c, so a view computes P_c f_c = DGQ PF[c] + Pf1[c] with no P multiply.
+struct TexelPair {
+  float2 n0, n1, n2;  // unit normal
+  float2 mpx, mpy;    // -position
+  float2 a2, k, K1;   // alpha^2, Smith k, 4 pi (1 - alpha^2)
+  float2 Pf1[3], PF[3];
+};
+
+// coloc_prepare for two texels. t9 = parameters already clamped to [-1, 1]; P = light power.
+__device__ __forceinline__ void coloc_prepare_pair(const float2 t9[9], float2 px, float2 py, const float P[3],
+                                                   TexelPair& u) {
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     const float2 d = pow22_2(half_up2(t9[c]));
     const float2 sp = pow22_2(half_up2(t9[6 + c]));
     const float2 oms = one_minus2(sp);
-    u.f1[c] = mul2(mul2(d, bc2(kInvPi)), oms);
-    u.F[c] = fma2(oms, bc2(kSphgColoc), sp);
+    u.Pf1[c] = mul2(mul2(mul2(d, bc2(kInvPi)), oms), bc2(P[c]));
+    u.PF[c] = mul2(fma2(oms, bc2(kSphgColoc), sp), bc2(P[c]));
   }
   const float2 r = pow22_2(half_up2(t9[5]));
   const float2 alpha = mul2(r, r);
   u.a2 = mul2(alpha, alpha);
   u.k = fma2(alpha, bc2(0.5f), bc2(kEps));
-  u.omk = one_minus2(u.k);
-  u.ma2m1x2 = mul2(bc2(-2.0f), add2(u.a2, bc2(-1.0f)));
+  u.K1 = mul2(bc2(4.0f * kPi), one_minus2(u.a2));
   const float2 nx = t9[3], ny = t9[4];
   const float2 s = fma2(nx, nx, mul2(ny, ny));
   const float2 sxy = make_float2(fminf(s.x, 1.0f - kEps), fminf(s.y, 1.0f - kEps));
@@ -688,33 +697,110 @@ __device__ __forceinline__ void coloc_prepare_pair(const float2 t9[9], float2 px
   u.n0 = mul2(nx, inv);
   u.n1 = mul2(ny, inv);
   u.n2 = mul2(nz, inv);
-  u.mn0 = neg2(u.n0);
-  u.mn1 = neg2(u.n1);
-  u.mn2 = neg2(u.n2);
   u.mpx = neg2(px);
   u.mpy = neg2(py);
+}
+
+// One co-located view of two texels (lanes), the camera broadcast: the arithmetic of
+// coloc_view with the light power folded into the texel constants. a.gf1 and a.gfd
+// accumulate dL/df1 and dL/dF divided by P_c; coloc_finish_pair multiplies P_c back;
+// a.gk accumulates -dL/dk. One front-facing predicate (n.v > 0) drives all three selects:
+// at n.v = 0 the view's weight W is 0, the image is clamped and every gradient term is 0.
+// 1 - (n.v)^2 is |v - (n.v) n|^2 / |v|^2, the squared length of v's component across n:
+// no cancellation at the highlight, as with the cross product of coloc_view.
+template <int LOSS>
+__device__ __forceinline__ void coloc_view_pair(const TexelPair& t, float2 cx, float2 cy, float2 cz,
+                                                const float2 tg[3], AccC2& a) {
+  const float2 vx = add2(cx, t.mpx), vy = add2(cy, t.mpy), vz = cz;
+  const float2 q = fma2(vx, vx, fma2(vy, vy, mul2(vz, vz)));
+  const float2 iv = rsqrt2(q);
+  const float2 inv_d2 = mul2(iv, iv);
+  const float2 dn = fma2(t.n0, vx, fma2(t.n1, vy, mul2(t.n2, vz)));  // n.v, |v| units
+  const float2 nvr = mul2(dn, iv);
+  const bool fx = nvr.x > 0.0f, fy = nvr.y > 0.0f;
+  const float2 nv = make_float2(fx ? nvr.x : 0.0f, fy ? nvr.y : 0.0f);
+  const float2 mdn = mul2(dn, bc2(-1.0f));
+  const float2 r0 = fma2(t.n0, mdn, vx), r1 = fma2(t.n1, mdn, vy), r2 = fma2(t.n2, mdn, vz);
+  const float2 s2c = mul2(fma2(r0, r0, fma2(r1, r1, mul2(r2, r2))), inv_d2);
+  const float2 s2 = make_float2(fx ? s2c.x : 1.0f, fy ? s2c.y : 1.0f);
+  const float2 c2 = mul2(nv, nv);
+  const float2 den = fma2(c2, t.a2, s2);
+  const float2 rE = rcp2(fma2(bc2(kPi), mul2(den, den), bc2(kEps)));
+  const float2 D = mul2(t.a2, rE);
+  const float2 omn = one_minus2(nv);
+  const float2 rB = rcp2(fma2(t.k, omn, nv));  // 1 / (nv (1-k) + k)
+  const float2 G1 = mul2(nv, rB);
+  const float2 G = mul2(G1, G1);
+  const float2 rQ = rcp2(fma2(bc2(4.0f), c2, bc2(kEps)));
+  const float2 DGQ = mul2(mul2(D, G), rQ);
+  const float2 W = mul2(nv, inv_d2);
+  float2 gDGQ = make_float2(0.f, 0.f), gW = make_float2(0.f, 0.f);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const float2 f = fma2(DGQ, t.PF[c], t.Pf1[c]);  // P_c (f1 + DGQ F)
+    const float2 img = mul2(f, W);
+    const float2 x = make_float2(fminf(fmaxf(img.x, kEps), 1.0f), fminf(fmaxf(img.y, kEps), 1.0f));
+    const float2 xp = ex22(mul2(lg22(x), bc2(kInvGamma - 1.0f)));
+    const float2 out = mul2(x, xp);
+    float2 e, gout;
+    if (LOSS == kLossMSE) {
+      e = fma2(tg[c], bc2(-1.0f), out);
+      gout = e;
+    } else {
+      const float2 op1 = add2(out, bc2(1.0f));
+      const float2 lo = lg22(op1);
+      e = (LOSS == kLossLog1p) ? add2(lo, make_float2(-lg2_approx(1.0f + tg[c].x), -lg2_approx(1.0f + tg[c].y)))
+                               : fma2(tg[c], bc2(-1.44269504088896341f), lo);
+      gout = mul2(e, rcp2(op1));
+    }
+    a.loss = fma2(e, e, a.loss);
+    const float2 gm = mul2(gout, xp);
+    const float2 gimg = make_float2(x.x == img.x ? gm.x : 0.0f, x.y == img.y ? gm.y : 0.0f);
+    const float2 gw = mul2(gimg, W);  // dL/d f1_c / P_c
+    gW = fma2(gimg, f, gW);
+    a.gf1[c] = add2(a.gf1[c], gw);
+    gDGQ = fma2(gw, t.PF[c], gDGQ);
+    a.gfd[c] = fma2(gw, DGQ, a.gfd[c]);
+  }
+  const float2 tq = mul2(gDGQ, rQ);
+  const float2 gD = mul2(tq, G);
+  const float2 gG1 = mul2(mul2(tq, D), add2(G1, G1));
+  const float2 rB2 = mul2(rB, rB);
+  float2 gnv = fma2(mul2(gG1, t.k), rB2, fma2(mul2(tq, mul2(DGQ, bc2(-8.0f))), nv, mul2(gW, inv_d2)));
+  a.gk = fma2(mul2(mul2(gG1, nv), omn), rB2, a.gk);  // -dL/dk: gG1 nv (1-nv) rB^2
+  const float2 t2 = mul2(mul2(D, rE), den);          // dD/d den = -2 pi t2
+  a.ga2 = fma2(gD, fma2(t2, mul2(c2, bc2(-2.0f * kPi)), rE), a.ga2);
+  gnv = fma2(mul2(mul2(gD, t2), t.K1), nv, gnv);     // d den/d nv = 2 nv (alpha^2 - 1)
+  const float2 gsv = mul2(gnv, iv);
+  const float2 gs = make_float2(fx ? gsv.x : 0.0f, fy ? gsv.y : 0.0f);
+  a.gn0 = fma2(gs, vx, a.gn0);
+  a.gn1 = fma2(gs, vy, a.gn1);
+  a.gn2 = fma2(gs, vz, a.gn2);
 }
 
 // coloc_finish for two texels: dL/dt of both (scaled by `scale`) and their squared errors.
 // The maps are re-derived from t9 (clamped parameters); the unit normal comes from u.
 template <int LOSS>
-__device__ __forceinline__ float2 coloc_finish_pair(const float2 t9[9], const TexelC2& u, const AccC2& a, float scale,
-                                                    float2 g[9]) {
+__device__ __forceinline__ float2 coloc_finish_pair(const float2 t9[9], const TexelPair& u, const AccC2& a,
+                                                    const float P[3], float scale, float2 g[9]) {
   const float unit = (LOSS == kLossMSE) ? 1.0f : kLn2;  // log1p errors were kept in log2 units
-  const float2 sc = bc2(scale * kInvGamma * unit);
+  const float sc1 = scale * kInvGamma * unit;
+  const float2 sc = bc2(sc1);
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     float2 dd, ds;
     const float2 d = pow22_2d(half_up2(t9[c]), dd);
     const float2 sp = pow22_2d(half_up2(t9[6 + c]), ds);
-    g[c] = mul2(mul2(mul2(a.gf1[c], mul2(one_minus2(sp), bc2(kInvPi))), dd), sc);
-    const float2 gsp = fma2(a.gfd[c], bc2(1.0f - kSphgColoc), mul2(a.gf1[c], mul2(d, bc2(-kInvPi))));
+    const float2 gf1 = mul2(a.gf1[c], bc2(P[c]));
+    const float2 gfd = mul2(a.gfd[c], bc2(P[c]));
+    g[c] = mul2(mul2(mul2(gf1, mul2(one_minus2(sp), bc2(kInvPi))), dd), sc);
+    const float2 gsp = fma2(gfd, bc2(1.0f - kSphgColoc), mul2(gf1, mul2(d, bc2(-kInvPi))));
     g[6 + c] = mul2(mul2(gsp, ds), sc);
   }
   float2 dr;
   const float2 r = pow22_2d(half_up2(t9[5]), dr);
   const float2 alpha = mul2(r, r);
-  const float2 galpha = fma2(a.ga2, add2(alpha, alpha), mul2(a.gk, bc2(0.5f)));
+  const float2 galpha = fma2(a.ga2, add2(alpha, alpha), mul2(a.gk, bc2(-0.5f)));  // a.gk holds -dL/dk
   g[5] = mul2(mul2(mul2(galpha, add2(r, r)), dr), sc);
   // normal: n = m/|m|, m = (nx, ny, sqrt(1 - min(nx^2+ny^2, 1-eps)))
   const float2 nx = t9[3], ny = t9[4];
@@ -722,10 +808,10 @@ __device__ __forceinline__ float2 coloc_finish_pair(const float2 t9[9], const Te
   const float2 oz = make_float2(1.0f - fminf(s.x, 1.0f - kEps), 1.0f - fminf(s.y, 1.0f - kEps));
   const float2 nz = make_float2(sqrt_approx(oz.x), sqrt_approx(oz.y));
   const float2 inv = rsqrt2(fma2(nx, nx, fma2(ny, ny, mul2(nz, nz))));
-  const float2 ndg = fma2(u.n0, a.gn0, fma2(u.n1, a.gn1, mul2(u.n2, a.gn2)));
-  const float2 gmx = mul2(fma2(u.mn0, ndg, a.gn0), inv);
-  const float2 gmy = mul2(fma2(u.mn1, ndg, a.gn1), inv);
-  const float2 gmz = mul2(fma2(u.mn2, ndg, a.gn2), inv);
+  const float2 mndg = mul2(fma2(u.n0, a.gn0, fma2(u.n1, a.gn1, mul2(u.n2, a.gn2))), bc2(-1.0f));
+  const float2 gmx = mul2(fma2(u.n0, mndg, a.gn0), inv);
+  const float2 gmy = mul2(fma2(u.n1, mndg, a.gn1), inv);
+  const float2 gmz = mul2(fma2(u.n2, mndg, a.gn2), inv);
   const float2 hz = mul2(mul2(bc2(-1.0f), gmz), rcp2(nz));  // -gmz/nz = 2 dL/d sxy
   const float2 gsxy2 = make_float2(s.x <= 1.0f - kEps ? hz.x : 0.0f, s.y <= 1.0f - kEps ? hz.y : 0.0f);
   g[3] = mul2(fma2(gsxy2, nx, gmx), sc);
@@ -742,7 +828,7 @@ struct AdamScalars {
 
 // Two elements of the Adam update in FP32x2 (same arithmetic as adam_update per lane).
 __device__ __forceinline__ void adam_update2(float2& p, float2& mo, float2& vo, float2 g, const AdamScalars& s) {
-  mo = fma2(bc2(s.one_minus_b1), add2(g, make_float2(-mo.x, -mo.y)), mo);
+  mo = fma2(bc2(s.one_minus_b1), fma2(mo, bc2(-1.0f), g), mo);  // fma(m, -1, g) = g - m exactly
   vo = fma2(bc2(s.one_minus_b2), mul2(g, g), mul2(vo, bc2(s.b2)));
   const float2 den = fma2(make_float2(sqrt_approx(vo.x), sqrt_approx(vo.y)), bc2(s.inv_bc2_sqrt), bc2(s.eps));
   p = fma2(bc2(s.neg_step_size), mul2(mo, rcp2(den)), p);

@@ -4,6 +4,7 @@
 //   PlanHeader | MatDesc[n_mat] | View[total views] | int cta_off[n_ctas+1]
 //   | int order[n_tiles] | int2 tiles[n_tiles] (material, first texel)
 //   | int mat_tile_off[n_mat+1] | float coord tables (per material: x[W], then y[H])
+//   | int4 seq[n_tiles] (order[k]'s tile, material and first texel, in CTA order)
 // Tiles of one material are contiguous in tile-index order (mat_tile_off), so each
 // material's loss is a fixed-order sum over a tile range. cta_off[c]..cta_off[c+1]
 // indexes `order`, the planner's balanced permutation of tile ids for CTA c.
@@ -30,6 +31,8 @@ struct PlanHeader {
   int variant;      // 0: direct loads, 1: bulk-copy (TMA) pipeline, 2: the pipeline on texel pairs
   int ring_slots;   // variants 1 and 2: shared-memory ring depth
   int general;      // 1 when some material has a view whose light is not at the camera
+  int off_seq;      // int4 (tile, material, first texel, 0) per entry of `order`
+  int pad;
   long long total_bytes;
   double total_cost;
 };

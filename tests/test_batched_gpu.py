@@ -23,7 +23,7 @@ def _batch(svb, cuda, n=6, general=True):
     (0, 128, 128, True), (0, 256, 512, True), (0, 512, 2048, True),
     (1, 256, 256, True), (1, 384, 384, True), (1, 480, 480, True), (1, 608, 608, True),
     (2, 256, 512, True), (2, 384, 768, True), (2, 480, 960, True),
-    (2, 480, 960, False), (2, 256, 512, False)])
+    (2, 480, 960, False), (2, 256, 512, False), (2, 224, 448, True), (2, 224, 448, False)])
 def test_batched_equals_single(svb, cuda, variant, threads, tile, general):
     """`general` puts one material's light off the camera; without it every view is
     co-located and the texel-pair variant launches its instantiation without the general

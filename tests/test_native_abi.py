@@ -91,10 +91,13 @@ def test_batched_plan_host_logic(svb, lib):
         t = tiles[mt[m]:mt[m + 1]]
         assert (t[:, 0] == m).all()
         assert t[:, 1].tolist() == list(range(0, h * w, 1024))
-    # LPT balance: the heaviest CTA carries at most the mean plus one tile
-    cost = np.array([min(1024, shapes[m][0] * shapes[m][1] - x) * (shapes[m][2] + 3) for m, x in tiles], float)
+    # contiguous split: each CTA takes a run of tiles in material order and carries at most
+    # the mean plus one tile
+    assert order.tolist() == list(range(n_tiles))
+    cost = np.array([min(1024, shapes[m][0] * shapes[m][1] - x) * (shapes[m][2] + 5) for m, x in tiles], float)
     loads = [cost[order[cta[c]:cta[c + 1]]].sum() for c in range(n_ctas)]
     assert max(loads) <= cost.sum() / n_ctas + cost.max() + 1e-6
+    assert min(loads) >= cost.sum() / n_ctas - cost.max() - 1e-6
     ws = lib.svbrdf_batched_workspace_bytes(buf.ctypes.data)
     assert ws >= 4 * n_tiles
 
@@ -147,19 +150,34 @@ def test_pair_plan_requirements_and_ring(svb, lib):
     cfg = SV.svbrdf_batch_config(480, 960, 3, 2)
     n = lib.svbrdf_batched_plan_bytes(mats, 2, ctypes.byref(cfg))
     assert n > 0
-    # tile must be twice the consumer thread count; 608 threads is not offered
+    # tile must be twice the consumer thread count; 512 threads is not offered
     assert lib.svbrdf_batched_plan_bytes(mats, 2, ctypes.byref(SV.svbrdf_batch_config(480, 480, 3, 2))) == 0
     assert b"twice" in lib.svbrdf_last_error()
-    assert lib.svbrdf_batched_plan_bytes(mats, 2, ctypes.byref(SV.svbrdf_batch_config(608, 1216, 3, 2))) == 0
+    assert lib.svbrdf_batched_plan_bytes(mats, 2, ctypes.byref(SV.svbrdf_batch_config(512, 1024, 3, 2))) == 0
     buf = np.zeros(n, np.uint8)
     assert lib.svbrdf_batched_plan(mats, 2, ctypes.byref(cfg), buf.ctypes.data, n) == 0
-    hdr = np.frombuffer(buf[:64].tobytes(), np.int32)
+    hdr = np.frombuffer(buf[:72].tobytes(), np.int32)
     n_tiles, variant, ring, general = hdr[2], hdr[13], hdr[14], hdr[15]
     assert variant == 2 and general == 0  # _materials gives co-located views
     assert n_tiles == -(-64 * 64 // 960) + -(-32 * 32 // 960)
     # 9-plane slots of 960 floats within the 216 KB ring budget
-    assert 2 <= ring <= 64 and ring * 9 * 960 * 4 <= 216 * 1024 < (ring + 1) * 9 * 960 * 4
+    budget = 216 * 1024
+    assert 2 <= ring <= 64 and ring * 9 * 960 * 4 <= budget < (ring + 1) * 9 * 960 * 4
     assert lib.svbrdf_batched_workspace_bytes(buf.ctypes.data) == 256 + 4 * n_tiles * (480 // 32)
+    # seq: (tile, material, first texel) for each entry of the CTA-ordered tile list
+    off_order, off_tiles, off_seq = hdr[9], hdr[10], hdr[16]
+    order = np.frombuffer(buf[off_order:off_order + 4 * n_tiles].tobytes(), np.int32)
+    tiles = np.frombuffer(buf[off_tiles:off_tiles + 8 * n_tiles].tobytes(), np.int32).reshape(-1, 2)
+    seq = np.frombuffer(buf[off_seq:off_seq + 16 * n_tiles].tobytes(), np.int32).reshape(-1, 4)
+    assert np.array_equal(seq[:, 0], order) and np.array_equal(seq[:, 1:3], tiles[order]) and not seq[:, 3].any()
+    # the 7-warp shape runs two CTAs per SM: half the shared memory for its ring
+    cfg7 = SV.svbrdf_batch_config(224, 448, 3, 2)
+    n7 = lib.svbrdf_batched_plan_bytes(mats, 2, ctypes.byref(cfg7))
+    buf7 = np.zeros(n7, np.uint8)
+    assert lib.svbrdf_batched_plan(mats, 2, ctypes.byref(cfg7), buf7.ctypes.data, n7) == 0
+    ring7 = np.frombuffer(buf7[:64].tobytes(), np.int32)[14]
+    budget7 = 104 * 1024
+    assert ring7 * 9 * 448 * 4 <= budget7 < (ring7 + 1) * 9 * 448 * 4
 
 
 def test_pipelined_plan_ring_and_workspace(svb, lib):

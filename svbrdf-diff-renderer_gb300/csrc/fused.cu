@@ -703,6 +703,24 @@ __device__ __forceinline__ const float2* pair_acquire(RingCursor& rc, const floa
   return reinterpret_cast<const float2*>(ring + (size_t)rc.slot * SLOT);
 }
 
+// Record the producer publishes in each ring slot next to its planes (behind the ring in
+// dynamic shared memory). P chunks carry the tile and its material, target chunks the views
+// of the chunk, so consumers read everything a tile needs from shared memory and never wait
+// on one another.
+struct __align__(16) PairSlotRec {
+  float4 cxy[kPairChunkViews];  // target chunks: (cx, cx, cy, cy) of views 3c .. 3c+2
+  float4 czz[kPairChunkViews];  // (cz, cz, 0, 0)
+  View view[kPairChunkViews];   // the full views, for the general path
+  float* tex;                   // P chunks: the tile's material ...
+  float* m1;
+  float* m2;
+  float* unused;
+  int tile, first, W, H;        // ... tile id and first texel
+  int V, all_coloc, pad0, pad1;
+  float scale, size, inv_w, pad2;
+  float P[4];                   // light power
+};
+
 template <int LOSS, int NCW, bool GEN>
 __global__ void __launch_bounds__((NCW + 1) * 32, NCW <= kPairTwoCtaNcw ? 2 : 1)
 batched_pair_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restrict__ step_counter,
@@ -713,13 +731,9 @@ batched_pair_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
   extern __shared__ __align__(128) float ring[];
   __shared__ __align__(8) uint64_t full_bar[kMaxRing];
   __shared__ __align__(8) uint64_t empty_bar[kMaxRing];
-  __shared__ View s_views[kMaxViews];
-  __shared__ float4 s_cxy[kMaxViews];  // (cx, cx, cy, cy): the camera broadcast into both lanes
-  __shared__ float2 s_cz[kMaxViews];   // (cz, cz)
-  __shared__ int4 s_slot_tile[kMaxRing];  // (tile id, material, first texel) of the P chunk in each slot
-  __shared__ MatDesc s_md;
-  __shared__ MatDesc s_prod_md;  // the producer's copy of its current material
-  __shared__ float s_pow[3];
+  __shared__ MatDesc s_prod_md;            // the producer's current material ...
+  __shared__ View s_prod_views[kMaxViews];  // ... its views
+  __shared__ float s_prod_pow[4];           // ... and light power
   __shared__ AdamScalars s_adam;
   __shared__ int s_step;
   __shared__ int s_last;
@@ -728,8 +742,8 @@ batched_pair_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
   const MatDesc* mats = (const MatDesc*)(plan + hdr->off_mats);
   const View* views = (const View*)(plan + hdr->off_views);
   const int* cta_off = (const int*)(plan + hdr->off_cta);
-  const int4* seq = (const int4*)(plan + hdr->off_seq);
   const int R = hdr->ring_slots;
+  PairSlotRec* recs = reinterpret_cast<PairSlotRec*>(ring + (size_t)R * SLOT);
   int* err = (int*)(ws + kWsError);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
@@ -748,10 +762,11 @@ batched_pair_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
 
   if (warp == NCW) {
     // ------------------------------------------------------------ producer (the whole warp)
-    // Lane 0 records the tile of each P chunk in s_slot_tile and posts the chunk's bytes
-    // on its full barrier (a release); lanes 0 .. nplanes-1 then issue one plane copy each.
-    // The next tile's record is loaded one tile ahead and the material's fields only when
-    // the material changes, so no global load sits in front of a chunk's copies.
+    // Lane 0 fills the slot's record and posts the chunk's bytes on its full barrier (a
+    // release that publishes the record); lanes 0 .. nplanes-1 then issue one plane copy
+    // each. The next tile's entry is loaded one tile ahead and a material's fields and
+    // views only when the material changes.
+    const int4* seq = (const int4*)(plan + hdr->off_seq);
     int slot = 0;
     uint32_t phase = 0;
     long long issued = 0;
@@ -764,14 +779,16 @@ batched_pair_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
       if (sq.y != cur) {
         cur = sq.y;
         __syncwarp();
-        if (lane == 0) s_prod_md = mats[cur];
+        const MatDesc& m = mats[cur];
+        if (lane == 0) s_prod_md = m;
+        if (lane < 3) s_prod_pow[lane] = m.lpow[lane];
+        for (int v = lane; v < m.V; v += 32) s_prod_views[v] = views[m.view_off + v];
         __syncwarp();
       }
       const MatDesc& md = s_prod_md;
       const int T = md.H * md.W, V = md.V;
-      const int tile = sq.x;
-      const int2 tl = make_int2(sq.y, sq.z);
-      const uint32_t bytes = (uint32_t)min(TT, T - tl.y) * 4u;
+      const int first = sq.z;
+      const uint32_t bytes = (uint32_t)min(TT, T - first) * 4u;
       const int nt = (V + kPairChunkViews - 1) / kPairChunkViews;
       for (int q = 0; q < nt + 4; ++q) {
         if (issued >= R) {
@@ -790,12 +807,26 @@ batched_pair_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
         else { base = md.m2; plane0 = 0; nplanes = 9; }
         const uint32_t fb = smem_u32(&full_bar[slot]);
         if (lane == 0) {
-          if (q == 0) s_slot_tile[slot] = make_int4(tile, tl.x, tl.y, 0);
+          PairSlotRec& r = recs[slot];
+          if (q == 0 || q >= nt + 1) {  // P, P', M and S chunks carry the tile record
+            r.tex = md.tex; r.m1 = md.m1; r.m2 = md.m2;
+            r.tile = sq.x; r.first = first; r.W = md.W; r.H = md.H;
+            r.V = V; r.all_coloc = md.all_coloc;
+            r.scale = md.scale; r.size = md.size; r.inv_w = md.inv_w;
+            r.P[0] = s_prod_pow[0]; r.P[1] = s_prod_pow[1]; r.P[2] = s_prod_pow[2];
+          } else if (q <= nt) {
+            for (int j = 0; j < kPairChunkViews && kPairChunkViews * (q - 1) + j < V; ++j) {
+              const View& w = s_prod_views[kPairChunkViews * (q - 1) + j];
+              r.cxy[j] = make_float4(w.cx, w.cx, w.cy, w.cy);
+              r.czz[j] = make_float4(w.cz, w.cz, 0.f, 0.f);
+              r.view[j] = w;
+            }
+          }
           mbar_arrive_expect_tx(fb, (uint32_t)nplanes * bytes);
         }
         __syncwarp();
         if (lane < nplanes)
-          bulk_g2s(ring_base + (uint32_t)(slot * SLOT + lane * TT) * 4u, base + (size_t)(plane0 + lane) * T + tl.y,
+          bulk_g2s(ring_base + (uint32_t)(slot * SLOT + lane * TT) * 4u, base + (size_t)(plane0 + lane) * T + first,
                    bytes, fb);
         ++issued;
         if (++slot == R) { slot = 0; phase ^= 1u; }
@@ -817,49 +848,30 @@ batched_pair_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
     __syncwarp();
   } else {
     // ------------------------------------------------------------ consumers
+    // A warp whose wait gave up (the error word is set) stops: no barrier among the
+    // consumer warps depends on it, and the launch's results are marked invalid.
     const int tid = threadIdx.x;
     RingCursor rc{0, 0u, true};
-    int cur = -1;
     for (int k = k0; k < k1; ++k) {
-      // the tile's P chunk; its slot record names the tile
       const float2* pp = pair_acquire<SLOT>(rc, ring, full_bar, err) + tid;
-      int tile, mat, first;
-      if (rc.ok) {
-        const int4 sq = s_slot_tile[rc.slot];
-        tile = sq.x; mat = sq.y; first = sq.z;
-      } else {  // the producer gave up: walk the CTA's tiles without data
-        const int4 sq = ((const int4*)(plan + ((const PlanHeader*)plan)->off_seq))[k];
-        tile = sq.x; mat = sq.y; first = sq.z;
-      }
-      const int2 tl = make_int2(mat, first);
-      if (tl.x != cur) {  // uniform over the consumer warps
-        named_sync(1, NT);
-        cur = tl.x;
-        if (tid == 0) s_md = mats[cur];
-        const int vo = mats[cur].view_off, nv = mats[cur].V;
-        for (int v = tid; v < nv; v += NT) {
-          const View w = views[vo + v];
-          s_views[v] = w;
-          s_cxy[v] = make_float4(w.cx, w.cx, w.cy, w.cy);
-          s_cz[v] = make_float2(w.cz, w.cz);
-        }
-        if (tid < 3) s_pow[tid] = mats[cur].lpow[tid];
-        named_sync(1, NT);
-      }
-      const int T = s_md.H * s_md.W, V = s_md.V;
+      if (!rc.ok) break;
+      const PairSlotRec& r0 = recs[rc.slot];
+      const int first = r0.first, W = r0.W, V = r0.V;
+      const int T = W * r0.H;
       // T is a multiple of 4 and tiles start at multiples of TT: both texels of a pair
       // are in range or neither is
-      const bool active = 2 * tid < T - tl.y;
-      const int idx = tl.y + 2 * tid;
-      const float scale = s_md.scale;
+      const bool active = 2 * tid < T - first;
+      const int idx = first + 2 * tid;
       float2 px = make_float2(0.f, 0.f), py = make_float2(0.f, 0.f);
       if (active) {
-        int i, j;
-        texel_rc(idx, s_md, i, j);
+        int i = (int)((float)idx * r0.inv_w);
+        int j = idx - i * W;
+        if (j < 0) { --i; j += W; }
+        else if (j >= W) { ++i; j -= W; }
         int i1 = i, j1 = j + 1;
-        if (j1 == s_md.W) { j1 = 0; ++i1; }
+        if (j1 == W) { j1 = 0; ++i1; }
         // the planner's coordinate table, recomputed with the same IEEE operations
-        const float size = s_md.size, fw = (float)s_md.W, fh = (float)s_md.H;
+        const float size = r0.size, fw = (float)W, fh = (float)r0.H;
         px = make_float2(pixel_centre(j, fw, size), pixel_centre(j1, fw, size));
         const float yi = -pixel_centre(i, fh, size);
         py = make_float2(yi, i1 == i ? yi : -pixel_centre(i1, fh, size));
@@ -867,10 +879,11 @@ batched_pair_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
       float2 g[9];
       float2 pv[9];  // raw parameters of the second P copy
       float2 loss2;
-      if (!GEN || s_md.all_coloc) {
-        const float P[3] = {s_pow[0], s_pow[1], s_pow[2]};
+      bool live = true;
+      if (!GEN || r0.all_coloc) {
         TexelPair u;
         {
+          const float P[3] = {r0.P[0], r0.P[1], r0.P[2]};
           float2 t9[9];
 #pragma unroll
           for (int c = 0; c < 9; ++c) t9[c] = clamp2(pp[c * NT]);
@@ -879,31 +892,39 @@ batched_pair_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
         }
         AccC2 a;
         acc2_zero(a);
-        auto view = [&](const float2* tp, int v, int j) {
-          const float2 tg[3] = {tp[(3 * j) * NT], tp[(3 * j + 1) * NT], tp[(3 * j + 2) * NT]};
-          const float4 cxy = s_cxy[v];
-          coloc_view_pair<LOSS>(u, make_float2(cxy.x, cxy.y), make_float2(cxy.z, cxy.w), s_cz[v], tg, a);
-        };
         for (int v0 = 0; v0 < V; v0 += kPairChunkViews) {
           const float2* tp = pair_acquire<SLOT>(rc, ring, full_bar, err) + tid;
+          if (!rc.ok) { live = false; break; }
+          const PairSlotRec& rv = recs[rc.slot];
           const int nv = min(kPairChunkViews, V - v0);
 #pragma unroll
-          for (int j = 0; j < kPairChunkViews; ++j)
-            if (j < nv) view(tp, v0 + j, j);
+          for (int j = 0; j < kPairChunkViews; ++j) {
+            if (j < nv) {
+              const float2 tg[3] = {tp[(3 * j) * NT], tp[(3 * j + 1) * NT], tp[(3 * j + 2) * NT]};
+              const float4 cxy = rv.cxy[j];
+              const float4 czz = rv.czz[j];
+              coloc_view_pair<LOSS>(u, make_float2(cxy.x, cxy.y), make_float2(cxy.z, cxy.w),
+                                    make_float2(czz.x, czz.y), tg, a);
+            }
+          }
           ring_release(rc, empty_bar, R);
         }
-        {
-          const float2* pq = pair_acquire<SLOT>(rc, ring, full_bar, err) + tid;
+        if (!live) break;
+        const float2* pq = pair_acquire<SLOT>(rc, ring, full_bar, err) + tid;
+        if (!rc.ok) break;
+        const PairSlotRec& r1 = recs[rc.slot];
+        const float P[3] = {r1.P[0], r1.P[1], r1.P[2]};
+        const float scale = r1.scale;
 #pragma unroll
-          for (int c = 0; c < 9; ++c) pv[c] = pq[c * NT];
-          ring_release(rc, empty_bar, R);
-        }
+        for (int c = 0; c < 9; ++c) pv[c] = pq[c * NT];
+        ring_release(rc, empty_bar, R);
         float2 t9[9];
 #pragma unroll
         for (int c = 0; c < 9; ++c) t9[c] = clamp2(pv[c]);
         loss2 = coloc_finish_pair<LOSS>(t9, u, a, P, scale, g);
       } else {
         // general views: the two texels one after the other through each chunk
+        const float P[3] = {r0.P[0], r0.P[1], r0.P[2]};
         Maps ma, mb;
         Adj aa, ab;
         {
@@ -923,27 +944,30 @@ batched_pair_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
         float la = 0.f, lb = 0.f;
         for (int v0 = 0; v0 < V; v0 += kPairChunkViews) {
           const float2* tp = pair_acquire<SLOT>(rc, ring, full_bar, err) + tid;
+          if (!rc.ok) { live = false; break; }
+          const PairSlotRec& rv = recs[rc.slot];
           const int nv = min(kPairChunkViews, V - v0);
           for (int j = 0; j < nv; ++j) {
             const float2 t0 = tp[(3 * j) * NT], t1 = tp[(3 * j + 1) * NT], t2 = tp[(3 * j + 2) * NT];
-            const View& w = s_views[v0 + j];
+            const View& w = rv.view[j];
             float ia[3] = {t0.x, t1.x, t2.x}, ib[3] = {t0.y, t1.y, t2.y};
             if (w.coloc != 0.f) {
-              texel_view<kModeFused, LOSS, false, true>(ma, px.x, py.x, w, s_pow, ia, la, aa);
-              texel_view<kModeFused, LOSS, false, true>(mb, px.y, py.y, w, s_pow, ib, lb, ab);
+              texel_view<kModeFused, LOSS, false, true>(ma, px.x, py.x, w, P, ia, la, aa);
+              texel_view<kModeFused, LOSS, false, true>(mb, px.y, py.y, w, P, ib, lb, ab);
             } else {
-              texel_view<kModeFused, LOSS, false, false>(ma, px.x, py.x, w, s_pow, ia, la, aa);
-              texel_view<kModeFused, LOSS, false, false>(mb, px.y, py.y, w, s_pow, ib, lb, ab);
+              texel_view<kModeFused, LOSS, false, false>(ma, px.x, py.x, w, P, ia, la, aa);
+              texel_view<kModeFused, LOSS, false, false>(mb, px.y, py.y, w, P, ib, lb, ab);
             }
           }
           ring_release(rc, empty_bar, R);
         }
-        {
-          const float2* pq = pair_acquire<SLOT>(rc, ring, full_bar, err) + tid;
+        if (!live) break;
+        const float2* pq = pair_acquire<SLOT>(rc, ring, full_bar, err) + tid;
+        if (!rc.ok) break;
+        const float scale = recs[rc.slot].scale;
 #pragma unroll
-          for (int c = 0; c < 9; ++c) pv[c] = pq[c * NT];
-          ring_release(rc, empty_bar, R);
-        }
+        for (int c = 0; c < 9; ++c) pv[c] = pq[c * NT];
+        ring_release(rc, empty_bar, R);
         float ta[9], tb[9], ga[9], gb[9];
 #pragma unroll
         for (int c = 0; c < 9; ++c) {
@@ -957,26 +981,28 @@ batched_pair_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
         for (int c = 0; c < 9; ++c) g[c] = make_float2(ga[c], gb[c]);
         loss2 = make_float2(la, lb);
       }
-      // ---- Adam moments, update, write back
+      // ---- Adam moments, update, write back (the destination comes from the S record)
       float2 m1[9], m2[9];
       {
         const float2* sp = pair_acquire<SLOT>(rc, ring, full_bar, err) + tid;
+        if (!rc.ok) break;
 #pragma unroll
         for (int c = 0; c < 9; ++c) m1[c] = sp[c * NT];
         ring_release(rc, empty_bar, R);
       }
-      {
-        const float2* sp = pair_acquire<SLOT>(rc, ring, full_bar, err) + tid;
+      const float2* sp2 = pair_acquire<SLOT>(rc, ring, full_bar, err) + tid;
+      if (!rc.ok) break;
+      const PairSlotRec& r3 = recs[rc.slot];
+      float* tex = r3.tex + idx;
+      float* gm1 = r3.m1 + idx;
+      float* gm2 = r3.m2 + idx;
+      const int tile = r3.tile;
 #pragma unroll
-        for (int c = 0; c < 9; ++c) m2[c] = sp[c * NT];
-        ring_release(rc, empty_bar, R);
-      }
+      for (int c = 0; c < 9; ++c) m2[c] = sp2[c * NT];
+      ring_release(rc, empty_bar, R);
       float loss = 0.f;
-      if (active && rc.ok) {
+      if (active) {
         const AdamScalars ad = s_adam;
-        float* tex = s_md.tex + idx;
-        float* gm1 = s_md.m1 + idx;
-        float* gm2 = s_md.m2 + idx;
 #pragma unroll
         for (int c = 0; c < 9; ++c) {
           float2 p = pv[c];
@@ -1011,7 +1037,7 @@ struct PlanLayout {
 int resident_ctas(int variant, int threads);
 
 static int slot_bytes(int threads) { return kSlotPlanes * threads * 4; }
-static int pair_slot_bytes(int threads) { return kPairSlotPlanes * 2 * threads * 4; }
+static int pair_slot_bytes(int threads) { return kPairSlotPlanes * 2 * threads * 4 + (int)sizeof(PairSlotRec); }
 static size_t pair_ring_budget(int threads) {
   return threads / 32 <= kPairTwoCtaNcw ? kPairRingBudgetTwoCta : kPairRingBudget;
 }
@@ -1103,7 +1129,7 @@ static size_t tma_smem(int ring) {
 
 template <int NCW>
 static size_t pair_smem(int ring) {
-  return (size_t)ring * kPairSlotPlanes * 2 * NCW * 32 * 4;
+  return (size_t)ring * (kPairSlotPlanes * 2 * NCW * 32 * 4 + sizeof(PairSlotRec));
 }
 
 // Once per kernel instantiation: allow the ring's dynamic shared memory.

@@ -160,9 +160,9 @@ def test_pair_plan_requirements_and_ring(svb, lib):
     n_tiles, variant, ring, general = hdr[2], hdr[13], hdr[14], hdr[15]
     assert variant == 2 and general == 0  # _materials gives co-located views
     assert n_tiles == -(-64 * 64 // 960) + -(-32 * 32 // 960)
-    # 9-plane slots of 960 floats within the 216 KB ring budget
-    budget = 216 * 1024
-    assert 2 <= ring <= 64 and ring * 9 * 960 * 4 <= budget < (ring + 1) * 9 * 960 * 4
+    # slots of 9 planes x 960 floats plus a 288-byte record, within the 216 KB ring budget
+    budget, slot = 216 * 1024, 9 * 960 * 4 + 288
+    assert 2 <= ring <= 64 and ring * slot <= budget < (ring + 1) * slot
     assert lib.svbrdf_batched_workspace_bytes(buf.ctypes.data) == 256 + 4 * n_tiles * (480 // 32)
     # seq: (tile, material, first texel) for each entry of the CTA-ordered tile list
     off_order, off_tiles, off_seq = hdr[9], hdr[10], hdr[16]
@@ -176,8 +176,8 @@ def test_pair_plan_requirements_and_ring(svb, lib):
     buf7 = np.zeros(n7, np.uint8)
     assert lib.svbrdf_batched_plan(mats, 2, ctypes.byref(cfg7), buf7.ctypes.data, n7) == 0
     ring7 = np.frombuffer(buf7[:64].tobytes(), np.int32)[14]
-    budget7 = 104 * 1024
-    assert ring7 * 9 * 448 * 4 <= budget7 < (ring7 + 1) * 9 * 448 * 4
+    budget7, slot7 = 104 * 1024, 9 * 448 * 4 + 288
+    assert ring7 * slot7 <= budget7 < (ring7 + 1) * slot7
 
 
 def test_pipelined_plan_ring_and_workspace(svb, lib):

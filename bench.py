@@ -310,10 +310,12 @@ def time_descriptor(dev, iters=10, views=9, res=512):
         d.loss_and_grad(r0)  # captures the forward + backward graph on first use
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.nvtx.range_push("descriptor")
     e0.record()
     for _ in range(iters):
         d.loss_and_grad(r0)
     e1.record()
+    torch.cuda.nvtx.range_pop()
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / iters
     tf = flops / (ms / 1e3) / 1e12

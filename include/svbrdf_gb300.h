@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define SVBRDF_ABI_VERSION 1
+#define SVBRDF_ABI_VERSION 2
 
 enum {
   SVBRDF_OK = 0,
@@ -188,6 +188,51 @@ int svbrdf_batched_step(const void* device_plan, const void* host_plan, int loss
  * non-zero code if a launch gave up waiting on its pipeline. */
 int svbrdf_conv3x3_bf16(const void* x, const void* weight, const float* bias, const void* mask, void* y, int n,
                         int h, int w, int cin, int cout, int epilogue, int* err, void* stream);
+
+/* As svbrdf_conv3x3_bf16, plus epilogue 3: (acc + addend) * (mask > 0), addend BF16 NHWC like
+ * y. In the descriptor's backward pass this adds a hooked layer's loss gradient to the data
+ * gradient arriving from the layer above and applies that hooked ReLU's mask, in one pass
+ * (the autograd graph of src/descriptor.py:77-79 does the add, the mask and the next
+ * convolution as separate kernels). */
+int svbrdf_conv3x3_bf16_ex(const void* x, const void* weight, const float* bias, const void* mask,
+                           const void* addend, void* y, int n, int h, int w, int cin, int cout, int epilogue,
+                           int* err, void* stream);
+
+/* ---- descriptor loss: fused glue around the convolutions (no counterpart kernels in the
+ * reference, whose VGGLoss runs torchvision modules and autograd, src/descriptor.py:7-79) ---- */
+
+/* Number of per-block partial sums svbrdf_desc_feat_loss writes. */
+int svbrdf_desc_partials(void);
+
+/* 2x2 box downsample (if `downsample`) of renders [v][3][2h][2w] FP32, ImageNet normalisation
+ * with the reference's statistics (src/descriptor.py:65-75), conv1_1 (weight [64][3][3][3],
+ * bias [64], FP32, zero padding 1) and ReLU. Writes NHWC [v][h][w][64] in FP32 (out_f32) and
+ * BF16 (out_bf16). */
+int svbrdf_desc_conv1_fwd(const float* renders, const float* weight, const float* bias, float* out_f32,
+                          void* out_bf16, int v, int h, int w, int downsample, void* stream);
+
+/* Data gradient of svbrdf_desc_conv1_fwd before its ReLU: gz BF16 NHWC [v][h][w][64] (the
+ * masked gradient at conv1_1's output) -> grad_renders FP32 [v][3][2h][2w] (or [v][3][h][w]
+ * without `downsample`), overwritten. */
+int svbrdf_desc_conv1_bwd(const void* gz, const float* weight, float* grad_renders, int v, int h, int w,
+                          int downsample, void* stream);
+
+/* 2x2 max-pool, BF16 NHWC [v][h][w][c] -> [v][h/2][w/2][c]; h, w even, c % 8 == 0. */
+int svbrdf_desc_pool_fwd(const void* x, void* y, int v, int h, int w, int c, void* stream);
+
+/* Max-pool backward fused with a hook gradient and a ReLU mask: gx = (route(gy) + addend) *
+ * (x > 0), where x [v][h][w][c] is the pool's input (a ReLU output), gy [v][h/2][w/2][c] the
+ * gradient at its output, addend (nullable) like x. The first maximum of each 2x2 window in
+ * row-major order takes the gradient, as ATen's max-pool does. BF16 throughout. */
+int svbrdf_desc_pool_bwd(const void* gy, const void* x, const void* addend, void* gx, int v, int h, int w, int c,
+                         void* stream);
+
+/* Feature term of one hook: partial[b] (b < svbrdf_desc_partials(), if partial) = block b's
+ * share of sum (f - t)^2, a fixed-order split; if g: g = coef (f - t) + gram_grad (nullable),
+ * times (f > 0) if `mask`, stored BF16. f is BF16 (f_is_bf16) or FP32, t and gram_grad FP32,
+ * all n elements. */
+int svbrdf_desc_feat_loss(const void* f, int f_is_bf16, const float* t, const float* gram_grad, float coef, int mask,
+                          void* g, float* partial, long long n, void* stream);
 
 #ifdef __cplusplus
 }

@@ -20,7 +20,7 @@ CSRC = PKG / "csrc"
 INCLUDE = REPO / "include"
 LIBDIR = PKG / "_lib"
 LIBNAME = "libsvbrdf_gb300.so"
-SOURCES = ["render.cu", "fused.cu", "conv_tc.cu"]
+SOURCES = ["render.cu", "fused.cu", "conv_tc.cu", "desc_ops.cu"]
 HEADERS = ["svbrdf_math.cuh", "svbrdf_common.cuh", "svbrdf_plan.cuh"]
 WORKSPACE_ERROR_OFFSET = 4
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -123,6 +123,19 @@ def _declare(L):
     L.svbrdf_fused_step_noalloc.argtypes = [P, P, P, P, P, P, P, P, I, I, I, F, I, I, F, F, F, F, P, P]
     L.svbrdf_conv3x3_bf16.restype = I
     L.svbrdf_conv3x3_bf16.argtypes = [P, P, P, P, P, I, I, I, I, I, I, P, P]
+    L.svbrdf_conv3x3_bf16_ex.restype = I
+    L.svbrdf_conv3x3_bf16_ex.argtypes = [P, P, P, P, P, P, I, I, I, I, I, I, P, P]
+    L.svbrdf_desc_partials.restype = I
+    L.svbrdf_desc_conv1_fwd.restype = I
+    L.svbrdf_desc_conv1_fwd.argtypes = [P, P, P, P, P, I, I, I, I, P]
+    L.svbrdf_desc_conv1_bwd.restype = I
+    L.svbrdf_desc_conv1_bwd.argtypes = [P, P, P, I, I, I, I, P]
+    L.svbrdf_desc_pool_fwd.restype = I
+    L.svbrdf_desc_pool_fwd.argtypes = [P, P, I, I, I, I, P]
+    L.svbrdf_desc_pool_bwd.restype = I
+    L.svbrdf_desc_pool_bwd.argtypes = [P, P, P, P, I, I, I, I, P]
+    L.svbrdf_desc_feat_loss.restype = I
+    L.svbrdf_desc_feat_loss.argtypes = [P, I, P, P, F, I, P, P, ctypes.c_longlong, P]
     L.svbrdf_batched_plan_bytes.restype = S
     L.svbrdf_batched_plan_bytes.argtypes = [ctypes.POINTER(svbrdf_material), I, ctypes.POINTER(svbrdf_batch_config)]
     L.svbrdf_batched_plan.restype = I
@@ -140,6 +153,8 @@ EXPORTS = [
     "svbrdf_render_fwd", "svbrdf_render_bwd", "svbrdf_fused_step", "svbrdf_fused_step_noalloc",
     "svbrdf_batched_plan_bytes",
     "svbrdf_batched_plan", "svbrdf_batched_workspace_bytes", "svbrdf_batched_step", "svbrdf_conv3x3_bf16",
+    "svbrdf_conv3x3_bf16_ex", "svbrdf_desc_partials", "svbrdf_desc_conv1_fwd", "svbrdf_desc_conv1_bwd",
+    "svbrdf_desc_pool_fwd", "svbrdf_desc_pool_bwd", "svbrdf_desc_feat_loss",
 ]
 
 

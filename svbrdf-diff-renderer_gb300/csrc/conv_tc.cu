@@ -32,7 +32,7 @@ constexpr int BK = 64;   // input channels per stage (one 128-byte swizzle row)
 constexpr int kThreads = 192;  // warp 0 TMA, warp 1 MMA + TMEM owner, warps 2..5 epilogue
 constexpr uint32_t kSpin = 1u << 22;
 
-enum Epilogue : int { kEpiNone = 0, kEpiBiasRelu = 1, kEpiMask = 2 };
+enum Epilogue : int { kEpiNone = 0, kEpiBiasRelu = 1, kEpiMask = 2, kEpiAddMask = 3 };
 enum ConvError : int { kErrTma = 11, kErrMma = 12, kErrEpi = 13 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -131,7 +131,8 @@ template <int BN, int STAGES, int EPI>
 __global__ void __launch_bounds__(kThreads, 2)
 conv3x3_tc_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_constant__ CUtensorMap tmap_w,
                   const float* __restrict__ bias, const __nv_bfloat16* __restrict__ mask,
-                  __nv_bfloat16* __restrict__ y, int H, int W, int Cin, int Cout, int* err) {
+                  const __nv_bfloat16* __restrict__ addend, __nv_bfloat16* __restrict__ y, int H, int W, int Cin,
+                  int Cout, int* err) {
   using S = Shape<BN>;
   extern __shared__ uint8_t dsmem[];
   __shared__ __align__(8) uint64_t full_bar[STAGES];
@@ -227,7 +228,21 @@ conv3x3_tc_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_const
         if (EPI == kEpiBiasRelu) {
 #pragma unroll
           for (int j = 0; j < 32; ++j) v[j] = fmaxf(v[j] + __ldg(bias + n0 + c0 + j), 0.0f);
-        } else if (EPI == kEpiMask) {
+        } else if (EPI == kEpiMask || EPI == kEpiAddMask) {
+          if (EPI == kEpiAddMask) {  // + the hook's loss gradient at this activation
+            const uint4* ap = reinterpret_cast<const uint4*>(addend + pix * Cout + n0 + c0);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              const uint4 av = __ldg(ap + u);
+              const __nv_bfloat162* a2 = reinterpret_cast<const __nv_bfloat162*>(&av);
+#pragma unroll
+              for (int e = 0; e < 4; ++e) {
+                const float2 f = __bfloat1622float2(a2[e]);
+                v[u * 8 + 2 * e] += f.x;
+                v[u * 8 + 2 * e + 1] += f.y;
+              }
+            }
+          }
           const uint4* mp = reinterpret_cast<const uint4*>(mask + pix * Cout + n0 + c0);
 #pragma unroll
           for (int u = 0; u < 4; ++u) {
@@ -281,8 +296,8 @@ static int get_encoder() {
 }
 
 template <int BN, int STAGES, int EPI>
-static int launch(const CUtensorMap& mx, const CUtensorMap& mw, const float* bias, const void* mask, void* y, int n,
-                  int h, int w, int cin, int cout, int* err, cudaStream_t st) {
+static int launch(const CUtensorMap& mx, const CUtensorMap& mw, const float* bias, const void* mask,
+                  const void* addend, void* y, int n, int h, int w, int cin, int cout, int* err, cudaStream_t st) {
   auto kern = conv3x3_tc_kernel<BN, STAGES, EPI>;
   const size_t smem = (size_t)STAGES * Shape<BN>::kStage + 1024;
   static bool attr = false;
@@ -292,20 +307,24 @@ static int launch(const CUtensorMap& mx, const CUtensorMap& mw, const float* bia
     attr = true;
   }
   dim3 grid((unsigned)(n * (h / TH) * (w / TW)), (unsigned)(cout / BN));
-  kern<<<grid, kThreads, smem, st>>>(mx, mw, bias, (const __nv_bfloat16*)mask, (__nv_bfloat16*)y, h, w, cin, cout, err);
+  kern<<<grid, kThreads, smem, st>>>(mx, mw, bias, (const __nv_bfloat16*)mask, (const __nv_bfloat16*)addend,
+                                     (__nv_bfloat16*)y, h, w, cin, cout, err);
   return check_launch("conv3x3_tc_kernel");
 }
 
 template <int BN>
 static int dispatch_epi(int epi, const CUtensorMap& mx, const CUtensorMap& mw, const float* bias, const void* mask,
-                        void* y, int n, int h, int w, int cin, int cout, int* err, cudaStream_t st) {
+                        const void* addend, void* y, int n, int h, int w, int cin, int cout, int* err,
+                        cudaStream_t st) {
   // 96 KB of stages per CTA: two CTAs share an SM (and its 512 TMEM columns), so one
   // CTA's epilogue overlaps the other's main loop
   constexpr int STAGES = BN == 256 ? 2 : (BN == 128 ? 3 : 4);
   switch (epi) {
-    case kEpiNone: return launch<BN, STAGES, kEpiNone>(mx, mw, bias, mask, y, n, h, w, cin, cout, err, st);
-    case kEpiBiasRelu: return launch<BN, STAGES, kEpiBiasRelu>(mx, mw, bias, mask, y, n, h, w, cin, cout, err, st);
-    default: return launch<BN, STAGES, kEpiMask>(mx, mw, bias, mask, y, n, h, w, cin, cout, err, st);
+    case kEpiNone: return launch<BN, STAGES, kEpiNone>(mx, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st);
+    case kEpiBiasRelu:
+      return launch<BN, STAGES, kEpiBiasRelu>(mx, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st);
+    case kEpiMask: return launch<BN, STAGES, kEpiMask>(mx, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st);
+    default: return launch<BN, STAGES, kEpiAddMask>(mx, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st);
   }
 }
 
@@ -314,18 +333,21 @@ static int dispatch_epi(int epi, const CUtensorMap& mx, const CUtensorMap& mw, c
 
 using namespace svb;
 
-extern "C" int svbrdf_conv3x3_bf16(const void* x, const void* weight, const float* bias, const void* mask, void* y,
-                                   int n, int h, int w, int cin, int cout, int epilogue, int* err, void* stream) {
+extern "C" int svbrdf_conv3x3_bf16_ex(const void* x, const void* weight, const float* bias, const void* mask,
+                                      const void* addend, void* y, int n, int h, int w, int cin, int cout, int epilogue,
+                                      int* err, void* stream) {
   using namespace svb::tc;
   if (!x || !weight || !y || !err) return fail(SVBRDF_ERR_INVALID, "null x/weight/y/err");
   if (n < 1 || h < TH || w < TW || h % TH || w % TW)
     return fail(SVBRDF_ERR_UNSUPPORTED, "conv3x3: H must be a multiple of %d and W of %d (got %dx%d)", TH, TW, h, w);
   if (cin < BK || cin % BK || cout < 64 || cout % 64 || cin > 4096 || cout > 4096)
     return fail(SVBRDF_ERR_UNSUPPORTED, "conv3x3: channels must be multiples of 64 (got %d -> %d)", cin, cout);
-  if (epilogue < kEpiNone || epilogue > kEpiMask) return fail(SVBRDF_ERR_INVALID, "bad epilogue %d", epilogue);
+  if (epilogue < kEpiNone || epilogue > kEpiAddMask) return fail(SVBRDF_ERR_INVALID, "bad epilogue %d", epilogue);
   if (epilogue == kEpiBiasRelu && !bias) return fail(SVBRDF_ERR_INVALID, "bias+relu epilogue needs bias");
-  if (epilogue == kEpiMask && !mask) return fail(SVBRDF_ERR_INVALID, "mask epilogue needs mask");
-  if (((uintptr_t)x | (uintptr_t)weight | (uintptr_t)y | (uintptr_t)mask) % 16)
+  if ((epilogue == kEpiMask || epilogue == kEpiAddMask) && !mask)
+    return fail(SVBRDF_ERR_INVALID, "mask epilogue needs mask");
+  if (epilogue == kEpiAddMask && !addend) return fail(SVBRDF_ERR_INVALID, "add+mask epilogue needs addend");
+  if (((uintptr_t)x | (uintptr_t)weight | (uintptr_t)y | (uintptr_t)mask | (uintptr_t)addend) % 16)
     return fail(SVBRDF_ERR_INVALID, "conv3x3: tensors must be 16-byte aligned");
   if ((long long)n * h * w * cin >= (1LL << 40)) return fail(SVBRDF_ERR_UNSUPPORTED, "conv3x3: tensor too large");
   int rc = get_encoder();
@@ -354,8 +376,14 @@ extern "C" int svbrdf_conv3x3_bf16(const void* x, const void* weight, const floa
   }
   cudaStream_t st = (cudaStream_t)stream;
   switch (bn) {
-    case 256: return dispatch_epi<256>(epilogue, mx, mw, bias, mask, y, n, h, w, cin, cout, err, st);
-    case 128: return dispatch_epi<128>(epilogue, mx, mw, bias, mask, y, n, h, w, cin, cout, err, st);
-    default: return dispatch_epi<64>(epilogue, mx, mw, bias, mask, y, n, h, w, cin, cout, err, st);
+    case 256: return dispatch_epi<256>(epilogue, mx, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st);
+    case 128: return dispatch_epi<128>(epilogue, mx, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st);
+    default: return dispatch_epi<64>(epilogue, mx, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st);
   }
+}
+
+extern "C" int svbrdf_conv3x3_bf16(const void* x, const void* weight, const float* bias, const void* mask, void* y,
+                                   int n, int h, int w, int cin, int cout, int epilogue, int* err, void* stream) {
+  if (epilogue == svb::tc::kEpiAddMask) return fail(SVBRDF_ERR_INVALID, "add+mask epilogue needs svbrdf_conv3x3_bf16_ex");
+  return svbrdf_conv3x3_bf16_ex(x, weight, bias, mask, nullptr, y, n, h, w, cin, cout, epilogue, err, stream);
 }

@@ -1,0 +1,371 @@
+// Fused operations of the descriptor loss around the tensor-core convolutions (conv_tc.cu).
+//
+// The descriptor (src/descriptor.py:7-79) normalises the renders with ImageNet statistics
+// (mean 0.485/0.456/0.406, std 0.229/0.224/0.255, :65-75), runs VGG19 features and compares
+// hooked ReLU outputs. Here the renders are first 2x2 box-downsampled, and the stack up to
+// conv4_1 runs in NHWC BF16. These kernels replace the elementwise glue:
+//
+//   desc_conv1_fwd_kernel  2x2 box downsample + normalise + conv1_1 (3 -> 64) + bias + ReLU,
+//                          FP32 and BF16 NHWC outputs (the FP32 copy feeds the relu1_1 hook)
+//   desc_pool_fwd_kernel   2x2 max-pool, NHWC BF16
+//   desc_pool_bwd_kernel   max-pool backward (the first maximum of each window takes the
+//                          gradient, as ATen's pool) + optional hook gradient + ReLU mask
+//   desc_feat_loss_kernel  sum of (f - t)^2 as per-block partials (a fixed-order sum), and
+//                          optionally g = coef (f - t) + gram_grad, masked by f > 0
+//   desc_conv1_bwd_kernel  conv1_1 data gradient, back through the normalisation and the
+//                          downsample to d/d render
+//
+// Each is HBM-bound elementwise or small-stencil work: one read and one write per element.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "svbrdf_common.cuh"
+
+namespace svb {
+namespace desc {
+
+__constant__ float c_mean[3] = {0.485f, 0.456f, 0.406f};
+__constant__ float c_std[3] = {0.229f, 0.224f, 0.255f};  // the reference's blue std is 0.255
+
+constexpr int kTile = 16;
+
+// ---------------------------------------------------------------- conv1_1 forward
+template <bool DOWN>
+__global__ void __launch_bounds__(256) desc_conv1_fwd_kernel(const float* __restrict__ r, const float* __restrict__ w,
+                                                             const float* __restrict__ b, float* __restrict__ out32,
+                                                             __nv_bfloat16* __restrict__ out16, int H, int W) {
+  __shared__ float s_in[3][kTile + 2][kTile + 2];
+  __shared__ float s_w[64][27];
+  __shared__ float s_b[64];
+  const int tid = threadIdx.y * kTile + threadIdx.x;
+  const int v = blockIdx.z, y0 = blockIdx.y * kTile, x0 = blockIdx.x * kTile;
+  for (int i = tid; i < 64 * 27; i += 256) s_w[i / 27][i % 27] = w[i];  // [co][ci][ky][kx]
+  if (tid < 64) s_b[tid] = b[tid];
+  const int RH = DOWN ? 2 * H : H, RW = DOWN ? 2 * W : W;
+  for (int i = tid; i < 3 * (kTile + 2) * (kTile + 2); i += 256) {
+    const int ci = i / ((kTile + 2) * (kTile + 2)), rem = i % ((kTile + 2) * (kTile + 2));
+    const int ty = rem / (kTile + 2), tx = rem % (kTile + 2);
+    const int gy = y0 + ty - 1, gx = x0 + tx - 1;
+    float val = 0.0f;  // zero padding of the normalised image
+    if (gy >= 0 && gy < H && gx >= 0 && gx < W) {
+      const float* rp = r + ((size_t)v * 3 + ci) * RH * RW;
+      float s;
+      if (DOWN) {
+        const float* q = rp + (size_t)(2 * gy) * RW + 2 * gx;
+        s = (q[0] + q[1] + q[RW] + q[RW + 1]) * 0.25f;
+      } else {
+        s = rp[(size_t)gy * RW + gx];
+      }
+      val = (s - c_mean[ci]) / c_std[ci];
+    }
+    s_in[ci][ty][tx] = val;
+  }
+  __syncthreads();
+  const int ty = threadIdx.y, tx = threadIdx.x;
+  const int y = y0 + ty, x = x0 + tx;
+  if (y >= H || x >= W) return;
+  float xin[27];
+#pragma unroll
+  for (int ci = 0; ci < 3; ++ci)
+#pragma unroll
+    for (int ky = 0; ky < 3; ++ky)
+#pragma unroll
+      for (int kx = 0; kx < 3; ++kx) xin[ci * 9 + ky * 3 + kx] = s_in[ci][ty + ky][tx + kx];
+  const size_t pix = ((size_t)v * H + y) * W + x;
+  float4* o32 = reinterpret_cast<float4*>(out32 + pix * 64);
+  uint2* o16 = reinterpret_cast<uint2*>(out16 + pix * 64);
+#pragma unroll 4
+  for (int c4 = 0; c4 < 16; ++c4) {
+    float a[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int co = c4 * 4 + e;
+      float acc = s_b[co];
+#pragma unroll
+      for (int k = 0; k < 27; ++k) acc = fmaf(s_w[co][k], xin[k], acc);
+      a[e] = fmaxf(acc, 0.0f);
+    }
+    o32[c4] = make_float4(a[0], a[1], a[2], a[3]);
+    __nv_bfloat162 h0 = __floats2bfloat162_rn(a[0], a[1]), h1 = __floats2bfloat162_rn(a[2], a[3]);
+    uint2 pk;
+    pk.x = *reinterpret_cast<uint32_t*>(&h0);
+    pk.y = *reinterpret_cast<uint32_t*>(&h1);
+    o16[c4] = pk;
+  }
+}
+
+// ---------------------------------------------------------------- conv1_1 data gradient
+// d in(y, x, ci) = sum_{co, ky, kx} w[co][ci][ky][kx] gz(y + 1 - ky, x + 1 - kx, co); then
+// d render = d in / std, spread over the 2x2 block with weight 1/4 when downsampling.
+template <bool DOWN>
+__global__ void __launch_bounds__(256) desc_conv1_bwd_kernel(const __nv_bfloat16* __restrict__ gz,
+                                                             const float* __restrict__ w, float* __restrict__ gr,
+                                                             int H, int W) {
+  __shared__ __nv_bfloat16 s_g[64][kTile + 2][kTile + 2];  // gz tile, channel-major
+  __shared__ float s_w[27][64];                             // [ci*9 + ky*3 + kx][co]
+  const int tid = threadIdx.y * kTile + threadIdx.x;
+  const int v = blockIdx.z, y0 = blockIdx.y * kTile, x0 = blockIdx.x * kTile;
+  for (int i = tid; i < 64 * 27; i += 256) s_w[i % 27][i / 27] = w[i];
+  // rows y0-1 .. y0+16 and columns x0-1 .. x0+16 of gz, 8 channels per step
+  for (int i = tid; i < (kTile + 2) * (kTile + 2) * 8; i += 256) {
+    const int p = i / 8, c8 = i % 8;
+    const int ty = p / (kTile + 2), tx = p % (kTile + 2);
+    const int gy = y0 + ty - 1, gx = x0 + tx - 1;
+    uint4 val = make_uint4(0u, 0u, 0u, 0u);
+    if (gy >= 0 && gy < H && gx >= 0 && gx < W)
+      val = *reinterpret_cast<const uint4*>(gz + (((size_t)v * H + gy) * W + gx) * 64 + c8 * 8);
+    const __nv_bfloat16* e = reinterpret_cast<const __nv_bfloat16*>(&val);
+#pragma unroll
+    for (int j = 0; j < 8; ++j) s_g[c8 * 8 + j][ty][tx] = e[j];
+  }
+  __syncthreads();
+  const int ty = threadIdx.y, tx = threadIdx.x;
+  const int y = y0 + ty, x = x0 + tx;
+  if (y >= H || x >= W) return;
+  float d[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+  for (int ky = 0; ky < 3; ++ky)
+#pragma unroll
+    for (int kx = 0; kx < 3; ++kx) {
+      // gz at output (y + 1 - ky, x + 1 - kx) = tile (ty + 2 - ky, tx + 2 - kx)
+      const int sy = ty + 2 - ky, sx = tx + 2 - kx;
+#pragma unroll 8
+      for (int co = 0; co < 64; ++co) {
+        const float g = __bfloat162float(s_g[co][sy][sx]);
+#pragma unroll
+        for (int ci = 0; ci < 3; ++ci) d[ci] = fmaf(s_w[ci * 9 + ky * 3 + kx][co], g, d[ci]);
+      }
+    }
+  const int RH = DOWN ? 2 * H : H, RW = DOWN ? 2 * W : W;
+#pragma unroll
+  for (int ci = 0; ci < 3; ++ci) {
+    float* rp = gr + ((size_t)v * 3 + ci) * RH * RW;
+    const float g = d[ci] / c_std[ci];
+    if (DOWN) {
+      const float q = 0.25f * g;
+      *reinterpret_cast<float2*>(rp + (size_t)(2 * y) * RW + 2 * x) = make_float2(q, q);
+      *reinterpret_cast<float2*>(rp + (size_t)(2 * y + 1) * RW + 2 * x) = make_float2(q, q);
+    } else {
+      rp[(size_t)y * RW + x] = g;
+    }
+  }
+}
+
+// ---------------------------------------------------------------- 2x2 max-pool
+__device__ __forceinline__ void bf8_load(const __nv_bfloat16* p, float f[8]) {
+  const uint4 u = *reinterpret_cast<const uint4*>(p);
+  const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&u);
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const float2 t = __bfloat1622float2(h[j]);
+    f[2 * j] = t.x;
+    f[2 * j + 1] = t.y;
+  }
+}
+__device__ __forceinline__ void bf8_store(__nv_bfloat16* p, const float f[8]) {
+  uint4 u;
+  uint32_t* w = reinterpret_cast<uint32_t*>(&u);
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    __nv_bfloat162 h = __floats2bfloat162_rn(f[2 * j], f[2 * j + 1]);
+    w[j] = *reinterpret_cast<uint32_t*>(&h);
+  }
+  *reinterpret_cast<uint4*>(p) = u;
+}
+
+// x [V, H, W, C] -> y [V, H/2, W/2, C]; one thread per output pixel and 8 channels.
+__global__ void desc_pool_fwd_kernel(const __nv_bfloat16* __restrict__ x, __nv_bfloat16* __restrict__ y, int V, int H,
+                                     int W, int C) {
+  const int Ho = H / 2, Wo = W / 2, C8 = C / 8;
+  const long long n = (long long)V * Ho * Wo * C8;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int c8 = (int)(i % C8);
+    const long long p = i / C8;
+    const int xo = (int)(p % Wo), yo = (int)((p / Wo) % Ho), v = (int)(p / ((long long)Wo * Ho));
+    const __nv_bfloat16* base = x + (((size_t)v * H + 2 * yo) * W + 2 * xo) * C + c8 * 8;
+    float m[8], t[8];
+    bf8_load(base, m);
+    const size_t offs[3] = {(size_t)C, (size_t)W * C, (size_t)W * C + C};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      bf8_load(base + offs[k], t);
+#pragma unroll
+      for (int j = 0; j < 8; ++j) m[j] = t[j] > m[j] ? t[j] : m[j];
+    }
+    bf8_store(y + p * C + c8 * 8, m);
+  }
+}
+
+// gx = (pool-route(gy) + addend) * (x > 0). x is the pool's input, a ReLU output, so x > 0 is
+// that ReLU's mask. The window's first maximum in row-major order takes the gradient.
+__global__ void desc_pool_bwd_kernel(const __nv_bfloat16* __restrict__ gy, const __nv_bfloat16* __restrict__ x,
+                                     const __nv_bfloat16* __restrict__ addend, __nv_bfloat16* __restrict__ gx, int V,
+                                     int H, int W, int C) {
+  const int Ho = H / 2, Wo = W / 2, C8 = C / 8;
+  const long long n = (long long)V * Ho * Wo * C8;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int c8 = (int)(i % C8);
+    const long long p = i / C8;
+    const int xo = (int)(p % Wo), yo = (int)((p / Wo) % Ho), v = (int)(p / ((long long)Wo * Ho));
+    const size_t b0 = (((size_t)v * H + 2 * yo) * W + 2 * xo) * C + c8 * 8;
+    const size_t offs[4] = {0, (size_t)C, (size_t)W * C, (size_t)W * C + C};
+    float xv[4][8], g[8];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) bf8_load(x + b0 + offs[k], xv[k]);
+    bf8_load(gy + p * C + c8 * 8, g);
+    int am[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      float m = xv[0][j];
+      am[j] = 0;
+#pragma unroll
+      for (int k = 1; k < 4; ++k)
+        if (xv[k][j] > m) { m = xv[k][j]; am[j] = k; }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      float o[8], ad[8];
+      if (addend) bf8_load(addend + b0 + offs[k], ad);
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        float val = (am[j] == k) ? g[j] : 0.0f;
+        if (addend) val += ad[j];
+        o[j] = xv[k][j] > 0.0f ? val : 0.0f;
+      }
+      bf8_store(gx + b0 + offs[k], o);
+    }
+  }
+}
+
+// ---------------------------------------------------------------- feature loss
+constexpr int kLossThreads = 256;
+constexpr int kLossBlocks = 1024;
+
+template <typename TF>
+__device__ __forceinline__ float ld(const TF* p, long long i);
+template <>
+__device__ __forceinline__ float ld<float>(const float* p, long long i) {
+  return __ldg(p + i);
+}
+template <>
+__device__ __forceinline__ float ld<__nv_bfloat16>(const __nv_bfloat16* p, long long i) {
+  return __bfloat162float(p[i]);
+}
+
+// partial[b] = sum over block b's elements of (f - t)^2 (elements i = b*T + t, step B*T);
+// if g: g = coef (f - t) + gram_grad, times (f > 0) when `mask`.
+template <typename TF>
+__global__ void __launch_bounds__(kLossThreads) desc_feat_loss_kernel(const TF* __restrict__ f,
+                                                                      const float* __restrict__ t,
+                                                                      const float* __restrict__ gram_grad, float coef,
+                                                                      int mask, __nv_bfloat16* __restrict__ g,
+                                                                      float* __restrict__ partial, long long n) {
+  __shared__ float s_red[kLossThreads / 32];
+  float acc = 0.0f;
+  for (long long i = blockIdx.x * (long long)kLossThreads + threadIdx.x; i < n; i += (long long)kLossBlocks * kLossThreads) {
+    const float fv = ld<TF>(f, i);
+    const float d = fv - __ldg(t + i);
+    acc = fmaf(d, d, acc);
+    if (g) {
+      float gv = coef * d;
+      if (gram_grad) gv += __ldg(gram_grad + i);
+      if (mask && !(fv > 0.0f)) gv = 0.0f;
+      g[i] = __float2bfloat16_rn(gv);
+    }
+  }
+  if (partial) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float s = 0.0f;
+      for (int w = 0; w < kLossThreads / 32; ++w) s += s_red[w];
+      partial[blockIdx.x] = s;
+    }
+  }
+}
+
+}  // namespace desc
+}  // namespace svb
+
+using namespace svb;
+using namespace svb::desc;
+
+static int grid_for_elems(long long n) {
+  const long long b = (n + 255) / 256;
+  return (int)(b < 4096 ? (b < 1 ? 1 : b) : 4096);
+}
+
+extern "C" {
+
+int svbrdf_desc_partials() { return kLossBlocks; }
+
+int svbrdf_desc_conv1_fwd(const float* renders, const float* weight, const float* bias, float* out_f32,
+                          void* out_bf16, int v, int h, int w, int downsample, void* stream) {
+  if (!renders || !weight || !bias || !out_f32 || !out_bf16) return fail(SVBRDF_ERR_INVALID, "null pointer");
+  if (v < 1 || h < 1 || w < 1) return fail(SVBRDF_ERR_INVALID, "bad shape");
+  if (((uintptr_t)out_f32 | (uintptr_t)out_bf16) % 16) return fail(SVBRDF_ERR_INVALID, "outputs must be 16-byte aligned");
+  dim3 grid((w + kTile - 1) / kTile, (h + kTile - 1) / kTile, v), block(kTile, kTile);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (downsample)
+    desc_conv1_fwd_kernel<true><<<grid, block, 0, st>>>(renders, weight, bias, out_f32, (__nv_bfloat16*)out_bf16, h, w);
+  else
+    desc_conv1_fwd_kernel<false><<<grid, block, 0, st>>>(renders, weight, bias, out_f32, (__nv_bfloat16*)out_bf16, h, w);
+  return check_launch("desc_conv1_fwd_kernel");
+}
+
+int svbrdf_desc_conv1_bwd(const void* gz, const float* weight, float* grad_renders, int v, int h, int w, int downsample,
+                          void* stream) {
+  if (!gz || !weight || !grad_renders) return fail(SVBRDF_ERR_INVALID, "null pointer");
+  if (v < 1 || h < 1 || w < 1) return fail(SVBRDF_ERR_INVALID, "bad shape");
+  if ((uintptr_t)gz % 16 || (downsample && (uintptr_t)grad_renders % 8))
+    return fail(SVBRDF_ERR_INVALID, "misaligned gz/grad_renders");
+  dim3 grid((w + kTile - 1) / kTile, (h + kTile - 1) / kTile, v), block(kTile, kTile);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (downsample)
+    desc_conv1_bwd_kernel<true><<<grid, block, 0, st>>>((const __nv_bfloat16*)gz, weight, grad_renders, h, w);
+  else
+    desc_conv1_bwd_kernel<false><<<grid, block, 0, st>>>((const __nv_bfloat16*)gz, weight, grad_renders, h, w);
+  return check_launch("desc_conv1_bwd_kernel");
+}
+
+int svbrdf_desc_pool_fwd(const void* x, void* y, int v, int h, int w, int c, void* stream) {
+  if (!x || !y) return fail(SVBRDF_ERR_INVALID, "null pointer");
+  if (v < 1 || h < 2 || w < 2 || h % 2 || w % 2 || c < 8 || c % 8)
+    return fail(SVBRDF_ERR_UNSUPPORTED, "pool: even H, W and C a multiple of 8 needed");
+  if (((uintptr_t)x | (uintptr_t)y) % 16) return fail(SVBRDF_ERR_INVALID, "pool: 16-byte alignment needed");
+  const long long n = (long long)v * (h / 2) * (w / 2) * (c / 8);
+  desc_pool_fwd_kernel<<<grid_for_elems(n), 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16*)x, (__nv_bfloat16*)y,
+                                                                          v, h, w, c);
+  return check_launch("desc_pool_fwd_kernel");
+}
+
+int svbrdf_desc_pool_bwd(const void* gy, const void* x, const void* addend, void* gx, int v, int h, int w, int c,
+                         void* stream) {
+  if (!gy || !x || !gx) return fail(SVBRDF_ERR_INVALID, "null pointer");
+  if (v < 1 || h < 2 || w < 2 || h % 2 || w % 2 || c < 8 || c % 8)
+    return fail(SVBRDF_ERR_UNSUPPORTED, "pool: even H, W and C a multiple of 8 needed");
+  if (((uintptr_t)gy | (uintptr_t)x | (uintptr_t)addend | (uintptr_t)gx) % 16)
+    return fail(SVBRDF_ERR_INVALID, "pool: 16-byte alignment needed");
+  const long long n = (long long)v * (h / 2) * (w / 2) * (c / 8);
+  desc_pool_bwd_kernel<<<grid_for_elems(n), 256, 0, (cudaStream_t)stream>>>(
+      (const __nv_bfloat16*)gy, (const __nv_bfloat16*)x, (const __nv_bfloat16*)addend, (__nv_bfloat16*)gx, v, h, w, c);
+  return check_launch("desc_pool_bwd_kernel");
+}
+
+int svbrdf_desc_feat_loss(const void* f, int f_is_bf16, const float* t, const float* gram_grad, float coef, int mask,
+                          void* g, float* partial, long long n, void* stream) {
+  if (!f || !t || n < 1) return fail(SVBRDF_ERR_INVALID, "null pointer or empty");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (f_is_bf16)
+    desc_feat_loss_kernel<__nv_bfloat16><<<kLossBlocks, kLossThreads, 0, st>>>(
+        (const __nv_bfloat16*)f, t, gram_grad, coef, mask, (__nv_bfloat16*)g, partial, n);
+  else
+    desc_feat_loss_kernel<float><<<kLossBlocks, kLossThreads, 0, st>>>((const float*)f, t, gram_grad, coef, mask,
+                                                                      (__nv_bfloat16*)g, partial, n);
+  return check_launch("desc_feat_loss_kernel");
+}
+
+}  // extern "C"

@@ -18,9 +18,18 @@ conv4_1), weights [1, 1, 1, 1] / 4 (the reference's default).
 
 Every 3x3 convolution with 64 or more input channels runs as a tcgen05 implicit GEMM
 (``svbrdf_conv3x3_bf16``: BF16 operands, FP32 accumulation in TMEM, bias + ReLU fused).
-Its data gradient is the same kernel on the transposed, flipped weights. conv1_1 (3 input
-channels, under 1% of the FLOPs), the pools and the normalisation use torch; the Gram
-products are plain batched BF16 GEMMs (cuBLAS tensor cores, FP32 accumulation).
+Its data gradient is the same kernel on the transposed, flipped weights. The glue around
+them is fused into a few kernels of the same library:
+
+* conv1_1 (3 input channels, under 1% of the FLOPs) with the downsample and the
+  normalisation in front of it, FP32;
+* NHWC max-pools;
+* the feature term with its gradient.
+
+The backward pass is a hand-written chain, not autograd. Each data-gradient convolution's
+epilogue adds the next hook's loss gradient and applies the ReLU mask below, and the
+max-pool backward does the same. The Gram products are plain batched BF16 GEMMs (cuBLAS
+tensor cores, FP32 accumulation).
 """
 from __future__ import annotations
 
@@ -39,7 +48,7 @@ VGG19_TO_CONV4_1 = [("conv1_1", 3, 64), ("conv1_2", 64, 64), "pool", ("conv2_1",
                     ("conv3_4", 256, 256), "pool", ("conv4_1", 256, 512)]
 HOOKS = ("conv1_1", "conv1_2", "conv3_2", "conv4_1")  # their ReLU outputs
 
-EPI_NONE, EPI_BIAS_RELU, EPI_MASK = 0, 1, 2
+EPI_NONE, EPI_BIAS_RELU, EPI_MASK, EPI_ADD_MASK = 0, 1, 2, 3
 
 
 def conv3x3_bf16(x: torch.Tensor, w: torch.Tensor, bias: Optional[torch.Tensor], epilogue: int,
@@ -52,24 +61,6 @@ def conv3x3_bf16(x: torch.Tensor, w: torch.Tensor, bias: Optional[torch.Tensor],
     N.check(L.svbrdf_conv3x3_bf16(x.data_ptr(), w.data_ptr(), N.ptr(bias), N.ptr(mask), y.data_ptr(), n, h, wd, cin,
                                   cout, epilogue, err.data_ptr(), N.stream_handle(x.device)))
     return y
-
-
-class _ConvReLU(torch.autograd.Function):
-    """relu(conv3x3(x) + b) with frozen weights; backward gives dL/dx only."""
-
-    @staticmethod
-    def forward(ctx, x, w_fwd, w_dgrad, bias, err):
-        x = x.to(torch.bfloat16).contiguous()
-        y = conv3x3_bf16(x, w_fwd, bias, EPI_BIAS_RELU, err)
-        ctx.save_for_backward(y, w_dgrad, err)
-        return y
-
-    @staticmethod
-    def backward(ctx, gy):
-        y, w_dgrad, err = ctx.saved_tensors
-        gz = (gy.to(torch.bfloat16) * (y > 0)).contiguous()
-        gx = conv3x3_bf16(gz, w_dgrad, None, EPI_NONE, err)
-        return gx, None, None, None, None
 
 
 _BMM_F32_OUT = {}
@@ -147,39 +138,127 @@ class VGGDescriptor:
                 entry["w_fwd"] = wb.permute(0, 2, 3, 1).reshape(cout, 9, cin).contiguous().to(self.device)
                 entry["w_dg"] = wb.flip(2, 3).permute(1, 2, 3, 0).reshape(cin, 9, cout).contiguous().to(self.device)
             self.params[name] = entry
-        self.mean = torch.tensor(MEAN, device=self.device).view(1, 3, 1, 1)
-        self.std = torch.tensor(STD, device=self.device).view(1, 3, 1, 1)
+        self._w2 = torch.tensor([wt * wt for wt in self.hook_weights], device=self.device, dtype=torch.float64)
         self.target = None
 
     def bf16_weights(self):
         """{name: (weight [Cout, Cin, 3, 3] as the kernels use it, bias)} in FP32."""
         return {k: (v["w32"].cpu(), v["b"].cpu()) for k, v in self.params.items()}
 
-    def prepare(self, renders: torch.Tensor) -> torch.Tensor:
-        x = renders
-        if self.downsample:
-            x = torch.nn.functional.avg_pool2d(x, 2)
-        return (x - self.mean) / self.std
+    # ---- forward -----------------------------------------------------------------------
+    def _forward(self, renders: torch.Tensor):
+        """Run the stack. Returns (acts, hooks): acts[i] is the output of layer i of
+        VGG19_TO_CONV4_1 (NHWC BF16); hooks maps each hooked layer to its feature (relu1_1 in
+        FP32, the others BF16)."""
+        L = N.lib()
+        st = N.stream_handle(self.device)
+        x = renders.detach().float().contiguous()
+        v, _, rh, rw = x.shape
+        h, w = (rh // 2, rw // 2) if self.downsample else (rh, rw)
+        p = self.params["conv1_1"]
+        y32 = torch.empty(v, h, w, 64, device=self.device, dtype=torch.float32)
+        y16 = torch.empty(v, h, w, 64, device=self.device, dtype=torch.bfloat16)
+        N.check(L.svbrdf_desc_conv1_fwd(x.data_ptr(), p["w32"].data_ptr(), p["b"].data_ptr(), y32.data_ptr(),
+                                        y16.data_ptr(), v, h, w, int(self.downsample), st))
+        acts, hooks = [y16], {"conv1_1": y32}
+        for item in VGG19_TO_CONV4_1[1:]:
+            prev = acts[-1]
+            if item == "pool":
+                n_, hh, ww, c = prev.shape
+                y = torch.empty(n_, hh // 2, ww // 2, c, device=self.device, dtype=torch.bfloat16)
+                N.check(L.svbrdf_desc_pool_fwd(prev.data_ptr(), y.data_ptr(), n_, hh, ww, c, st))
+                acts.append(y)
+                continue
+            name, cin, cout = item
+            q = self.params[name]
+            y = conv3x3_bf16(prev, q["w_fwd"], q["b"], EPI_BIAS_RELU, self.err)
+            acts.append(y)
+            if name in HOOKS:
+                hooks[name] = y
+        return acts, hooks
+
+    # ---- loss terms --------------------------------------------------------------------
+    def _terms(self, hooks, cf: Optional[float], cg: Optional[float]):
+        """Feature and Gram losses (0-d FP32 tensors). With cf/cg given, also the loss
+        gradient at each hooked activation, cf d(feature)/df + cg d(gram)/df, as BF16 NHWC; the
+        last layer's gradient is masked by its ReLU (it starts the backward chain)."""
+        L = N.lib()
+        st = N.stream_handle(self.device)
+        tf, tg = self.target
+        nf = sum(f.numel() for f in hooks.values())
+        ng = sum(g.numel() for g in tg)
+        nparts = L.svbrdf_desc_partials()
+        parts = torch.empty(len(HOOKS), nparts, device=self.device, dtype=torch.float32)
+        gram_terms, grads = [], {}
+        last = [it for it in VGG19_TO_CONV4_1 if it != "pool"][-1][0]
+        for k, (name, wt) in enumerate(zip(HOOKS, self.hook_weights)):
+            f = hooks[name]
+            v, h, w, c = f.shape
+            s = h * w
+            ff = f.reshape(v, s, c).to(torch.bfloat16)
+            gram = _bmm_f32out(ff.transpose(1, 2), ff) / s
+            diff = gram - tg[k]
+            gram_terms.append((wt * wt) * (diff * diff).sum())
+            gg = None
+            g = None
+            if cf is not None:
+                # d/dF of w^2 sum (G - Gt)^2 / ng with G = F^T F / s: F (2 dG) / s, dG = 2 w^2 (G - Gt) / ng
+                dgram = (4.0 * wt * wt * cg / (ng * s)) * diff
+                gg = _bmm_f32out(ff, dgram.to(torch.bfloat16)).reshape(v, h, w, c).contiguous()
+                g = torch.empty(v, h, w, c, device=self.device, dtype=torch.bfloat16)
+            coef = (2.0 * wt * wt * cf / nf) if cf is not None else 0.0
+            N.check(L.svbrdf_desc_feat_loss(f.data_ptr(), int(f.dtype == torch.bfloat16), tf[k].data_ptr(),
+                                            N.ptr(gg), coef, int(name == last), N.ptr(g), parts[k].data_ptr(),
+                                            f.numel(), st))
+            if g is not None:
+                grads[name] = g
+        fl = ((parts.double().sum(dim=1) * self._w2).sum() / nf).float()
+        gl = torch.stack(gram_terms).sum() / ng
+        return fl, gl, grads
+
+    # ---- backward chain ----------------------------------------------------------------
+    def _backward(self, acts, grads, render_shape):
+        """d(loss)/d renders from the hook gradients, layer by layer in reverse:
+        data-gradient convolutions whose epilogue adds the next hook's gradient and applies
+        the ReLU mask below, max-pool backward fused the same way, and conv1_1's data
+        gradient back through the normalisation and the downsample."""
+        L = N.lib()
+        st = N.stream_handle(self.device)
+        items = VGG19_TO_CONV4_1
+        g = grads[items[-1][0]]  # masked gradient at the last ReLU
+        for i in range(len(items) - 1, 0, -1):
+            item, below = items[i], items[i - 1]
+            x = acts[i - 1]  # the input of layer i: a ReLU output, or a pool output
+            n_, h, w, c = x.shape
+            if item == "pool":
+                # below is a convolution: route, add its hook gradient, mask by its ReLU
+                gx = torch.empty_like(x)
+                add = grads.get(below[0])
+                N.check(L.svbrdf_desc_pool_bwd(g.data_ptr(), x.data_ptr(), N.ptr(add), gx.data_ptr(), n_, h, w, c,
+                                               st))
+                g = gx
+                continue
+            q = self.params[item[0]]
+            gx = torch.empty(n_, h, w, c, device=self.device, dtype=torch.bfloat16)
+            if below == "pool":
+                epi, mask, add = EPI_NONE, None, None
+            else:
+                add = grads.get(below[0])
+                epi, mask = (EPI_ADD_MASK if add is not None else EPI_MASK), x
+            N.check(L.svbrdf_conv3x3_bf16_ex(g.data_ptr(), q["w_dg"].data_ptr(), None, N.ptr(mask), N.ptr(add),
+                                             gx.data_ptr(), n_, h, w, item[2], item[1], epi, self.err.data_ptr(), st))
+            g = gx
+        v, h, w, _ = g.shape
+        dr = torch.empty(render_shape, device=self.device, dtype=torch.float32)
+        p = self.params["conv1_1"]
+        N.check(L.svbrdf_desc_conv1_bwd(g.data_ptr(), p["w32"].data_ptr(), dr.data_ptr(), v, h, w,
+                                        int(self.downsample), st))
+        return dr
 
     def features(self, renders: torch.Tensor) -> List[torch.Tensor]:
         """Hooked ReLU outputs, each NHWC [V, H, W, C] (BF16, except relu1_1 in FP32)."""
-        x = self.prepare(renders)
-        feats = []
-        act = None
-        for item in VGG19_TO_CONV4_1:
-            if item == "pool":
-                act = torch.nn.functional.max_pool2d(act.permute(0, 3, 1, 2), 2).permute(0, 2, 3, 1).contiguous()
-                continue
-            name, cin, cout = item
-            p = self.params[name]
-            if cin < 64:
-                y = torch.relu(torch.nn.functional.conv2d(x, p["w32"], p["b"], padding=1))
-                act = y.permute(0, 2, 3, 1).contiguous()
-            else:
-                act = _ConvReLU.apply(act, p["w_fwd"], p["w_dg"], p["b"], self.err)
-            if name in HOOKS:
-                feats.append(act)
-        return feats
+        _, hooks = self._forward(renders)
+        return [hooks[n] for n in HOOKS]
 
     @staticmethod
     def _gram(f: torch.Tensor) -> torch.Tensor:
@@ -189,56 +268,71 @@ class VGGDescriptor:
         self._graph = None  # a captured graph holds the previous targets' features
         with torch.no_grad():
             feats = self.features(targets)
-            self.target = ([f.float() for f in feats], [self._gram(f) for f in feats])
+            self.target = ([f.float().contiguous() for f in feats], [self._gram(f) for f in feats])
 
     def loss(self, renders: torch.Tensor):
+        """(feature_loss, gram_loss) as 0-d tensors, differentiable w.r.t. ``renders``."""
         if self.target is None:
             raise RuntimeError("call load(targets) first")
-        feats = self.features(renders)
-        tf, tg = self.target
-        fl, gl, nf, ng = 0.0, 0.0, 0, 0
-        for w, f, t, gt in zip(self.hook_weights, feats, tf, tg):
-            fl = fl + (w * w) * torch.nn.functional.mse_loss(f.float(), t, reduction="sum")
-            nf += f.numel()
-            g = self._gram(f)
-            gl = gl + (w * w) * torch.nn.functional.mse_loss(g, gt, reduction="sum")
-            ng += g.numel()
-        return fl / nf, gl / ng
+        return _DescriptorLoss.apply(renders, self)
 
     def device_error(self) -> int:
         return int(self.err.item())
 
     # ---- CUDA-graph replay of forward + backward -------------------------------------
-    # One eager pass issues a few hundred small kernels; replaying them as one graph removes
-    # the host dispatch cost, which otherwise exceeds the GPU time of the whole stack.
-    @torch.enable_grad()
+    # One pass issues a few dozen kernels; replaying them as one graph removes the host
+    # dispatch cost, which otherwise exceeds the GPU time of the whole stack.
     def _capture(self, shape):
-        static_r = torch.zeros(shape, device=self.device, requires_grad=True)
+        static_r = torch.zeros(shape, device=self.device)
         side = torch.cuda.Stream(self.device)
         side.wait_stream(torch.cuda.current_stream(self.device))
         with torch.cuda.stream(side):
             for _ in range(2):
-                static_r.grad = None
-                fl, gl = self.loss(static_r)
-                (fl + gl).backward()
+                self._loss_and_grad_eager(static_r)
         torch.cuda.current_stream(self.device).wait_stream(side)
-        static_r.grad = None
         graph = torch.cuda.CUDAGraph()
         with torch.cuda.graph(graph):
-            fl, gl = self.loss(static_r)
-            (fl + gl).backward()
-        self._graph = (tuple(shape), graph, static_r, fl, gl)
+            fl, gl, dr = self._loss_and_grad_eager(static_r)
+        self._graph = (tuple(shape), graph, static_r, fl, gl, dr)
+
+    def _loss_and_grad_eager(self, renders):
+        acts, hooks = self._forward(renders)
+        fl, gl, grads = self._terms(hooks, 1.0, 1.0)
+        return fl, gl, self._backward(acts, grads, renders.shape)
 
     def loss_and_grad(self, renders: torch.Tensor):
         """(feature_loss, gram_loss, d(feature + gram)/d renders) by one graph replay. The
         returned tensors are reused by the next call."""
+        if self.target is None:
+            raise RuntimeError("call load(targets) first")
         if getattr(self, "_graph", None) is None or self._graph[0] != tuple(renders.shape):
             self._capture(renders.shape)
-        _, graph, static_r, fl, gl = self._graph
+        _, graph, static_r, fl, gl, dr = self._graph
         with torch.no_grad():
             static_r.copy_(renders)
         graph.replay()
-        return fl, gl, static_r.grad
+        return fl, gl, dr
+
+
+class _DescriptorLoss(torch.autograd.Function):
+    """(feature, Gram) losses with the hand-written backward chain of VGGDescriptor."""
+
+    @staticmethod
+    def forward(ctx, renders, desc):
+        acts, hooks = desc._forward(renders)
+        fl, gl, _ = desc._terms(hooks, None, None)
+        ctx.desc = desc
+        ctx.shape = renders.shape
+        ctx.acts, ctx.hooks = acts, hooks
+        return fl, gl
+
+    @staticmethod
+    def backward(ctx, gfl, ggl):
+        desc = ctx.desc
+        _, _, grads = desc._terms(ctx.hooks, float(gfl), float(ggl))
+        dr = desc._backward(ctx.acts, grads, ctx.shape)
+        ctx.acts = ctx.hooks = None
+        return dr, None
 
 
 class _DescriptorTerm(torch.autograd.Function):

@@ -23,7 +23,7 @@ def test_exports_match_header(svb, lib):
 
 
 def test_constants(lib):
-    assert lib.svbrdf_abi_version() == 1
+    assert lib.svbrdf_abi_version() == 2
     assert lib.svbrdf_max_views() >= 16
     assert lib.svbrdf_workspace_bytes() >= 16
 

@@ -31,16 +31,19 @@ __constant__ float c_std[3] = {0.229f, 0.224f, 0.255f};  // the reference's blue
 constexpr int kTile = 16;
 
 // ---------------------------------------------------------------- conv1_1 forward
+// A block computes a 16 x 16 pixel tile, all 64 channels. Thread t owns channels
+// 4 (t % 16) .. +3 of the 16 pixels of tile row t / 16, so the 16 threads of a half-warp store
+// one pixel's 64 channels as one contiguous 256-byte run (128 bytes in BF16).
 template <bool DOWN>
 __global__ void __launch_bounds__(256) desc_conv1_fwd_kernel(const float* __restrict__ r, const float* __restrict__ w,
                                                              const float* __restrict__ b, float* __restrict__ out32,
                                                              __nv_bfloat16* __restrict__ out16, int H, int W) {
   __shared__ float s_in[3][kTile + 2][kTile + 2];
-  __shared__ float s_w[64][27];
-  __shared__ float s_b[64];
-  const int tid = threadIdx.y * kTile + threadIdx.x;
+  __shared__ __align__(16) float s_w[27][64];  // [ci*9 + ky*3 + kx][co]
+  __shared__ __align__(16) float s_b[64];
+  const int tid = threadIdx.x;
   const int v = blockIdx.z, y0 = blockIdx.y * kTile, x0 = blockIdx.x * kTile;
-  for (int i = tid; i < 64 * 27; i += 256) s_w[i / 27][i % 27] = w[i];  // [co][ci][ky][kx]
+  for (int i = tid; i < 64 * 27; i += 256) s_w[i % 27][i / 27] = w[i];  // w is [co][ci][ky][kx]
   if (tid < 64) s_b[tid] = b[tid];
   const int RH = DOWN ? 2 * H : H, RW = DOWN ? 2 * W : W;
   for (int i = tid; i < 3 * (kTile + 2) * (kTile + 2); i += 256) {
@@ -62,36 +65,44 @@ __global__ void __launch_bounds__(256) desc_conv1_fwd_kernel(const float* __rest
     s_in[ci][ty][tx] = val;
   }
   __syncthreads();
-  const int ty = threadIdx.y, tx = threadIdx.x;
-  const int y = y0 + ty, x = x0 + tx;
-  if (y >= H || x >= W) return;
-  float xin[27];
+  const int cg = tid & 15, row = tid >> 4;
+  const int y = y0 + row;
+  float acc[kTile][4];
+  const float4 bias4 = reinterpret_cast<const float4*>(s_b)[cg];
+#pragma unroll
+  for (int px = 0; px < kTile; ++px) {
+    acc[px][0] = bias4.x; acc[px][1] = bias4.y; acc[px][2] = bias4.z; acc[px][3] = bias4.w;
+  }
 #pragma unroll
   for (int ci = 0; ci < 3; ++ci)
 #pragma unroll
     for (int ky = 0; ky < 3; ++ky)
 #pragma unroll
-      for (int kx = 0; kx < 3; ++kx) xin[ci * 9 + ky * 3 + kx] = s_in[ci][ty + ky][tx + kx];
-  const size_t pix = ((size_t)v * H + y) * W + x;
-  float4* o32 = reinterpret_cast<float4*>(out32 + pix * 64);
-  uint2* o16 = reinterpret_cast<uint2*>(out16 + pix * 64);
-#pragma unroll 4
-  for (int c4 = 0; c4 < 16; ++c4) {
-    float a[4];
+      for (int kx = 0; kx < 3; ++kx) {
+        const float4 w4 = reinterpret_cast<const float4*>(s_w[ci * 9 + ky * 3 + kx])[cg];
 #pragma unroll
-    for (int e = 0; e < 4; ++e) {
-      const int co = c4 * 4 + e;
-      float acc = s_b[co];
+        for (int px = 0; px < kTile; ++px) {
+          const float xv = s_in[ci][row + ky][px + kx];
+          acc[px][0] = fmaf(w4.x, xv, acc[px][0]);
+          acc[px][1] = fmaf(w4.y, xv, acc[px][1]);
+          acc[px][2] = fmaf(w4.z, xv, acc[px][2]);
+          acc[px][3] = fmaf(w4.w, xv, acc[px][3]);
+        }
+      }
+  if (y >= H) return;
 #pragma unroll
-      for (int k = 0; k < 27; ++k) acc = fmaf(s_w[co][k], xin[k], acc);
-      a[e] = fmaxf(acc, 0.0f);
-    }
-    o32[c4] = make_float4(a[0], a[1], a[2], a[3]);
-    __nv_bfloat162 h0 = __floats2bfloat162_rn(a[0], a[1]), h1 = __floats2bfloat162_rn(a[2], a[3]);
+  for (int px = 0; px < kTile; ++px) {
+    const int x = x0 + px;
+    if (x >= W) break;
+    const float a0 = fmaxf(acc[px][0], 0.f), a1 = fmaxf(acc[px][1], 0.f), a2 = fmaxf(acc[px][2], 0.f),
+                a3 = fmaxf(acc[px][3], 0.f);
+    const size_t pix = ((size_t)v * H + y) * W + x;
+    reinterpret_cast<float4*>(out32 + pix * 64)[cg] = make_float4(a0, a1, a2, a3);
+    __nv_bfloat162 h0 = __floats2bfloat162_rn(a0, a1), h1 = __floats2bfloat162_rn(a2, a3);
     uint2 pk;
     pk.x = *reinterpret_cast<uint32_t*>(&h0);
     pk.y = *reinterpret_cast<uint32_t*>(&h1);
-    o16[c4] = pk;
+    reinterpret_cast<uint2*>(out16 + pix * 64)[cg] = pk;
   }
 }
 
@@ -102,8 +113,8 @@ template <bool DOWN>
 __global__ void __launch_bounds__(256) desc_conv1_bwd_kernel(const __nv_bfloat16* __restrict__ gz,
                                                              const float* __restrict__ w, float* __restrict__ gr,
                                                              int H, int W) {
-  __shared__ __nv_bfloat16 s_g[64][kTile + 2][kTile + 2];  // gz tile, channel-major
-  __shared__ float s_w[27][64];                             // [ci*9 + ky*3 + kx][co]
+  __shared__ __nv_bfloat162 s_g[32][kTile + 2][kTile + 2];  // gz tile, channel pairs outermost
+  __shared__ __align__(8) float s_w[27][64];                 // [ci*9 + ky*3 + kx][co]
   const int tid = threadIdx.y * kTile + threadIdx.x;
   const int v = blockIdx.z, y0 = blockIdx.y * kTile, x0 = blockIdx.x * kTile;
   for (int i = tid; i < 64 * 27; i += 256) s_w[i % 27][i / 27] = w[i];
@@ -115,9 +126,9 @@ __global__ void __launch_bounds__(256) desc_conv1_bwd_kernel(const __nv_bfloat16
     uint4 val = make_uint4(0u, 0u, 0u, 0u);
     if (gy >= 0 && gy < H && gx >= 0 && gx < W)
       val = *reinterpret_cast<const uint4*>(gz + (((size_t)v * H + gy) * W + gx) * 64 + c8 * 8);
-    const __nv_bfloat16* e = reinterpret_cast<const __nv_bfloat16*>(&val);
+    const __nv_bfloat162* e = reinterpret_cast<const __nv_bfloat162*>(&val);
 #pragma unroll
-    for (int j = 0; j < 8; ++j) s_g[c8 * 8 + j][ty][tx] = e[j];
+    for (int j = 0; j < 4; ++j) s_g[c8 * 4 + j][ty][tx] = e[j];
   }
   __syncthreads();
   const int ty = threadIdx.y, tx = threadIdx.x;
@@ -130,11 +141,14 @@ __global__ void __launch_bounds__(256) desc_conv1_bwd_kernel(const __nv_bfloat16
     for (int kx = 0; kx < 3; ++kx) {
       // gz at output (y + 1 - ky, x + 1 - kx) = tile (ty + 2 - ky, tx + 2 - kx)
       const int sy = ty + 2 - ky, sx = tx + 2 - kx;
-#pragma unroll 8
-      for (int co = 0; co < 64; ++co) {
-        const float g = __bfloat162float(s_g[co][sy][sx]);
+#pragma unroll 4
+      for (int c2 = 0; c2 < 32; ++c2) {
+        const float2 g = __bfloat1622float2(s_g[c2][sy][sx]);
 #pragma unroll
-        for (int ci = 0; ci < 3; ++ci) d[ci] = fmaf(s_w[ci * 9 + ky * 3 + kx][co], g, d[ci]);
+        for (int ci = 0; ci < 3; ++ci) {
+          const float2 wv = reinterpret_cast<const float2*>(s_w[ci * 9 + ky * 3 + kx])[c2];
+          d[ci] = fmaf(wv.y, g.y, fmaf(wv.x, g.x, d[ci]));
+        }
       }
     }
   const int RH = DOWN ? 2 * H : H, RW = DOWN ? 2 * W : W;
@@ -307,7 +321,7 @@ int svbrdf_desc_conv1_fwd(const float* renders, const float* weight, const float
   if (!renders || !weight || !bias || !out_f32 || !out_bf16) return fail(SVBRDF_ERR_INVALID, "null pointer");
   if (v < 1 || h < 1 || w < 1) return fail(SVBRDF_ERR_INVALID, "bad shape");
   if (((uintptr_t)out_f32 | (uintptr_t)out_bf16) % 16) return fail(SVBRDF_ERR_INVALID, "outputs must be 16-byte aligned");
-  dim3 grid((w + kTile - 1) / kTile, (h + kTile - 1) / kTile, v), block(kTile, kTile);
+  dim3 grid((w + kTile - 1) / kTile, (h + kTile - 1) / kTile, v), block(256);
   cudaStream_t st = (cudaStream_t)stream;
   if (downsample)
     desc_conv1_fwd_kernel<true><<<grid, block, 0, st>>>(renders, weight, bias, out_f32, (__nv_bfloat16*)out_bf16, h, w);

@@ -81,6 +81,20 @@ def _bmm_f32out(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
     return torch.bmm(a, b).float()
 
 
+def _gram_f32(ff: torch.Tensor) -> torch.Tensor:
+    """F^T F for F [V, S, C] BF16, FP32 result. A long S with few channels is split into
+    chunks that form one larger batch of GEMMs, so that enough CTAs run, and the chunk
+    products are summed in FP32."""
+    v, s, c = ff.shape
+    p = 1
+    while p < 32 and s % (2 * p) == 0 and s // (2 * p) >= 2048 and c <= 128:
+        p *= 2
+    if p == 1:
+        return _bmm_f32out(ff.transpose(1, 2), ff)
+    fc = ff.reshape(v * p, s // p, c)
+    return _bmm_f32out(fc.transpose(1, 2), fc).reshape(v, p, c, c).sum(dim=1)
+
+
 class _Gram(torch.autograd.Function):
     """G = F^T F / S for NHWC features F [V, H, W, C] (BF16); gradient F (dG + dG^T) / S."""
 
@@ -90,7 +104,7 @@ class _Gram(torch.autograd.Function):
         ff = f.reshape(v, h * w, c).to(torch.bfloat16)
         ctx.save_for_backward(ff)
         ctx.shape = f.shape
-        return _bmm_f32out(ff.transpose(1, 2), ff) / (h * w)
+        return _gram_f32(ff) / (h * w)
 
     @staticmethod
     def backward(ctx, g):
@@ -196,7 +210,7 @@ class VGGDescriptor:
             v, h, w, c = f.shape
             s = h * w
             ff = f.reshape(v, s, c).to(torch.bfloat16)
-            gram = _bmm_f32out(ff.transpose(1, 2), ff) / s
+            gram = _gram_f32(ff) / s
             diff = gram - tg[k]
             gram_terms.append((wt * wt) * (diff * diff).sum())
             gg = None

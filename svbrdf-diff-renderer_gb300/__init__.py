@@ -6,18 +6,21 @@ Drop-ins for the hot path of tflsguoyu/svbrdf-diff-renderer:
   hand-written adjoint behind torch.autograd;
 * ``SvbrdfOptim`` - the per-pixel Adam loop (src/svbrdf.py:15-83) as one fused
   render+adjoint+Adam kernel per iteration;
-* ``BatchedOptim`` - many materials of uneven size in one persistent launch per iteration.
+* ``BatchedOptim`` - many materials of uneven size in one persistent launch per iteration;
+* ``BatchedPipeline`` - a stream of such batches, double-buffered so the host transfers
+  overlap the compute.
 
 The package directory name contains hyphens; import it with
 ``importlib.import_module("svbrdf-diff-renderer_gb300")``.
 """
 from . import _native
 from ._native import SvbrdfError, build
-from .batched import BatchConfig, BatchedOptim, autotune
+from .batched import BatchConfig, BatchedOptim, BatchedPipeline, autotune
 from .microfacet import Microfacet
 from .svbrdf import SvbrdfIO, SvbrdfOptim
 from .scripts import optim_perpixel, render
 from . import descriptor, imageio, materialgan, scenes
 
-__all__ = ["Microfacet", "SvbrdfOptim", "SvbrdfIO", "optim_perpixel", "render", "BatchedOptim", "BatchConfig",
+__all__ = ["Microfacet", "SvbrdfOptim", "SvbrdfIO", "optim_perpixel", "render", "BatchedOptim", "BatchedPipeline",
+           "BatchConfig",
            "autotune", "SvbrdfError", "build", "scenes", "imageio", "descriptor", "materialgan", "_native"]

@@ -193,6 +193,83 @@ class BatchedOptim:
             raise N.SvbrdfError(-3, f"batched kernel reported device error {e}")
 
 
+class BatchedPipeline:
+    """A stream of batches of one shape, double-buffered so the host transfers hide behind
+    the compute.
+
+    Every batch has the same materials layout as ``materials``: resolutions, view counts,
+    cameras, lights and light power. Only the initial maps and targets change. While one
+    buffer's batch is optimised, the next batch's maps and targets upload on a copy stream
+    and the previous batch's results download on another.
+
+    * ``submit(inits, targets)`` enqueues ``iters`` iterations of one batch and returns a
+      ticket. The inputs are host tensors, pinned for asynchronous copies, one per material.
+      They must stay unchanged until the batch's upload has run.
+    * ``result(ticket)`` waits for that batch. It returns (maps, loss history) as pinned host
+      tensors, valid until the submit two tickets later reuses the buffer."""
+
+    def __init__(self, materials: Sequence, iters: int, lr: float = 0.01, loss: str = "log1p", device="cuda",
+                 config: Optional[BatchConfig] = None, betas=(0.9, 0.999), eps: float = 1e-8):
+        self.device = torch.device(device)
+        self.iters = int(iters)
+        a = BatchedOptim(materials, lr=lr, loss=loss, device=device, config=config, betas=betas, eps=eps,
+                         hist_len=self.iters)
+        b = BatchedOptim(materials, lr=lr, loss=loss, device=device, config=a.config, betas=betas, eps=eps,
+                         hist_len=self.iters)
+        self.bufs = [a, b]
+        for o in self.bufs:
+            o.capture(self.iters)
+        self.config = a.config
+        self.up = torch.cuda.Stream(self.device)
+        self.down = torch.cuda.Stream(self.device)
+        self.host_maps = [[torch.empty(t.shape, dtype=torch.float32).pin_memory() for t in o.tex] for o in self.bufs]
+        self.host_loss = [torch.empty(o.loss_hist.shape, dtype=torch.float32).pin_memory() for o in self.bufs]
+        self.done: List[Optional[torch.cuda.Event]] = [None, None]
+        self.next_ticket = 0
+
+    def h2d_bytes(self, inits, targets) -> int:
+        return sum(t.numel() * t.element_size() for t in inits) + sum(t.numel() * t.element_size() for t in targets)
+
+    def d2h_bytes(self) -> int:
+        return sum(t.numel() * 4 for t in self.host_maps[0]) + self.host_loss[0].numel() * 4
+
+    def submit(self, inits, targets) -> int:
+        j = self.next_ticket % 2
+        o = self.bufs[j]
+        comp = torch.cuda.current_stream(self.device)
+        with torch.cuda.stream(self.up):
+            if self.done[j] is not None:  # the buffer's previous batch has been read back
+                self.up.wait_event(self.done[j])
+            o.reset(inits=inits, targets=targets)
+            uploaded = torch.cuda.Event()
+            uploaded.record(self.up)
+        comp.wait_event(uploaded)
+        o.graph.replay()
+        o.step_count += self.iters
+        computed = torch.cuda.Event()
+        computed.record(comp)
+        with torch.cuda.stream(self.down):
+            self.down.wait_event(computed)
+            for h, t in zip(self.host_maps[j], o.tex):
+                h.copy_(t, non_blocking=True)
+            self.host_loss[j].copy_(o.loss_hist, non_blocking=True)
+            ev = torch.cuda.Event()
+            ev.record(self.down)
+        self.done[j] = ev
+        self.next_ticket += 1
+        return self.next_ticket - 1
+
+    def result(self, ticket: int):
+        if not (self.next_ticket - 2 <= ticket < self.next_ticket):
+            raise ValueError(f"ticket {ticket} is no longer (or not yet) held; the pipeline keeps two")
+        j = ticket % 2
+        self.done[j].synchronize()
+        return self.host_maps[j], self.host_loss[j]
+
+    def device_error(self) -> int:
+        return max(o.device_error() for o in self.bufs)
+
+
 def _time_config(opt: BatchedOptim, cfg: BatchConfig, iters: int = 3) -> float:
     tex = [t.clone() for t in opt.tex]
     m1 = [torch.zeros_like(t) for t in tex]

@@ -110,3 +110,36 @@ def test_autotune_picks_a_valid_config(svb, cuda, tmp_path, monkeypatch):
     assert len(b.tune_results if hasattr(b, "tune_results") else [1]) >= 1
     b.step()
     assert torch.isfinite(b.loss_out).all()
+
+
+def test_pipeline_matches_sequential_batches(svb, cuda):
+    """BatchedPipeline (two buffers, copies on side streams) gives each batch exactly the
+    maps and losses that a sequential reset + run of BatchedOptim gives it."""
+    mats = _batch(svb, cuda, n=4, general=False)
+    cfg = svb.BatchConfig(threads=480, tile_texels=960, ctas=0, variant=2)
+    g = torch.Generator().manual_seed(5)
+    batches = []
+    for _ in range(3):
+        inits = [(m.init + 0.05 * torch.randn(m.init.shape, generator=g)).clamp(-1, 1).pin_memory() for m in mats]
+        tgts = [(m.targets * (1.0 + 0.1 * torch.rand(1, generator=g))).pin_memory() for m in mats]
+        batches.append((inits, tgts))
+    def copy(res):
+        return [m.clone() for m in res[0]], res[1].clone()
+
+    pipe = svb.BatchedPipeline(mats, iters=6, lr=0.01, loss="log1p", device=cuda, config=cfg)
+    t0 = pipe.submit(*batches[0])
+    t1 = pipe.submit(*batches[1])
+    got = [copy(pipe.result(t0))]
+    t2 = pipe.submit(*batches[2])  # reuses batch 0's buffer
+    got += [copy(pipe.result(t1)), copy(pipe.result(t2))]
+    assert pipe.device_error() == 0
+    ref = svb.BatchedOptim(mats, lr=0.01, loss="log1p", device=cuda, config=cfg, hist_len=6)
+    for (inits, tgts), (maps, losses) in zip(batches, got):
+        ref.reset(inits=inits, targets=tgts)
+        ref.run(6)
+        torch.cuda.synchronize()
+        for a, b in zip(maps, ref.tex):
+            assert torch.equal(a, b.cpu())
+        assert torch.equal(losses, ref.loss_hist.cpu())
+    with pytest.raises(ValueError):
+        pipe.result(t0)  # its buffer has been reused

@@ -73,6 +73,11 @@ def dist_env():
     return rank, world, local
 
 
+def material_cost(res, views):
+    """Cost model of one material per iteration, as the planner's: texels x (views + 5)."""
+    return res * res * (views + 5)
+
+
 def shard(costs, world):
     """Greedy (largest first) assignment of materials to ranks; returns a list per rank."""
     order = sorted(range(len(costs)), key=lambda i: -costs[i])
@@ -395,7 +400,7 @@ def impl_ours(args):
 
         dist.init_process_group("nccl", device_id=dev)
     specs = workload_specs(args.materials)
-    costs = [r * r * (v + 3) for r, v in specs]
+    costs = [material_cost(r, v) for r, v in specs]
     mine = shard(costs, world)[rank]
     all_sc = PKG.scenes.batched_scenes(n=args.materials, device=dev, render_fn=None)
     mats = []

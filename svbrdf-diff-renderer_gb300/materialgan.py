@@ -61,20 +61,51 @@ def _fir_kernel(device=None, dtype=torch.float32):
     return k2 / k2.sum()
 
 
+_FIR_CACHE = {}
+
+
+def _fir_depthwise(device, dtype, c):
+    """The [c, 1, 4, 4] depthwise FIR weight, built once per (device, dtype, c): a capture
+    of the generator in a CUDA graph cannot copy a new constant to the device."""
+    key = (str(device), dtype, c)
+    if key not in _FIR_CACHE:
+        _FIR_CACHE[key] = _fir_kernel(device, dtype).view(1, 1, 4, 4).repeat(c, 1, 1, 1)
+    return _FIR_CACHE[key]
+
+
 def _blur(x, pad):
     """Depthwise [1,3,3,1] x [1,3,3,1] FIR with (pad0, pad1) padding on both axes."""
     c = x.shape[1]
-    k = _fir_kernel(x.device, x.dtype).view(1, 1, 4, 4).repeat(c, 1, 1, 1)
+    k = _fir_depthwise(x.device, x.dtype, c)
     x = Fn.pad(x, (pad[0], pad[1], pad[0], pad[1]))
     return Fn.conv2d(x, k, groups=c)
 
 
-def _upsample2(x):
-    """2x up-sampling: zero insertion + FIR (gain 4 keeps the mean)."""
+def _upsample2_fir(x):
+    """2x up-sampling as written: zero insertion, then the FIR (gain 4 keeps the mean)."""
     b, c, h, w = x.shape
     up = torch.zeros(b, c, h * 2, w * 2, device=x.device, dtype=x.dtype)
     up[:, :, ::2, ::2] = x * 4.0
     return _blur(up, (2, 1))
+
+
+def _up1d(x, dim):
+    """One axis of _upsample2_fir in polyphase form: out[2m] = (x[m-1] + 3 x[m]) / 4 and
+    out[2m+1] = (3 x[m] + x[m+1]) / 4, with x zero outside (the FIR's zero padding)."""
+    n = x.shape[dim]
+    xp = Fn.pad(x, (1, 1) if dim == -1 else (0, 0, 1, 1))
+    lo, mid, hi = xp.narrow(dim, 0, n), xp.narrow(dim, 1, n), xp.narrow(dim, 2, n)
+    even = 0.25 * lo + 0.75 * mid
+    odd = 0.75 * mid + 0.25 * hi
+    if dim == -1:
+        return torch.stack((even, odd), dim=-1).flatten(-2, -1)
+    return torch.stack((even, odd), dim=-2).flatten(-3, -2)
+
+
+def _upsample2(x):
+    """2x up-sampling (zero insertion + [1,3,3,1] FIR, gain 4), computed separably in
+    polyphase form: the same function as _upsample2_fir without multiplying the zeros."""
+    return _up1d(_up1d(x, -1), -2)
 
 
 class _ModConv(torch.nn.Module):
@@ -88,18 +119,24 @@ class _ModConv(torch.nn.Module):
         self.demod, self.up, self.k = demod, up, k
 
     def forward(self, x, w):
-        b, cin, h, wd = x.shape
+        # The modulated weight scale w_oi s_bi d_bo factors out of the convolution: scale the
+        # input channels by the style, convolve with the shared weight, scale the output
+        # channels by the demodulation d_bo = rsqrt(sum_i,taps (scale w_oi s_bi)^2 + 1e-8).
+        # This is the same function as convolving with per-sample weights (StyleGAN2's fused
+        # form), but it runs as one batched convolution. With the generator frozen, its
+        # backward is a data gradient plus small reductions, with no per-sample weight
+        # gradients.
         s = self.affine(w)  # [B, cin]
-        wt = self.weight[None] * self.scale * s[:, None, :, None, None]  # [B, cout, cin, k, k]
-        if self.demod:
-            wt = wt * torch.rsqrt(wt.pow(2).sum(dim=(2, 3, 4), keepdim=True) + 1e-8)
-        cout = wt.shape[1]
+        wsc = self.weight * self.scale
+        x = x * s[:, :, None, None]
         if self.up:
-            x = _upsample2(x)
-            h, wd = h * 2, wd * 2
-        xg = x.reshape(1, b * cin, h, wd)
-        y = Fn.conv2d(xg, wt.reshape(b * cout, cin, self.k, self.k), padding=self.k // 2, groups=b)
-        return y.reshape(b, cout, h, wd)
+            x = _upsample2(x)  # per-channel linear: commutes with the channel scaling
+        y = Fn.conv2d(x, wsc, padding=self.k // 2)
+        if self.demod:
+            w2 = wsc.pow(2).sum(dim=(2, 3))  # [cout, cin]
+            d = torch.rsqrt(s.pow(2) @ w2.t() + 1e-8)  # [B, cout]
+            y = y * d[:, :, None, None]
+        return y
 
 
 class _StyleLayer(torch.nn.Module):
@@ -208,6 +245,7 @@ class MaterialGANOptim:
         self.descriptor = descriptor
         self.descriptor_weight = descriptor_weight
         self.loss_image_list, self.loss_feature_list = [], []
+        self._graphs = {}
 
     def init_from(self, latent: Optional[torch.Tensor] = None, batch: int = 1, seed: int = 0, noise: str = "zero"):
         """W+ from a given latent, else the truncated mapping of seeded z (src/materialgan.py:58-75)."""
@@ -220,20 +258,75 @@ class MaterialGANOptim:
         self.latent = latent.detach().to(self.device, torch.float32).clone().requires_grad_(True)
         self.noises = [n.requires_grad_(True) for n in
                        self.net.make_noises(noise, self.latent.shape[0], self.device, seed)]
+        self._graphs = {}  # captured epochs hold the previous parameters' addresses
 
     def load_targets(self, targets: torch.Tensor):
         """targets [B*V, 3, H, W] (materials major)."""
         self.targets = targets.to(self.device, torch.float32).contiguous()
+        self._graphs = {}
         if self.descriptor is not None:
             self.descriptor.load(self.targets)
 
     def latent_to_textures(self, latent=None):
         return latent_to_textures(self.net, self.latent if latent is None else latent, self.noises)
 
-    def optim(self, epochs, lr, svbrdf_obj=None, optim_light=False, reset_adam_each_iter=True):
-        """``epochs = [total, l, n]``: alternate l latent epochs and n noise epochs."""
+    # ---- one epoch as a CUDA graph -------------------------------------------------------
+    # An epoch is a few hundred small kernels (the generator's layers, forward and backward),
+    # so launching them one by one costs more host time than they take on the GPU. With the
+    # reference's fresh Adam every epoch (src/materialgan.py:119-129), an epoch is a fixed
+    # function of the parameters and replays as one graph: forward, backward and a
+    # capturable torch Adam whose state is zeroed inside the graph, which is what a new
+    # Adam's first step computes.
+    def _epoch(self, params):
+        for p in (self.latent, *self.noises):
+            p.grad = None
+        rendered = self.renderer_obj.eval(self.latent_to_textures())
+        loss = torch.nn.functional.mse_loss(rendered, self.targets)
+        loss.backward()
+        return loss
+
+    def _graph_for(self, phase_latent: bool, lr: float):
+        key = (phase_latent, float(lr))
+        if key in self._graphs:
+            return self._graphs[key]
+        params = [self.latent] if phase_latent else self.noises
+        opt = torch.optim.Adam(params, lr=lr, betas=(0.9, 0.999), capturable=True)
+        for p in params:
+            opt.state[p] = {"step": torch.zeros((), dtype=torch.float32, device=self.device),
+                            "exp_avg": torch.zeros_like(p), "exp_avg_sq": torch.zeros_like(p)}
+        side = torch.cuda.Stream(self.device)
+        side.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(side):  # warm autograd and the allocator; the parameters stay as they are
+            for _ in range(2):
+                self._epoch(params)
+        torch.cuda.current_stream(self.device).wait_stream(side)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            loss = self._epoch(params)
+            for st in opt.state.values():
+                st["step"].zero_()
+                st["exp_avg"].zero_()
+                st["exp_avg_sq"].zero_()
+            opt.step()
+        self._graphs[key] = (graph, loss, opt)
+        return self._graphs[key]
+
+    def optim(self, epochs, lr, svbrdf_obj=None, optim_light=False, reset_adam_each_iter=True, graph=True):
+        """``epochs = [total, l, n]``: alternate l latent epochs and n noise epochs. With
+        ``graph`` (and the reference's fresh Adam each epoch, no descriptor term) each epoch
+        is one CUDA-graph replay."""
         total, l_ep, n_ep = epochs
         cycle = l_ep + n_ep
+        if graph and reset_adam_each_iter and self.descriptor is None and self.device.type == "cuda":
+            for epoch in range(total):
+                g, loss, _ = self._graph_for((epoch % cycle) < l_ep, lr)
+                g.replay()
+                self.loss_image_list.append(loss.detach().clone())
+            for p in (self.latent, *self.noises):
+                p.grad = None
+            self.textures = self.latent_to_textures().detach()
+            self.loss_image_list = [float(x) for x in torch.stack(self.loss_image_list).tolist()]
+            return self.textures
         opt = None
         for epoch in range(total):
             phase_latent = (epoch % cycle) < l_ep

@@ -2,6 +2,8 @@
 import pytest
 import torch
 
+from conftest import rel_l2
+
 
 def _small_gen(svb, res=32, seed=0):
     return svb.materialgan.StyleGAN2Generator(resolution=res, w_dim=64, fmap_base=512, fmap_max=64, seed=seed,
@@ -66,6 +68,43 @@ def test_latent_loop_through_gpu_renderer(svb, cuda):
 
 
 @pytest.mark.gpu
+def test_latent_graph_matches_eager(svb, cuda):
+    """The CUDA-graph epochs follow the eager loop (fresh torch Adam each epoch).
+
+    A fresh Adam's step is lr g / (|g| + eps): every element moves by about lr whatever its
+    gradient's size, so rounding-level differences in near-zero gradients flip steps and the
+    two trajectories part after a step or two. The first loss (no step yet) and the second
+    (one step) agree to rounding. After that, both runs only have to descend alike. TF32 is
+    off for both runs, since the convolution algorithms picked under capture and eagerly
+    may round differently."""
+    from oracle import microfacet_ref as R
+
+    tf32 = torch.backends.cudnn.allow_tf32, torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cudnn.allow_tf32 = torch.backends.cuda.matmul.allow_tf32 = False
+
+    gen = svb.materialgan.StyleGAN2Generator(resolution=256, fmap_max=64, seed=0)
+    sc = svb.scenes.single_scene(res=256, seed=1012)
+    tg = torch.cat([R.render(svb.scenes.make_material(256, 1012 + i), sc.camera_pos, sc.light_pos, sc.light_pow,
+                             sc.size, torch.float32) for i in range(2)])
+    r = svb.Microfacet(256, 9, sc.size, [t.to(cuda) for t in sc.cl], cuda)
+    runs = []
+    for graph in (False, True):
+        o = svb.materialgan.MaterialGANOptim(cuda, r, gen)
+        o.load_targets(tg.to(cuda))
+        o.init_from(batch=2, seed=6)
+        tex = o.optim([9, 3, 2], 0.02, graph=graph)
+        runs.append((tex.clone(), list(o.loss_image_list), o.latent.detach().clone()))
+    torch.backends.cudnn.allow_tf32, torch.backends.cuda.matmul.allow_tf32 = tf32
+    (t0, l0, w0), (t1, l1, w1) = runs
+    assert len(l1) == 9
+    assert abs(l1[0] - l0[0]) <= 1e-6 * l0[0]
+    assert abs(l1[1] - l0[1]) <= 1e-5 * l0[1]
+    assert l0[-1] < 0.7 * l0[0] and l1[-1] < 0.7 * l1[0]
+    assert abs(l1[-1] - l0[-1]) <= 0.15 * l0[-1]
+    assert torch.isfinite(t1).all() and t1.shape == t0.shape
+
+
+@pytest.mark.gpu
 def test_refinement_handoff(svb, cuda):
     """Generator maps at 256 -> Lanczos 512 -> batched fused per-pixel refinement."""
     from oracle import microfacet_ref as R
@@ -78,3 +117,27 @@ def test_refinement_handoff(svb, cuda):
     b.run(20)
     losses = b.loss_hist[:20, 0].tolist()
     assert losses[-1] < losses[0]
+
+
+def test_upsample_polyphase_matches_fir(svb):
+    """The separable polyphase 2x up-sampling equals zero insertion + the 4x4 FIR."""
+    MG = svb.materialgan
+    x = torch.randn(2, 5, 7, 9, dtype=torch.float64, generator=torch.Generator().manual_seed(3))
+    assert torch.allclose(MG._upsample2(x), MG._upsample2_fir(x), rtol=0, atol=1e-14)
+
+
+def test_unfused_modulated_conv_matches_per_sample_weights(svb):
+    """Input scaling + shared-weight conv + output demodulation equals the convolution with
+    per-sample modulated, demodulated weights."""
+    import math
+
+    MG = svb.materialgan
+    g = torch.Generator().manual_seed(4)
+    conv = MG._ModConv(8, 6, 3, 16, g).double()
+    x = torch.randn(3, 8, 10, 10, dtype=torch.float64, generator=g)
+    w = torch.randn(3, 16, dtype=torch.float64, generator=g)
+    s = conv.affine(w)
+    wt = conv.weight[None] * conv.scale * s[:, None, :, None, None]
+    wt = wt * torch.rsqrt(wt.pow(2).sum(dim=(2, 3, 4), keepdim=True) + 1e-8)
+    ref = torch.nn.functional.conv2d(x.reshape(1, 24, 10, 10), wt.reshape(18, 8, 3, 3), padding=1, groups=3)
+    assert torch.allclose(conv(x, w), ref.reshape(3, 6, 10, 10), rtol=1e-12, atol=1e-12)

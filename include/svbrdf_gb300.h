@@ -234,6 +234,18 @@ int svbrdf_desc_pool_bwd(const void* gy, const void* x, const void* addend, void
 int svbrdf_desc_feat_loss(const void* f, int f_is_bf16, const float* t, const float* gram_grad, float coef, int mask,
                           void* g, float* partial, long long n, void* stream);
 
+/* ---- MaterialGAN generator: 2x up-sampling of its feature maps and skip images (the
+ * reference's generator, src/higan_models/*, up-samples by zero insertion and a [1,3,3,1]
+ * FIR; src/materialgan.py:91-173 runs it in the latent loop) ---- */
+
+/* y [planes][2h][2w] = zero insertion of x [planes][h][w], then the separable [1,3,3,1]^2 / 64
+ * FIR with gain 4 and zero padding: along each axis out[2m] = (x[m-1] + 3 x[m]) / 4 and
+ * out[2m+1] = (3 x[m] + x[m+1]) / 4. FP32, contiguous planes. */
+int svbrdf_gen_upsample2(const float* x, float* y, long long planes, int h, int w, void* stream);
+
+/* The adjoint of svbrdf_gen_upsample2: gx [planes][h][w] from g [planes][2h][2w]. */
+int svbrdf_gen_upsample2_bwd(const float* g, float* gx, long long planes, int h, int w, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -20,7 +20,7 @@ CSRC = PKG / "csrc"
 INCLUDE = REPO / "include"
 LIBDIR = PKG / "_lib"
 LIBNAME = "libsvbrdf_gb300.so"
-SOURCES = ["render.cu", "fused.cu", "conv_tc.cu", "desc_ops.cu"]
+SOURCES = ["render.cu", "fused.cu", "conv_tc.cu", "desc_ops.cu", "gen_ops.cu"]
 HEADERS = ["svbrdf_math.cuh", "svbrdf_common.cuh", "svbrdf_plan.cuh"]
 WORKSPACE_ERROR_OFFSET = 4
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -136,6 +136,10 @@ def _declare(L):
     L.svbrdf_desc_pool_bwd.argtypes = [P, P, P, P, I, I, I, I, P]
     L.svbrdf_desc_feat_loss.restype = I
     L.svbrdf_desc_feat_loss.argtypes = [P, I, P, P, F, I, P, P, ctypes.c_longlong, P]
+    L.svbrdf_gen_upsample2.restype = I
+    L.svbrdf_gen_upsample2.argtypes = [P, P, ctypes.c_longlong, I, I, P]
+    L.svbrdf_gen_upsample2_bwd.restype = I
+    L.svbrdf_gen_upsample2_bwd.argtypes = [P, P, ctypes.c_longlong, I, I, P]
     L.svbrdf_batched_plan_bytes.restype = S
     L.svbrdf_batched_plan_bytes.argtypes = [ctypes.POINTER(svbrdf_material), I, ctypes.POINTER(svbrdf_batch_config)]
     L.svbrdf_batched_plan.restype = I
@@ -154,7 +158,8 @@ EXPORTS = [
     "svbrdf_batched_plan_bytes",
     "svbrdf_batched_plan", "svbrdf_batched_workspace_bytes", "svbrdf_batched_step", "svbrdf_conv3x3_bf16",
     "svbrdf_conv3x3_bf16_ex", "svbrdf_desc_partials", "svbrdf_desc_conv1_fwd", "svbrdf_desc_conv1_bwd",
-    "svbrdf_desc_pool_fwd", "svbrdf_desc_pool_bwd", "svbrdf_desc_feat_loss",
+    "svbrdf_desc_pool_fwd", "svbrdf_desc_pool_bwd", "svbrdf_desc_feat_loss", "svbrdf_gen_upsample2",
+    "svbrdf_gen_upsample2_bwd",
 ]
 
 

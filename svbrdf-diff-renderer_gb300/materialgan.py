@@ -102,9 +102,39 @@ def _up1d(x, dim):
     return torch.stack((even, odd), dim=-2).flatten(-3, -2)
 
 
+class _Upsample2Cuda(torch.autograd.Function):
+    """The polyphase 2x up-sampling as one kernel each way (svbrdf_gen_upsample2[_bwd])."""
+
+    @staticmethod
+    def forward(ctx, x):
+        from . import _native as N
+
+        L = N.lib()
+        x = x.contiguous()
+        b, c, h, w = x.shape
+        y = torch.empty(b, c, 2 * h, 2 * w, device=x.device, dtype=torch.float32)
+        N.check(L.svbrdf_gen_upsample2(x.data_ptr(), y.data_ptr(), b * c, h, w, N.stream_handle(x.device)))
+        ctx.hw = (b, c, h, w)
+        return y
+
+    @staticmethod
+    def backward(ctx, g):
+        from . import _native as N
+
+        L = N.lib()
+        b, c, h, w = ctx.hw
+        g = g.contiguous()
+        gx = torch.empty(b, c, h, w, device=g.device, dtype=torch.float32)
+        N.check(L.svbrdf_gen_upsample2_bwd(g.data_ptr(), gx.data_ptr(), b * c, h, w, N.stream_handle(g.device)))
+        return gx
+
+
 def _upsample2(x):
     """2x up-sampling (zero insertion + [1,3,3,1] FIR, gain 4), computed separably in
-    polyphase form: the same function as _upsample2_fir without multiplying the zeros."""
+    polyphase form: the same function as _upsample2_fir without multiplying the zeros. On the
+    GPU (FP32) it is one kernel each way; the torch form serves CPU tensors."""
+    if x.is_cuda and x.dtype == torch.float32:
+        return _Upsample2Cuda.apply(x)
     return _up1d(_up1d(x, -1), -2)
 
 

@@ -141,3 +141,20 @@ def test_unfused_modulated_conv_matches_per_sample_weights(svb):
     wt = wt * torch.rsqrt(wt.pow(2).sum(dim=(2, 3, 4), keepdim=True) + 1e-8)
     ref = torch.nn.functional.conv2d(x.reshape(1, 24, 10, 10), wt.reshape(18, 8, 3, 3), padding=1, groups=3)
     assert torch.allclose(conv(x, w), ref.reshape(3, 6, 10, 10), rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.gpu
+def test_upsample_kernel_matches_fir(svb, cuda):
+    """The CUDA up-sampling and its adjoint against the FIR form (FP64 on the CPU)."""
+    MG = svb.materialgan
+    g = torch.Generator().manual_seed(7)
+    x = torch.randn(2, 5, 7, 9, generator=g)
+    ref = MG._upsample2_fir(x.double())
+    xc = x.to(cuda).requires_grad_(True)
+    y = MG._upsample2(xc)
+    assert torch.allclose(y.double().cpu(), ref, rtol=0, atol=1e-5)
+    go = torch.randn(2, 5, 14, 18, generator=g)
+    y.backward(go.to(cuda))
+    xr = x.double().requires_grad_(True)
+    MG._upsample2_fir(xr).backward(go.double())
+    assert torch.allclose(xc.grad.double().cpu(), xr.grad, rtol=0, atol=1e-5)

@@ -47,7 +47,7 @@ import torch  # noqa: E402
 PKG = importlib.import_module("svbrdf-diff-renderer_gb300")
 METRIC = "texel*view render+adjoint+Adam updates/s, fused batched vs plain, 1 GB300"
 UNIT = "texel*view updates/s"
-KERNEL_NAMES = {0: "batched_step_kernel", 1: "batched_tma_kernel", 2: "batched_pair_kernel"}
+KERNEL_NAMES = {0: "batched_step_kernel", 1: "batched_tma_kernel", 2: "batched_pair_kernel", 3: "batched_fuse_kernel"}
 WORKLOAD = "batched 64 materials, res {256,512,1024}, V 5-16, 100 iterations per graph replay, log1p L2, Adam lr 0.01"
 
 
@@ -453,20 +453,26 @@ def impl_ours(args):
     else:
         tv_all = float(tv)
     value = tv_all * args.iters * args.steps / (ms / 1e3)
-    launch_ms = ms / (args.steps * args.iters)
+    launches_per_run = opt.launches(args.iters)
+    iters_per_launch = args.iters / launches_per_run
+    launch_ms = ms / (args.steps * launches_per_run)
     peak, peak_kind = peaks()
-    achieved = abytes / (launch_ms / 1e3) / 1e9
+    # algorithmic bytes of one launch: the per-texel-iteration figure x the iterations it runs
+    launch_abytes = abytes * iters_per_launch
+    achieved = launch_abytes / (launch_ms / 1e3) / 1e9
     # DRAM bytes per launch: an ncu capture of a smaller case of the same kernel, scaled to
     # this launch by the algorithmic bytes (traffic is proportional to texels x views)
     traffic = None
     cfg_used = opt.config
     n_ctas = opt.n_ctas()
-    tune = [list(r) for r in getattr(opt, "tune_results", [])[:6]]
+    tune = [list(r) for r in getattr(opt, "tune_results", [])[:8]]
     kernel = KERNEL_NAMES[cfg_used.variant]
     tfile = HERE / "profiles" / f"{kernel}_traffic.json"
     if tfile.exists():
         try:
-            traffic = float(json.loads(tfile.read_text())["dram_bytes_per_algorithmic_byte"]) * abytes
+            tj = json.loads(tfile.read_text())
+            # a resident-state launch moves its state and targets once, whatever its iterations
+            traffic = float(tj["dram_bytes_per_algorithmic_byte"]) * (abytes if tj.get("per_launch_pass") else launch_abytes)
         except Exception:
             traffic = None
 
@@ -528,6 +534,32 @@ def impl_ours(args):
     del pipe
     torch.cuda.empty_cache()
 
+    # the one-launch-per-iteration kernel (variant 2) on the same materials: the HBM-bound
+    # form, for which the per-iteration algorithmic bytes are the real DRAM traffic
+    per_iter = None
+    if cfg_used.variant == 3:
+        pairs = [r for r in tune if r[1] == 2]
+        pc = PKG.BatchConfig(pairs[0][2], pairs[0][2] * pairs[0][3], 0, 2) if pairs else PKG.BatchConfig(480, 960, 0, 2)
+        o2 = PKG.BatchedOptim(mats, lr=0.01, loss="log1p", device=dev, hist_len=args.iters, config=pc)
+        o2.capture(args.iters)
+        for _ in range(args.warmup):
+            o2.run(args.iters)
+        torch.cuda.synchronize()
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record(stream)
+        for _ in range(args.steps):
+            o2.run(args.iters)
+        a1.record(stream)
+        torch.cuda.synchronize()
+        ms2 = a0.elapsed_time(a1)
+        l2ms = ms2 / (args.steps * args.iters)
+        ach2 = abytes / (l2ms / 1e3) / 1e9
+        per_iter = {"kernel": KERNEL_NAMES[2], "batch_config": pc.__dict__,
+                    "value": float(tv) * args.iters * args.steps / (ms2 / 1e3), "launch_ms": l2ms,
+                    "achieved_gbs": ach2, "frac": ach2 / peak, "device_error": o2.device_error()}
+        del o2
+        torch.cuda.empty_cache()
+
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded materials and flash views)",
@@ -538,12 +570,14 @@ def impl_ours(args):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                          "kernel": kernel,
-                         "algorithmic_bytes_per_launch": abytes,
+                         "algorithmic_bytes_per_launch": launch_abytes,
+                         "iterations_per_launch": iters_per_launch,
                          "launch_ms": launch_ms},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "mode": "BatchedPipeline: two buffers, uploads and downloads on copy streams overlap the compute",
                     "sequential_value": seq_value, "device_error": pipe_err},
-            "gpu_launches": args.steps * args.iters,
+            "per_iteration_kernel": per_iter,
+            "gpu_launches": args.steps * launches_per_run,
             "clocks": clocks}
     if rank == 0 and not args.no_extras:
         line["plain"] = time_single(dev, fused=False, iters=20)

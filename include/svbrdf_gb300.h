@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define SVBRDF_ABI_VERSION 2
+#define SVBRDF_ABI_VERSION 3
 
 enum {
   SVBRDF_OK = 0,
@@ -140,6 +140,11 @@ typedef struct svbrdf_material {
  * variant 2 (the variant 1 pipeline with two adjacent texels per consumer thread, every
  *   per-texel stage in FP32x2): threads 224, 256, 384 or 480, tile_texels == 2 * threads,
  *   the material requirements of variant 1. threads 224 runs two CTAs per SM.
+ * variant 3 (resident state: the variant 2 arithmetic, but a launch runs up to 32
+ *   iterations on each tile, keeping the tile's parameters and Adam moments in shared
+ *   memory between them, so HBM carries them once per launch; only the targets stream per
+ *   iteration, from L2 after the first): threads 224, 256, 384 or 480, tile_texels ==
+ *   2 * threads, the material requirements of variant 1. Use svbrdf_batched_steps.
  * ctas: persistent CTAs (0 = SM count x resident CTAs per SM). */
 typedef struct svbrdf_batch_config {
   int threads;
@@ -174,6 +179,13 @@ size_t svbrdf_batched_workspace_bytes(const void* host_plan);
 int svbrdf_batched_step(const void* device_plan, const void* host_plan, int loss_kind, int* step_counter,
                         float lr, float beta1, float beta2, float eps, float* loss_hist, int hist_len,
                         void* workspace, size_t workspace_bytes, void* stream);
+/* `iters` iterations of svbrdf_batched_step (the whole `for epoch in range(epochs)` loop of
+ * src/svbrdf.py:56-71 for every material). Variants 0-2 launch once per iteration; variant 3
+ * runs ceil(iters / 32) launches of up to 32 iterations each. The parameters, moments, step
+ * counter and loss history afterwards equal those of `iters` svbrdf_batched_step calls. */
+int svbrdf_batched_steps(const void* device_plan, const void* host_plan, int loss_kind, int* step_counter,
+                         float lr, float beta1, float beta2, float eps, float* loss_hist, int hist_len, int iters,
+                         void* workspace, size_t workspace_bytes, void* stream);
 
 /* ---- descriptor loss: BF16 3x3 convolutions on the tensor cores ---- */
 
@@ -243,8 +255,35 @@ int svbrdf_desc_feat_loss(const void* f, int f_is_bf16, const float* t, const fl
  * out[2m+1] = (3 x[m] + x[m+1]) / 4. FP32, contiguous planes. */
 int svbrdf_gen_upsample2(const float* x, float* y, long long planes, int h, int w, void* stream);
 
+/* svbrdf_gen_upsample2 of x[p] s[p] (a modulated up-sampling conv's input scaling, which
+ * commutes with the up-sampling), s nullable. Needs w % 4 == 0 and 16-byte aligned x, y. */
+int svbrdf_gen_upsample2_scaled(const float* x, const float* s, float* y, long long planes, int h, int w,
+                                void* stream);
+
 /* The adjoint of svbrdf_gen_upsample2: gx [planes][h][w] from g [planes][2h][2w]. */
 int svbrdf_gen_upsample2_bwd(const float* g, float* gx, long long planes, int h, int w, void* stream);
+
+/* ---- MaterialGAN generator: a style layer's elementwise work around its modulated conv (the
+ * reference's StyleGAN2 layer in src/higan_models/*: input channels scaled by the style, output
+ * channels by the demodulation, then per-layer noise, bias and leaky ReLU x sqrt 2) ---- */
+
+/* y[p][i] = x[p][i] s[p] over planes p = b C + c (planes <= 65535), hw elements per plane. */
+int svbrdf_gen_scale(const float* x, const float* s, float* y, long long planes, int hw, void* stream);
+
+/* Adjoint of svbrdf_gen_scale: gx = g s[p] and gs[p] = sum_i g[p][i] x[p][i] (fixed order). */
+int svbrdf_gen_scale_bwd(const float* g, const float* x, const float* s, float* gx, float* gs, long long planes,
+                         int hw, void* stream);
+
+/* out[b][c][i] = lrelu(y[b][c][i] d[b][c] + ns noise[b][i] + bias[c], 0.2) gain. d nullable
+ * (taken as 1), noise nullable (no noise term); ns points at the device scalar noise strength. */
+int svbrdf_gen_act(const float* y, const float* d, const float* noise, const float* ns, const float* bias, float gain,
+                   float* out, int b, int c, int hw, void* stream);
+
+/* Adjoint of svbrdf_gen_act with respect to y, d and noise: gy = gpre d, gd[b][c] = sum_i gpre y
+ * (gd nullable), gnoise[b][i] = ns sum_c gpre (gnoise nullable), gpre = gout gain slope. */
+int svbrdf_gen_act_bwd(const float* gout, const float* y, const float* d, const float* noise, const float* ns,
+                       const float* bias, float gain, float* gy, float* gd, float* gnoise, int b, int c, int hw,
+                       void* stream);
 
 #ifdef __cplusplus
 }

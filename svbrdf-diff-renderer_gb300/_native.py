@@ -138,8 +138,18 @@ def _declare(L):
     L.svbrdf_desc_feat_loss.argtypes = [P, I, P, P, F, I, P, P, ctypes.c_longlong, P]
     L.svbrdf_gen_upsample2.restype = I
     L.svbrdf_gen_upsample2.argtypes = [P, P, ctypes.c_longlong, I, I, P]
+    L.svbrdf_gen_upsample2_scaled.restype = I
+    L.svbrdf_gen_upsample2_scaled.argtypes = [P, P, P, ctypes.c_longlong, I, I, P]
     L.svbrdf_gen_upsample2_bwd.restype = I
     L.svbrdf_gen_upsample2_bwd.argtypes = [P, P, ctypes.c_longlong, I, I, P]
+    L.svbrdf_gen_scale.restype = I
+    L.svbrdf_gen_scale.argtypes = [P, P, P, ctypes.c_longlong, I, P]
+    L.svbrdf_gen_scale_bwd.restype = I
+    L.svbrdf_gen_scale_bwd.argtypes = [P, P, P, P, P, ctypes.c_longlong, I, P]
+    L.svbrdf_gen_act.restype = I
+    L.svbrdf_gen_act.argtypes = [P, P, P, P, P, F, P, I, I, I, P]
+    L.svbrdf_gen_act_bwd.restype = I
+    L.svbrdf_gen_act_bwd.argtypes = [P, P, P, P, P, P, F, P, P, P, I, I, I, P]
     L.svbrdf_batched_plan_bytes.restype = S
     L.svbrdf_batched_plan_bytes.argtypes = [ctypes.POINTER(svbrdf_material), I, ctypes.POINTER(svbrdf_batch_config)]
     L.svbrdf_batched_plan.restype = I
@@ -148,6 +158,8 @@ def _declare(L):
     L.svbrdf_batched_workspace_bytes.argtypes = [P]
     L.svbrdf_batched_step.restype = I
     L.svbrdf_batched_step.argtypes = [P, P, I, P, F, F, F, F, P, I, P, S, P]
+    L.svbrdf_batched_steps.restype = I
+    L.svbrdf_batched_steps.argtypes = [P, P, I, P, F, F, F, F, P, I, I, P, S, P]
     return L
 
 
@@ -156,10 +168,10 @@ EXPORTS = [
     "svbrdf_last_error", "svbrdf_abi_version", "svbrdf_max_views", "svbrdf_workspace_bytes",
     "svbrdf_render_fwd", "svbrdf_render_bwd", "svbrdf_fused_step", "svbrdf_fused_step_noalloc",
     "svbrdf_batched_plan_bytes",
-    "svbrdf_batched_plan", "svbrdf_batched_workspace_bytes", "svbrdf_batched_step", "svbrdf_conv3x3_bf16",
+    "svbrdf_batched_plan", "svbrdf_batched_workspace_bytes", "svbrdf_batched_step", "svbrdf_batched_steps", "svbrdf_conv3x3_bf16",
     "svbrdf_conv3x3_bf16_ex", "svbrdf_desc_partials", "svbrdf_desc_conv1_fwd", "svbrdf_desc_conv1_bwd",
     "svbrdf_desc_pool_fwd", "svbrdf_desc_pool_bwd", "svbrdf_desc_feat_loss", "svbrdf_gen_upsample2",
-    "svbrdf_gen_upsample2_bwd",
+    "svbrdf_gen_upsample2_bwd", "svbrdf_gen_upsample2_scaled", "svbrdf_gen_scale", "svbrdf_gen_scale_bwd", "svbrdf_gen_act", "svbrdf_gen_act_bwd",
 ]
 
 

@@ -2,8 +2,9 @@
 
 Each material is what one ``SvbrdfOptim`` owns in the reference (src/svbrdf.py:15-83):
 textures, Adam moments, targets and its own views. ``BatchedOptim`` advances all of them
-with one persistent launch of ``svbrdf_batched_step`` per iteration (fused render, loss,
-adjoint and Adam), and ``run(iters)`` captures ``iters`` launches into one CUDA graph.
+with persistent launches of fused render, loss, adjoint and Adam (``svbrdf_batched_steps``):
+one launch per iteration, or, with the resident-state variant, one launch per up to 32
+iterations. ``run(iters)`` captures the launches of ``iters`` iterations into one CUDA graph.
 
 The launch shape (threads per CTA, texels per work tile, persistent CTA count) comes from
 ``autotune``: it times each candidate on the real workload for a few iterations, on copies
@@ -25,8 +26,10 @@ import torch
 from . import _native as N
 
 LOSS_KINDS = {"mse": 0, "log1p": 1, "log1p_pre": 2}
+FUSE_MAX = 32  # iterations per launch of the resident-state variant (kFuseMax in fused.cu)
 # (variant, threads, tile_texels / threads)
-CANDIDATES = ([(2, t, 2) for t in (224, 256, 384, 480)] +
+CANDIDATES = ([(3, t, 2) for t in (224, 256, 384, 480)] +
+              [(2, t, 2) for t in (224, 256, 384, 480)] +
               [(1, t, 1) for t in (256, 384, 480, 608)] +
               [(0, t, k) for t in (128, 256, 512) for k in (1, 4, 16)])
 CACHE_FILE = pathlib.Path(os.environ.get("SVBRDF_TUNE_CACHE", str(pathlib.Path.home() / ".cache" / "svbrdf_gb300_tune.json")))
@@ -37,7 +40,8 @@ class BatchConfig:
     threads: int = 256
     tile_texels: int = 1024
     ctas: int = 0     # 0 = SM count x resident CTAs per SM
-    variant: int = 0  # 0 direct loads, 1 bulk-copy (TMA) pipeline, 2 the pipeline on texel pairs
+    variant: int = 0  # 0 direct loads, 1 bulk-copy (TMA) pipeline, 2 the pipeline on texel pairs,
+    #                   3 texel pairs with the state resident across the iterations of a launch
 
     def as_c(self):
         return N.svbrdf_batch_config(self.threads, self.tile_texels, self.ctas, self.variant)
@@ -89,6 +93,10 @@ class BatchedOptim:
         """HBM bytes one iteration must move: params+m+v read and written, targets read."""
         return sum(H * W * (216 + 12 * V) for H, W, V, _ in self.meta)
 
+    def launches(self, iters: int) -> int:
+        """Kernel launches ``iters`` iterations take with this plan's variant."""
+        return -(-iters // FUSE_MAX) if self.config.variant == 3 else iters
+
     def signature(self) -> str:
         h = hashlib.sha1(json.dumps(sorted(self.meta)).encode()).hexdigest()[:16]
         return f"{torch.cuda.get_device_name(self.device)}|{self.loss}|{h}"
@@ -127,12 +135,12 @@ class BatchedOptim:
         return int(np.frombuffer(self.plan_host[:16].tobytes(), dtype=np.int32)[3])
 
     # ---- stepping ----
-    def _launch(self, plan_host, plan_dev, ws, step_dev, loss_hist):
+    def _launch(self, plan_host, plan_dev, ws, step_dev, loss_hist, iters: int = 1):
         b1, b2 = self.betas
-        N.check(self.L.svbrdf_batched_step(plan_dev.data_ptr(), plan_host.ctypes.data, self.kind,
-                                           step_dev.data_ptr(), self.lr, float(b1), float(b2), self.eps,
-                                           loss_hist.data_ptr(), int(loss_hist.shape[0]), ws.data_ptr(),
-                                           ws.numel(), N.stream_handle(self.device)))
+        N.check(self.L.svbrdf_batched_steps(plan_dev.data_ptr(), plan_host.ctypes.data, self.kind,
+                                            step_dev.data_ptr(), self.lr, float(b1), float(b2), self.eps,
+                                            loss_hist.data_ptr(), int(loss_hist.shape[0]), int(iters),
+                                            ws.data_ptr(), ws.numel(), N.stream_handle(self.device)))
 
     def step(self):
         """One iteration for every material (one eager launch). The step count is kept on
@@ -150,8 +158,7 @@ class BatchedOptim:
         material by ``iters`` Adam steps (the step counter is device-resident)."""
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g):
-            for _ in range(iters):
-                self._launch(self.plan_host, self.plan_dev, self.ws, self.step_dev, self.loss_hist)
+            self._launch(self.plan_host, self.plan_dev, self.ws, self.step_dev, self.loss_hist, iters)
         self.graph, self.graph_iters = g, iters
         return g
 
@@ -165,13 +172,24 @@ class BatchedOptim:
     def reset(self, inits=None, targets=None):
         """Restart the optimisation (step 0, zero moments), optionally from new initial maps
         and targets (host or device tensors; pinned host memory copies asynchronously)."""
+        self.upload(inits, targets)
+        self.prepare(targets is not None)
+
+    def upload(self, inits=None, targets=None):
+        """The copy half of ``reset``: new initial maps and raw targets into the device
+        buffers (copies only, no kernels, so it can run on a copy stream beside the compute)."""
         for i in range(self.n):
             if inits is not None:
                 self.tex[i].copy_(inits[i], non_blocking=True)
             if targets is not None:
                 self.tgt[i].copy_(targets[i], non_blocking=True)
-                if self.loss == "log1p":
-                    self.tgt[i].log1p_()
+
+    def prepare(self, new_targets: bool = True):
+        """The device half of ``reset``: transform freshly uploaded targets for the loss, zero
+        the moments, the step counter and the loss history."""
+        for i in range(self.n):
+            if new_targets and self.loss == "log1p":
+                self.tgt[i].log1p_()
             self.m1[i].zero_()
             self.m2[i].zero_()
         self.step_dev.zero_()
@@ -200,7 +218,8 @@ class BatchedPipeline:
     Every batch has the same materials layout as ``materials``: resolutions, view counts,
     cameras, lights and light power. Only the initial maps and targets change. While one
     buffer's batch is optimised, the next batch's maps and targets upload on a copy stream
-    and the previous batch's results download on another.
+    and the previous batch's results download on another; the short device-side preparation
+    of a batch (target transform, zeroed moments) runs on the compute stream.
 
     * ``submit(inits, targets)`` enqueues ``iters`` iterations of one batch and returns a
       ticket. The inputs are host tensors, pinned for asynchronous copies, one per material.
@@ -240,10 +259,13 @@ class BatchedPipeline:
         with torch.cuda.stream(self.up):
             if self.done[j] is not None:  # the buffer's previous batch has been read back
                 self.up.wait_event(self.done[j])
-            o.reset(inits=inits, targets=targets)
+            o.upload(inits=inits, targets=targets)  # copy engines only
             uploaded = torch.cuda.Event()
             uploaded.record(self.up)
         comp.wait_event(uploaded)
+        # the kernels of the reset run on the compute stream: on the copy stream they would
+        # wait for SMs that the persistent launches of the previous batch hold
+        o.prepare()
         o.graph.replay()
         o.step_count += self.iters
         computed = torch.cuda.Event()
@@ -270,18 +292,19 @@ class BatchedPipeline:
         return max(o.device_error() for o in self.bufs)
 
 
-def _time_config(opt: BatchedOptim, cfg: BatchConfig, iters: int = 3) -> float:
+def _time_config(opt: BatchedOptim, cfg: BatchConfig, iters: int = 8) -> float:
+    """Milliseconds per iteration of ``cfg``, timed over ``iters`` iterations in one call (so
+    the resident-state variant runs them in one launch, as a graph of a longer run does)."""
     tex = [t.clone() for t in opt.tex]
     m1 = [torch.zeros_like(t) for t in tex]
     m2 = [torch.zeros_like(t) for t in tex]
     host, dev, ws = opt._make_plan(cfg, tex, m1, m2)
     loss = torch.zeros(1, opt.n, device=opt.device)
     step = torch.zeros(1, device=opt.device, dtype=torch.int32)
-    opt._launch(host, dev, ws, step, loss)  # warm
+    opt._launch(host, dev, ws, step, loss, 2)  # warm
     s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     s.record()
-    for _ in range(iters):
-        opt._launch(host, dev, ws, step, loss)
+    opt._launch(host, dev, ws, step, loss, iters)
     e.record()
     e.synchronize()
     off = N.WORKSPACE_ERROR_OFFSET

@@ -219,11 +219,13 @@ __device__ __forceinline__ void texel_rc(int idx, const MatDesc& md, int& i, int
 
 // Last CTA of a batched launch: per-material mean loss from the fixed-order partial sums
 // (`per_tile` partials per tile), step counter store, completion counter reset.
+// A launch that ran `iters` iterations (steps step - iters + 1 .. step) holds iteration i's
+// partials at partial + i * n_tiles * per_tile and fills one loss_hist row per iteration.
 template <int NT>
 __device__ __forceinline__ void batched_finish(const char* plan, const PlanHeader* hdr, const MatDesc* mats,
                                                const float* partial, int per_tile, float* loss_hist, int hist_len,
                                                int step, int* step_counter, unsigned* counter, int* s_flag,
-                                               int nwarps) {
+                                               int nwarps, int iters = 1) {
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
@@ -234,16 +236,19 @@ __device__ __forceinline__ void batched_finish(const char* plan, const PlanHeade
   if (!*s_flag) return;
   __threadfence();
   const int* mat_tiles = (const int*)(plan + hdr->off_mat_tiles);
-  float* loss_out = loss_hist + (size_t)((step - 1) % hist_len) * hdr->n_mat;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  if (w < nwarps) {
-    for (int mi = w; mi < hdr->n_mat; mi += nwarps) {
-      double acc = 0.0;
-      const int e0 = mat_tiles[mi] * per_tile, e1 = mat_tiles[mi + 1] * per_tile;
-      for (int t = e0 + lane; t < e1; t += 32) acc += (double)__ldcg(partial + t);
+  for (int i = 0; i < iters; ++i) {
+    float* loss_out = loss_hist + (size_t)((step - iters + i) % hist_len) * hdr->n_mat;
+    const float* part = partial + (size_t)i * hdr->n_tiles * per_tile;
+    if (w < nwarps) {
+      for (int mi = w; mi < hdr->n_mat; mi += nwarps) {
+        double acc = 0.0;
+        const int e0 = mat_tiles[mi] * per_tile, e1 = mat_tiles[mi + 1] * per_tile;
+        for (int t = e0 + lane; t < e1; t += 32) acc += (double)__ldcg(part + t);
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-      if (lane == 0) loss_out[mi] = (float)(acc * mats[mi].inv_n);
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) loss_out[mi] = (float)(acc * mats[mi].inv_n);
+      }
     }
   }
   if (threadIdx.x == 0) {
@@ -1025,6 +1030,359 @@ batched_pair_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
                           ws + kWsCounter, &s_last, NCW);
 }
 
+// ============================================================== variant 3: resident state
+//
+// Texels are independent across the whole optimisation: a texel's gradient depends only on
+// its own parameters and targets, and Adam is elementwise. So one launch can run several
+// iterations on a tile before moving on, keeping the tile's parameters and both moments in
+// shared memory in between. Per tile the producer copies
+//   state = P, M, S (27 planes of TT floats) into a dedicated shared-memory area, then
+//   K times: Tc = targets of views 3c .. 3c+2 through the ring (as variant 2),
+// and the consumers run K iterations (render, adjoint, Adam) on the resident state, writing
+// parameters and moments back to global memory after the last. HBM then carries a tile's
+// state and targets once per launch instead of once per iteration; the targets of
+// iterations 2 .. K are L2 hits (a tile's targets are at most 16 x 3 x 4 x TT bytes, and
+// 152 CTAs keep well under L2 in flight). Per-iteration losses go to per-(iteration, tile,
+// warp) partials, so the loss history equals K separate launches'. The state area is
+// single-buffered: the producer reloads it once every consumer warp has signalled it done
+// with the tile (state_empty), after a proxy fence orders their shared-memory writes before
+// the bulk copies. Waits, error recording and draining follow variant 2.
+constexpr int kFuseMax = 32;
+constexpr int kStatePlanes = 27;
+constexpr size_t kFuseBudget = 220 * 1024;
+constexpr size_t kFuseBudgetTwoCta = 100 * 1024;
+
+// The tile the state area currently holds (written by the producer before it posts the
+// state's bytes, read by the consumers after the state barrier completes).
+struct __align__(16) FuseStateRec {
+  float* tex;
+  float* m1;
+  float* m2;
+  float* unused;
+  int tile, first, W, H;
+  int V, all_coloc, pad0, pad1;
+  float scale, size, inv_w, pad2;
+  float P[4];
+};
+
+// Pixel centres of consumer thread tid's texel pair (first + 2 tid, first + 2 tid + 1), as
+// variant 2 computes them.
+__device__ __forceinline__ void pair_coords(const FuseStateRec& r, int tid, float2& px, float2& py) {
+  const int W = r.W, idx = r.first + 2 * tid;
+  int i = (int)((float)idx * r.inv_w);
+  int j = idx - i * W;
+  if (j < 0) { --i; j += W; }
+  else if (j >= W) { ++i; j -= W; }
+  int i1 = i, j1 = j + 1;
+  if (j1 == W) { j1 = 0; ++i1; }
+  const float size = r.size, fw = (float)W, fh = (float)r.H;
+  px = make_float2(pixel_centre(j, fw, size), pixel_centre(j1, fw, size));
+  const float yi = -pixel_centre(i, fh, size);
+  py = make_float2(yi, i1 == i ? yi : -pixel_centre(i1, fh, size));
+}
+
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+template <int LOSS, int NCW, bool GEN>
+__global__ void __launch_bounds__((NCW + 1) * 32, NCW <= kPairTwoCtaNcw ? 2 : 1)
+batched_fuse_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restrict__ step_counter,
+                    float* __restrict__ loss_hist, int hist_len, int iters, float* __restrict__ warp_loss,
+                    unsigned* ws) {
+  constexpr int NT = NCW * 32;
+  constexpr int TT = 2 * NT;                  // texels per tile
+  constexpr int SLOT = kPairSlotPlanes * TT;  // floats per ring slot
+  constexpr int STATE = kStatePlanes * TT;    // floats of the state area
+  extern __shared__ __align__(128) float smem[];
+  float* state = smem;
+  float* ring = smem + STATE;
+  __shared__ __align__(8) uint64_t full_bar[kMaxRing];
+  __shared__ __align__(8) uint64_t empty_bar[kMaxRing];
+  __shared__ __align__(8) uint64_t state_full;
+  __shared__ __align__(8) uint64_t state_empty;
+  __shared__ FuseStateRec s_rec;
+  __shared__ MatDesc s_prod_md;
+  __shared__ View s_prod_views[kMaxViews];
+  __shared__ float s_prod_pow[4];
+  __shared__ AdamScalars s_adam[kFuseMax];
+  __shared__ int s_step;
+  __shared__ int s_last;
+
+  const PlanHeader* hdr = (const PlanHeader*)plan;
+  const MatDesc* mats = (const MatDesc*)(plan + hdr->off_mats);
+  const View* views = (const View*)(plan + hdr->off_views);
+  const int* cta_off = (const int*)(plan + hdr->off_cta);
+  const int R = hdr->ring_slots;
+  const int n_tiles = hdr->n_tiles;
+  PairSlotRec* recs = reinterpret_cast<PairSlotRec*>(ring + (size_t)R * SLOT);
+  int* err = (int*)(ws + kWsError);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  const int step0 = *step_counter;  // steps step0 + 1 .. step0 + iters
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < R; ++s) {
+      mbar_init(smem_u32(&full_bar[s]), 1);
+      mbar_init(smem_u32(&empty_bar[s]), NCW);
+    }
+    mbar_init(smem_u32(&state_full), 1);
+    mbar_init(smem_u32(&state_empty), NCW);
+    fence_mbar_init();
+    s_step = step0 + iters;
+  }
+  for (int i = threadIdx.x; i < iters; i += blockDim.x) s_adam[i] = device_adam(hyper, step0 + 1 + i);
+  __syncthreads();
+  const int k0 = cta_off[blockIdx.x], k1 = cta_off[blockIdx.x + 1];
+
+  if (warp == NCW) {
+    // ------------------------------------------------------------ producer (the whole warp)
+    const uint32_t ring_base = smem_u32(ring), state_base = smem_u32(state);
+    const uint32_t sfull = smem_u32(&state_full), sempty = smem_u32(&state_empty);
+    const int4* seq = (const int4*)(plan + hdr->off_seq);
+    int slot = 0;
+    uint32_t phase = 0, sphase = 0;
+    long long issued = 0, states = 0;
+    bool ok = true;
+    int4 sq_next = k0 < k1 ? seq[k0] : make_int4(0, 0, 0, 0);
+    int cur = -1;
+    for (int k = k0; k < k1 && ok; ++k) {
+      const int4 sq = sq_next;
+      if (k + 1 < k1) sq_next = seq[k + 1];
+      if (sq.y != cur) {
+        cur = sq.y;
+        __syncwarp();
+        const MatDesc& m = mats[cur];
+        if (lane == 0) s_prod_md = m;
+        if (lane < 3) s_prod_pow[lane] = m.lpow[lane];
+        for (int v = lane; v < m.V; v += 32) s_prod_views[v] = views[m.view_off + v];
+        __syncwarp();
+      }
+      const MatDesc& md = s_prod_md;
+      const int T = md.H * md.W, V = md.V;
+      const int first = sq.z;
+      const uint32_t bytes = (uint32_t)min(TT, T - first) * 4u;
+      const int nt = (V + kPairChunkViews - 1) / kPairChunkViews;
+      // the state area is free once every consumer warp is done with the previous tile
+      if (k > k0) {
+        ok = __all_sync(0xffffffffu, wait_phase(sempty, sphase, err, kDevTimeoutEmpty));
+        sphase ^= 1u;
+        if (!ok) break;
+      }
+      if (lane == 0) {
+        FuseStateRec& r = s_rec;
+        r.tex = md.tex; r.m1 = md.m1; r.m2 = md.m2;
+        r.tile = sq.x; r.first = first; r.W = md.W; r.H = md.H;
+        r.V = V; r.all_coloc = md.all_coloc;
+        r.scale = md.scale; r.size = md.size; r.inv_w = md.inv_w;
+        r.P[0] = s_prod_pow[0]; r.P[1] = s_prod_pow[1]; r.P[2] = s_prod_pow[2];
+        mbar_arrive_expect_tx(sfull, (uint32_t)kStatePlanes * bytes);
+      }
+      __syncwarp();
+      if (lane < kStatePlanes) {
+        const float* base = lane < 9 ? md.tex : lane < 18 ? md.m1 : md.m2;
+        bulk_g2s(state_base + (uint32_t)(lane * TT) * 4u, base + (size_t)(lane % 9) * T + first, bytes, sfull);
+      }
+      ++states;
+      for (int it = 0; it < iters && ok; ++it) {
+        for (int q = 0; q < nt; ++q) {
+          if (issued >= R) {
+            ok = __all_sync(0xffffffffu, wait_phase(smem_u32(&empty_bar[slot]), phase ^ 1u, err, kDevTimeoutEmpty));
+            if (!ok) break;
+          }
+          const int plane0 = 3 * kPairChunkViews * q;
+          const int nplanes = min(3 * kPairChunkViews, 3 * V - plane0);
+          const uint32_t fb = smem_u32(&full_bar[slot]);
+          if (lane == 0) {
+            PairSlotRec& r = recs[slot];
+            for (int j = 0; j < kPairChunkViews && kPairChunkViews * q + j < V; ++j) {
+              const View& w = s_prod_views[kPairChunkViews * q + j];
+              r.cxy[j] = make_float4(w.cx, w.cx, w.cy, w.cy);
+              r.czz[j] = make_float4(w.cz, w.cz, 0.f, 0.f);
+              r.view[j] = w;
+            }
+            mbar_arrive_expect_tx(fb, (uint32_t)nplanes * bytes);
+          }
+          __syncwarp();
+          if (lane < nplanes)
+            bulk_g2s(ring_base + (uint32_t)(slot * SLOT + lane * TT) * 4u,
+                     md.tgt + (size_t)(plane0 + lane) * T + first, bytes, fb);
+          ++issued;
+          if (++slot == R) { slot = 0; phase ^= 1u; }
+        }
+      }
+    }
+    if (!ok && lane == 0) {
+      // drain: the last min(R, issued) ring chunks and the last state copy must land
+      const long long n = issued < R ? issued : R;
+      int s = slot;
+      uint32_t ph = phase;
+      for (long long i = 0; i < n; ++i) {
+        if (--s < 0) { s = R - 1; ph ^= 1u; }
+        uint32_t it = 0;
+        while (!mbar_try_wait(smem_u32(&full_bar[s]), ph)) {
+          if (++it >= kSpinLimit) { atomicCAS(err, 0, kDevTimeoutDrain); break; }
+        }
+      }
+      if (states > 0) {
+        uint32_t it = 0;
+        while (!mbar_try_wait(sfull, (uint32_t)((states - 1) & 1))) {
+          if (++it >= kSpinLimit) { atomicCAS(err, 0, kDevTimeoutDrain); break; }
+        }
+      }
+    }
+    __syncwarp();
+  } else {
+    // ------------------------------------------------------------ consumers
+    const int tid = threadIdx.x;
+    const float2* sp = reinterpret_cast<const float2*>(state) + tid;  // plane c at sp[c * NT]
+    float2* sw = reinterpret_cast<float2*>(state) + tid;
+    RingCursor rc{0, 0u, true};
+    uint32_t sfp = 0;
+    for (int k = k0; k < k1; ++k) {
+      if (rc.ok) rc.ok = __all_sync(0xffffffffu, wait_phase(smem_u32(&state_full), sfp, err, kDevTimeoutFull));
+      sfp ^= 1u;
+      if (!rc.ok) break;
+      // The tile's fields are read from the shared record where they are used (it stays put
+      // until this warp signals state_empty), which keeps them out of registers in the loop.
+      const FuseStateRec& r0 = s_rec;
+      const int V = r0.V;
+      const bool coloc = !GEN || r0.all_coloc;
+      const bool active = 2 * tid < r0.W * r0.H - r0.first;
+      bool live = true;
+      for (int it = 0; it < iters; ++it) {
+        float2 g[9];
+        float2 loss2;
+        float2 px = make_float2(0.f, 0.f), py = make_float2(0.f, 0.f);
+        if (active) pair_coords(r0, tid, px, py);
+        if (coloc) {
+          TexelPair u;
+          {
+            const float P[3] = {r0.P[0], r0.P[1], r0.P[2]};
+            float2 t9[9];
+#pragma unroll
+            for (int c = 0; c < 9; ++c) t9[c] = clamp2(sp[c * NT]);
+            coloc_prepare_pair(t9, px, py, P, u);
+          }
+          AccC2 a;
+          acc2_zero(a);
+          for (int v0 = 0; v0 < V; v0 += kPairChunkViews) {
+            const float2* tp = pair_acquire<SLOT>(rc, ring, full_bar, err) + tid;
+            if (!rc.ok) { live = false; break; }
+            const PairSlotRec& rv = recs[rc.slot];
+            const int nv = min(kPairChunkViews, V - v0);
+#pragma unroll
+            for (int j = 0; j < kPairChunkViews; ++j) {
+              if (j < nv) {
+                const float2 tg[3] = {tp[(3 * j) * NT], tp[(3 * j + 1) * NT], tp[(3 * j + 2) * NT]};
+                const float4 cxy = rv.cxy[j];
+                const float4 czz = rv.czz[j];
+                coloc_view_pair<LOSS>(u, make_float2(cxy.x, cxy.y), make_float2(cxy.z, cxy.w),
+                                      make_float2(czz.x, czz.y), tg, a);
+              }
+            }
+            ring_release(rc, empty_bar, R);
+          }
+          if (!live) break;
+          float2 t9[9];
+#pragma unroll
+          for (int c = 0; c < 9; ++c) t9[c] = clamp2(sp[c * NT]);
+          const float P[3] = {r0.P[0], r0.P[1], r0.P[2]};
+          loss2 = coloc_finish_pair<LOSS>(t9, u, a, P, r0.scale, g);
+        } else {
+          // general views: the two texels one after the other through each chunk
+          const float P[3] = {r0.P[0], r0.P[1], r0.P[2]};
+          Maps ma, mb;
+          Adj aa, ab;
+          {
+            float ta[9], tb[9];
+#pragma unroll
+            for (int c = 0; c < 9; ++c) {
+              const float2 t = clamp2(sp[c * NT]);
+              ta[c] = t.x;
+              tb[c] = t.y;
+            }
+            decode(ta, ma);
+            decode(tb, mb);
+          }
+          adj_zero(aa);
+          adj_zero(ab);
+          float la = 0.f, lb = 0.f;
+          for (int v0 = 0; v0 < V; v0 += kPairChunkViews) {
+            const float2* tp = pair_acquire<SLOT>(rc, ring, full_bar, err) + tid;
+            if (!rc.ok) { live = false; break; }
+            const PairSlotRec& rv = recs[rc.slot];
+            const int nv = min(kPairChunkViews, V - v0);
+            for (int j = 0; j < nv; ++j) {
+              const float2 t0 = tp[(3 * j) * NT], t1 = tp[(3 * j + 1) * NT], t2 = tp[(3 * j + 2) * NT];
+              const View& w = rv.view[j];
+              float ia[3] = {t0.x, t1.x, t2.x}, ib[3] = {t0.y, t1.y, t2.y};
+              if (w.coloc != 0.f) {
+                texel_view<kModeFused, LOSS, false, true>(ma, px.x, py.x, w, P, ia, la, aa);
+                texel_view<kModeFused, LOSS, false, true>(mb, px.y, py.y, w, P, ib, lb, ab);
+              } else {
+                texel_view<kModeFused, LOSS, false, false>(ma, px.x, py.x, w, P, ia, la, aa);
+                texel_view<kModeFused, LOSS, false, false>(mb, px.y, py.y, w, P, ib, lb, ab);
+              }
+            }
+            ring_release(rc, empty_bar, R);
+          }
+          if (!live) break;
+          float ta[9], tb[9], ga[9], gb[9];
+#pragma unroll
+          for (int c = 0; c < 9; ++c) {
+            const float2 t = clamp2(sp[c * NT]);
+            ta[c] = t.x;
+            tb[c] = t.y;
+          }
+          adj_to_params(ta, ma, aa, r0.scale, ga);
+          adj_to_params(tb, mb, ab, r0.scale, gb);
+#pragma unroll
+          for (int c = 0; c < 9; ++c) g[c] = make_float2(ga[c], gb[c]);
+          loss2 = make_float2(la, lb);
+        }
+        // ---- Adam on the resident state; the last iteration writes to global memory
+        float loss = 0.f;
+        if (active) {
+          const AdamScalars ad = s_adam[it];
+          const bool last = it + 1 == iters;
+          const int T = r0.W * r0.H, idx = r0.first + 2 * tid;
+          float* tex = r0.tex;
+          float* gm1 = r0.m1;
+          float* gm2 = r0.m2;
+#pragma unroll
+          for (int c = 0; c < 9; ++c) {
+            float2 p = sp[c * NT], m1 = sp[(9 + c) * NT], m2 = sp[(18 + c) * NT];
+            // textures.clamp(-1, 1): no gradient outside the range (nor for NaN)
+            const float2 gc = make_float2(fabsf(p.x) <= 1.0f ? g[c].x : 0.0f, fabsf(p.y) <= 1.0f ? g[c].y : 0.0f);
+            adam_update2(p, m1, m2, gc, ad);
+            if (last) {
+              const size_t off = (size_t)c * T + idx;
+              *reinterpret_cast<float2*>(tex + off) = p;
+              *reinterpret_cast<float2*>(gm1 + off) = m1;
+              *reinterpret_cast<float2*>(gm2 + off) = m2;
+            } else {
+              sw[c * NT] = p;
+              sw[(9 + c) * NT] = m1;
+              sw[(18 + c) * NT] = m2;
+            }
+          }
+          loss = loss2.x + loss2.y;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, o);
+        if (lane == 0) warp_loss[((size_t)it * n_tiles + r0.tile) * NCW + warp] = loss;
+      }
+      if (!live) break;
+      // this warp's shared-memory writes come before the next tile's bulk copies into the area
+      fence_proxy_async_smem();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(smem_u32(&state_empty));
+    }
+  }
+  batched_finish<NT + 32>(plan, hdr, mats, warp_loss, NCW, loss_hist, hist_len, s_step, step_counter,
+                          ws + kWsCounter, &s_last, NCW, iters);
+}
+
 // ============================================================== planner
 static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
@@ -1041,12 +1399,20 @@ static int pair_slot_bytes(int threads) { return kPairSlotPlanes * 2 * threads *
 static size_t pair_ring_budget(int threads) {
   return threads / 32 <= kPairTwoCtaNcw ? kPairRingBudgetTwoCta : kPairRingBudget;
 }
+// variant 3: the state area (27 planes of the tile) comes out of the budget first
+static size_t fuse_state_bytes(int threads) { return (size_t)kStatePlanes * 2 * threads * 4; }
+static int fuse_ring(int threads) {
+  const size_t budget = threads / 32 <= kPairTwoCtaNcw ? kFuseBudgetTwoCta : kFuseBudget;
+  const size_t state = fuse_state_bytes(threads);
+  if (state >= budget) return 0;
+  return (int)std::min<size_t>(kMaxRing, (budget - state) / pair_slot_bytes(threads));
+}
 
 static int plan_layout(const svbrdf_material* mats, int n, const svbrdf_batch_config* cfg, PlanLayout& L) {
   if (!mats || n <= 0) return fail(SVBRDF_ERR_INVALID, "no materials");
   if (!cfg) return fail(SVBRDF_ERR_INVALID, "null config");
   const int variant = cfg->variant;
-  if (variant < 0 || variant > 2) return fail(SVBRDF_ERR_INVALID, "variant must be 0, 1 or 2 (got %d)", variant);
+  if (variant < 0 || variant > 3) return fail(SVBRDF_ERR_INVALID, "variant must be 0, 1, 2 or 3 (got %d)", variant);
   if (variant == 0) {
     if (cfg->threads != 128 && cfg->threads != 256 && cfg->threads != 512)
       return fail(SVBRDF_ERR_UNSUPPORTED, "threads must be 128, 256 or 512 (got %d)", cfg->threads);
@@ -1064,6 +1430,11 @@ static int plan_layout(const svbrdf_material* mats, int n, const svbrdf_batch_co
                   cfg->threads);
     if (variant == 2 && cfg->tile_texels != 2 * cfg->threads)
       return fail(SVBRDF_ERR_INVALID, "texel-pair variant: tile_texels must be twice threads");
+    if (variant == 3 && cfg->threads != 224 && cfg->threads != 256 && cfg->threads != 384 && cfg->threads != 480)
+      return fail(SVBRDF_ERR_UNSUPPORTED, "resident-state variant: threads must be 224, 256, 384 or 480 (got %d)",
+                  cfg->threads);
+    if (variant == 3 && cfg->tile_texels != 2 * cfg->threads)
+      return fail(SVBRDF_ERR_INVALID, "resident-state variant: tile_texels must be twice threads");
   }
   long long tiles = 0, coords = 0;
   int views = 0, max_views = 0;
@@ -1097,7 +1468,11 @@ static int plan_layout(const svbrdf_material* mats, int n, const svbrdf_batch_co
   L.coord_floats = coords;
   L.ring = variant == 1   ? (int)std::min<size_t>(kMaxRing, kRingBudget / slot_bytes(cfg->threads))
            : variant == 2 ? (int)std::min<size_t>(kMaxRing, pair_ring_budget(cfg->threads) / pair_slot_bytes(cfg->threads))
+           : variant == 3 ? fuse_ring(cfg->threads)
                           : 0;
+  if (variant == 3 && L.ring < 2)
+    return fail(SVBRDF_ERR_UNSUPPORTED, "resident-state variant: %d threads leave room for %d ring slots", cfg->threads,
+                L.ring);
   // variant 1 holds a tile's parameter slot until its last chunk (S) has been read, so
   // all 3 + ceil(V/4) chunks of a tile must fit in the ring at once
   if (variant == 1 && 3 + (max_views + 3) / 4 > L.ring)
@@ -1151,6 +1526,18 @@ static int tma_prepare(int ring) {
   return allow_smem(batched_tma_kernel<LOSS, NCW>, tma_smem<NCW>(ring), done, have);
 }
 
+template <int NCW>
+static size_t fuse_smem(int ring) {
+  return (size_t)kStatePlanes * 2 * NCW * 32 * 4 + pair_smem<NCW>(ring);
+}
+
+template <int LOSS, int NCW, bool GEN>
+static int fuse_prepare(int ring) {
+  static int done = 0;
+  static size_t have = 0;
+  return allow_smem(batched_fuse_kernel<LOSS, NCW, GEN>, fuse_smem<NCW>(ring), done, have);
+}
+
 template <int LOSS, int NCW, bool GEN>
 static int pair_prepare(int ring) {
   static int done = 0;
@@ -1162,7 +1549,7 @@ int resident_ctas(int variant, int threads) {
   const int sms = device_sm_count();
   if (sms <= 0) return 0;
   // one pipelined CTA per SM (its ring takes the shared memory); two for the small texel-pair shape
-  if (variant == 2 && threads / 32 <= kPairTwoCtaNcw) return 2 * sms;
+  if (variant >= 2 && threads / 32 <= kPairTwoCtaNcw) return 2 * sms;
   if (variant >= 1) return sms;
   int occ = 1;
   switch (threads) {
@@ -1428,12 +1815,25 @@ size_t svbrdf_batched_workspace_bytes(const void* host_plan) {
   const PlanHeader* h = (const PlanHeader*)host_plan;
   if (h->magic != kPlanMagic) return 0;
   const size_t per_tile = h->variant >= 1 ? (size_t)(h->threads / 32) : 1;
-  return kWsLossOffset + sizeof(float) * (size_t)h->n_tiles * per_tile;
+  const size_t iters = h->variant == 3 ? (size_t)kFuseMax : 1;  // partials of every iteration of a launch
+  return kWsLossOffset + sizeof(float) * (size_t)h->n_tiles * per_tile * iters;
 }
 
 int svbrdf_batched_step(const void* device_plan, const void* host_plan, int loss_kind, int* step_counter, float lr,
                         float beta1, float beta2, float eps, float* loss_hist, int hist_len, void* workspace,
                         size_t workspace_bytes, void* stream) {
+  return svbrdf_batched_steps(device_plan, host_plan, loss_kind, step_counter, lr, beta1, beta2, eps, loss_hist,
+                              hist_len, 1, workspace, workspace_bytes, stream);
+}
+
+// One launch of the single-iteration variants (0, 1, 2).
+static int batched_launch_one(const PlanHeader* h, const char* plan, int loss_kind, int* step_counter,
+                              AdamHyper hyper, float* loss_hist, int hist_len, unsigned* ws, float* part,
+                              cudaStream_t st);
+
+int svbrdf_batched_steps(const void* device_plan, const void* host_plan, int loss_kind, int* step_counter, float lr,
+                         float beta1, float beta2, float eps, float* loss_hist, int hist_len, int iters,
+                         void* workspace, size_t workspace_bytes, void* stream) {
   if (!device_plan || !host_plan || !loss_hist || !step_counter)
     return fail(SVBRDF_ERR_INVALID, "null plan/step_counter/loss_hist");
   const PlanHeader* h = (const PlanHeader*)host_plan;
@@ -1441,6 +1841,7 @@ int svbrdf_batched_step(const void* device_plan, const void* host_plan, int loss
   if (loss_kind < SVBRDF_LOSS_MSE || loss_kind > SVBRDF_LOSS_LOG1P_PRE)
     return fail(SVBRDF_ERR_INVALID, "bad loss_kind %d", loss_kind);
   if (hist_len < 1) return fail(SVBRDF_ERR_INVALID, "hist_len must be >= 1");
+  if (iters < 0) return fail(SVBRDF_ERR_INVALID, "iters must be >= 0");
   const size_t need = svbrdf_batched_workspace_bytes(host_plan);
   if (!workspace || workspace_bytes < need) return fail(SVBRDF_ERR_WORKSPACE, "workspace of %zu bytes needed", need);
   unsigned* ws = (unsigned*)workspace;
@@ -1452,6 +1853,40 @@ int svbrdf_batched_step(const void* device_plan, const void* host_plan, int loss
   hyper.eps = eps;
   cudaStream_t st = (cudaStream_t)stream;
   const char* plan = (const char*)device_plan;
+  if (h->variant != 3) {
+    for (int i = 0; i < iters; ++i) {
+      const int rc = batched_launch_one(h, plan, loss_kind, step_counter, hyper, loss_hist, hist_len, ws, part, st);
+      if (rc) return rc;
+    }
+    return SVBRDF_OK;
+  }
+  const int ring = h->ring_slots;
+  if (ring < 2 || ring > kMaxRing) return fail(SVBRDF_ERR_INVALID, "bad ring depth %d", ring);
+  // iters split evenly over ceil(iters / kFuseMax) launches
+  const int launches = (iters + kFuseMax - 1) / kFuseMax;
+  for (int l = 0; l < launches; ++l) {
+    const int k = iters / launches + (l < iters % launches ? 1 : 0);
+#define SVB_F(L, NCW, G)                                                                                       {                                                                                                              int prc = fuse_prepare<L, NCW, G>(ring);                                                                     if (prc) return prc;                                                                                         batched_fuse_kernel<L, NCW, G><<<h->n_ctas, (NCW + 1) * 32, fuse_smem<NCW>(ring), st>>>(                         plan, hyper, step_counter, loss_hist, hist_len, k, part, ws);                                          }
+#define SVB_FG(L, NCW)                  if (h->general) SVB_F(L, NCW, true)   else SVB_F(L, NCW, false)
+#define SVB_FL(NCW)                                         if (loss_kind == SVBRDF_LOSS_MSE) SVB_FG(0, NCW)          else if (loss_kind == SVBRDF_LOSS_LOG1P) SVB_FG(1, NCW)   else SVB_FG(2, NCW)
+    switch (h->threads) {
+      case 224: SVB_FL(7) break;
+      case 256: SVB_FL(8) break;
+      case 384: SVB_FL(12) break;
+      default: SVB_FL(15) break;
+    }
+#undef SVB_FL
+#undef SVB_FG
+#undef SVB_F
+    const int rc = check_launch("batched_fuse_kernel");
+    if (rc) return rc;
+  }
+  return SVBRDF_OK;
+}
+
+static int batched_launch_one(const PlanHeader* h, const char* plan, int loss_kind, int* step_counter,
+                              AdamHyper hyper, float* loss_hist, int hist_len, unsigned* ws, float* part,
+                              cudaStream_t st) {
   if (h->variant == 0) {
 #define SVB_B(L, NT) \
   batched_step_kernel<L, NT><<<h->n_ctas, NT, 0, st>>>(plan, hyper, step_counter, loss_hist, hist_len, part, ws)

@@ -138,6 +138,112 @@ def _upsample2(x):
     return _up1d(_up1d(x, -1), -2)
 
 
+def _use_kernels(x):
+    return x.is_cuda and x.dtype == torch.float32
+
+
+class _ScaleCuda(torch.autograd.Function):
+    """x[b, c] * s[b, c] (a modulated conv's input scaling) as one kernel each way; the
+    backward also forms the style gradient sum_hw g x per plane (svbrdf_gen_scale[_bwd])."""
+
+    @staticmethod
+    def forward(ctx, x, s):
+        from . import _native as N
+
+        x, s = x.contiguous(), s.contiguous()
+        b, c, h, w = x.shape
+        y = torch.empty_like(x)
+        N.check(N.lib().svbrdf_gen_scale(x.data_ptr(), s.data_ptr(), y.data_ptr(), b * c, h * w,
+                                         N.stream_handle(x.device)))
+        ctx.save_for_backward(x, s)
+        return y
+
+    @staticmethod
+    def backward(ctx, g):
+        from . import _native as N
+
+        x, s = ctx.saved_tensors
+        b, c, h, w = x.shape
+        g = g.contiguous()
+        gx = torch.empty_like(x)
+        gs = torch.empty(b, c, device=x.device, dtype=torch.float32)
+        N.check(N.lib().svbrdf_gen_scale_bwd(g.data_ptr(), x.data_ptr(), s.data_ptr(), gx.data_ptr(), gs.data_ptr(),
+                                             b * c, h * w, N.stream_handle(x.device)))
+        return gx, gs
+
+
+class _ActCuda(torch.autograd.Function):
+    """A style layer's epilogue lrelu(y d + ns noise + bias, 0.2) gain as one kernel each way
+    (svbrdf_gen_act[_bwd]). d: [B, C] demodulation; noise: [B, 1, H, W] or None; ns: the
+    0-d noise strength; bias: [C]. The generator is frozen, so bias and ns get no gradient."""
+
+    @staticmethod
+    def forward(ctx, y, d, noise, ns, bias, gain):
+        from . import _native as N
+
+        y, d, bias = y.contiguous(), d.contiguous(), bias.contiguous()
+        noise = noise.contiguous() if noise is not None else None
+        b, c, h, w = y.shape
+        out = torch.empty_like(y)
+        N.check(N.lib().svbrdf_gen_act(y.data_ptr(), d.data_ptr(), noise.data_ptr() if noise is not None else None,
+                                       ns.data_ptr() if noise is not None else None, bias.data_ptr(), gain,
+                                       out.data_ptr(), b, c, h * w, N.stream_handle(y.device)))
+        ctx.save_for_backward(y, d, noise, ns, bias)
+        ctx.gain = gain
+        return out
+
+    @staticmethod
+    def backward(ctx, g):
+        from . import _native as N
+
+        y, d, noise, ns, bias = ctx.saved_tensors
+        b, c, h, w = y.shape
+        g = g.contiguous()
+        gy = torch.empty_like(y)
+        gd = torch.empty(b, c, device=y.device, dtype=torch.float32)
+        want_noise = noise is not None and ctx.needs_input_grad[2]
+        gn = torch.empty_like(noise) if want_noise else None
+        N.check(N.lib().svbrdf_gen_act_bwd(g.data_ptr(), y.data_ptr(), d.data_ptr(),
+                                           noise.data_ptr() if noise is not None else None,
+                                           ns.data_ptr() if noise is not None else None, bias.data_ptr(), ctx.gain,
+                                           gy.data_ptr(), gd.data_ptr(), gn.data_ptr() if want_noise else None,
+                                           b, c, h * w, N.stream_handle(y.device)))
+        return gy, gd, gn, None, None, None
+
+
+class _UpScaleCuda(torch.autograd.Function):
+    """2x up-sampling of x[b, c] * s[b, c] in one kernel (svbrdf_gen_upsample2_scaled); the
+    backward is the up-sampling adjoint followed by svbrdf_gen_scale_bwd."""
+
+    @staticmethod
+    def forward(ctx, x, s):
+        from . import _native as N
+
+        x, s = x.contiguous(), s.contiguous()
+        b, c, h, w = x.shape
+        y = torch.empty(b, c, 2 * h, 2 * w, device=x.device, dtype=torch.float32)
+        N.check(N.lib().svbrdf_gen_upsample2_scaled(x.data_ptr(), s.data_ptr(), y.data_ptr(), b * c, h, w,
+                                                    N.stream_handle(x.device)))
+        ctx.save_for_backward(x, s)
+        return y
+
+    @staticmethod
+    def backward(ctx, g):
+        from . import _native as N
+
+        x, s = ctx.saved_tensors
+        b, c, h, w = x.shape
+        L, st = N.lib(), N.stream_handle(x.device)
+        g = g.contiguous()
+        gu = torch.empty_like(x)
+        N.check(L.svbrdf_gen_upsample2_bwd(g.data_ptr(), gu.data_ptr(), b * c, h, w, st))
+        gx = torch.empty_like(x)
+        gs = torch.empty(b, c, device=x.device, dtype=torch.float32)
+        N.check(L.svbrdf_gen_scale_bwd(gu.data_ptr(), x.data_ptr(), s.data_ptr(), gx.data_ptr(), gs.data_ptr(),
+                                       b * c, h * w, st))
+        return gx, gs
+
+
 class _ModConv(torch.nn.Module):
     """Modulated (and optionally demodulated) conv, optionally 2x up-sampling first."""
 
@@ -156,17 +262,26 @@ class _ModConv(torch.nn.Module):
         # form), but it runs as one batched convolution. With the generator frozen, its
         # backward is a data gradient plus small reductions, with no per-sample weight
         # gradients.
+        y, d = self.parts(x, w)
+        return y if d is None else y * d[:, :, None, None]
+
+    def parts(self, x, w):
+        """The shared-weight convolution of the style-scaled input, and the demodulation
+        d [B, cout] (None without demodulation) still to be applied to its output."""
         s = self.affine(w)  # [B, cin]
         wsc = self.weight * self.scale
-        x = x * s[:, :, None, None]
-        if self.up:
-            x = _upsample2(x)  # per-channel linear: commutes with the channel scaling
+        if self.up and _use_kernels(x) and x.shape[-1] % 4 == 0 and x.data_ptr() % 16 == 0:
+            x = _UpScaleCuda.apply(x, s)  # the up-sampling commutes with the channel scaling
+        else:
+            x = _ScaleCuda.apply(x, s) if _use_kernels(x) else x * s[:, :, None, None]
+            if self.up:
+                x = _upsample2(x)  # per-channel linear: commutes with the channel scaling
         y = Fn.conv2d(x, wsc, padding=self.k // 2)
+        d = None
         if self.demod:
             w2 = wsc.pow(2).sum(dim=(2, 3))  # [cout, cin]
             d = torch.rsqrt(s.pow(2) @ w2.t() + 1e-8)  # [B, cout]
-            y = y * d[:, :, None, None]
-        return y
+        return y, d
 
 
 class _StyleLayer(torch.nn.Module):
@@ -177,6 +292,10 @@ class _StyleLayer(torch.nn.Module):
         self.bias = torch.nn.Parameter(torch.zeros(cout))
 
     def forward(self, x, w, noise):
+        if _use_kernels(x) and not (self.bias.requires_grad or self.noise_strength.requires_grad) and (
+                noise is None or (noise.shape[0] == x.shape[0] and noise.shape[1] == 1)):
+            y, d = self.conv.parts(x, w)
+            return _ActCuda.apply(y, d, noise, self.noise_strength, self.bias, LRELU_GAIN)
         y = self.conv(x, w)
         if noise is not None:
             y = y + self.noise_strength * noise

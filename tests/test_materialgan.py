@@ -144,17 +144,64 @@ def test_unfused_modulated_conv_matches_per_sample_weights(svb):
 
 
 @pytest.mark.gpu
-def test_upsample_kernel_matches_fir(svb, cuda):
-    """The CUDA up-sampling and its adjoint against the FIR form (FP64 on the CPU)."""
+@pytest.mark.parametrize("shape", [(2, 5, 7, 9), (2, 5, 4, 8), (1, 3, 12, 4)])
+def test_upsample_kernel_matches_fir(svb, cuda, shape):
+    """The CUDA up-sampling and its adjoint against the FIR form (FP64 on the CPU): scalar
+    kernels for odd widths, float4 kernels for widths that are multiples of 4."""
     MG = svb.materialgan
     g = torch.Generator().manual_seed(7)
-    x = torch.randn(2, 5, 7, 9, generator=g)
+    x = torch.randn(*shape, generator=g)
     ref = MG._upsample2_fir(x.double())
     xc = x.to(cuda).requires_grad_(True)
     y = MG._upsample2(xc)
     assert torch.allclose(y.double().cpu(), ref, rtol=0, atol=1e-5)
-    go = torch.randn(2, 5, 14, 18, generator=g)
+    go = torch.randn(shape[0], shape[1], 2 * shape[2], 2 * shape[3], generator=g)
     y.backward(go.to(cuda))
     xr = x.double().requires_grad_(True)
     MG._upsample2_fir(xr).backward(go.double())
     assert torch.allclose(xc.grad.double().cpu(), xr.grad, rtol=0, atol=1e-5)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("with_noise,hw", [(True, (9, 7)), (False, (9, 7)), (True, (8, 12)), (False, (4, 4))])
+def test_style_layer_kernels_match_torch(svb, cuda, with_noise, hw):
+    """A style layer through the modulation and epilogue kernels against the same layer in
+    FP64 torch on the CPU: the output and the gradients of the input, the style vector and the
+    noise map (the latent loop's only gradients)."""
+    MG = svb.materialgan
+    g = torch.Generator().manual_seed(11)
+    layer = MG._StyleLayer(12, 10, 16, g, up=True)
+    with torch.no_grad():
+        layer.bias.copy_(torch.randn(10, generator=g) * 0.3)
+        layer.noise_strength.fill_(0.7)
+    for p in layer.parameters():
+        p.requires_grad_(False)
+    h, wd = hw  # (9, 7) runs the scalar kernels, multiples of 4 the float4 ones
+    x = torch.randn(3, 12, h, wd, generator=g)
+    w = torch.randn(3, 16, generator=g)
+    nz = torch.randn(3, 1, 2 * h, 2 * wd, generator=g) if with_noise else None
+    go = torch.randn(3, 10, 2 * h, 2 * wd, generator=g)
+
+    ref = MG._StyleLayer(12, 10, 16, torch.Generator().manual_seed(0), up=True).double()
+    ref.load_state_dict({k: v.double() for k, v in layer.state_dict().items()})
+    for p in ref.parameters():
+        p.requires_grad_(False)
+    xr, wr = x.double().requires_grad_(True), w.double().requires_grad_(True)
+    nr = nz.double().requires_grad_(True) if with_noise else None
+    yr = ref(xr, wr, nr)
+    yr.backward(go.double())
+
+    lc = layer.to(cuda)
+    xc, wc = x.to(cuda).requires_grad_(True), w.to(cuda).requires_grad_(True)
+    nc = nz.to(cuda).requires_grad_(True) if with_noise else None
+    torch.backends.cudnn.allow_tf32 = False
+    try:
+        yc = lc(xc, wc, nc)
+        yc.backward(go.to(cuda))
+    finally:
+        torch.backends.cudnn.allow_tf32 = True
+    assert rel_l2(yc.detach(), yr.detach()) < 1e-5
+    assert rel_l2(xc.grad.double().cpu(), xr.grad) < 1e-5
+    assert rel_l2(wc.grad.double().cpu(), wr.grad) < 1e-5
+    if with_noise:
+        assert rel_l2(nc.grad.double().cpu(), nr.grad) < 1e-5

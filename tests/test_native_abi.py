@@ -23,7 +23,7 @@ def test_exports_match_header(svb, lib):
 
 
 def test_constants(lib):
-    assert lib.svbrdf_abi_version() == 2
+    assert lib.svbrdf_abi_version() == 3
     assert lib.svbrdf_max_views() >= 16
     assert lib.svbrdf_workspace_bytes() >= 16
 
@@ -178,6 +178,29 @@ def test_pair_plan_requirements_and_ring(svb, lib):
     ring7 = np.frombuffer(buf7[:64].tobytes(), np.int32)[14]
     budget7, slot7 = 104 * 1024, 9 * 448 * 4 + 288
     assert ring7 * slot7 <= budget7 < (ring7 + 1) * slot7
+
+
+@pytest.mark.parametrize("threads,budget,ring", [(480, 220, 3), (384, 220, 5), (256, 220, 9), (224, 100, 3)])
+def test_resident_state_plan_ring_and_workspace(svb, lib, threads, budget, ring):
+    """Variant 3: the 27-plane state area comes out of the shared-memory budget before the
+    ring of 9-plane target slots; the workspace holds partials for 32 iterations."""
+    SV = svb._native
+    mats, keep = _materials(SV, [(64, 64, 9), (32, 32, 5)])
+    tt = 2 * threads
+    cfg = SV.svbrdf_batch_config(threads, tt, 3, 3)
+    n = lib.svbrdf_batched_plan_bytes(mats, 2, ctypes.byref(cfg))
+    assert n > 0
+    buf = np.zeros(n, np.uint8)
+    assert lib.svbrdf_batched_plan(mats, 2, ctypes.byref(cfg), buf.ctypes.data, n) == 0
+    hdr = np.frombuffer(buf[:72].tobytes(), np.int32)
+    n_tiles, variant, got = hdr[2], hdr[13], hdr[14]
+    assert variant == 3 and got == ring
+    state, slot = 27 * tt * 4, 9 * tt * 4 + 288
+    assert state + ring * slot <= budget * 1024 < state + (ring + 1) * slot
+    assert lib.svbrdf_batched_workspace_bytes(buf.ctypes.data) == 256 + 4 * n_tiles * (threads // 32) * 32
+    # 608 threads is not offered by the resident-state variant; tiles must be twice threads
+    assert lib.svbrdf_batched_plan_bytes(mats, 2, ctypes.byref(SV.svbrdf_batch_config(608, 1216, 3, 3))) == 0
+    assert lib.svbrdf_batched_plan_bytes(mats, 2, ctypes.byref(SV.svbrdf_batch_config(480, 480, 3, 3))) == 0
 
 
 def test_pipelined_plan_ring_and_workspace(svb, lib):

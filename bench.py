@@ -47,7 +47,8 @@ import torch  # noqa: E402
 PKG = importlib.import_module("svbrdf-diff-renderer_gb300")
 METRIC = "texel*view render+adjoint+Adam updates/s, fused batched vs plain, 1 GB300"
 UNIT = "texel*view updates/s"
-KERNEL_NAMES = {0: "batched_step_kernel", 1: "batched_tma_kernel", 2: "batched_pair_kernel", 3: "batched_fuse_kernel"}
+KERNEL_NAMES = {0: "batched_step_kernel", 1: "batched_tma_kernel", 2: "batched_pair_kernel", 3: "batched_fuse_kernel",
+                4: "batched_fuse2_kernel"}
 WORKLOAD = "batched 64 materials, res {256,512,1024}, V 5-16, 100 iterations per graph replay, log1p L2, Adam lr 0.01"
 
 
@@ -537,7 +538,7 @@ def impl_ours(args):
     # the one-launch-per-iteration kernel (variant 2) on the same materials: the HBM-bound
     # form, for which the per-iteration algorithmic bytes are the real DRAM traffic
     per_iter = None
-    if cfg_used.variant == 3:
+    if cfg_used.variant >= 3:
         pairs = [r for r in tune if r[1] == 2]
         pc = PKG.BatchConfig(pairs[0][2], pairs[0][2] * pairs[0][3], 0, 2) if pairs else PKG.BatchConfig(480, 960, 0, 2)
         o2 = PKG.BatchedOptim(mats, lr=0.01, loss="log1p", device=dev, hist_len=args.iters, config=pc)

@@ -145,6 +145,9 @@ typedef struct svbrdf_material {
  *   memory between them, so HBM carries them once per launch; only the targets stream per
  *   iteration, from L2 after the first): threads 224, 256, 384 or 480, tile_texels ==
  *   2 * threads, the material requirements of variant 1. Use svbrdf_batched_steps.
+ * variant 4 (variant 3 without the producer warp: the last warp to finish with a ring slot
+ *   or the state refills it, so all warps compute): threads 256 (two CTAs per SM) or 512,
+ *   tile_texels == 2 * threads, the material requirements of variant 1.
  * ctas: persistent CTAs (0 = SM count x resident CTAs per SM). */
 typedef struct svbrdf_batch_config {
   int threads;
@@ -180,8 +183,8 @@ int svbrdf_batched_step(const void* device_plan, const void* host_plan, int loss
                         float lr, float beta1, float beta2, float eps, float* loss_hist, int hist_len,
                         void* workspace, size_t workspace_bytes, void* stream);
 /* `iters` iterations of svbrdf_batched_step (the whole `for epoch in range(epochs)` loop of
- * src/svbrdf.py:56-71 for every material). Variants 0-2 launch once per iteration; variant 3
- * runs ceil(iters / 32) launches of up to 32 iterations each. The parameters, moments, step
+ * src/svbrdf.py:56-71 for every material). Variants 0-2 launch once per iteration; variants
+ * 3 and 4 run ceil(iters / 32) launches of up to 32 iterations each. The parameters, moments, step
  * counter and loss history afterwards equal those of `iters` svbrdf_batched_step calls. */
 int svbrdf_batched_steps(const void* device_plan, const void* host_plan, int loss_kind, int* step_counter,
                          float lr, float beta1, float beta2, float eps, float* loss_hist, int hist_len, int iters,

@@ -26,9 +26,10 @@ import torch
 from . import _native as N
 
 LOSS_KINDS = {"mse": 0, "log1p": 1, "log1p_pre": 2}
-FUSE_MAX = 32  # iterations per launch of the resident-state variant (kFuseMax in fused.cu)
+FUSE_MAX = 32  # iterations per launch of the resident-state variants (kFuseMax in fused.cu)
 # (variant, threads, tile_texels / threads)
 CANDIDATES = ([(3, t, 2) for t in (224, 256, 384, 480)] +
+              [(4, t, 2) for t in (512, 256)] +
               [(2, t, 2) for t in (224, 256, 384, 480)] +
               [(1, t, 1) for t in (256, 384, 480, 608)] +
               [(0, t, k) for t in (128, 256, 512) for k in (1, 4, 16)])
@@ -41,7 +42,8 @@ class BatchConfig:
     tile_texels: int = 1024
     ctas: int = 0     # 0 = SM count x resident CTAs per SM
     variant: int = 0  # 0 direct loads, 1 bulk-copy (TMA) pipeline, 2 the pipeline on texel pairs,
-    #                   3 texel pairs with the state resident across the iterations of a launch
+    #                   3 texel pairs with the state resident across the iterations of a launch,
+    #                   4 the same without a producer warp (the last reader of a buffer refills it)
 
     def as_c(self):
         return N.svbrdf_batch_config(self.threads, self.tile_texels, self.ctas, self.variant)
@@ -95,7 +97,7 @@ class BatchedOptim:
 
     def launches(self, iters: int) -> int:
         """Kernel launches ``iters`` iterations take with this plan's variant."""
-        return -(-iters // FUSE_MAX) if self.config.variant == 3 else iters
+        return -(-iters // FUSE_MAX) if self.config.variant >= 3 else iters
 
     def signature(self) -> str:
         h = hashlib.sha1(json.dumps(sorted(self.meta)).encode()).hexdigest()[:16]

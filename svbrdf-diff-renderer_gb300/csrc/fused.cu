@@ -1383,6 +1383,358 @@ batched_fuse_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
                           ws + kWsCounter, &s_last, NCW, iters);
 }
 
+// ============================================================== variant 4: resident state, no producer
+//
+// Variant 3's schedule without a producer warp: every warp computes, and the copies are
+// issued by whichever warp finishes with a buffer last.
+//   * Ring: a warp that has read a target chunk counts itself out of its slot with a
+//     shared-memory atomic; the last of the NCW warps refills the slot with the chunk R
+//     positions later in the CTA's chunk sequence (tile by tile: K iterations x
+//     ceil(V/3) chunks), found by walking the tile list forward from its own position.
+//   * State: the last warp to finish a tile copies the next tile's state and record.
+// Warp 0 issues the first tile's state and the first R chunks. Sixteen compute warps fill
+// the four sub-partitions evenly (variant 3 has fifteen beside the producer), and the
+// 256-thread shape runs two independent CTAs per SM. Each warp orders its shared-memory
+// reads (and its state writes) before the copies that overwrite them with a CTA fence before
+// its count and, in the refilling warp, an async-proxy fence before the copy. Waits are
+// bounded as in the other variants; a CTA whose warps gave up drains every copy it issued
+// before returning.
+constexpr int kFuse2TwoCtaNcw = 8;
+constexpr size_t kFuse2Budget = 220 * 1024;
+constexpr size_t kFuse2BudgetTwoCta = 100 * 1024;
+
+// Position `steps` chunks after local chunk l of CTA tile k (tiles k .. k1-1 in schedule
+// order, iters x ceil(V/3) chunks each). False past the CTA's last chunk.
+__device__ __forceinline__ bool fuse_walk(const int4* seq, const MatDesc* mats, int k, int l, int steps, int k1,
+                                          int iters, int& kout, int& lout) {
+  int rem = l + steps;
+  while (k < k1) {
+    const int n = iters * ((mats[seq[k].y].V + kPairChunkViews - 1) / kPairChunkViews);
+    if (rem < n) {
+      kout = k;
+      lout = rem;
+      return true;
+    }
+    rem -= n;
+    ++k;
+  }
+  return false;
+}
+
+// Whole warp: target chunk l of CTA tile k into ring slot `slot`.
+template <int TT>
+__device__ __forceinline__ void fuse_issue_chunk(const int4* seq, const MatDesc* mats, const View* views, int k, int l,
+                                                 int slot, uint32_t ring_base, PairSlotRec* recs, uint64_t* full_bar,
+                                                 int* issue_cnt) {
+  constexpr int SLOT = kPairSlotPlanes * TT;
+  const int lane = threadIdx.x & 31;
+  const int4 sq = seq[k];
+  const MatDesc& md = mats[sq.y];
+  const int V = md.V, T = md.H * md.W, first = sq.z;
+  const int nt = (V + kPairChunkViews - 1) / kPairChunkViews;
+  const int q = l % nt;
+  const uint32_t bytes = (uint32_t)min(TT, T - first) * 4u;
+  const int plane0 = 3 * kPairChunkViews * q;
+  const int nplanes = min(3 * kPairChunkViews, 3 * V - plane0);
+  const uint32_t fb = smem_u32(&full_bar[slot]);
+  if (lane == 0) {
+    PairSlotRec& r = recs[slot];
+    for (int j = 0; j < kPairChunkViews && kPairChunkViews * q + j < V; ++j) {
+      const View w = views[md.view_off + kPairChunkViews * q + j];
+      r.cxy[j] = make_float4(w.cx, w.cx, w.cy, w.cy);
+      r.czz[j] = make_float4(w.cz, w.cz, 0.f, 0.f);
+      r.view[j] = w;
+    }
+    ++issue_cnt[slot];
+    mbar_arrive_expect_tx(fb, (uint32_t)nplanes * bytes);
+  }
+  __syncwarp();
+  if (lane < nplanes)
+    bulk_g2s(ring_base + (uint32_t)(slot * SLOT + lane * TT) * 4u, md.tgt + (size_t)(plane0 + lane) * T + first,
+             bytes, fb);
+}
+
+// Whole warp: the state (parameters, exp_avg, exp_avg_sq) and record of CTA tile k.
+template <int TT>
+__device__ __forceinline__ void fuse_issue_state(const int4* seq, const MatDesc* mats, int k, uint32_t state_base,
+                                                 FuseStateRec* rec, uint64_t* state_full, int* state_cnt) {
+  const int lane = threadIdx.x & 31;
+  const int4 sq = seq[k];
+  const MatDesc& md = mats[sq.y];
+  const int T = md.H * md.W, first = sq.z;
+  const uint32_t bytes = (uint32_t)min(TT, T - first) * 4u;
+  const uint32_t sfull = smem_u32(state_full);
+  if (lane == 0) {
+    rec->tex = md.tex; rec->m1 = md.m1; rec->m2 = md.m2;
+    rec->tile = sq.x; rec->first = first; rec->W = md.W; rec->H = md.H;
+    rec->V = md.V; rec->all_coloc = md.all_coloc;
+    rec->scale = md.scale; rec->size = md.size; rec->inv_w = md.inv_w;
+    rec->P[0] = md.lpow[0]; rec->P[1] = md.lpow[1]; rec->P[2] = md.lpow[2];
+    ++*state_cnt;
+    mbar_arrive_expect_tx(sfull, (uint32_t)kStatePlanes * bytes);
+  }
+  __syncwarp();
+  if (lane < kStatePlanes) {
+    const float* base = lane < 9 ? md.tex : lane < 18 ? md.m1 : md.m2;
+    bulk_g2s(state_base + (uint32_t)(lane * TT) * 4u, base + (size_t)(lane % 9) * T + first, bytes, sfull);
+  }
+}
+
+// Whole warp: count this warp out of a buffer; true in the one warp that counted last
+// (the counter is reset for the buffer's next use). The CTA fence orders the warp's reads
+// and writes of the buffer before its count.
+__device__ __forceinline__ bool fuse_count_out(int* cnt, int nwarps) {
+  __syncwarp();
+  int old = 0;
+  if ((threadIdx.x & 31) == 0) {
+    __threadfence_block();
+    old = atomicAdd(cnt, 1);
+    if (old == nwarps - 1) {
+      __threadfence_block();  // with the other warps' fence-then-count: their accesses happen before ours
+      *cnt = 0;
+    }
+  }
+  old = __shfl_sync(0xffffffffu, old, 0);
+  return old == nwarps - 1;
+}
+
+template <int LOSS, int NCW, bool GEN>
+__global__ void __launch_bounds__(NCW * 32, NCW <= kFuse2TwoCtaNcw ? 2 : 1)
+batched_fuse2_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restrict__ step_counter,
+                     float* __restrict__ loss_hist, int hist_len, int iters, float* __restrict__ warp_loss,
+                     unsigned* ws) {
+  constexpr int NT = NCW * 32;
+  constexpr int TT = 2 * NT;                  // texels per tile
+  constexpr int SLOT = kPairSlotPlanes * TT;  // floats per ring slot
+  constexpr int STATE = kStatePlanes * TT;    // floats of the state area
+  extern __shared__ __align__(128) float smem[];
+  float* state = smem;
+  float* ring = smem + STATE;
+  __shared__ __align__(8) uint64_t full_bar[kMaxRing];
+  __shared__ __align__(8) uint64_t state_full;
+  __shared__ int rel_cnt[kMaxRing];
+  __shared__ int issue_cnt[kMaxRing];
+  __shared__ int st_rel;
+  __shared__ int st_issued;
+  __shared__ FuseStateRec s_rec;
+  __shared__ AdamScalars s_adam[kFuseMax];
+  __shared__ int s_step;
+  __shared__ int s_last;
+
+  const PlanHeader* hdr = (const PlanHeader*)plan;
+  const MatDesc* mats = (const MatDesc*)(plan + hdr->off_mats);
+  const View* views = (const View*)(plan + hdr->off_views);
+  const int* cta_off = (const int*)(plan + hdr->off_cta);
+  const int4* seq = (const int4*)(plan + hdr->off_seq);
+  const int R = hdr->ring_slots;
+  const int n_tiles = hdr->n_tiles;
+  PairSlotRec* recs = reinterpret_cast<PairSlotRec*>(ring + (size_t)R * SLOT);
+  int* err = (int*)(ws + kWsError);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, tid = threadIdx.x;
+  const uint32_t ring_base = smem_u32(ring), state_base = smem_u32(state);
+
+  const int step0 = *step_counter;  // steps step0 + 1 .. step0 + iters
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < R; ++s) {
+      mbar_init(smem_u32(&full_bar[s]), 1);
+      rel_cnt[s] = 0;
+      issue_cnt[s] = 0;
+    }
+    mbar_init(smem_u32(&state_full), 1);
+    st_rel = 0;
+    st_issued = 0;
+    fence_mbar_init();
+    s_step = step0 + iters;
+  }
+  for (int i = threadIdx.x; i < iters; i += blockDim.x) s_adam[i] = device_adam(hyper, step0 + 1 + i);
+  __syncthreads();
+  const int k0 = cta_off[blockIdx.x], k1 = cta_off[blockIdx.x + 1];
+  if (warp == 0 && k0 < k1) {
+    fuse_issue_state<TT>(seq, mats, k0, state_base, &s_rec, &state_full, &st_issued);
+    for (int c = 0; c < R; ++c) {
+      int kk, ll;
+      if (!fuse_walk(seq, mats, k0, 0, c, k1, iters, kk, ll)) break;
+      fuse_issue_chunk<TT>(seq, mats, views, kk, ll, c, ring_base, recs, full_bar, issue_cnt);
+    }
+  }
+
+  const float2* sp = reinterpret_cast<const float2*>(state) + tid;  // plane c at sp[c * NT]
+  float2* sw = reinterpret_cast<float2*>(state) + tid;
+  RingCursor rc{0, 0u, true};
+  uint32_t sfp = 0;
+  for (int k = k0; k < k1; ++k) {
+    if (rc.ok) rc.ok = __all_sync(0xffffffffu, wait_phase(smem_u32(&state_full), sfp, err, kDevTimeoutFull));
+    sfp ^= 1u;
+    if (!rc.ok) break;
+    const FuseStateRec& r0 = s_rec;
+    const int V = r0.V;
+    const int nt = (V + kPairChunkViews - 1) / kPairChunkViews;
+    const bool coloc = !GEN || r0.all_coloc;
+    const bool active = 2 * tid < r0.W * r0.H - r0.first;
+    bool live = true;
+    for (int it = 0; it < iters; ++it) {
+      float2 g[9];
+      float2 loss2;
+      float2 px = make_float2(0.f, 0.f), py = make_float2(0.f, 0.f);
+      if (active) pair_coords(r0, tid, px, py);
+      if (coloc) {
+        TexelPair u;
+        {
+          const float P[3] = {r0.P[0], r0.P[1], r0.P[2]};
+          float2 t9[9];
+#pragma unroll
+          for (int c = 0; c < 9; ++c) t9[c] = clamp2(sp[c * NT]);
+          coloc_prepare_pair(t9, px, py, P, u);
+        }
+        AccC2 a;
+        acc2_zero(a);
+        for (int qq = 0; qq < nt; ++qq) {
+          const float2* tp = pair_acquire<SLOT>(rc, ring, full_bar, err) + tid;
+          if (!rc.ok) { live = false; break; }
+          const PairSlotRec& rv = recs[rc.slot];
+          const int nv = min(kPairChunkViews, V - kPairChunkViews * qq);
+#pragma unroll
+          for (int j = 0; j < kPairChunkViews; ++j) {
+            if (j < nv) {
+              const float2 tg[3] = {tp[(3 * j) * NT], tp[(3 * j + 1) * NT], tp[(3 * j + 2) * NT]};
+              const float4 cxy = rv.cxy[j];
+              const float4 czz = rv.czz[j];
+              coloc_view_pair<LOSS>(u, make_float2(cxy.x, cxy.y), make_float2(cxy.z, cxy.w),
+                                    make_float2(czz.x, czz.y), tg, a);
+            }
+          }
+          if (fuse_count_out(&rel_cnt[rc.slot], NCW)) {
+            int kk, ll;
+            if (fuse_walk(seq, mats, k, it * nt + qq, R, k1, iters, kk, ll)) {
+              fence_proxy_async_smem();
+              fuse_issue_chunk<TT>(seq, mats, views, kk, ll, rc.slot, ring_base, recs, full_bar, issue_cnt);
+            }
+          }
+          if (++rc.slot == R) { rc.slot = 0; rc.phase ^= 1u; }
+        }
+        if (!live) break;
+        float2 t9[9];
+#pragma unroll
+        for (int c = 0; c < 9; ++c) t9[c] = clamp2(sp[c * NT]);
+        const float P[3] = {r0.P[0], r0.P[1], r0.P[2]};
+        loss2 = coloc_finish_pair<LOSS>(t9, u, a, P, r0.scale, g);
+      } else {
+        const float P[3] = {r0.P[0], r0.P[1], r0.P[2]};
+        Maps ma, mb;
+        Adj aa, ab;
+        {
+          float ta[9], tb[9];
+#pragma unroll
+          for (int c = 0; c < 9; ++c) {
+            const float2 t = clamp2(sp[c * NT]);
+            ta[c] = t.x;
+            tb[c] = t.y;
+          }
+          decode(ta, ma);
+          decode(tb, mb);
+        }
+        adj_zero(aa);
+        adj_zero(ab);
+        float la = 0.f, lb = 0.f;
+        for (int qq = 0; qq < nt; ++qq) {
+          const float2* tp = pair_acquire<SLOT>(rc, ring, full_bar, err) + tid;
+          if (!rc.ok) { live = false; break; }
+          const PairSlotRec& rv = recs[rc.slot];
+          const int nv = min(kPairChunkViews, V - kPairChunkViews * qq);
+          for (int j = 0; j < nv; ++j) {
+            const float2 t0 = tp[(3 * j) * NT], t1 = tp[(3 * j + 1) * NT], t2 = tp[(3 * j + 2) * NT];
+            const View& w = rv.view[j];
+            float ia[3] = {t0.x, t1.x, t2.x}, ib[3] = {t0.y, t1.y, t2.y};
+            if (w.coloc != 0.f) {
+              texel_view<kModeFused, LOSS, false, true>(ma, px.x, py.x, w, P, ia, la, aa);
+              texel_view<kModeFused, LOSS, false, true>(mb, px.y, py.y, w, P, ib, lb, ab);
+            } else {
+              texel_view<kModeFused, LOSS, false, false>(ma, px.x, py.x, w, P, ia, la, aa);
+              texel_view<kModeFused, LOSS, false, false>(mb, px.y, py.y, w, P, ib, lb, ab);
+            }
+          }
+          if (fuse_count_out(&rel_cnt[rc.slot], NCW)) {
+            int kk, ll;
+            if (fuse_walk(seq, mats, k, it * nt + qq, R, k1, iters, kk, ll)) {
+              fence_proxy_async_smem();
+              fuse_issue_chunk<TT>(seq, mats, views, kk, ll, rc.slot, ring_base, recs, full_bar, issue_cnt);
+            }
+          }
+          if (++rc.slot == R) { rc.slot = 0; rc.phase ^= 1u; }
+        }
+        if (!live) break;
+        float ta[9], tb[9], ga[9], gb[9];
+#pragma unroll
+        for (int c = 0; c < 9; ++c) {
+          const float2 t = clamp2(sp[c * NT]);
+          ta[c] = t.x;
+          tb[c] = t.y;
+        }
+        adj_to_params(ta, ma, aa, r0.scale, ga);
+        adj_to_params(tb, mb, ab, r0.scale, gb);
+#pragma unroll
+        for (int c = 0; c < 9; ++c) g[c] = make_float2(ga[c], gb[c]);
+        loss2 = make_float2(la, lb);
+      }
+      float loss = 0.f;
+      if (active) {
+        const AdamScalars ad = s_adam[it];
+        const bool last = it + 1 == iters;
+        const int T = r0.W * r0.H, idx = r0.first + 2 * tid;
+        float* tex = r0.tex;
+        float* gm1 = r0.m1;
+        float* gm2 = r0.m2;
+#pragma unroll
+        for (int c = 0; c < 9; ++c) {
+          float2 p = sp[c * NT], m1 = sp[(9 + c) * NT], m2 = sp[(18 + c) * NT];
+          const float2 gc = make_float2(fabsf(p.x) <= 1.0f ? g[c].x : 0.0f, fabsf(p.y) <= 1.0f ? g[c].y : 0.0f);
+          adam_update2(p, m1, m2, gc, ad);
+          if (last) {
+            const size_t off = (size_t)c * T + idx;
+            *reinterpret_cast<float2*>(tex + off) = p;
+            *reinterpret_cast<float2*>(gm1 + off) = m1;
+            *reinterpret_cast<float2*>(gm2 + off) = m2;
+          } else {
+            sw[c * NT] = p;
+            sw[(9 + c) * NT] = m1;
+            sw[(18 + c) * NT] = m2;
+          }
+        }
+        loss = loss2.x + loss2.y;
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, o);
+      if (lane == 0) warp_loss[((size_t)it * n_tiles + r0.tile) * NCW + warp] = loss;
+    }
+    if (!live) break;
+    // this warp's state writes come before the next tile's bulk copies into the area
+    fence_proxy_async_smem();
+    if (fuse_count_out(&st_rel, NCW) && k + 1 < k1) {
+      fence_proxy_async_smem();
+      fuse_issue_state<TT>(seq, mats, k + 1, state_base, &s_rec, &state_full, &st_issued);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && *(volatile int*)err != 0) {
+    // drain: every copy this CTA issued must land before the CTA's shared memory goes away
+    for (int s = 0; s < R; ++s) {
+      if (issue_cnt[s] == 0) continue;
+      uint32_t it = 0;
+      while (!mbar_try_wait(smem_u32(&full_bar[s]), (uint32_t)((issue_cnt[s] - 1) & 1))) {
+        if (++it >= kSpinLimit) { atomicCAS(err, 0, kDevTimeoutDrain); break; }
+      }
+    }
+    if (st_issued > 0) {
+      uint32_t it = 0;
+      while (!mbar_try_wait(smem_u32(&state_full), (uint32_t)((st_issued - 1) & 1))) {
+        if (++it >= kSpinLimit) { atomicCAS(err, 0, kDevTimeoutDrain); break; }
+      }
+    }
+  }
+  batched_finish<NT>(plan, hdr, mats, warp_loss, NCW, loss_hist, hist_len, s_step, step_counter,
+                     ws + kWsCounter, &s_last, NCW, iters);
+}
+
 // ============================================================== planner
 static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
@@ -1401,8 +1753,9 @@ static size_t pair_ring_budget(int threads) {
 }
 // variant 3: the state area (27 planes of the tile) comes out of the budget first
 static size_t fuse_state_bytes(int threads) { return (size_t)kStatePlanes * 2 * threads * 4; }
-static int fuse_ring(int threads) {
-  const size_t budget = threads / 32 <= kPairTwoCtaNcw ? kFuseBudgetTwoCta : kFuseBudget;
+static int fuse_ring(int threads, int variant) {
+  const bool two = variant == 4 ? threads / 32 <= kFuse2TwoCtaNcw : threads / 32 <= kPairTwoCtaNcw;
+  const size_t budget = variant == 4 ? (two ? kFuse2BudgetTwoCta : kFuse2Budget) : (two ? kFuseBudgetTwoCta : kFuseBudget);
   const size_t state = fuse_state_bytes(threads);
   if (state >= budget) return 0;
   return (int)std::min<size_t>(kMaxRing, (budget - state) / pair_slot_bytes(threads));
@@ -1412,7 +1765,7 @@ static int plan_layout(const svbrdf_material* mats, int n, const svbrdf_batch_co
   if (!mats || n <= 0) return fail(SVBRDF_ERR_INVALID, "no materials");
   if (!cfg) return fail(SVBRDF_ERR_INVALID, "null config");
   const int variant = cfg->variant;
-  if (variant < 0 || variant > 3) return fail(SVBRDF_ERR_INVALID, "variant must be 0, 1, 2 or 3 (got %d)", variant);
+  if (variant < 0 || variant > 4) return fail(SVBRDF_ERR_INVALID, "variant must be 0 .. 4 (got %d)", variant);
   if (variant == 0) {
     if (cfg->threads != 128 && cfg->threads != 256 && cfg->threads != 512)
       return fail(SVBRDF_ERR_UNSUPPORTED, "threads must be 128, 256 or 512 (got %d)", cfg->threads);
@@ -1435,6 +1788,11 @@ static int plan_layout(const svbrdf_material* mats, int n, const svbrdf_batch_co
                   cfg->threads);
     if (variant == 3 && cfg->tile_texels != 2 * cfg->threads)
       return fail(SVBRDF_ERR_INVALID, "resident-state variant: tile_texels must be twice threads");
+    if (variant == 4 && cfg->threads != 256 && cfg->threads != 512)
+      return fail(SVBRDF_ERR_UNSUPPORTED, "producer-less resident-state variant: threads must be 256 or 512 (got %d)",
+                  cfg->threads);
+    if (variant == 4 && cfg->tile_texels != 2 * cfg->threads)
+      return fail(SVBRDF_ERR_INVALID, "producer-less resident-state variant: tile_texels must be twice threads");
   }
   long long tiles = 0, coords = 0;
   int views = 0, max_views = 0;
@@ -1468,9 +1826,9 @@ static int plan_layout(const svbrdf_material* mats, int n, const svbrdf_batch_co
   L.coord_floats = coords;
   L.ring = variant == 1   ? (int)std::min<size_t>(kMaxRing, kRingBudget / slot_bytes(cfg->threads))
            : variant == 2 ? (int)std::min<size_t>(kMaxRing, pair_ring_budget(cfg->threads) / pair_slot_bytes(cfg->threads))
-           : variant == 3 ? fuse_ring(cfg->threads)
+           : variant >= 3 ? fuse_ring(cfg->threads, variant)
                           : 0;
-  if (variant == 3 && L.ring < 2)
+  if (variant >= 3 && L.ring < 2)
     return fail(SVBRDF_ERR_UNSUPPORTED, "resident-state variant: %d threads leave room for %d ring slots", cfg->threads,
                 L.ring);
   // variant 1 holds a tile's parameter slot until its last chunk (S) has been read, so
@@ -1532,6 +1890,13 @@ static size_t fuse_smem(int ring) {
 }
 
 template <int LOSS, int NCW, bool GEN>
+static int fuse2_prepare(int ring) {
+  static int done = 0;
+  static size_t have = 0;
+  return allow_smem(batched_fuse2_kernel<LOSS, NCW, GEN>, fuse_smem<NCW>(ring), done, have);
+}
+
+template <int LOSS, int NCW, bool GEN>
 static int fuse_prepare(int ring) {
   static int done = 0;
   static size_t have = 0;
@@ -1549,6 +1914,7 @@ int resident_ctas(int variant, int threads) {
   const int sms = device_sm_count();
   if (sms <= 0) return 0;
   // one pipelined CTA per SM (its ring takes the shared memory); two for the small texel-pair shape
+  if (variant == 4) return threads / 32 <= kFuse2TwoCtaNcw ? 2 * sms : sms;
   if (variant >= 2 && threads / 32 <= kPairTwoCtaNcw) return 2 * sms;
   if (variant >= 1) return sms;
   int occ = 1;
@@ -1815,7 +2181,7 @@ size_t svbrdf_batched_workspace_bytes(const void* host_plan) {
   const PlanHeader* h = (const PlanHeader*)host_plan;
   if (h->magic != kPlanMagic) return 0;
   const size_t per_tile = h->variant >= 1 ? (size_t)(h->threads / 32) : 1;
-  const size_t iters = h->variant == 3 ? (size_t)kFuseMax : 1;  // partials of every iteration of a launch
+  const size_t iters = h->variant >= 3 ? (size_t)kFuseMax : 1;  // partials of every iteration of a launch
   return kWsLossOffset + sizeof(float) * (size_t)h->n_tiles * per_tile * iters;
 }
 
@@ -1853,7 +2219,7 @@ int svbrdf_batched_steps(const void* device_plan, const void* host_plan, int los
   hyper.eps = eps;
   cudaStream_t st = (cudaStream_t)stream;
   const char* plan = (const char*)device_plan;
-  if (h->variant != 3) {
+  if (h->variant < 3) {
     for (int i = 0; i < iters; ++i) {
       const int rc = batched_launch_one(h, plan, loss_kind, step_counter, hyper, loss_hist, hist_len, ws, part, st);
       if (rc) return rc;
@@ -1869,16 +2235,28 @@ int svbrdf_batched_steps(const void* device_plan, const void* host_plan, int los
 #define SVB_F(L, NCW, G)                                                                                       {                                                                                                              int prc = fuse_prepare<L, NCW, G>(ring);                                                                     if (prc) return prc;                                                                                         batched_fuse_kernel<L, NCW, G><<<h->n_ctas, (NCW + 1) * 32, fuse_smem<NCW>(ring), st>>>(                         plan, hyper, step_counter, loss_hist, hist_len, k, part, ws);                                          }
 #define SVB_FG(L, NCW)                  if (h->general) SVB_F(L, NCW, true)   else SVB_F(L, NCW, false)
 #define SVB_FL(NCW)                                         if (loss_kind == SVBRDF_LOSS_MSE) SVB_FG(0, NCW)          else if (loss_kind == SVBRDF_LOSS_LOG1P) SVB_FG(1, NCW)   else SVB_FG(2, NCW)
-    switch (h->threads) {
-      case 224: SVB_FL(7) break;
-      case 256: SVB_FL(8) break;
-      case 384: SVB_FL(12) break;
-      default: SVB_FL(15) break;
+    if (h->variant == 3) {
+      switch (h->threads) {
+        case 224: SVB_FL(7) break;
+        case 256: SVB_FL(8) break;
+        case 384: SVB_FL(12) break;
+        default: SVB_FL(15) break;
+      }
     }
 #undef SVB_FL
 #undef SVB_FG
 #undef SVB_F
-    const int rc = check_launch("batched_fuse_kernel");
+#define SVB_F2(L, NCW, G)                                                                                      {                                                                                                              int prc = fuse2_prepare<L, NCW, G>(ring);                                                                    if (prc) return prc;                                                                                         batched_fuse2_kernel<L, NCW, G><<<h->n_ctas, NCW * 32, fuse_smem<NCW>(ring), st>>>(                              plan, hyper, step_counter, loss_hist, hist_len, k, part, ws);                                          }
+#define SVB_F2G(L, NCW)                  if (h->general) SVB_F2(L, NCW, true)   else SVB_F2(L, NCW, false)
+#define SVB_F2L(NCW)                                         if (loss_kind == SVBRDF_LOSS_MSE) SVB_F2G(0, NCW)          else if (loss_kind == SVBRDF_LOSS_LOG1P) SVB_F2G(1, NCW)   else SVB_F2G(2, NCW)
+    if (h->variant == 4) {
+      if (h->threads == 256) SVB_F2L(8)
+      else SVB_F2L(16)
+    }
+#undef SVB_F2L
+#undef SVB_F2G
+#undef SVB_F2
+    const int rc = check_launch(h->variant == 3 ? "batched_fuse_kernel" : "batched_fuse2_kernel");
     if (rc) return rc;
   }
   return SVBRDF_OK;

@@ -24,7 +24,8 @@ def _batch(svb, cuda, n=6, general=True):
     (1, 256, 256, True), (1, 384, 384, True), (1, 480, 480, True), (1, 608, 608, True),
     (2, 256, 512, True), (2, 384, 768, True), (2, 480, 960, True),
     (2, 480, 960, False), (2, 256, 512, False), (2, 224, 448, True), (2, 224, 448, False),
-    (3, 480, 960, True), (3, 480, 960, False), (3, 224, 448, True), (3, 384, 768, False)])
+    (3, 480, 960, True), (3, 480, 960, False), (3, 224, 448, True), (3, 384, 768, False),
+    (4, 512, 1024, True), (4, 512, 1024, False), (4, 256, 512, True), (4, 256, 512, False)])
 def test_batched_equals_single(svb, cuda, variant, threads, tile, general):
     """`general` puts one material's light off the camera; without it every view is
     co-located and the texel-pair variant launches its instantiation without the general
@@ -113,12 +114,13 @@ def test_autotune_picks_a_valid_config(svb, cuda, tmp_path, monkeypatch):
     assert torch.isfinite(b.loss_out).all()
 
 
-@pytest.mark.parametrize("variant", [2, 3])
+@pytest.mark.parametrize("variant", [2, 3, 4])
 def test_pipeline_matches_sequential_batches(svb, cuda, variant):
     """BatchedPipeline (two buffers, copies on side streams) gives each batch exactly the
     maps and losses that a sequential reset + run of BatchedOptim gives it."""
     mats = _batch(svb, cuda, n=4, general=False)
-    cfg = svb.BatchConfig(threads=480, tile_texels=960, ctas=0, variant=variant)
+    threads = 512 if variant == 4 else 480
+    cfg = svb.BatchConfig(threads=threads, tile_texels=2 * threads, ctas=0, variant=variant)
     g = torch.Generator().manual_seed(5)
     batches = []
     for _ in range(3):
@@ -156,14 +158,16 @@ def _single(svb, cuda, m, iters):
     return o
 
 
-@pytest.mark.parametrize("threads,general,iters", [
-    (480, False, 7), (480, True, 7), (224, False, 9), (256, True, 5), (384, False, 6), (480, False, 45)])
-def test_resident_state_equals_single(svb, cuda, threads, general, iters):
-    """Variant 3 runs `iters` iterations per launch (45: two launches of 23 and 22) on the
-    shared-memory state; every material's maps, moments and per-iteration losses must match
-    the single-material optimiser's."""
+@pytest.mark.parametrize("variant,threads,general,iters", [
+    (3, 480, False, 7), (3, 480, True, 7), (3, 224, False, 9), (3, 256, True, 5), (3, 384, False, 6),
+    (3, 480, False, 45), (4, 512, False, 7), (4, 512, True, 7), (4, 256, False, 9), (4, 256, True, 5),
+    (4, 512, False, 45), (4, 512, False, 1)])
+def test_resident_state_equals_single(svb, cuda, variant, threads, general, iters):
+    """Variants 3 and 4 run `iters` iterations per launch (45: two launches of 23 and 22) on
+    the shared-memory state; every material's maps, moments and per-iteration losses must
+    match the single-material optimiser's."""
     mats = _batch(svb, cuda, general=general)
-    cfg = svb.BatchConfig(threads=threads, tile_texels=2 * threads, ctas=5, variant=3)
+    cfg = svb.BatchConfig(threads=threads, tile_texels=2 * threads, ctas=5, variant=variant)
     b = svb.BatchedOptim(mats, lr=0.01, loss="log1p", device=cuda, config=cfg, hist_len=iters)
     b.run(iters)
     assert b.device_error() == 0
@@ -176,13 +180,13 @@ def test_resident_state_equals_single(svb, cuda, threads, general, iters):
             assert abs(float(b.loss_hist[k, i]) - o.loss_image_list[k]) <= 1e-6 * o.loss_image_list[k]
 
 
-def test_resident_state_matches_pair_variant(svb, cuda):
-    """Variant 3 against variant 2 (one launch per iteration) over 70 iterations: three
-    launches of 24, 23 and 23 iterations, then single-iteration steps, on the same plan
-    shape."""
+@pytest.mark.parametrize("variant,threads", [(3, 480), (4, 512), (4, 256)])
+def test_resident_state_matches_pair_variant(svb, cuda, variant, threads):
+    """Variants 3 and 4 against variant 2 (one launch per iteration) over 70 iterations:
+    three launches of 24, 23 and 23 iterations, then single-iteration steps."""
     mats = _batch(svb, cuda, n=5, general=False)
     a = svb.BatchedOptim(mats, device=cuda, config=svb.BatchConfig(480, 960, 0, 2), hist_len=75)
-    b = svb.BatchedOptim(mats, device=cuda, config=svb.BatchConfig(480, 960, 0, 3), hist_len=75)
+    b = svb.BatchedOptim(mats, device=cuda, config=svb.BatchConfig(threads, 2 * threads, 0, variant), hist_len=75)
     a.run(70)
     b.run(70)
     for _ in range(5):
@@ -196,17 +200,18 @@ def test_resident_state_matches_pair_variant(svb, cuda):
     assert int(b.step_dev.item()) == 75
 
 
+@pytest.mark.parametrize("variant,threads", [(3, 480), (4, 512), (4, 256)])
 @pytest.mark.parametrize("general", [False, True])
-def test_resident_state_many_views(svb, cuda, general):
-    """40 views: 14 target chunks per iteration through variant 3's 3-slot ring, 6
-    iterations per launch."""
+def test_resident_state_many_views(svb, cuda, general, variant, threads):
+    """40 views: 14 target chunks per iteration through a 2- or 3-slot ring, 6 iterations
+    per launch."""
     from oracle import microfacet_ref as R
     mats = svb.scenes.batched_scenes(n=2, resolutions=(32,), vmin=40, vmax=40,
                                      render_fn=lambda *a: R.render(*a, dtype=torch.float32))
     if general:
         mats[0].light_pos = mats[0].light_pos + torch.tensor([0.5, 1.0, -2.0])
     b = svb.BatchedOptim(mats, lr=0.01, loss="log1p", device=cuda,
-                         config=svb.BatchConfig(threads=480, tile_texels=960, ctas=2, variant=3))
+                         config=svb.BatchConfig(threads=threads, tile_texels=2 * threads, ctas=2, variant=variant))
     b.run(6)
     assert b.device_error() == 0
     for i, m in enumerate(mats):

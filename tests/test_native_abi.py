@@ -180,21 +180,22 @@ def test_pair_plan_requirements_and_ring(svb, lib):
     assert ring7 * slot7 <= budget7 < (ring7 + 1) * slot7
 
 
-@pytest.mark.parametrize("threads,budget,ring", [(480, 220, 3), (384, 220, 5), (256, 220, 9), (224, 100, 3)])
-def test_resident_state_plan_ring_and_workspace(svb, lib, threads, budget, ring):
-    """Variant 3: the 27-plane state area comes out of the shared-memory budget before the
-    ring of 9-plane target slots; the workspace holds partials for 32 iterations."""
+@pytest.mark.parametrize("variant,threads,budget,ring", [(3, 480, 220, 3), (3, 384, 220, 5), (3, 256, 220, 9),
+                                                          (3, 224, 100, 3), (4, 512, 220, 3), (4, 256, 100, 2)])
+def test_resident_state_plan_ring_and_workspace(svb, lib, variant, threads, budget, ring):
+    """Variants 3 and 4: the 27-plane state area comes out of the shared-memory budget before
+    the ring of 9-plane target slots; the workspace holds partials for 32 iterations."""
     SV = svb._native
     mats, keep = _materials(SV, [(64, 64, 9), (32, 32, 5)])
     tt = 2 * threads
-    cfg = SV.svbrdf_batch_config(threads, tt, 3, 3)
+    cfg = SV.svbrdf_batch_config(threads, tt, 3, variant)
     n = lib.svbrdf_batched_plan_bytes(mats, 2, ctypes.byref(cfg))
     assert n > 0
     buf = np.zeros(n, np.uint8)
     assert lib.svbrdf_batched_plan(mats, 2, ctypes.byref(cfg), buf.ctypes.data, n) == 0
     hdr = np.frombuffer(buf[:72].tobytes(), np.int32)
-    n_tiles, variant, got = hdr[2], hdr[13], hdr[14]
-    assert variant == 3 and got == ring
+    n_tiles, got = hdr[2], hdr[14]
+    assert hdr[13] == variant and got == ring
     state, slot = 27 * tt * 4, 9 * tt * 4 + 288
     assert state + ring * slot <= budget * 1024 < state + (ring + 1) * slot
     assert lib.svbrdf_batched_workspace_bytes(buf.ctypes.data) == 256 + 4 * n_tiles * (threads // 32) * 32

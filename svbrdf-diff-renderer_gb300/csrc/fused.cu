@@ -1234,8 +1234,8 @@ batched_fuse_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
   } else {
     // ------------------------------------------------------------ consumers
     const int tid = threadIdx.x;
-    const float2* sp = reinterpret_cast<const float2*>(state) + tid;  // plane c at sp[c * NT]
-    float2* sw = reinterpret_cast<float2*>(state) + tid;
+    float2* sw = reinterpret_cast<float2*>(state) + tid;  // plane c at sw[c * NT]
+    const float2* sp = sw;
     RingCursor rc{0, 0u, true};
     uint32_t sfp = 0;
     for (int k = k0; k < k1; ++k) {

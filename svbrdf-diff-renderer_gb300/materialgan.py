@@ -466,15 +466,19 @@ class MaterialGANOptim:
         is one CUDA-graph replay."""
         total, l_ep, n_ep = epochs
         cycle = l_ep + n_ep
+        # this call's losses stay on the device and are read once at the end; the lists
+        # accumulate over calls, as the reference's do
+        img_losses, feat_losses = [], []
         if graph and reset_adam_each_iter and self.descriptor is None and self.device.type == "cuda":
             for epoch in range(total):
                 g, loss, _ = self._graph_for((epoch % cycle) < l_ep, lr)
                 g.replay()
-                self.loss_image_list.append(loss.detach().clone())
+                img_losses.append(loss.detach().clone())
             for p in (self.latent, *self.noises):
                 p.grad = None
             self.textures = self.latent_to_textures().detach()
-            self.loss_image_list = [float(x) for x in torch.stack(self.loss_image_list).tolist()]
+            if img_losses:
+                self.loss_image_list += [float(x) for x in torch.stack(img_losses).tolist()]
             return self.textures
         opt = None
         for epoch in range(total):
@@ -486,20 +490,21 @@ class MaterialGANOptim:
             textures = self.latent_to_textures()
             rendered = self.renderer_obj.eval(textures)
             loss = torch.nn.functional.mse_loss(rendered, self.targets)
-            self.loss_image_list.append(loss.detach())
+            img_losses.append(loss.detach())
             if self.descriptor is not None:
                 from .descriptor import descriptor_term
 
                 fl = descriptor_term(rendered, self.descriptor) * self.descriptor_weight
-                self.loss_feature_list.append(fl.detach())
+                feat_losses.append(fl.detach())
                 loss = loss + fl
             opt.zero_grad()
             loss.backward()
             opt.step()
         self.textures = self.latent_to_textures().detach()
-        self.loss_image_list = [float(x) for x in torch.stack(self.loss_image_list).tolist()]
-        self.loss_feature_list = [float(x) for x in torch.stack(self.loss_feature_list).tolist()] \
-            if self.loss_feature_list else []
+        if img_losses:
+            self.loss_image_list += [float(x) for x in torch.stack(img_losses).tolist()]
+        if feat_losses:
+            self.loss_feature_list += [float(x) for x in torch.stack(feat_losses).tolist()]
         return self.textures
 
 

@@ -65,6 +65,11 @@ def test_latent_loop_through_gpu_renderer(svb, cuda):
     assert tex.shape == (2, 9, 256, 256)
     assert len(o.loss_image_list) == 12
     assert min(o.loss_image_list[-4:]) < o.loss_image_list[0]
+    # a second call continues from the current latent and appends its losses, on both the
+    # graph path and the eager one
+    o.optim([3, 2, 1], 0.02)
+    o.optim([2, 1, 1], 0.02, graph=False)
+    assert len(o.loss_image_list) == 17 and all(isinstance(x, float) for x in o.loss_image_list)
 
 
 @pytest.mark.gpu

@@ -288,6 +288,38 @@ int svbrdf_gen_act_bwd(const float* gout, const float* y, const float* d, const 
                        const float* bias, float gain, float* gy, float* gd, float* gnoise, int b, int c, int hw,
                        void* stream);
 
+/* ---- the same generator work on channels-last maps [b][h][w][c] (the layout cuDNN's
+ * convolutions run in, so the generator needs no NCHW<->NHWC conversions). float4 over channels
+ * when c % 4 == 0 and the maps are 16-byte aligned. The backward calls with column sums take a
+ * scratch `part` of svbrdf_gen_nhwc_partial_floats(b, c) floats and are deterministic. ---- */
+
+/* Floats of the `part` scratch the *_nhwc_bwd calls need. */
+int svbrdf_gen_nhwc_partial_floats(int b, int c);
+
+/* y [b][2h][2w][c] = 2x up-sampling (as svbrdf_gen_upsample2) of x [b][h][w][c], times s[b][c]
+ * when s is not null. */
+int svbrdf_gen_upsample2_nhwc(const float* x, const float* s, float* y, int b, int h, int w, int c, void* stream);
+
+/* Adjoint of the up-sampling: gx [b][h][w][c] from g [b][2h][2w][c]. */
+int svbrdf_gen_upsample2_nhwc_bwd(const float* g, float* gx, int b, int h, int w, int c, void* stream);
+
+/* y[b][p][c] = x[b][p][c] s[b][c], hw pixels. */
+int svbrdf_gen_scale_nhwc(const float* x, const float* s, float* y, int b, int hw, int c, void* stream);
+
+/* gx = g s[b][c]; gs[b][c] = sum_p g x. c / 4 (c % 4 == 0) or c at most 256. */
+int svbrdf_gen_scale_nhwc_bwd(const float* g, const float* x, const float* s, float* gx, float* gs, float* part, int b,
+                              int hw, int c, void* stream);
+
+/* out = lrelu(y d[b][c] + ns noise[b][p] + bias[c], 0.2) gain; d and noise nullable. */
+int svbrdf_gen_act_nhwc(const float* y, const float* d, const float* noise, const float* ns, const float* bias,
+                        float gain, float* out, int b, int hw, int c, void* stream);
+
+/* Adjoint of svbrdf_gen_act_nhwc: gy, gd[b][c] = sum_p gpre y (nullable), gnoise[b][p] =
+ * ns sum_c gpre (nullable). */
+int svbrdf_gen_act_nhwc_bwd(const float* gout, const float* y, const float* d, const float* noise, const float* ns,
+                            const float* bias, float gain, float* gy, float* gd, float* gnoise, float* part, int b,
+                            int hw, int c, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -20,7 +20,7 @@ CSRC = PKG / "csrc"
 INCLUDE = REPO / "include"
 LIBDIR = PKG / "_lib"
 LIBNAME = "libsvbrdf_gb300.so"
-SOURCES = ["render.cu", "fused.cu", "conv_tc.cu", "desc_ops.cu", "gen_ops.cu"]
+SOURCES = ["render.cu", "fused.cu", "conv_tc.cu", "desc_ops.cu", "gen_ops.cu", "gen_nhwc.cu"]
 HEADERS = ["svbrdf_math.cuh", "svbrdf_common.cuh", "svbrdf_plan.cuh"]
 WORKSPACE_ERROR_OFFSET = 4
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -150,6 +150,20 @@ def _declare(L):
     L.svbrdf_gen_act.argtypes = [P, P, P, P, P, F, P, I, I, I, P]
     L.svbrdf_gen_act_bwd.restype = I
     L.svbrdf_gen_act_bwd.argtypes = [P, P, P, P, P, P, F, P, P, P, I, I, I, P]
+    L.svbrdf_gen_nhwc_partial_floats.restype = I
+    L.svbrdf_gen_nhwc_partial_floats.argtypes = [I, I]
+    L.svbrdf_gen_upsample2_nhwc.restype = I
+    L.svbrdf_gen_upsample2_nhwc.argtypes = [P, P, P, I, I, I, I, P]
+    L.svbrdf_gen_upsample2_nhwc_bwd.restype = I
+    L.svbrdf_gen_upsample2_nhwc_bwd.argtypes = [P, P, I, I, I, I, P]
+    L.svbrdf_gen_scale_nhwc.restype = I
+    L.svbrdf_gen_scale_nhwc.argtypes = [P, P, P, I, I, I, P]
+    L.svbrdf_gen_scale_nhwc_bwd.restype = I
+    L.svbrdf_gen_scale_nhwc_bwd.argtypes = [P, P, P, P, P, P, I, I, I, P]
+    L.svbrdf_gen_act_nhwc.restype = I
+    L.svbrdf_gen_act_nhwc.argtypes = [P, P, P, P, P, F, P, I, I, I, P]
+    L.svbrdf_gen_act_nhwc_bwd.restype = I
+    L.svbrdf_gen_act_nhwc_bwd.argtypes = [P, P, P, P, P, P, F, P, P, P, P, I, I, I, P]
     L.svbrdf_batched_plan_bytes.restype = S
     L.svbrdf_batched_plan_bytes.argtypes = [ctypes.POINTER(svbrdf_material), I, ctypes.POINTER(svbrdf_batch_config)]
     L.svbrdf_batched_plan.restype = I
@@ -172,6 +186,8 @@ EXPORTS = [
     "svbrdf_conv3x3_bf16_ex", "svbrdf_desc_partials", "svbrdf_desc_conv1_fwd", "svbrdf_desc_conv1_bwd",
     "svbrdf_desc_pool_fwd", "svbrdf_desc_pool_bwd", "svbrdf_desc_feat_loss", "svbrdf_gen_upsample2",
     "svbrdf_gen_upsample2_bwd", "svbrdf_gen_upsample2_scaled", "svbrdf_gen_scale", "svbrdf_gen_scale_bwd", "svbrdf_gen_act", "svbrdf_gen_act_bwd",
+    "svbrdf_gen_nhwc_partial_floats", "svbrdf_gen_upsample2_nhwc", "svbrdf_gen_upsample2_nhwc_bwd",
+    "svbrdf_gen_scale_nhwc", "svbrdf_gen_scale_nhwc_bwd", "svbrdf_gen_act_nhwc", "svbrdf_gen_act_nhwc_bwd",
 ]
 
 

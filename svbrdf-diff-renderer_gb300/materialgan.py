@@ -132,14 +132,137 @@ class _Upsample2Cuda(torch.autograd.Function):
 def _upsample2(x):
     """2x up-sampling (zero insertion + [1,3,3,1] FIR, gain 4), computed separably in
     polyphase form: the same function as _upsample2_fir without multiplying the zeros. On the
-    GPU (FP32) it is one kernel each way; the torch form serves CPU tensors."""
+    GPU (FP32) it is one kernel each way, in the map's layout; the torch form serves CPU
+    tensors."""
     if x.is_cuda and x.dtype == torch.float32:
-        return _Upsample2Cuda.apply(x)
+        return _UpsampleNHWC.apply(x, None) if _is_nhwc(x) else _Upsample2Cuda.apply(x)
     return _up1d(_up1d(x, -1), -2)
 
 
 def _use_kernels(x):
     return x.is_cuda and x.dtype == torch.float32
+
+
+CL = torch.channels_last
+
+
+def _is_nhwc(x):
+    """A channels-last map (and not also a plain contiguous one, as C = 1 maps are)."""
+    return x.dim() == 4 and x.is_contiguous(memory_format=CL) and not x.is_contiguous()
+
+
+def _cl(t):
+    return t.contiguous(memory_format=CL)
+
+
+class _UpsampleNHWC(torch.autograd.Function):
+    """2x up-sampling of channels-last maps, optionally of x[b, c] * s[b, c] (the modulation
+    of an up-sampling conv) in the same kernel (svbrdf_gen_upsample2_nhwc). The backward is
+    the up-sampling adjoint, then with s svbrdf_gen_scale_nhwc_bwd for the input and style
+    gradients."""
+
+    @staticmethod
+    def forward(ctx, x, s):
+        from . import _native as N
+
+        x = _cl(x)
+        s = s.contiguous() if s is not None else None
+        b, c, h, w = x.shape
+        y = torch.empty(b, c, 2 * h, 2 * w, device=x.device, dtype=torch.float32, memory_format=CL)
+        N.check(N.lib().svbrdf_gen_upsample2_nhwc(x.data_ptr(), s.data_ptr() if s is not None else None, y.data_ptr(),
+                                                  b, h, w, c, N.stream_handle(x.device)))
+        ctx.save_for_backward(x, s)
+        return y
+
+    @staticmethod
+    def backward(ctx, g):
+        from . import _native as N
+
+        x, s = ctx.saved_tensors
+        b, c, h, w = x.shape
+        L, st = N.lib(), N.stream_handle(x.device)
+        g = _cl(g)
+        gu = torch.empty_like(x)
+        N.check(L.svbrdf_gen_upsample2_nhwc_bwd(g.data_ptr(), gu.data_ptr(), b, h, w, c, st))
+        if s is None:
+            return gu, None
+        gx = torch.empty_like(x)
+        gs = torch.empty(b, c, device=x.device, dtype=torch.float32)
+        part = torch.empty(L.svbrdf_gen_nhwc_partial_floats(b, c), device=x.device, dtype=torch.float32)
+        N.check(L.svbrdf_gen_scale_nhwc_bwd(gu.data_ptr(), x.data_ptr(), s.data_ptr(), gx.data_ptr(), gs.data_ptr(),
+                                            part.data_ptr(), b, h * w, c, st))
+        return gx, gs
+
+
+class _ScaleNHWC(torch.autograd.Function):
+    """x[b, c] * s[b, c] on channels-last maps (svbrdf_gen_scale_nhwc[_bwd])."""
+
+    @staticmethod
+    def forward(ctx, x, s):
+        from . import _native as N
+
+        x, s = _cl(x), s.contiguous()
+        b, c, h, w = x.shape
+        y = torch.empty_like(x)
+        N.check(N.lib().svbrdf_gen_scale_nhwc(x.data_ptr(), s.data_ptr(), y.data_ptr(), b, h * w, c,
+                                              N.stream_handle(x.device)))
+        ctx.save_for_backward(x, s)
+        return y
+
+    @staticmethod
+    def backward(ctx, g):
+        from . import _native as N
+
+        x, s = ctx.saved_tensors
+        b, c, h, w = x.shape
+        L = N.lib()
+        g = _cl(g)
+        gx = torch.empty_like(x)
+        gs = torch.empty(b, c, device=x.device, dtype=torch.float32)
+        part = torch.empty(L.svbrdf_gen_nhwc_partial_floats(b, c), device=x.device, dtype=torch.float32)
+        N.check(L.svbrdf_gen_scale_nhwc_bwd(g.data_ptr(), x.data_ptr(), s.data_ptr(), gx.data_ptr(), gs.data_ptr(),
+                                            part.data_ptr(), b, h * w, c, N.stream_handle(x.device)))
+        return gx, gs
+
+
+class _ActNHWC(torch.autograd.Function):
+    """The style layer's epilogue on channels-last maps (svbrdf_gen_act_nhwc[_bwd]); the
+    arguments are those of _ActCuda."""
+
+    @staticmethod
+    def forward(ctx, y, d, noise, ns, bias, gain):
+        from . import _native as N
+
+        y, d, bias = _cl(y), d.contiguous(), bias.contiguous()
+        noise = noise.contiguous() if noise is not None else None
+        b, c, h, w = y.shape
+        out = torch.empty_like(y)
+        N.check(N.lib().svbrdf_gen_act_nhwc(y.data_ptr(), d.data_ptr(), noise.data_ptr() if noise is not None else None,
+                                            ns.data_ptr() if noise is not None else None, bias.data_ptr(), gain,
+                                            out.data_ptr(), b, h * w, c, N.stream_handle(y.device)))
+        ctx.save_for_backward(y, d, noise, ns, bias)
+        ctx.gain = gain
+        return out
+
+    @staticmethod
+    def backward(ctx, g):
+        from . import _native as N
+
+        y, d, noise, ns, bias = ctx.saved_tensors
+        b, c, h, w = y.shape
+        L = N.lib()
+        g = _cl(g)
+        gy = torch.empty_like(y)
+        gd = torch.empty(b, c, device=y.device, dtype=torch.float32)
+        want_noise = noise is not None and ctx.needs_input_grad[2]
+        gn = torch.empty_like(noise) if want_noise else None
+        part = torch.empty(L.svbrdf_gen_nhwc_partial_floats(b, c), device=y.device, dtype=torch.float32)
+        N.check(L.svbrdf_gen_act_nhwc_bwd(g.data_ptr(), y.data_ptr(), d.data_ptr(),
+                                          noise.data_ptr() if noise is not None else None,
+                                          ns.data_ptr() if noise is not None else None, bias.data_ptr(), ctx.gain,
+                                          gy.data_ptr(), gd.data_ptr(), gn.data_ptr() if want_noise else None,
+                                          part.data_ptr(), b, h * w, c, N.stream_handle(y.device)))
+        return gy, gd, gn, None, None, None
 
 
 class _ScaleCuda(torch.autograd.Function):
@@ -270,7 +393,11 @@ class _ModConv(torch.nn.Module):
         d [B, cout] (None without demodulation) still to be applied to its output."""
         s = self.affine(w)  # [B, cin]
         wsc = self.weight * self.scale
-        if self.up and _use_kernels(x) and x.shape[-1] % 4 == 0 and x.data_ptr() % 16 == 0:
+        if _use_kernels(x) and _is_nhwc(x):
+            # channels-last: the layout cuDNN's convolutions run in, so none converts its operands
+            x = _UpsampleNHWC.apply(x, s) if self.up else _ScaleNHWC.apply(x, s)
+            wsc = _cl(wsc)
+        elif self.up and _use_kernels(x) and x.shape[-1] % 4 == 0 and x.data_ptr() % 16 == 0:
             x = _UpScaleCuda.apply(x, s)  # the up-sampling commutes with the channel scaling
         else:
             x = _ScaleCuda.apply(x, s) if _use_kernels(x) else x * s[:, :, None, None]
@@ -295,7 +422,8 @@ class _StyleLayer(torch.nn.Module):
         if _use_kernels(x) and not (self.bias.requires_grad or self.noise_strength.requires_grad) and (
                 noise is None or (noise.shape[0] == x.shape[0] and noise.shape[1] == 1)):
             y, d = self.conv.parts(x, w)
-            return _ActCuda.apply(y, d, noise, self.noise_strength, self.bias, LRELU_GAIN)
+            act = _ActNHWC if _is_nhwc(y) else _ActCuda
+            return act.apply(y, d, noise, self.noise_strength, self.bias, LRELU_GAIN)
         y = self.conv(x, w)
         if noise is not None:
             y = y + self.noise_strength * noise
@@ -317,8 +445,10 @@ class StyleGAN2Generator(torch.nn.Module):
     """StyleGAN2-shaped generator (seeded random weights) producing [B, 9, res, res] textures."""
 
     def __init__(self, resolution: int = 256, w_dim: int = 512, out_channels: int = 9, seed: int = 0,
-                 fmap_base: int = 16384, fmap_max: int = 512, mapping_layers: int = 8):
+                 fmap_base: int = 16384, fmap_max: int = 512, mapping_layers: int = 8, channels_last: bool = True):
         super().__init__()
+        # on the GPU the feature maps run channels-last (NHWC), cuDNN's convolution layout
+        self.channels_last = channels_last
         g = torch.Generator().manual_seed(seed)
         self.resolution, self.w_dim = resolution, w_dim
         log2 = int(round(math.log2(resolution)))
@@ -366,6 +496,8 @@ class StyleGAN2Generator(torch.nn.Module):
         b = wp.shape[0]
         noises = noises if noises is not None else [None] * len(self.noise_res)
         x = self.const.expand(b, -1, -1, -1)
+        if self.channels_last and _use_kernels(x):
+            x = _cl(x)
         x = self.conv4(x, wp[:, 0], noises[0])
         img = self.rgb4(x, wp[:, 1], None)
         for i, (up, conv, rgb) in enumerate(zip(self.ups, self.convs, self.rgbs)):

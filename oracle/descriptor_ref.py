@@ -63,4 +63,4 @@ def loss_terms(renders, targets, weights, hook_weights=(0.25, 0.25, 0.25, 0.25),
     fl = fl / nf
     gl = gl / ng
     (fl + gl).backward()
-    return float(fl), float(gl), r.grad.detach()
+    return float(fl.detach()), float(gl.detach()), r.grad.detach()

@@ -49,4 +49,4 @@ def cuda():
 def rel_l2(a, b):
     a = a.double().cpu()
     b = b.double().cpu()
-    return float((a - b).norm() / b.norm().clamp_min(1e-300))
+    return float(((a - b).norm() / b.norm().clamp_min(1e-300)).detach())

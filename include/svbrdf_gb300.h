@@ -242,6 +242,12 @@ int svbrdf_desc_pool_fwd(const void* x, void* y, int v, int h, int w, int c, voi
 int svbrdf_desc_pool_bwd(const void* gy, const void* x, const void* addend, void* gx, int v, int h, int w, int c,
                          void* stream);
 
+/* The same pair with 2x2 average pools (the reference's VGGLoss replaces VGG19's max-pools
+ * with average pools, src/descriptor.py:16-19): each window element takes gy / 4. */
+int svbrdf_desc_avgpool_fwd(const void* x, void* y, int v, int h, int w, int c, void* stream);
+int svbrdf_desc_avgpool_bwd(const void* gy, const void* x, const void* addend, void* gx, int v, int h, int w, int c,
+                            void* stream);
+
 /* Feature term of one hook: partial[b] (b < svbrdf_desc_partials(), if partial) = block b's
  * share of sum (f - t)^2, a fixed-order split; if g: g = coef (f - t) + gram_grad (nullable),
  * times (f > 0) if `mask`, stored BF16. f is BF16 (f_is_bf16) or FP32, t and gram_grad FP32,

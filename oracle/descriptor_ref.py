@@ -7,6 +7,12 @@ conv1_1..conv4_1 (3x3, padding 1, ReLU, 2x2 max-pool), hooks at relu1_1, relu1_2
 relu4_1, and the weighted feature-L2 (src/descriptor.py:39-60, 77-79) and Gram (:50-56)
 terms. Runs in FP64 on the exact weights the BF16 kernels use, so the difference to the GPU
 measures the BF16 activations and FP32 tensor-core accumulation alone.
+
+mode="reference" restates the reference's own VGGLoss instead: full-resolution renders,
+VGG19 to relu4_2 with its max-pools replaced by 2x2 average pools (src/descriptor.py:16-19),
+hooks at features 1, 3, 13, 22 = relu1_1, relu1_2, relu3_2, relu4_2 (:26-27), and the
+feature MSE alone (:77-79). torchvision is absent here, so the reference module itself cannot
+be imported; the restatement follows its source line by line.
 """
 from __future__ import annotations
 
@@ -18,9 +24,13 @@ LAYERS = [("conv1_1", 3, 64), ("conv1_2", 64, 64), "pool", ("conv2_1", 64, 128),
           ("conv3_1", 128, 256), ("conv3_2", 256, 256), ("conv3_3", 256, 256), ("conv3_4", 256, 256), "pool",
           ("conv4_1", 256, 512)]
 HOOKS = ("conv1_1", "conv1_2", "conv3_2", "conv4_1")
+REF_LAYERS = LAYERS + [("conv4_2", 512, 512)]
+REF_HOOKS = ("conv1_1", "conv1_2", "conv3_2", "conv4_2")
 
 
-def features(renders, weights, downsample=True):
+def features(renders, weights, downsample=True, mode="config"):
+    ref = mode == "reference"
+    layers, hooks = (REF_LAYERS, REF_HOOKS) if ref else (LAYERS, HOOKS)
     x = renders.double()
     if downsample:
         x = torch.nn.functional.avg_pool2d(x, 2)
@@ -28,14 +38,14 @@ def features(renders, weights, downsample=True):
     std = torch.tensor(STD, dtype=torch.float64).view(1, 3, 1, 1)
     x = (x - mean) / std
     out = []
-    for item in LAYERS:
+    for item in layers:
         if item == "pool":
-            x = torch.nn.functional.max_pool2d(x, 2)
+            x = torch.nn.functional.avg_pool2d(x, 2) if ref else torch.nn.functional.max_pool2d(x, 2)
             continue
         name = item[0]
         w, b = weights[name]
         x = torch.relu(torch.nn.functional.conv2d(x, w.double(), b.double(), padding=1))
-        if name in HOOKS:
+        if name in hooks:
             out.append(x)
     return out
 
@@ -46,21 +56,26 @@ def gram(f):
     return torch.bmm(ff, ff.transpose(1, 2)) / (h * w)
 
 
-def loss_terms(renders, targets, weights, hook_weights=(0.25, 0.25, 0.25, 0.25), downsample=True):
-    """(feature_loss, gram_loss, d(feature+gram)/d renders) in FP64."""
+def loss_terms(renders, targets, weights, hook_weights=(0.25, 0.25, 0.25, 0.25), downsample=None, mode="config"):
+    """(feature_loss, gram_loss, d(feature+gram)/d renders) in FP64. In reference mode the
+    Gram loss is 0 and the renders are not downsampled."""
+    ref = mode == "reference"
+    downsample = (not ref) if downsample is None else downsample
     r = renders.detach().double().clone().requires_grad_(True)
     with torch.no_grad():
-        tf = features(targets, weights, downsample)
+        tf = features(targets, weights, downsample, mode)
         tg = [gram(f) for f in tf]
-    feats = features(r, weights, downsample)
+    feats = features(r, weights, downsample, mode)
     fl, gl, nf, ng = 0.0, 0.0, 0, 0
     for w, f, t, g_t in zip(hook_weights, feats, tf, tg):
+        # the reference's MSE of the concatenated weighted features (src/descriptor.py:39-60)
         fl = fl + (w * w) * ((f - t) ** 2).sum()
         nf += f.numel()
-        g = gram(f)
-        gl = gl + (w * w) * ((g - g_t) ** 2).sum()
-        ng += g.numel()
+        if not ref:
+            g = gram(f)
+            gl = gl + (w * w) * ((g - g_t) ** 2).sum()
+            ng += g.numel()
     fl = fl / nf
-    gl = gl / ng
+    gl = gl / ng if not ref else torch.zeros((), dtype=torch.float64)
     (fl + gl).backward()
     return float(fl.detach()), float(gl.detach()), r.grad.detach()

@@ -134,6 +134,10 @@ def _declare(L):
     L.svbrdf_desc_pool_fwd.argtypes = [P, P, I, I, I, I, P]
     L.svbrdf_desc_pool_bwd.restype = I
     L.svbrdf_desc_pool_bwd.argtypes = [P, P, P, P, I, I, I, I, P]
+    L.svbrdf_desc_avgpool_fwd.restype = I
+    L.svbrdf_desc_avgpool_fwd.argtypes = [P, P, I, I, I, I, P]
+    L.svbrdf_desc_avgpool_bwd.restype = I
+    L.svbrdf_desc_avgpool_bwd.argtypes = [P, P, P, P, I, I, I, I, P]
     L.svbrdf_desc_feat_loss.restype = I
     L.svbrdf_desc_feat_loss.argtypes = [P, I, P, P, F, I, P, P, ctypes.c_longlong, P]
     L.svbrdf_gen_upsample2.restype = I
@@ -184,7 +188,8 @@ EXPORTS = [
     "svbrdf_batched_plan_bytes",
     "svbrdf_batched_plan", "svbrdf_batched_workspace_bytes", "svbrdf_batched_step", "svbrdf_batched_steps", "svbrdf_conv3x3_bf16",
     "svbrdf_conv3x3_bf16_ex", "svbrdf_desc_partials", "svbrdf_desc_conv1_fwd", "svbrdf_desc_conv1_bwd",
-    "svbrdf_desc_pool_fwd", "svbrdf_desc_pool_bwd", "svbrdf_desc_feat_loss", "svbrdf_gen_upsample2",
+    "svbrdf_desc_pool_fwd", "svbrdf_desc_pool_bwd", "svbrdf_desc_avgpool_fwd", "svbrdf_desc_avgpool_bwd",
+    "svbrdf_desc_feat_loss", "svbrdf_gen_upsample2",
     "svbrdf_gen_upsample2_bwd", "svbrdf_gen_upsample2_scaled", "svbrdf_gen_scale", "svbrdf_gen_scale_bwd", "svbrdf_gen_act", "svbrdf_gen_act_bwd",
     "svbrdf_gen_nhwc_partial_floats", "svbrdf_gen_upsample2_nhwc", "svbrdf_gen_upsample2_nhwc_bwd",
     "svbrdf_gen_scale_nhwc", "svbrdf_gen_scale_nhwc_bwd", "svbrdf_gen_act_nhwc", "svbrdf_gen_act_nhwc_bwd",

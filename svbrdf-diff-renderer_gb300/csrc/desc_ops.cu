@@ -7,9 +7,10 @@
 //
 //   desc_conv1_fwd_kernel  2x2 box downsample + normalise + conv1_1 (3 -> 64) + bias + ReLU,
 //                          FP32 and BF16 NHWC outputs (the FP32 copy feeds the relu1_1 hook)
-//   desc_pool_fwd_kernel   2x2 max-pool, NHWC BF16
-//   desc_pool_bwd_kernel   max-pool backward (the first maximum of each window takes the
-//                          gradient, as ATen's pool) + optional hook gradient + ReLU mask
+//   desc_pool_fwd_kernel   2x2 max-pool (or average pool), NHWC BF16
+//   desc_pool_bwd_kernel   its backward (max: the first maximum of each window takes the
+//                          gradient, as ATen's pool; average: a quarter to each) + optional
+//                          hook gradient + ReLU mask
 //   desc_feat_loss_kernel  sum of (f - t)^2 as per-block partials (a fixed-order sum), and
 //                          optionally g = coef (f - t) + gram_grad, masked by f > 0
 //   desc_conv1_bwd_kernel  conv1_1 data gradient, back through the normalisation and the
@@ -189,6 +190,9 @@ __device__ __forceinline__ void bf8_store(__nv_bfloat16* p, const float f[8]) {
 }
 
 // x [V, H, W, C] -> y [V, H/2, W/2, C]; one thread per output pixel and 8 channels.
+// AVG: the window's mean (the reference's VGGLoss swaps VGG19's max-pools for 2x2 average
+// pools, src/descriptor.py:16-19), summed in row-major order in FP32 then halved twice.
+template <bool AVG>
 __global__ void desc_pool_fwd_kernel(const __nv_bfloat16* __restrict__ x, __nv_bfloat16* __restrict__ y, int V, int H,
                                      int W, int C) {
   const int Ho = H / 2, Wo = W / 2, C8 = C / 8;
@@ -205,14 +209,20 @@ __global__ void desc_pool_fwd_kernel(const __nv_bfloat16* __restrict__ x, __nv_b
     for (int k = 0; k < 3; ++k) {
       bf8_load(base + offs[k], t);
 #pragma unroll
-      for (int j = 0; j < 8; ++j) m[j] = t[j] > m[j] ? t[j] : m[j];
+      for (int j = 0; j < 8; ++j) m[j] = AVG ? m[j] + t[j] : (t[j] > m[j] ? t[j] : m[j]);
+    }
+    if (AVG) {
+#pragma unroll
+      for (int j = 0; j < 8; ++j) m[j] *= 0.25f;
     }
     bf8_store(y + p * C + c8 * 8, m);
   }
 }
 
 // gx = (pool-route(gy) + addend) * (x > 0). x is the pool's input, a ReLU output, so x > 0 is
-// that ReLU's mask. The window's first maximum in row-major order takes the gradient.
+// that ReLU's mask. Max-pool: the window's first maximum in row-major order takes the
+// gradient. AVG: every element of the window takes gy / 4.
+template <bool AVG>
 __global__ void desc_pool_bwd_kernel(const __nv_bfloat16* __restrict__ gy, const __nv_bfloat16* __restrict__ x,
                                      const __nv_bfloat16* __restrict__ addend, __nv_bfloat16* __restrict__ gx, int V,
                                      int H, int W, int C) {
@@ -243,7 +253,7 @@ __global__ void desc_pool_bwd_kernel(const __nv_bfloat16* __restrict__ gy, const
       if (addend) bf8_load(addend + b0 + offs[k], ad);
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
-        float val = (am[j] == k) ? g[j] : 0.0f;
+        float val = AVG ? 0.25f * g[j] : ((am[j] == k) ? g[j] : 0.0f);
         if (addend) val += ad[j];
         o[j] = xv[k][j] > 0.0f ? val : 0.0f;
       }
@@ -312,6 +322,33 @@ static int grid_for_elems(long long n) {
   return (int)(b < 4096 ? (b < 1 ? 1 : b) : 4096);
 }
 
+template <bool AVG>
+static int pool_fwd(const void* x, void* y, int v, int h, int w, int c, void* stream) {
+  if (!x || !y) return fail(SVBRDF_ERR_INVALID, "null pointer");
+  if (v < 1 || h < 2 || w < 2 || h % 2 || w % 2 || c < 8 || c % 8)
+    return fail(SVBRDF_ERR_UNSUPPORTED, "pool: even H, W and C a multiple of 8 needed");
+  if (((uintptr_t)x | (uintptr_t)y) % 16) return fail(SVBRDF_ERR_INVALID, "pool: 16-byte alignment needed");
+  const long long n = (long long)v * (h / 2) * (w / 2) * (c / 8);
+  desc_pool_fwd_kernel<AVG><<<grid_for_elems(n), 256, 0, (cudaStream_t)stream>>>(
+      (const __nv_bfloat16*)x, (__nv_bfloat16*)y, v, h, w, c);
+  return check_launch("desc_pool_fwd_kernel");
+}
+
+template <bool AVG>
+static int pool_bwd(const void* gy, const void* x, const void* addend, void* gx, int v, int h, int w, int c,
+                    void* stream) {
+  if (!gy || !x || !gx) return fail(SVBRDF_ERR_INVALID, "null pointer");
+  if (v < 1 || h < 2 || w < 2 || h % 2 || w % 2 || c < 8 || c % 8)
+    return fail(SVBRDF_ERR_UNSUPPORTED, "pool: even H, W and C a multiple of 8 needed");
+  if (((uintptr_t)gy | (uintptr_t)x | (uintptr_t)addend | (uintptr_t)gx) % 16)
+    return fail(SVBRDF_ERR_INVALID, "pool: 16-byte alignment needed");
+  const long long n = (long long)v * (h / 2) * (w / 2) * (c / 8);
+  desc_pool_bwd_kernel<AVG><<<grid_for_elems(n), 256, 0, (cudaStream_t)stream>>>(
+      (const __nv_bfloat16*)gy, (const __nv_bfloat16*)x, (const __nv_bfloat16*)addend, (__nv_bfloat16*)gx, v, h, w,
+      c);
+  return check_launch("desc_pool_bwd_kernel");
+}
+
 extern "C" {
 
 int svbrdf_desc_partials() { return kLossBlocks; }
@@ -346,27 +383,21 @@ int svbrdf_desc_conv1_bwd(const void* gz, const float* weight, float* grad_rende
 }
 
 int svbrdf_desc_pool_fwd(const void* x, void* y, int v, int h, int w, int c, void* stream) {
-  if (!x || !y) return fail(SVBRDF_ERR_INVALID, "null pointer");
-  if (v < 1 || h < 2 || w < 2 || h % 2 || w % 2 || c < 8 || c % 8)
-    return fail(SVBRDF_ERR_UNSUPPORTED, "pool: even H, W and C a multiple of 8 needed");
-  if (((uintptr_t)x | (uintptr_t)y) % 16) return fail(SVBRDF_ERR_INVALID, "pool: 16-byte alignment needed");
-  const long long n = (long long)v * (h / 2) * (w / 2) * (c / 8);
-  desc_pool_fwd_kernel<<<grid_for_elems(n), 256, 0, (cudaStream_t)stream>>>((const __nv_bfloat16*)x, (__nv_bfloat16*)y,
-                                                                          v, h, w, c);
-  return check_launch("desc_pool_fwd_kernel");
+  return pool_fwd<false>(x, y, v, h, w, c, stream);
 }
 
 int svbrdf_desc_pool_bwd(const void* gy, const void* x, const void* addend, void* gx, int v, int h, int w, int c,
                          void* stream) {
-  if (!gy || !x || !gx) return fail(SVBRDF_ERR_INVALID, "null pointer");
-  if (v < 1 || h < 2 || w < 2 || h % 2 || w % 2 || c < 8 || c % 8)
-    return fail(SVBRDF_ERR_UNSUPPORTED, "pool: even H, W and C a multiple of 8 needed");
-  if (((uintptr_t)gy | (uintptr_t)x | (uintptr_t)addend | (uintptr_t)gx) % 16)
-    return fail(SVBRDF_ERR_INVALID, "pool: 16-byte alignment needed");
-  const long long n = (long long)v * (h / 2) * (w / 2) * (c / 8);
-  desc_pool_bwd_kernel<<<grid_for_elems(n), 256, 0, (cudaStream_t)stream>>>(
-      (const __nv_bfloat16*)gy, (const __nv_bfloat16*)x, (const __nv_bfloat16*)addend, (__nv_bfloat16*)gx, v, h, w, c);
-  return check_launch("desc_pool_bwd_kernel");
+  return pool_bwd<false>(gy, x, addend, gx, v, h, w, c, stream);
+}
+
+int svbrdf_desc_avgpool_fwd(const void* x, void* y, int v, int h, int w, int c, void* stream) {
+  return pool_fwd<true>(x, y, v, h, w, c, stream);
+}
+
+int svbrdf_desc_avgpool_bwd(const void* gy, const void* x, const void* addend, void* gx, int v, int h, int w, int c,
+                            void* stream) {
+  return pool_bwd<true>(gy, x, addend, gx, v, h, w, c, stream);
 }
 
 int svbrdf_desc_feat_loss(const void* f, int f_is_bf16, const float* t, const float* gram_grad, float coef, int mask,

@@ -16,6 +16,9 @@ offline), the renders are 2x2 box-downsampled first, and both terms are on:
 Hooks: relu1_1, relu1_2, relu3_2, relu4_1 (the reference hooks relu4_2, which lies past
 conv4_1), weights [1, 1, 1, 1] / 4 (the reference's default).
 
+``mode="reference"`` runs the reference's own semantics instead: VGG19 to relu4_2 with
+average pools, hooks relu1_1, relu1_2, relu3_2, relu4_2, no downsample, no Gram term.
+
 Every 3x3 convolution with 64 or more input channels runs as a tcgen05 implicit GEMM
 (``svbrdf_conv3x3_bf16``: BF16 operands, FP32 accumulation in TMEM, bias + ReLU fused).
 Its data gradient is the same kernel on the transposed, flipped weights. The glue around
@@ -47,6 +50,11 @@ VGG19_TO_CONV4_1 = [("conv1_1", 3, 64), ("conv1_2", 64, 64), "pool", ("conv2_1",
                     "pool", ("conv3_1", 128, 256), ("conv3_2", 256, 256), ("conv3_3", 256, 256),
                     ("conv3_4", 256, 256), "pool", ("conv4_1", 256, 512)]
 HOOKS = ("conv1_1", "conv1_2", "conv3_2", "conv4_1")  # their ReLU outputs
+# The reference's own stack: VGG19 up to relu4_2 (src/descriptor.py:26-27 hooks features
+# 1, 3, 13, 22 = relu1_1, relu1_2, relu3_2, relu4_2), its max-pools swapped for average pools
+# (:16-19), full-resolution renders and the feature term alone (is_gram off, :77-79).
+VGG19_TO_CONV4_2 = VGG19_TO_CONV4_1 + [("conv4_2", 512, 512)]
+REF_HOOKS = ("conv1_1", "conv1_2", "conv3_2", "conv4_2")
 
 EPI_NONE, EPI_BIAS_RELU, EPI_MASK, EPI_ADD_MASK = 0, 1, 2, 3
 
@@ -136,12 +144,20 @@ class VGGDescriptor:
     """
 
     def __init__(self, device="cuda", seed: int = 0, weights: Sequence[float] = (0.25, 0.25, 0.25, 0.25),
-                 downsample: bool = True):
+                 downsample: Optional[bool] = None, mode: str = "config"):
+        if mode not in ("config", "reference"):
+            raise ValueError(f"mode must be 'config' or 'reference', not {mode!r}")
         self.device = torch.device(device)
+        self.mode = mode
+        ref = mode == "reference"
+        self.layers = VGG19_TO_CONV4_2 if ref else VGG19_TO_CONV4_1
+        self.hooks = REF_HOOKS if ref else HOOKS
+        self.avg_pool = ref
+        self.gram = not ref
         self.hook_weights = list(weights)
-        self.downsample = downsample
+        self.downsample = (not ref) if downsample is None else downsample
         self.err = torch.zeros(1, dtype=torch.int32, device=self.device)
-        raw = he_normal_weights(seed)
+        raw = he_normal_weights(seed, self.layers)
         self.params = {}
         for name, (w, b) in raw.items():
             wb = w.to(torch.bfloat16)  # the weights the tensor cores see
@@ -162,7 +178,7 @@ class VGGDescriptor:
     # ---- forward -----------------------------------------------------------------------
     def _forward(self, renders: torch.Tensor):
         """Run the stack. Returns (acts, hooks): acts[i] is the output of layer i of
-        VGG19_TO_CONV4_1 (NHWC BF16); hooks maps each hooked layer to its feature (relu1_1 in
+        self.layers (NHWC BF16); hooks maps each hooked layer to its feature (relu1_1 in
         FP32, the others BF16)."""
         L = N.lib()
         st = N.stream_handle(self.device)
@@ -175,19 +191,20 @@ class VGGDescriptor:
         N.check(L.svbrdf_desc_conv1_fwd(x.data_ptr(), p["w32"].data_ptr(), p["b"].data_ptr(), y32.data_ptr(),
                                         y16.data_ptr(), v, h, w, int(self.downsample), st))
         acts, hooks = [y16], {"conv1_1": y32}
-        for item in VGG19_TO_CONV4_1[1:]:
+        pool_fwd = L.svbrdf_desc_avgpool_fwd if self.avg_pool else L.svbrdf_desc_pool_fwd
+        for item in self.layers[1:]:
             prev = acts[-1]
             if item == "pool":
                 n_, hh, ww, c = prev.shape
                 y = torch.empty(n_, hh // 2, ww // 2, c, device=self.device, dtype=torch.bfloat16)
-                N.check(L.svbrdf_desc_pool_fwd(prev.data_ptr(), y.data_ptr(), n_, hh, ww, c, st))
+                N.check(pool_fwd(prev.data_ptr(), y.data_ptr(), n_, hh, ww, c, st))
                 acts.append(y)
                 continue
             name, cin, cout = item
             q = self.params[name]
             y = conv3x3_bf16(prev, q["w_fwd"], q["b"], EPI_BIAS_RELU, self.err)
             acts.append(y)
-            if name in HOOKS:
+            if name in self.hooks:
                 hooks[name] = y
         return acts, hooks
 
@@ -202,23 +219,25 @@ class VGGDescriptor:
         nf = sum(f.numel() for f in hooks.values())
         ng = sum(g.numel() for g in tg)
         nparts = L.svbrdf_desc_partials()
-        parts = torch.empty(len(HOOKS), nparts, device=self.device, dtype=torch.float32)
+        parts = torch.empty(len(self.hooks), nparts, device=self.device, dtype=torch.float32)
         gram_terms, grads = [], {}
-        last = [it for it in VGG19_TO_CONV4_1 if it != "pool"][-1][0]
-        for k, (name, wt) in enumerate(zip(HOOKS, self.hook_weights)):
+        last = [it for it in self.layers if it != "pool"][-1][0]
+        for k, (name, wt) in enumerate(zip(self.hooks, self.hook_weights)):
             f = hooks[name]
             v, h, w, c = f.shape
             s = h * w
-            ff = f.reshape(v, s, c).to(torch.bfloat16)
-            gram = _gram_f32(ff) / s
-            diff = gram - tg[k]
-            gram_terms.append((wt * wt) * (diff * diff).sum())
             gg = None
             g = None
+            if self.gram:
+                ff = f.reshape(v, s, c).to(torch.bfloat16)
+                gram = _gram_f32(ff) / s
+                diff = gram - tg[k]
+                gram_terms.append((wt * wt) * (diff * diff).sum())
             if cf is not None:
-                # d/dF of w^2 sum (G - Gt)^2 / ng with G = F^T F / s: F (2 dG) / s, dG = 2 w^2 (G - Gt) / ng
-                dgram = (4.0 * wt * wt * cg / (ng * s)) * diff
-                gg = _bmm_f32out(ff, dgram.to(torch.bfloat16)).reshape(v, h, w, c).contiguous()
+                if self.gram:
+                    # d/dF of w^2 sum (G - Gt)^2 / ng with G = F^T F / s: F (2 dG) / s, dG = 2 w^2 (G - Gt) / ng
+                    dgram = (4.0 * wt * wt * cg / (ng * s)) * diff
+                    gg = _bmm_f32out(ff, dgram.to(torch.bfloat16)).reshape(v, h, w, c).contiguous()
                 g = torch.empty(v, h, w, c, device=self.device, dtype=torch.bfloat16)
             coef = (2.0 * wt * wt * cf / nf) if cf is not None else 0.0
             N.check(L.svbrdf_desc_feat_loss(f.data_ptr(), int(f.dtype == torch.bfloat16), tf[k].data_ptr(),
@@ -227,7 +246,7 @@ class VGGDescriptor:
             if g is not None:
                 grads[name] = g
         fl = ((parts.double().sum(dim=1) * self._w2).sum() / nf).float()
-        gl = torch.stack(gram_terms).sum() / ng
+        gl = torch.stack(gram_terms).sum() / ng if self.gram else torch.zeros((), device=self.device)
         return fl, gl, grads
 
     # ---- backward chain ----------------------------------------------------------------
@@ -238,7 +257,8 @@ class VGGDescriptor:
         gradient back through the normalisation and the downsample."""
         L = N.lib()
         st = N.stream_handle(self.device)
-        items = VGG19_TO_CONV4_1
+        items = self.layers
+        pool_bwd = L.svbrdf_desc_avgpool_bwd if self.avg_pool else L.svbrdf_desc_pool_bwd
         g = grads[items[-1][0]]  # masked gradient at the last ReLU
         for i in range(len(items) - 1, 0, -1):
             item, below = items[i], items[i - 1]
@@ -248,8 +268,7 @@ class VGGDescriptor:
                 # below is a convolution: route, add its hook gradient, mask by its ReLU
                 gx = torch.empty_like(x)
                 add = grads.get(below[0])
-                N.check(L.svbrdf_desc_pool_bwd(g.data_ptr(), x.data_ptr(), N.ptr(add), gx.data_ptr(), n_, h, w, c,
-                                               st))
+                N.check(pool_bwd(g.data_ptr(), x.data_ptr(), N.ptr(add), gx.data_ptr(), n_, h, w, c, st))
                 g = gx
                 continue
             q = self.params[item[0]]
@@ -272,7 +291,7 @@ class VGGDescriptor:
     def features(self, renders: torch.Tensor) -> List[torch.Tensor]:
         """Hooked ReLU outputs, each NHWC [V, H, W, C] (BF16, except relu1_1 in FP32)."""
         _, hooks = self._forward(renders)
-        return [hooks[n] for n in HOOKS]
+        return [hooks[n] for n in self.hooks]
 
     @staticmethod
     def _gram(f: torch.Tensor) -> torch.Tensor:
@@ -282,7 +301,8 @@ class VGGDescriptor:
         self._graph = None  # a captured graph holds the previous targets' features
         with torch.no_grad():
             feats = self.features(targets)
-            self.target = ([f.float().contiguous() for f in feats], [self._gram(f) for f in feats])
+            grams = [self._gram(f) for f in feats] if self.gram else []
+            self.target = ([f.float().contiguous() for f in feats], grams)
 
     def loss(self, renders: torch.Tensor):
         """(feature_loss, gram_loss) as 0-d tensors, differentiable w.r.t. ``renders``."""

@@ -63,7 +63,8 @@ def parse():
     ap.add_argument("--no-extras", action="store_true", help="skip the plain/single/cpu comparison legs")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline budget")
     ap.add_argument("--config", default=None, help="threads,tile_texels[,ctas[,variant]] instead of autotuning")
-    ap.add_argument("--only", default=None, choices=["descriptor", "latent"], help="run one comparison leg alone")
+    ap.add_argument("--only", default=None, choices=["descriptor", "latent", "envmap"],
+                    help="run one comparison leg alone")
     return ap.parse_args()
 
 
@@ -293,6 +294,26 @@ def time_single(dev, fused, iters, res=1024):
             "workload": f"1 material {res}^2, 9 views, {iters} Adam iterations, log1p L2"
                         + (", fused kernel in one CUDA graph" if fused else
                            ", forward kernel + torch loss + adjoint kernel (autograd) + torch.optim.Adam")}
+
+
+def time_envmap(dev, res=256, spp=256, frames=5):
+    """One frame of the reference's novel-view video (src/scripts.py:44-59, Mitsuba at
+    256 spp in the reference, src/mitsubarender.py:36): a 256^2 seeded material under the
+    seeded synthetic environment, 256 samples per pixel, CUDA events over `frames` frames."""
+    mat = PKG.scenes.make_material(256, 777)[0]
+    r = PKG.EnvmapRenderer([res, res], None, mat, device=dev, spp=spp, seed=0)
+    out = r.render_device(0.0, 0.5)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for k, a in enumerate(PKG.envmap.video_angles(frames)):
+        r.render_device(float(a), 0.5, out=out)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / frames
+    return {"workload": f"{res}^2 frame, {spp} spp, 256^2 material, synthetic {r.env.shape[0]}x{r.env.shape[1]} "
+                        "environment (the reference's fig/ennis.exr is not in its repository)",
+            "ms_per_frame": ms, "camera_samples_per_s": res * res * spp / (ms / 1e3)}
 
 
 def time_descriptor(dev, iters=10, views=9, res=512):
@@ -586,6 +607,7 @@ def impl_ours(args):
         line["fused_vs_plain"] = value / line["plain"]["value"]
         line["descriptor"] = time_descriptor(dev)
         line["latent"] = time_latent(dev, iters=5)
+        line["envmap"] = time_envmap(dev)
         if world == 1:
             line["cpu_baseline"] = run_cpu_baseline(specs, args.cpu_seconds, os.cpu_count() or 1)
     if rank == 0:
@@ -606,6 +628,10 @@ def main():
     if args.only == "latent":
         dev = torch.device("cuda", dist_env()[2])
         print(json.dumps({"latent": time_latent(dev, iters=max(args.steps, 1))}), flush=True)
+        return 0
+    if args.only == "envmap":
+        dev = torch.device("cuda", dist_env()[2])
+        print(json.dumps({"envmap": time_envmap(dev)}), flush=True)
         return 0
     if args.impl == "reference":
         return impl_reference(args)

@@ -326,6 +326,20 @@ int svbrdf_gen_act_nhwc_bwd(const float* gout, const float* y, const float* d, c
                             const float* bias, float gain, float* gy, float* gd, float* gnoise, float* part, int b,
                             int hw, int c, void* stream);
 
+/* ---- novel-view rendering under an environment map (the reference's MitsubaRender,
+ * src/mitsubarender.py:7-105, for the video of src/scripts.py:44-59) ---- */
+
+/* image [res][res][3] (clipped to [0, 1], raised to 1/2.2) of the material textures
+ * [9][h][w] (parameters in [-1, 1]) on the reference's rectangle, turned Ry(angle_deg)
+ * Rx(-15) Rz(-5) and scaled by 0.3, seen by a 50-degree camera at (0, 0, 1), lit by the
+ * lat-long environment env [he][we][3] (linear radiance, times `intensity`). Direct
+ * illumination, spp samples per pixel, each one environment sample (row_cdf [he+1], row_pdf
+ * [he], col_cdf [he][we+1], col_pdf [he][we]: luminance x sin(theta) tables) and one BSDF
+ * sample, power-heuristic weights; random numbers hashed from (seed, pixel, sample, dim). */
+int svbrdf_envmap_render(const float* textures, int h, int w, const float* env, int he, int we, const float* row_cdf,
+                         const float* row_pdf, const float* col_cdf, const float* col_pdf, float* image, int res,
+                         float angle_deg, float intensity, int spp, unsigned seed, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -19,8 +19,10 @@ from .batched import BatchConfig, BatchedOptim, BatchedPipeline, autotune
 from .microfacet import Microfacet
 from .svbrdf import SvbrdfIO, SvbrdfOptim
 from .scripts import optim_perpixel, render
-from . import descriptor, imageio, materialgan, scenes
+from . import descriptor, envmap, imageio, materialgan, scenes
+from .envmap import EnvmapRenderer
 
 __all__ = ["Microfacet", "SvbrdfOptim", "SvbrdfIO", "optim_perpixel", "render", "BatchedOptim", "BatchedPipeline",
+           "EnvmapRenderer",
            "BatchConfig",
            "autotune", "SvbrdfError", "build", "scenes", "imageio", "descriptor", "materialgan", "_native"]

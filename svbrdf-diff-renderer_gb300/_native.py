@@ -20,7 +20,7 @@ CSRC = PKG / "csrc"
 INCLUDE = REPO / "include"
 LIBDIR = PKG / "_lib"
 LIBNAME = "libsvbrdf_gb300.so"
-SOURCES = ["render.cu", "fused.cu", "conv_tc.cu", "desc_ops.cu", "gen_ops.cu", "gen_nhwc.cu"]
+SOURCES = ["render.cu", "fused.cu", "conv_tc.cu", "desc_ops.cu", "gen_ops.cu", "gen_nhwc.cu", "envmap.cu"]
 HEADERS = ["svbrdf_math.cuh", "svbrdf_common.cuh", "svbrdf_plan.cuh"]
 WORKSPACE_ERROR_OFFSET = 4
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -168,6 +168,8 @@ def _declare(L):
     L.svbrdf_gen_act_nhwc.argtypes = [P, P, P, P, P, F, P, I, I, I, P]
     L.svbrdf_gen_act_nhwc_bwd.restype = I
     L.svbrdf_gen_act_nhwc_bwd.argtypes = [P, P, P, P, P, P, F, P, P, P, P, I, I, I, P]
+    L.svbrdf_envmap_render.restype = I
+    L.svbrdf_envmap_render.argtypes = [P, I, I, P, I, I, P, P, P, P, P, I, F, F, I, ctypes.c_uint, P]
     L.svbrdf_batched_plan_bytes.restype = S
     L.svbrdf_batched_plan_bytes.argtypes = [ctypes.POINTER(svbrdf_material), I, ctypes.POINTER(svbrdf_batch_config)]
     L.svbrdf_batched_plan.restype = I
@@ -193,6 +195,7 @@ EXPORTS = [
     "svbrdf_gen_upsample2_bwd", "svbrdf_gen_upsample2_scaled", "svbrdf_gen_scale", "svbrdf_gen_scale_bwd", "svbrdf_gen_act", "svbrdf_gen_act_bwd",
     "svbrdf_gen_nhwc_partial_floats", "svbrdf_gen_upsample2_nhwc", "svbrdf_gen_upsample2_nhwc_bwd",
     "svbrdf_gen_scale_nhwc", "svbrdf_gen_scale_nhwc_bwd", "svbrdf_gen_act_nhwc", "svbrdf_gen_act_nhwc_bwd",
+    "svbrdf_envmap_render",
 ]
 
 

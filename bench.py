@@ -4,8 +4,9 @@
 Workload (the uneven batched per-pixel optimisation): 64 seeded synthetic materials,
 resolution drawn from {256, 512, 1024}, 5-16 co-located flash views within +-8 cm at
 25-35 cm, log(1+x) L2 loss, Adam lr 0.01. One *step* is one replay of a CUDA graph of
-100 iterations, each iteration one persistent launch of the fused batched kernel over
-every material. Metric unit: texel*view updates per second = sum(H*W*V) * iterations / s.
+100 iterations over every material: with the autotuner's usual pick, the resident-state
+kernel, that is 4 persistent launches of 25 iterations each (one launch per iteration for
+the other kernels). Metric unit: texel*view updates per second = sum(H*W*V) * iterations / s.
 
 Lines printed (rank 0, one JSON line):
 * ``value``: device-resident inputs, CUDA events around K graph replays;
@@ -13,13 +14,19 @@ Lines printed (rank 0, one JSON line):
   the initial maps and the targets host->device, restarts the optimiser, runs the 100
   iterations and copies the optimised maps and the loss history back;
 * ``roofline``: the batched kernel's algorithmic bytes per launch (params+moments read and
-  written, targets read: sum H*W*(216+12V)) over its average launch time, against the
-  measured HBM copy bandwidth;
+  written, targets read: sum H*W*(216+12V) per iteration, times the iterations the launch
+  runs) over its average launch time, against the measured HBM copy bandwidth; ``traffic``
+  is the kernel's DRAM bytes per launch (ncu), far below the algorithmic bytes for the
+  resident-state kernel, which moves its state through DRAM once per launch;
+* ``per_iteration_kernel``: the one-launch-per-iteration texel-pair kernel on the same
+  materials, whose DRAM traffic equals its algorithmic bytes;
 * ``plain`` / ``fused_single``: the unfused single-material GPU form (forward kernel +
   torch loss + adjoint kernel via autograd + torch.optim.Adam) and the fused single-material
   kernel, both on the 1024^2, 9-view scene;
 * ``cpu_baseline``: the reference's PyTorch CPU loop (the oracle restatement, same op
-  sequence) on a bounded sample of the workload, all host threads.
+  sequence) on a bounded sample of the workload, all host threads;
+* ``descriptor``, ``latent``, ``envmap``: the VGG-feature loss, the MaterialGAN latent loop
+  with the per-pixel refinement, and a frame of the environment-map video.
 
 ``--impl reference`` times only that CPU implementation (rank 0), one step = one
 iteration over the sample.

@@ -5,13 +5,20 @@
 //   zero_grad(); loss.backward(); optimizer.step()
 // Each texel's 9 parameters, its Adam moments and its V targets are read once, every
 // per-view term is recomputed in registers, and the parameters and moments are written
-// back. Per-iteration HBM traffic: 108 B read + 108 B written + 12*V B of targets per texel.
+// back. Per-iteration HBM traffic: 108 B read + 108 B written + 12*V B of targets per texel
+// (variants 3 and 4 move that once per launch of up to 32 iterations).
 //
 // Kernels:
 //   fused_step_kernel     one material, grid-stride, direct loads (drop-in SvbrdfOptim)
 //   batched_step_kernel   many materials, persistent, direct loads           (variant 0)
 //   batched_tma_kernel    many materials, persistent, warp-specialised bulk-copy
 //                         (TMA) pipeline through a shared-memory ring         (variant 1)
+//   batched_pair_kernel   the variant 1 pipeline with two texels per thread in
+//                         FP32x2                                              (variant 2)
+//   batched_fuse_kernel   variant 2's arithmetic, up to 32 iterations per launch on
+//                         each tile's state held in shared memory             (variant 3)
+//   batched_fuse2_kernel  variant 3 without the producer warp: the last warp to
+//                         finish with a buffer refills it                     (variant 4)
 #include <math.h>
 #include <string.h>
 

@@ -222,3 +222,43 @@ def test_pipelined_plan_ring_and_workspace(svb, lib):
     xs = np.frombuffer(buf[off_coords:off_coords + 4 * 64].tobytes(), np.float32)
     ref = ((np.arange(64, dtype=np.float32) + np.float32(0.5)) / np.float32(64) - np.float32(0.5)) * np.float32(17.0)
     assert np.array_equal(xs, ref)
+
+
+def test_new_entry_points_reject_bad_arguments_on_host(svb, lib):
+    """The multi-iteration batched call, the generator, descriptor and environment-map
+    kernels check their arguments on the host, before any device work."""
+    SV = svb._native
+    fake = ctypes.c_void_p(16)
+    # svbrdf_batched_steps: negative iteration count, too small a workspace
+    mats, keep = _materials(SV, [(64, 64, 9)])
+    cfg = SV.svbrdf_batch_config(480, 960, 3, 3)
+    n = lib.svbrdf_batched_plan_bytes(mats, 1, ctypes.byref(cfg))
+    buf = np.zeros(n, np.uint8)
+    assert lib.svbrdf_batched_plan(mats, 1, ctypes.byref(cfg), buf.ctypes.data, n) == 0
+    need = lib.svbrdf_batched_workspace_bytes(buf.ctypes.data)
+    step = [fake, buf.ctypes.data, 1, fake, 0.01, 0.9, 0.999, 1e-8, fake, 4]
+    assert lib.svbrdf_batched_steps(*step, -1, fake, need, None) == -1
+    assert lib.svbrdf_batched_steps(*step, 5, fake, need - 4, None) == -4
+    assert lib.svbrdf_batched_steps(fake, buf.ctypes.data, 9, fake, 0.01, 0.9, 0.999, 1e-8, fake, 4, 5, fake, need,
+                                    None) == -1  # bad loss kind
+    assert lib.svbrdf_batched_steps(fake, buf.ctypes.data, 1, fake, 0.01, 0.9, 0.999, 1e-8, fake, 0, 5, fake, need,
+                                    None) == -1  # no loss history rows
+    # generator kernels
+    assert lib.svbrdf_gen_upsample2(None, fake, 4, 8, 8, None) == -1
+    assert lib.svbrdf_gen_upsample2_scaled(fake, fake, fake, 4, 8, 6, None) == -2  # scaling needs w % 4 == 0
+    assert lib.svbrdf_gen_scale(fake, fake, fake, 70000, 64, None) == -1            # planes beyond a grid axis
+    assert lib.svbrdf_gen_act_bwd(fake, fake, None, None, fake, fake, 1.0, fake, None, fake, 2, 4, 64, None) == -1
+    assert lib.svbrdf_gen_scale_nhwc_bwd(fake, fake, fake, fake, fake, fake, 2, 64, 2048, None) == -2
+    assert lib.svbrdf_gen_act_nhwc(fake, None, fake, None, fake, 1.0, fake, 2, 64, 8, None) == -1  # noise, no strength
+    assert lib.svbrdf_gen_upsample2_nhwc(fake, None, fake, 40000, 2, 8, 8, None) == -2           # B 2h beyond a grid axis
+    assert lib.svbrdf_gen_nhwc_partial_floats(3, 128) == 3 * 64 * 128
+    # descriptor average pool: odd size
+    assert lib.svbrdf_desc_avgpool_fwd(fake, fake, 1, 7, 8, 64, None) == -2
+    assert lib.svbrdf_desc_avgpool_bwd(None, fake, None, fake, 1, 8, 8, 64, None) == -1
+    # environment map: null tables, bad sizes
+    args = [fake, 8, 8, fake, 8, 16, fake, fake, fake, None, fake, 32, 0.0, 1.0, 16, 1, None]
+    assert lib.svbrdf_envmap_render(*args) == -1
+    args[9] = fake
+    args[14] = 0  # no samples
+    assert lib.svbrdf_envmap_render(*args) == -1
+    assert b"envmap" in lib.svbrdf_last_error()

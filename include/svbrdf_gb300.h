@@ -163,6 +163,13 @@ typedef struct svbrdf_batch_config {
  * synchronising and treats non-zero as a failed step. */
 #define SVBRDF_WORKSPACE_ERROR_OFFSET 4
 
+/* Self-test of the batched kernels' failure path: a one-warp kernel waits on an mbarrier
+ * phase that nothing completes, gives up after `limit` polls (at most 2^24), stores 1 (the
+ * "copy never landed" code) in the error word at byte SVBRDF_WORKSPACE_ERROR_OFFSET, and
+ * returns with the context usable. Bytes 8 and 12 receive 1 and 0: a wait its own arrival
+ * completed, and the one that ran out. The workspace must start zeroed (16 bytes). */
+int svbrdf_selftest_wait_timeout(void* workspace, size_t workspace_bytes, int limit, void* stream);
+
 /* Bytes of the plan for this batch (0 on error). */
 size_t svbrdf_batched_plan_bytes(const svbrdf_material* materials, int n_materials,
                                  const svbrdf_batch_config* config);

@@ -168,6 +168,8 @@ def _declare(L):
     L.svbrdf_gen_act_nhwc.argtypes = [P, P, P, P, P, F, P, I, I, I, P]
     L.svbrdf_gen_act_nhwc_bwd.restype = I
     L.svbrdf_gen_act_nhwc_bwd.argtypes = [P, P, P, P, P, P, F, P, P, P, P, I, I, I, P]
+    L.svbrdf_selftest_wait_timeout.restype = I
+    L.svbrdf_selftest_wait_timeout.argtypes = [P, S, I, P]
     L.svbrdf_envmap_render.restype = I
     L.svbrdf_envmap_render.argtypes = [P, I, I, P, I, I, P, P, P, P, P, I, F, F, I, ctypes.c_uint, P]
     L.svbrdf_batched_plan_bytes.restype = S
@@ -195,7 +197,7 @@ EXPORTS = [
     "svbrdf_gen_upsample2_bwd", "svbrdf_gen_upsample2_scaled", "svbrdf_gen_scale", "svbrdf_gen_scale_bwd", "svbrdf_gen_act", "svbrdf_gen_act_bwd",
     "svbrdf_gen_nhwc_partial_floats", "svbrdf_gen_upsample2_nhwc", "svbrdf_gen_upsample2_nhwc_bwd",
     "svbrdf_gen_scale_nhwc", "svbrdf_gen_scale_nhwc_bwd", "svbrdf_gen_act_nhwc", "svbrdf_gen_act_nhwc_bwd",
-    "svbrdf_envmap_render",
+    "svbrdf_envmap_render", "svbrdf_selftest_wait_timeout",
 ]
 
 

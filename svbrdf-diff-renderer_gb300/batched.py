@@ -201,6 +201,35 @@ class BatchedOptim:
     def textures(self, i: int) -> torch.Tensor:
         return self.tex[i]
 
+    # ---- checkpoints ---------------------------------------------------------------------
+    def state_dict(self) -> dict:
+        """Everything a later run needs to continue bit-identically: maps, both Adam moments,
+        the device step counter and the loss history (FP32, on the host)."""
+        torch.cuda.synchronize(self.device)
+        return {"tex": [t.cpu() for t in self.tex], "exp_avg": [t.cpu() for t in self.m1],
+                "exp_avg_sq": [t.cpu() for t in self.m2], "step": int(self.step_dev.item()),
+                "loss_hist": self.loss_hist.cpu(), "step_count": self.step_count, "signature": self.signature()}
+
+    def load_state_dict(self, st: dict):
+        if st.get("signature") not in (None, self.signature()):
+            raise ValueError("checkpoint was written for a different set of materials")
+        for dst, src in ((self.tex, st["tex"]), (self.m1, st["exp_avg"]), (self.m2, st["exp_avg_sq"])):
+            if len(dst) != len(src):
+                raise ValueError("checkpoint has a different number of materials")
+            for d, s_ in zip(dst, src):
+                d.copy_(s_)
+        self.step_dev.fill_(int(st["step"]))
+        lh = st["loss_hist"]
+        if lh.shape == self.loss_hist.shape:
+            self.loss_hist.copy_(lh)
+        self.step_count = int(st.get("step_count", st["step"]))
+
+    def save(self, path):
+        torch.save(self.state_dict(), path)
+
+    def load(self, path):
+        self.load_state_dict(torch.load(path, map_location="cpu"))
+
     def device_error(self) -> int:
         """The workspace error word (0 = healthy); synchronises with the device."""
         off = N.WORKSPACE_ERROR_OFFSET

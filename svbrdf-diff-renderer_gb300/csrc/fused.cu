@@ -377,18 +377,22 @@ __device__ __forceinline__ void named_sync(int id, int nthreads) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
 }
 
-// Bounded wait on an mbarrier phase. Gives up (and records `code`) after kSpinLimit
-// polls, or early once another warp has recorded an error.
-__device__ __forceinline__ bool wait_phase(uint32_t bar, uint32_t parity, int* err, int code) {
+// Bounded wait on an mbarrier phase. Gives up (and records `code`) after `limit` polls, or
+// early once another warp has recorded an error.
+__device__ __forceinline__ bool wait_phase_n(uint32_t bar, uint32_t parity, int* err, int code, uint32_t limit) {
   uint32_t it = 0;
   while (!mbar_try_wait(bar, parity)) {
-    if (++it >= kSpinLimit) {
+    if (++it >= limit) {
       atomicCAS(err, 0, code);
       return false;
     }
     if ((it & 255u) == 0 && *(volatile int*)err != 0) return false;
   }
   return true;
+}
+
+__device__ __forceinline__ bool wait_phase(uint32_t bar, uint32_t parity, int* err, int code) {
+  return wait_phase_n(bar, parity, err, code, kSpinLimit);
 }
 
 // Consumer-side ring cursor.
@@ -1742,6 +1746,31 @@ batched_fuse2_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __rest
                      ws + kWsCounter, &s_last, NCW, iters);
 }
 
+// ============================================================== wait self-test
+// The failure path of every bounded wait, exercised on purpose: one warp waits on a barrier
+// phase that its own arrival completes (the healthy path), then on a barrier that nothing
+// ever arrives on, giving up after `limit` polls. It records kDevTimeoutFull in the error
+// word and returns; no copy is in flight, so the context stays usable. ws[2] and ws[3] report
+// the two waits' outcomes (1 = completed).
+__global__ void __launch_bounds__(32) wait_selftest_kernel(unsigned* ws, uint32_t limit) {
+  __shared__ __align__(8) uint64_t bar_done, bar_never;
+  if (threadIdx.x == 0) {
+    mbar_init(smem_u32(&bar_done), 1);
+    mbar_init(smem_u32(&bar_never), 1);
+    fence_mbar_init();
+  }
+  __syncwarp();
+  int* err = (int*)(ws + kWsError);
+  if (threadIdx.x == 0) mbar_arrive(smem_u32(&bar_done));
+  __syncwarp();
+  const bool done = __all_sync(0xffffffffu, wait_phase_n(smem_u32(&bar_done), 0u, err, kDevTimeoutFull, limit));
+  const bool never = __all_sync(0xffffffffu, wait_phase_n(smem_u32(&bar_never), 0u, err, kDevTimeoutFull, limit));
+  if (threadIdx.x == 0) {
+    ws[2] = done ? 1u : 0u;
+    ws[3] = never ? 1u : 0u;
+  }
+}
+
 // ============================================================== planner
 static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
@@ -2190,6 +2219,13 @@ size_t svbrdf_batched_workspace_bytes(const void* host_plan) {
   const size_t per_tile = h->variant >= 1 ? (size_t)(h->threads / 32) : 1;
   const size_t iters = h->variant >= 3 ? (size_t)kFuseMax : 1;  // partials of every iteration of a launch
   return kWsLossOffset + sizeof(float) * (size_t)h->n_tiles * per_tile * iters;
+}
+
+int svbrdf_selftest_wait_timeout(void* workspace, size_t workspace_bytes, int limit, void* stream) {
+  if (!workspace || workspace_bytes < 16) return fail(SVBRDF_ERR_WORKSPACE, "self-test: 16 bytes of workspace needed");
+  if (limit < 1 || limit > (1 << 24)) return fail(SVBRDF_ERR_INVALID, "self-test: limit must be in [1, 2^24]");
+  wait_selftest_kernel<<<1, 32, 0, (cudaStream_t)stream>>>((unsigned*)workspace, (uint32_t)limit);
+  return check_launch("wait_selftest_kernel");
 }
 
 int svbrdf_batched_step(const void* device_plan, const void* host_plan, int loss_kind, int* step_counter, float lr,

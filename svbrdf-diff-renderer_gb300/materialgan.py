@@ -541,6 +541,21 @@ class MaterialGANOptim:
                        self.net.make_noises(noise, self.latent.shape[0], self.device, seed)]
         self._graphs = {}  # captured epochs hold the previous parameters' addresses
 
+    def save_latent(self, latent_path, noise_path=None):
+        """The latent and the noise maps with torch.save, as the reference's save points do
+        (src/materialgan.py:161-162: optim_latent.pt, optim_noise.pt)."""
+        torch.save(self.latent.detach().cpu(), latent_path)
+        if noise_path is not None:
+            torch.save([n.detach().cpu() for n in self.noises], noise_path)
+
+    def load_latent(self, latent_path, noise_path=None):
+        """Resume from save_latent's files."""
+        self.latent = torch.load(latent_path, map_location="cpu").to(self.device, torch.float32).requires_grad_(True)
+        if noise_path is not None:
+            self.noises = [n.to(self.device, torch.float32).requires_grad_(True)
+                           for n in torch.load(noise_path, map_location="cpu")]
+        self._graphs = {}  # captured epochs hold the previous parameters' addresses
+
     def load_targets(self, targets: torch.Tensor):
         """targets [B*V, 3, H, W] (materials major)."""
         self.targets = targets.to(self.device, torch.float32).contiguous()

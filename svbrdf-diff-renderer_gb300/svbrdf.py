@@ -77,6 +77,31 @@ class SvbrdfOptim:
         if self.descriptor is not None:
             self.descriptor.load(self.targets)
 
+    # ---- checkpoints: FP32 maps, the last call's Adam moments and step, the light -------
+    # The reference keeps 8-bit PNG maps as its only per-pixel checkpoint
+    # (src/svbrdf.py:74-83) and resumes by reloading them; these keep full precision.
+    def state_dict(self) -> dict:
+        return _optimiser_state(self)
+
+    def load_state_dict(self, st: dict):
+        """Restore the maps (and, when present, the last call's moments and the optimised
+        light). The next ``optim`` call starts a fresh Adam from these maps, as the
+        reference's does from reloaded maps."""
+        self.textures = self._leaf(st["textures"])
+        self._step = int(st.get("step", 0))
+        self.loss_image_list = list(st.get("loss_image_list", []))
+        for k in ("exp_avg", "exp_avg_sq", "light_pow", "light_exp_avg", "light_exp_avg_sq"):
+            if k in st:
+                setattr(self, k, st[k].to(self.device))
+        if "light_pow" in st:
+            self.renderer_obj.update_light(st["light_pow"].to(self.device))
+
+    def save(self, path):
+        torch.save(self.state_dict(), path)
+
+    def load(self, path):
+        self.load_state_dict(torch.load(path, map_location=self.device))
+
     def compute_image_loss(self, predicts):
         """src/optimization.py:28-29 (MSE), or the log(1+x) L2 loss."""
         if self.loss == "mse":
@@ -150,9 +175,9 @@ class SvbrdfOptim:
         L = N.lib()
         r = self.renderer_obj
         tex = self.textures.detach()  # same storage: the kernel updates the leaf in place
-        if not hasattr(self, "exp_avg") or self.exp_avg is None or self.exp_avg.shape != tex.shape:
-            self.exp_avg = torch.zeros_like(tex)
-            self.exp_avg_sq = torch.zeros_like(tex)
+        # every call starts a fresh Adam, as the reference creates one per call (src/svbrdf.py:48-52)
+        self.exp_avg = torch.zeros_like(tex)
+        self.exp_avg_sq = torch.zeros_like(tex)
         self._step = 0
         targets = self.targets
         kind = LOSS_KINDS[self.loss]
@@ -205,6 +230,16 @@ class SvbrdfOptim:
                 r.update_light(lp_dev.clone())
             self.light_exp_avg, self.light_exp_avg_sq = lstate[:3].clone(), lstate[3:].clone()
         self.light_pow = lp_dev
+
+
+def _optimiser_state(o) -> dict:
+    st = {"textures": o.textures.detach().clone(), "step": int(getattr(o, "_step", 0)),
+          "loss_image_list": list(getattr(o, "loss_image_list", []))}
+    for k in ("exp_avg", "exp_avg_sq", "light_pow", "light_exp_avg", "light_exp_avg_sq"):
+        v = getattr(o, k, None)
+        if isinstance(v, torch.Tensor):
+            st[k] = v.detach().clone()
+    return st
 
 
 class SvbrdfIO:

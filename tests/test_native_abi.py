@@ -262,3 +262,24 @@ def test_new_entry_points_reject_bad_arguments_on_host(svb, lib):
     args[14] = 0  # no samples
     assert lib.svbrdf_envmap_render(*args) == -1
     assert b"envmap" in lib.svbrdf_last_error()
+
+
+def test_corrupt_plan_is_rejected_on_host(svb, lib):
+    """Host-side fault injection: a plan whose header was overwritten is refused before any
+    launch."""
+    SV = svb._native
+    mats, keep = _materials(SV, [(64, 64, 9)])
+    cfg = SV.svbrdf_batch_config(480, 960, 3, 3)
+    n = lib.svbrdf_batched_plan_bytes(mats, 1, ctypes.byref(cfg))
+    buf = np.zeros(n, np.uint8)
+    assert lib.svbrdf_batched_plan(mats, 1, ctypes.byref(cfg), buf.ctypes.data, n) == 0
+    need = lib.svbrdf_batched_workspace_bytes(buf.ctypes.data)
+    buf[0:4] = 0  # the magic
+    fake = ctypes.c_void_p(16)
+    assert lib.svbrdf_batched_workspace_bytes(buf.ctypes.data) == 0
+    assert lib.svbrdf_batched_steps(fake, buf.ctypes.data, 1, fake, 0.01, 0.9, 0.999, 1e-8, fake, 4, 3, fake, need,
+                                    None) == -1
+    assert b"not a plan" in lib.svbrdf_last_error()
+    # the wait self-test needs its 16-byte workspace and a sane poll limit
+    assert lib.svbrdf_selftest_wait_timeout(fake, 8, 100, None) == -4
+    assert lib.svbrdf_selftest_wait_timeout(fake, 16, 0, None) == -1

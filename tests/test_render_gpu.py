@@ -56,7 +56,7 @@ def test_adjoint_general_matches_reference(svb, golden, cuda, kind):
     assert rel_l2(tex.grad, g64) <= tol
     assert rel_l2(tex.grad, g32) <= tol
     assert rel_l2(lp.grad, d[f"gradpow_{kind}64"]) <= 1e-4
-    assert abs(float(loss) - float(d[f"loss_{kind}64"])) <= 1e-5 * float(d[f"loss_{kind}64"])
+    assert abs(float(loss.detach()) - float(d[f"loss_{kind}64"])) <= 1e-5 * float(d[f"loss_{kind}64"])
 
 
 def test_adjoint_coloc_matches_reference(svb, golden, cuda):

@@ -1,4 +1,6 @@
-"""FP64 CPU oracle of the descriptor loss.
+"""FP64 CPU oracle of the descriptor loss. Parity unpinned: the reference's VGGLoss needs
+torchvision (absent here) and pretrained weights (not offline), so no golden vectors exist
+for it; this is a restatement of its source.
 
 TEST INFRASTRUCTURE ONLY (tests and bench's CPU legs). Restates the VGG-feature loss of
 src/descriptor.py:7-79 with the stack the GPU module uses: 2x2 box downsample, ImageNet

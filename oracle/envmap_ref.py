@@ -1,4 +1,6 @@
-"""CPU oracle of the environment-map renderer (numpy, FP64).
+"""CPU oracle of the environment-map renderer (numpy, FP64). Parity unpinned: the reference
+renders with Mitsuba 3 (not installed) under fig/ennis.exr (missing), so no golden images
+exist; this is a restatement of the scene and of the direct-illumination algorithm.
 
 TEST INFRASTRUCTURE ONLY (tests). Restates, step by step, the direct-illumination renderer
 that svbrdf_envmap_render runs on the GPU for the reference's novel-view video

@@ -11,11 +11,12 @@ diffuse lobe, read from the stored texture parameters the way the reference's PN
 encode them (sRGB values for diffuse, specular and roughness, raw normals).
 
 ``fig/ennis.exr`` is not in the reference repository, so ``synthetic_envmap`` makes a seeded
-stand-in (sky gradient, ground, a few bright lobes). Any [He, We, 3] linear-radiance array
-can be passed instead.
+stand-in (sky gradient, ground, a few bright lobes). Any [He, We, 3] linear-radiance array,
+or a lat-long OpenEXR file (``imageio.exr_read``), can be passed instead.
 """
 from __future__ import annotations
 
+import pathlib
 from typing import List, Optional, Sequence
 
 import numpy as np
@@ -79,7 +80,8 @@ class EnvmapRenderer:
     """``MitsubaRender``'s interface (src/mitsubarender.py:7-19) on the GPU.
 
     ``EnvmapRenderer(im_size, envmap, textures)``: ``im_size`` [res, res]; ``envmap`` a
-    [He, We, 3] linear-radiance array (None: ``synthetic_envmap()``); ``textures`` the
+    [He, We, 3] linear-radiance array or the path of a lat-long OpenEXR file (None:
+    ``synthetic_envmap()``); ``textures`` the
     material's [9, H, W] (or [1, 9, H, W]) parameters in [-1, 1], the layout the optimisers
     produce. ``render(angle, light_intensity)`` returns the [res, res, 3] image clipped to
     [0, 1] and raised to 1/2.2, as the reference's does."""
@@ -94,7 +96,12 @@ class EnvmapRenderer:
         self.load_envmap(synthetic_envmap() if envmap is None else envmap)
         self.load_texturemaps(textures)
 
-    def load_envmap(self, env: np.ndarray):
+    def load_envmap(self, env):
+        """A [He, We, 3] linear-radiance array, or the path of a lat-long OpenEXR file."""
+        if isinstance(env, (str, pathlib.Path)):
+            from .imageio import exr_read
+
+            env = exr_read(env)
         env = np.ascontiguousarray(env, dtype=np.float32)
         if env.ndim != 3 or env.shape[2] != 3:
             raise ValueError("envmap must be [He, We, 3]")

@@ -203,3 +203,148 @@ def imwrite(im, filename, flag=None, dim=None) -> None:
     elif flag == "normal":
         im = (im.clip(-1, 1) + 1) / 2
     png_write(filename, (im * 255).astype(np.uint8))
+
+
+# ---------------------------------------------------------------- OpenEXR (scanline)
+# The reference lights its novel-view video with an OpenEXR environment map
+# (src/scripts.py:47, fig/ennis.exr, read by Mitsuba). This is a reader and writer of
+# single-part scanline OpenEXR files, following the published file layout: magic 20000630,
+# version 2, the attribute header (channels, compression, dataWindow, ...), an offset table
+# of 64-bit chunk positions, then chunks of (y, size, data) holding per line each channel's
+# samples in channel-name order. Supported: HALF and FLOAT channels, compressions NONE,
+# ZIPS (one line per chunk) and ZIP (16 lines): zlib over bytes that were delta-coded
+# (d[i] = b[i] - b[i-1] + 128) and split into even and odd halves. Tiled, deep, multi-part
+# and the other compressions are refused with a clear error.
+
+_EXR_MAGIC = 20000630
+_EXR_LINES = {0: 1, 2: 1, 3: 16}  # compression -> scanlines per chunk
+_EXR_TYPES = {1: np.float16, 2: np.float32}
+
+
+def _exr_unpredict(t: np.ndarray) -> np.ndarray:
+    """Inverse of the ZIP predictor: b[0] = d[0], b[i] = (b[i-1] + d[i] - 128) mod 256."""
+    out = np.empty_like(t)
+    if t.size:
+        out[0] = t[0]
+        out[1:] = (t[0] + np.cumsum(t[1:].astype(np.int64) - 128)) % 256
+    return out
+
+
+def _exr_deinterleave(t: np.ndarray) -> np.ndarray:
+    """The predictor's input was bytes 0, 2, 4, ... followed by bytes 1, 3, 5, ..."""
+    half = (t.size + 1) // 2
+    out = np.empty_like(t)
+    out[0::2] = t[:half]
+    out[1::2] = t[half:]
+    return out
+
+
+def _exr_decode_zip(data: bytes, raw_size: int) -> bytes:
+    if len(data) == raw_size:
+        return data
+    t = np.frombuffer(zlib.decompress(data), dtype=np.uint8)
+    if t.size != raw_size:
+        raise ValueError("EXR chunk decompresses to the wrong size")
+    return _exr_deinterleave(_exr_unpredict(t)).astype(np.uint8).tobytes()
+
+
+def _exr_encode_zip(raw: bytes) -> bytes:
+    b = np.frombuffer(raw, dtype=np.uint8)
+    t = np.concatenate([b[0::2], b[1::2]]).astype(np.int64)
+    d = t.copy()
+    d[1:] = (t[1:] - t[:-1] + 128) % 256
+    z = zlib.compress(d.astype(np.uint8).tobytes(), 6)
+    return z if len(z) < len(raw) else raw
+
+
+def exr_read(path) -> np.ndarray:
+    """[H, W, 3] float32 RGB of a scanline OpenEXR file (a single Y channel is repeated)."""
+    buf = pathlib.Path(path).read_bytes()
+    if len(buf) < 8 or struct.unpack_from("<i", buf, 0)[0] != _EXR_MAGIC:
+        raise ValueError(f"{path}: not an OpenEXR file")
+    version = struct.unpack_from("<i", buf, 4)[0]
+    if version & 0xFF != 2 or version & (0x200 | 0x800 | 0x1000):
+        raise ValueError(f"{path}: only single-part scanline OpenEXR files are supported")
+    pos, attrs = 8, {}
+    while True:
+        end = buf.index(b"\0", pos)
+        name = buf[pos:end].decode()
+        pos = end + 1
+        if not name:
+            break
+        end = buf.index(b"\0", pos)
+        typ = buf[pos:end].decode()
+        size = struct.unpack_from("<i", buf, end + 1)[0]
+        attrs[name] = (typ, buf[end + 5:end + 5 + size])
+        pos = end + 5 + size
+    chans = []
+    raw = attrs["channels"][1]
+    q = 0
+    while raw[q] != 0:
+        end = raw.index(b"\0", q)
+        cname = raw[q:end].decode()
+        ptype, _, xs, ys = struct.unpack_from("<iB3xii", raw, end + 1)
+        if ptype not in _EXR_TYPES or xs != 1 or ys != 1:
+            raise ValueError(f"{path}: channel {cname}: only unsubsampled HALF/FLOAT channels are supported")
+        chans.append((cname, _EXR_TYPES[ptype]))
+        q = end + 1 + 16
+    comp = attrs["compression"][1][0]
+    if comp not in _EXR_LINES:
+        raise ValueError(f"{path}: compression {comp} is not supported (NONE, ZIPS and ZIP are)")
+    x0, y0, x1, y1 = struct.unpack("<iiii", attrs["dataWindow"][1])
+    w, h = x1 - x0 + 1, y1 - y0 + 1
+    lines = _EXR_LINES[comp]
+    nchunks = (h + lines - 1) // lines
+    offsets = struct.unpack_from(f"<{nchunks}Q", buf, pos)
+    line_bytes = sum(np.dtype(t).itemsize for _, t in chans) * w
+    planes = {c: np.zeros((h, w), np.float32) for c, _ in chans}
+    for off in offsets:
+        y, size = struct.unpack_from("<ii", buf, off)
+        first = y - y0
+        n = min(lines, h - first)
+        data = buf[off + 8:off + 8 + size]
+        block = data if comp == 0 else _exr_decode_zip(data, n * line_bytes)
+        p = 0
+        for r in range(n):
+            for c, t in chans:
+                nb = np.dtype(t).itemsize * w
+                planes[c][first + r] = np.frombuffer(block, dtype=np.dtype(t).newbyteorder("<"), count=w, offset=p)
+                p += nb
+    if all(c in planes for c in "RGB"):
+        return np.stack([planes["R"], planes["G"], planes["B"]], -1)
+    if "Y" in planes:
+        return np.repeat(planes["Y"][..., None], 3, -1)
+    raise ValueError(f"{path}: no R, G, B or Y channels")
+
+
+def exr_write(path, rgb: np.ndarray, half: bool = True, compression: str = "zip") -> None:
+    """Write [H, W, 3] RGB as a scanline OpenEXR file (HALF or FLOAT; "none", "zips", "zip")."""
+    rgb = np.asarray(rgb, dtype=np.float32)
+    h, w = rgb.shape[:2]
+    comp = {"none": 0, "zips": 2, "zip": 3}[compression]
+    dt = np.float16 if half else np.float32
+
+    def attr(name, typ, value):
+        return name.encode() + b"\0" + typ.encode() + b"\0" + struct.pack("<i", len(value)) + value
+
+    chl = b"".join(c.encode() + b"\0" + struct.pack("<iB3xii", 1 if half else 2, 0, 1, 1) for c in "BGR") + b"\0"
+    header = (struct.pack("<ii", _EXR_MAGIC, 2) + attr("channels", "chlist", chl) +
+              attr("compression", "compression", bytes([comp])) +
+              attr("dataWindow", "box2i", struct.pack("<iiii", 0, 0, w - 1, h - 1)) +
+              attr("displayWindow", "box2i", struct.pack("<iiii", 0, 0, w - 1, h - 1)) +
+              attr("lineOrder", "lineOrder", bytes([0])) + attr("pixelAspectRatio", "float", struct.pack("<f", 1.0)) +
+              attr("screenWindowCenter", "v2f", struct.pack("<ff", 0.0, 0.0)) +
+              attr("screenWindowWidth", "float", struct.pack("<f", 1.0)) + b"\0")
+    lines = _EXR_LINES[comp]
+    chunks = []
+    for y in range(0, h, lines):
+        block = b"".join(rgb[r, :, ci].astype(dt).astype(np.dtype(dt).newbyteorder("<")).tobytes()
+                         for r in range(y, min(h, y + lines)) for ci in (2, 1, 0))
+        data = block if comp == 0 else _exr_encode_zip(block)
+        chunks.append(struct.pack("<ii", y, len(data)) + data)
+    pos = len(header) + 8 * len(chunks)
+    offsets = []
+    for c in chunks:
+        offsets.append(pos)
+        pos += len(c)
+    pathlib.Path(path).write_bytes(header + struct.pack(f"<{len(offsets)}Q", *offsets) + b"".join(chunks))

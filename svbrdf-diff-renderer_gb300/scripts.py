@@ -1,4 +1,5 @@
-"""Pipeline drop-ins: ``render`` and ``optim_perpixel`` (src/scripts.py:31-41, 67-97).
+"""Pipeline drop-ins: ``render``, ``render_envmap`` and ``optim_perpixel``
+(src/scripts.py:31-41, 44-59, 67-97).
 
 Same arguments and file layout as the reference: a scene JSON read by ``SvbrdfIO``,
 target photos ``{idx:02d}.png`` in ``target_dir``, maps ``nom/dif/spe/rgh.png`` in
@@ -12,7 +13,7 @@ import pathlib
 import torch
 
 from .microfacet import Microfacet
-from .svbrdf import SvbrdfIO, SvbrdfOptim
+from .svbrdf import SvbrdfIO, SvbrdfOptim, load_texture_maps
 
 
 def render(json_dir, res, device="cuda:0"):
@@ -24,6 +25,25 @@ def render(json_dir, res, device="cuda:0"):
         out = r.eval(textures)
     io.save_images_th(out, io.target_dir)
     return out
+
+
+def render_envmap(data_dir, res, envmap=None, device="cuda:0", spp=256, seed=0):
+    """The novel-view video of the maps in ``data_dir`` (src/scripts.py:44-59): the material
+    (nom/dif/spe/rgh.png at their own size) under ``envmap`` (an OpenEXR path or a [He, We, 3]
+    array; None: the seeded synthetic environment), written as ``data_dir/vid/000.png`` ...
+    ``115.png``: 59 angles forward, then 57 back, light intensity 0.5. The reference also
+    packs them into a GIF with Pillow, which is not available here. Returns the frames."""
+    from .envmap import EnvmapRenderer
+    from .imageio import imwrite
+
+    data_dir = pathlib.Path(data_dir)
+    vid = data_dir / "vid"
+    vid.mkdir(parents=True, exist_ok=True)
+    textures = load_texture_maps(data_dir, None, device)
+    frames = EnvmapRenderer([res, res], envmap, textures, device=device, spp=spp, seed=seed).render_video(59, 0.5)
+    for i, f in enumerate(frames):
+        imwrite(f, vid / f"{i:03d}.png", flag="srgb")
+    return frames
 
 
 def optim_perpixel(json_dir, res, lr, epochs, tex_init, optim_light=False, device="cuda:0", loss="mse",

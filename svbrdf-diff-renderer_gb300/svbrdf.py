@@ -232,6 +232,24 @@ class SvbrdfOptim:
         self.light_pow = lp_dev
 
 
+def load_texture_maps(textures_dir, res=None, device="cpu") -> torch.Tensor:
+    """[1, 9, H, W] parameters in [-1, 1] from nom/dif/spe/rgh.png (src/svbrdf.py:150-166),
+    resized to res x res (None: the files' own size)."""
+    from .imageio import imread
+
+    d = pathlib.Path(textures_dir)
+    dim = (res, res) if res is not None else None
+    normal = imread(d / "nom.png", "normal", dim)
+    diffuse = imread(d / "dif.png", "srgb", dim)
+    specular = imread(d / "spe.png", "srgb", dim)
+    roughness = imread(d / "rgh.png", "rough", dim)
+    t = lambda a: torch.from_numpy(a).to(device)
+    return torch.cat((t(diffuse * 2 - 1).permute(2, 0, 1).unsqueeze(0),
+                      t(normal).permute(2, 0, 1).unsqueeze(0)[:, :2],
+                      t(roughness * 2 - 1).unsqueeze(0).unsqueeze(0),
+                      t(specular * 2 - 1).permute(2, 0, 1).unsqueeze(0)), 1)
+
+
 def _optimiser_state(o) -> dict:
     st = {"textures": o.textures.detach().clone(), "step": int(getattr(o, "_step", 0)),
           "loss_image_list": list(getattr(o, "loss_image_list", []))}
@@ -285,18 +303,7 @@ class SvbrdfIO:
 
     def load_textures_th(self, textures_dir, res):
         """[1, 9, res, res] in [-1, 1] from nom/dif/spe/rgh.png (src/svbrdf.py:150-166)."""
-        from .imageio import imread
-
-        d = pathlib.Path(textures_dir)
-        normal = imread(d / "nom.png", "normal", (res, res))
-        diffuse = imread(d / "dif.png", "srgb", (res, res))
-        specular = imread(d / "spe.png", "srgb", (res, res))
-        roughness = imread(d / "rgh.png", "rough", (res, res))
-        t = lambda a: torch.from_numpy(a).to(self.device)
-        return torch.cat((t(diffuse * 2 - 1).permute(2, 0, 1).unsqueeze(0),
-                          t(normal).permute(2, 0, 1).unsqueeze(0)[:, :2],
-                          t(roughness * 2 - 1).unsqueeze(0).unsqueeze(0),
-                          t(specular * 2 - 1).permute(2, 0, 1).unsqueeze(0)), 1)
+        return load_texture_maps(textures_dir, res, self.device)
 
     @staticmethod
     def _normal3(t2):

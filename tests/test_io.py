@@ -189,3 +189,30 @@ def test_envmap_renderer_reads_exr_path(svb, tmp_path):
     r = svb.EnvmapRenderer([16, 16], p, torch.zeros(9, 4, 4), device="cpu")
     assert np.array_equal(r.env_np, env)
     assert r.tables_np[0].shape == (9,)
+
+
+def test_render_envmap_writes_the_video_frames(svb, tmp_path, monkeypatch):
+    """render_envmap (src/scripts.py:44-59): maps read from the folder at their own size,
+    116 frames written as vid/000.png .. 115.png. The renderer is replaced by a stand-in here
+    (no GPU on this machine); its own kernel is tested on the GPU."""
+    g = np.random.default_rng(0)
+    svb.imageio.imwrite(g.random((12, 10, 3)), tmp_path / "dif.png", flag="srgb")
+    svb.imageio.imwrite(g.random((12, 10, 3)), tmp_path / "spe.png", flag="srgb")
+    svb.imageio.imwrite(g.random((12, 10)), tmp_path / "rgh.png", flag="rough")
+    n = np.zeros((12, 10, 3)); n[..., 2] = 1.0
+    svb.imageio.imwrite(n, tmp_path / "nom.png", flag="normal")
+    seen = {}
+
+    def fake_video(self, n=59, light_intensity=0.5):
+        seen["tex"] = tuple(self.textures.shape)
+        seen["args"] = (n, light_intensity)
+        fwd = [np.full((8, 8, 3), k / 60.0, np.float32) for k in range(n)]
+        return fwd + fwd[-2:0:-1]
+
+    monkeypatch.setattr(svb.envmap.EnvmapRenderer, "render_video", fake_video)
+    frames = svb.render_envmap(tmp_path, 8, envmap=np.ones((4, 8, 3), np.float32), device="cpu")
+    assert seen["tex"] == (9, 12, 10) and seen["args"] == (59, 0.5)
+    assert len(frames) == 116
+    files = sorted((tmp_path / "vid").glob("*.png"))
+    assert [f.name for f in files[:2]] == ["000.png", "001.png"] and len(files) == 116
+    assert np.allclose(svb.imageio.imread(files[115], "srgb"), 1 / 60.0, atol=1 / 255)

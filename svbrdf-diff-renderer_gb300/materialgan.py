@@ -609,14 +609,19 @@ class MaterialGANOptim:
 
     def optim(self, epochs, lr, svbrdf_obj=None, optim_light=False, reset_adam_each_iter=True, graph=True):
         """``epochs = [total, l, n]``: alternate l latent epochs and n noise epochs. With
-        ``graph`` (and the reference's fresh Adam each epoch, no descriptor term) each epoch
-        is one CUDA-graph replay."""
+        ``graph`` (and the reference's fresh Adam each epoch, no descriptor term, no light
+        optimisation) each epoch is one CUDA-graph replay.
+
+        ``optim_light``: the light power ``svbrdf_obj.cl[2]`` joins each epoch's Adam and is
+        handed to the renderer before each render, as src/materialgan.py:110-135 does; it is
+        left as the optimised leaf in ``svbrdf_obj.cl[2]`` and in the renderer."""
         total, l_ep, n_ep = epochs
         cycle = l_ep + n_ep
         # this call's losses stay on the device and are read once at the end; the lists
         # accumulate over calls, as the reference's do
         img_losses, feat_losses = [], []
-        if graph and reset_adam_each_iter and self.descriptor is None and self.device.type == "cuda":
+        if (graph and reset_adam_each_iter and self.descriptor is None and self.device.type == "cuda"
+                and not optim_light):
             for epoch in range(total):
                 g, loss, _ = self._graph_for((epoch % cycle) < l_ep, lr)
                 g.replay()
@@ -627,13 +632,22 @@ class MaterialGANOptim:
             if img_losses:
                 self.loss_image_list += [float(x) for x in torch.stack(img_losses).tolist()]
             return self.textures
+        light = None
+        if optim_light:
+            if svbrdf_obj is None or not hasattr(svbrdf_obj, "cl"):
+                raise ValueError("optim_light needs svbrdf_obj with the scene's cl = [camera, light, light power]")
+            light = torch.as_tensor(svbrdf_obj.cl[2]).detach().to(self.device, torch.float32).clone()
+            light.requires_grad_(True)
+            svbrdf_obj.cl[2] = light
         opt = None
         for epoch in range(total):
             phase_latent = (epoch % cycle) < l_ep
-            params = [self.latent] if phase_latent else self.noises
+            params = ([self.latent] if phase_latent else list(self.noises)) + ([light] if light is not None else [])
             if opt is None or reset_adam_each_iter or getattr(self, "_phase", None) != phase_latent:
                 opt = torch.optim.Adam(params, lr=lr, betas=(0.9, 0.999))
             self._phase = phase_latent
+            if light is not None:
+                self.renderer_obj.update_light(light)
             textures = self.latent_to_textures()
             rendered = self.renderer_obj.eval(textures)
             loss = torch.nn.functional.mse_loss(rendered, self.targets)

@@ -1,5 +1,5 @@
-"""Pipeline drop-ins: ``render``, ``render_envmap`` and ``optim_perpixel``
-(src/scripts.py:31-41, 44-59, 67-97).
+"""Pipeline drop-ins: ``render``, ``render_envmap``, ``optim_perpixel`` and
+``optim_ganlatent`` (src/scripts.py:31-41, 44-59, 67-97, 100-143).
 
 Same arguments and file layout as the reference: a scene JSON read by ``SvbrdfIO``,
 target photos ``{idx:02d}.png`` in ``target_dir``, maps ``nom/dif/spe/rgh.png`` in
@@ -74,5 +74,47 @@ def optim_perpixel(json_dir, res, lr, epochs, tex_init, optim_light=False, devic
         renderer.update_light(io.cl[2].detach())
     with torch.no_grad():
         out = renderer.eval(opt.textures.detach().clamp(-1, 1))
+    io.save_images_th(out, io.rerender_dir)
+    return opt
+
+
+def optim_ganlatent(json_dir, res, lr, epochs, tex_init, optim_light=False, device="cuda:0", generator=None,
+                    seed=0):
+    """MaterialGAN latent fit (src/scripts.py:100-143): targets -> latent (and noise) Adam
+    through the generator and the renderer -> maps in ``optimize_dir``, re-renders in
+    ``rerender_dir``.
+
+    ``epochs`` is [total, latent epochs, noise epochs] per cycle. ``tex_init`` follows the
+    reference's ``init_from`` (src/materialgan.py:58-75): [] starts from the truncated
+    mapping of a random z with random noise, [latent.pt] from a saved latent with the
+    average (zero) noise, [latent.pt, noise.pt] from both (``MaterialGANOptim.save_latent``'s
+    files). The reference's "auto" choice between its two downloaded starting latents needs
+    those checkpoints, which are not available offline. ``generator`` defaults to the
+    seeded StyleGAN2-shaped generator at ``res`` (the trained MaterialGAN weights are not
+    available either). Returns the ``MaterialGANOptim``.
+    """
+    from .materialgan import MaterialGANOptim, StyleGAN2Generator
+
+    if tex_init == "auto":
+        raise ValueError("tex_init 'auto' needs the reference's latent_avg / latent_const checkpoints, which are "
+                         "downloaded at run time and not available offline; pass [latent.pt] or [latent.pt, noise.pt]")
+    paths = list(tex_init or [])
+    if len(paths) > 2:
+        raise ValueError("tex_init holds at most a latent file and a noise file")
+    io = SvbrdfIO(pathlib.Path(json_dir), device)
+    targets = io.load_images_th(io.target_dir, res)
+    renderer = Microfacet(res, io.n_of_imgs, io.im_size, io.cl, device)
+    gen = generator if generator is not None else StyleGAN2Generator(res, seed=seed)
+    opt = MaterialGANOptim(device, renderer, gen)
+    opt.load_targets(targets)
+    opt.init_from(batch=1, seed=seed, noise="random" if not paths else "zero")
+    if paths:
+        opt.load_latent(paths[0], paths[1] if len(paths) == 2 else None)
+    textures = opt.optim(epochs, lr, io, optim_light)
+    io.save_textures_th(textures, io.optimize_dir)
+    if optim_light:
+        renderer.update_light(io.cl[2].detach())
+    with torch.no_grad():
+        out = renderer.eval(textures)
     io.save_images_th(out, io.rerender_dir)
     return opt

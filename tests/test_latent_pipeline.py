@@ -1,0 +1,101 @@
+"""The latent-loop script and light optimisation on the CPU: the renderer is the oracle's
+differentiable torch render behind Microfacet's interface, the generator a small seeded one,
+so the host logic (initialisation modes, light handling, files) runs without a GPU. The CUDA
+paths of the same loop are tested in test_materialgan.py."""
+import json
+import types
+
+import pytest
+import torch
+
+from oracle import microfacet_ref as R
+
+
+class TorchRenderer:
+    """Microfacet's interface (.res, .n_of_imgs, .update_light, .eval) on the oracle."""
+
+    def __init__(self, res, n, size, cl, device="cpu"):
+        self.res, self.n_of_imgs, self.size = res, n, float(size)
+        self.cam, self.lit = torch.as_tensor(cl[0]).float(), torch.as_tensor(cl[1]).float()
+        self.light_pow = torch.as_tensor(cl[2]).float()
+
+    def update_light(self, light_pow):
+        self.light_pow = light_pow
+
+    def eval(self, textures):
+        return R.render(textures, self.cam, self.lit, self.light_pow, self.size, torch.float32)
+
+
+def _setup(svb, res=16):
+    sc = svb.scenes.single_scene(res=res, seed=1016)
+    tg = R.render(sc.gt, sc.camera_pos, sc.light_pos, sc.light_pow * 1.3, sc.size, torch.float32)
+    gen = svb.materialgan.StyleGAN2Generator(resolution=res, fmap_max=16, w_dim=32, seed=1, channels_last=False)
+    return sc, tg, gen
+
+
+def test_latent_loop_optimises_the_light(svb):
+    sc, tg, gen = _setup(svb)
+    r = TorchRenderer(16, 9, sc.size, sc.cl)
+    o = svb.materialgan.MaterialGANOptim("cpu", r, gen)
+    o.load_targets(tg)
+    o.init_from(batch=1, seed=2)
+    scene = types.SimpleNamespace(cl=[sc.camera_pos, sc.light_pos, sc.light_pow.clone()])
+    o.optim([8, 2, 2], 0.05, scene, optim_light=True)
+    light = scene.cl[2]
+    assert light.requires_grad and light.is_leaf and r.light_pow is light
+    assert not torch.allclose(light.detach(), sc.light_pow)  # the light moved
+    assert len(o.loss_image_list) == 8 and all(x == x for x in o.loss_image_list)
+    with pytest.raises(ValueError):
+        o.optim([1, 1, 1], 0.05, None, optim_light=True)
+
+
+def _scene_dir(svb, tmp_path, sc):
+    cams = sc.camera_pos.tolist()
+    cfg = {"reference_dir": "ref", "target_dir": "target", "optimize_dir": "optim", "rerender_dir": "rerender",
+           "im_size": sc.size, "idx": list(range(9)), "camera_pos": cams, "light_pos": cams,
+           "light_pow": sc.light_pow.tolist()}
+    j = tmp_path / "scene.json"
+    j.write_text(json.dumps(cfg))
+    io = svb.SvbrdfIO(j, "cpu")
+    io.save_images_th(R.render(sc.gt, sc.camera_pos, sc.light_pos, sc.light_pow, sc.size, torch.float32),
+                      io.target_dir)
+    return j
+
+
+@pytest.mark.parametrize("init", ["none", "latent", "latent+noise"])
+def test_optim_ganlatent_script(svb, tmp_path, monkeypatch, init):
+    """optim_ganlatent (src/scripts.py:100-143): the three tex_init forms, the output files."""
+    sc, _, gen = _setup(svb)
+    j = _scene_dir(svb, tmp_path, sc)
+    monkeypatch.setattr(svb.scripts, "Microfacet", TorchRenderer)
+    tex_init = []
+    if init != "none":
+        seed_opt = svb.materialgan.MaterialGANOptim("cpu", TorchRenderer(16, 9, sc.size, sc.cl), gen)
+        seed_opt.init_from(batch=1, seed=7, noise="random")
+        seed_opt.save_latent(tmp_path / "optim_latent.pt", tmp_path / "optim_noise.pt")
+        tex_init = [tmp_path / "optim_latent.pt"] + ([tmp_path / "optim_noise.pt"] if init == "latent+noise" else [])
+    start = {}
+    real_optim = svb.materialgan.MaterialGANOptim.optim
+
+    def spy(self, *a, **k):  # the state the optimisation starts from
+        start["latent"] = self.latent.detach().clone()
+        start["noises"] = [n.detach().clone() for n in self.noises]
+        return real_optim(self, *a, **k)
+
+    monkeypatch.setattr(svb.materialgan.MaterialGANOptim, "optim", spy)
+    opt = svb.optim_ganlatent(j, 16, 0.02, [4, 2, 1], tex_init, device="cpu", generator=gen)
+    assert len(opt.loss_image_list) == 4
+    for name in ("nom.png", "dif.png", "spe.png", "rgh.png"):
+        assert (tmp_path / "optim" / name).exists()
+    assert (tmp_path / "rerender" / "08.png").exists()
+    if init != "none":
+        assert torch.equal(start["latent"], torch.load(tmp_path / "optim_latent.pt"))
+    if init == "latent":  # a latent alone starts from the reference's average (zero) noise
+        assert all(float(n.abs().max()) == 0.0 for n in start["noises"])
+    if init == "latent+noise":
+        saved = torch.load(tmp_path / "optim_noise.pt")
+        assert all(torch.equal(a, b) for a, b in zip(start["noises"], saved))
+    if init == "none":  # random noise, as init_from([]) draws
+        assert any(float(n.abs().max()) > 0.0 for n in start["noises"])
+    with pytest.raises(ValueError):
+        svb.optim_ganlatent(j, 16, 0.02, [1, 1, 1], "auto", device="cpu", generator=gen)

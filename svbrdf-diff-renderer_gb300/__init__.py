@@ -18,11 +18,11 @@ from ._native import SvbrdfError, build
 from .batched import BatchConfig, BatchedOptim, BatchedPipeline, autotune
 from .microfacet import Microfacet
 from .svbrdf import SvbrdfIO, SvbrdfOptim
-from .scripts import optim_ganlatent, optim_perpixel, render, render_envmap
+from .scripts import gen_textures_from_materialgan, optim_ganlatent, optim_perpixel, render, render_envmap
 from . import descriptor, envmap, imageio, materialgan, scenes
 from .envmap import EnvmapRenderer
 
 __all__ = ["Microfacet", "SvbrdfOptim", "SvbrdfIO", "optim_perpixel", "render", "BatchedOptim", "BatchedPipeline",
-           "EnvmapRenderer", "render_envmap", "optim_ganlatent",
+           "EnvmapRenderer", "render_envmap", "optim_ganlatent", "gen_textures_from_materialgan",
            "BatchConfig",
            "autotune", "SvbrdfError", "build", "scenes", "imageio", "descriptor", "materialgan", "_native"]

@@ -1,5 +1,5 @@
-"""Pipeline drop-ins: ``render``, ``render_envmap``, ``optim_perpixel`` and
-``optim_ganlatent`` (src/scripts.py:31-41, 44-59, 67-97, 100-143).
+"""Pipeline drop-ins: ``gen_textures_from_materialgan``, ``render``, ``render_envmap``,
+``optim_perpixel`` and ``optim_ganlatent`` (src/scripts.py:18-143).
 
 Same arguments and file layout as the reference: a scene JSON read by ``SvbrdfIO``,
 target photos ``{idx:02d}.png`` in ``target_dir``, maps ``nom/dif/spe/rgh.png`` in
@@ -14,6 +14,23 @@ import torch
 
 from .microfacet import Microfacet
 from .svbrdf import SvbrdfIO, SvbrdfOptim, load_texture_maps
+
+
+def gen_textures_from_materialgan(json_dir, device="cuda:0", generator=None, seed=0):
+    """Maps of a random material from the generator into ``reference_dir``
+    (src/scripts.py:18-28): the truncated mapping of a random z, no optimisation. The
+    generator defaults to the seeded StyleGAN2-shaped one at 256 (the trained MaterialGAN
+    weights are downloaded at run time by the reference and are not available offline)."""
+    from .materialgan import MaterialGANOptim, StyleGAN2Generator
+
+    io = SvbrdfIO(pathlib.Path(json_dir), device)
+    gen = generator if generator is not None else StyleGAN2Generator(256, seed=seed)
+    opt = MaterialGANOptim(device, None, gen)
+    opt.init_from(batch=1, seed=seed, noise="random")
+    with torch.no_grad():
+        textures = opt.latent_to_textures().detach()
+    io.save_textures_th(textures, io.reference_dir)
+    return textures
 
 
 def render(json_dir, res, device="cuda:0"):

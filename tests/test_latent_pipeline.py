@@ -99,3 +99,15 @@ def test_optim_ganlatent_script(svb, tmp_path, monkeypatch, init):
         assert any(float(n.abs().max()) > 0.0 for n in start["noises"])
     with pytest.raises(ValueError):
         svb.optim_ganlatent(j, 16, 0.02, [1, 1, 1], "auto", device="cpu", generator=gen)
+
+
+def test_gen_textures_from_materialgan(svb, tmp_path):
+    """src/scripts.py:18-28: a random material's maps written to reference_dir."""
+    sc, _, gen = _setup(svb)
+    j = _scene_dir(svb, tmp_path, sc)
+    t = svb.gen_textures_from_materialgan(j, device="cpu", generator=gen, seed=4)
+    assert t.shape == (1, 9, 16, 16) and float(t.abs().max()) <= 1.0
+    for name in ("nom.png", "dif.png", "spe.png", "rgh.png"):
+        assert (tmp_path / "ref" / name).exists()
+    back = svb.SvbrdfIO(j, "cpu").load_textures_th(tmp_path / "ref", 16)
+    assert float((back[:, 0:3] - t[:, 0:3]).abs().max()) <= 2.0 / 255 + 1e-6  # 8-bit PNG round trip

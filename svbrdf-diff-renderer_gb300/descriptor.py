@@ -348,6 +348,16 @@ class VGGDescriptor:
         return fl, gl, dr
 
 
+def reference_descriptors(device="cuda", seed: int = 0):
+    """The reference latent loop's two feature losses (src/materialgan.py:28-34): the VGG in
+    the reference's own semantics, hook weights [1, 1, 4, 8] / 14 for latent epochs and
+    [8, 8, 2, 1] / 19 for noise epochs, the same network weights. The pair is
+    MaterialGANOptim's ``descriptor``."""
+    large = VGGDescriptor(device, seed=seed, weights=[w / 14 for w in (1, 1, 4, 8)], mode="reference")
+    small = VGGDescriptor(device, seed=seed, weights=[w / 19 for w in (8, 8, 2, 1)], mode="reference")
+    return large, small
+
+
 class _DescriptorLoss(torch.autograd.Function):
     """(feature, Gram) losses with the hand-written backward chain of VGGDescriptor."""
 

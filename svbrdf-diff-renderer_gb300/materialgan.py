@@ -514,7 +514,11 @@ def latent_to_textures(gen: StyleGAN2Generator, latent: torch.Tensor, noises=Non
 
 
 class MaterialGANOptim:
-    """Latent (W+) and noise optimisation through the renderer (src/materialgan.py:21-206)."""
+    """Latent (W+) and noise optimisation through the renderer (src/materialgan.py:21-206).
+
+    ``descriptor``: None (image loss only), one feature loss, or a (latent-phase,
+    noise-phase) pair such as ``descriptor.reference_descriptors()``, the reference's "L"
+    and "N" VGG losses; the feature term is weighted by ``descriptor_weight`` (0.1)."""
 
     def __init__(self, device, renderer_obj, generator: StyleGAN2Generator, descriptor=None,
                  descriptor_weight: float = 0.1):
@@ -556,12 +560,26 @@ class MaterialGANOptim:
                            for n in torch.load(noise_path, map_location="cpu")]
         self._graphs = {}  # captured epochs hold the previous parameters' addresses
 
+    def _descriptors(self):
+        d = self.descriptor
+        if d is None:
+            return []
+        return list(d) if isinstance(d, (tuple, list)) else [d]
+
+    def _descriptor_for(self, phase_latent: bool):
+        """The feature loss of this phase: a (latent-phase, noise-phase) pair picks by phase,
+        as the reference's "L" and "N" losses do (src/materialgan.py:28-34, 137-139)."""
+        d = self.descriptor
+        if isinstance(d, (tuple, list)):
+            return d[0] if phase_latent else d[1]
+        return d
+
     def load_targets(self, targets: torch.Tensor):
         """targets [B*V, 3, H, W] (materials major)."""
         self.targets = targets.to(self.device, torch.float32).contiguous()
         self._graphs = {}
-        if self.descriptor is not None:
-            self.descriptor.load(self.targets)
+        for d in self._descriptors():
+            d.load(self.targets)
 
     def latent_to_textures(self, latent=None):
         return latent_to_textures(self.net, self.latent if latent is None else latent, self.noises)
@@ -652,10 +670,11 @@ class MaterialGANOptim:
             rendered = self.renderer_obj.eval(textures)
             loss = torch.nn.functional.mse_loss(rendered, self.targets)
             img_losses.append(loss.detach())
-            if self.descriptor is not None:
+            desc = self._descriptor_for(phase_latent)
+            if desc is not None:
                 from .descriptor import descriptor_term
 
-                fl = descriptor_term(rendered, self.descriptor) * self.descriptor_weight
+                fl = descriptor_term(rendered, desc) * self.descriptor_weight
                 feat_losses.append(fl.detach())
                 loss = loss + fl
             opt.zero_grad()

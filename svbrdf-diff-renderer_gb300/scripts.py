@@ -96,7 +96,7 @@ def optim_perpixel(json_dir, res, lr, epochs, tex_init, optim_light=False, devic
 
 
 def optim_ganlatent(json_dir, res, lr, epochs, tex_init, optim_light=False, device="cuda:0", generator=None,
-                    seed=0):
+                    seed=0, feature_loss=None):
     """MaterialGAN latent fit (src/scripts.py:100-143): targets -> latent (and noise) Adam
     through the generator and the renderer -> maps in ``optimize_dir``, re-renders in
     ``rerender_dir``.
@@ -108,7 +108,9 @@ def optim_ganlatent(json_dir, res, lr, epochs, tex_init, optim_light=False, devi
     files). The reference's "auto" choice between its two downloaded starting latents needs
     those checkpoints, which are not available offline. ``generator`` defaults to the
     seeded StyleGAN2-shaped generator at ``res`` (the trained MaterialGAN weights are not
-    available either). Returns the ``MaterialGANOptim``.
+    available either). ``feature_loss`` (default: on for CUDA devices) adds the reference's
+    two phase-dependent VGG feature losses (``descriptor.reference_descriptors``, seeded
+    weights) at 0.1. Returns the ``MaterialGANOptim``.
     """
     from .materialgan import MaterialGANOptim, StyleGAN2Generator
 
@@ -122,7 +124,14 @@ def optim_ganlatent(json_dir, res, lr, epochs, tex_init, optim_light=False, devi
     targets = io.load_images_th(io.target_dir, res)
     renderer = Microfacet(res, io.n_of_imgs, io.im_size, io.cl, device)
     gen = generator if generator is not None else StyleGAN2Generator(res, seed=seed)
-    opt = MaterialGANOptim(device, renderer, gen)
+    if feature_loss is None:
+        feature_loss = torch.device(device).type == "cuda"
+    desc = None
+    if feature_loss:
+        from .descriptor import reference_descriptors
+
+        desc = reference_descriptors(device, seed=seed)
+    opt = MaterialGANOptim(device, renderer, gen, descriptor=desc)
     opt.load_targets(targets)
     opt.init_from(batch=1, seed=seed, noise="random" if not paths else "zero")
     if paths:

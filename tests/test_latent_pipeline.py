@@ -111,3 +111,33 @@ def test_gen_textures_from_materialgan(svb, tmp_path):
         assert (tmp_path / "ref" / name).exists()
     back = svb.SvbrdfIO(j, "cpu").load_textures_th(tmp_path / "ref", 16)
     assert float((back[:, 0:3] - t[:, 0:3]).abs().max()) <= 2.0 / 255 + 1e-6  # 8-bit PNG round trip
+
+
+class FakeDescriptor:
+    """loss_and_grad of a feature loss (0.5 |r - t|^2 mean), recording when it is used."""
+
+    def __init__(self, name, log):
+        self.name, self.log = name, log
+
+    def load(self, targets):
+        self.t = targets.detach().clone()
+
+    def loss_and_grad(self, renders):
+        self.log.append(self.name)
+        d = renders - self.t
+        return (0.5 * (d * d).mean()), torch.zeros(()), d / d.numel()
+
+
+def test_latent_loop_picks_the_phase_feature_loss(svb):
+    """A (latent-phase, noise-phase) descriptor pair: latent epochs use the first, noise
+    epochs the second, as the reference's "L" and "N" losses; both load the targets."""
+    sc, tg, gen = _setup(svb)
+    log = []
+    pair = (FakeDescriptor("L", log), FakeDescriptor("N", log))
+    o = svb.materialgan.MaterialGANOptim("cpu", TorchRenderer(16, 9, sc.size, sc.cl), gen, descriptor=pair)
+    o.load_targets(tg)
+    assert torch.equal(pair[0].t, tg) and torch.equal(pair[1].t, tg)
+    o.init_from(batch=1, seed=2)
+    o.optim([7, 2, 1], 0.02)
+    assert log == ["L", "L", "N", "L", "L", "N", "L"]
+    assert len(o.loss_feature_list) == 7

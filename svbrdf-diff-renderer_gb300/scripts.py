@@ -110,7 +110,8 @@ def optim_ganlatent(json_dir, res, lr, epochs, tex_init, optim_light=False, devi
     seeded StyleGAN2-shaped generator at ``res`` (the trained MaterialGAN weights are not
     available either). ``feature_loss`` (default: on for CUDA devices) adds the reference's
     two phase-dependent VGG feature losses (``descriptor.reference_descriptors``, seeded
-    weights) at 0.1. Returns the ``MaterialGANOptim``.
+    weights) at 0.1; their tensor-core convolutions need ``res`` a multiple of 128 (relu4_2
+    at 1/8 resolution fills the 8 x 16 tile). Returns the ``MaterialGANOptim``.
     """
     from .materialgan import MaterialGANOptim, StyleGAN2Generator
 

@@ -348,3 +348,99 @@ def exr_write(path, rgb: np.ndarray, half: bool = True, compression: str = "zip"
         offsets.append(pos)
         pos += len(c)
     pathlib.Path(path).write_bytes(header + struct.pack(f"<{len(offsets)}Q", *offsets) + b"".join(chunks))
+
+
+# ---------------------------------------------------------------- mosaics and GIFs
+def imconcat(im_list, size=(2, 2)):
+    """w x h mosaic of equally sized images, row by row (src/imageio.py:79-89)."""
+    w, h = size
+    rows = [np.concatenate([np.asarray(im_list[i * w + j]) for j in range(w)], 1) for i in range(h)]
+    return np.concatenate(rows, 0)
+
+
+def img9to1(folder, names=None):
+    """all.png: the 3 x 3 mosaic of a folder's nine renders (src/imageio.py:92-98);
+    ``names`` lists the nine files (default 00.png .. 08.png, as the reference reads)."""
+    folder = pathlib.Path(folder)
+    names = names or [f"{i:02d}.png" for i in range(9)]
+    imwrite(imconcat([imread(folder / n) for n in names], (3, 3)), folder / "all.png")
+
+
+def tex4to1(folder):
+    """tex.png: the 2 x 2 mosaic normal | diffuse / specular | roughness (src/imageio.py:101-111)."""
+    folder = pathlib.Path(folder)
+    normal, diffuse = imread(folder / "nom.png"), imread(folder / "dif.png")
+    specular, roughness = imread(folder / "spe.png"), imread(folder / "rgh.png")
+    if roughness.ndim == 2:
+        roughness = np.dstack((roughness, roughness, roughness))
+    imwrite(imconcat([normal, diffuse, specular, roughness]), folder / "tex.png")
+
+
+def _gif_palette() -> np.ndarray:
+    """3-3-2 palette: index = r3 << 5 | g3 << 2 | b2, each level spread over 0..255."""
+    i = np.arange(256)
+    r, g, b = (i >> 5) & 7, (i >> 2) & 7, i & 3
+    return np.stack([r * 255 // 7, g * 255 // 7, b * 255 // 3], 1).astype(np.uint8)
+
+
+def _gif_indices(rgb: np.ndarray) -> np.ndarray:
+    q = rgb.astype(np.uint16)
+    r = (q[..., 0] * 7 + 127) // 255
+    g = (q[..., 1] * 7 + 127) // 255
+    b = (q[..., 2] * 3 + 127) // 255
+    return ((r << 5) | (g << 2) | b).astype(np.uint8)
+
+
+def _gif_lzw(indices: np.ndarray) -> bytes:
+    """The image data of one frame: minimum code size 8, then 9-bit codes (clear, up to 250
+    literals, clear, ...), end code, in sub-blocks of at most 255 bytes. Literal codes and a
+    clear before the code table would outgrow 9 bits make a valid, uncompressed LZW stream."""
+    px = indices.reshape(-1).astype(np.uint16)
+    run = 250
+    n = px.size
+    groups = (n + run - 1) // run
+    codes = np.full(groups * (run + 1), 0xFFFF, np.uint16)
+    codes[0::run + 1] = 256  # a clear code before each run
+    body = codes.reshape(groups, run + 1)
+    padded = np.full(groups * run, 0xFFFF, np.uint16)
+    padded[:n] = px
+    body[:, 1:] = padded.reshape(groups, run)
+    codes = np.concatenate([codes[codes != 0xFFFF], np.array([257], np.uint16)])
+    bits = ((codes[:, None] >> np.arange(9)) & 1).astype(np.uint8).reshape(-1)
+    data = np.packbits(bits, bitorder="little").tobytes()
+    out = bytearray([8])
+    for k in range(0, len(data), 255):
+        chunk = data[k:k + 255]
+        out += bytes([len(chunk)]) + chunk
+    out += b"\0"
+    return bytes(out)
+
+
+def gif_write(frames, path, delay_ms: int = 40, loop: int = 0) -> None:
+    """Animated GIF89a of RGB frames (uint8, or floats in [0, 1]) with a 3-3-2 palette."""
+    frames = [np.asarray(f) for f in frames]
+    if not frames:
+        raise ValueError("no frames")
+    h, w = frames[0].shape[:2]
+    out = bytearray(b"GIF89a")
+    out += struct.pack("<HHBBB", w, h, 0xF7, 0, 0) + _gif_palette().tobytes()
+    out += b"\x21\xff\x0bNETSCAPE2.0\x03\x01" + struct.pack("<H", loop) + b"\0"
+    for f in frames:
+        if f.dtype == np.uint16:
+            f = (f >> 8).astype(np.uint8)
+        elif f.dtype != np.uint8:
+            f = (np.clip(f, 0, 1) * 255 + 0.5).astype(np.uint8)
+        if f.ndim == 2:
+            f = np.dstack((f, f, f))
+        if f.shape[:2] != (h, w):
+            raise ValueError("all frames must have the same size")
+        out += b"\x21\xf9\x04\x00" + struct.pack("<H", max(delay_ms // 10, 1)) + b"\x00\x00"
+        out += b"\x2c" + struct.pack("<HHHHB", 0, 0, w, h, 0) + _gif_lzw(_gif_indices(f[..., :3]))
+    out += b"\x3b"
+    pathlib.Path(path).write_bytes(bytes(out))
+
+
+def img2gif(in_filenames, out_filename, method="Pillow"):
+    """GIF of PNG frames, 40 ms each, looping (src/imageio.py:114-123). ``method`` is
+    accepted for the reference's signature; the encoder is this module's own either way."""
+    gif_write([png_read(f) for f in in_filenames], out_filename, delay_ms=40)

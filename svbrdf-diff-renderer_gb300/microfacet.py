@@ -96,6 +96,53 @@ class Microfacet:
     def light_pos(self):
         return self._lit
 
+    # ---- the reference's tensor helpers (src/microfacet.py:16-20, 54-79) in torch, on the
+    # renderer's device. The kernels compute the same quantities in registers; these are for
+    # callers of the reference's methods.
+    @property
+    def pos(self):
+        """Pixel-centre grid [n, 3, res, res]: (x, -y, 0), x = ((k + 0.5) / res - 0.5) size."""
+        if getattr(self, "_pos", None) is None:
+            k = (torch.arange(self.res, dtype=torch.float32, device=self.device) + 0.5) / self.res - 0.5
+            k = k * self.size
+            x = k.view(1, -1).expand(self.res, -1)
+            y = k.view(-1, 1).expand(-1, self.res)
+            self._pos = torch.stack((x, -y, torch.zeros_like(x)), 0).unsqueeze(0).expand(self.n_of_imgs, -1, -1, -1)
+        return self._pos
+
+    def dot(self, a, b):
+        """Channel dot product, expanded to 3 channels (src/microfacet.py:54-55)."""
+        return (a * b).sum(1, keepdim=True).expand(-1, 3, -1, -1)
+
+    def normalize(self, vec):
+        """vec / |vec| over channels (src/microfacet.py:57-58)."""
+        return vec / vec.norm(2.0, 1, keepdim=True)
+
+    def get_dir(self, pos):
+        """(unit direction, squared distance) from every pixel to ``pos`` ([n, 3] or
+        [n, 3, res, res]) (src/microfacet.py:60-62)."""
+        if pos.dim() == 2:
+            pos = pos[:, :, None, None]
+        vec = pos - self.pos
+        return self.normalize(vec), self.dot(vec, vec)
+
+    def reconstruct_normal(self, texture):
+        """Unit normals [B, 3, H, W] from the stored xy [B, 2, H, W] (src/microfacet.py:64-70)."""
+        nx = texture[:, 0].clamp(-1, 1)
+        ny = texture[:, 1].clamp(-1, 1)
+        nz = (1 - (nx ** 2 + ny ** 2).clamp(0, 1 - self.eps)).sqrt()
+        return self.normalize(torch.stack((nx, ny, nz), 1))
+
+    def tex2map(self, textures):
+        """(normal, diffuse, specular, roughness), each [n, 3, res, res], from [1, 9, res, res]
+        (src/microfacet.py:72-79): the sRGB-like maps decoded with ^2.2."""
+        n = self.n_of_imgs
+        diffuse = (((textures[:, 0:3] + 1) / 2) ** 2.2).expand(n, -1, -1, -1)
+        normal = self.reconstruct_normal(textures[:, 3:5]).expand(n, -1, -1, -1)
+        roughness = (((textures[:, 5] + 1) / 2) ** 2.2).expand(n, 3, -1, -1)
+        specular = (((textures[:, 6:9] + 1) / 2) ** 2.2).expand(n, -1, -1, -1)
+        return normal, diffuse, specular, roughness
+
     def update_light(self, light_pow):
         """src/microfacet.py:81-82: use ``light_pow [3]`` (possibly a learnable tensor)."""
         self.light_pow = light_pow

@@ -48,18 +48,21 @@ def render_envmap(data_dir, res, envmap=None, device="cuda:0", spp=256, seed=0):
     """The novel-view video of the maps in ``data_dir`` (src/scripts.py:44-59): the material
     (nom/dif/spe/rgh.png at their own size) under ``envmap`` (an OpenEXR path or a [He, We, 3]
     array; None: the seeded synthetic environment), written as ``data_dir/vid/000.png`` ...
-    ``115.png``: 59 angles forward, then 57 back, light intensity 0.5. The reference also
-    packs them into a GIF with Pillow, which is not available here. Returns the frames."""
+    ``115.png`` (59 angles forward, then 57 back, light intensity 0.5) and packed into
+    ``data_dir/vid.gif`` (40 ms a frame, looping). Returns the frames."""
     from .envmap import EnvmapRenderer
-    from .imageio import imwrite
+    from .imageio import img2gif, imwrite
 
     data_dir = pathlib.Path(data_dir)
     vid = data_dir / "vid"
     vid.mkdir(parents=True, exist_ok=True)
     textures = load_texture_maps(data_dir, None, device)
     frames = EnvmapRenderer([res, res], envmap, textures, device=device, spp=spp, seed=seed).render_video(59, 0.5)
+    names = []
     for i, f in enumerate(frames):
-        imwrite(f, vid / f"{i:03d}.png", flag="srgb")
+        names.append(vid / f"{i:03d}.png")
+        imwrite(f, names[-1], flag="srgb")
+    img2gif(names, data_dir / "vid.gif")
     return frames
 
 

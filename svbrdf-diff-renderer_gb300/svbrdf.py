@@ -102,6 +102,12 @@ class SvbrdfOptim:
     def load(self, path):
         self.load_state_dict(torch.load(path, map_location=self.device))
 
+    def gradient(self, parameters):
+        """The reference's helper (src/optimization.py:17-23): leaves that require grad."""
+        if isinstance(parameters, list):
+            return [p.detach().requires_grad_(True) for p in parameters]
+        return parameters.detach().requires_grad_(True)
+
     def compute_image_loss(self, predicts):
         """src/optimization.py:28-29 (MSE), or the log(1+x) L2 loss."""
         if self.loss == "mse":
@@ -292,6 +298,16 @@ class SvbrdfIO:
             self.light_pow = data["light_pow"]
             self.load_calibration_th()
 
+    def np_to_th(self, arr):
+        return torch.from_numpy(arr).to(self.device)
+
+    def th_to_np(self, arr):
+        return arr.detach().cpu().numpy()
+
+    def reconstruct_normal(self, texture):
+        """Unit normals from the stored xy (src/svbrdf.py:126-132)."""
+        return self._normal3(texture)
+
     def load_calibration_th(self):
         import numpy as np
 
@@ -314,8 +330,8 @@ class SvbrdfIO:
         return n / n.norm(2.0, 1, keepdim=True)
 
     def save_textures_th(self, textures_th, textures_dir):
-        """nom/dif/spe/rgh.png from [1, 9, H, W] (src/svbrdf.py:168-189, without the mosaic)."""
-        from .imageio import imwrite
+        """nom/dif/spe/rgh.png from [1, 9, H, W], and their tex.png mosaic (src/svbrdf.py:168-189)."""
+        from .imageio import imwrite, tex4to1
 
         d = pathlib.Path(textures_dir)
         d.mkdir(parents=True, exist_ok=True)
@@ -325,6 +341,7 @@ class SvbrdfIO:
         imwrite(np_((t[:, 0:3] + 1) / 2), d / "dif.png", "srgb")
         imwrite(np_((t[:, 6:9] + 1) / 2), d / "spe.png", "srgb")
         imwrite(((t[0, 5] + 1) / 2).cpu().numpy(), d / "rgh.png", "rough")
+        tex4to1(d)
 
     def load_images_th(self, images_dir, res=256):
         """[n, 3, res, res] from {idx:02d}.png (src/svbrdf.py:191-204)."""
@@ -337,8 +354,8 @@ class SvbrdfIO:
         return out
 
     def save_images_th(self, images_th, images_dir):
-        """{idx:02d}.png per view (src/svbrdf.py:206-221, without the 3x3 mosaic)."""
-        from .imageio import imwrite
+        """{idx:02d}.png per view, and with nine views their all.png mosaic (src/svbrdf.py:206-221)."""
+        from .imageio import img9to1, imwrite
 
         d = pathlib.Path(images_dir)
         d.mkdir(parents=True, exist_ok=True)
@@ -346,3 +363,5 @@ class SvbrdfIO:
             raise ValueError(f"expected {self.n_of_imgs} images, got {images_th.shape[0]}")
         for i, idx in enumerate(self.idx):
             imwrite(images_th[i].detach().permute(1, 2, 0).cpu().numpy(), d / f"{idx:02d}.png", "srgb")
+        if self.n_of_imgs == 9:
+            img9to1(d, [f"{idx:02d}.png" for idx in self.idx])

@@ -216,3 +216,114 @@ def test_render_envmap_writes_the_video_frames(svb, tmp_path, monkeypatch):
     files = sorted((tmp_path / "vid").glob("*.png"))
     assert [f.name for f in files[:2]] == ["000.png", "001.png"] and len(files) == 116
     assert np.allclose(svb.imageio.imread(files[115], "srgb"), 1 / 60.0, atol=1 / 255)
+
+
+def _gif_decode(data):
+    """A plain GIF89a reader for the tests: global palette, per-frame LZW (any code widths)."""
+    import struct
+    assert data[:6] == b"GIF89a"
+    w, h, packed = struct.unpack_from("<HHB", data, 6)
+    p = 13
+    pal = None
+    if packed & 0x80:
+        n = 2 << (packed & 7)
+        pal = np.frombuffer(data[p:p + 3 * n], np.uint8).reshape(n, 3)
+        p += 3 * n
+    frames, delays, loops = [], [], None
+    while data[p] != 0x3B:
+        if data[p] == 0x21:
+            label = data[p + 1]
+            q = p + 2
+            blocks = []
+            while data[q]:
+                blocks.append(data[q + 1:q + 1 + data[q]])
+                q += 1 + data[q]
+            if label == 0xF9:
+                delays.append(struct.unpack_from("<H", blocks[0], 1)[0])
+            if label == 0xFF and blocks[0] == b"NETSCAPE2.0":
+                loops = struct.unpack_from("<H", blocks[1], 1)[0]
+            p = q + 1
+        elif data[p] == 0x2C:
+            fw, fh = struct.unpack_from("<HH", data, p + 5)
+            mcs = data[p + 10]
+            q = p + 11
+            raw = bytearray()
+            while data[q]:
+                raw += data[q + 1:q + 1 + data[q]]
+                q += 1 + data[q]
+            p = q + 1
+            bits = np.unpackbits(np.frombuffer(bytes(raw), np.uint8), bitorder="little")
+            clear, end = 1 << mcs, (1 << mcs) + 1
+            width, pos, out, table, prev = mcs + 1, 0, [], None, None
+            while True:
+                code = int(sum(int(bits[pos + k]) << k for k in range(width)))
+                pos += width
+                if code == clear:
+                    table = [[i] for i in range(clear)] + [[], []]
+                    width, prev = mcs + 1, None
+                    continue
+                if code == end:
+                    break
+                if prev is None:
+                    entry = table[code]
+                else:
+                    entry = table[code] if code < len(table) else table[prev] + table[prev][:1]
+                    table.append(table[prev] + entry[:1])
+                    if len(table) == (1 << width) and width < 12:
+                        width += 1
+                out += entry
+                prev = code
+            frames.append(pal[np.array(out, np.int64)].reshape(fh, fw, 3))
+        else:
+            raise AssertionError(f"unexpected GIF block {data[p]:#x}")
+    return frames, delays, loops
+
+
+def test_gif_write_and_img2gif(svb, tmp_path):
+    IO = svb.imageio
+    g = np.random.default_rng(3)
+    frames = [(g.random((21, 34, 3)) * 255).astype(np.uint8) for _ in range(3)]
+    IO.gif_write(frames, tmp_path / "a.gif", delay_ms=40)
+    dec, delays, loops = _gif_decode((tmp_path / "a.gif").read_bytes())
+    assert len(dec) == 3 and delays == [4, 4, 4] and loops == 0
+    pal = IO._gif_palette()
+    for f, d in zip(frames, dec):
+        assert np.array_equal(d, pal[IO._gif_indices(f)])  # the 3-3-2 quantisation, losslessly coded
+        assert np.abs(d.astype(int) - f.astype(int)).max() <= 43  # within half a blue level
+    names = []
+    for i, f in enumerate(frames):
+        names.append(tmp_path / f"{i:03d}.png")
+        IO.png_write(names[-1], f)
+    IO.img2gif(names, tmp_path / "b.gif")
+    assert _gif_decode((tmp_path / "b.gif").read_bytes())[0][2].shape == (21, 34, 3)
+
+
+def test_mosaics(svb, tmp_path):
+    IO = svb.imageio
+    ims = [np.full((4, 5, 3), k / 10.0, np.float32) for k in range(9)]
+    for k, im in enumerate(ims):
+        IO.imwrite(im, tmp_path / f"{k:02d}.png")
+    IO.img9to1(tmp_path)
+    allp = IO.imread(tmp_path / "all.png")
+    assert allp.shape == (12, 15, 3) and np.allclose(allp[4, 5], 0.4, atol=1 / 255)  # row 1, column 1
+    m = IO.imconcat([np.zeros((2, 3)), np.ones((2, 3)), np.ones((2, 3)) * 2, np.ones((2, 3)) * 3])
+    assert m.shape == (4, 6) and m[3, 5] == 3 and m[0, 4] == 1
+
+
+def test_savers_write_the_reference_mosaics(svb, tmp_path):
+    """save_textures_th adds tex.png and save_images_th (nine views) all.png, as the reference does."""
+    cfg = {"reference_dir": "ref", "target_dir": "target", "optimize_dir": "optim", "rerender_dir": "rerender",
+           "im_size": 17.0, "idx": list(range(9)), "camera_pos": [[0, 0, 30]] * 9, "light_pos": [[0, 0, 30]] * 9,
+           "light_pow": [1500, 1500, 1500]}
+    j = tmp_path / "scene.json"
+    j.write_text(json.dumps(cfg))
+    io = svb.SvbrdfIO(j, "cpu")
+    io.save_textures_th(svb.scenes.make_material(32, 5), io.reference_dir)
+    assert (tmp_path / "ref" / "tex.png").exists()
+    assert IO_shape(svb, tmp_path / "ref" / "tex.png") == (64, 64, 3)
+    io.save_images_th(torch.rand(9, 3, 6, 6), io.target_dir)
+    assert IO_shape(svb, tmp_path / "target" / "all.png") == (18, 18, 3)
+
+
+def IO_shape(svb, p):
+    return svb.imageio.imread(p).shape

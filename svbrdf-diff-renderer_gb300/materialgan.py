@@ -560,6 +560,29 @@ class MaterialGANOptim:
                            for n in torch.load(noise_path, map_location="cpu")]
         self._graphs = {}  # captured epochs hold the previous parameters' addresses
 
+    # ---- the reference's helpers (src/optimization.py:17-29, src/materialgan.py:82-89) ----
+    def gradient(self, parameters):
+        """Leaves that require grad, as the reference's ``Optim.gradient``."""
+        if isinstance(parameters, list):
+            return [p.detach().requires_grad_(True) for p in parameters]
+        return parameters.detach().requires_grad_(True)
+
+    def compute_image_loss(self, predicts):
+        """MSE against the loaded targets (src/optimization.py:28-29)."""
+        return torch.nn.functional.mse_loss(predicts, self.targets)
+
+    def compute_feature_loss(self, predicts, flag):
+        """The feature loss of the latent ("L") or noise ("N") phase (src/materialgan.py:82-89),
+        0 without a descriptor."""
+        if flag not in ("L", "N"):
+            raise ValueError(f"flag must be 'L' or 'N', not {flag!r}")
+        desc = self._descriptor_for(flag == "L")
+        if desc is None:
+            return torch.zeros((), device=predicts.device)
+        from .descriptor import descriptor_term
+
+        return descriptor_term(predicts, desc)
+
     def _descriptors(self):
         d = self.descriptor
         if d is None:

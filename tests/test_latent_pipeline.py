@@ -141,3 +141,21 @@ def test_latent_loop_picks_the_phase_feature_loss(svb):
     o.optim([7, 2, 1], 0.02)
     assert log == ["L", "L", "N", "L", "L", "N", "L"]
     assert len(o.loss_feature_list) == 7
+
+
+def test_reference_helpers_of_the_latent_optimiser(svb):
+    sc, tg, gen = _setup(svb)
+    log = []
+    pair = (FakeDescriptor("L", log), FakeDescriptor("N", log))
+    o = svb.materialgan.MaterialGANOptim("cpu", TorchRenderer(16, 9, sc.size, sc.cl), gen, descriptor=pair)
+    o.load_targets(tg)
+    r = tg + 0.1
+    assert torch.allclose(o.compute_image_loss(r), torch.tensor(0.01), atol=1e-6)
+    assert float(o.compute_feature_loss(r, "N")) > 0 and log == ["N"]
+    with pytest.raises(ValueError):
+        o.compute_feature_loss(r, "X")
+    leaves = o.gradient([torch.zeros(2), torch.ones(3)])
+    assert all(t.requires_grad and t.is_leaf for t in leaves)
+    bare = svb.materialgan.MaterialGANOptim("cpu", None, gen)
+    bare.load_targets(tg)
+    assert float(bare.compute_feature_loss(r, "L")) == 0.0

@@ -22,7 +22,6 @@ from datetime import datetime
 import torch
 
 from . import _native as N
-from .microfacet import Microfacet
 
 LOSS_KINDS = {"mse": 0, "log1p": 1, "log1p_pre": 2}
 

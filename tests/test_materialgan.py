@@ -136,8 +136,6 @@ def test_upsample_polyphase_matches_fir(svb):
 def test_unfused_modulated_conv_matches_per_sample_weights(svb):
     """Input scaling + shared-weight conv + output demodulation equals the convolution with
     per-sample modulated, demodulated weights."""
-    import math
-
     MG = svb.materialgan
     g = torch.Generator().manual_seed(4)
     conv = MG._ModConv(8, 6, 3, 16, g).double()

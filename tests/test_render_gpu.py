@@ -7,8 +7,6 @@ Tolerances (written here, measured on the reference itself):
   pixels (1 - cos^2 cancellation), hence max-abs 1e-3 per element;
 * gradients: relative L2 <= max(1e-4, 2 x the reference's own FP32-vs-FP64 error).
 """
-import math
-
 import pytest
 import torch
 

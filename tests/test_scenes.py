@@ -1,7 +1,5 @@
 """The seeded synthetic workload that stands in for captured datasets: the value ranges,
 view layouts and seeding its docstrings state."""
-import math
-
 import torch
 
 

@@ -70,7 +70,7 @@ def parse():
     ap.add_argument("--no-extras", action="store_true", help="skip the plain/single/cpu comparison legs")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU baseline budget")
     ap.add_argument("--config", default=None, help="threads,tile_texels[,ctas[,variant]] instead of autotuning")
-    ap.add_argument("--only", default=None, choices=["descriptor", "latent", "envmap"],
+    ap.add_argument("--only", default=None, choices=["descriptor", "latent", "envmap", "single"],
                     help="run one comparison leg alone")
     return ap.parse_args()
 
@@ -646,6 +646,16 @@ def main():
     if args.only == "envmap":
         dev = torch.device("cuda", dist_env()[2])
         print(json.dumps({"envmap": time_envmap(dev)}), flush=True)
+        return 0
+    if args.only == "single":
+        # the drop-in single-material forms on the 1024^2, 9-view scene: plain (forward and
+        # adjoint kernels behind autograd, torch loss and Adam) and fused
+        dev = torch.device("cuda", dist_env()[2])
+        torch.cuda.nvtx.range_push("single")
+        out = {"plain": time_single(dev, fused=False, iters=max(args.steps, 1)),
+               "fused_single": time_single(dev, fused=True, iters=max(args.steps, 1) * 10)}
+        torch.cuda.nvtx.range_pop()
+        print(json.dumps(out), flush=True)
         return 0
     if args.impl == "reference":
         return impl_reference(args)

@@ -5,7 +5,7 @@
  * the flash-lit GGX/Cook-Torrance renderer Microfacet.eval (src/microfacet.py:84-120),
  * its autograd backward, and the per-pixel Adam loop SvbrdfOptim.optim
  * (src/svbrdf.py:44-83). The reference is pure Python and has no FFI; these entry
- * points are what its Python classes call through ctypes (see INTEGRATION.md).
+ * points are what its Python classes call through ctypes.
  *
  * Conventions shared by every entry point:
  *  - All tensor pointers are DEVICE pointers to contiguous FP32 data unless marked HOST.

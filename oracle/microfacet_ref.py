@@ -108,12 +108,53 @@ def render(textures, camera_pos, light_pos, light_pow, size, dtype=torch.float32
     assert textures.dim() == 4 and textures.shape[0] == 1 and textures.shape[1] == 9
     assert textures.shape[2] == textures.shape[3]  # src/microfacet.py:85
     res = textures.shape[2]
-    n = camera_pos.shape[0]
+    cam = camera_pos.to(dtype).unsqueeze(2).unsqueeze(3)
+    lit = light_pos.to(dtype).unsqueeze(2).unsqueeze(3)
+    lpow = light_pow.to(dtype).unsqueeze(0).unsqueeze(2).unsqueeze(3)
+    return _render_at(textures, pixel_positions(res, size, dtype), cam, lit, lpow, dtype)
+
+
+def texel_positions(idx, height, width, size):
+    """FP32 pixel centres ``(px[n], py[n])`` of flat texel indices ``idx`` (row-major, H x W),
+    computed as ``pixel_positions`` builds the grid (src/microfacet.py:16-19)."""
+    idx = torch.as_tensor(idx, dtype=torch.int64)
+    i = (idx // width).to(torch.float32)
+    j = (idx % width).to(torch.float32)
+    px = ((j + 0.5) / width - 0.5) * size
+    py = -(((i + 0.5) / height - 0.5) * size)
+    return px, py
+
+
+def render_texels(t9, px, py, camera_pos, light_pos, light_pow, dtype=torch.float64):
+    """Render ``n`` texels ``t9[9, n]`` at pixel centres ``(px[n], py[n])`` -> ``[V, 3, n]``.
+
+    Rendered pixel (i, j) of src/microfacet.py:84-120 depends only on texel (i, j) and its
+    position, so any set of texels can be rendered on its own: this is ``render`` on a
+    1 x n strip with the strip's positions given instead of the regular grid (same op
+    sequence). ``camera_pos``/``light_pos`` are ``[V, 3]`` (shared) or ``[V, 3, n]`` (per
+    texel, for texels of different materials in one call), ``light_pow`` ``[3]`` or ``[3, n]``."""
+    n = t9.shape[1]
+    pos = torch.stack((px.to(torch.float32), py.to(torch.float32), torch.zeros(n)), 0).view(3, 1, n)
+    cam = camera_pos.to(dtype)
+    lit = light_pos.to(dtype)
+    lpow = light_pow.to(dtype)
+    cam = cam.view(*cam.shape[:2], 1, n) if cam.dim() == 3 else cam.unsqueeze(2).unsqueeze(3)
+    lit = lit.view(*lit.shape[:2], 1, n) if lit.dim() == 3 else lit.unsqueeze(2).unsqueeze(3)
+    lpow = lpow.view(1, 3, 1, n) if lpow.dim() == 2 else lpow.view(1, 3, 1, 1)
+    out = _render_at(t9.reshape(1, 9, 1, n), pos.to(dtype), cam, lit, lpow, dtype)
+    return out.reshape(-1, 3, n)
+
+
+def _render_at(textures, pos3, cam4, lit4, lpow4, dtype):
+    """src/microfacet.py:84-120 for textures ``[1, 9, H, W]`` at positions ``pos3[3, H, W]``;
+    ``cam4``/``lit4`` broadcast to ``[V, 3, H, W]``, ``lpow4`` to ``[1, 3, H, W]``."""
+    hh, ww = textures.shape[2], textures.shape[3]
+    n = cam4.shape[0]
     t = textures.to(dtype)
-    pos = pixel_positions(res, size, dtype).unsqueeze(0).expand(n, -1, -1, -1)
-    cam = camera_pos.to(dtype).unsqueeze(2).unsqueeze(3).expand(-1, -1, res, res)
-    lit = light_pos.to(dtype).unsqueeze(2).unsqueeze(3).expand(-1, -1, res, res)
-    lpow = light_pow.to(dtype).unsqueeze(0).unsqueeze(2).unsqueeze(3).expand(n, -1, res, res)
+    pos = pos3.to(dtype).unsqueeze(0).expand(n, -1, -1, -1)
+    cam = cam4.expand(-1, -1, hh, ww)
+    lit = lit4.expand(-1, -1, hh, ww)
+    lpow = lpow4.expand(n, -1, hh, ww)
 
     # tex2map, src/microfacet.py:72-79
     diffuse = (((t[:, 0:3] + 1) / 2) ** 2.2).expand(n, -1, -1, -1)
@@ -193,6 +234,56 @@ def optim_loop(textures0, targets, camera_pos, light_pos, light_pow, size, epoch
     if optim_light:
         res["light_pow"] = lpow.detach()
     return res
+
+
+def optim_texels(t9, px, py, targets, camera_pos, light_pos, light_pow, n_full, epochs, lr,
+                 loss_kind="mse", dtype=torch.float64, view_mask=None):
+    """``optim_loop`` (src/svbrdf.py:44-71) restricted to ``n`` texels.
+
+    ``t9[9, n]`` are the texels' initial parameters at pixel centres ``(px, py)``,
+    ``targets[V, 3, n]`` their targets, ``n_full`` the element count ``V*3*H*W`` of the whole
+    material, which the reference's mean loss divides by. Each texel's render, gradient and
+    Adam update (elementwise) depend on that texel alone, so its trajectory here is the one
+    it follows in the full-material loop. Texels of several materials can share one call:
+    per-texel views ``[V, 3, n]`` (see ``render_texels``), ``n_full`` per texel ``[n]``, and
+    ``view_mask[V, n]`` (1 for a material's own views, 0 for padding up to the largest V).
+    The summed loss is then the sum of the materials' losses, whose gradient at each texel
+    is its own material's. Returns the final ``textures`` (unclamped), ``exp_avg``,
+    ``exp_avg_sq`` (all ``[9, n]``) and ``sq_err[epochs, n]``: each texel's summed squared
+    error per epoch (before that epoch's update), in the loss's units."""
+    tex = t9.detach().to(dtype).clone().requires_grad_(True)
+    opt = torch.optim.Adam([tex], lr=lr, betas=(0.9, 0.999))
+    tgt = targets.to(dtype)
+    if loss_kind == "log1p":
+        tgt = torch.log1p(tgt)
+    mask = None if view_mask is None else view_mask.to(dtype).unsqueeze(1)
+    per_texel = torch.is_tensor(n_full) and n_full.dim() > 0
+    inv_n = (1.0 / n_full.to(dtype)) if per_texel else None
+    sq = []
+    for _ in range(epochs):
+        out = render_texels(tex.clamp(-1, 1), px, py, camera_pos, light_pos, light_pow, dtype)
+        if loss_kind == "log1p":
+            out = torch.log1p(out)
+        e2 = (out - tgt) ** 2
+        if mask is not None:
+            e2 = e2 * mask
+        sq.append(e2.detach().sum((0, 1)))
+        loss = (e2 * inv_n).sum() if per_texel else e2.sum() / n_full
+        opt.zero_grad()
+        loss.backward()
+        opt.step()
+    st = opt.state[tex]
+    return {"textures": tex.detach(), "exp_avg": st["exp_avg"].detach(), "exp_avg_sq": st["exp_avg_sq"].detach(),
+            "sq_err": torch.stack(sq)}
+
+
+def loss_texels(t9, px, py, targets, camera_pos, light_pos, light_pow, loss_kind="mse", dtype=torch.float64):
+    """Summed squared error (the numerator of ``image_loss``) of ``n`` texels, FP64 sum."""
+    out = render_texels(t9.clamp(-1, 1), px, py, camera_pos, light_pos, light_pow, dtype)
+    tgt = targets.to(dtype)
+    if loss_kind == "log1p":
+        out, tgt = torch.log1p(out), torch.log1p(tgt)
+    return float(((out - tgt) ** 2).sum(dtype=torch.float64))
 
 
 def loss_and_grad(textures, targets, camera_pos, light_pos, light_pow, size, loss_kind="mse",

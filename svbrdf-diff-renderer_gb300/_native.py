@@ -211,6 +211,22 @@ def load(path=None):
         return _lib
 
 
+_build_id = None
+
+
+def build_id() -> str:
+    """ABI version and a hash of the loaded library file: tuning results and other cached
+    choices are keyed on it, so a rebuilt library never reuses a stale pick."""
+    global _build_id
+    if _build_id is None:
+        import hashlib
+
+        L = load()
+        h = hashlib.sha1(lib_path().read_bytes()).hexdigest()[:12]
+        _build_id = f"abi{L.svbrdf_abi_version()}-{h}"
+    return _build_id
+
+
 def lib():
     """The loaded library, for compute calls: raises when no CUDA device is present."""
     import torch

@@ -103,6 +103,11 @@ class BatchedOptim:
         h = hashlib.sha1(json.dumps(sorted(self.meta)).encode()).hexdigest()[:16]
         return f"{torch.cuda.get_device_name(self.device)}|{self.loss}|{h}"
 
+    def tune_key(self) -> str:
+        """The autotuner's cache key: the workload signature plus the library's ABI version and
+        build hash, so a pick made with another build of the kernels is never reused."""
+        return f"{self.signature()}|{N.build_id()}"
+
     # ---- plan ----
     def _mat_array(self, tex=None, m1=None, m2=None):
         tex = tex or self.tex
@@ -353,7 +358,7 @@ def _load_cache():
 
 def autotune(opt: BatchedOptim, candidates=None, use_cache: bool = True) -> BatchConfig:
     """Pick threads/tile_texels/ctas for ``opt``'s workload by timing every candidate."""
-    key = opt.signature()
+    key = opt.tune_key()
     cache = _load_cache() if use_cache else {}
     if key in cache:
         return BatchConfig(**cache[key])

@@ -21,6 +21,8 @@
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 
+#include <atomic>
+
 #include "svbrdf_common.cuh"
 
 namespace svb {
@@ -173,6 +175,7 @@ conv3x3_tc_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_const
   if (warp == 0) {
     if (lane == 0) {
       // ---------------------------------------------------------------- TMA producer
+      int issued = 0;
       for (int i = 0; i < total; ++i) {
         const int s = i % STAGES;
         const uint32_t ph = (uint32_t)(i / STAGES) & 1u;
@@ -184,20 +187,28 @@ conv3x3_tc_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_const
         mbar_expect_tx(fb, (uint32_t)S::kStage);
         tma_4d(st, &tmap_x, cc * BK, x0 + dx, y0 + dy, img, fb);
         tma_2d(st + S::kABytes, &tmap_w, tap * Cin + cc * BK, n0, fb);
+        ++issued;
+      }
+      if (issued < total) {
+        // aborted: no load may still be writing shared memory when the CTA exits, so wait
+        // (bounded) for the loads of the last min(issued, STAGES) stages to land
+        for (int i = issued > STAGES ? issued - STAGES : 0; i < issued; ++i) {
+          const uint32_t bar = smem_u32(&full_bar[i % STAGES]);
+          const uint32_t ph = (uint32_t)(i / STAGES) & 1u;
+          uint32_t it = 0;
+          while (!mbar_try(bar, ph) && ++it < kSpin) {
+          }
+        }
       }
     }
   } else if (warp == 1) {
     if (lane == 0) {
       // ---------------------------------------------------------------- MMA issuer
       constexpr uint32_t idesc = idesc_bf16(BM, BN);
-      bool ok = true;
       for (int i = 0; i < total; ++i) {
         const int s = i % STAGES;
         const uint32_t ph = (uint32_t)(i / STAGES) & 1u;
-        if (!mbar_wait(smem_u32(&full_bar[s]), ph, err, kErrMma)) {
-          ok = false;
-          break;
-        }
+        if (!mbar_wait(smem_u32(&full_bar[s]), ph, err, kErrMma)) break;
         fence_after();
         const uint32_t a = base + (uint32_t)(s * S::kStage);
         const uint32_t b = a + S::kABytes;
@@ -206,14 +217,18 @@ conv3x3_tc_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_const
           mma_bf16(tmem, sw128_desc(a + 32u * k), sw128_desc(b + 32u * k), idesc, (i > 0 || k > 0) ? 1u : 0u);
         mma_commit(smem_u32(&empty_bar[s]));
       }
-      if (ok) mma_commit(smem_u32(&acc_bar));
+      // Committed on the abort path too: acc_bar then completes once every MMA issued so far
+      // has finished, so TMEM is not written after the CTA releases it. The epilogue skips
+      // its stores when the error word is set.
+      mma_commit(smem_u32(&acc_bar));
     }
   } else {
     // ---------------------------------------------------------------- epilogue (warps 2..5)
     const int q = warp & 3;  // TMEM lane quadrant this warp may read
     const int m = q * 32 + lane;
     const int py = y0 + m / TW, px = x0 + m % TW;
-    const bool ok = __all_sync(0xffffffffu, mbar_wait(smem_u32(&acc_bar), 0u, err, kErrEpi));
+    const bool ok = __all_sync(0xffffffffu, mbar_wait(smem_u32(&acc_bar), 0u, err, kErrEpi)) &&
+                    *(volatile int*)err == 0;
     fence_after();
     if (ok) {
       const size_t pix = ((size_t)img * H + py) * W + px;
@@ -276,6 +291,11 @@ conv3x3_tc_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_const
   fence_before();
   __syncthreads();
   if (warp == 1) {
+    // The MMAs must be complete before TMEM is released. acc_bar has completed already
+    // unless the epilogue's wait gave up; then wait again, bounded, for the issuer's commit.
+    uint32_t it = 0;
+    while (!mbar_try(smem_u32(&acc_bar), 0u) && ++it < kSpin) {
+    }
     fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)BN) : "memory");
   }
@@ -300,11 +320,15 @@ static int launch(const CUtensorMap& mx, const CUtensorMap& mw, const float* bia
                   const void* addend, void* y, int n, int h, int w, int cin, int cout, int* err, cudaStream_t st) {
   auto kern = conv3x3_tc_kernel<BN, STAGES, EPI>;
   const size_t smem = (size_t)STAGES * Shape<BN>::kStage + 1024;
-  static bool attr = false;
-  if (!attr) {
+  // cudaFuncSetAttribute applies to the current device only: remember it per device ordinal
+  static std::atomic<bool> attr[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
+    return fail(SVBRDF_ERR_CUDA, "conv3x3: no usable current device");
+  if (!attr[dev].load()) {
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
       return fail(SVBRDF_ERR_CUDA, "cudaFuncSetAttribute: %s", cudaGetErrorString(cudaGetLastError()));
-    attr = true;
+    attr[dev].store(true);
   }
   dim3 grid((unsigned)(n * (h / TH) * (w / TW)), (unsigned)(cout / BN));
   kern<<<grid, kThreads, smem, st>>>(mx, mw, bias, (const __nv_bfloat16*)mask, (const __nv_bfloat16*)addend,

@@ -108,8 +108,8 @@ __device__ __forceinline__ float texel_fused_grad(const float raw[9], float px, 
 // One texel of one fused iteration with direct global loads. Returns the squared error.
 template <int LOSS, bool GRAD_POW, bool ALL_COLOC>
 __device__ __forceinline__ float fused_texel(float* __restrict__ tex, float* __restrict__ mom1,
-                                             float* __restrict__ mom2, const float* __restrict__ tgt, int T,
-                                             int idx, float px, float py, int V, const View* s_views,
+                                             float* __restrict__ mom2, const float* __restrict__ tgt, long long T,
+                                             long long idx, float px, float py, int V, const View* s_views,
                                              const float* s_pow, float scale, const AdamScalars& adam,
                                              float gp[3]) {
   float raw[9];
@@ -156,22 +156,24 @@ fused_step_kernel(float* __restrict__ tex, float* __restrict__ mom1, float* __re
   if (threadIdx.x < 3) s_pow[threadIdx.x] = lpow[threadIdx.x];
   __syncthreads();
 
-  const int T = H * W;
+  // 64-bit texel index: the grid-stride step cannot wrap for any H*W the host accepts
+  const long long T = (long long)H * W;
+  const long long stride = (long long)gridDim.x * blockDim.x;
   float loss = 0.f;
   float gp[3] = {0.f, 0.f, 0.f};
   bool allc = true;
   for (int v = 0; v < V; ++v) allc = allc && (s_views[v].coloc != 0.f);
   if (allc) {
-    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < T; idx += gridDim.x * blockDim.x) {
+    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < T; idx += stride) {
       float px, py;
-      texel_pos(idx / W, idx % W, W, H, size, px, py);
+      texel_pos((int)(idx / W), (int)(idx % W), W, H, size, px, py);
       loss += fused_texel<LOSS, GRAD_POW, true>(tex, mom1, mom2, tgt, T, idx, px, py, V, s_views, s_pow, scale,
                                                 adam, gp);
     }
   } else {
-    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < T; idx += gridDim.x * blockDim.x) {
+    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < T; idx += stride) {
       float px, py;
-      texel_pos(idx / W, idx % W, W, H, size, px, py);
+      texel_pos((int)(idx / W), (int)(idx % W), W, H, size, px, py);
       loss += fused_texel<LOSS, GRAD_POW, false>(tex, mom1, mom2, tgt, T, idx, px, py, V, s_views, s_pow, scale,
                                                  adam, gp);
     }
@@ -1901,23 +1903,33 @@ static size_t pair_smem(int ring) {
   return (size_t)ring * (kPairSlotPlanes * 2 * NCW * 32 * 4 + sizeof(PairSlotRec));
 }
 
-// Once per kernel instantiation: allow the ring's dynamic shared memory.
+// Dynamic shared memory already allowed for one kernel instantiation, per device ordinal:
+// cudaFuncSetAttribute applies to the current device only.
+struct SmemAllowance {
+  std::mutex mu;
+  size_t have[64] = {};
+};
+
+// Once per kernel instantiation and device: allow the ring's dynamic shared memory.
 template <typename Kernel>
-static int allow_smem(Kernel kernel, size_t need, int& done, size_t& have) {
-  if (!done || need > have) {
+static int allow_smem(Kernel kernel, size_t need, SmemAllowance& a) {
+  int dev = 0;
+  const cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return fail(SVBRDF_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
+  if (dev < 0 || dev >= 64) return fail(SVBRDF_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
+  std::lock_guard<std::mutex> lock(a.mu);
+  if (need > a.have[dev]) {
     if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need) != cudaSuccess)
       return fail(SVBRDF_ERR_CUDA, "cudaFuncSetAttribute: %s", cudaGetErrorString(cudaGetLastError()));
-    done = 1;
-    have = need;
+    a.have[dev] = need;
   }
   return SVBRDF_OK;
 }
 
 template <int LOSS, int NCW>
 static int tma_prepare(int ring) {
-  static int done = 0;
-  static size_t have = 0;
-  return allow_smem(batched_tma_kernel<LOSS, NCW>, tma_smem<NCW>(ring), done, have);
+  static SmemAllowance a;
+  return allow_smem(batched_tma_kernel<LOSS, NCW>, tma_smem<NCW>(ring), a);
 }
 
 template <int NCW>
@@ -1927,23 +1939,20 @@ static size_t fuse_smem(int ring) {
 
 template <int LOSS, int NCW, bool GEN>
 static int fuse2_prepare(int ring) {
-  static int done = 0;
-  static size_t have = 0;
-  return allow_smem(batched_fuse2_kernel<LOSS, NCW, GEN>, fuse_smem<NCW>(ring), done, have);
+  static SmemAllowance a;
+  return allow_smem(batched_fuse2_kernel<LOSS, NCW, GEN>, fuse_smem<NCW>(ring), a);
 }
 
 template <int LOSS, int NCW, bool GEN>
 static int fuse_prepare(int ring) {
-  static int done = 0;
-  static size_t have = 0;
-  return allow_smem(batched_fuse_kernel<LOSS, NCW, GEN>, fuse_smem<NCW>(ring), done, have);
+  static SmemAllowance a;
+  return allow_smem(batched_fuse_kernel<LOSS, NCW, GEN>, fuse_smem<NCW>(ring), a);
 }
 
 template <int LOSS, int NCW, bool GEN>
 static int pair_prepare(int ring) {
-  static int done = 0;
-  static size_t have = 0;
-  return allow_smem(batched_pair_kernel<LOSS, NCW, GEN>, pair_smem<NCW>(ring), done, have);
+  static SmemAllowance a;
+  return allow_smem(batched_pair_kernel<LOSS, NCW, GEN>, pair_smem<NCW>(ring), a);
 }
 
 int resident_ctas(int variant, int threads) {
@@ -2060,32 +2069,46 @@ int svbrdf_fused_step_noalloc(float* textures, float* exp_avg, float* exp_avg_sq
   if (loss_kind < SVBRDF_LOSS_MSE || loss_kind > SVBRDF_LOSS_LOG1P_PRE)
     return fail(SVBRDF_ERR_INVALID, "bad loss_kind %d", loss_kind);
   if (step < 1) return fail(SVBRDF_ERR_INVALID, "step must be >= 1");
+  const long long T = (long long)height * width;
+  const bool gp = light_adam_state != nullptr;
+  // The grid is fixed (and checked against the scratch) before anything is enqueued, so a
+  // rejected call leaves no work on the stream and no node in a capture.
+  int grid = 0;
+#define SVB_GRID_NA(L, G)                                                    \
+  {                                                                          \
+    static int occ = occupancy_of(fused_step_kernel<L, G>, kFusedThreads);   \
+    grid = grid_for(T, kFusedThreads, occ);                                  \
+  }
+  if (gp) {
+    if (loss_kind == SVBRDF_LOSS_MSE) SVB_GRID_NA(0, true)
+    else if (loss_kind == SVBRDF_LOSS_LOG1P) SVB_GRID_NA(1, true)
+    else SVB_GRID_NA(2, true)
+  } else {
+    if (loss_kind == SVBRDF_LOSS_MSE) SVB_GRID_NA(0, false)
+    else if (loss_kind == SVBRDF_LOSS_LOG1P) SVB_GRID_NA(1, false)
+    else SVB_GRID_NA(2, false)
+  }
+#undef SVB_GRID_NA
+  if (grid > kNoAllocMaxBlocks)
+    return fail(SVBRDF_ERR_UNSUPPORTED, "no-allocation step needs %d CTAs of scratch; the static array holds %d", grid,
+                kNoAllocMaxBlocks);
   void* scratch = nullptr;
   rc = noalloc_scratch(&scratch);
   if (rc) return rc;
-  const long long T = (long long)height * width;
   const double N = 3.0 * n_views * (double)T;
   const float scale = (float)(2.0 / N);
   const AdamScalars adam = make_adam(step, lr, beta1, beta2, eps);
   unsigned* counter = (unsigned*)scratch;
   float4* partials = (float4*)((char*)scratch + 16);
   cudaStream_t st = (cudaStream_t)stream;
-  const bool gp = light_adam_state != nullptr;
   // the counter must start at zero; the array keeps whatever the previous call left
   cudaError_t e = cudaMemsetAsync(counter, 0, 16, st);
   if (e != cudaSuccess) return fail(SVBRDF_ERR_CUDA, "cudaMemsetAsync(scratch counter): %s", cudaGetErrorString(e));
-#define SVB_FUSED_NA(L, G)                                                                                       \
-  {                                                                                                              \
-    static int occ = occupancy_of(fused_step_kernel<L, G>, kFusedThreads);                                       \
-    const int grid = grid_for(T, kFusedThreads, occ);                                                            \
-    if (grid > kNoAllocMaxBlocks)                                                                                \
-      return fail(SVBRDF_ERR_UNSUPPORTED, "no-allocation step needs %d CTAs of scratch; the static array holds %d", \
-                  grid, kNoAllocMaxBlocks);                                                                      \
-    fused_step_kernel<L, G><<<grid, kFusedThreads, 0, st>>>(textures, exp_avg, exp_avg_sq, targets, camera_pos,   \
-                                                            light_pos, light_pow, light_adam_state, n_views,      \
-                                                            height, width, size, scale, 1.0 / N, adam,            \
-                                                            loss_out, partials, counter);                         \
-  }
+#define SVB_FUSED_NA(L, G)                                                                                     \
+  fused_step_kernel<L, G><<<grid, kFusedThreads, 0, st>>>(textures, exp_avg, exp_avg_sq, targets, camera_pos, \
+                                                          light_pos, light_pow, light_adam_state, n_views,    \
+                                                          height, width, size, scale, 1.0 / N, adam,          \
+                                                          loss_out, partials, counter);
   if (gp) {
     if (loss_kind == SVBRDF_LOSS_MSE) SVB_FUSED_NA(0, true)
     else if (loss_kind == SVBRDF_LOSS_LOG1P) SVB_FUSED_NA(1, true)

@@ -170,7 +170,8 @@ int check_common(const float* tex, const float* cam, const float* lit, const flo
   if (V <= 0 || H <= 0 || W <= 0) return fail(SVBRDF_ERR_INVALID, "bad shape V=%d H=%d W=%d", V, H, W);
   if (V > kMaxViews) return fail(SVBRDF_ERR_UNSUPPORTED, "n_views=%d exceeds the maximum %d", V, kMaxViews);
   if (!(size > 0.0f)) return fail(SVBRDF_ERR_INVALID, "size must be > 0");
-  if ((long long)H * W > (1LL << 31)) return fail(SVBRDF_ERR_UNSUPPORTED, "H*W too large");
+  // every kernel indexes texels in 64 bits; row and column indices stay 32-bit
+  if ((long long)H * W >= (1LL << 31)) return fail(SVBRDF_ERR_UNSUPPORTED, "H*W = %lld is not below 2^31", (long long)H * W);
   return SVBRDF_OK;
 }
 

@@ -197,7 +197,7 @@ def save(name, d):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", required=True, help="root of a checkout of the reference repository")
     a = ap.parse_args()
     torch.manual_seed(0)
     micro, svb = load_reference(pathlib.Path(a.ref))

@@ -1,0 +1,179 @@
+"""Parity of the benchmark's batched kernels on the benchmark's own workload.
+
+bench.py times 64 seeded materials (resolutions 256/512/1024, 5-16 co-located flash views)
+for 100 Adam iterations with the log(1+x) L2 loss, on 152 persistent CTAs, tiles of 960
+texels, the resident-state kernel splitting the 100 iterations into 4 launches of 25. This
+runs that exact configuration (and the one-launch-per-iteration texel-pair kernel at the
+same shapes) and checks it against the FP64 oracle, the restatement of the reference's
+SvbrdfOptim.optim loop (src/svbrdf.py:44-83) and Microfacet.eval (src/microfacet.py:84-120):
+
+* maps and both Adam moments after 100 iterations, at 256 seeded random texels of every
+  material plus the texels at each end of the material and around a tile boundary: a
+  texel's trajectory depends on that texel alone, so the oracle follows the sampled texels
+  exactly, without the rest of the material. Tolerance: relative L2 per material of at most
+  max(2e-5, twice the reference's own FP32 error) for the maps, and max(1e-4, twice that
+  error) for the moments; the FP32 error is measured on the first 72 sampled texels;
+* every loss of one whole 256^2 material (all its texels through the oracle, 100 iterations)
+  within 1e-5 relative;
+* the first iteration's loss of one material of each resolution, every texel through the
+  oracle, within 1e-5 relative (the reduction over tiles, warps and CTAs at full size);
+* all 100 losses of every material against the single-material fused kernel, within 1e-5.
+"""
+import time
+
+import pytest
+import torch
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+ITERS = 100
+SAMPLE = 256
+NOISE_SAMPLE = 72  # texels per material of the FP32 (reference arithmetic) run
+LR = 0.01
+
+
+def _gpu_render(svb, dev):
+    def fn(tex, cam, lit, lp, size):
+        r = svb.Microfacet(tex.shape[-1], cam.shape[0], size, [cam.to(dev), lit.to(dev), lp.to(dev)], dev)
+        with torch.no_grad():
+            return r.eval(tex.to(dev))
+    return fn
+
+
+def sample_texels(T, g, tile=960):
+    """Seeded random texels plus the two ends of the material and the first tile boundary."""
+    fixed = torch.tensor([0, 1, tile - 2, tile - 1, tile, tile + 1, T - 2, T - 1])
+    return torch.cat((fixed, torch.randint(T, (SAMPLE,), generator=g))).clamp_(0, T - 1)
+
+
+def oracle_samples(R, mats, dtype, keep=None):
+    """One oracle call over the sampled texels of every material (views padded to the
+    largest count and masked, per-texel loss normaliser); `keep` texels per material when
+    given."""
+    g = torch.Generator().manual_seed(42)
+    vmax = max(m.n_views for m in mats)
+    cols = {k: [] for k in ("t9", "px", "py", "tg", "cam", "lit", "pow", "n", "mask")}
+    idxs = []
+    for m in mats:
+        T = m.res * m.res
+        idx = sample_texels(T, g)
+        if keep is not None:
+            idx = idx[:keep]
+        idxs.append(idx)
+        n = idx.numel()
+        px, py = R.texel_positions(idx, m.res, m.res, m.size)
+        pad = vmax - m.n_views
+        cam = m.camera_pos.cpu()
+        lit = m.light_pos.cpu()
+        cols["t9"].append(m.init.cpu().reshape(9, -1)[:, idx])
+        cols["px"].append(px)
+        cols["py"].append(py)
+        tg = m.targets.cpu().reshape(m.n_views, 3, -1)[:, :, idx]
+        cols["tg"].append(torch.cat((tg, torch.zeros(pad, 3, n)), 0))
+        cols["cam"].append(torch.cat((cam, cam[:1].expand(pad, 3)), 0).unsqueeze(2).expand(-1, -1, n))
+        cols["lit"].append(torch.cat((lit, lit[:1].expand(pad, 3)), 0).unsqueeze(2).expand(-1, -1, n))
+        cols["pow"].append(m.light_pow.cpu().view(3, 1).expand(3, n))
+        cols["n"].append(torch.full((n,), float(m.n_views * 3 * T), dtype=torch.float64))
+        cols["mask"].append(torch.cat((torch.ones(m.n_views, n), torch.zeros(pad, n)), 0))
+    c = {k: torch.cat(v, -1) for k, v in cols.items()}
+    out = R.optim_texels(c["t9"], c["px"], c["py"], c["tg"], c["cam"], c["lit"], c["pow"], c["n"], ITERS, LR,
+                         "log1p", dtype, view_mask=c["mask"])
+    return idxs, out
+
+
+@pytest.fixture(scope="module")
+def workload(svb, cuda):
+    from oracle import microfacet_ref as R
+
+    torch.set_num_threads(max(torch.get_num_threads(), 1))
+    mats = svb.scenes.batched_scenes(n=64, device=cuda, render_fn=None)
+    rf = _gpu_render(svb, cuda)
+    for m in mats:
+        svb.scenes.add_targets(m, rf)
+    t0 = time.perf_counter()
+    idxs, o64 = oracle_samples(R, mats, torch.float64)
+    _, o32 = oracle_samples(R, mats, torch.float32, keep=NOISE_SAMPLE)
+    # one whole 256^2 material (the fewest views) through the oracle for every loss
+    small = min((i for i, m in enumerate(mats) if m.res == 256), key=lambda i: mats[i].n_views)
+    m = mats[small]
+    T = m.res * m.res
+    ax, ay = R.texel_positions(torch.arange(T), m.res, m.res, m.size)
+    whole = R.optim_texels(m.init.cpu().reshape(9, -1), ax, ay, m.targets.cpu().reshape(m.n_views, 3, -1),
+                           m.camera_pos.cpu(), m.light_pos.cpu(), m.light_pow.cpu(), m.n_views * 3 * T, ITERS, LR,
+                           "log1p", torch.float64)
+    whole_loss = (whole["sq_err"].sum(1) / (m.n_views * 3 * T)).tolist()
+    # the first loss of one material of each resolution, every texel
+    first = {}
+    for res in (256, 512, 1024):
+        i = next(k for k, mm in enumerate(mats) if mm.res == res)
+        mm = mats[i]
+        T = mm.res * mm.res
+        px, py = R.texel_positions(torch.arange(T), mm.res, mm.res, mm.size)
+        t9 = mm.init.cpu().reshape(9, -1)
+        tg = mm.targets.cpu().reshape(mm.n_views, 3, -1)
+        tot = 0.0
+        for c0 in range(0, T, 1 << 16):
+            sl = slice(c0, c0 + (1 << 16))
+            tot += R.loss_texels(t9[:, sl], px[sl], py[sl], tg[:, :, sl], mm.camera_pos.cpu(), mm.light_pos.cpu(),
+                                 mm.light_pow.cpu(), "log1p")
+        first[i] = tot / (mm.n_views * 3 * T)
+    print(f"oracle work {time.perf_counter() - t0:.1f} s")
+    # every material's 100 losses through the single-material fused kernel
+    single = []
+    for mm in mats:
+        r = svb.Microfacet(mm.res, mm.n_views, mm.size, mm.cl, cuda)
+        o = svb.SvbrdfOptim(cuda, r, loss="log1p", graph=True)
+        o.load_targets(mm.targets)
+        o.init_from_tex(mm.init)
+        o.optim(ITERS, LR, None, False)
+        single.append(o.loss_image_list)
+    return {"mats": mats, "idxs": idxs, "o64": o64, "o32": o32, "small": small, "whole": whole,
+            "whole_loss": whole_loss, "first": first, "single": single}
+
+
+def _col_ranges(idxs):
+    out, c = [], 0
+    for idx in idxs:
+        out.append(slice(c, c + idx.numel()))
+        c += idx.numel()
+    return out
+
+
+@pytest.mark.parametrize("variant", [3, 2])
+def test_bench_workload_matches_oracle(svb, cuda, workload, variant):
+    mats = workload["mats"]
+    cfg = svb.BatchConfig(threads=480, tile_texels=960, ctas=0, variant=variant)
+    b = svb.BatchedOptim(mats, lr=LR, loss="log1p", device=cuda, config=cfg, hist_len=ITERS)
+    assert b.n_ctas() == torch.cuda.get_device_properties(cuda).multi_processor_count
+    if variant == 3:
+        assert b.launches(ITERS) == 4  # 4 launches of 25 iterations
+    b.run(ITERS)
+    torch.cuda.synchronize()
+    assert b.device_error() == 0
+    hist = b.loss_hist.cpu()
+    o64, o32 = workload["o64"], workload["o32"]
+    nsl = [slice(k * NOISE_SAMPLE, (k + 1) * NOISE_SAMPLE) for k in range(len(mats))]
+    for i, (m, sl, idx) in enumerate(zip(mats, _col_ranges(workload["idxs"]), workload["idxs"])):
+        got = {"textures": b.tex[i].reshape(9, -1)[:, idx.to(cuda)], "exp_avg": b.m1[i].reshape(9, -1)[:, idx.to(cuda)],
+               "exp_avg_sq": b.m2[i].reshape(9, -1)[:, idx.to(cuda)]}
+        for k, floor in (("textures", 2e-5), ("exp_avg", 1e-4), ("exp_avg_sq", 1e-4)):
+            ref = o64[k][:, sl]
+            # the reference's own FP32 arithmetic on the first NOISE_SAMPLE of these texels
+            noise = rel_l2(o32[k][:, nsl[i]], ref[:, :NOISE_SAMPLE])
+            err = rel_l2(got[k], ref)
+            assert err <= max(floor, 2 * noise), (i, m.res, m.n_views, k, err, noise)
+        for it in range(ITERS):
+            ref = workload["single"][i][it]
+            assert abs(float(hist[it, i]) - ref) <= 1e-5 * ref, (i, it)
+    s = workload["small"]
+    for it in range(ITERS):
+        ref = workload["whole_loss"][it]
+        assert abs(float(hist[it, s]) - ref) <= 1e-5 * ref, ("whole material", it)
+    for k in ("textures", "exp_avg", "exp_avg_sq"):
+        ref = workload["whole"][k]
+        got = {"textures": b.tex, "exp_avg": b.m1, "exp_avg_sq": b.m2}[k][s].reshape(9, -1)
+        assert rel_l2(got, ref) <= (2e-5 if k == "textures" else 1e-4), ("whole material", k)
+    for i, ref in workload["first"].items():
+        assert abs(float(hist[0, i]) - ref) <= 1e-5 * ref, ("first loss", i)

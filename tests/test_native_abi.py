@@ -283,3 +283,15 @@ def test_corrupt_plan_is_rejected_on_host(svb, lib):
     # the wait self-test needs its 16-byte workspace and a sane poll limit
     assert lib.svbrdf_selftest_wait_timeout(fake, 8, 100, None) == -4
     assert lib.svbrdf_selftest_wait_timeout(fake, 16, 0, None) == -1
+
+
+def test_texel_count_limit_rejected_on_host(lib):
+    """H*W must stay below 2^31 (the kernels index texels in 64 bits, rows and columns in 32):
+    the host rejects larger shapes before touching the device. Nothing is launched here."""
+    fake = ctypes.c_void_p(16)
+    for h, w in ((32768, 65536), (46341, 46341), (65536, 65536)):  # 2^31 exactly, just above, 2^32
+        rc = lib.svbrdf_render_fwd(fake, fake, fake, fake, 9, h, w, 17.0, fake, None, -1, None, None, 0, None)
+        assert rc == -2 and b"2^31" in lib.svbrdf_last_error()
+        args = [fake] * 8 + [9, h, w, 17.0, 0, 1, 0.01, 0.9, 0.999, 1e-8, fake, fake, 1 << 20, None]
+        assert lib.svbrdf_fused_step(*args) == -2
+        assert lib.svbrdf_fused_step_noalloc(*(args[:19] + [None])) == -2

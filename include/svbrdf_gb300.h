@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define SVBRDF_ABI_VERSION 3
+#define SVBRDF_ABI_VERSION 4
 
 enum {
   SVBRDF_OK = 0,
@@ -116,19 +116,28 @@ int svbrdf_fused_step_noalloc(float* textures, float* exp_avg, float* exp_avg_sq
 /* ---- batched: many materials of uneven resolution and view count in one launch ---- */
 
 /* One material of a batch. Device pointers except camera_pos/light_pos (HOST, read by the
- * planner only). Each material is what one SvbrdfOptim instance owns. */
+ * planner only). Each material is what one SvbrdfOptim instance owns.
+ * With light_adam_state non-NULL the material's light power is learnable, as with
+ * SvbrdfOptim.optim(..., optim_light=True) (src/svbrdf.py:48-50, 58-59): light_pow is then
+ * updated in place each iteration by the same Adam as the maps (one optimiser over
+ * [textures, light_pow], src/svbrdf.py:50), with state light_adam_state [6] =
+ * {exp_avg[3], exp_avg_sq[3]} (zeroed by the caller before the first step). The light is
+ * shared by every texel, so its gradient is a reduction over the whole material each
+ * iteration: such plans need variant 2 or 3, and variant 3 then runs one iteration per
+ * launch. Without it light_pow is only read. */
 typedef struct svbrdf_material {
   float* textures;         /* [9][H][W], updated in place */
   float* exp_avg;          /* [9][H][W] Adam first moment */
   float* exp_avg_sq;       /* [9][H][W] Adam second moment */
   const float* targets;    /* [V][3][H][W] */
-  const float* light_pow;  /* [3] */
+  float* light_pow;        /* [3]; written only when light_adam_state is non-NULL */
   const float* camera_pos; /* HOST [V][3] */
   const float* light_pos;  /* HOST [V][3] */
   int n_views;
   int height;
   int width;
   float size;
+  float* light_adam_state; /* [6] or NULL (light power fixed) */
 } svbrdf_material;
 
 /* Launch shape of the persistent batched kernel (chosen by the autotuner).
@@ -309,12 +318,17 @@ int svbrdf_gen_act_bwd(const float* gout, const float* y, const float* d, const 
 /* Floats of the `part` scratch the *_nhwc_bwd calls need. */
 int svbrdf_gen_nhwc_partial_floats(int b, int c);
 
-/* y [b][2h][2w][c] = 2x up-sampling (as svbrdf_gen_upsample2) of x [b][h][w][c], times s[b][c]
- * when s is not null. */
-int svbrdf_gen_upsample2_nhwc(const float* x, const float* s, float* y, int b, int h, int w, int c, void* stream);
+/* y [b][2h+2 halo][2w+2 halo][c] = 2x up-sampling (as svbrdf_gen_upsample2) of x [b][h][w][c],
+ * times s[b][c] when s is not null. halo 0 or 1: with 1 the map also holds the up-sampled
+ * samples at -1 and 2h (2w), x[0] / 4 and x[h-1] / 4 along each axis. A valid (unpadded) 3x3
+ * convolution of that map is the reference's up-sampling convolution: a stride-2 transposed
+ * convolution followed by the [1,3,3,1] filter (src/higan_models/stylegan2_generator_network.py:
+ * 727-735); a zero-padded convolution of the halo-free map differs from it on the border. */
+int svbrdf_gen_upsample2_nhwc(const float* x, const float* s, float* y, int b, int h, int w, int c, int halo,
+                              void* stream);
 
-/* Adjoint of the up-sampling: gx [b][h][w][c] from g [b][2h][2w][c]. */
-int svbrdf_gen_upsample2_nhwc_bwd(const float* g, float* gx, int b, int h, int w, int c, void* stream);
+/* Adjoint of the up-sampling: gx [b][h][w][c] from g [b][2h+2 halo][2w+2 halo][c]. */
+int svbrdf_gen_upsample2_nhwc_bwd(const float* g, float* gx, int b, int h, int w, int c, int halo, void* stream);
 
 /* y[b][p][c] = x[b][p][c] s[b][c], hw pixels. */
 int svbrdf_gen_scale_nhwc(const float* x, const float* s, float* y, int b, int hw, int c, void* stream);

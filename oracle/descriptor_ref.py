@@ -1,6 +1,11 @@
-"""FP64 CPU oracle of the descriptor loss. Parity unpinned: the reference's VGGLoss needs
-torchvision (absent here) and pretrained weights (not offline), so no golden vectors exist
-for it; this is a restatement of its source.
+"""FP64 CPU oracle of the descriptor loss.
+
+Parity is pinned for mode="reference": tests/golden/make_golden_nets.py runs the reference's
+own VGGLoss (src/descriptor.py:7-79) in FP64 with torchvision's vgg19 replaced by VGG19's
+layer list carrying seeded weights (the pretrained ImageNet weights cannot be downloaded),
+and tests/test_descriptor_oracle.py checks this module's features, Gram branch, loss and
+gradient against that fixture. The configs mode (max-pool, downsample, Gram term, hooks to
+relu4_1) shares every building block with the pinned mode.
 
 TEST INFRASTRUCTURE ONLY (tests and bench's CPU legs). Restates the VGG-feature loss of
 src/descriptor.py:7-79 with the stack the GPU module uses: 2x2 box downsample, ImageNet
@@ -13,8 +18,7 @@ measures the BF16 activations and FP32 tensor-core accumulation alone.
 mode="reference" restates the reference's own VGGLoss instead: full-resolution renders,
 VGG19 to relu4_2 with its max-pools replaced by 2x2 average pools (src/descriptor.py:16-19),
 hooks at features 1, 3, 13, 22 = relu1_1, relu1_2, relu3_2, relu4_2 (:26-27), and the
-feature MSE alone (:77-79). torchvision is absent here, so the reference module itself cannot
-be imported; the restatement follows its source line by line.
+feature MSE alone (:77-79).
 """
 from __future__ import annotations
 
@@ -50,6 +54,21 @@ def features(renders, weights, downsample=True, mode="config"):
         if name in hooks:
             out.append(x)
     return out
+
+
+def feature_vector(renders, weights, hook_weights=(0.25, 0.25, 0.25, 0.25), downsample=False, mode="reference"):
+    """The concatenated weighted feature vector of ``VGGLoss.compute_feature_vector``
+    (src/descriptor.py:39-60): per hook, the whole batch's features flattened (N, C, H, W
+    order) times the hook's weight, hooks in order."""
+    feats = features(renders, weights, downsample, mode)
+    return torch.cat([f.flatten() * w for f, w in zip(feats, hook_weights)])
+
+
+def gram_vector(render, weights, hook_weights=(0.25, 0.25, 0.25, 0.25), downsample=False, mode="reference"):
+    """``compute_feature_vector(x, is_gram=True)`` of one render (src/descriptor.py:50-56):
+    per hook G = F F^T / S of the [C, S] feature matrix, flattened, times the hook's weight."""
+    feats = features(render.unsqueeze(0) if render.dim() == 3 else render, weights, downsample, mode)
+    return torch.cat([gram(f).flatten() * w for f, w in zip(feats, hook_weights)])
 
 
 def gram(f):

@@ -98,6 +98,7 @@ class svbrdf_material(ctypes.Structure):
         ("height", ctypes.c_int),
         ("width", ctypes.c_int),
         ("size", ctypes.c_float),
+        ("light_adam_state", ctypes.c_void_p),
     ]
 
 
@@ -157,9 +158,9 @@ def _declare(L):
     L.svbrdf_gen_nhwc_partial_floats.restype = I
     L.svbrdf_gen_nhwc_partial_floats.argtypes = [I, I]
     L.svbrdf_gen_upsample2_nhwc.restype = I
-    L.svbrdf_gen_upsample2_nhwc.argtypes = [P, P, P, I, I, I, I, P]
+    L.svbrdf_gen_upsample2_nhwc.argtypes = [P, P, P, I, I, I, I, I, P]
     L.svbrdf_gen_upsample2_nhwc_bwd.restype = I
-    L.svbrdf_gen_upsample2_nhwc_bwd.argtypes = [P, P, I, I, I, I, P]
+    L.svbrdf_gen_upsample2_nhwc_bwd.argtypes = [P, P, I, I, I, I, I, P]
     L.svbrdf_gen_scale_nhwc.restype = I
     L.svbrdf_gen_scale_nhwc.argtypes = [P, P, P, I, I, I, P]
     L.svbrdf_gen_scale_nhwc_bwd.restype = I

@@ -52,11 +52,19 @@ class BatchConfig:
 class BatchedOptim:
     """Batched per-pixel optimisation. ``materials`` items need ``init`` ([1,9,H,W]),
     ``targets`` ([V,3,H,W]), ``camera_pos``/``light_pos`` ([V,3]), ``light_pow`` ([3]) and
-    ``size`` (cm); e.g. ``scenes.Scene`` objects."""
+    ``size`` (cm); e.g. ``scenes.Scene`` objects.
+
+    With ``optim_light`` every material's light power is optimised with its maps, as
+    ``SvbrdfOptim.optim(..., optim_light=True)`` does (src/svbrdf.py:48-50, 58-59); the
+    current values are ``light_pow(i)``. That needs the texel-pair kernels (variants 2 and 3),
+    and each iteration is then its own launch. With ``adopt_maps`` a material's ``init``
+    tensor that is already a contiguous FP32 tensor on the device becomes the optimised
+    maps in place instead of being copied."""
 
     def __init__(self, materials: Sequence, lr: float = 0.01, loss: str = "log1p", device="cuda",
                  config: Optional[BatchConfig] = None, betas=(0.9, 0.999), eps: float = 1e-8,
-                 hist_len: int = 100):
+                 hist_len: int = 100, optim_light: bool = False, adopt_maps: bool = False,
+                 candidates=None):
         self.L = N.lib()
         self.device = torch.device(device)
         self.lr, self.betas, self.eps = float(lr), betas, float(eps)
@@ -67,14 +75,20 @@ class BatchedOptim:
             raise ValueError("loss must be 'mse' or 'log1p'")
         self.loss = loss
         self.kind = LOSS_KINDS["mse"] if loss == "mse" else LOSS_KINDS["log1p_pre"]
+        self.optim_light = bool(optim_light)
+        self.lstate, self.lpow0 = [], []
         for m in materials:
-            t = m.init.detach().to(self.device, torch.float32).contiguous().clone()
+            t = m.init.detach()
+            if not (adopt_maps and t.device == self.device and t.dtype == torch.float32 and t.is_contiguous()):
+                t = t.to(self.device, torch.float32).contiguous().clone()
             self.tex.append(t)
             self.m1.append(torch.zeros_like(t))
             self.m2.append(torch.zeros_like(t))
             tg = m.targets.to(self.device, torch.float32).contiguous()
             self.tgt.append(torch.log1p(tg) if loss == "log1p" else tg)
-            self.lpow.append(torch.as_tensor(m.light_pow, dtype=torch.float32).to(self.device).contiguous())
+            self.lpow.append(torch.as_tensor(m.light_pow, dtype=torch.float32).to(self.device).contiguous().clone())
+            self.lpow0.append(self.lpow[-1].clone())
+            self.lstate.append(torch.zeros(6, device=self.device, dtype=torch.float32) if self.optim_light else None)
             self.cam_host.append(np.ascontiguousarray(torch.as_tensor(m.camera_pos).cpu().numpy(), dtype=np.float32))
             self.lit_host.append(np.ascontiguousarray(torch.as_tensor(m.light_pos).cpu().numpy(), dtype=np.float32))
             _, _, H, W = t.shape
@@ -84,7 +98,9 @@ class BatchedOptim:
         self.step_dev = torch.zeros(1, device=self.device, dtype=torch.int32)
         self.step_count = 0
         self.graph = None
-        self.config = config or autotune(self)
+        if config is None and self.optim_light:
+            candidates = candidates or [c for c in CANDIDATES if c[0] in (2, 3)]
+        self.config = config or autotune(self, candidates)
         self._build_plan(self.config)
 
     # ---- work accounting ----
@@ -97,7 +113,11 @@ class BatchedOptim:
 
     def launches(self, iters: int) -> int:
         """Kernel launches ``iters`` iterations take with this plan's variant."""
-        return -(-iters // FUSE_MAX) if self.config.variant >= 3 else iters
+        return -(-iters // FUSE_MAX) if self.config.variant >= 3 and not self.optim_light else iters
+
+    def light_pow(self, i: int) -> torch.Tensor:
+        """Material ``i``'s light power (optimised in place with ``optim_light``)."""
+        return self.lpow[i]
 
     def signature(self) -> str:
         h = hashlib.sha1(json.dumps(sorted(self.meta)).encode()).hexdigest()[:16]
@@ -106,23 +126,25 @@ class BatchedOptim:
     def tune_key(self) -> str:
         """The autotuner's cache key: the workload signature plus the library's ABI version and
         build hash, so a pick made with another build of the kernels is never reused."""
-        return f"{self.signature()}|{N.build_id()}"
+        return f"{self.signature()}|{N.build_id()}" + ("|light" if self.optim_light else "")
 
     # ---- plan ----
-    def _mat_array(self, tex=None, m1=None, m2=None):
+    def _mat_array(self, tex=None, m1=None, m2=None, lpow=None, lstate=None):
         tex = tex or self.tex
         m1 = m1 or self.m1
         m2 = m2 or self.m2
+        lpow = lpow or self.lpow
+        lstate = lstate or self.lstate
         arr = (N.svbrdf_material * self.n)()
         for i in range(self.n):
             H, W, V, size = self.meta[i]
             arr[i] = N.svbrdf_material(tex[i].data_ptr(), m1[i].data_ptr(), m2[i].data_ptr(), self.tgt[i].data_ptr(),
-                                       self.lpow[i].data_ptr(), self.cam_host[i].ctypes.data,
-                                       self.lit_host[i].ctypes.data, V, H, W, size)
+                                       lpow[i].data_ptr(), self.cam_host[i].ctypes.data,
+                                       self.lit_host[i].ctypes.data, V, H, W, size, N.ptr(lstate[i]))
         return arr
 
-    def _make_plan(self, cfg: BatchConfig, tex=None, m1=None, m2=None):
-        arr = self._mat_array(tex, m1, m2)
+    def _make_plan(self, cfg: BatchConfig, tex=None, m1=None, m2=None, lpow=None, lstate=None):
+        arr = self._mat_array(tex, m1, m2, lpow, lstate)
         c = cfg.as_c()
         nbytes = self.L.svbrdf_batched_plan_bytes(arr, self.n, ctypes.byref(c))
         if nbytes == 0:
@@ -193,12 +215,16 @@ class BatchedOptim:
 
     def prepare(self, new_targets: bool = True):
         """The device half of ``reset``: transform freshly uploaded targets for the loss, zero
-        the moments, the step counter and the loss history."""
+        the moments, the step counter and the loss history (and, with ``optim_light``, put
+        each light power back to its initial value with a fresh Adam state)."""
         for i in range(self.n):
             if new_targets and self.loss == "log1p":
                 self.tgt[i].log1p_()
             self.m1[i].zero_()
             self.m2[i].zero_()
+            if self.optim_light:
+                self.lpow[i].copy_(self.lpow0[i])
+                self.lstate[i].zero_()
         self.step_dev.zero_()
         self.loss_hist.zero_()
         self.step_count = 0
@@ -211,9 +237,13 @@ class BatchedOptim:
         """Everything a later run needs to continue bit-identically: maps, both Adam moments,
         the device step counter and the loss history (FP32, on the host)."""
         torch.cuda.synchronize(self.device)
-        return {"tex": [t.cpu() for t in self.tex], "exp_avg": [t.cpu() for t in self.m1],
-                "exp_avg_sq": [t.cpu() for t in self.m2], "step": int(self.step_dev.item()),
-                "loss_hist": self.loss_hist.cpu(), "step_count": self.step_count, "signature": self.signature()}
+        st = {"tex": [t.cpu() for t in self.tex], "exp_avg": [t.cpu() for t in self.m1],
+              "exp_avg_sq": [t.cpu() for t in self.m2], "step": int(self.step_dev.item()),
+              "loss_hist": self.loss_hist.cpu(), "step_count": self.step_count, "signature": self.signature()}
+        if self.optim_light:
+            st["light_pow"] = [t.cpu() for t in self.lpow]
+            st["light_adam"] = [t.cpu() for t in self.lstate]
+        return st
 
     def load_state_dict(self, st: dict):
         if st.get("signature") not in (None, self.signature()):
@@ -222,6 +252,11 @@ class BatchedOptim:
             if len(dst) != len(src):
                 raise ValueError("checkpoint has a different number of materials")
             for d, s_ in zip(dst, src):
+                d.copy_(s_)
+        if self.optim_light and "light_pow" in st:
+            for d, s_ in zip(self.lpow, st["light_pow"]):
+                d.copy_(s_)
+            for d, s_ in zip(self.lstate, st["light_adam"]):
                 d.copy_(s_)
         self.step_dev.fill_(int(st["step"]))
         lh = st["loss_hist"]
@@ -334,7 +369,9 @@ def _time_config(opt: BatchedOptim, cfg: BatchConfig, iters: int = 8) -> float:
     tex = [t.clone() for t in opt.tex]
     m1 = [torch.zeros_like(t) for t in tex]
     m2 = [torch.zeros_like(t) for t in tex]
-    host, dev, ws = opt._make_plan(cfg, tex, m1, m2)
+    lpow = [t.clone() for t in opt.lpow]
+    lstate = [None if t is None else torch.zeros_like(t) for t in opt.lstate]
+    host, dev, ws = opt._make_plan(cfg, tex, m1, m2, lpow, lstate)
     loss = torch.zeros(1, opt.n, device=opt.device)
     step = torch.zeros(1, device=opt.device, dtype=torch.int32)
     opt._launch(host, dev, ws, step, loss, 2)  # warm

@@ -234,7 +234,8 @@ template <int NT>
 __device__ __forceinline__ void batched_finish(const char* plan, const PlanHeader* hdr, const MatDesc* mats,
                                                const float* partial, int per_tile, float* loss_hist, int hist_len,
                                                int step, int* step_counter, unsigned* counter, int* s_flag,
-                                               int nwarps, int iters = 1) {
+                                               int nwarps, int iters = 1, const float* lpart = nullptr,
+                                               const AdamScalars* light_adam = nullptr) {
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
@@ -260,9 +261,57 @@ __device__ __forceinline__ void batched_finish(const char* plan, const PlanHeade
       }
     }
   }
+  if (lpart && w < nwarps) {
+    // Learnable light (one-iteration launches): per material, the light-power gradient summed
+    // over its (tile, warp) partials in a fixed order, then Adam on the light with the maps'
+    // hyper-parameters and step (one optimiser over [textures, light_pow], src/svbrdf.py:50).
+    const AdamScalars ad = *light_adam;
+    for (int mi = w; mi < hdr->n_mat; mi += nwarps) {
+      const MatDesc& md = mats[mi];
+      if (!md.lstate) continue;
+      double g[3] = {0.0, 0.0, 0.0};
+      const int e0 = mat_tiles[mi] * per_tile, e1 = mat_tiles[mi + 1] * per_tile;
+      for (int t = e0 + lane; t < e1; t += 32) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) g[c] += (double)__ldcg(lpart + 3 * (size_t)t + c);
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) g[c] += __shfl_xor_sync(0xffffffffu, g[c], o);
+      }
+      if (lane == 0) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          float p = md.lpow[c], m1 = md.lstate[c], m2 = md.lstate[3 + c];
+          adam_update(p, m1, m2, (float)g[c], ad);
+          md.lpow[c] = p;
+          md.lstate[c] = m1;
+          md.lstate[3 + c] = m2;
+        }
+      }
+    }
+  }
   if (threadIdx.x == 0) {
     *step_counter = step;
     *counter = 0u;
+  }
+}
+
+// Light-power gradient partial of one warp's texels of one tile: lanes' values summed in a
+// fixed order, written by lane 0 to slot (tile, warp).
+__device__ __forceinline__ void write_light_partial(float* lpart, int tile, int nwarps, float s0, float s1, float s2) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+    s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+    s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    float* p = lpart + 3 * ((size_t)tile * nwarps + (threadIdx.x >> 5));
+    p[0] = s0;
+    p[1] = s1;
+    p[2] = s2;
   }
 }
 
@@ -742,7 +791,8 @@ struct __align__(16) PairSlotRec {
 template <int LOSS, int NCW, bool GEN>
 __global__ void __launch_bounds__((NCW + 1) * 32, NCW <= kPairTwoCtaNcw ? 2 : 1)
 batched_pair_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restrict__ step_counter,
-                    float* __restrict__ loss_hist, int hist_len, float* __restrict__ warp_loss, unsigned* ws) {
+                    float* __restrict__ loss_hist, int hist_len, float* __restrict__ warp_loss, unsigned* ws,
+                    float* __restrict__ lpart) {
   constexpr int NT = NCW * 32;
   constexpr int TT = 2 * NT;                  // texels per tile
   constexpr int SLOT = kPairSlotPlanes * TT;  // floats per ring slot
@@ -897,6 +947,7 @@ batched_pair_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
       float2 g[9];
       float2 pv[9];  // raw parameters of the second P copy
       float2 loss2;
+      float2 gpl[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};  // dL/d light
       bool live = true;
       if (!GEN || r0.all_coloc) {
         TexelPair u;
@@ -940,6 +991,7 @@ batched_pair_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
 #pragma unroll
         for (int c = 0; c < 9; ++c) t9[c] = clamp2(pv[c]);
         loss2 = coloc_finish_pair<LOSS>(t9, u, a, P, scale, g);
+        if (lpart) coloc_light_grad_pair<LOSS>(t9, a, scale, gpl);
       } else {
         // general views: the two texels one after the other through each chunk
         const float P[3] = {r0.P[0], r0.P[1], r0.P[2]};
@@ -970,11 +1022,11 @@ batched_pair_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
             const View& w = rv.view[j];
             float ia[3] = {t0.x, t1.x, t2.x}, ib[3] = {t0.y, t1.y, t2.y};
             if (w.coloc != 0.f) {
-              texel_view<kModeFused, LOSS, false, true>(ma, px.x, py.x, w, P, ia, la, aa);
-              texel_view<kModeFused, LOSS, false, true>(mb, px.y, py.y, w, P, ib, lb, ab);
+              texel_view<kModeFused, LOSS, true, true>(ma, px.x, py.x, w, P, ia, la, aa);
+              texel_view<kModeFused, LOSS, true, true>(mb, px.y, py.y, w, P, ib, lb, ab);
             } else {
-              texel_view<kModeFused, LOSS, false, false>(ma, px.x, py.x, w, P, ia, la, aa);
-              texel_view<kModeFused, LOSS, false, false>(mb, px.y, py.y, w, P, ib, lb, ab);
+              texel_view<kModeFused, LOSS, true, false>(ma, px.x, py.x, w, P, ia, la, aa);
+              texel_view<kModeFused, LOSS, true, false>(mb, px.y, py.y, w, P, ib, lb, ab);
             }
           }
           ring_release(rc, empty_bar, R);
@@ -983,6 +1035,8 @@ batched_pair_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
         const float2* pq = pair_acquire<SLOT>(rc, ring, full_bar, err) + tid;
         if (!rc.ok) break;
         const float scale = recs[rc.slot].scale;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) gpl[c] = make_float2(aa.gp[c] * scale, ab.gp[c] * scale);
 #pragma unroll
         for (int c = 0; c < 9; ++c) pv[c] = pq[c * NT];
         ring_release(rc, empty_bar, R);
@@ -1037,10 +1091,13 @@ batched_pair_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, o);
       if (lane == 0) warp_loss[(size_t)tile * NCW + warp] = loss;
+      if (lpart)
+        write_light_partial(lpart, tile, NCW, active ? gpl[0].x + gpl[0].y : 0.f, active ? gpl[1].x + gpl[1].y : 0.f,
+                            active ? gpl[2].x + gpl[2].y : 0.f);
     }
   }
   batched_finish<NT + 32>(plan, hdr, mats, warp_loss, NCW, loss_hist, hist_len, s_step, step_counter,
-                          ws + kWsCounter, &s_last, NCW);
+                          ws + kWsCounter, &s_last, NCW, 1, lpart, &s_adam);
 }
 
 // ============================================================== variant 3: resident state
@@ -1102,7 +1159,7 @@ template <int LOSS, int NCW, bool GEN>
 __global__ void __launch_bounds__((NCW + 1) * 32, NCW <= kPairTwoCtaNcw ? 2 : 1)
 batched_fuse_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restrict__ step_counter,
                     float* __restrict__ loss_hist, int hist_len, int iters, float* __restrict__ warp_loss,
-                    unsigned* ws) {
+                    unsigned* ws, float* __restrict__ lpart) {
   constexpr int NT = NCW * 32;
   constexpr int TT = 2 * NT;                  // texels per tile
   constexpr int SLOT = kPairSlotPlanes * TT;  // floats per ring slot
@@ -1265,6 +1322,7 @@ batched_fuse_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
       for (int it = 0; it < iters; ++it) {
         float2 g[9];
         float2 loss2;
+        float2 gpl[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};  // dL/d light
         float2 px = make_float2(0.f, 0.f), py = make_float2(0.f, 0.f);
         if (active) pair_coords(r0, tid, px, py);
         if (coloc) {
@@ -1301,6 +1359,7 @@ batched_fuse_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
           for (int c = 0; c < 9; ++c) t9[c] = clamp2(sp[c * NT]);
           const float P[3] = {r0.P[0], r0.P[1], r0.P[2]};
           loss2 = coloc_finish_pair<LOSS>(t9, u, a, P, r0.scale, g);
+          if (lpart) coloc_light_grad_pair<LOSS>(t9, a, r0.scale, gpl);
         } else {
           // general views: the two texels one after the other through each chunk
           const float P[3] = {r0.P[0], r0.P[1], r0.P[2]};
@@ -1330,16 +1389,18 @@ batched_fuse_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
               const View& w = rv.view[j];
               float ia[3] = {t0.x, t1.x, t2.x}, ib[3] = {t0.y, t1.y, t2.y};
               if (w.coloc != 0.f) {
-                texel_view<kModeFused, LOSS, false, true>(ma, px.x, py.x, w, P, ia, la, aa);
-                texel_view<kModeFused, LOSS, false, true>(mb, px.y, py.y, w, P, ib, lb, ab);
+                texel_view<kModeFused, LOSS, true, true>(ma, px.x, py.x, w, P, ia, la, aa);
+                texel_view<kModeFused, LOSS, true, true>(mb, px.y, py.y, w, P, ib, lb, ab);
               } else {
-                texel_view<kModeFused, LOSS, false, false>(ma, px.x, py.x, w, P, ia, la, aa);
-                texel_view<kModeFused, LOSS, false, false>(mb, px.y, py.y, w, P, ib, lb, ab);
+                texel_view<kModeFused, LOSS, true, false>(ma, px.x, py.x, w, P, ia, la, aa);
+                texel_view<kModeFused, LOSS, true, false>(mb, px.y, py.y, w, P, ib, lb, ab);
               }
             }
             ring_release(rc, empty_bar, R);
           }
           if (!live) break;
+#pragma unroll
+          for (int c = 0; c < 3; ++c) gpl[c] = make_float2(aa.gp[c] * r0.scale, ab.gp[c] * r0.scale);
           float ta[9], tb[9], ga[9], gb[9];
 #pragma unroll
           for (int c = 0; c < 9; ++c) {
@@ -1384,6 +1445,9 @@ batched_fuse_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, o);
         if (lane == 0) warp_loss[((size_t)it * n_tiles + r0.tile) * NCW + warp] = loss;
+        if (lpart)  // plans with a learnable light run one iteration per launch
+          write_light_partial(lpart, r0.tile, NCW, active ? gpl[0].x + gpl[0].y : 0.f,
+                              active ? gpl[1].x + gpl[1].y : 0.f, active ? gpl[2].x + gpl[2].y : 0.f);
       }
       if (!live) break;
       // this warp's shared-memory writes come before the next tile's bulk copies into the area
@@ -1393,7 +1457,7 @@ batched_fuse_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
     }
   }
   batched_finish<NT + 32>(plan, hdr, mats, warp_loss, NCW, loss_hist, hist_len, s_step, step_counter,
-                          ws + kWsCounter, &s_last, NCW, iters);
+                          ws + kWsCounter, &s_last, NCW, iters, lpart, &s_adam[0]);
 }
 
 // ============================================================== variant 4: resident state, no producer
@@ -1841,6 +1905,9 @@ static int plan_layout(const svbrdf_material* mats, int n, const svbrdf_batch_co
     if (m.n_views <= 0 || m.height <= 0 || m.width <= 0 || !(m.size > 0.f))
       return fail(SVBRDF_ERR_INVALID, "material %d has a bad shape", i);
     if (m.n_views > kMaxViews) return fail(SVBRDF_ERR_UNSUPPORTED, "material %d: too many views", i);
+    if (m.light_adam_state && variant != 2 && variant != 3)
+      return fail(SVBRDF_ERR_UNSUPPORTED, "material %d: a learnable light power needs variant 2 or 3 (got %d)", i,
+                  variant);
     const long long T = (long long)m.height * m.width;
     if (T >= (1LL << 24)) return fail(SVBRDF_ERR_UNSUPPORTED, "material %d: more than 2^24 texels", i);
     if (variant >= 1) {
@@ -2122,6 +2189,19 @@ int svbrdf_fused_step_noalloc(float* textures, float* exp_avg, float* exp_avg_sq
   return check_launch("fused_step_kernel (no-allocation)");
 }
 
+}  // extern "C"
+
+namespace svb {
+// (tile, warp) partial slots of one iteration, and the loss-partial floats of a launch
+// (every iteration of a resident-state launch keeps its own).
+static size_t ws_slots(const PlanHeader* h) {
+  return (size_t)h->n_tiles * (h->variant >= 1 ? (size_t)(h->threads / 32) : 1);
+}
+static size_t ws_loss_floats(const PlanHeader* h) { return ws_slots(h) * (h->variant >= 3 ? (size_t)kFuseMax : 1); }
+}  // namespace svb
+
+extern "C" {
+
 size_t svbrdf_batched_plan_bytes(const svbrdf_material* materials, int n_materials,
                                  const svbrdf_batch_config* config) {
   PlanLayout L;
@@ -2175,6 +2255,8 @@ int svbrdf_batched_plan(const svbrdf_material* materials, int n_materials, const
     md[i].m2 = m.exp_avg_sq;
     md[i].tgt = m.targets;
     md[i].lpow = m.light_pow;
+    md[i].lstate = m.light_adam_state;
+    if (m.light_adam_state) h->light = 1;
     md[i].H = m.height;
     md[i].W = m.width;
     md[i].V = m.n_views;
@@ -2239,9 +2321,7 @@ size_t svbrdf_batched_workspace_bytes(const void* host_plan) {
   if (!host_plan) return 0;
   const PlanHeader* h = (const PlanHeader*)host_plan;
   if (h->magic != kPlanMagic) return 0;
-  const size_t per_tile = h->variant >= 1 ? (size_t)(h->threads / 32) : 1;
-  const size_t iters = h->variant >= 3 ? (size_t)kFuseMax : 1;  // partials of every iteration of a launch
-  return kWsLossOffset + sizeof(float) * (size_t)h->n_tiles * per_tile * iters;
+  return kWsLossOffset + sizeof(float) * ws_loss_floats(h) + (h->light ? sizeof(float) * 3 * ws_slots(h) : 0);
 }
 
 int svbrdf_selftest_wait_timeout(void* workspace, size_t workspace_bytes, int limit, void* stream) {
@@ -2261,7 +2341,7 @@ int svbrdf_batched_step(const void* device_plan, const void* host_plan, int loss
 // One launch of the single-iteration variants (0, 1, 2).
 static int batched_launch_one(const PlanHeader* h, const char* plan, int loss_kind, int* step_counter,
                               AdamHyper hyper, float* loss_hist, int hist_len, unsigned* ws, float* part,
-                              cudaStream_t st);
+                              float* lpart, cudaStream_t st);
 
 int svbrdf_batched_steps(const void* device_plan, const void* host_plan, int loss_kind, int* step_counter, float lr,
                          float beta1, float beta2, float eps, float* loss_hist, int hist_len, int iters,
@@ -2278,6 +2358,7 @@ int svbrdf_batched_steps(const void* device_plan, const void* host_plan, int los
   if (!workspace || workspace_bytes < need) return fail(SVBRDF_ERR_WORKSPACE, "workspace of %zu bytes needed", need);
   unsigned* ws = (unsigned*)workspace;
   float* part = (float*)((char*)workspace + kWsLossOffset);
+  float* lpart = h->light ? part + ws_loss_floats(h) : nullptr;
   AdamHyper hyper;
   hyper.lr = lr;
   hyper.beta1 = beta1;
@@ -2287,18 +2368,20 @@ int svbrdf_batched_steps(const void* device_plan, const void* host_plan, int los
   const char* plan = (const char*)device_plan;
   if (h->variant < 3) {
     for (int i = 0; i < iters; ++i) {
-      const int rc = batched_launch_one(h, plan, loss_kind, step_counter, hyper, loss_hist, hist_len, ws, part, st);
+      const int rc =
+          batched_launch_one(h, plan, loss_kind, step_counter, hyper, loss_hist, hist_len, ws, part, lpart, st);
       if (rc) return rc;
     }
     return SVBRDF_OK;
   }
   const int ring = h->ring_slots;
   if (ring < 2 || ring > kMaxRing) return fail(SVBRDF_ERR_INVALID, "bad ring depth %d", ring);
-  // iters split evenly over ceil(iters / kFuseMax) launches
-  const int launches = (iters + kFuseMax - 1) / kFuseMax;
+  // iters split evenly over ceil(iters / kFuseMax) launches; a learnable light couples every
+  // texel of a material once per iteration, so such plans run one iteration per launch
+  const int launches = h->light ? iters : (iters + kFuseMax - 1) / kFuseMax;
   for (int l = 0; l < launches; ++l) {
     const int k = iters / launches + (l < iters % launches ? 1 : 0);
-#define SVB_F(L, NCW, G)                                                                                       {                                                                                                              int prc = fuse_prepare<L, NCW, G>(ring);                                                                     if (prc) return prc;                                                                                         batched_fuse_kernel<L, NCW, G><<<h->n_ctas, (NCW + 1) * 32, fuse_smem<NCW>(ring), st>>>(                         plan, hyper, step_counter, loss_hist, hist_len, k, part, ws);                                          }
+#define SVB_F(L, NCW, G)                                                                                       {                                                                                                              int prc = fuse_prepare<L, NCW, G>(ring);                                                                     if (prc) return prc;                                                                                         batched_fuse_kernel<L, NCW, G><<<h->n_ctas, (NCW + 1) * 32, fuse_smem<NCW>(ring), st>>>(                         plan, hyper, step_counter, loss_hist, hist_len, k, part, ws, lpart);                                   }
 #define SVB_FG(L, NCW)                  if (h->general) SVB_F(L, NCW, true)   else SVB_F(L, NCW, false)
 #define SVB_FL(NCW)                                         if (loss_kind == SVBRDF_LOSS_MSE) SVB_FG(0, NCW)          else if (loss_kind == SVBRDF_LOSS_LOG1P) SVB_FG(1, NCW)   else SVB_FG(2, NCW)
     if (h->variant == 3) {
@@ -2330,7 +2413,7 @@ int svbrdf_batched_steps(const void* device_plan, const void* host_plan, int los
 
 static int batched_launch_one(const PlanHeader* h, const char* plan, int loss_kind, int* step_counter,
                               AdamHyper hyper, float* loss_hist, int hist_len, unsigned* ws, float* part,
-                              cudaStream_t st) {
+                              float* lpart, cudaStream_t st) {
   if (h->variant == 0) {
 #define SVB_B(L, NT) \
   batched_step_kernel<L, NT><<<h->n_ctas, NT, 0, st>>>(plan, hyper, step_counter, loss_hist, hist_len, part, ws)
@@ -2355,7 +2438,7 @@ static int batched_launch_one(const PlanHeader* h, const char* plan, int loss_ki
     int prc = pair_prepare<L, NCW, G>(ring);                                                                 \
     if (prc) return prc;                                                                                     \
     batched_pair_kernel<L, NCW, G><<<h->n_ctas, (NCW + 1) * 32, pair_smem<NCW>(ring), st>>>(                 \
-        plan, hyper, step_counter, loss_hist, hist_len, part, ws);                                           \
+        plan, hyper, step_counter, loss_hist, hist_len, part, ws, lpart);                                    \
   }
 #define SVB_PG(L, NCW)         \
   if (h->general) SVB_P(L, NCW, true) \

@@ -5,7 +5,11 @@
 //
 //   nhwc_up_fwd_kernel     2x up-sampling (zero insertion + [1,3,3,1]^2 / 64 FIR, gain 4, zero
 //                          padding) of x, optionally times s[b][c]: out[2m] = (x[m-1] + 3 x[m]) / 4,
-//                          out[2m+1] = (3 x[m] + x[m+1]) / 4 along each axis
+//                          out[2m+1] = (3 x[m] + x[m+1]) / 4 along each axis; with a halo of one,
+//                          also the samples at -1 and 2n (x[0] / 4 and x[n-1] / 4), which a valid
+//                          3x3 convolution of the result needs to equal the reference's transposed
+//                          convolution followed by the filter (src/higan_models/
+//                          stylegan2_generator_network.py:727-735)
 //   nhwc_up_bwd_kernel     its adjoint: gx[m] = (g[2m-1] + 3 g[2m] + 3 g[2m+1] + g[2m+2]) / 4 per axis
 //   nhwc_scale_fwd_kernel  y = x s[b][c]
 //   nhwc_scale_bwd_kernel  gx = g s[b][c] and per-chunk column sums of g x (the style gradient)
@@ -61,16 +65,17 @@ __device__ __forceinline__ void taps(int o, int n, int& lo, int& hi, float& wlo,
 
 __device__ __forceinline__ float act_pre(float y, float dv, float nz, float bias) { return fmaf(y, dv, nz) + bias; }
 
-// grid (ceil(2w cv / 256), B 2h): block row (b, Y); thread t of the row is output vector
-// (X, c) = (t / cv, t % cv). 32-bit index math within a row.
+// grid (ceil(W2 cv / 256), B H2), W2 = 2w + 2 halo: block row (b, Y); thread t of the row is
+// output vector (X, c) = (t / cv, t % cv), at up-sampled index X - halo. 32-bit index math
+// within a row.
 template <int VEC>
 __global__ void __launch_bounds__(256) nhwc_up_fwd_kernel(const float* __restrict__ x, const float* __restrict__ s,
-                                                          float* __restrict__ y, int h, int w, int C) {
-  const int cv = C / VEC, W2 = 2 * w;
-  const int Y = blockIdx.y % (2 * h), b = blockIdx.y / (2 * h);
+                                                          float* __restrict__ y, int h, int w, int C, int halo) {
+  const int cv = C / VEC, W2 = 2 * w + 2 * halo, H2 = 2 * h + 2 * halo;
+  const int Y = blockIdx.y % H2, b = blockIdx.y / H2;
   int y0, y1;
   float wy0, wy1;
-  taps(Y, h, y0, y1, wy0, wy1);
+  taps(Y - halo, h, y0, y1, wy0, wy1);
   const float* r0 = x + ((long long)b * h + y0) * w * C;
   const float* r1 = x + ((long long)b * h + y1) * w * C;
   const float* sb = s ? s + (long long)b * C : nullptr;
@@ -79,7 +84,7 @@ __global__ void __launch_bounds__(256) nhwc_up_fwd_kernel(const float* __restric
     const int c = t % cv, X = t / cv;
     int x0, x1;
     float wx0, wx1;
-    taps(X, w, x0, x1, wx0, wx1);
+    taps(X - halo, w, x0, x1, wx0, wx1);
     float a[VEC], bq[VEC], cq[VEC], d[VEC], o[VEC];
     ldv<VEC>(r0 + x0 * C + c * VEC, a);
     ldv<VEC>(r0 + x1 * C + c * VEC, bq);
@@ -98,11 +103,12 @@ __global__ void __launch_bounds__(256) nhwc_up_fwd_kernel(const float* __restric
 }
 
 // grid (ceil(w cv / 256), B h): block row (b, ym); thread t is input vector (xm, c), summed
-// from output rows 2ym-1 .. 2ym+2 and columns 2xm-1 .. 2xm+2.
+// from output rows 2ym-1 .. 2ym+2 and columns 2xm-1 .. 2xm+2 (up-sampled indices; g holds
+// them from -halo on).
 template <int VEC>
 __global__ void __launch_bounds__(256) nhwc_up_bwd_kernel(const float* __restrict__ g, float* __restrict__ gx, int h,
-                                                          int w, int C) {
-  const int cv = C / VEC, H = 2 * h, W = 2 * w;
+                                                          int w, int C, int halo) {
+  const int cv = C / VEC, H = 2 * h + 2 * halo, W = 2 * w + 2 * halo;
   const int ym = blockIdx.y % h, b = blockIdx.y / h;
   const float wt[4] = {0.25f, 0.75f, 0.75f, 0.25f};
   const float* gb = g + (long long)b * H * W * C;
@@ -114,7 +120,7 @@ __global__ void __launch_bounds__(256) nhwc_up_bwd_kernel(const float* __restric
     for (int j = 0; j < VEC; ++j) acc[j] = 0.0f;
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
-      const int Yr = 2 * ym - 1 + a;
+      const int Yr = 2 * ym - 1 + a + halo;
       if (Yr < 0 || Yr >= H) continue;
       const float* row = gb + (long long)Yr * W * C + c * VEC;
       float r[VEC];
@@ -122,7 +128,7 @@ __global__ void __launch_bounds__(256) nhwc_up_bwd_kernel(const float* __restric
       for (int j = 0; j < VEC; ++j) r[j] = 0.0f;
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
-        const int Xc = 2 * xm - 1 + e;
+        const int Xc = 2 * xm - 1 + e + halo;
         if (Xc < 0 || Xc >= W) continue;
         float tv[VEC];
         ldv<VEC>(row + Xc * C, tv);
@@ -402,29 +408,32 @@ extern "C" {
 
 int svbrdf_gen_nhwc_partial_floats(int b, int c) { return b * gen_nhwc::kMaxChunks * c; }
 
-int svbrdf_gen_upsample2_nhwc(const float* x, const float* s, float* y, int b, int h, int w, int c, void* stream) {
+int svbrdf_gen_upsample2_nhwc(const float* x, const float* s, float* y, int b, int h, int w, int c, int halo,
+                              void* stream) {
   if (!x || !y || b < 1 || h < 1 || w < 1 || c < 1) return fail(SVBRDF_ERR_INVALID, "upsample2_nhwc: bad arguments");
-  if ((long long)b * 2 * h > 65535 || 2LL * w * c > (1LL << 30))
+  if (halo != 0 && halo != 1) return fail(SVBRDF_ERR_INVALID, "upsample2_nhwc: halo must be 0 or 1 (got %d)", halo);
+  if ((long long)b * (2 * h + 2 * halo) > 65535 || (2LL * w + 2 * halo) * c > (1LL << 30))
     return fail(SVBRDF_ERR_UNSUPPORTED, "upsample2_nhwc: too large");
   const bool v4 = c % 4 == 0 && a16(x) && a16(y) && a16(s);
-  const int row = 2 * w * (v4 ? c / 4 : c);
-  dim3 grid((unsigned)((row + 255) / 256), (unsigned)(b * 2 * h));
+  const int row = (2 * w + 2 * halo) * (v4 ? c / 4 : c);
+  dim3 grid((unsigned)((row + 255) / 256), (unsigned)(b * (2 * h + 2 * halo)));
   cudaStream_t st = (cudaStream_t)stream;
-  if (v4) gen_nhwc::nhwc_up_fwd_kernel<4><<<grid, 256, 0, st>>>(x, s, y, h, w, c);
-  else gen_nhwc::nhwc_up_fwd_kernel<1><<<grid, 256, 0, st>>>(x, s, y, h, w, c);
+  if (v4) gen_nhwc::nhwc_up_fwd_kernel<4><<<grid, 256, 0, st>>>(x, s, y, h, w, c, halo);
+  else gen_nhwc::nhwc_up_fwd_kernel<1><<<grid, 256, 0, st>>>(x, s, y, h, w, c, halo);
   return check_launch("nhwc_up_fwd_kernel");
 }
 
-int svbrdf_gen_upsample2_nhwc_bwd(const float* g, float* gx, int b, int h, int w, int c, void* stream) {
+int svbrdf_gen_upsample2_nhwc_bwd(const float* g, float* gx, int b, int h, int w, int c, int halo, void* stream) {
   if (!g || !gx || b < 1 || h < 1 || w < 1 || c < 1) return fail(SVBRDF_ERR_INVALID, "upsample2_nhwc_bwd: bad arguments");
+  if (halo != 0 && halo != 1) return fail(SVBRDF_ERR_INVALID, "upsample2_nhwc_bwd: halo must be 0 or 1 (got %d)", halo);
   if ((long long)b * h > 65535 || (long long)w * c > (1LL << 30))
     return fail(SVBRDF_ERR_UNSUPPORTED, "upsample2_nhwc_bwd: too large");
   const bool v4 = c % 4 == 0 && a16(g) && a16(gx);
   const int row = w * (v4 ? c / 4 : c);
   dim3 grid((unsigned)((row + 255) / 256), (unsigned)(b * h));
   cudaStream_t st = (cudaStream_t)stream;
-  if (v4) gen_nhwc::nhwc_up_bwd_kernel<4><<<grid, 256, 0, st>>>(g, gx, h, w, c);
-  else gen_nhwc::nhwc_up_bwd_kernel<1><<<grid, 256, 0, st>>>(g, gx, h, w, c);
+  if (v4) gen_nhwc::nhwc_up_bwd_kernel<4><<<grid, 256, 0, st>>>(g, gx, h, w, c, halo);
+  else gen_nhwc::nhwc_up_bwd_kernel<1><<<grid, 256, 0, st>>>(g, gx, h, w, c, halo);
   return check_launch("nhwc_up_bwd_kernel");
 }
 

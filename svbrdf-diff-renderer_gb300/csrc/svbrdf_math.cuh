@@ -819,6 +819,25 @@ __device__ __forceinline__ float2 coloc_finish_pair(const float2 t9[9], const Te
   return (LOSS == kLossMSE) ? a.loss : mul2(a.loss, bc2(kLn2 * kLn2));
 }
 
+// dL/d(light power) of two co-located texels from the view-loop sums of coloc_view_pair,
+// scaled like coloc_finish_pair's gradients. The render is P_c (f1_c + DGQ F_c) W per view,
+// so dL/dP_c = f1_c sum(dL/dimg W) + F_c sum(dL/dimg W DGQ) = f1_c a.gf1_c + F_c a.gfd_c
+// (a.gf1 and a.gfd hold those sums; src/microfacet.py:117 and src/svbrdf.py:48-50).
+template <int LOSS>
+__device__ __forceinline__ void coloc_light_grad_pair(const float2 t9[9], const AccC2& a, float scale, float2 gp[3]) {
+  const float unit = (LOSS == kLossMSE) ? 1.0f : kLn2;
+  const float2 sc = bc2(scale * kInvGamma * unit);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const float2 d = pow22_2(half_up2(t9[c]));
+    const float2 sp = pow22_2(half_up2(t9[6 + c]));
+    const float2 oms = one_minus2(sp);
+    const float2 f1 = mul2(mul2(d, bc2(kInvPi)), oms);
+    const float2 F = fma2(oms, bc2(kSphgColoc), sp);
+    gp[c] = mul2(fma2(F, a.gfd[c], mul2(f1, a.gf1[c])), sc);
+  }
+}
+
 // torch.optim.Adam's update for one element (amsgrad off, no weight decay):
 //   m.lerp_(g, 1-b1); v.mul_(b2).addcmul_(g, g, 1-b2);
 //   p.addcdiv_(m, sqrt(v)/sqrt(bc2) + eps, -lr/bc1)

@@ -32,7 +32,7 @@ struct PlanHeader {
   int ring_slots;   // variants 1 and 2: shared-memory ring depth
   int general;      // 1 when some material has a view whose light is not at the camera
   int off_seq;      // int4 (tile, material, first texel, 0) per entry of `order`
-  int pad;
+  int light;        // 1 when some material's light power is learnable (MatDesc::lstate)
   long long total_bytes;
   double total_cost;
 };
@@ -42,7 +42,8 @@ struct __align__(16) MatDesc {
   float* m1;
   float* m2;
   const float* tgt;
-  const float* lpow;
+  float* lpow;
+  float* lstate;      // light power Adam state [6] (exp_avg, exp_avg_sq), or null: light fixed
   int H, W, V, view_off;
   float size, scale;  // scale = 2 / (3 V H W), the loss-gradient normaliser
   float inv_w;        // 1 / W for the row/column split of a texel index
@@ -61,7 +62,8 @@ struct AdamHyper {
 };
 
 // Workspace of a batched launch: [0] completion counter, [1] error word, then from byte
-// 256 the per-(tile, warp) partial losses.
+// 256 the per-(tile, warp) partial losses, then (plans with a learnable light) the
+// per-(tile, warp) partial light-power gradients, 3 floats each.
 constexpr int kWsCounter = 0;
 constexpr int kWsError = 1;
 constexpr size_t kWsLossOffset = 256;

@@ -135,8 +135,20 @@ def _upsample2(x):
     GPU (FP32) it is one kernel each way, in the map's layout; the torch form serves CPU
     tensors."""
     if x.is_cuda and x.dtype == torch.float32:
-        return _UpsampleNHWC.apply(x, None) if _is_nhwc(x) else _Upsample2Cuda.apply(x)
+        return _UpsampleNHWC.apply(x, None, 0) if _is_nhwc(x) else _Upsample2Cuda.apply(x)
     return _up1d(_up1d(x, -1), -2)
+
+
+def _upsample2_halo(x):
+    """``_upsample2`` with one more up-sampled sample on each side ([B, C, 2H+2, 2W+2]: the
+    samples at -1 and 2H, x[0] / 4 and x[H-1] / 4 per axis). A valid 3x3 convolution of it is
+    the reference's up-sampling convolution, a stride-2 transposed convolution followed by
+    the [1, 3, 3, 1] filter (src/higan_models/stylegan2_generator_network.py:715-729): both
+    are the same shift-invariant map of the zero-extended input, cropped alike. Computed as
+    the up-sampling of the input zero-padded by one, cropped by one."""
+    if x.is_cuda and x.dtype == torch.float32 and _is_nhwc(x):
+        return _UpsampleNHWC.apply(x, None, 1)
+    return _upsample2(Fn.pad(x, (1, 1, 1, 1)))[:, :, 1:-1, 1:-1]
 
 
 def _use_kernels(x):
@@ -162,16 +174,18 @@ class _UpsampleNHWC(torch.autograd.Function):
     gradients."""
 
     @staticmethod
-    def forward(ctx, x, s):
+    def forward(ctx, x, s, halo=0):
         from . import _native as N
 
         x = _cl(x)
         s = s.contiguous() if s is not None else None
         b, c, h, w = x.shape
-        y = torch.empty(b, c, 2 * h, 2 * w, device=x.device, dtype=torch.float32, memory_format=CL)
+        y = torch.empty(b, c, 2 * h + 2 * halo, 2 * w + 2 * halo, device=x.device, dtype=torch.float32,
+                        memory_format=CL)
         N.check(N.lib().svbrdf_gen_upsample2_nhwc(x.data_ptr(), s.data_ptr() if s is not None else None, y.data_ptr(),
-                                                  b, h, w, c, N.stream_handle(x.device)))
+                                                  b, h, w, c, halo, N.stream_handle(x.device)))
         ctx.save_for_backward(x, s)
+        ctx.halo = halo
         return y
 
     @staticmethod
@@ -183,15 +197,15 @@ class _UpsampleNHWC(torch.autograd.Function):
         L, st = N.lib(), N.stream_handle(x.device)
         g = _cl(g)
         gu = torch.empty_like(x)
-        N.check(L.svbrdf_gen_upsample2_nhwc_bwd(g.data_ptr(), gu.data_ptr(), b, h, w, c, st))
+        N.check(L.svbrdf_gen_upsample2_nhwc_bwd(g.data_ptr(), gu.data_ptr(), b, h, w, c, ctx.halo, st))
         if s is None:
-            return gu, None
+            return gu, None, None
         gx = torch.empty_like(x)
         gs = torch.empty(b, c, device=x.device, dtype=torch.float32)
         part = torch.empty(L.svbrdf_gen_nhwc_partial_floats(b, c), device=x.device, dtype=torch.float32)
         N.check(L.svbrdf_gen_scale_nhwc_bwd(gu.data_ptr(), x.data_ptr(), s.data_ptr(), gx.data_ptr(), gs.data_ptr(),
                                             part.data_ptr(), b, h * w, c, st))
-        return gx, gs
+        return gx, gs, None
 
 
 class _ScaleNHWC(torch.autograd.Function):
@@ -334,39 +348,6 @@ class _ActCuda(torch.autograd.Function):
         return gy, gd, gn, None, None, None
 
 
-class _UpScaleCuda(torch.autograd.Function):
-    """2x up-sampling of x[b, c] * s[b, c] in one kernel (svbrdf_gen_upsample2_scaled); the
-    backward is the up-sampling adjoint followed by svbrdf_gen_scale_bwd."""
-
-    @staticmethod
-    def forward(ctx, x, s):
-        from . import _native as N
-
-        x, s = x.contiguous(), s.contiguous()
-        b, c, h, w = x.shape
-        y = torch.empty(b, c, 2 * h, 2 * w, device=x.device, dtype=torch.float32)
-        N.check(N.lib().svbrdf_gen_upsample2_scaled(x.data_ptr(), s.data_ptr(), y.data_ptr(), b * c, h, w,
-                                                    N.stream_handle(x.device)))
-        ctx.save_for_backward(x, s)
-        return y
-
-    @staticmethod
-    def backward(ctx, g):
-        from . import _native as N
-
-        x, s = ctx.saved_tensors
-        b, c, h, w = x.shape
-        L, st = N.lib(), N.stream_handle(x.device)
-        g = g.contiguous()
-        gu = torch.empty_like(x)
-        N.check(L.svbrdf_gen_upsample2_bwd(g.data_ptr(), gu.data_ptr(), b * c, h, w, st))
-        gx = torch.empty_like(x)
-        gs = torch.empty(b, c, device=x.device, dtype=torch.float32)
-        N.check(L.svbrdf_gen_scale_bwd(gu.data_ptr(), x.data_ptr(), s.data_ptr(), gx.data_ptr(), gs.data_ptr(),
-                                       b * c, h * w, st))
-        return gx, gs
-
-
 class _ModConv(torch.nn.Module):
     """Modulated (and optionally demodulated) conv, optionally 2x up-sampling first."""
 
@@ -393,17 +374,17 @@ class _ModConv(torch.nn.Module):
         d [B, cout] (None without demodulation) still to be applied to its output."""
         s = self.affine(w)  # [B, cin]
         wsc = self.weight * self.scale
+        # an up-sampling layer convolves the up-sampled map with its one-sample halo, unpadded
+        # (_upsample2_halo): the reference's transposed convolution + filter on the border too
         if _use_kernels(x) and _is_nhwc(x):
             # channels-last: the layout cuDNN's convolutions run in, so none converts its operands
-            x = _UpsampleNHWC.apply(x, s) if self.up else _ScaleNHWC.apply(x, s)
+            x = _UpsampleNHWC.apply(x, s, 1) if self.up else _ScaleNHWC.apply(x, s)
             wsc = _cl(wsc)
-        elif self.up and _use_kernels(x) and x.shape[-1] % 4 == 0 and x.data_ptr() % 16 == 0:
-            x = _UpScaleCuda.apply(x, s)  # the up-sampling commutes with the channel scaling
         else:
             x = _ScaleCuda.apply(x, s) if _use_kernels(x) else x * s[:, :, None, None]
             if self.up:
-                x = _upsample2(x)  # per-channel linear: commutes with the channel scaling
-        y = Fn.conv2d(x, wsc, padding=self.k // 2)
+                x = _upsample2_halo(x)  # per-channel linear: commutes with the channel scaling
+        y = Fn.conv2d(x, wsc, padding=0 if self.up else self.k // 2)
         d = None
         if self.demod:
             w2 = wsc.pow(2).sum(dim=(2, 3))  # [cout, cin]
@@ -479,8 +460,65 @@ class StyleGAN2Generator(torch.nn.Module):
             x = layer(x)
         return x
 
-    def truncate(self, w: torch.Tensor, psi: float = 0.7) -> torch.Tensor:
-        return self.w_avg + psi * (w - self.w_avg)
+    def truncate(self, w: torch.Tensor, psi: float = 1.0) -> torch.Tensor:
+        """w_avg + psi (w - w_avg); MaterialGAN builds its generator with psi 1
+        (src/higan_models/stylegan2_generator.py:32), the default here."""
+        return self.w_avg + (w - self.w_avg) * psi
+
+    @torch.no_grad()
+    def load_reference_state_dict(self, sd: dict):
+        """Load the weights of the reference's ``StyleGAN2GeneratorNet`` (its ``state_dict``, e.g.
+        MaterialGAN's ``ckp/materialgan.pth``; src/higan_models/stylegan2_generator_network.py:36,
+        base_generator.py:129-135) into this generator. Key by key:
+
+        * ``mapping.dense{i}.fc.weight`` / ``.bias`` -> ``mapping[i]`` (both scale by lr 0.01 and
+          1/sqrt(512) at run time, stylegan2_generator_network.py:762-824);
+        * ``synthesis.early_layer.const`` -> ``const``;
+        * ``synthesis.layer0`` -> ``conv4``; ``layer{2b-1}`` (2x up-sampling) -> ``ups[b-1]``,
+          ``layer{2b}`` -> ``convs[b-1]``; ``output0`` -> ``rgb4``, ``output{b}`` -> ``rgbs[b-1]``.
+          Conv weights are stored [k, k, in, out] and become [out, in, k, k]; the style layer's
+          constant bias 1 (``init_bias``) moves into the affine bias; ``noise_strength`` and
+          ``bias`` copy over;
+        * ``truncation.w_avg`` -> ``w_avg``.
+
+        The reference's up-sampling layer (a stride-2 transposed convolution with the flipped
+        kernel, then the [1, 3, 3, 1] filter) is the same linear map as this generator's
+        (zero insertion and the filter, then the 3x3 convolution), so the weights carry over
+        unchanged."""
+        def src(k):
+            if k not in sd:
+                raise KeyError(f"reference state dict has no {k!r}")
+            return torch.as_tensor(sd[k])
+
+        for i, layer in enumerate(self.mapping):
+            layer.weight.copy_(src(f"mapping.dense{i}.fc.weight"))
+            layer.bias.copy_(src(f"mapping.dense{i}.bias"))
+        self.const.copy_(src("synthesis.early_layer.const"))
+        if "truncation.w_avg" in sd:
+            self.w_avg.copy_(src("truncation.w_avg"))
+
+        def modconv(dst, key):
+            dst.weight.copy_(src(f"{key}.weight").permute(3, 2, 0, 1))
+            dst.affine.weight.copy_(src(f"{key}.style.fc.weight"))
+            # the style DenseBlock adds a constant init_bias of 1 (stylegan2_generator_network.py:661)
+            dst.affine.bias.copy_(src(f"{key}.style.bias") + 1.0)
+
+        def style(dst, key):
+            modconv(dst.conv, key)
+            dst.bias.copy_(src(f"{key}.bias"))
+            dst.noise_strength.copy_(src(f"{key}.noise_strength").reshape(()))
+
+        def rgb(dst, key):
+            modconv(dst.conv, key)
+            dst.bias.copy_(src(f"{key}.bias"))
+
+        style(self.conv4, "synthesis.layer0")
+        rgb(self.rgb4, "synthesis.output0")
+        for b, (up, conv, out) in enumerate(zip(self.ups, self.convs, self.rgbs), start=1):
+            style(up, f"synthesis.layer{2 * b - 1}")
+            style(conv, f"synthesis.layer{2 * b}")
+            rgb(out, f"synthesis.output{b}")
+        return self
 
     def make_noises(self, mode: str = "zero", batch: int = 1, device=None, seed: int = 0) -> List[torch.Tensor]:
         """One noise map per style layer ([batch, 1, r, r]); 'zero' like the reference's "avg"."""

@@ -4,11 +4,17 @@ Same interface as the reference class: ``SvbrdfOptim(device, renderer_obj)``,
 ``init_from_tex``, ``init_from_const``, ``init_from_randn``, ``load_targets`` and
 ``optim(epochs, lr, svbrdf_obj, optim_light)``.
 
-``optim`` runs ``svbrdf_fused_step`` once per epoch: render of clamp(textures, -1, 1),
-image loss, hand-written adjoint and Adam(lr, betas=(0.9, 0.999)) in a single pass per
-texel (the loop body of src/svbrdf.py:56-71). The per-epoch losses stay on the device
-and are read once at the end (the reference reads them every epoch, src/svbrdf.py:64-66).
-With ``graph=True`` the whole epoch loop is captured once into a CUDA graph and replayed.
+``optim`` runs the loop body of src/svbrdf.py:56-71 (render of clamp(textures, -1, 1),
+image loss, hand-written adjoint and Adam(lr, betas=(0.9, 0.999))) as one fused pass per
+texel. By default (``kernel="batched"``) the material is a one-material plan of the batched
+persistent kernels: the resident-state kernel runs up to 32 epochs per launch on state held
+in shared memory, or, with ``optim_light``, the texel-pair kernels run one launch per epoch
+with the light-power gradient reduced on the device. ``kernel="single"`` runs the
+single-material kernel ``svbrdf_fused_step`` once per epoch instead (it also serves shapes
+the batched kernels do not take: H*W not a multiple of 4). The per-epoch losses stay on the
+device and are read once at the end (the reference reads them every epoch,
+src/svbrdf.py:64-66). With ``graph=True`` the whole epoch loop is captured once into a CUDA
+graph and replayed.
 
 Setting ``fused=False`` gives the plain, unfused GPU form instead: the reference's own loop
 (``eval`` -> loss -> ``backward`` -> ``torch.optim.Adam.step``) with the forward and
@@ -28,7 +34,7 @@ LOSS_KINDS = {"mse": 0, "log1p": 1, "log1p_pre": 2}
 
 class SvbrdfOptim:
     def __init__(self, device, renderer_obj, loss="mse", fused=True, graph=False, save_process=False,
-                 descriptor=None, descriptor_weight=0.1):
+                 descriptor=None, descriptor_weight=0.1, kernel="batched"):
         self.device = torch.device(device)
         # optional descriptor (VGG-feature) term, e.g. descriptor.VGGDescriptor; like the
         # reference's loss + 0.1 * VGG loss (src/materialgan.py:139-146) it needs the renders,
@@ -44,6 +50,9 @@ class SvbrdfOptim:
             raise ValueError("loss must be 'mse' or 'log1p'")
         self.loss = loss
         self.fused = fused
+        if kernel not in ("batched", "single"):
+            raise ValueError("kernel must be 'batched' or 'single'")
+        self.kernel = kernel
         self.graph = graph
         self.save_process = save_process
         self.loss_image_list = []
@@ -177,6 +186,70 @@ class SvbrdfOptim:
         self.exp_avg, self.exp_avg_sq = st.get("exp_avg"), st.get("exp_avg_sq")
 
     def _optim_fused(self, epochs, lr, svbrdf_obj, optim_light):
+        tex = self.textures.detach()
+        if self.kernel == "batched" and tex.shape[2] * tex.shape[3] % 4 == 0 and tex.data_ptr() % 16 == 0:
+            return self._optim_batched(epochs, lr, svbrdf_obj, optim_light)
+        return self._optim_single(epochs, lr, svbrdf_obj, optim_light)
+
+    def _optim_batched(self, epochs, lr, svbrdf_obj, optim_light):
+        """The epoch loop as a one-material plan of the batched persistent kernels."""
+        from .batched import BatchedOptim, CANDIDATES
+        from .scenes import Scene
+
+        r = self.renderer_obj
+        tex = self.textures.detach()  # same storage: the kernels update the leaf in place
+        _, _, H, W = tex.shape
+        lp = self._light_tensor(svbrdf_obj)
+        sc = Scene(res=H, size=float(r.size), camera_pos=r._cam, light_pos=r._lit,
+                   light_pow=lp.detach().to(self.device, torch.float32), gt=None, targets=self.targets, init=tex)
+        n = max(epochs, 1)
+        # A repeated call on the same maps, targets and settings reuses the previous call's plan,
+        # buffers and captured graph; every call still starts a fresh Adam (src/svbrdf.py:48-52).
+        key = (tex.data_ptr(), tuple(tex.shape), self.targets.data_ptr(), tuple(self.targets.shape), float(lr),
+               self.loss, bool(optim_light), n, r._cam.data_ptr(), r._lit.data_ptr(), float(r.size))
+        b = self._batched if getattr(self, "_batched_key", None) == key else None
+        if b is not None:  # the light may have changed since (update_light, or the last call's optim_light)
+            b.lpow0[0].copy_(sc.light_pow)
+            b.lpow[0].copy_(sc.light_pow)
+            b.prepare(new_targets=False)
+        else:
+            # the texel-pair kernels (the resident-state one first) suit one material; the
+            # tuner's pick is cached per shape and library build
+            cands = [c for c in CANDIDATES if c[0] in (2, 3)]
+            b = BatchedOptim([sc], lr=lr, loss=self.loss, device=self.device, hist_len=n, optim_light=optim_light,
+                             adopt_maps=True, candidates=cands)
+            self._batched, self._batched_key = b, key
+        tmp_dir = self._save_dir(svbrdf_obj)
+        if tmp_dir is None:
+            if epochs > 0:
+                if self.graph:
+                    b.run(epochs)
+                else:
+                    b._launch(b.plan_host, b.plan_dev, b.ws, b.step_dev, b.loss_hist, epochs)
+                    b.step_count += epochs
+        else:
+            # save points of src/svbrdf.py:74-83: run to each one, then save
+            done = 0
+            for e in range(epochs):
+                if (e + 1) % 100 == 0 or e == 0 or e == epochs - 1:
+                    b._launch(b.plan_host, b.plan_dev, b.ws, b.step_dev, b.loss_hist, e + 1 - done)
+                    b.step_count += e + 1 - done
+                    done = e + 1
+                    self._maybe_save(tmp_dir, e, epochs, svbrdf_obj)
+        self.exp_avg, self.exp_avg_sq = b.m1[0], b.m2[0]
+        self._step = epochs
+        self.loss_image_list = b.loss_hist[:epochs, 0].tolist()
+        b.check()
+        if optim_light:
+            lp_dev = b.lpow[0]
+            with torch.no_grad():
+                if svbrdf_obj is not None and hasattr(svbrdf_obj, "cl"):
+                    svbrdf_obj.cl[2] = lp_dev.clone().requires_grad_(True)
+                r.update_light(lp_dev.clone())
+            self.light_exp_avg, self.light_exp_avg_sq = b.lstate[0][:3].clone(), b.lstate[0][3:].clone()
+            self.light_pow = lp_dev
+
+    def _optim_single(self, epochs, lr, svbrdf_obj, optim_light):
         L = N.lib()
         r = self.renderer_obj
         tex = self.textures.detach()  # same storage: the kernel updates the leaf in place

@@ -218,3 +218,46 @@ def test_resident_state_many_views(svb, cuda, general, variant, threads):
         o = _single(svb, cuda, m, 6)
         assert rel_l2(b.tex[i], o.textures.detach()) <= 1e-6
         assert rel_l2(b.m2[i], o.exp_avg_sq) <= 1e-5
+
+
+@pytest.mark.parametrize("variant,threads,general", [(2, 480, False), (2, 480, True), (3, 480, False),
+                                                      (3, 224, True), (2, 224, False), (3, 384, False)])
+def test_batched_learnable_light_equals_single(svb, cuda, variant, threads, general):
+    """optim_light on a batch: each material's light power and maps follow the trajectory the
+    single-material kernel gives them (src/svbrdf.py:48-50, 58-59); the resident-state
+    variant runs one iteration per launch then."""
+    mats = _batch(svb, cuda, general=general)
+    for k, m in enumerate(mats):  # distinct starting powers, off the targets' 1500
+        m.light_pow = m.light_pow * (0.8 + 0.1 * k)
+    cfg = svb.BatchConfig(threads=threads, tile_texels=2 * threads, ctas=5, variant=variant)
+    b = svb.BatchedOptim(mats, lr=0.01, loss="log1p", device=cuda, config=cfg, optim_light=True, hist_len=7)
+    assert b.launches(7) == 7
+    b.run(7)
+    assert b.device_error() == 0
+    for i, m in enumerate(mats):
+        r = svb.Microfacet(m.res, m.n_views, m.size, [t.to(cuda) for t in m.cl], cuda)
+        o = svb.SvbrdfOptim(cuda, r, loss="log1p", kernel="single")
+        o.load_targets(m.targets.to(cuda))
+        o.init_from_tex(m.init.to(cuda))
+        o.optim(7, 0.01, None, True)
+        assert rel_l2(b.tex[i], o.textures.detach()) <= 1e-6
+        assert rel_l2(b.m2[i], o.exp_avg_sq) <= 1e-5
+        assert rel_l2(b.light_pow(i), o.light_pow) <= 1e-6
+        for k in range(7):
+            assert abs(float(b.loss_hist[k, i]) - o.loss_image_list[k]) <= 1e-6 * o.loss_image_list[k]
+
+
+@pytest.mark.parametrize("variant", [2, 3])
+def test_batched_learnable_light_matches_reference(svb, golden, cuda, variant):
+    """The reference's own 20-epoch trajectory with a learnable light (optim_traj_light_16)."""
+    d = golden("optim_traj_light_16.npz")
+    sc = svb.scenes.Scene(res=d["init"].shape[-1], size=float(d["size"]), camera_pos=d["camera_pos"],
+                          light_pos=d["light_pos"], light_pow=d["light_pow0"], gt=None, targets=d["targets"],
+                          init=d["init"])
+    b = svb.BatchedOptim([sc], lr=float(d["lr"]), loss="mse", device=cuda, optim_light=True,
+                         config=svb.BatchConfig(480, 960, 0, variant), hist_len=int(d["epochs"]))
+    b.run(int(d["epochs"]))
+    assert rel_l2(b.tex[0], d["textures"]) <= 2e-5
+    assert rel_l2(b.light_pow(0), d["light_pow"]) <= 1e-6
+    ref = d["loss"].tolist()
+    assert max(abs(float(b.loss_hist[k, 0]) - ref[k]) / ref[k] for k in range(len(ref))) <= 1e-5

@@ -1,8 +1,9 @@
-"""Fused render+adjoint+Adam (svbrdf_fused_step) against the reference's own optimiser
-trajectories (tests/golden, made by running src/svbrdf.py:SvbrdfOptim.optim) and the
-FP64 oracle loop. The reference's FP32 trajectory is 1.5e-6 (relative L2) from FP64 on
-these scenes; the kernels are held to 2e-5 on textures, 1e-4 on the Adam moments and
-1e-5 (relative) on every per-epoch loss."""
+"""Fused render+adjoint+Adam against the reference's own optimiser trajectories
+(tests/golden, made by running src/svbrdf.py:SvbrdfOptim.optim) and the FP64 oracle loop,
+through both drop-in kernels: the one-material batched plan (the default) and the
+single-material kernel svbrdf_fused_step. The reference's FP32 trajectory is 1.5e-6
+(relative L2) from FP64 on these scenes; the kernels are held to 2e-5 on textures, 1e-4 on
+the Adam moments and 1e-5 (relative) on every per-epoch loss."""
 import pytest
 import torch
 
@@ -16,11 +17,11 @@ class _Obj:
         self.cl = cl
 
 
-def _run(svb, d, cuda, light, fused=True, graph=False, loss="mse"):
+def _run(svb, d, cuda, light, fused=True, graph=False, loss="mse", kernel="batched"):
     cl = [d["camera_pos"].to(cuda), d["light_pos"].to(cuda), d["light_pow0"].to(cuda)]
     res = d["init"].shape[-1]
     r = svb.Microfacet(res, cl[0].shape[0], float(d["size"]), cl, cuda)
-    o = svb.SvbrdfOptim(cuda, r, loss=loss, fused=fused, graph=graph)
+    o = svb.SvbrdfOptim(cuda, r, loss=loss, fused=fused, graph=graph, kernel=kernel)
     o.load_targets(d["targets"].to(cuda))
     o.init_from_tex(d["init"].to(cuda))
     obj = _Obj(cl)
@@ -28,10 +29,11 @@ def _run(svb, d, cuda, light, fused=True, graph=False, loss="mse"):
     return o, obj
 
 
+@pytest.mark.parametrize("kernel", ["batched", "single"])
 @pytest.mark.parametrize("name,light", [("optim_traj_16.npz", False), ("optim_traj_light_16.npz", True)])
-def test_fused_matches_reference_trajectory(svb, golden, cuda, name, light):
+def test_fused_matches_reference_trajectory(svb, golden, cuda, name, light, kernel):
     d = golden(name)
-    o, obj = _run(svb, d, cuda, light)
+    o, obj = _run(svb, d, cuda, light, kernel=kernel)
     assert rel_l2(o.textures.detach(), d["textures"]) <= 2e-5
     assert rel_l2(o.exp_avg, d["exp_avg"]) <= 1e-4
     assert rel_l2(o.exp_avg_sq, d["exp_avg_sq"]) <= 1e-4
@@ -50,10 +52,11 @@ def test_plain_unfused_form_matches_reference(svb, golden, cuda, name, light):
     assert max(abs(a - b) / b for a, b in zip(o.loss_image_list, d["loss"].tolist())) <= 1e-5
 
 
-def test_graph_replay_is_bitwise_eager(svb, golden, cuda):
+@pytest.mark.parametrize("kernel", ["batched", "single"])
+def test_graph_replay_is_bitwise_eager(svb, golden, cuda, kernel):
     d = golden("optim_traj_16.npz")
-    a, _ = _run(svb, d, cuda, False, graph=False)
-    b, _ = _run(svb, d, cuda, False, graph=True)
+    a, _ = _run(svb, d, cuda, False, graph=False, kernel=kernel)
+    b, _ = _run(svb, d, cuda, False, graph=True, kernel=kernel)
     assert torch.equal(a.textures.detach(), b.textures.detach())
     assert torch.equal(a.exp_avg_sq, b.exp_avg_sq)
     assert a.loss_image_list == b.loss_image_list
@@ -91,3 +94,22 @@ def test_out_of_range_parameters_still_move(svb, cuda):
     o.optim(5, 0.01, None, False)
     assert rel_l2(o.textures.detach(), ref["textures"]) <= 2e-5
     assert torch.equal(o.textures.detach()[0, :, 0:3, :].cpu(), init[0, :, 0:3, :])
+
+
+@pytest.mark.parametrize("light", [False, True])
+def test_repeated_calls_start_fresh(svb, golden, cuda, light):
+    """A second optim call on the same maps reuses the cached plan but restarts Adam from the
+    first call's result, as two reference calls do (src/svbrdf.py:48-52)."""
+    from oracle import microfacet_ref as R
+    d = golden("optim_traj_light_16.npz")
+    o, obj = _run(svb, d, cuda, light)
+    o.optim(int(d["epochs"]), float(d["lr"]), obj, light)
+    first = R.optim_loop(d["init"], d["targets"], d["camera_pos"], d["light_pos"], d["light_pow0"], float(d["size"]),
+                         int(d["epochs"]), float(d["lr"]), "mse", light, torch.float64)
+    lp1 = first["light_pow"] if light else d["light_pow0"]
+    second = R.optim_loop(first["textures"], d["targets"], d["camera_pos"], d["light_pos"], lp1, float(d["size"]),
+                          int(d["epochs"]), float(d["lr"]), "mse", light, torch.float64)
+    assert rel_l2(o.textures.detach(), second["textures"]) <= 2e-5
+    assert max(abs(a - b) / b for a, b in zip(o.loss_image_list, second["loss"])) <= 1e-5
+    if light:
+        assert rel_l2(obj.cl[2].detach(), second["light_pow"]) <= 1e-6

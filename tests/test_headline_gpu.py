@@ -124,9 +124,9 @@ def workload(svb, cuda):
     single = []
     for mm in mats:
         r = svb.Microfacet(mm.res, mm.n_views, mm.size, mm.cl, cuda)
-        o = svb.SvbrdfOptim(cuda, r, loss="log1p", graph=True)
+        o = svb.SvbrdfOptim(cuda, r, loss="log1p", graph=True, kernel="single")
         o.load_targets(mm.targets)
-        o.init_from_tex(mm.init)
+        o.init_from_tex(mm.init.clone())  # init_from_tex aliases a device tensor, as the reference's does
         o.optim(ITERS, LR, None, False)
         single.append(o.loss_image_list)
     return {"mats": mats, "idxs": idxs, "o64": o64, "o32": o32, "small": small, "whole": whole,

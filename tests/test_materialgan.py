@@ -253,3 +253,81 @@ def test_generator_channels_last_matches_nchw(svb, cuda):
     assert rel_l2(g1, g0) < 1e-4
     for a, b in zip(n1, n0):
         assert rel_l2(a, b) < 1e-4
+
+
+def _reference_generator(svb, device="cpu", dtype=torch.float64):
+    """Our generator carrying the weights of tests/golden/generator_ref_256.npz (drawn from
+    numpy, loaded through load_reference_state_dict), plus the fixture and its inputs."""
+    import importlib
+    import sys
+
+    import numpy as np
+
+    from conftest import GOLDEN
+    if str(GOLDEN) not in sys.path:
+        sys.path.insert(0, str(GOLDEN))
+    MG = importlib.import_module("make_golden_nets")
+    d = dict(np.load(GOLDEN / "generator_ref_256.npz"))
+    vals = MG.generator_state(MG.fixture_key_shapes(d["keys"], d["key_shapes"]), int(d["seed_weights"]))
+    gen = svb.materialgan.StyleGAN2Generator(256, out_channels=9, seed=0, channels_last=True).to(device, dtype)
+    gen.load_reference_state_dict({k: torch.from_numpy(v) for k, v in vals.items()})
+    wp, noises, R, z = MG.generator_inputs(seed=int(d["seed_inputs"]))
+    return gen, d, wp, noises, R, z
+
+
+def test_generator_matches_reference_network(svb):
+    """Pinned to the reference's own StyleGAN2GeneratorNet (src/higan_models/
+    stylegan2_generator_network.py:36) as MaterialGAN builds it, run in FP64 on numpy-drawn
+    weights (tests/golden/generator_ref_256.npz): synthesis(W+) output, its gradient with
+    respect to W+ and the 13 noise maps, and the mapping network, all within 1e-9. This ties
+    channel counts, W+ indices, noise order, the up-sampling convolutions, toRGB skips and the
+    style/demodulation arithmetic to the reference."""
+    gen, d, wp_np, noises_np, R_np, z_np = _reference_generator(svb)
+    wp = torch.from_numpy(wp_np).requires_grad_(True)
+    noises = [torch.from_numpy(n).requires_grad_(True) for n in noises_np]
+    out = gen.synthesis(wp, noises)
+    loss = (out * torch.from_numpy(R_np)).sum()
+    loss.backward()
+    o = out.detach().reshape(-1)
+    assert abs(float(loss.detach()) - float(d["loss"])) <= 1e-9 * abs(float(d["loss"]))
+    assert torch.allclose(o[torch.from_numpy(d["out_idx"])], torch.from_numpy(d["out_val"]), rtol=1e-9, atol=1e-12)
+    on = out.detach().pow(2).sum((0, 2, 3)).sqrt()
+    assert torch.allclose(on, torch.from_numpy(d["out_norm"]), rtol=1e-10)
+    assert rel_l2(wp.grad, torch.from_numpy(d["grad_wp"])) <= 1e-9
+    for i, n in enumerate(noises):
+        g = n.grad.reshape(-1)
+        assert abs(float(g.norm()) - float(d[f"noise{i}_norm"])) <= 1e-9 * float(d[f"noise{i}_norm"])
+        assert torch.allclose(g[torch.from_numpy(d[f"noise{i}_idx"])], torch.from_numpy(d[f"noise{i}_val"]),
+                              rtol=1e-8, atol=1e-10)
+    with torch.no_grad():
+        w = gen.truncate(gen.map(torch.from_numpy(z_np)))
+    assert rel_l2(w[0], torch.from_numpy(d["w_mapped"])) <= 1e-12
+
+
+@pytest.mark.gpu
+def test_gpu_generator_matches_reference_network(svb, cuda):
+    """The GPU generator (channels-last maps, the NHWC kernels with the up-sampling halo,
+    cuDNN convolutions in FP32 with TF32 off) on the reference network's fixture
+    (tests/golden/generator_ref_256.npz): output, W+ gradient and noise gradients within
+    FP32 accuracy of the reference's FP64 run."""
+    gen, d, wp_np, noises_np, R_np, _ = _reference_generator(svb, cuda, torch.float32)
+    for p in gen.parameters():
+        p.requires_grad_(False)
+    torch.backends.cudnn.allow_tf32 = False
+    try:
+        wp = torch.from_numpy(wp_np).float().to(cuda).requires_grad_(True)
+        noises = [torch.from_numpy(n).float().to(cuda).requires_grad_(True) for n in noises_np]
+        out = gen.synthesis(wp, noises)
+        loss = (out * torch.from_numpy(R_np).float().to(cuda)).sum()
+        loss.backward()
+    finally:
+        torch.backends.cudnn.allow_tf32 = True
+    o = out.detach().double().cpu()
+    assert abs(float(loss.detach()) - float(d["loss"])) <= 1e-4 * abs(float(d["loss"]))
+    ov = o.reshape(-1)[torch.from_numpy(d["out_idx"])]
+    assert rel_l2(ov, torch.from_numpy(d["out_val"])) <= 1e-5
+    assert rel_l2(o.pow(2).sum((0, 2, 3)).sqrt(), torch.from_numpy(d["out_norm"])) <= 1e-5
+    assert rel_l2(wp.grad, torch.from_numpy(d["grad_wp"])) <= 1e-4
+    for i, n in enumerate(noises):
+        g = n.grad.reshape(-1).double().cpu()
+        assert abs(float(g.norm()) - float(d[f"noise{i}_norm"])) <= 1e-4 * float(d[f"noise{i}_norm"])

@@ -23,7 +23,7 @@ def test_exports_match_header(svb, lib):
 
 
 def test_constants(lib):
-    assert lib.svbrdf_abi_version() == 3
+    assert lib.svbrdf_abi_version() == 4
     assert lib.svbrdf_max_views() >= 16
     assert lib.svbrdf_workspace_bytes() >= 16
 
@@ -250,7 +250,9 @@ def test_new_entry_points_reject_bad_arguments_on_host(svb, lib):
     assert lib.svbrdf_gen_act_bwd(fake, fake, None, None, fake, fake, 1.0, fake, None, fake, 2, 4, 64, None) == -1
     assert lib.svbrdf_gen_scale_nhwc_bwd(fake, fake, fake, fake, fake, fake, 2, 64, 2048, None) == -2
     assert lib.svbrdf_gen_act_nhwc(fake, None, fake, None, fake, 1.0, fake, 2, 64, 8, None) == -1  # noise, no strength
-    assert lib.svbrdf_gen_upsample2_nhwc(fake, None, fake, 40000, 2, 8, 8, None) == -2           # B 2h beyond a grid axis
+    assert lib.svbrdf_gen_upsample2_nhwc(fake, None, fake, 40000, 2, 8, 8, 0, None) == -2        # B 2h beyond a grid axis
+    assert lib.svbrdf_gen_upsample2_nhwc(fake, None, fake, 2, 2, 8, 8, 2, None) == -1            # halo 0 or 1
+    assert lib.svbrdf_gen_upsample2_nhwc_bwd(fake, fake, 2, 2, 8, 8, -1, None) == -1
     assert lib.svbrdf_gen_nhwc_partial_floats(3, 128) == 3 * 64 * 128
     # descriptor average pool: odd size
     assert lib.svbrdf_desc_avgpool_fwd(fake, fake, 1, 7, 8, 64, None) == -2

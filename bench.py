@@ -282,25 +282,28 @@ def impl_reference(args):
 
 
 # ---------------------------------------------------------------- GPU legs
-def time_single(dev, fused, iters, res=1024):
-    """Single material 1024^2, 9 views: plain (unfused) or fused kernel, texel*view/s."""
+def time_single(dev, fused, iters, res=1024, kernel="batched"):
+    """Single material 1024^2, 9 views, through the drop-in SvbrdfOptim: plain (unfused), or
+    fused with the default one-material batched plan (kernel="batched") or the per-epoch
+    single-material kernel (kernel="single"); texel*view/s."""
     sc = PKG.scenes.single_scene(res=res, device=dev, render_fn=gpu_render_fn(dev))
     r = PKG.Microfacet(res, 9, sc.size, sc.cl, dev)
-    o = PKG.SvbrdfOptim(dev, r, loss="log1p", fused=fused, graph=fused)
+    o = PKG.SvbrdfOptim(dev, r, loss="log1p", fused=fused, graph=fused, kernel=kernel)
     o.load_targets(sc.targets)
-    o.init_from_tex(sc.init)
-    o.optim(3, 0.01, None, False)  # warm
-    o.init_from_tex(sc.init)
-    o.exp_avg = None
+    o.init_from_tex(sc.init.clone())
+    o.optim(iters, 0.01, None, False)  # warm: the same call (plan, tuning and graph are reused after it)
+    with torch.no_grad():
+        o.textures.copy_(sc.init)  # restart from the initial maps in the same buffer
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     o.optim(iters, 0.01, None, False)
     torch.cuda.synchronize()
     el = time.perf_counter() - t0
+    form = (", forward kernel + torch loss + adjoint kernel (autograd) + torch.optim.Adam" if not fused else
+            ", one-material plan of the batched kernels in one CUDA graph" if kernel == "batched" else
+            ", single-material fused kernel, one launch per iteration, in one CUDA graph")
     return {"value": res * res * 9 * iters / el, "unit": UNIT,
-            "workload": f"1 material {res}^2, 9 views, {iters} Adam iterations, log1p L2"
-                        + (", fused kernel in one CUDA graph" if fused else
-                           ", forward kernel + torch loss + adjoint kernel (autograd) + torch.optim.Adam")}
+            "workload": f"1 material {res}^2, 9 views, {iters} Adam iterations, log1p L2" + form}
 
 
 def time_envmap(dev, res=256, spp=256, frames=5):
@@ -618,6 +621,7 @@ def impl_ours(args):
     if rank == 0 and not args.no_extras:
         line["plain"] = time_single(dev, fused=False, iters=20)
         line["fused_single"] = time_single(dev, fused=True, iters=200)
+        line["fused_single_kernel"] = time_single(dev, fused=True, iters=200, kernel="single")
         line["fused_vs_plain"] = value / line["plain"]["value"]
         line["descriptor"] = time_descriptor(dev)
         line["latent"] = time_latent(dev, iters=5)
@@ -653,7 +657,8 @@ def main():
         dev = torch.device("cuda", dist_env()[2])
         torch.cuda.nvtx.range_push("single")
         out = {"plain": time_single(dev, fused=False, iters=max(args.steps, 1)),
-               "fused_single": time_single(dev, fused=True, iters=max(args.steps, 1) * 10)}
+               "fused_single": time_single(dev, fused=True, iters=max(args.steps, 1) * 10),
+               "fused_single_kernel": time_single(dev, fused=True, iters=max(args.steps, 1) * 10, kernel="single")}
         torch.cuda.nvtx.range_pop()
         print(json.dumps(out), flush=True)
         return 0

@@ -271,6 +271,30 @@ int svbrdf_desc_avgpool_bwd(const void* gy, const void* x, const void* addend, v
 int svbrdf_desc_feat_loss(const void* f, int f_is_bf16, const float* t, const float* gram_grad, float coef, int mask,
                           void* g, float* partial, long long n, void* stream);
 
+/* ---- descriptor loss: the Gram term on the tensor cores (the reference's Gram branch
+ * G = F F^T / S, src/descriptor.py:50-56, for NHWC features F [V][S][C]) ---- */
+
+/* Split count (over the pixels) that svbrdf_desc_gram should use for v views of s pixels and
+ * c channels (0 for unsupported sizes). */
+int svbrdf_desc_gram_splits(int v, int s, int c);
+
+/* partial[v][split][c][c] = sum over split `split` of the pixels of F[v][p][i] F[v][p][j]: BF16
+ * features [v][s][c] (s % 64 == 0; c 64, 128 or a multiple of 256; 16-byte aligned), FP32
+ * partial products (tcgen05, FP32 accumulation). `err` as in svbrdf_conv3x3_bf16. */
+int svbrdf_desc_gram(const void* features, float* partial, int v, int s, int c, int splits, int* err, void* stream);
+
+/* G[v][i][j] = (sum over splits of partial, in split order) / s; with gram_target (FP32
+ * [v][c][c], nullable) d = G - target, else d = G. Writes, each when non-NULL: gram_out = G
+ * (FP32), dgram = coef d (BF16), loss_part[v][i] = sum_j d^2 (FP32, fixed order). */
+int svbrdf_desc_gram_finish(const float* partial, int splits, int v, int c, int s, const float* gram_target,
+                            float coef, float* gram_out, void* dgram, float* loss_part, void* stream);
+
+/* out[b][m][n] = sum_k A[b][m][k] B[b][n][k] (FP32), A BF16 [batch][m][k], B BF16 [batch][n][k]:
+ * m % 128 == 0, k % 64 == 0, n 64, 128 or a multiple of 256, 16-byte aligned. For the Gram term's
+ * gradient dF = F dG (dG symmetric, so B = dG). */
+int svbrdf_desc_gemm_nt(const void* a, const void* b, float* out, int batch, int m, int n, int k, int* err,
+                        void* stream);
+
 /* ---- MaterialGAN generator: 2x up-sampling of its feature maps and skip images (the
  * reference's generator, src/higan_models/*, up-samples by zero insertion and a [1,3,3,1]
  * FIR; src/materialgan.py:91-173 runs it in the latent loop) ---- */

@@ -34,7 +34,17 @@ REF_LAYERS = LAYERS + [("conv4_2", 512, 512)]
 REF_HOOKS = ("conv1_1", "conv1_2", "conv3_2", "conv4_2")
 
 
-def features(renders, weights, downsample=True, mode="config"):
+def _bf16(x):
+    """x rounded to BF16 (nearest even) in the forward pass, the identity in the backward."""
+    return x + (x.to(torch.bfloat16).to(x.dtype) - x).detach()
+
+
+def features(renders, weights, downsample=True, mode="config", bf16=False, gram_inputs=None):
+    """Hooked ReLU outputs. With ``bf16`` every convolution's output is rounded to BF16 after
+    its ReLU (straight through in the backward pass), as the tensor-core stack stores its
+    activations, except the relu1_1 hook itself, which that stack keeps in FP32 for the feature
+    term while feeding the rounded copy on; ``gram_inputs`` (a list) then receives the features
+    the Gram term reads (the rounded copies)."""
     ref = mode == "reference"
     layers, hooks = (REF_LAYERS, REF_HOOKS) if ref else (LAYERS, HOOKS)
     x = renders.double()
@@ -50,9 +60,12 @@ def features(renders, weights, downsample=True, mode="config"):
             continue
         name = item[0]
         w, b = weights[name]
-        x = torch.relu(torch.nn.functional.conv2d(x, w.double(), b.double(), padding=1))
+        y = torch.relu(torch.nn.functional.conv2d(x, w.double(), b.double(), padding=1))
+        x = _bf16(y) if bf16 else y
         if name in hooks:
-            out.append(x)
+            out.append(y if (bf16 and name == "conv1_1") else x)
+            if gram_inputs is not None:
+                gram_inputs.append(x)
     return out
 
 
@@ -77,26 +90,33 @@ def gram(f):
     return torch.bmm(ff, ff.transpose(1, 2)) / (h * w)
 
 
-def loss_terms(renders, targets, weights, hook_weights=(0.25, 0.25, 0.25, 0.25), downsample=None, mode="config"):
+def loss_terms(renders, targets, weights, hook_weights=(0.25, 0.25, 0.25, 0.25), downsample=None, mode="config",
+               bf16=False, views_total=None):
     """(feature_loss, gram_loss, d(feature+gram)/d renders) in FP64. In reference mode the
-    Gram loss is 0 and the renders are not downsampled."""
+    Gram loss is 0 and the renders are not downsampled. ``bf16`` rounds the activations as the
+    tensor-core stack does (see ``features``). Both terms are sums over the views, so a subset
+    of the views of a larger batch gives that batch's per-view terms: ``views_total`` is the
+    batch's view count, whose element counts normalise the means."""
     ref = mode == "reference"
     downsample = (not ref) if downsample is None else downsample
     r = renders.detach().double().clone().requires_grad_(True)
     with torch.no_grad():
-        tf = features(targets, weights, downsample, mode)
-        tg = [gram(f) for f in tf]
-    feats = features(r, weights, downsample, mode)
+        tgi = []
+        tf = features(targets, weights, downsample, mode, bf16, tgi)
+        tg = [gram(f) for f in (tgi if bf16 else tf)]
+    gi = []
+    feats = features(r, weights, downsample, mode, bf16, gi)
+    scale = (views_total / renders.shape[0]) if views_total else 1.0
     fl, gl, nf, ng = 0.0, 0.0, 0, 0
-    for w, f, t, g_t in zip(hook_weights, feats, tf, tg):
+    for k, (w, f, t, g_t) in enumerate(zip(hook_weights, feats, tf, tg)):
         # the reference's MSE of the concatenated weighted features (src/descriptor.py:39-60)
         fl = fl + (w * w) * ((f - t) ** 2).sum()
         nf += f.numel()
         if not ref:
-            g = gram(f)
+            g = gram(gi[k] if bf16 else f)
             gl = gl + (w * w) * ((g - g_t) ** 2).sum()
             ng += g.numel()
-    fl = fl / nf
-    gl = gl / ng if not ref else torch.zeros((), dtype=torch.float64)
+    fl = fl / (nf * scale)
+    gl = gl / (ng * scale) if not ref else torch.zeros((), dtype=torch.float64)
     (fl + gl).backward()
     return float(fl.detach()), float(gl.detach()), r.grad.detach()

@@ -20,8 +20,9 @@ CSRC = PKG / "csrc"
 INCLUDE = REPO / "include"
 LIBDIR = PKG / "_lib"
 LIBNAME = "libsvbrdf_gb300.so"
-SOURCES = ["render.cu", "fused.cu", "conv_tc.cu", "desc_ops.cu", "gen_ops.cu", "gen_nhwc.cu", "envmap.cu"]
-HEADERS = ["svbrdf_math.cuh", "svbrdf_common.cuh", "svbrdf_plan.cuh"]
+SOURCES = ["render.cu", "fused.cu", "conv_tc.cu", "gram_tc.cu", "desc_ops.cu", "gen_ops.cu", "gen_nhwc.cu",
+           "envmap.cu"]
+HEADERS = ["svbrdf_math.cuh", "svbrdf_common.cuh", "svbrdf_plan.cuh", "tc_ptx.cuh"]
 WORKSPACE_ERROR_OFFSET = 4
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
@@ -141,6 +142,14 @@ def _declare(L):
     L.svbrdf_desc_avgpool_bwd.argtypes = [P, P, P, P, I, I, I, I, P]
     L.svbrdf_desc_feat_loss.restype = I
     L.svbrdf_desc_feat_loss.argtypes = [P, I, P, P, F, I, P, P, ctypes.c_longlong, P]
+    L.svbrdf_desc_gram_splits.restype = I
+    L.svbrdf_desc_gram_splits.argtypes = [I, I, I]
+    L.svbrdf_desc_gram.restype = I
+    L.svbrdf_desc_gram.argtypes = [P, P, I, I, I, I, P, P]
+    L.svbrdf_desc_gram_finish.restype = I
+    L.svbrdf_desc_gram_finish.argtypes = [P, I, I, I, I, P, F, P, P, P, P]
+    L.svbrdf_desc_gemm_nt.restype = I
+    L.svbrdf_desc_gemm_nt.argtypes = [P, P, P, I, I, I, I, P, P]
     L.svbrdf_gen_upsample2.restype = I
     L.svbrdf_gen_upsample2.argtypes = [P, P, ctypes.c_longlong, I, I, P]
     L.svbrdf_gen_upsample2_scaled.restype = I
@@ -194,7 +203,8 @@ EXPORTS = [
     "svbrdf_batched_plan", "svbrdf_batched_workspace_bytes", "svbrdf_batched_step", "svbrdf_batched_steps", "svbrdf_conv3x3_bf16",
     "svbrdf_conv3x3_bf16_ex", "svbrdf_desc_partials", "svbrdf_desc_conv1_fwd", "svbrdf_desc_conv1_bwd",
     "svbrdf_desc_pool_fwd", "svbrdf_desc_pool_bwd", "svbrdf_desc_avgpool_fwd", "svbrdf_desc_avgpool_bwd",
-    "svbrdf_desc_feat_loss", "svbrdf_gen_upsample2",
+    "svbrdf_desc_feat_loss", "svbrdf_desc_gram_splits", "svbrdf_desc_gram", "svbrdf_desc_gram_finish",
+    "svbrdf_desc_gemm_nt", "svbrdf_gen_upsample2",
     "svbrdf_gen_upsample2_bwd", "svbrdf_gen_upsample2_scaled", "svbrdf_gen_scale", "svbrdf_gen_scale_bwd", "svbrdf_gen_act", "svbrdf_gen_act_bwd",
     "svbrdf_gen_nhwc_partial_floats", "svbrdf_gen_upsample2_nhwc", "svbrdf_gen_upsample2_nhwc_bwd",
     "svbrdf_gen_scale_nhwc", "svbrdf_gen_scale_nhwc_bwd", "svbrdf_gen_act_nhwc", "svbrdf_gen_act_nhwc_bwd",

@@ -23,7 +23,7 @@
 
 #include <atomic>
 
-#include "svbrdf_common.cuh"
+#include "tc_ptx.cuh"
 
 namespace svb {
 namespace tc {
@@ -32,95 +32,9 @@ constexpr int BM = 128;  // output pixels per CTA
 constexpr int TH = 8, TW = 16;
 constexpr int BK = 64;   // input channels per stage (one 128-byte swizzle row)
 constexpr int kThreads = 192;  // warp 0 TMA, warp 1 MMA + TMEM owner, warps 2..5 epilogue
-constexpr uint32_t kSpin = 1u << 22;
 
 enum Epilogue : int { kEpiNone = 0, kEpiBiasRelu = 1, kEpiMask = 2, kEpiAddMask = 3 };
 enum ConvError : int { kErrTma = 11, kErrMma = 12, kErrEpi = 13 };
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(ok)
-      : "r"(bar), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// Bounded wait; false (and `code` recorded) on timeout or when another thread failed.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* err, int code) {
-  uint32_t it = 0;
-  while (!mbar_try(bar, parity)) {
-    if (++it >= kSpin) {
-      atomicCAS(err, 0, code);
-      return false;
-    }
-    if ((it & 1023u) == 0 && *(volatile int*)err != 0) return false;
-  }
-  return true;
-}
-__device__ __forceinline__ void tma_4d(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
-                                       uint32_t bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
-      "[%6];" ::"r"(dst),
-      "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
-      : "memory");
-}
-__device__ __forceinline__ void tma_2d(uint32_t dst, const CUtensorMap* map, int c0, int c1, uint32_t bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-          dst),
-      "l"(map), "r"(c0), "r"(c1), "r"(bar)
-      : "memory");
-}
-// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 bytes apart.
-__device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
-  uint64_t d = (uint64_t)((addr & 0x3FFFFu) >> 4);  // start address
-  d |= (uint64_t)1 << 16;                             // leading byte offset (unused by this layout)
-  d |= (uint64_t)(1024 >> 4) << 32;                   // stride byte offset: next 8-row group
-  d |= (uint64_t)1 << 46;                             // descriptor version
-  d |= (uint64_t)2 << 61;                             // 128-byte swizzle
-  return d;
-}
-// Instruction descriptor, kind::f16: FP32 accumulator, BF16 A and B, both K-major.
-__host__ __device__ constexpr uint32_t idesc_bf16(int m, int n) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
-}
-__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accum) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\t"
-      "setp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem_d),
-      "l"(a), "l"(b), "r"(idesc), "r"(accum)
-      : "memory");
-}
-__device__ __forceinline__ void mma_commit(uint32_t bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
-}
-__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
-      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
-        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-}
 
 template <int BN>
 struct Shape {
@@ -302,16 +216,18 @@ conv3x3_tc_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_const
 }
 
 // ---------------------------------------------------------------- host side
-static PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
-
-static int get_encoder() {
-  if (g_encode) return SVBRDF_OK;
-  void* fn = nullptr;
-  cudaDriverEntryPointQueryResult q;
-  const cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
-  if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn)
-    return fail(SVBRDF_ERR_CUDA, "cuTensorMapEncodeTiled is not available (%s)", cudaGetErrorString(e));
-  g_encode = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+int get_tensor_map_encoder(PFN_cuTensorMapEncodeTiled_v12000* out) {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn_cached = nullptr;
+  if (!fn_cached) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    const cudaError_t e =
+        cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || !fn)
+      return fail(SVBRDF_ERR_CUDA, "cuTensorMapEncodeTiled is not available (%s)", cudaGetErrorString(e));
+    fn_cached = (PFN_cuTensorMapEncodeTiled_v12000)fn;
+  }
+  *out = fn_cached;
   return SVBRDF_OK;
 }
 
@@ -374,7 +290,8 @@ extern "C" int svbrdf_conv3x3_bf16_ex(const void* x, const void* weight, const f
   if (((uintptr_t)x | (uintptr_t)weight | (uintptr_t)y | (uintptr_t)mask | (uintptr_t)addend) % 16)
     return fail(SVBRDF_ERR_INVALID, "conv3x3: tensors must be 16-byte aligned");
   if ((long long)n * h * w * cin >= (1LL << 40)) return fail(SVBRDF_ERR_UNSUPPORTED, "conv3x3: tensor too large");
-  int rc = get_encoder();
+  PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+  int rc = get_tensor_map_encoder(&g_encode);
   if (rc) return rc;
   const int bn = (cout % 256 == 0) ? 256 : (cout % 128 == 0 ? 128 : 64);
   CUtensorMap mx, mw;

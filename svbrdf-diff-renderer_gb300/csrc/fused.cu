@@ -1319,12 +1319,13 @@ batched_fuse_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
       const bool coloc = !GEN || r0.all_coloc;
       const bool active = 2 * tid < r0.W * r0.H - r0.first;
       bool live = true;
+      // the pair's pixel centres, once per tile (they do not change across its iterations)
+      float2 px = make_float2(0.f, 0.f), py = make_float2(0.f, 0.f);
+      if (active) pair_coords(r0, tid, px, py);
       for (int it = 0; it < iters; ++it) {
         float2 g[9];
         float2 loss2;
         float2 gpl[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};  // dL/d light
-        float2 px = make_float2(0.f, 0.f), py = make_float2(0.f, 0.f);
-        if (active) pair_coords(r0, tid, px, py);
         if (coloc) {
           TexelPair u;
           {

@@ -704,8 +704,10 @@ __device__ __forceinline__ void coloc_prepare_pair(const float2 t9[9], float2 px
 // One co-located view of two texels (lanes), the camera broadcast: the arithmetic of
 // coloc_view with the light power folded into the texel constants. a.gf1 and a.gfd
 // accumulate dL/df1 and dL/dF divided by P_c; coloc_finish_pair multiplies P_c back;
-// a.gk accumulates -dL/dk. One front-facing predicate (n.v > 0) drives all three selects:
-// at n.v = 0 the view's weight W is 0, the image is clamped and every gradient term is 0.
+// a.gk accumulates -dL/dk. Back-facing views (n.v <= 0) need no selects beyond the clamp of
+// n.v itself: their weight W = max(n.v, 0) / d^2 is 0, so the image is clamped to eps, its
+// gradient is 0, and every term below is an exact 0 times a finite value (the reference's
+// 1 - c2 = 1 there, which only reaches D, which only reaches the zero-weighted image).
 // 1 - (n.v)^2 is |v - (n.v) n|^2 / |v|^2, the squared length of v's component across n:
 // no cancellation at the highlight, as with the cross product of coloc_view.
 template <int LOSS>
@@ -717,12 +719,10 @@ __device__ __forceinline__ void coloc_view_pair(const TexelPair& t, float2 cx, f
   const float2 inv_d2 = mul2(iv, iv);
   const float2 dn = fma2(t.n0, vx, fma2(t.n1, vy, mul2(t.n2, vz)));  // n.v, |v| units
   const float2 nvr = mul2(dn, iv);
-  const bool fx = nvr.x > 0.0f, fy = nvr.y > 0.0f;
-  const float2 nv = make_float2(fx ? nvr.x : 0.0f, fy ? nvr.y : 0.0f);
+  const float2 nv = make_float2(fmaxf(nvr.x, 0.0f), fmaxf(nvr.y, 0.0f));  // clamp(min=0)
   const float2 mdn = mul2(dn, bc2(-1.0f));
   const float2 r0 = fma2(t.n0, mdn, vx), r1 = fma2(t.n1, mdn, vy), r2 = fma2(t.n2, mdn, vz);
-  const float2 s2c = mul2(fma2(r0, r0, fma2(r1, r1, mul2(r2, r2))), inv_d2);
-  const float2 s2 = make_float2(fx ? s2c.x : 1.0f, fy ? s2c.y : 1.0f);
+  const float2 s2 = mul2(fma2(r0, r0, fma2(r1, r1, mul2(r2, r2))), inv_d2);
   const float2 c2 = mul2(nv, nv);
   const float2 den = fma2(c2, t.a2, s2);
   const float2 rE = rcp2(fma2(bc2(kPi), mul2(den, den), bc2(kEps)));
@@ -771,8 +771,7 @@ __device__ __forceinline__ void coloc_view_pair(const TexelPair& t, float2 cx, f
   const float2 t2 = mul2(mul2(D, rE), den);          // dD/d den = -2 pi t2
   a.ga2 = fma2(gD, fma2(t2, mul2(c2, bc2(-2.0f * kPi)), rE), a.ga2);
   gnv = fma2(mul2(mul2(gD, t2), t.K1), nv, gnv);     // d den/d nv = 2 nv (alpha^2 - 1)
-  const float2 gsv = mul2(gnv, iv);
-  const float2 gs = make_float2(fx ? gsv.x : 0.0f, fy ? gsv.y : 0.0f);
+  const float2 gs = mul2(gnv, iv);                   // 0 for back-facing views
   a.gn0 = fma2(gs, vx, a.gn0);
   a.gn1 = fma2(gs, vy, a.gn1);
   a.gn2 = fma2(gs, vz, a.gn2);

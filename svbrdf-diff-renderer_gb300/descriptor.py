@@ -31,8 +31,10 @@ them is fused into a few kernels of the same library:
 
 The backward pass is a hand-written chain, not autograd. Each data-gradient convolution's
 epilogue adds the next hook's loss gradient and applies the ReLU mask below, and the
-max-pool backward does the same. The Gram products are plain batched BF16 GEMMs (cuBLAS
-tensor cores, FP32 accumulation).
+max-pool backward does the same. The Gram products run on tcgen05 too (gram_tc.cu): G = F^T F
+straight from the NHWC feature map (MN-major operands, split over the pixels, partials summed
+in a fixed order by a finish kernel that also forms the loss rows and the BF16 dG), and the
+gradient F dG as a K-major BF16 GEMM; BF16 operands, FP32 accumulation.
 """
 from __future__ import annotations
 
@@ -71,55 +73,42 @@ def conv3x3_bf16(x: torch.Tensor, w: torch.Tensor, bias: Optional[torch.Tensor],
     return y
 
 
-_BMM_F32_OUT = {}
+def gram_bf16(f: torch.Tensor, err: torch.Tensor, target: Optional[torch.Tensor] = None, coef: float = 0.0,
+              want_dgram: bool = False):
+    """The Gram term of NHWC BF16 features f [V, H, W, C] on the tensor cores
+    (svbrdf_desc_gram + svbrdf_desc_gram_finish): G = F^T F / S per view (FP32 [V, C, C]). With
+    ``target``: (None, loss rows [V, C] = sum_j (G - target)^2, BF16 coef (G - target) if
+    ``want_dgram``); without: (G, None, None)."""
+    L = N.lib()
+    st = N.stream_handle(f.device)
+    v, h, w, c = f.shape
+    s = h * w
+    f = f.contiguous()
+    splits = L.svbrdf_desc_gram_splits(v, s, c)
+    if splits <= 0:
+        raise N.SvbrdfError(-2, f"gram: unsupported shape {tuple(f.shape)}")
+    part = torch.empty(v, splits, c, c, device=f.device, dtype=torch.float32)
+    N.check(L.svbrdf_desc_gram(f.data_ptr(), part.data_ptr(), v, s, c, splits, err.data_ptr(), st))
+    if target is None:
+        g = torch.empty(v, c, c, device=f.device, dtype=torch.float32)
+        N.check(L.svbrdf_desc_gram_finish(part.data_ptr(), splits, v, c, s, None, 0.0, g.data_ptr(), None, None, st))
+        return g, None, None
+    rows = torch.empty(v, c, device=f.device, dtype=torch.float32)
+    dg = torch.empty(v, c, c, device=f.device, dtype=torch.bfloat16) if want_dgram else None
+    N.check(L.svbrdf_desc_gram_finish(part.data_ptr(), splits, v, c, s, target.data_ptr(), float(coef), None,
+                                      N.ptr(dg), rows.data_ptr(), st))
+    return None, rows, dg
 
 
-def _bmm_f32out(a: torch.Tensor, b: torch.Tensor) -> torch.Tensor:
-    """Batched BF16 x BF16 product on the tensor cores, FP32 accumulation, FP32 result when
-    torch exposes bmm's out_dtype (checked once per device), else a BF16 result widened."""
-    key = a.device
-    if key not in _BMM_F32_OUT:
-        try:
-            z = torch.zeros(1, 2, 2, device=a.device, dtype=torch.bfloat16)
-            _BMM_F32_OUT[key] = torch.bmm(z, z, out_dtype=torch.float32).dtype == torch.float32
-        except (TypeError, RuntimeError):
-            _BMM_F32_OUT[key] = False
-    if _BMM_F32_OUT[key]:
-        return torch.bmm(a, b, out_dtype=torch.float32)
-    return torch.bmm(a, b).float()
-
-
-def _gram_f32(ff: torch.Tensor) -> torch.Tensor:
-    """F^T F for F [V, S, C] BF16, FP32 result. A long S with few channels is split into
-    chunks that form one larger batch of GEMMs, so that enough CTAs run, and the chunk
-    products are summed in FP32."""
-    v, s, c = ff.shape
-    p = 1
-    while p < 32 and s % (2 * p) == 0 and s // (2 * p) >= 2048 and c <= 128:
-        p *= 2
-    if p == 1:
-        return _bmm_f32out(ff.transpose(1, 2), ff)
-    fc = ff.reshape(v * p, s // p, c)
-    return _bmm_f32out(fc.transpose(1, 2), fc).reshape(v, p, c, c).sum(dim=1)
-
-
-class _Gram(torch.autograd.Function):
-    """G = F^T F / S for NHWC features F [V, H, W, C] (BF16); gradient F (dG + dG^T) / S."""
-
-    @staticmethod
-    def forward(ctx, f):
-        v, h, w, c = f.shape
-        ff = f.reshape(v, h * w, c).to(torch.bfloat16)
-        ctx.save_for_backward(ff)
-        ctx.shape = f.shape
-        return _gram_f32(ff) / (h * w)
-
-    @staticmethod
-    def backward(ctx, g):
-        (ff,) = ctx.saved_tensors
-        v, h, w, c = ctx.shape
-        gs = ((g + g.transpose(1, 2)) / (h * w)).to(torch.bfloat16)
-        return torch.bmm(ff, gs).reshape(v, h, w, c)
+def gemm_nt_bf16(a: torch.Tensor, b: torch.Tensor, err: torch.Tensor) -> torch.Tensor:
+    """out[b, m, n] = sum_k a[b, m, k] b[b, n, k] (BF16 operands, FP32 out) on the tensor cores."""
+    L = N.lib()
+    bt, m, k = a.shape
+    n = b.shape[1]
+    out = torch.empty(bt, m, n, device=a.device, dtype=torch.float32)
+    N.check(L.svbrdf_desc_gemm_nt(a.contiguous().data_ptr(), b.contiguous().data_ptr(), out.data_ptr(), bt, m, n, k,
+                                  err.data_ptr(), N.stream_handle(a.device)))
+    return out
 
 
 def he_normal_weights(seed: int, layers=VGG19_TO_CONV4_1):
@@ -209,13 +198,15 @@ class VGGDescriptor:
         return acts, hooks
 
     # ---- loss terms --------------------------------------------------------------------
-    def _terms(self, hooks, cf: Optional[float], cg: Optional[float]):
+    def _terms(self, hooks, cf: Optional[float], cg: Optional[float], hooks16=None):
         """Feature and Gram losses (0-d FP32 tensors). With cf/cg given, also the loss
         gradient at each hooked activation, cf d(feature)/df + cg d(gram)/df, as BF16 NHWC; the
         last layer's gradient is masked by its ReLU (it starts the backward chain)."""
         L = N.lib()
         st = N.stream_handle(self.device)
         tf, tg = self.target
+        if hooks16 is None:
+            hooks16 = {n: (f if f.dtype == torch.bfloat16 else f.to(torch.bfloat16)) for n, f in hooks.items()}
         nf = sum(f.numel() for f in hooks.values())
         ng = sum(g.numel() for g in tg)
         nparts = L.svbrdf_desc_partials()
@@ -229,15 +220,15 @@ class VGGDescriptor:
             gg = None
             g = None
             if self.gram:
-                ff = f.reshape(v, s, c).to(torch.bfloat16)
-                gram = _gram_f32(ff) / s
-                diff = gram - tg[k]
-                gram_terms.append((wt * wt) * (diff * diff).sum())
+                # the BF16 feature map (relu1_1's hook is FP32; its BF16 copy feeds conv1_2)
+                ff = hooks16[name]
+                # d/dF of w^2 sum (G - Gt)^2 / ng with G = F^T F / s: F (2 dG) / s, dG = 2 w^2 (G - Gt) / ng
+                coef_g = (4.0 * wt * wt * cg / (ng * s)) if cf is not None else 0.0
+                _, rows, dgram = gram_bf16(ff, self.err, tg[k], coef_g, want_dgram=cf is not None)
+                gram_terms.append((wt * wt) * rows.sum())
             if cf is not None:
                 if self.gram:
-                    # d/dF of w^2 sum (G - Gt)^2 / ng with G = F^T F / s: F (2 dG) / s, dG = 2 w^2 (G - Gt) / ng
-                    dgram = (4.0 * wt * wt * cg / (ng * s)) * diff
-                    gg = _bmm_f32out(ff, dgram.to(torch.bfloat16)).reshape(v, h, w, c).contiguous()
+                    gg = gemm_nt_bf16(ff.reshape(v, s, c), dgram, self.err).reshape(v, h, w, c)
                 g = torch.empty(v, h, w, c, device=self.device, dtype=torch.bfloat16)
             coef = (2.0 * wt * wt * cf / nf) if cf is not None else 0.0
             N.check(L.svbrdf_desc_feat_loss(f.data_ptr(), int(f.dtype == torch.bfloat16), tf[k].data_ptr(),
@@ -293,16 +284,19 @@ class VGGDescriptor:
         _, hooks = self._forward(renders)
         return [hooks[n] for n in self.hooks]
 
-    @staticmethod
-    def _gram(f: torch.Tensor) -> torch.Tensor:
-        return _Gram.apply(f)
-
     def load(self, targets: torch.Tensor):
         self._graph = None  # a captured graph holds the previous targets' features
         with torch.no_grad():
-            feats = self.features(targets)
-            grams = [self._gram(f) for f in feats] if self.gram else []
+            acts, hooks = self._forward(targets)
+            feats = [hooks[n] for n in self.hooks]
+            grams = ([gram_bf16(self._bf16_hooks(acts, hooks)[n], self.err)[0] for n in self.hooks]
+                     if self.gram else [])
             self.target = ([f.float().contiguous() for f in feats], grams)
+
+    @staticmethod
+    def _bf16_hooks(acts, hooks):
+        """The hooked features as BF16 NHWC maps: relu1_1's BF16 copy is the first activation."""
+        return {n: (acts[0] if n == "conv1_1" else f) for n, f in hooks.items()}
 
     def loss(self, renders: torch.Tensor):
         """(feature_loss, gram_loss) as 0-d tensors, differentiable w.r.t. ``renders``."""
@@ -331,7 +325,7 @@ class VGGDescriptor:
 
     def _loss_and_grad_eager(self, renders):
         acts, hooks = self._forward(renders)
-        fl, gl, grads = self._terms(hooks, 1.0, 1.0)
+        fl, gl, grads = self._terms(hooks, 1.0, 1.0, self._bf16_hooks(acts, hooks))
         return fl, gl, self._backward(acts, grads, renders.shape)
 
     def loss_and_grad(self, renders: torch.Tensor):
@@ -364,7 +358,7 @@ class _DescriptorLoss(torch.autograd.Function):
     @staticmethod
     def forward(ctx, renders, desc):
         acts, hooks = desc._forward(renders)
-        fl, gl, _ = desc._terms(hooks, None, None)
+        fl, gl, _ = desc._terms(hooks, None, None, desc._bf16_hooks(acts, hooks))
         ctx.desc = desc
         ctx.shape = renders.shape
         ctx.acts, ctx.hooks = acts, hooks
@@ -373,7 +367,7 @@ class _DescriptorLoss(torch.autograd.Function):
     @staticmethod
     def backward(ctx, gfl, ggl):
         desc = ctx.desc
-        _, _, grads = desc._terms(ctx.hooks, float(gfl), float(ggl))
+        _, _, grads = desc._terms(ctx.hooks, float(gfl), float(ggl), desc._bf16_hooks(ctx.acts, ctx.hooks))
         dr = desc._backward(ctx.acts, grads, ctx.shape)
         ctx.acts = ctx.hooks = None
         return dr, None

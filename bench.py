@@ -25,6 +25,8 @@ Lines printed (rank 0, one JSON line):
   kernel, both on the 1024^2, 9-view scene;
 * ``cpu_baseline``: the reference's PyTorch CPU loop (the oracle restatement, same op
   sequence) on a bounded sample of the workload, all host threads;
+* ``config0``: the reference's own scale (1 material 256^2, 9 views, 20 iterations, MSE) on
+  the CPU (the same restatement, all host threads) and through the GPU drop-in optimiser;
 * ``descriptor``, ``latent``, ``envmap``: the VGG-feature loss, the MaterialGAN latent loop
   with the per-pixel refinement, and a frame of the environment-map video.
 
@@ -253,6 +255,43 @@ def run_cpu_baseline(specs, seconds, threads):
                       f"reference loop restated in torch (oracle), {threads} threads"}
 
 
+def time_config0(dev, threads):
+    """The reference's own scale (configs[0]): one 256^2 material, 9 co-located views on the 3x3
+    grid, 20 Adam iterations (lr 0.01), MSE loss. CPU: the oracle's restatement of the
+    reference's loop on all host threads; GPU: the drop-in SvbrdfOptim.optim (one-material
+    batched plan, graph replay), warmed by one identical call."""
+    from oracle import microfacet_ref as R
+
+    sc = PKG.scenes.single_scene(res=256, seed=1000, render_fn=lambda *a: R.render(*a, dtype=torch.float32))
+    tv = 256 * 256 * sc.n_views * 20
+    torch.set_num_threads(threads)
+    R.optim_loop(sc.init, sc.targets, sc.camera_pos, sc.light_pos, sc.light_pow, sc.size, 2, 0.01, "mse", False,
+                 torch.float32)
+    t0 = time.perf_counter()
+    R.optim_loop(sc.init, sc.targets, sc.camera_pos, sc.light_pos, sc.light_pow, sc.size, 20, 0.01, "mse", False,
+                 torch.float32)
+    cpu_s = time.perf_counter() - t0
+    r = PKG.Microfacet(256, sc.n_views, sc.size, [t.to(dev) for t in sc.cl], dev)
+    o = PKG.SvbrdfOptim(dev, r, loss="mse", graph=True)
+    o.load_targets(sc.targets.to(dev))
+    o.init_from_tex(sc.init.to(dev))
+    o.optim(20, 0.01, None, False)
+    with torch.no_grad():
+        o.textures.copy_(sc.init.to(dev))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    o.optim(20, 0.01, None, False)
+    torch.cuda.synchronize()
+    gpu_s = time.perf_counter() - t0
+    sample = "1 material 256^2, 9 co-located views, 20 Adam iterations, MSE (the reference's scale)"
+    return {"workload": sample,
+            "cpu": {"value": tv / cpu_s, "unit": UNIT, "cores": threads, "kind": "port", "seconds": cpu_s,
+                    "sample": sample + ", reference loop restated in torch (oracle)"},
+            "gpu": {"value": tv / gpu_s, "unit": UNIT, "seconds": gpu_s,
+                    "form": "drop-in SvbrdfOptim.optim, one-material batched plan in one CUDA graph, wall clock"},
+            "gpu_over_cpu": cpu_s / gpu_s}
+
+
 def impl_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -302,8 +341,13 @@ def time_single(dev, fused, iters, res=1024, kernel="batched"):
     form = (", forward kernel + torch loss + adjoint kernel (autograd) + torch.optim.Adam" if not fused else
             ", one-material plan of the batched kernels in one CUDA graph" if kernel == "batched" else
             ", single-material fused kernel, one launch per iteration, in one CUDA graph")
-    return {"value": res * res * 9 * iters / el, "unit": UNIT,
-            "workload": f"1 material {res}^2, 9 views, {iters} Adam iterations, log1p L2" + form}
+    out = {"value": res * res * 9 * iters / el, "unit": UNIT,
+           "workload": f"1 material {res}^2, 9 views, {iters} Adam iterations, log1p L2" + form}
+    b = getattr(o, "_batched", None) if fused and kernel == "batched" else None
+    if b is not None:
+        out["batch_config"] = b.config.__dict__
+        out["autotune_ms"] = [list(r) for r in getattr(b, "tune_results", [])[:6]]
+    return out
 
 
 def time_envmap(dev, res=256, spp=256, frames=5):
@@ -507,11 +551,27 @@ def impl_ours(args):
     tune = [list(r) for r in getattr(opt, "tune_results", [])[:8]]
     kernel = KERNEL_NAMES[cfg_used.variant]
     tfile = HERE / "profiles" / f"{kernel}_traffic.json"
+    issue = None
     if tfile.exists():
         try:
             tj = json.loads(tfile.read_text())
             # a resident-state launch moves its state and targets once, whatever its iterations
             traffic = float(tj["dram_bytes_per_algorithmic_byte"]) * (abytes if tj.get("per_launch_pass") else launch_abytes)
+            # the instruction-issue roofline: warp instructions per texel*view (from the same
+            # capture) times the measured rate, against one issue per cycle per scheduler
+            if tj.get("warp_instructions_per_texel_view"):
+                wi = float(tj["warp_instructions_per_texel_view"])
+                sms = torch.cuda.get_device_properties(dev).multi_processor_count
+                mhz = None
+                try:
+                    mhz = float(json.loads((HERE / "MEASURED_PEAKS.json").read_text())["sm_max_mhz"])
+                except Exception:
+                    mhz = 2070.0
+                issue_rate = value * wi
+                issue_peak = sms * 4 * mhz * 1e6
+                issue = {"warp_instructions_per_texel_view": wi, "achieved": issue_rate, "peak": issue_peak,
+                         "unit": "warp instructions/s", "frac": issue_rate / issue_peak,
+                         "source": f"profiles/{kernel}_traffic.json"}
         except Exception:
             traffic = None
 
@@ -611,7 +671,7 @@ def impl_ours(args):
                          "kernel": kernel,
                          "algorithmic_bytes_per_launch": launch_abytes,
                          "iterations_per_launch": iters_per_launch,
-                         "launch_ms": launch_ms},
+                         "launch_ms": launch_ms, "issue": issue},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "mode": "BatchedPipeline: two buffers, uploads and downloads on copy streams overlap the compute",
                     "sequential_value": seq_value, "device_error": pipe_err},
@@ -628,6 +688,7 @@ def impl_ours(args):
         line["envmap"] = time_envmap(dev)
         if world == 1:
             line["cpu_baseline"] = run_cpu_baseline(specs, args.cpu_seconds, os.cpu_count() or 1)
+            line["config0"] = time_config0(dev, os.cpu_count() or 1)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -371,6 +371,19 @@ int svbrdf_gen_act_nhwc_bwd(const float* gout, const float* y, const float* d, c
                             const float* bias, float gain, float* gy, float* gd, float* gnoise, float* part, int b,
                             int hw, int c, void* stream);
 
+/* ---- MaterialGAN generator: its convolutions in TF32 on the tensor cores (the reference's
+ * modulated convolutions, src/higan_models/stylegan2_generator_network.py:585-759, computed as a
+ * shared-weight convolution between the modulation and demodulation kernels above) ---- */
+
+/* y [b][ho][wo][cout] = k x k convolution (ksize 3 or 1) of x [b][hin][win][cin] with weight
+ * [cout][ksize*ksize][cin] (tap = 3 ky + kx), zero padding `pad` (0..2 for 3x3, 0 for 1x1):
+ * ho = hin + 2 pad - (ksize - 1). FP32 data, TF32 products, FP32 accumulation in tensor memory.
+ * cin % 32 == 0; cout 32, 64, 128 or a multiple of 256; wo >= 4; 16-byte aligned. The data
+ * gradient of a convolution is this call on dL/dY with weight'[cin][8 - tap][cout] =
+ * weight[cout][tap][cin] and pad' = ksize - 1 - pad. `err` as in svbrdf_conv3x3_bf16. */
+int svbrdf_gen_conv_tf32(const float* x, const float* weight, float* y, int b, int hin, int win, int cin, int cout,
+                         int ksize, int pad, int* err, void* stream);
+
 /* ---- novel-view rendering under an environment map (the reference's MitsubaRender,
  * src/mitsubarender.py:7-105, for the video of src/scripts.py:44-59) ---- */
 

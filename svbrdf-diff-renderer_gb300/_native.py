@@ -20,8 +20,8 @@ CSRC = PKG / "csrc"
 INCLUDE = REPO / "include"
 LIBDIR = PKG / "_lib"
 LIBNAME = "libsvbrdf_gb300.so"
-SOURCES = ["render.cu", "fused.cu", "conv_tc.cu", "gram_tc.cu", "desc_ops.cu", "gen_ops.cu", "gen_nhwc.cu",
-           "envmap.cu"]
+SOURCES = ["render.cu", "fused.cu", "conv_tc.cu", "gram_tc.cu", "conv_tf32.cu", "desc_ops.cu", "gen_ops.cu",
+           "gen_nhwc.cu", "envmap.cu"]
 HEADERS = ["svbrdf_math.cuh", "svbrdf_common.cuh", "svbrdf_plan.cuh", "tc_ptx.cuh"]
 WORKSPACE_ERROR_OFFSET = 4
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -150,6 +150,8 @@ def _declare(L):
     L.svbrdf_desc_gram_finish.argtypes = [P, I, I, I, I, P, F, P, P, P, P]
     L.svbrdf_desc_gemm_nt.restype = I
     L.svbrdf_desc_gemm_nt.argtypes = [P, P, P, I, I, I, I, P, P]
+    L.svbrdf_gen_conv_tf32.restype = I
+    L.svbrdf_gen_conv_tf32.argtypes = [P, P, P, I, I, I, I, I, I, I, P, P]
     L.svbrdf_gen_upsample2.restype = I
     L.svbrdf_gen_upsample2.argtypes = [P, P, ctypes.c_longlong, I, I, P]
     L.svbrdf_gen_upsample2_scaled.restype = I
@@ -208,6 +210,7 @@ EXPORTS = [
     "svbrdf_gen_upsample2_bwd", "svbrdf_gen_upsample2_scaled", "svbrdf_gen_scale", "svbrdf_gen_scale_bwd", "svbrdf_gen_act", "svbrdf_gen_act_bwd",
     "svbrdf_gen_nhwc_partial_floats", "svbrdf_gen_upsample2_nhwc", "svbrdf_gen_upsample2_nhwc_bwd",
     "svbrdf_gen_scale_nhwc", "svbrdf_gen_scale_nhwc_bwd", "svbrdf_gen_act_nhwc", "svbrdf_gen_act_nhwc_bwd",
+    "svbrdf_gen_conv_tf32",
     "svbrdf_envmap_render", "svbrdf_selftest_wait_timeout",
 ]
 

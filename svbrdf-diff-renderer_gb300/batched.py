@@ -363,9 +363,10 @@ class BatchedPipeline:
         return max(o.device_error() for o in self.bufs)
 
 
-def _time_config(opt: BatchedOptim, cfg: BatchConfig, iters: int = 8) -> float:
-    """Milliseconds per iteration of ``cfg``, timed over ``iters`` iterations in one call (so
-    the resident-state variant runs them in one launch, as a graph of a longer run does)."""
+def _time_config(opt: BatchedOptim, cfg: BatchConfig, iters: int = 16, repeats: int = 2) -> float:
+    """Milliseconds per iteration of ``cfg``: the best of ``repeats`` timings of ``iters``
+    iterations in one call (so the resident-state variant runs them in one launch, as a graph
+    of a longer run does)."""
     tex = [t.clone() for t in opt.tex]
     m1 = [torch.zeros_like(t) for t in tex]
     m2 = [torch.zeros_like(t) for t in tex]
@@ -375,15 +376,18 @@ def _time_config(opt: BatchedOptim, cfg: BatchConfig, iters: int = 8) -> float:
     loss = torch.zeros(1, opt.n, device=opt.device)
     step = torch.zeros(1, device=opt.device, dtype=torch.int32)
     opt._launch(host, dev, ws, step, loss, 2)  # warm
-    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    s.record()
-    opt._launch(host, dev, ws, step, loss, iters)
-    e.record()
-    e.synchronize()
+    best = float("inf")
+    for _ in range(repeats):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        opt._launch(host, dev, ws, step, loss, iters)
+        e.record()
+        e.synchronize()
+        best = min(best, s.elapsed_time(e) / iters)
     off = N.WORKSPACE_ERROR_OFFSET
     if int(ws[off:off + 4].view(torch.int32).item()):
         raise N.SvbrdfError(-3, "device error during tuning")
-    return s.elapsed_time(e) / iters
+    return best
 
 
 def _load_cache():

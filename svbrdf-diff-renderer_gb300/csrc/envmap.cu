@@ -168,6 +168,11 @@ __device__ __forceinline__ float srgb_to_linear(float c) {
   return c <= 0.04045f ? c * (1.0f / 12.92f) : powf((c + 0.055f) * (1.0f / 1.055f), 2.4f);
 }
 
+// Lanes per pixel: the pixel's camera samples are dealt round-robin to a group of kGroup
+// adjacent lanes and their sums combined by shuffles, so a 256^2 frame runs 8 x 65536 threads
+// (one thread per pixel left most of the GPU's warp slots empty).
+constexpr int kGroup = 8;
+
 __global__ void __launch_bounds__(128) envmap_render_kernel(Scene sc, const float* __restrict__ tex,
                                                             const float* __restrict__ env,
                                                             const float* __restrict__ row_cdf,
@@ -175,16 +180,17 @@ __global__ void __launch_bounds__(128) envmap_render_kernel(Scene sc, const floa
                                                             const float* __restrict__ col_cdf,
                                                             const float* __restrict__ col_pdf,
                                                             float* __restrict__ image) {
-  const int pix = blockIdx.x * blockDim.x + threadIdx.x;
-  if (pix >= sc.res * sc.res) return;
-  const int py = pix / sc.res, px = pix - py * sc.res;
+  const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int pix = gid / kGroup, sub = gid % kGroup;
+  const bool live = pix < sc.res * sc.res;  // every lane stays for the group's shuffles
+  const int py = live ? pix / sc.res : 0, px = live ? pix - py * sc.res : 0;
   const V3 R0 = v3(sc.rot[0], sc.rot[3], sc.rot[6]);  // world images of the local x, y, z axes
   const V3 R1 = v3(sc.rot[1], sc.rot[4], sc.rot[7]);
   const V3 R2 = v3(sc.rot[2], sc.rot[5], sc.rot[8]);
   const V3 org = v3(0.0f, 0.0f, 1.0f);
   const size_t plane = (size_t)sc.H * sc.W;
   V3 acc = v3(0.f, 0.f, 0.f);
-  for (int s = 0; s < sc.spp; ++s) {
+  for (int s = live ? sub : sc.spp; s < sc.spp; s += kGroup) {
     const float jx = rnd(sc.seed, pix, s, 0), jy = rnd(sc.seed, pix, s, 1);
     const float sx = (2.0f * (px + jx) / sc.res - 1.0f) * sc.tan_half;
     const float sy = (1.0f - 2.0f * (py + jy) / sc.res) * sc.tan_half;
@@ -275,6 +281,13 @@ __global__ void __launch_bounds__(128) envmap_render_kernel(Scene sc, const floa
     }
     acc = add(acc, L);
   }
+#pragma unroll
+  for (int o = kGroup / 2; o > 0; o >>= 1) {
+    acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+    acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+    acc.z += __shfl_xor_sync(0xffffffffu, acc.z, o);
+  }
+  if (!live || sub != 0) return;
   const float inv = 1.0f / sc.spp;
   float* o = image + (size_t)pix * 3;
   const float rgb[3] = {acc.x * inv, acc.y * inv, acc.z * inv};
@@ -294,7 +307,7 @@ int svbrdf_envmap_render(const float* textures, int h, int w, const float* env, 
                          float angle_deg, float intensity, int spp, unsigned seed, void* stream) {
   if (!textures || !env || !row_cdf || !row_pdf || !col_cdf || !col_pdf || !image)
     return fail(SVBRDF_ERR_INVALID, "envmap: null pointer");
-  if (h < 1 || w < 1 || he < 2 || we < 2 || res < 1 || spp < 1 || (long long)res * res > (1LL << 30))
+  if (h < 1 || w < 1 || he < 2 || we < 2 || res < 1 || spp < 1 || (long long)res * res * env::kGroup > (1LL << 30))
     return fail(SVBRDF_ERR_INVALID, "envmap: bad sizes");
   env::Scene sc;
   // rotation R = Ry(angle) Rx(-15) Rz(-5), applied to local points (Mitsuba's rotate order
@@ -326,9 +339,9 @@ int svbrdf_envmap_render(const float* textures, int h, int w, const float* env, 
   sc.We = we;
   sc.spp = spp;
   sc.seed = seed;
-  const int n = res * res;
-  env::envmap_render_kernel<<<(n + 127) / 128, 128, 0, (cudaStream_t)stream>>>(sc, textures, env, row_cdf, row_pdf,
-                                                                               col_cdf, col_pdf, image);
+  const long long n = (long long)res * res * env::kGroup;
+  env::envmap_render_kernel<<<(unsigned)((n + 127) / 128), 128, 0, (cudaStream_t)stream>>>(
+      sc, textures, env, row_cdf, row_pdf, col_cdf, col_pdf, image);
   return check_launch("envmap_render_kernel");
 }
 

@@ -208,6 +208,62 @@ class _UpsampleNHWC(torch.autograd.Function):
         return gx, gs, None
 
 
+_TF32_ERR = {}
+
+
+def _tf32_err(device):
+    """Per-device error word of the TF32 convolutions (non-zero if a launch gave up waiting)."""
+    key = str(device)
+    if key not in _TF32_ERR:
+        _TF32_ERR[key] = torch.zeros(1, dtype=torch.int32, device=device)
+    return _TF32_ERR[key]
+
+
+def generator_device_error(device="cuda") -> int:
+    """The TF32 convolutions' error word (0 = healthy); synchronises with the device."""
+    return int(_tf32_err(torch.device(device)).item())
+
+
+class _ConvTF32(torch.autograd.Function):
+    """A k x k convolution (k = 3 or 1) of a channels-last FP32 map on the tensor cores in TF32
+    (svbrdf_gen_conv_tf32): ``pad`` 1 for a same-padded 3x3 convolution, 0 for a valid one (the
+    up-sampling layers) or a 1x1. The weights come prepared: ``w_fwd`` [Cout_p][k*k][Cin] and
+    ``w_dg`` [Cin][k*k][Cout_p] (transposed, taps flipped), Cout_p = Cout padded to the
+    kernel's minimum of 32 with zero rows. The data gradient is the same kernel on w_dg with pad
+    k - 1 - pad; the weights are frozen (no weight gradient)."""
+
+    @staticmethod
+    def forward(ctx, x, w_fwd, w_dg, cout, k, pad):
+        from . import _native as N
+
+        x = _cl(x)
+        b, c, h, wd = x.shape
+        coutp = w_fwd.shape[0]
+        ho, wo = h + 2 * pad - (k - 1), wd + 2 * pad - (k - 1)
+        y = torch.empty(b, coutp, ho, wo, device=x.device, dtype=torch.float32, memory_format=CL)
+        N.check(N.lib().svbrdf_gen_conv_tf32(x.data_ptr(), w_fwd.data_ptr(), y.data_ptr(), b, h, wd, c, coutp, k, pad,
+                                             _tf32_err(x.device).data_ptr(), N.stream_handle(x.device)))
+        ctx.save_for_backward(w_dg)
+        ctx.geom = (b, c, h, wd, coutp, cout, k, pad, ho, wo)
+        return y if coutp == cout else y[:, :cout]
+
+    @staticmethod
+    def backward(ctx, gy):
+        from . import _native as N
+
+        (w_dg,) = ctx.saved_tensors
+        b, c, h, wd, coutp, cout, k, pad, ho, wo = ctx.geom
+        if coutp != cout:
+            gp = torch.zeros(b, coutp, ho, wo, device=gy.device, dtype=torch.float32, memory_format=CL)
+            gp[:, :cout] = gy
+            gy = gp
+        gy = _cl(gy)
+        gx = torch.empty(b, c, h, wd, device=gy.device, dtype=torch.float32, memory_format=CL)
+        N.check(N.lib().svbrdf_gen_conv_tf32(gy.data_ptr(), w_dg.data_ptr(), gx.data_ptr(), b, ho, wo, coutp, c, k,
+                                             k - 1 - pad, _tf32_err(gy.device).data_ptr(), N.stream_handle(gy.device)))
+        return gx, None, None, None, None, None
+
+
 class _ScaleNHWC(torch.autograd.Function):
     """x[b, c] * s[b, c] on channels-last maps (svbrdf_gen_scale_nhwc[_bwd])."""
 
@@ -369,6 +425,30 @@ class _ModConv(torch.nn.Module):
         y, d = self.parts(x, w)
         return y if d is None else y * d[:, :, None, None]
 
+    def _tf32_ok(self, x) -> bool:
+        """The TF32 tensor-core convolution serves a frozen layer whenever TF32 is allowed
+        (cuDNN's default, and what the reference's PyTorch GPU path computes in); with TF32 off
+        the layer runs in FP32 through cuDNN."""
+        cin = self.weight.shape[1]
+        return (torch.backends.cudnn.allow_tf32 and not self.weight.requires_grad and cin % 32 == 0 and
+                x.shape[-1] + 2 * (0 if self.up else self.k // 2) - (self.k - 1) >= 4)
+
+    def _tf32_weights(self, wsc):
+        """(w_fwd [Cout_p][k*k][Cin], w_dg [Cin][k*k][Cout_p]) of the scaled weight, Cout_p =
+        Cout rounded up to 32; cached while the weight is unchanged."""
+        key = (self.weight.data_ptr(), self.weight._version, str(self.weight.device))
+        if getattr(self, "_tf32_key", None) != key:
+            with torch.no_grad():
+                w = wsc.detach().float()
+                cout, cin, k, _ = w.shape
+                coutp = max(32, -(-cout // 32) * 32)
+                if coutp != cout:
+                    w = torch.cat((w, torch.zeros(coutp - cout, cin, k, k, device=w.device)), 0)
+                self._w_fwd = w.permute(0, 2, 3, 1).reshape(coutp, k * k, cin).contiguous()
+                self._w_dg = w.flip(2, 3).permute(1, 2, 3, 0).reshape(cin, k * k, coutp).contiguous()
+            self._tf32_key = key
+        return self._w_fwd, self._w_dg
+
     def parts(self, x, w):
         """The shared-weight convolution of the style-scaled input, and the demodulation
         d [B, cout] (None without demodulation) still to be applied to its output."""
@@ -376,15 +456,20 @@ class _ModConv(torch.nn.Module):
         wsc = self.weight * self.scale
         # an up-sampling layer convolves the up-sampled map with its one-sample halo, unpadded
         # (_upsample2_halo): the reference's transposed convolution + filter on the border too
+        pad = 0 if self.up else self.k // 2
         if _use_kernels(x) and _is_nhwc(x):
-            # channels-last: the layout cuDNN's convolutions run in, so none converts its operands
+            # channels-last: the layout of the TF32 tensor-core convolutions (and of cuDNN's)
             x = _UpsampleNHWC.apply(x, s, 1) if self.up else _ScaleNHWC.apply(x, s)
-            wsc = _cl(wsc)
+            if self._tf32_ok(x):
+                w_fwd, w_dg = self._tf32_weights(wsc)
+                y = _ConvTF32.apply(x, w_fwd, w_dg, self.weight.shape[0], self.k, pad)
+            else:
+                y = Fn.conv2d(x, _cl(wsc), padding=pad)
         else:
             x = _ScaleCuda.apply(x, s) if _use_kernels(x) else x * s[:, :, None, None]
             if self.up:
                 x = _upsample2_halo(x)  # per-channel linear: commutes with the channel scaling
-        y = Fn.conv2d(x, wsc, padding=0 if self.up else self.k // 2)
+            y = Fn.conv2d(x, wsc, padding=pad)
         d = None
         if self.demod:
             w2 = wsc.pow(2).sum(dim=(2, 3))  # [cout, cin]

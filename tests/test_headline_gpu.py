@@ -11,8 +11,9 @@ SvbrdfOptim.optim loop (src/svbrdf.py:44-83) and Microfacet.eval (src/microfacet
   material plus the texels at each end of the material and around a tile boundary: a
   texel's trajectory depends on that texel alone, so the oracle follows the sampled texels
   exactly, without the rest of the material. Tolerance: relative L2 per material of at most
-  max(2e-5, twice the reference's own FP32 error) for the maps, and max(1e-4, twice that
-  error) for the moments; the FP32 error is measured on the first 72 sampled texels;
+  max(2e-5, twice the reference's own FP32 error on the same texels) for the maps, and
+  max(1e-4, twice that error) for the moments (a texel near a clamp of the render can take a
+  slightly different path in FP32 than in FP64; the reference's own FP32 loop does too);
 * every loss of one whole 256^2 material (all its texels through the oracle, 100 iterations)
   within 1e-5 relative;
 * the first iteration's loss of one material of each resolution, every texel through the
@@ -32,7 +33,6 @@ pytestmark = pytest.mark.gpu
 
 ITERS = 100
 SAMPLE = 256
-NOISE_SAMPLE = 72  # texels per material of the FP32 (reference arithmetic) run
 LR = 0.01
 
 
@@ -96,7 +96,7 @@ def workload(svb, cuda):
         svb.scenes.add_targets(m, rf)
     t0 = time.perf_counter()
     idxs, o64 = oracle_samples(R, mats, torch.float64)
-    _, o32 = oracle_samples(R, mats, torch.float32, keep=NOISE_SAMPLE)
+    _, o32 = oracle_samples(R, mats, torch.float32)
     # one whole 256^2 material (the fewest views) through the oracle for every loss
     small = min((i for i, m in enumerate(mats) if m.res == 256), key=lambda i: mats[i].n_views)
     m = mats[small]
@@ -156,15 +156,13 @@ def test_bench_workload_matches_oracle(svb, cuda, workload, variant):
     assert b.device_error() == 0
     hist = b.loss_hist.cpu()
     o64, o32 = workload["o64"], workload["o32"]
-    nsl = [slice(k * NOISE_SAMPLE, (k + 1) * NOISE_SAMPLE) for k in range(len(mats))]
     e_single = 0.0
     for i, (m, sl, idx) in enumerate(zip(mats, _col_ranges(workload["idxs"]), workload["idxs"])):
         got = {"textures": b.tex[i].reshape(9, -1)[:, idx.to(cuda)], "exp_avg": b.m1[i].reshape(9, -1)[:, idx.to(cuda)],
                "exp_avg_sq": b.m2[i].reshape(9, -1)[:, idx.to(cuda)]}
         for k, floor in (("textures", 2e-5), ("exp_avg", 1e-4), ("exp_avg_sq", 1e-4)):
             ref = o64[k][:, sl]
-            # the reference's own FP32 arithmetic on the first NOISE_SAMPLE of these texels
-            noise = rel_l2(o32[k][:, nsl[i]], ref[:, :NOISE_SAMPLE])
+            noise = rel_l2(o32[k][:, sl], ref)  # the reference's own FP32 arithmetic on these texels
             err = rel_l2(got[k], ref)
             assert err <= max(floor, 2 * noise), (i, m.res, m.n_views, k, err, noise)
         for it in range(ITERS):

@@ -309,7 +309,8 @@ def test_gpu_generator_matches_reference_network(svb, cuda):
     """The GPU generator (channels-last maps, the NHWC kernels with the up-sampling halo,
     cuDNN convolutions in FP32 with TF32 off) on the reference network's fixture
     (tests/golden/generator_ref_256.npz): output, W+ gradient and noise gradients within
-    FP32 accuracy of the reference's FP64 run."""
+    FP32 accuracy of the reference's FP64 run: the output within 1e-5, the gradients within
+    three times the error of the same network run in FP32 on the CPU (at least 1e-4)."""
     gen, d, wp_np, noises_np, R_np, _ = _reference_generator(svb, cuda, torch.float32)
     for p in gen.parameters():
         p.requires_grad_(False)
@@ -323,11 +324,82 @@ def test_gpu_generator_matches_reference_network(svb, cuda):
     finally:
         torch.backends.cudnn.allow_tf32 = True
     o = out.detach().double().cpu()
+    # the same network in FP32 on the CPU (torch ops) sets the FP32 error floor of the gradients
+    gc, _, _, _, _, _ = _reference_generator(svb, "cpu", torch.float32)
+    wc = torch.from_numpy(wp_np).float().requires_grad_(True)
+    nc = [torch.from_numpy(n).float().requires_grad_(True) for n in noises_np]
+    (gc.synthesis(wc, nc) * torch.from_numpy(R_np).float()).sum().backward()
+    e32_wp = rel_l2(wc.grad, torch.from_numpy(d["grad_wp"]))
+    e32_n = max(abs(float(n.grad.double().norm()) - float(d[f"noise{i}_norm"])) / float(d[f"noise{i}_norm"])
+                for i, n in enumerate(nc))
+    e_wp = rel_l2(wp.grad, torch.from_numpy(d["grad_wp"]))
+    e_n = max(abs(float(n.grad.double().norm()) - float(d[f"noise{i}_norm"])) / float(d[f"noise{i}_norm"])
+              for i, n in enumerate(noises))
+    print(f"FP32 generator vs reference FP64: W+ gradient GPU {e_wp:.2e} (CPU FP32 {e32_wp:.2e}), "
+          f"noise-gradient norms GPU {e_n:.2e} (CPU FP32 {e32_n:.2e})")
     assert abs(float(loss.detach()) - float(d["loss"])) <= 1e-4 * abs(float(d["loss"]))
     ov = o.reshape(-1)[torch.from_numpy(d["out_idx"])]
     assert rel_l2(ov, torch.from_numpy(d["out_val"])) <= 1e-5
     assert rel_l2(o.pow(2).sum((0, 2, 3)).sqrt(), torch.from_numpy(d["out_norm"])) <= 1e-5
-    assert rel_l2(wp.grad, torch.from_numpy(d["grad_wp"])) <= 1e-4
-    for i, n in enumerate(noises):
-        g = n.grad.reshape(-1).double().cpu()
-        assert abs(float(g.norm()) - float(d[f"noise{i}_norm"])) <= 1e-4 * float(d[f"noise{i}_norm"])
+    assert e_wp <= max(1e-4, 3 * e32_wp)
+    assert e_n <= max(1e-4, 3 * e32_n)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("b,h,cin,cout,k,pad", [(16, 4, 512, 512, 3, 1), (3, 8, 512, 512, 3, 1), (2, 10, 512, 256, 3, 0),
+                                                 (2, 18, 256, 128, 3, 0), (1, 32, 128, 128, 3, 1),
+                                                 (2, 16, 128, 9, 1, 0)])
+def test_conv_tf32_matches_torch(svb, cuda, b, h, cin, cout, k, pad):
+    """The TF32 tensor-core convolution (forward and data gradient through _ConvTF32) against
+    torch's FP32 convolution of the same channels-last maps: relative L2 <= 2e-3 (TF32 rounds
+    both operands to 10 mantissa bits; FP32 accumulation)."""
+    MG = svb.materialgan
+    g = torch.Generator().manual_seed(b * h + cin)
+    x = torch.randn(b, cin, h, h, generator=g).to(cuda).contiguous(memory_format=torch.channels_last)
+    w = (torch.randn(cout, cin, k, k, generator=g) / (cin * k * k) ** 0.5).to(cuda)
+    conv = MG._ModConv(cin, cout, k, 512, torch.Generator().manual_seed(0)).to(cuda)
+    conv.requires_grad_(False)
+    with torch.no_grad():
+        conv.weight.copy_(w / conv.scale)
+    w_fwd, w_dg = conv._tf32_weights(conv.weight * conv.scale)
+    xr = x.clone().requires_grad_(True)
+    y = MG._ConvTF32.apply(xr, w_fwd, w_dg, cout, k, pad)
+    gy = torch.randn(y.shape, generator=g).to(cuda)
+    (y * gy).sum().backward()
+    torch.backends.cudnn.allow_tf32 = False
+    try:
+        x2 = x.clone().requires_grad_(True)
+        ref = torch.nn.functional.conv2d(x2, w, padding=pad)
+        (ref * gy).sum().backward()
+    finally:
+        torch.backends.cudnn.allow_tf32 = True
+    torch.cuda.synchronize()
+    assert MG.generator_device_error(cuda) == 0
+    assert y.shape == ref.shape
+    assert rel_l2(y, ref) <= 2e-3
+    assert rel_l2(xr.grad, x2.grad) <= 2e-3
+
+
+@pytest.mark.gpu
+def test_gpu_generator_tf32_matches_reference_network(svb, cuda):
+    """The generator as it runs by default on the GPU (channels-last maps, the TF32 tensor-core
+    convolutions, the NHWC kernels) on the reference network's fixture
+    (tests/golden/generator_ref_256.npz, the reference's FP64 run): output and gradients within
+    TF32 accuracy."""
+    gen, d, wp_np, noises_np, R_np, _ = _reference_generator(svb, cuda, torch.float32)
+    for p in gen.parameters():
+        p.requires_grad_(False)
+    assert torch.backends.cudnn.allow_tf32
+    wp = torch.from_numpy(wp_np).float().to(cuda).requires_grad_(True)
+    noises = [torch.from_numpy(n).float().to(cuda).requires_grad_(True) for n in noises_np]
+    out = gen.synthesis(wp, noises)
+    (out * torch.from_numpy(R_np).float().to(cuda)).sum().backward()
+    torch.cuda.synchronize()
+    assert svb.materialgan.generator_device_error(cuda) == 0
+    o = out.detach().double().cpu()
+    e_out = rel_l2(o.reshape(-1)[torch.from_numpy(d["out_idx"])], torch.from_numpy(d["out_val"]))
+    e_wp = rel_l2(wp.grad, torch.from_numpy(d["grad_wp"]))
+    e_n = max(abs(float(n.grad.double().norm()) - float(d[f"noise{i}_norm"])) / float(d[f"noise{i}_norm"])
+              for i, n in enumerate(noises))
+    print(f"TF32 generator vs reference FP64: output {e_out:.2e}, W+ gradient {e_wp:.2e}, noise-gradient norms {e_n:.2e}")
+    assert e_out <= 1e-2 and e_wp <= 3e-2 and e_n <= 3e-2

@@ -181,7 +181,7 @@ __global__ void __launch_bounds__(128) envmap_render_kernel(Scene sc, const floa
                                                             const float* __restrict__ col_pdf,
                                                             float* __restrict__ image) {
   const int gid = blockIdx.x * blockDim.x + threadIdx.x;
-  const int pix = gid / kGroup, sub = gid % kGroup;
+  const int pix = gid / kGroup, part = gid % kGroup;
   const bool live = pix < sc.res * sc.res;  // every lane stays for the group's shuffles
   const int py = live ? pix / sc.res : 0, px = live ? pix - py * sc.res : 0;
   const V3 R0 = v3(sc.rot[0], sc.rot[3], sc.rot[6]);  // world images of the local x, y, z axes
@@ -190,7 +190,7 @@ __global__ void __launch_bounds__(128) envmap_render_kernel(Scene sc, const floa
   const V3 org = v3(0.0f, 0.0f, 1.0f);
   const size_t plane = (size_t)sc.H * sc.W;
   V3 acc = v3(0.f, 0.f, 0.f);
-  for (int s = live ? sub : sc.spp; s < sc.spp; s += kGroup) {
+  for (int s = live ? part : sc.spp; s < sc.spp; s += kGroup) {
     const float jx = rnd(sc.seed, pix, s, 0), jy = rnd(sc.seed, pix, s, 1);
     const float sx = (2.0f * (px + jx) / sc.res - 1.0f) * sc.tan_half;
     const float sy = (1.0f - 2.0f * (py + jy) / sc.res) * sc.tan_half;
@@ -287,7 +287,7 @@ __global__ void __launch_bounds__(128) envmap_render_kernel(Scene sc, const floa
     acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
     acc.z += __shfl_xor_sync(0xffffffffu, acc.z, o);
   }
-  if (!live || sub != 0) return;
+  if (!live || part != 0) return;
   const float inv = 1.0f / sc.spp;
   float* o = image + (size_t)pix * 3;
   const float rgb[3] = {acc.x * inv, acc.y * inv, acc.z * inv};

@@ -34,6 +34,10 @@ namespace svb {
 
 int check_common(const float* tex, const float* cam, const float* lit, const float* lpow, int V, int H, int W,
                  float size);
+
+// Most iterations one launch of the resident-state kernels runs (svbrdf_batched_steps splits
+// longer runs evenly); the workspace holds loss partials for that many.
+constexpr int kFuseMax = 32;
 int grid_for(long long T, int threads, int occupancy_blocks);
 
 AdamScalars make_adam(int step, float lr, float beta1, float beta2, float eps) {
@@ -226,16 +230,47 @@ __device__ __forceinline__ void texel_rc(int idx, const MatDesc& md, int& i, int
   else if (j >= md.W) { ++i; j -= md.W; }
 }
 
-// Last CTA of a batched launch: per-material mean loss from the fixed-order partial sums
-// (`per_tile` partials per tile), step counter store, completion counter reset.
-// A launch that ran `iters` iterations (steps step - iters + 1 .. step) holds iteration i's
-// partials at partial + i * n_tiles * per_tile and fills one loss_hist row per iteration.
+// End of a batched launch, in every CTA: the warps' partial losses (`per_tile` per tile and
+// iteration; and with a learnable light, the light-gradient partials) of this CTA's own tiles
+// are summed per (iteration, tile) in warp order into the tile totals that follow the partials
+// in the workspace. The last CTA to finish then forms each material's mean loss from its
+// tiles' totals in tile order (a launch that ran `iters` iterations, steps step - iters + 1 ..
+// step, fills one loss_hist row per iteration), runs Adam on the learnable light powers, stores
+// the step counter and resets the completion counter. Both levels have a fixed order, so the
+// losses are deterministic; the last CTA reads one value per tile and iteration instead of
+// one per warp (15x fewer), in parallel across its warps.
 template <int NT>
 __device__ __forceinline__ void batched_finish(const char* plan, const PlanHeader* hdr, const MatDesc* mats,
                                                const float* partial, int per_tile, float* loss_hist, int hist_len,
                                                int step, int* step_counter, unsigned* counter, int* s_flag,
                                                int nwarps, int iters = 1, const float* lpart = nullptr,
                                                const AdamScalars* light_adam = nullptr) {
+  const int n_tiles = hdr->n_tiles;
+  const size_t slots = (size_t)n_tiles * per_tile;
+  float* tile_tot = const_cast<float*>(partial) + slots * (hdr->variant >= 3 ? kFuseMax : 1) + (hdr->light ? 3 * slots : 0);
+  __syncthreads();  // every warp of this CTA has written its partials
+  {
+    const int* cta_off = (const int*)(plan + hdr->off_cta);
+    const int* order = (const int*)(plan + hdr->off_order);
+    const int k0 = cta_off[blockIdx.x], nk = cta_off[blockIdx.x + 1] - k0;
+    for (int e = threadIdx.x; e < iters * nk; e += blockDim.x) {
+      const int i = e / nk, tile = order[k0 + e % nk];
+      const float* p = partial + ((size_t)i * n_tiles + tile) * per_tile;
+      float t = 0.f;
+      for (int q = 0; q < per_tile; ++q) t += __ldcg(p + q);
+      tile_tot[(size_t)i * n_tiles + tile] = t;
+    }
+    if (lpart) {
+      for (int e = threadIdx.x; e < 3 * nk; e += blockDim.x) {
+        const int c = e / nk, tile = order[k0 + e % nk];
+        const float* p = lpart + 3 * (size_t)tile * per_tile + c;  // (tile, warp, channel)
+        float t = 0.f;
+        for (int q = 0; q < per_tile; ++q) t += __ldcg(p + 3 * q);
+        tile_tot[(size_t)(kFuseMax + c) * n_tiles + tile] = t;
+      }
+    }
+    __threadfence();
+  }
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
@@ -246,34 +281,29 @@ __device__ __forceinline__ void batched_finish(const char* plan, const PlanHeade
   if (!*s_flag) return;
   __threadfence();
   const int* mat_tiles = (const int*)(plan + hdr->off_mat_tiles);
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  for (int i = 0; i < iters; ++i) {
-    float* loss_out = loss_hist + (size_t)((step - iters + i) % hist_len) * hdr->n_mat;
-    const float* part = partial + (size_t)i * hdr->n_tiles * per_tile;
-    if (w < nwarps) {
-      for (int mi = w; mi < hdr->n_mat; mi += nwarps) {
-        double acc = 0.0;
-        const int e0 = mat_tiles[mi] * per_tile, e1 = mat_tiles[mi + 1] * per_tile;
-        for (int t = e0 + lane; t < e1; t += 32) acc += (double)__ldcg(part + t);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  // one warp per (iteration, material)
+  for (int e = w; e < iters * hdr->n_mat; e += nw) {
+    const int i = e / hdr->n_mat, mi = e % hdr->n_mat;
+    const float* tt = tile_tot + (size_t)i * n_tiles;
+    double acc = 0.0;
+    for (int t = mat_tiles[mi] + lane; t < mat_tiles[mi + 1]; t += 32) acc += (double)__ldcg(tt + t);
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if (lane == 0) loss_out[mi] = (float)(acc * mats[mi].inv_n);
-      }
-    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) loss_hist[(size_t)((step - iters + i) % hist_len) * hdr->n_mat + mi] = (float)(acc * mats[mi].inv_n);
   }
-  if (lpart && w < nwarps) {
+  if (lpart) {
     // Learnable light (one-iteration launches): per material, the light-power gradient summed
-    // over its (tile, warp) partials in a fixed order, then Adam on the light with the maps'
-    // hyper-parameters and step (one optimiser over [textures, light_pow], src/svbrdf.py:50).
+    // over its tiles in a fixed order, then Adam on the light with the maps' hyper-parameters
+    // and step (one optimiser over [textures, light_pow], src/svbrdf.py:50).
     const AdamScalars ad = *light_adam;
-    for (int mi = w; mi < hdr->n_mat; mi += nwarps) {
+    for (int mi = w; mi < hdr->n_mat; mi += nw) {
       const MatDesc& md = mats[mi];
       if (!md.lstate) continue;
       double g[3] = {0.0, 0.0, 0.0};
-      const int e0 = mat_tiles[mi] * per_tile, e1 = mat_tiles[mi + 1] * per_tile;
-      for (int t = e0 + lane; t < e1; t += 32) {
+      for (int t = mat_tiles[mi] + lane; t < mat_tiles[mi + 1]; t += 32) {
 #pragma unroll
-        for (int c = 0; c < 3; ++c) g[c] += (double)__ldcg(lpart + 3 * (size_t)t + c);
+        for (int c = 0; c < 3; ++c) g[c] += (double)__ldcg(tile_tot + (size_t)(kFuseMax + c) * n_tiles + t);
       }
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
@@ -1117,7 +1147,6 @@ batched_pair_kernel(const char* __restrict__ plan, AdamHyper hyper, int* __restr
 // single-buffered: the producer reloads it once every consumer warp has signalled it done
 // with the tile (state_empty), after a proxy fence orders their shared-memory writes before
 // the bulk copies. Waits, error recording and draining follow variant 2.
-constexpr int kFuseMax = 32;
 constexpr int kStatePlanes = 27;
 constexpr size_t kFuseBudget = 220 * 1024;
 constexpr size_t kFuseBudgetTwoCta = 100 * 1024;
@@ -2322,7 +2351,10 @@ size_t svbrdf_batched_workspace_bytes(const void* host_plan) {
   if (!host_plan) return 0;
   const PlanHeader* h = (const PlanHeader*)host_plan;
   if (h->magic != kPlanMagic) return 0;
-  return kWsLossOffset + sizeof(float) * ws_loss_floats(h) + (h->light ? sizeof(float) * 3 * ws_slots(h) : 0);
+  // loss partials, light partials, then the per-(iteration, tile) totals (kFuseMax rows) and
+  // the per-tile light totals (3 rows)
+  return kWsLossOffset + sizeof(float) * ws_loss_floats(h) + (h->light ? sizeof(float) * 3 * ws_slots(h) : 0) +
+         sizeof(float) * (size_t)h->n_tiles * (kFuseMax + 3);
 }
 
 int svbrdf_selftest_wait_timeout(void* workspace, size_t workspace_bytes, int limit, void* stream) {

@@ -254,7 +254,8 @@ class _ConvTF32(torch.autograd.Function):
         (w_dg,) = ctx.saved_tensors
         b, c, h, wd, coutp, cout, k, pad, ho, wo = ctx.geom
         if coutp != cout:
-            gp = torch.zeros(b, coutp, ho, wo, device=gy.device, dtype=torch.float32, memory_format=CL)
+            gp = torch.empty(b, coutp, ho, wo, device=gy.device, dtype=torch.float32, memory_format=CL)
+            gp[:, cout:].zero_()
             gp[:, :cout] = gy
             gy = gp
         gy = _cl(gy)

@@ -15,7 +15,7 @@ SvbrdfOptim.optim loop (src/svbrdf.py:44-83) and Microfacet.eval (src/microfacet
   max(1e-4, twice that error) for the moments (a texel near a clamp of the render can take a
   slightly different path in FP32 than in FP64; the reference's own FP32 loop does too);
 * every loss of one whole 256^2 material (all its texels through the oracle, 100 iterations)
-  within 1e-5 relative;
+  within max(1e-5, twice the reference's own FP32 loop's error on that material) relative;
 * the first iteration's loss of one material of each resolution, every texel through the
   oracle, within 1e-5 relative (the reduction over tiles, warps and CTAs at full size);
 * all 100 losses of every material against the single-material fused kernel (a different
@@ -106,6 +106,12 @@ def workload(svb, cuda):
                            m.camera_pos.cpu(), m.light_pos.cpu(), m.light_pow.cpu(), m.n_views * 3 * T, ITERS, LR,
                            "log1p", torch.float64)
     whole_loss = (whole["sq_err"].sum(1) / (m.n_views * 3 * T)).tolist()
+    # the reference's own FP32 arithmetic on the same material: the floor of the loss check
+    whole32 = R.optim_texels(m.init.cpu().reshape(9, -1), ax, ay, m.targets.cpu().reshape(m.n_views, 3, -1),
+                             m.camera_pos.cpu(), m.light_pos.cpu(), m.light_pow.cpu(), m.n_views * 3 * T, ITERS, LR,
+                             "log1p", torch.float32)
+    whole32_loss = (whole32["sq_err"].double().sum(1) / (m.n_views * 3 * T)).tolist()
+    e32_whole = max(abs(a - b) / b for a, b in zip(whole32_loss, whole_loss))
     # the first loss of one material of each resolution, every texel
     first = {}
     for res in (256, 512, 1024):
@@ -132,7 +138,7 @@ def workload(svb, cuda):
         o.optim(ITERS, LR, None, False)
         single.append(o.loss_image_list)
     return {"mats": mats, "idxs": idxs, "o64": o64, "o32": o32, "small": small, "whole": whole,
-            "whole_loss": whole_loss, "first": first, "single": single}
+            "whole_loss": whole_loss, "e32_whole": e32_whole, "first": first, "single": single}
 
 
 def _col_ranges(idxs):
@@ -171,9 +177,11 @@ def test_bench_workload_matches_oracle(svb, cuda, workload, variant):
     s = workload["small"]
     e_whole = max(abs(float(hist[it, s]) - workload["whole_loss"][it]) / workload["whole_loss"][it]
                   for it in range(ITERS))
-    print(f"variant {variant}: losses vs single-material kernel {e_single:.2e}, whole material vs FP64 {e_whole:.2e}")
+    e32 = workload["e32_whole"]
+    print(f"variant {variant}: losses vs single-material kernel {e_single:.2e}, whole material vs FP64 {e_whole:.2e} "
+          f"(the reference's FP32 loop {e32:.2e})")
     assert e_single <= 5e-5
-    assert e_whole <= 1e-5
+    assert e_whole <= max(1e-5, 2 * e32)
     for k in ("textures", "exp_avg", "exp_avg_sq"):
         ref = workload["whole"][k]
         got = {"textures": b.tex, "exp_avg": b.m1, "exp_avg_sq": b.m2}[k][s].reshape(9, -1)

@@ -295,6 +295,18 @@ int svbrdf_desc_gram_finish(const float* partial, int splits, int v, int c, int 
 int svbrdf_desc_gemm_nt(const void* a, const void* b, float* out, int batch, int m, int n, int k, int* err,
                         void* stream);
 
+/* The Gram gradient dF = F dG with the feature term of the same hook in its epilogue (the
+ * reference's feature + Gram loss of one hooked layer, src/descriptor.py:39-60, 77-79): per
+ * element of the [batch * m, n] maps, d = f - t, g = coef d + dF, times (f > 0) if `mask`,
+ * stored BF16 (as svbrdf_desc_feat_loss with gram_grad = dF, which then never reaches memory);
+ * partial[i] (i < svbrdf_desc_gemm_nt_feat_partials(batch, m, n)) = a fixed-order share of
+ * sum d^2. a = the hook's BF16 features [batch][m][k = n], b = dG BF16 [batch][n][n]; f is the
+ * same map as a (f_is_bf16) or its FP32 original; t FP32. Shapes as svbrdf_desc_gemm_nt. */
+long long svbrdf_desc_gemm_nt_feat_partials(int batch, int m, int n);
+int svbrdf_desc_gemm_nt_feat(const void* a, const void* b, const void* f, int f_is_bf16, const float* t, float coef,
+                             int mask, void* g, float* partial, int batch, int m, int n, int k, int* err,
+                             void* stream);
+
 /* ---- MaterialGAN generator: 2x up-sampling of its feature maps and skip images (the
  * reference's generator, src/higan_models/*, up-samples by zero insertion and a [1,3,3,1]
  * FIR; src/materialgan.py:91-173 runs it in the latent loop) ---- */

@@ -150,6 +150,10 @@ def _declare(L):
     L.svbrdf_desc_gram_finish.argtypes = [P, I, I, I, I, P, F, P, P, P, P]
     L.svbrdf_desc_gemm_nt.restype = I
     L.svbrdf_desc_gemm_nt.argtypes = [P, P, P, I, I, I, I, P, P]
+    L.svbrdf_desc_gemm_nt_feat_partials.restype = ctypes.c_longlong
+    L.svbrdf_desc_gemm_nt_feat_partials.argtypes = [I, I, I]
+    L.svbrdf_desc_gemm_nt_feat.restype = I
+    L.svbrdf_desc_gemm_nt_feat.argtypes = [P, P, P, I, P, F, I, P, P, I, I, I, I, P, P]
     L.svbrdf_gen_conv_tf32.restype = I
     L.svbrdf_gen_conv_tf32.argtypes = [P, P, P, I, I, I, I, I, I, I, P, P]
     L.svbrdf_gen_upsample2.restype = I
@@ -206,7 +210,8 @@ EXPORTS = [
     "svbrdf_conv3x3_bf16_ex", "svbrdf_desc_partials", "svbrdf_desc_conv1_fwd", "svbrdf_desc_conv1_bwd",
     "svbrdf_desc_pool_fwd", "svbrdf_desc_pool_bwd", "svbrdf_desc_avgpool_fwd", "svbrdf_desc_avgpool_bwd",
     "svbrdf_desc_feat_loss", "svbrdf_desc_gram_splits", "svbrdf_desc_gram", "svbrdf_desc_gram_finish",
-    "svbrdf_desc_gemm_nt", "svbrdf_gen_upsample2",
+    "svbrdf_desc_gemm_nt", "svbrdf_desc_gemm_nt_feat_partials", "svbrdf_desc_gemm_nt_feat",
+    "svbrdf_gen_upsample2",
     "svbrdf_gen_upsample2_bwd", "svbrdf_gen_upsample2_scaled", "svbrdf_gen_scale", "svbrdf_gen_scale_bwd", "svbrdf_gen_act", "svbrdf_gen_act_bwd",
     "svbrdf_gen_nhwc_partial_floats", "svbrdf_gen_upsample2_nhwc", "svbrdf_gen_upsample2_nhwc_bwd",
     "svbrdf_gen_scale_nhwc", "svbrdf_gen_scale_nhwc_bwd", "svbrdf_gen_act_nhwc", "svbrdf_gen_act_nhwc_bwd",

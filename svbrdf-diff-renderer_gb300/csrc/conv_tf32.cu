@@ -7,14 +7,18 @@
 // shared-weight convolution (input channels scaled by the style before it, output channels by
 // the demodulation after it, in the elementwise kernels of gen_nhwc.cu), so each layer's
 // convolution is one implicit GEMM:
-//   M = 128 output pixels: a TH x TW patch of NB images (16 x 8 of one image for maps of 16
-//       and more columns; 8 x 8 x 2 images and 4 x 4 x 8 images for the 8^2 and 4^2 maps),
+//   M = 128 output pixels per M-tile: a TH x TW patch of NB images (16 x 8 of one image for
+//       maps of 16 and more columns; 8 x 8 x 2 images and 4 x 4 x 8 images for the 8^2 and
+//       4^2 maps); a CTA tile stacks MT = 2 M-tiles along y where Cout <= 128 and the map has
+//       16+ rows, so each weight slice staged in shared memory feeds 256 pixels,
 //   N = BN output channels, K = taps x Cin, consumed 32 channels (128 bytes of FP32) at a time.
-// For each (tap, 32-channel chunk) the producer warp TMA-loads the shifted input patch (taps
-// that fall outside the map read the TMA zero fill, which is the zero padding) and the
-// BN x 32 weight slice, 128-byte swizzled, into a ring of shared-memory stages; one thread
-// issues tcgen05.mma kind::tf32 (K = 8 per instruction) into a 128 x BN FP32 accumulator in
-// TMEM; four epilogue warps read it with tcgen05.ld and store FP32 NHWC.
+// The kernel is persistent (one CTA per SM walking the tiles i, i + grid, ...). For each
+// (tap, 32-channel chunk) the producer warp TMA-loads the MT shifted input patches (taps that
+// fall outside the map read the TMA zero fill, which is the zero padding) and the BN x 32
+// weight slice, 128-byte swizzled, into a ring of shared-memory stages that runs on across
+// tiles; one thread issues tcgen05.mma kind::tf32 (K = 8 per instruction) into MT 128 x BN
+// FP32 accumulators in TMEM, double-buffered, so four epilogue warps drain tile j (tcgen05.ld,
+// FP32 NHWC stores) while the MMAs of tile j + 1 run.
 //
 // `pad` is the input offset of the first tap: 1 for the same-padded 3x3 convolutions, 0 for
 // the valid 3x3 convolution of the up-sampling layers (whose input is the up-sampled map with
@@ -59,30 +63,52 @@ __device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t a, uint64_t b
 
 struct Geom {
   int B, Hin, Win, Cin, Ho, Wo, Cout;
-  int TH, TW, NB;  // output patch of one CTA: NB images x TH rows x TW columns = 128 pixels
+  int TH, TW, NB;  // one M-tile: NB images x TH rows x TW columns = 128 output pixels
   int pad, taps;
+  int tiles_x, tiles_y, tiles_b, tiles_n;  // CTA tiles along x, y (TH * MT rows), images, Cout / BN
 };
 
-template <int BN, int STAGES>
+// One CTA tile: MT M-tiles stacked along y (MT * TH rows) x BN output channels.
+struct TileCoord {
+  int b0, y0, x0, n0;
+};
+template <int BN, int MT>
+__device__ __forceinline__ TileCoord tile_coord(const Geom& g, int t) {
+  TileCoord c;
+  const int nb = t % g.tiles_n;
+  int r = t / g.tiles_n;  // consecutive tiles share the input patch (one per Cout block)
+  c.x0 = (r % g.tiles_x) * g.TW;
+  r /= g.tiles_x;
+  c.y0 = (r % g.tiles_y) * (g.TH * MT);
+  c.b0 = (r / g.tiles_y) * g.NB;
+  c.n0 = nb * BN;
+  return c;
+}
+
+// Persistent: grid = min(tiles, SMs); CTA i runs tiles i, i + grid, ... The producer's ring
+// runs across tile boundaries, and the accumulator is double-buffered in TMEM (2 x MT x BN
+// columns), so the epilogue of tile j overlaps the MMAs of tile j + 1.
+template <int BN, int MT, int STAGES>
 __global__ void __launch_bounds__(kThreads, 1)
 conv_tf32_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_constant__ CUtensorMap tmap_w,
                  float* __restrict__ y, Geom g, int* err) {
   constexpr int A_BYTES = BM * BK * 4;
   constexpr int B_BYTES = BN * BK * 4;
-  constexpr int STAGE = A_BYTES + B_BYTES;
+  constexpr int STAGE = MT * A_BYTES + B_BYTES;
+  constexpr uint32_t ACC_COLS = MT * BN;          // one tile's accumulators
+  constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;    // double-buffered
+  static_assert(TMEM_COLS >= 32 && TMEM_COLS <= 512 && (TMEM_COLS & (TMEM_COLS - 1)) == 0, "TMEM columns");
   extern __shared__ uint8_t dsmem[];
   __shared__ __align__(8) uint64_t full_bar[STAGES];
   __shared__ __align__(8) uint64_t empty_bar[STAGES];
-  __shared__ __align__(8) uint64_t acc_bar;
+  __shared__ __align__(8) uint64_t tfull_bar[2];   // accumulator buffer ready (MMA commit)
+  __shared__ __align__(8) uint64_t tempty_bar[2];  // accumulator buffer drained (4 epilogue warps)
+  __shared__ __align__(8) uint64_t done_bar;       // every MMA of this CTA complete
   __shared__ uint32_t tmem_slot;
 
   const uint32_t base = (smem_u32(dsmem) + 1023u) & ~1023u;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int tiles_x = (g.Wo + g.TW - 1) / g.TW, tiles_y = (g.Ho + g.TH - 1) / g.TH;
-  const int tb = blockIdx.x / (tiles_x * tiles_y);
-  const int trem = blockIdx.x % (tiles_x * tiles_y);
-  const int b0 = tb * g.NB, y0 = (trem / tiles_x) * g.TH, x0 = (trem % tiles_x) * g.TW;
-  const int n0 = blockIdx.y * BN;
+  const int n_tiles = g.tiles_b * g.tiles_y * g.tiles_x * g.tiles_n;
   const int kchunks = g.Cin / BK;
   const int total = g.taps * kchunks;
   const int ks = g.taps == 9 ? 3 : 1;
@@ -92,12 +118,16 @@ conv_tf32_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_consta
       mbar_init(smem_u32(&full_bar[s]), 1);
       mbar_init(smem_u32(&empty_bar[s]), 1);
     }
-    mbar_init(smem_u32(&acc_bar), 1);
+    for (int a = 0; a < 2; ++a) {
+      mbar_init(smem_u32(&tfull_bar[a]), 1);
+      mbar_init(smem_u32(&tempty_bar[a]), 4);
+    }
+    mbar_init(smem_u32(&done_bar), 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
-                 "r"((uint32_t)BN)
+                 "r"(TMEM_COLS)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -108,22 +138,31 @@ conv_tf32_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_consta
 
   if (warp == 0) {
     if (lane == 0) {
-      int issued = 0;
-      for (int i = 0; i < total; ++i) {
-        const int s = i % STAGES;
-        const uint32_t ph = (uint32_t)(i / STAGES) & 1u;
-        if (i >= STAGES && !mbar_wait(smem_u32(&empty_bar[s]), ph ^ 1u, err, kErrTma)) break;
-        const int tap = i / kchunks, cc = i % kchunks;
-        const int dy = tap / ks - g.pad, dx = tap % ks - g.pad;
-        const uint32_t st = base + (uint32_t)(s * STAGE);
-        const uint32_t fb = smem_u32(&full_bar[s]);
-        mbar_expect_tx(fb, (uint32_t)STAGE);
-        tma_4d(st, &tmap_x, cc * BK, x0 + dx, y0 + dy, b0, fb);
-        tma_2d(st + A_BYTES, &tmap_w, tap * g.Cin + cc * BK, n0, fb);
-        ++issued;
+      int q = 0;  // stages issued by this CTA
+      bool bad = false;
+      for (int t = blockIdx.x; t < n_tiles && !bad; t += gridDim.x) {
+        const TileCoord c = tile_coord<BN, MT>(g, t);
+        for (int i = 0; i < total; ++i) {
+          const int s = q % STAGES;
+          const uint32_t ph = (uint32_t)(q / STAGES) & 1u;
+          if (q >= STAGES && !mbar_wait(smem_u32(&empty_bar[s]), ph ^ 1u, err, kErrTma)) {
+            bad = true;
+            break;
+          }
+          const int tap = i / kchunks, cc = i % kchunks;
+          const int dy = tap / ks - g.pad, dx = tap % ks - g.pad;
+          const uint32_t st = base + (uint32_t)(s * STAGE);
+          const uint32_t fb = smem_u32(&full_bar[s]);
+          mbar_expect_tx(fb, (uint32_t)STAGE);
+#pragma unroll
+          for (int mt = 0; mt < MT; ++mt)
+            tma_4d(st + (uint32_t)(mt * A_BYTES), &tmap_x, cc * BK, c.x0 + dx, c.y0 + mt * g.TH + dy, c.b0, fb);
+          tma_2d(st + (uint32_t)(MT * A_BYTES), &tmap_w, tap * g.Cin + cc * BK, c.n0, fb);
+          ++q;
+        }
       }
-      if (issued < total) {
-        for (int i = issued > STAGES ? issued - STAGES : 0; i < issued; ++i) {
+      if (bad) {  // let the copies in flight land before the CTA can exit
+        for (int i = q > STAGES ? q - STAGES : 0; i < q; ++i) {
           uint32_t it = 0;
           while (!mbar_try(smem_u32(&full_bar[i % STAGES]), (uint32_t)(i / STAGES) & 1u) && ++it < kSpin) {
           }
@@ -133,62 +172,103 @@ conv_tf32_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_consta
   } else if (warp == 1) {
     if (lane == 0) {
       constexpr uint32_t id = idesc_tf32(BM, BN);
-      for (int i = 0; i < total; ++i) {
-        const int s = i % STAGES;
-        const uint32_t ph = (uint32_t)(i / STAGES) & 1u;
-        if (!mbar_wait(smem_u32(&full_bar[s]), ph, err, kErrMma)) break;
+      int q = 0, j = 0;
+      bool bad = false;
+      for (int t = blockIdx.x; t < n_tiles && !bad; t += gridDim.x, ++j) {
+        const int a = j & 1;
+        // the epilogue must have drained this buffer's previous tile (j - 2)
+        if (j >= 2 && !mbar_wait(smem_u32(&tempty_bar[a]), ((uint32_t)(j >> 1) & 1u) ^ 1u, err, kErrMma)) break;
         fence_after();
-        const uint32_t a = base + (uint32_t)(s * STAGE);
-        const uint32_t b = a + A_BYTES;
+        const uint32_t acc = tmem + (uint32_t)a * ACC_COLS;
+        for (int i = 0; i < total; ++i, ++q) {
+          const int s = q % STAGES;
+          const uint32_t ph = (uint32_t)(q / STAGES) & 1u;
+          if (!mbar_wait(smem_u32(&full_bar[s]), ph, err, kErrMma)) {
+            bad = true;
+            break;
+          }
+          fence_after();
+          const uint32_t sa = base + (uint32_t)(s * STAGE);
+          const uint32_t sb = sa + (uint32_t)(MT * A_BYTES);
 #pragma unroll
-        for (int k = 0; k < BK / 8; ++k)  // 8 TF32 channels = 32 bytes per MMA
-          mma_tf32(tmem, sw128_desc(a + 32u * k), sw128_desc(b + 32u * k), id, (i > 0 || k > 0) ? 1u : 0u);
-        mma_commit(smem_u32(&empty_bar[s]));
+          for (int k = 0; k < BK / 8; ++k) {  // 8 TF32 channels = 32 bytes per MMA
+#pragma unroll
+            for (int mt = 0; mt < MT; ++mt)
+              mma_tf32(acc + (uint32_t)(mt * BN), sw128_desc(sa + (uint32_t)(mt * A_BYTES) + 32u * k),
+                       sw128_desc(sb + 32u * k), id, (i > 0 || k > 0) ? 1u : 0u);
+          }
+          mma_commit(smem_u32(&empty_bar[s]));
+        }
+        if (!bad) mma_commit(smem_u32(&tfull_bar[a]));
       }
-      mma_commit(smem_u32(&acc_bar));  // also on abort, so TMEM is idle before it is freed
+      mma_commit(smem_u32(&done_bar));  // also on abort, so TMEM is idle before it is freed
     }
   } else {
-    const int q = warp & 3;
-    const int m = q * 32 + lane;
-    const int pb = b0 + m / (g.TH * g.TW);
-    const int rem = m % (g.TH * g.TW);
-    const int py = y0 + rem / g.TW, px = x0 + rem % g.TW;
-    const bool inside = pb < g.B && py < g.Ho && px < g.Wo;
-    const bool ok = __all_sync(0xffffffffu, mbar_wait(smem_u32(&acc_bar), 0u, err, kErrEpi)) &&
-                    *(volatile int*)err == 0;
-    fence_after();
-    if (ok) {
-      float* out = y + (((size_t)pb * g.Ho + py) * g.Wo + px) * g.Cout + n0;
-#pragma unroll 1
-      for (int c0 = 0; c0 < BN; c0 += 32) {
-        uint32_t r[32];
-        tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, r);
-        if (inside) {
-          float4* o4 = reinterpret_cast<float4*>(out + c0);
+    const int qw = warp & 3;  // TMEM lanes 32 qw .. 32 qw + 31
+    const int m = qw * 32 + lane;
+    int j = 0;
+    for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, ++j) {
+      const int a = j & 1;
+      const bool ok = __all_sync(0xffffffffu, mbar_wait(smem_u32(&tfull_bar[a]), (uint32_t)(j >> 1) & 1u, err,
+                                                        kErrEpi)) &&
+                      *(volatile int*)err == 0;
+      fence_after();
+      if (!ok) break;
+      const TileCoord c = tile_coord<BN, MT>(g, t);
+      const int pb = c.b0 + m / (g.TH * g.TW);
+      const int rem = m % (g.TH * g.TW);
+      const int px = c.x0 + rem % g.TW;
 #pragma unroll
-          for (int u = 0; u < 8; ++u)
-            o4[u] = make_float4(__uint_as_float(r[4 * u]), __uint_as_float(r[4 * u + 1]),
-                                __uint_as_float(r[4 * u + 2]), __uint_as_float(r[4 * u + 3]));
+      for (int mt = 0; mt < MT; ++mt) {
+        const int py = c.y0 + mt * g.TH + rem / g.TW;
+        const bool inside = pb < g.B && py < g.Ho && px < g.Wo;
+        float* out = y + (((size_t)pb * g.Ho + py) * g.Wo + px) * g.Cout + c.n0;
+#pragma unroll 1
+        for (int c0 = 0; c0 < BN; c0 += 32) {
+          uint32_t r[32];
+          tmem_ld32(tmem + ((uint32_t)(qw * 32) << 16) + (uint32_t)(a * ACC_COLS + mt * BN + c0), r);
+          if (inside) {
+            float4* o4 = reinterpret_cast<float4*>(out + c0);
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+              o4[u] = make_float4(__uint_as_float(r[4 * u]), __uint_as_float(r[4 * u + 1]),
+                                  __uint_as_float(r[4 * u + 2]), __uint_as_float(r[4 * u + 3]));
+          }
         }
       }
+      fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(smem_u32(&tempty_bar[a]));
     }
   }
   fence_before();
   __syncthreads();
   if (warp == 1) {
     uint32_t it = 0;
-    while (!mbar_try(smem_u32(&acc_bar), 0u) && ++it < kSpin) {
+    while (!mbar_try(smem_u32(&done_bar), 0u) && ++it < kSpin) {
     }
     fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)BN) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
   }
 }
 
-template <int BN, int STAGES>
-static int launch(const CUtensorMap& mx, const CUtensorMap& mw, float* y, const Geom& g, int* err, cudaStream_t st) {
+constexpr size_t kStageBudget = 200 * 1024;  // ring bytes per CTA (one CTA per SM)
+
+template <int BN, int MT>
+constexpr int stages_for() {
+  return (int)(kStageBudget / (size_t)(MT * BM * BK * 4 + BN * BK * 4)) < 8
+             ? (int)(kStageBudget / (size_t)(MT * BM * BK * 4 + BN * BK * 4))
+             : 8;
+}
+
+template <int BN, int MT>
+static int launch(const CUtensorMap& mx, const CUtensorMap& mw, float* y, Geom g, int* err, cudaStream_t st) {
+  constexpr int STAGES = stages_for<BN, MT>();
+  static_assert(STAGES >= 3, "ring too shallow");
   static std::atomic<size_t> have[64];
-  const size_t smem = (size_t)STAGES * (BM * BK * 4 + BN * BK * 4) + 1024;
-  auto kern = conv_tf32_kernel<BN, STAGES>;
+  static std::atomic<int> sms[64];
+  const size_t smem = (size_t)STAGES * (MT * BM * BK * 4 + BN * BK * 4) + 1024;
+  auto kern = conv_tf32_kernel<BN, MT, STAGES>;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return fail(SVBRDF_ERR_CUDA, "no usable device");
   if (have[dev].load() < smem) {
@@ -196,8 +276,19 @@ static int launch(const CUtensorMap& mx, const CUtensorMap& mw, float* y, const 
       return fail(SVBRDF_ERR_CUDA, "cudaFuncSetAttribute: %s", cudaGetErrorString(cudaGetLastError()));
     have[dev].store(smem);
   }
-  const long long tiles = (long long)((g.B + g.NB - 1) / g.NB) * ((g.Ho + g.TH - 1) / g.TH) * ((g.Wo + g.TW - 1) / g.TW);
-  dim3 grid((unsigned)tiles, (unsigned)(g.Cout / BN));
+  if (sms[dev].load() == 0) {
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1)
+      return fail(SVBRDF_ERR_CUDA, "no SM count");
+    sms[dev].store(n);
+  }
+  g.tiles_x = (g.Wo + g.TW - 1) / g.TW;
+  g.tiles_y = (g.Ho + g.TH * MT - 1) / (g.TH * MT);
+  g.tiles_b = (g.B + g.NB - 1) / g.NB;
+  g.tiles_n = g.Cout / BN;
+  const long long tiles = (long long)g.tiles_b * g.tiles_y * g.tiles_x * g.tiles_n;
+  if (tiles >= (1LL << 31)) return fail(SVBRDF_ERR_UNSUPPORTED, "conv_tf32: too many tiles");
+  const int grid = (int)(tiles < sms[dev].load() ? tiles : sms[dev].load());
   kern<<<grid, kThreads, smem, st>>>(mx, mw, y, g, err);
   return check_launch("conv_tf32_kernel");
 }
@@ -256,10 +347,13 @@ extern "C" int svbrdf_gen_conv_tf32(const float* x, const float* weight, float* 
     if (r != CUDA_SUCCESS) return fail(SVBRDF_ERR_CUDA, "cuTensorMapEncodeTiled(weight) failed: %d", (int)r);
   }
   cudaStream_t st = (cudaStream_t)stream;
+  // two M-tiles per CTA tile (one weight slice feeds 256 output pixels) where the map has 16+
+  // rows and Cout fits two double-buffered accumulators in TMEM
+  const bool two = g.NB == 1 && g.Ho >= 16 && bn <= 128;
   switch (bn) {
-    case 256: return launch<256, 4>(mx, mw, y, g, err, st);
-    case 128: return launch<128, 5>(mx, mw, y, g, err, st);
-    case 64: return launch<64, 6>(mx, mw, y, g, err, st);
-    default: return launch<32, 6>(mx, mw, y, g, err, st);
+    case 256: return launch<256, 1>(mx, mw, y, g, err, st);
+    case 128: return two ? launch<128, 2>(mx, mw, y, g, err, st) : launch<128, 1>(mx, mw, y, g, err, st);
+    case 64: return two ? launch<64, 2>(mx, mw, y, g, err, st) : launch<64, 1>(mx, mw, y, g, err, st);
+    default: return two ? launch<32, 2>(mx, mw, y, g, err, st) : launch<32, 1>(mx, mw, y, g, err, st);
   }
 }

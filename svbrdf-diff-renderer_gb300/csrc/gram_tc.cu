@@ -202,12 +202,25 @@ gram_finish_kernel(const float* __restrict__ partial, int splits, int C, float i
   }
 }
 
+// The feature term fused into the Gram gradient's epilogue (FUSE): per element of row r,
+// channel n of the [batch * m, n] maps, d = f - t, g = coef d + (F dG)[r][n], times (f > 0)
+// if `mask`, stored BF16; each epilogue warp's sum of d^2 goes to partial[cta * 4 + warp].
+struct FeatEpi {
+  const void* f;  // the hook's features, BF16 or FP32
+  int f_bf16;
+  const float* t;  // target features
+  float coef;
+  int mask;
+  __nv_bfloat16* g;  // the loss gradient at the hook
+  float* partial;
+};
+
 // out[b][m][n] = sum_k A[b][m][k] B[b][n][k]; grid (batch * m / 128, n / BN). A: rows
 // b * m + r of a [batch * m, k] map; B: rows b * n + r of a [batch * n, k] map.
-template <int BN, int STAGES>
+template <int BN, int STAGES, bool FUSE>
 __global__ void __launch_bounds__(kThreads, 1)
 gemm_nt_kernel(const __grid_constant__ CUtensorMap tmap_a, const __grid_constant__ CUtensorMap tmap_b,
-               float* __restrict__ out, int M, int Nn, int K, int* err) {
+               float* __restrict__ out, int M, int Nn, int K, int* err, FeatEpi fe) {
   constexpr int A_BYTES = 128 * 64 * 2;
   constexpr int B_BYTES = BN * 64 * 2;
   constexpr int STAGE = A_BYTES + B_BYTES;
@@ -282,7 +295,68 @@ gemm_nt_kernel(const __grid_constant__ CUtensorMap tmap_a, const __grid_constant
     const bool ok = __all_sync(0xffffffffu, mbar_wait(smem_u32(&acc_bar), 0u, err, kErrEpi)) &&
                     *(volatile int*)err == 0;
     fence_after();
-    if (ok) {
+    if (FUSE) {
+      const size_t off = ((size_t)b * M + m) * Nn + n0;
+      float acc = 0.0f;
+      if (ok) {
+#pragma unroll 1
+        for (int c0 = 0; c0 < BN; c0 += 32) {
+          uint32_t r[32];
+          tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, r);
+          float fv[32];
+          if (fe.f_bf16) {
+            const uint4* fp = reinterpret_cast<const uint4*>(reinterpret_cast<const __nv_bfloat16*>(fe.f) + off + c0);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              const uint4 v4 = __ldg(fp + u);
+              const __nv_bfloat162* h2 = reinterpret_cast<const __nv_bfloat162*>(&v4);
+#pragma unroll
+              for (int e = 0; e < 4; ++e) {
+                const float2 f2 = __bfloat1622float2(h2[e]);
+                fv[8 * u + 2 * e] = f2.x;
+                fv[8 * u + 2 * e + 1] = f2.y;
+              }
+            }
+          } else {
+            const float4* fp = reinterpret_cast<const float4*>(reinterpret_cast<const float*>(fe.f) + off + c0);
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+              const float4 v4 = __ldg(fp + u);
+              fv[4 * u] = v4.x;
+              fv[4 * u + 1] = v4.y;
+              fv[4 * u + 2] = v4.z;
+              fv[4 * u + 3] = v4.w;
+            }
+          }
+          const float4* tp = reinterpret_cast<const float4*>(fe.t + off + c0);
+          uint32_t packed[16];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            const float4 t4 = __ldg(tp + u);
+            const float tv[4] = {t4.x, t4.y, t4.z, t4.w};
+            float gv[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              const int j = 4 * u + e;
+              const float d = fv[j] - tv[e];
+              acc = fmaf(d, d, acc);
+              gv[e] = fe.mask && !(fv[j] > 0.0f) ? 0.0f : fmaf(fe.coef, d, __uint_as_float(r[j]));
+            }
+            __nv_bfloat162 h0 = __floats2bfloat162_rn(gv[0], gv[1]);
+            __nv_bfloat162 h1 = __floats2bfloat162_rn(gv[2], gv[3]);
+            packed[2 * u] = *reinterpret_cast<uint32_t*>(&h0);
+            packed[2 * u + 1] = *reinterpret_cast<uint32_t*>(&h1);
+          }
+          uint4* gp = reinterpret_cast<uint4*>(fe.g + off + c0);
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+            gp[u] = make_uint4(packed[4 * u], packed[4 * u + 1], packed[4 * u + 2], packed[4 * u + 3]);
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      if (lane == 0) fe.partial[((size_t)blockIdx.y * gridDim.x + blockIdx.x) * 4 + q] = acc;
+    } else if (ok) {
       float* o = out + ((size_t)b * M + m) * Nn + n0;
 #pragma unroll 1
       for (int c0 = 0; c0 < BN; c0 += 32) {
@@ -344,17 +418,50 @@ static int launch_gram(const CUtensorMap& m, float* partial, int v, int s, int c
   return check_launch("gram_kernel");
 }
 
-template <int BN, int STAGES>
+template <int BN, int STAGES, bool FUSE>
 static int launch_gemm(const CUtensorMap& ma, const CUtensorMap& mb, float* out, int batch, int m, int n, int k,
-                       int* err, cudaStream_t st) {
+                       int* err, const FeatEpi& fe, cudaStream_t st) {
   static std::atomic<size_t> have[64];
   const size_t smem = (size_t)STAGES * (128 * 64 * 2 + BN * 64 * 2) + 1024;
-  auto kern = gemm_nt_kernel<BN, STAGES>;
+  auto kern = gemm_nt_kernel<BN, STAGES, FUSE>;
   int rc = allow(kern, smem, have);
   if (rc) return rc;
   dim3 grid((unsigned)(batch * (m / 128)), (unsigned)(n / BN));
-  kern<<<grid, kThreads, smem, st>>>(ma, mb, out, m, n, k, err);
+  kern<<<grid, kThreads, smem, st>>>(ma, mb, out, m, n, k, err, fe);
   return check_launch("gemm_nt_kernel");
+}
+
+// Shared by svbrdf_desc_gemm_nt (FUSE false, out) and svbrdf_desc_gemm_nt_feat (FUSE true, fe).
+template <bool FUSE>
+static int gemm_nt_entry(const void* a, const void* b, float* out, int batch, int m, int n, int k, int* err,
+                         const FeatEpi& fe, void* stream) {
+  if (!a || !b || !err || (!FUSE && !out)) return fail(SVBRDF_ERR_INVALID, "gemm_nt: null a/b/out/err");
+  if (FUSE && (!fe.f || !fe.t || !fe.g || !fe.partial)) return fail(SVBRDF_ERR_INVALID, "gemm_nt_feat: null f/t/g/partial");
+  if (batch < 1 || m < 128 || m % 128 || k < 64 || k % 64 || (n != 64 && n != 128 && n % 256))
+    return fail(SVBRDF_ERR_UNSUPPORTED, "gemm_nt: m %% 128, k %% 64 and n in {64, 128, 256 x j} needed");
+  if ((long long)batch * m >= (1LL << 31) || (long long)batch * n >= (1LL << 31) || k > 65536)
+    return fail(SVBRDF_ERR_UNSUPPORTED, "gemm_nt: too large");
+  if ((long long)batch * (m / 128) > 0x7fffffffLL || n / (n >= 256 ? 256 : n) > 65535)
+    return fail(SVBRDF_ERR_UNSUPPORTED, "gemm_nt: grid too large");
+  if (((uintptr_t)a | (uintptr_t)b | (uintptr_t)out | (uintptr_t)fe.f | (uintptr_t)fe.t | (uintptr_t)fe.g) % 16)
+    return fail(SVBRDF_ERR_INVALID, "gemm_nt: 16-byte alignment");
+  CUtensorMap ma, mb;
+  const int bn = n >= 256 ? 256 : n;
+  int rc = encode_2d(&ma, a, (uint64_t)k, (uint64_t)batch * m, 64, 128);
+  if (rc) return rc;
+  rc = encode_2d(&mb, b, (uint64_t)k, (uint64_t)batch * n, 64, (uint32_t)bn);
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (k <= 128) {
+    // one or two k-steps per tile: a 2-stage ring keeps the CTA small (49-97 KB), so several
+    // CTAs share an SM and one's set-up and epilogue overlap another's loads and MMAs
+    if (bn == 64) return launch_gemm<64, 2, FUSE>(ma, mb, out, batch, m, n, k, err, fe, st);
+    if (bn == 128) return launch_gemm<128, 2, FUSE>(ma, mb, out, batch, m, n, k, err, fe, st);
+    return launch_gemm<256, 2, FUSE>(ma, mb, out, batch, m, n, k, err, fe, st);
+  }
+  if (bn == 64) return launch_gemm<64, 6, FUSE>(ma, mb, out, batch, m, n, k, err, fe, st);
+  if (bn == 128) return launch_gemm<128, 5, FUSE>(ma, mb, out, batch, m, n, k, err, fe, st);
+  return launch_gemm<256, 4, FUSE>(ma, mb, out, batch, m, n, k, err, fe, st);
 }
 
 }  // namespace gram
@@ -409,25 +516,20 @@ int svbrdf_desc_gram_finish(const float* partial, int splits, int v, int c, int 
 
 int svbrdf_desc_gemm_nt(const void* a, const void* b, float* out, int batch, int m, int n, int k, int* err,
                         void* stream) {
-  using namespace svb::gram;
-  if (!a || !b || !out || !err) return fail(SVBRDF_ERR_INVALID, "gemm_nt: null a/b/out/err");
-  if (batch < 1 || m < 128 || m % 128 || k < 64 || k % 64 || (n != 64 && n != 128 && n % 256))
-    return fail(SVBRDF_ERR_UNSUPPORTED, "gemm_nt: m %% 128, k %% 64 and n in {64, 128, 256 x j} needed");
-  if ((long long)batch * m >= (1LL << 31) || (long long)batch * n >= (1LL << 31) || k > 65536)
-    return fail(SVBRDF_ERR_UNSUPPORTED, "gemm_nt: too large");
-  if ((long long)batch * (m / 128) > 0x7fffffffLL || n / (n >= 256 ? 256 : n) > 65535)
-    return fail(SVBRDF_ERR_UNSUPPORTED, "gemm_nt: grid too large");
-  if (((uintptr_t)a | (uintptr_t)b | (uintptr_t)out) % 16) return fail(SVBRDF_ERR_INVALID, "gemm_nt: 16-byte alignment");
-  CUtensorMap ma, mb;
-  const int bn = n >= 256 ? 256 : n;
-  int rc = encode_2d(&ma, a, (uint64_t)k, (uint64_t)batch * m, 64, 128);
-  if (rc) return rc;
-  rc = encode_2d(&mb, b, (uint64_t)k, (uint64_t)batch * n, 64, (uint32_t)bn);
-  if (rc) return rc;
-  cudaStream_t st = (cudaStream_t)stream;
-  if (bn == 64) return launch_gemm<64, 6>(ma, mb, out, batch, m, n, k, err, st);
-  if (bn == 128) return launch_gemm<128, 5>(ma, mb, out, batch, m, n, k, err, st);
-  return launch_gemm<256, 4>(ma, mb, out, batch, m, n, k, err, st);
+  const gram::FeatEpi none{};
+  return gram::gemm_nt_entry<false>(a, b, out, batch, m, n, k, err, none, stream);
+}
+
+long long svbrdf_desc_gemm_nt_feat_partials(int batch, int m, int n) {
+  if (batch < 1 || m < 128 || n < 64) return 0;
+  return (long long)batch * (m / 128) * (n / (n >= 256 ? 256 : n)) * 4;
+}
+
+int svbrdf_desc_gemm_nt_feat(const void* a, const void* b, const void* f, int f_is_bf16, const float* t, float coef,
+                             int mask, void* g, float* partial, int batch, int m, int n, int k, int* err,
+                             void* stream) {
+  const gram::FeatEpi fe{f, f_is_bf16 ? 1 : 0, t, coef, mask ? 1 : 0, (__nv_bfloat16*)g, partial};
+  return gram::gemm_nt_entry<true>(a, b, nullptr, batch, m, n, k, err, fe, stream);
 }
 
 }  // extern "C"

@@ -210,14 +210,12 @@ class VGGDescriptor:
         nf = sum(f.numel() for f in hooks.values())
         ng = sum(g.numel() for g in tg)
         nparts = L.svbrdf_desc_partials()
-        parts = torch.empty(len(self.hooks), nparts, device=self.device, dtype=torch.float32)
-        gram_terms, grads = [], {}
+        feat_sums, gram_terms, grads = [], [], {}
         last = [it for it in self.layers if it != "pool"][-1][0]
         for k, (name, wt) in enumerate(zip(self.hooks, self.hook_weights)):
             f = hooks[name]
             v, h, w, c = f.shape
             s = h * w
-            gg = None
             g = None
             if self.gram:
                 # the BF16 feature map (relu1_1's hook is FP32; its BF16 copy feeds conv1_2)
@@ -226,17 +224,25 @@ class VGGDescriptor:
                 coef_g = (4.0 * wt * wt * cg / (ng * s)) if cf is not None else 0.0
                 _, rows, dgram = gram_bf16(ff, self.err, tg[k], coef_g, want_dgram=cf is not None)
                 gram_terms.append((wt * wt) * rows.sum())
-            if cf is not None:
-                if self.gram:
-                    gg = gemm_nt_bf16(ff.reshape(v, s, c), dgram, self.err).reshape(v, h, w, c)
-                g = torch.empty(v, h, w, c, device=self.device, dtype=torch.bfloat16)
             coef = (2.0 * wt * wt * cf / nf) if cf is not None else 0.0
-            N.check(L.svbrdf_desc_feat_loss(f.data_ptr(), int(f.dtype == torch.bfloat16), tf[k].data_ptr(),
-                                            N.ptr(gg), coef, int(name == last), N.ptr(g), parts[k].data_ptr(),
-                                            f.numel(), st))
-            if g is not None:
+            if cf is not None:
+                g = torch.empty(v, h, w, c, device=self.device, dtype=torch.bfloat16)
                 grads[name] = g
-        fl = ((parts.double().sum(dim=1) * self._w2).sum() / nf).float()
+            if cf is not None and self.gram:
+                # the Gram gradient F dG with this hook's feature term in its epilogue
+                part = torch.empty(int(L.svbrdf_desc_gemm_nt_feat_partials(v, s, c)), device=self.device,
+                                   dtype=torch.float32)
+                N.check(L.svbrdf_desc_gemm_nt_feat(ff.data_ptr(), dgram.data_ptr(), f.data_ptr(),
+                                                   int(f.dtype == torch.bfloat16), tf[k].data_ptr(), coef,
+                                                   int(name == last), g.data_ptr(), part.data_ptr(), v, s, c, c,
+                                                   self.err.data_ptr(), st))
+            else:
+                part = torch.empty(nparts, device=self.device, dtype=torch.float32)
+                N.check(L.svbrdf_desc_feat_loss(f.data_ptr(), int(f.dtype == torch.bfloat16), tf[k].data_ptr(),
+                                                None, coef, int(name == last), N.ptr(g), part.data_ptr(),
+                                                f.numel(), st))
+            feat_sums.append(part.double().sum())
+        fl = ((torch.stack(feat_sums) * self._w2).sum() / nf).float()
         gl = torch.stack(gram_terms).sum() / ng if self.gram else torch.zeros((), device=self.device)
         return fl, gl, grads
 

@@ -24,8 +24,13 @@ def _ref_conv(x_nhwc, w_cout_tap_cin, bias=None):
 
 
 @pytest.mark.parametrize("n,h,w,cin,cout", [(1, 8, 16, 64, 64), (2, 16, 32, 64, 128), (1, 24, 48, 128, 256),
-                                            (2, 32, 32, 256, 512), (1, 8, 16, 192, 64)])
+                                            (2, 32, 32, 256, 512), (1, 8, 16, 192, 64), (4, 128, 128, 64, 64),
+                                            (3, 40, 96, 64, 128), (6, 64, 64, 64, 256)])
 def test_conv3x3_tc_matches_torch(svb, cuda, n, h, w, cin, cout):
+    """Every epilogue against torch's FP32 convolution of the same BF16 operands. The shapes
+    cover one and two stacked patches per tile (H a multiple of 16 or not), 64/128/256-channel
+    accumulators, and maps with more tiles than SMs (several tiles per persistent CTA, both
+    TMEM accumulator buffers)."""
     D = svb.descriptor
     g = torch.Generator().manual_seed(n * 1000 + cin)
     x = torch.randn(n, h, w, cin, generator=g).to(cuda, torch.bfloat16)
@@ -56,6 +61,28 @@ def test_conv3x3_tc_data_gradient(svb, cuda):
     gx = D.conv3x3_bf16(gy, w_dg, None, D.EPI_NONE, err)
     ref = torch.nn.grad.conv2d_input((n, cin, h, w), wb.float().to(cuda), gy.float().permute(0, 3, 1, 2), padding=1)
     assert rel_l2(gx.float(), ref.permute(0, 2, 3, 1)) <= 1e-2
+
+
+@pytest.mark.parametrize("n,h,w,c", [(4, 128, 128, 64), (9, 24, 32, 128)])
+def test_conv3x3_tc_add_mask_epilogue(svb, cuda, n, h, w, c):
+    """The backward pass's add+mask epilogue (data gradient + the hook's loss gradient, times
+    the ReLU mask) against torch on the same BF16 operands."""
+    D = svb.descriptor
+    L = svb._native.lib()
+    g = torch.Generator().manual_seed(h * c)
+    gy = torch.randn(n, h, w, c, generator=g).to(cuda, torch.bfloat16)
+    wt = (torch.randn(c, 9, c, generator=g) * (2.0 / (9 * c)) ** 0.5).to(cuda, torch.bfloat16)
+    add = torch.randn(n, h, w, c, generator=g).to(cuda, torch.bfloat16)
+    mask = torch.randn(n, h, w, c, generator=g).to(cuda, torch.bfloat16)
+    out = torch.empty(n, h, w, c, device=cuda, dtype=torch.bfloat16)
+    err = torch.zeros(1, dtype=torch.int32, device=cuda)
+    svb._native.check(L.svbrdf_conv3x3_bf16_ex(gy.data_ptr(), wt.data_ptr(), None, mask.data_ptr(), add.data_ptr(),
+                                               out.data_ptr(), n, h, w, c, c, D.EPI_ADD_MASK, err.data_ptr(),
+                                               svb._native.stream_handle(cuda)))
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    ref = (_ref_conv(gy, wt) + add.float()) * (mask.float() > 0)
+    assert rel_l2(out.float(), ref) <= 1e-2
 
 
 def test_conv3x3_rejects_bad_shapes(svb, cuda):
@@ -228,6 +255,44 @@ def test_gemm_nt_tc_matches_torch(svb, cuda, b, m, n, k):
     torch.cuda.synchronize()
     assert int(err.item()) == 0
     assert rel_l2(out, ref) <= 1e-5
+
+
+@pytest.mark.parametrize("v,s,c,f32,mask", [(2, 4096, 64, True, False), (3, 1024, 128, False, True),
+                                            (2, 256, 256, False, False), (9, 1024, 512, False, True)])
+def test_gemm_nt_feat_matches_separate_kernels(svb, cuda, v, s, c, f32, mask):
+    """The Gram gradient with the feature term in its epilogue (svbrdf_desc_gemm_nt_feat)
+    against the two kernels it replaces: F dG in FP32 (svbrdf_desc_gemm_nt), then the feature
+    term on it (svbrdf_desc_feat_loss). The BF16 gradient within one BF16 rounding, the sum of
+    squared feature differences within FP32 summation order."""
+    D = svb.descriptor
+    L = svb._native.lib()
+    st = svb._native.stream_handle(cuda)
+    g = torch.Generator().manual_seed(v * 10 + c)
+    f32v = torch.relu(torch.randn(v, s, c, generator=g)).to(cuda)
+    f16 = f32v.to(torch.bfloat16)
+    f = f32v if f32 else f16
+    t = (f.float() + 0.3 * torch.randn(v, s, c, generator=g).to(cuda)).contiguous()
+    dg = (torch.randn(v, c, c, generator=g) * 0.01).to(cuda, torch.bfloat16)
+    dg = ((dg.float() + dg.float().transpose(1, 2)) * 0.5).to(torch.bfloat16).contiguous()
+    coef = 0.013
+    err = torch.zeros(1, dtype=torch.int32, device=cuda)
+    gg = D.gemm_nt_bf16(f16, dg, err)
+    g_ref = torch.empty(v, s, c, device=cuda, dtype=torch.bfloat16)
+    p_ref = torch.empty(L.svbrdf_desc_partials(), device=cuda)
+    svb._native.check(L.svbrdf_desc_feat_loss(f.data_ptr(), int(not f32), t.data_ptr(), gg.data_ptr(), coef, int(mask),
+                                              g_ref.data_ptr(), p_ref.data_ptr(), f.numel(), st))
+    g_out = torch.empty(v, s, c, device=cuda, dtype=torch.bfloat16)
+    p_out = torch.full((int(L.svbrdf_desc_gemm_nt_feat_partials(v, s, c)),), float("nan"), device=cuda)
+    svb._native.check(L.svbrdf_desc_gemm_nt_feat(f16.data_ptr(), dg.data_ptr(), f.data_ptr(), int(not f32),
+                                                 t.data_ptr(), coef, int(mask), g_out.data_ptr(), p_out.data_ptr(), v,
+                                                 s, c, c, err.data_ptr(), st))
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    assert rel_l2(g_out.float(), g_ref.float()) <= 4e-3
+    ref_sum = p_ref.double().sum()
+    assert abs(float(p_out.double().sum() - ref_sum)) <= 1e-5 * float(ref_sum)
+    if mask:
+        assert bool((g_out.float()[f.float() <= 0] == 0).all())
 
 
 def test_descriptor_at_config_shape_vs_fp64_oracle(svb, cuda):

@@ -14,8 +14,10 @@ SvbrdfOptim.optim loop (src/svbrdf.py:44-83) and Microfacet.eval (src/microfacet
   max(2e-5, twice the reference's own FP32 error on the same texels) for the maps, and
   max(1e-4, twice that error) for the moments (a texel near a clamp of the render can take a
   slightly different path in FP32 than in FP64; the reference's own FP32 loop does too);
-* every loss of one whole 256^2 material (all its texels through the oracle, 100 iterations)
-  within max(1e-5, twice the reference's own FP32 loop's error on that material) relative;
+* every loss, the maps and both moments of one whole 256^2 material (all its texels through
+  the oracle, 100 iterations) within max(1e-5, twice the reference's own FP32 loop's error on
+  that material) relative for the losses, and the map and moment bounds above with that
+  loop's error on the whole material;
 * the first iteration's loss of one material of each resolution, every texel through the
   oracle, within 1e-5 relative (the reduction over tiles, warps and CTAs at full size);
 * all 100 losses of every material against the single-material fused kernel (a different
@@ -112,6 +114,7 @@ def workload(svb, cuda):
                              "log1p", torch.float32)
     whole32_loss = (whole32["sq_err"].double().sum(1) / (m.n_views * 3 * T)).tolist()
     e32_whole = max(abs(a - b) / b for a, b in zip(whole32_loss, whole_loss))
+    e32_maps = {k: rel_l2(whole32[k], whole[k]) for k in ("textures", "exp_avg", "exp_avg_sq")}
     # the first loss of one material of each resolution, every texel
     first = {}
     for res in (256, 512, 1024):
@@ -138,7 +141,8 @@ def workload(svb, cuda):
         o.optim(ITERS, LR, None, False)
         single.append(o.loss_image_list)
     return {"mats": mats, "idxs": idxs, "o64": o64, "o32": o32, "small": small, "whole": whole,
-            "whole_loss": whole_loss, "e32_whole": e32_whole, "first": first, "single": single}
+            "whole_loss": whole_loss, "e32_whole": e32_whole, "e32_maps": e32_maps, "first": first,
+            "single": single}
 
 
 def _col_ranges(idxs):
@@ -182,9 +186,12 @@ def test_bench_workload_matches_oracle(svb, cuda, workload, variant):
           f"(the reference's FP32 loop {e32:.2e})")
     assert e_single <= 5e-5
     assert e_whole <= max(1e-5, 2 * e32)
-    for k in ("textures", "exp_avg", "exp_avg_sq"):
+    for k, floor in (("textures", 2e-5), ("exp_avg", 1e-4), ("exp_avg_sq", 1e-4)):
         ref = workload["whole"][k]
         got = {"textures": b.tex, "exp_avg": b.m1, "exp_avg_sq": b.m2}[k][s].reshape(9, -1)
-        assert rel_l2(got, ref) <= (2e-5 if k == "textures" else 1e-4), ("whole material", k)
+        noise = workload["e32_maps"][k]  # the reference's own FP32 loop on the whole material
+        err = rel_l2(got, ref)
+        print(f"variant {variant}: whole material {k} vs FP64 {err:.2e} (the reference's FP32 loop {noise:.2e})")
+        assert err <= max(floor, 2 * noise), ("whole material", k, err, noise)
     for i, ref in workload["first"].items():
         assert abs(float(hist[0, i]) - ref) <= 1e-5 * ref, ("first loss", i)

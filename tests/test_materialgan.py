@@ -348,11 +348,16 @@ def test_gpu_generator_matches_reference_network(svb, cuda):
 @pytest.mark.gpu
 @pytest.mark.parametrize("b,h,cin,cout,k,pad", [(16, 4, 512, 512, 3, 1), (3, 8, 512, 512, 3, 1), (2, 10, 512, 256, 3, 0),
                                                  (2, 18, 256, 128, 3, 0), (1, 32, 128, 128, 3, 1),
-                                                 (2, 16, 128, 9, 1, 0)])
+                                                 (2, 16, 128, 9, 1, 0), (2, 20, 128, 64, 3, 1),
+                                                 (16, 64, 64, 64, 3, 1), (24, 64, 64, 256, 3, 1),
+                                                 (16, 66, 128, 128, 3, 0)])
 def test_conv_tf32_matches_torch(svb, cuda, b, h, cin, cout, k, pad):
     """The TF32 tensor-core convolution (forward and data gradient through _ConvTF32) against
     torch's FP32 convolution of the same channels-last maps: relative L2 <= 2e-3 (TF32 rounds
-    both operands to 10 mantissa bits; FP32 accumulation)."""
+    both operands to 10 mantissa bits; FP32 accumulation). The shapes cover the 4^2 and 8^2
+    patches, two M-tiles per CTA tile (with a partial second one at 20 rows), and maps with
+    more tiles than SMs, where each persistent CTA runs several tiles through both TMEM
+    accumulator buffers."""
     MG = svb.materialgan
     g = torch.Generator().manual_seed(b * h + cin)
     x = torch.randn(b, cin, h, h, generator=g).to(cuda).contiguous(memory_format=torch.channels_last)
@@ -380,16 +385,9 @@ def test_conv_tf32_matches_torch(svb, cuda, b, h, cin, cout, k, pad):
     assert rel_l2(xr.grad, x2.grad) <= 2e-3
 
 
-@pytest.mark.gpu
-def test_gpu_generator_tf32_matches_reference_network(svb, cuda):
-    """The generator as it runs by default on the GPU (channels-last maps, the TF32 tensor-core
-    convolutions, the NHWC kernels) on the reference network's fixture
-    (tests/golden/generator_ref_256.npz, the reference's FP64 run): output and gradients within
-    TF32 accuracy."""
-    gen, d, wp_np, noises_np, R_np, _ = _reference_generator(svb, cuda, torch.float32)
-    for p in gen.parameters():
-        p.requires_grad_(False)
-    assert torch.backends.cudnn.allow_tf32
+def _tf32_generator_errors(svb, cuda, gen, d, wp_np, noises_np, R_np):
+    """Errors of one GPU synthesis + backward against the reference network's FP64 fixture:
+    (output at the fixture's indices, W+ gradient, worst noise-gradient norm), relative."""
     wp = torch.from_numpy(wp_np).float().to(cuda).requires_grad_(True)
     noises = [torch.from_numpy(n).float().to(cuda).requires_grad_(True) for n in noises_np]
     out = gen.synthesis(wp, noises)
@@ -401,5 +399,30 @@ def test_gpu_generator_tf32_matches_reference_network(svb, cuda):
     e_wp = rel_l2(wp.grad, torch.from_numpy(d["grad_wp"]))
     e_n = max(abs(float(n.grad.double().norm()) - float(d[f"noise{i}_norm"])) / float(d[f"noise{i}_norm"])
               for i, n in enumerate(noises))
-    print(f"TF32 generator vs reference FP64: output {e_out:.2e}, W+ gradient {e_wp:.2e}, noise-gradient norms {e_n:.2e}")
-    assert e_out <= 1e-2 and e_wp <= 3e-2 and e_n <= 3e-2
+    return e_out, e_wp, e_n
+
+
+@pytest.mark.gpu
+def test_gpu_generator_tf32_matches_reference_network(svb, cuda):
+    """The generator as it runs by default on the GPU (channels-last maps, the TF32 tensor-core
+    convolutions, the NHWC kernels) on the reference network's fixture
+    (tests/golden/generator_ref_256.npz, the reference's FP64 run). The reference's own GPU path
+    runs these convolutions in TF32 too (PyTorch's cuDNN default), so the bound is that path's
+    error: the same generator with its convolutions on cuDNN in TF32 (convolution weights
+    marked trainable, which keeps a layer off the frozen-weight kernels). Output within
+    max(1e-2, twice cuDNN's error), W+ and noise gradients within max(3e-2, twice cuDNN's)."""
+    MG = svb.materialgan
+    gen, d, wp_np, noises_np, R_np, _ = _reference_generator(svb, cuda, torch.float32)
+    for p in gen.parameters():
+        p.requires_grad_(False)
+    assert torch.backends.cudnn.allow_tf32
+    ours = _tf32_generator_errors(svb, cuda, gen, d, wp_np, noises_np, R_np)
+    convs = [m for m in gen.modules() if isinstance(m, MG._ModConv)]
+    assert convs and all(getattr(m, "_tf32_key", None) is not None for m in convs)  # the TF32 kernels ran
+    for m in convs:
+        m.weight.requires_grad_(True)
+    lib = _tf32_generator_errors(svb, cuda, gen, d, wp_np, noises_np, R_np)
+    print("TF32 generator vs reference FP64 (output, W+ gradient, noise-gradient norms): tcgen05 kernels "
+          + ", ".join(f"{e:.2e}" for e in ours) + "; cuDNN TF32 " + ", ".join(f"{e:.2e}" for e in lib))
+    for e, e_lib, floor in zip(ours, lib, (1e-2, 3e-2, 3e-2)):
+        assert e <= max(floor, 2 * e_lib)

@@ -163,7 +163,9 @@ def test_pair_plan_requirements_and_ring(svb, lib):
     # slots of 9 planes x 960 floats plus a 288-byte record, within the 216 KB ring budget
     budget, slot = 216 * 1024, 9 * 960 * 4 + 288
     assert 2 <= ring <= 64 and ring * slot <= budget < (ring + 1) * slot
-    assert lib.svbrdf_batched_workspace_bytes(buf.ctypes.data) == 256 + 4 * n_tiles * (480 // 32)
+    # header, per-(tile, warp) loss partials (per iteration for the resident-state variant),
+    # then per-tile totals of up to 32 iterations and 3 light-power sums (two-level reduction)
+    assert lib.svbrdf_batched_workspace_bytes(buf.ctypes.data) == 256 + 4 * n_tiles * (480 // 32) + 4 * n_tiles * (32 + 3)
     # seq: (tile, material, first texel) for each entry of the CTA-ordered tile list
     off_order, off_tiles, off_seq = hdr[9], hdr[10], hdr[16]
     order = np.frombuffer(buf[off_order:off_order + 4 * n_tiles].tobytes(), np.int32)
@@ -198,7 +200,7 @@ def test_resident_state_plan_ring_and_workspace(svb, lib, variant, threads, budg
     assert hdr[13] == variant and got == ring
     state, slot = 27 * tt * 4, 9 * tt * 4 + 288
     assert state + ring * slot <= budget * 1024 < state + (ring + 1) * slot
-    assert lib.svbrdf_batched_workspace_bytes(buf.ctypes.data) == 256 + 4 * n_tiles * (threads // 32) * 32
+    assert lib.svbrdf_batched_workspace_bytes(buf.ctypes.data) == 256 + 4 * n_tiles * (threads // 32) * 32 + 4 * n_tiles * (32 + 3)
     # 608 threads is not offered by the resident-state variant; tiles must be twice threads
     assert lib.svbrdf_batched_plan_bytes(mats, 2, ctypes.byref(SV.svbrdf_batch_config(608, 1216, 3, 3))) == 0
     assert lib.svbrdf_batched_plan_bytes(mats, 2, ctypes.byref(SV.svbrdf_batch_config(480, 480, 3, 3))) == 0
@@ -216,7 +218,7 @@ def test_pipelined_plan_ring_and_workspace(svb, lib):
     assert variant == 1
     assert 2 <= ring <= 64 and ring * 12 * 480 * 4 <= 200 * 1024
     # one partial loss per (tile, consumer warp) after the 256-byte header
-    assert lib.svbrdf_batched_workspace_bytes(buf.ctypes.data) == 256 + 4 * n_tiles * (480 // 32)
+    assert lib.svbrdf_batched_workspace_bytes(buf.ctypes.data) == 256 + 4 * n_tiles * (480 // 32) + 4 * n_tiles * (32 + 3)
     # coordinate tables: the reference's pixel-centre grid (src/microfacet.py:16-19)
     off_coords = hdr[12]
     xs = np.frombuffer(buf[off_coords:off_coords + 4 * 64].tobytes(), np.float32)

@@ -80,6 +80,20 @@ int svbrdf_render_bwd(const float* textures, const float* camera_pos, const floa
                       const float* grad_out, float* grad_textures, float* grad_light_pow,
                       void* workspace, size_t workspace_bytes, void* stream);
 
+/* The same two calls over a leading batch of `batch` materials of one shape, all under the same
+ * views and light (the reference's Microfacet.eval on textures [B, 9, H, W], which renders to
+ * [B * n_views, 3, H, W], src/microfacet.py:84-120): textures [batch][9][H][W], out / targets /
+ * grad_out [batch][n_views][3][H][W], grad_textures [batch][9][H][W]; the loss is the mean over
+ * the whole batch and grad_light_pow sums over it. One launch each. */
+int svbrdf_render_fwd_batch(const float* textures, const float* camera_pos, const float* light_pos,
+                            const float* light_pow, int n_views, int height, int width, float size, int batch,
+                            float* out, const float* targets, int loss_kind, float* loss_out, void* workspace,
+                            size_t workspace_bytes, void* stream);
+int svbrdf_render_bwd_batch(const float* textures, const float* camera_pos, const float* light_pos,
+                            const float* light_pow, int n_views, int height, int width, float size, int batch,
+                            const float* grad_out, float* grad_textures, float* grad_light_pow, void* workspace,
+                            size_t workspace_bytes, void* stream);
+
 /* One fused iteration of SvbrdfOptim.optim (src/svbrdf.py:56-71): render of
  * clamp(textures, -1, 1), image loss, adjoint and torch.optim.Adam update
  * (betas beta1/beta2, eps, no weight decay, 1-based `step` after this update), in one
@@ -395,6 +409,15 @@ int svbrdf_gen_act_nhwc_bwd(const float* gout, const float* y, const float* d, c
  * weight[cout][tap][cin] and pad' = ksize - 1 - pad. `err` as in svbrdf_conv3x3_bf16. */
 int svbrdf_gen_conv_tf32(const float* x, const float* weight, float* y, int b, int hin, int win, int cin, int cout,
                          int ksize, int pad, int* err, void* stream);
+
+/* The same convolution with a caller-owned workspace: a map with fewer output tiles than half
+ * the SMs (the generator's 4^2 to 16^2 layers) splits K over the tiles' CTAs, each split writing
+ * an FP32 partial of y into ws, then sums the partials in split order (deterministic).
+ * svbrdf_gen_conv_tf32_ws_bytes gives the bytes such a call uses (0: no split; -1: an
+ * unsupported shape); with a smaller or NULL ws the call runs unsplit, as svbrdf_gen_conv_tf32. */
+long long svbrdf_gen_conv_tf32_ws_bytes(int b, int hin, int win, int cin, int cout, int ksize, int pad);
+int svbrdf_gen_conv_tf32_ex(const float* x, const float* weight, float* y, void* ws, long long ws_bytes, int b,
+                            int hin, int win, int cin, int cout, int ksize, int pad, int* err, void* stream);
 
 /* ---- novel-view rendering under an environment map (the reference's MitsubaRender,
  * src/mitsubarender.py:7-105, for the video of src/scripts.py:44-59) ---- */

@@ -119,6 +119,10 @@ def _declare(L):
     L.svbrdf_render_fwd.argtypes = [P, P, P, P, I, I, I, F, P, P, I, P, P, S, P]
     L.svbrdf_render_bwd.restype = I
     L.svbrdf_render_bwd.argtypes = [P, P, P, P, I, I, I, F, P, P, P, P, S, P]
+    L.svbrdf_render_fwd_batch.restype = I
+    L.svbrdf_render_fwd_batch.argtypes = [P, P, P, P, I, I, I, F, I, P, P, I, P, P, S, P]
+    L.svbrdf_render_bwd_batch.restype = I
+    L.svbrdf_render_bwd_batch.argtypes = [P, P, P, P, I, I, I, F, I, P, P, P, P, S, P]
     L.svbrdf_fused_step.restype = I
     L.svbrdf_fused_step.argtypes = [P, P, P, P, P, P, P, P, I, I, I, F, I, I, F, F, F, F, P, P, S, P]
     L.svbrdf_fused_step_noalloc.restype = I
@@ -156,6 +160,10 @@ def _declare(L):
     L.svbrdf_desc_gemm_nt_feat.argtypes = [P, P, P, I, P, F, I, P, P, I, I, I, I, P, P]
     L.svbrdf_gen_conv_tf32.restype = I
     L.svbrdf_gen_conv_tf32.argtypes = [P, P, P, I, I, I, I, I, I, I, P, P]
+    L.svbrdf_gen_conv_tf32_ws_bytes.restype = ctypes.c_longlong
+    L.svbrdf_gen_conv_tf32_ws_bytes.argtypes = [I, I, I, I, I, I, I]
+    L.svbrdf_gen_conv_tf32_ex.restype = I
+    L.svbrdf_gen_conv_tf32_ex.argtypes = [P, P, P, P, ctypes.c_longlong, I, I, I, I, I, I, I, P, P]
     L.svbrdf_gen_upsample2.restype = I
     L.svbrdf_gen_upsample2.argtypes = [P, P, ctypes.c_longlong, I, I, P]
     L.svbrdf_gen_upsample2_scaled.restype = I
@@ -204,7 +212,8 @@ def _declare(L):
 # Every symbol include/svbrdf_gb300.h declares.
 EXPORTS = [
     "svbrdf_last_error", "svbrdf_abi_version", "svbrdf_max_views", "svbrdf_workspace_bytes",
-    "svbrdf_render_fwd", "svbrdf_render_bwd", "svbrdf_fused_step", "svbrdf_fused_step_noalloc",
+    "svbrdf_render_fwd", "svbrdf_render_bwd", "svbrdf_render_fwd_batch", "svbrdf_render_bwd_batch",
+    "svbrdf_fused_step", "svbrdf_fused_step_noalloc",
     "svbrdf_batched_plan_bytes",
     "svbrdf_batched_plan", "svbrdf_batched_workspace_bytes", "svbrdf_batched_step", "svbrdf_batched_steps", "svbrdf_conv3x3_bf16",
     "svbrdf_conv3x3_bf16_ex", "svbrdf_desc_partials", "svbrdf_desc_conv1_fwd", "svbrdf_desc_conv1_bwd",
@@ -215,7 +224,7 @@ EXPORTS = [
     "svbrdf_gen_upsample2_bwd", "svbrdf_gen_upsample2_scaled", "svbrdf_gen_scale", "svbrdf_gen_scale_bwd", "svbrdf_gen_act", "svbrdf_gen_act_bwd",
     "svbrdf_gen_nhwc_partial_floats", "svbrdf_gen_upsample2_nhwc", "svbrdf_gen_upsample2_nhwc_bwd",
     "svbrdf_gen_scale_nhwc", "svbrdf_gen_scale_nhwc_bwd", "svbrdf_gen_act_nhwc", "svbrdf_gen_act_nhwc_bwd",
-    "svbrdf_gen_conv_tf32",
+    "svbrdf_gen_conv_tf32", "svbrdf_gen_conv_tf32_ws_bytes", "svbrdf_gen_conv_tf32_ex",
     "svbrdf_envmap_render", "svbrdf_selftest_wait_timeout",
 ]
 

@@ -3,18 +3,19 @@
 // The descriptor loss of the reference (VGGLoss, src/descriptor.py:7-79) runs a VGG19
 // feature stack over the renders. Here every 3x3 convolution with at least 64 input
 // channels is an implicit GEMM on tcgen05:
-//   M = 128 output pixels per M-tile (an 8 x 16 patch of one image; a tile stacks MT = 2 of
-//   them along y where Cout <= 128, so one weight slice feeds 256 pixels), N = BN output
-//   channels, K = 9 taps x Cin, consumed 64 channels (128 bytes of BF16) at a time.
-// The kernel is persistent: one CTA per SM walks the tiles i, i + grid, ... For each (tap,
-// 64-channel chunk) the producer warp TMA-loads the shifted 8x16x64 input patches from the
-// NHWC activation tensor (out-of-image taps read the TMA zero fill, which is exactly the
-// padding) and the BN x 64 weight slice, 128-byte swizzled, into a ring of shared-memory
-// stages that runs on across tiles. One thread issues tcgen05.mma (kind::f16, BF16 in, FP32
-// accumulate) into MT 128 x BN TMEM accumulators, double-buffered; tcgen05.commit frees each
-// stage and signals the epilogue per tile. Four epilogue warps read TMEM with tcgen05.ld,
-// apply the epilogue (bias + ReLU, or a ReLU-mask multiply for the backward pass) and store
-// BF16 NHWC while the MMAs of the next tile run.
+//   M = 128 output pixels per M-tile (a 16-row x 8-column patch of one image; a tile stacks
+//   MT = 2 of them along y where Cout <= 128, so one weight slice feeds 256 pixels), N = BN
+//   output channels, K = 9 taps x Cin, consumed 64 channels (128 bytes of BF16) at a time.
+// The kernel is persistent: one CTA per SM walks the tiles i, i + grid, ... For each 64-channel
+// chunk the producer warp TMA-loads the tile's input patch once, with its one-pixel halo
+// (out-of-image pixels read the TMA zero fill, which is exactly the padding), and the 9 taps'
+// BN x 64 weight slices, 128-byte swizzled, into two rings of shared-memory stages that run on
+// across tiles; the 9 taps read the one patch through shifted descriptors (the halo form
+// below). One thread issues tcgen05.mma (kind::f16, BF16 in, FP32 accumulate) into MT
+// 128 x BN TMEM accumulators, double-buffered; tcgen05.commit frees each stage and signals the
+// epilogue per tile. Eight epilogue warps (two per TMEM lane quadrant, each with half the
+// columns) read TMEM with tcgen05.ld, apply the epilogue (bias + ReLU, or a ReLU-mask multiply
+// for the backward pass) and store BF16 NHWC while the MMAs of the next tile run.
 // The data gradient of a convolution is the same kernel run on dL/dY with the weights
 // transposed (Cin <-> Cout) and flipped (tap -> 8 - tap).
 //
@@ -32,9 +33,10 @@ namespace svb {
 namespace tc {
 
 constexpr int BM = 128;  // output pixels per M-tile
-constexpr int TH = 8, TW = 16;
-constexpr int BK = 64;   // input channels per stage (one 128-byte swizzle row)
-constexpr int kThreads = 192;  // warp 0 TMA, warp 1 MMA + TMEM owner, warps 2..5 epilogue
+constexpr int TH = 8, TW = 16;  // the entry point's shape granularity (H % 8, W % 16)
+constexpr int BK = 64;   // input channels per chunk (one 128-byte weight row)
+constexpr int kThreads = 320;  // warp 0 TMA, warp 1 MMA + TMEM owner, warps 2..9 epilogue
+constexpr int kEpiWarps = 8;  // two per TMEM lane quadrant, each draining half the columns
 
 enum Epilogue : int { kEpiNone = 0, kEpiBiasRelu = 1, kEpiMask = 2, kEpiAddMask = 3 };
 enum ConvError : int { kErrTma = 11, kErrMma = 12, kErrEpi = 13 };
@@ -95,54 +97,68 @@ __device__ __forceinline__ void epilogue_store32(const uint32_t (&r)[32], const 
   }
 }
 
-// Persistent: grid = min(tiles, SMs), CTA i runs tiles i, i + grid, ... A tile is MT stacked
-// 8 x 16 patches of one image (MT x 128 output pixels) x BN output channels; tiles sharing a
-// patch are consecutive, so their input loads meet in L2. The producer's ring runs on across
-// tiles and the MT accumulators are double-buffered in TMEM, so the epilogue of tile j
-// overlaps the MMAs of tile j + 1.
-template <int BN, int MT, int STAGES, int EPI>
+// ---------------------------------------------------------------- halo form
+// The same convolution with each input patch loaded once per 64-channel chunk, halo included,
+// and shared by the 9 taps. A tile is MT stacked 16-row x 8-column patches of one image; its
+// input is the (16 MT + 2) x 10 halo patch. Shared memory holds that patch K-major without
+// swizzle: for each 8-channel group g, the halo pixels (row-major, 10 per row) at 16 bytes each,
+// groups kHaloKg bytes apart. The 128 accumulator rows of M-tile mt are the patch's 16 rows of
+// 8 pixels: row group r (8 pixels) of tap (ky, kx) starts at halo pixel (16 mt + r + ky) x 10 +
+// kx, so a tap is the same descriptor shifted by (10 ky + kx) x 16 bytes, with 8-row groups 160
+// bytes apart (SBO) and K-adjacent core matrices one channel group apart (LBO). The weight
+// slices [BN][64] of the 9 taps stream through their own ring (128-byte swizzle, as above).
+// Per chunk the tile loads (16 MT + 2) x 10 x 128 bytes of input instead of 9 x MT x 16 KB.
+template <int MT>
+struct Halo {
+  static constexpr int kRows = 16 * MT + 2, kCols = 10;
+  static constexpr int kKg = ((kRows * kCols * 16 + 127) / 128) * 128;  // one channel group, 128-byte aligned
+  static constexpr int kABytes = 8 * kKg;                               // one 64-channel chunk
+};
+
+template <int BN, int MT, int AST, int BST, int EPI>
 __global__ void __launch_bounds__(kThreads, 1)
-conv3x3_tc_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_constant__ CUtensorMap tmap_w,
-                  const float* __restrict__ bias, const __nv_bfloat16* __restrict__ mask,
-                  const __nv_bfloat16* __restrict__ addend, __nv_bfloat16* __restrict__ y, int N, int H, int W,
-                  int Cin, int Cout, int* err) {
-  constexpr int A_BYTES = BM * BK * 2;
+conv3x3_halo_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_constant__ CUtensorMap tmap_w,
+                    const float* __restrict__ bias, const __nv_bfloat16* __restrict__ mask,
+                    const __nv_bfloat16* __restrict__ addend, __nv_bfloat16* __restrict__ y, int N, int H, int W,
+                    int Cin, int Cout, int* err) {
+  using HP = Halo<MT>;
   constexpr int B_BYTES = BN * BK * 2;
-  constexpr int STAGE = MT * A_BYTES + B_BYTES;
   constexpr uint32_t ACC_COLS = MT * BN;
   constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;
   static_assert(TMEM_COLS >= 32 && TMEM_COLS <= 512 && (TMEM_COLS & (TMEM_COLS - 1)) == 0, "TMEM columns");
+  static_assert(B_BYTES % 1024 == 0, "weight slices keep the 1024-byte swizzle alignment");
   extern __shared__ uint8_t dsmem[];
-  __shared__ __align__(8) uint64_t full_bar[STAGES];
-  __shared__ __align__(8) uint64_t empty_bar[STAGES];
-  __shared__ __align__(8) uint64_t tfull_bar[2];   // accumulator buffer ready (MMA commit)
-  __shared__ __align__(8) uint64_t tempty_bar[2];  // accumulator buffer drained (4 epilogue warps)
-  __shared__ __align__(8) uint64_t done_bar;       // every MMA of this CTA complete
+  __shared__ __align__(8) uint64_t afull[AST], aempty[AST], bfull[BST], bempty[BST];
+  __shared__ __align__(8) uint64_t tfull_bar[2], tempty_bar[2], done_bar;
   __shared__ uint32_t tmem_slot;
 
-  const uint32_t base = (smem_u32(dsmem) + 1023u) & ~1023u;  // 128-byte swizzle atoms need 1024-byte alignment
+  const uint32_t bbase = (smem_u32(dsmem) + 1023u) & ~1023u;  // weight ring, then the halo ring
+  const uint32_t abase = bbase + (uint32_t)(BST * B_BYTES);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int tiles_x = W / TW, tiles_y = H / (TH * MT), tiles_n = Cout / BN;
+  const int tiles_x = W / 8, tiles_y = (H + 16 * MT - 1) / (16 * MT), tiles_n = Cout / BN;
   const int n_tiles = N * tiles_y * tiles_x * tiles_n;
   const int kchunks = Cin / BK;
-  const int total = 9 * kchunks;
   auto coord = [&](int t, int& img, int& y0, int& x0, int& n0) {
     n0 = (t % tiles_n) * BN;
     int r = t / tiles_n;
-    x0 = (r % tiles_x) * TW;
+    x0 = (r % tiles_x) * 8;
     r /= tiles_x;
-    y0 = (r % tiles_y) * (TH * MT);
+    y0 = (r % tiles_y) * (16 * MT);
     img = r / tiles_y;
   };
 
   if (threadIdx.x == 0) {
-    for (int s = 0; s < STAGES; ++s) {
-      mbar_init(smem_u32(&full_bar[s]), 1);
-      mbar_init(smem_u32(&empty_bar[s]), 1);
+    for (int s = 0; s < AST; ++s) {
+      mbar_init(smem_u32(&afull[s]), 1);
+      mbar_init(smem_u32(&aempty[s]), 1);
+    }
+    for (int s = 0; s < BST; ++s) {
+      mbar_init(smem_u32(&bfull[s]), 1);
+      mbar_init(smem_u32(&bempty[s]), 1);
     }
     for (int a = 0; a < 2; ++a) {
       mbar_init(smem_u32(&tfull_bar[a]), 1);
-      mbar_init(smem_u32(&tempty_bar[a]), 4);
+      mbar_init(smem_u32(&tempty_bar[a]), kEpiWarps);
     }
     mbar_init(smem_u32(&done_bar), 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -161,36 +177,47 @@ conv3x3_tc_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_const
   if (warp == 0) {
     if (lane == 0) {
       // ---------------------------------------------------------------- TMA producer
-      int q = 0;  // stages issued by this CTA
+      int qa = 0, qb = 0;
       bool bad = false;
       for (int t = blockIdx.x; t < n_tiles && !bad; t += gridDim.x) {
         int img, y0, x0, n0;
         coord(t, img, y0, x0, n0);
-        for (int i = 0; i < total; ++i) {
-          const int s = q % STAGES;
-          const uint32_t ph = (uint32_t)(q / STAGES) & 1u;
-          if (q >= STAGES && !mbar_wait(smem_u32(&empty_bar[s]), ph ^ 1u, err, kErrTma)) {
+        for (int cc = 0; cc < kchunks && !bad; ++cc) {
+          const int sa = qa % AST;
+          if (qa >= AST && !mbar_wait(smem_u32(&aempty[sa]), ((uint32_t)(qa / AST) & 1u) ^ 1u, err, kErrTma)) {
             bad = true;
             break;
           }
-          const int tap = i / kchunks, cc = i % kchunks;
-          const int dy = tap / 3 - 1, dx = tap % 3 - 1;
-          const uint32_t st = base + (uint32_t)(s * STAGE);
-          const uint32_t fb = smem_u32(&full_bar[s]);
-          mbar_expect_tx(fb, (uint32_t)STAGE);
-#pragma unroll
-          for (int mt = 0; mt < MT; ++mt)
-            tma_4d(st + (uint32_t)(mt * A_BYTES), &tmap_x, cc * BK, x0 + dx, y0 + mt * TH + dy, img, fb);
-          tma_2d(st + (uint32_t)(MT * A_BYTES), &tmap_w, tap * Cin + cc * BK, n0, fb);
-          ++q;
+          const uint32_t fa = smem_u32(&afull[sa]);
+          mbar_expect_tx(fa, (uint32_t)(8 * HP::kRows * HP::kCols * 16));
+#pragma unroll 1
+          for (int g = 0; g < 8; ++g)
+            tma_4d(abase + (uint32_t)(sa * HP::kABytes + g * HP::kKg), &tmap_x, cc * BK + 8 * g, x0 - 1, y0 - 1, img,
+                   fa);
+          ++qa;
+          for (int tap = 0; tap < 9; ++tap) {
+            const int sb = qb % BST;
+            if (qb >= BST && !mbar_wait(smem_u32(&bempty[sb]), ((uint32_t)(qb / BST) & 1u) ^ 1u, err, kErrTma)) {
+              bad = true;
+              break;
+            }
+            const uint32_t fb = smem_u32(&bfull[sb]);
+            mbar_expect_tx(fb, (uint32_t)B_BYTES);
+            tma_2d(bbase + (uint32_t)(sb * B_BYTES), &tmap_w, tap * Cin + cc * BK, n0, fb);
+            ++qb;
+          }
         }
       }
       if (bad) {
-        // aborted: no load may still be writing shared memory when the CTA exits, so wait
-        // (bounded) for the loads of the last min(q, STAGES) stages to land
-        for (int i = q > STAGES ? q - STAGES : 0; i < q; ++i) {
+        // aborted: no load may still be writing shared memory when the CTA exits
+        for (int i = qa > AST ? qa - AST : 0; i < qa; ++i) {
           uint32_t it = 0;
-          while (!mbar_try(smem_u32(&full_bar[i % STAGES]), (uint32_t)(i / STAGES) & 1u) && ++it < kSpin) {
+          while (!mbar_try(smem_u32(&afull[i % AST]), (uint32_t)(i / AST) & 1u) && ++it < kSpin) {
+          }
+        }
+        for (int i = qb > BST ? qb - BST : 0; i < qb; ++i) {
+          uint32_t it = 0;
+          while (!mbar_try(smem_u32(&bfull[i % BST]), (uint32_t)(i / BST) & 1u) && ++it < kSpin) {
           }
         }
       }
@@ -199,43 +226,54 @@ conv3x3_tc_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_const
     if (lane == 0) {
       // ---------------------------------------------------------------- MMA issuer
       constexpr uint32_t idesc = idesc_bf16(BM, BN);
-      int q = 0, j = 0;
+      int qa = 0, qb = 0, j = 0;
       bool bad = false;
       for (int t = blockIdx.x; t < n_tiles && !bad; t += gridDim.x, ++j) {
         const int a = j & 1;
-        // the epilogue must have drained this buffer's previous tile (j - 2)
         if (j >= 2 && !mbar_wait(smem_u32(&tempty_bar[a]), ((uint32_t)(j >> 1) & 1u) ^ 1u, err, kErrMma)) break;
         fence_after();
         const uint32_t acc = tmem + (uint32_t)a * ACC_COLS;
-        for (int i = 0; i < total; ++i, ++q) {
-          const int s = q % STAGES;
-          const uint32_t ph = (uint32_t)(q / STAGES) & 1u;
-          if (!mbar_wait(smem_u32(&full_bar[s]), ph, err, kErrMma)) {
+        for (int cc = 0; cc < kchunks && !bad; ++cc) {
+          const int sa = qa % AST;
+          if (!mbar_wait(smem_u32(&afull[sa]), (uint32_t)(qa / AST) & 1u, err, kErrMma)) {
             bad = true;
             break;
           }
-          fence_after();
-          const uint32_t sa = base + (uint32_t)(s * STAGE);
-          const uint32_t sb = sa + (uint32_t)(MT * A_BYTES);
+          const uint32_t achunk = abase + (uint32_t)(sa * HP::kABytes);
+          for (int tap = 0; tap < 9; ++tap) {
+            const int sb = qb % BST;
+            if (!mbar_wait(smem_u32(&bfull[sb]), (uint32_t)(qb / BST) & 1u, err, kErrMma)) {
+              bad = true;
+              break;
+            }
+            fence_after();
+            const uint32_t atap = achunk + (uint32_t)(((tap / 3) * HP::kCols + tap % 3) * 16);
+            const uint32_t bs = bbase + (uint32_t)(sb * B_BYTES);
 #pragma unroll
-          for (int k = 0; k < BK / 16; ++k) {
+            for (int k = 0; k < BK / 16; ++k) {  // 16 channels = two channel groups per MMA
 #pragma unroll
-            for (int mt = 0; mt < MT; ++mt)
-              mma_bf16(acc + (uint32_t)(mt * BN), sw128_desc(sa + (uint32_t)(mt * A_BYTES) + 32u * k),
-                       sw128_desc(sb + 32u * k), idesc, (i > 0 || k > 0) ? 1u : 0u);
+              for (int mt = 0; mt < MT; ++mt)
+                mma_bf16(acc + (uint32_t)(mt * BN),
+                         noswz_desc(atap + (uint32_t)(2 * k * HP::kKg + mt * 16 * HP::kCols * 16), (uint32_t)HP::kKg,
+                                    (uint32_t)(HP::kCols * 16)),
+                         sw128_desc(bs + 32u * k), idesc, (cc > 0 || tap > 0 || k > 0) ? 1u : 0u);
+            }
+            mma_commit(smem_u32(&bempty[sb]));
+            ++qb;
           }
-          mma_commit(smem_u32(&empty_bar[s]));
+          if (bad) break;
+          mma_commit(smem_u32(&aempty[sa]));
+          ++qa;
         }
         if (!bad) mma_commit(smem_u32(&tfull_bar[a]));
       }
-      // Committed on the abort path too: done_bar completes once every MMA issued so far has
-      // finished, so TMEM is not written after the CTA releases it.
-      mma_commit(smem_u32(&done_bar));
+      mma_commit(smem_u32(&done_bar));  // also on abort, so TMEM is idle before it is freed
     }
   } else {
     // ---------------------------------------------------------------- epilogue (warps 2..5)
-    const int qw = warp & 3;  // TMEM lane quadrant this warp may read
-    const int m = qw * 32 + lane;
+    const int qw = warp & 3;        // the TMEM lane quadrant this warp may read
+    const int half = (warp - 2) >> 2;  // which half of the columns it drains
+    const int m = qw * 32 + lane;  // accumulator row: patch row m / 8, column m % 8
     int j = 0;
     for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, ++j) {
       const int a = j & 1;
@@ -243,17 +281,19 @@ conv3x3_tc_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_const
                                                         kErrEpi)) &&
                       *(volatile int*)err == 0;
       fence_after();
-      if (!ok) break;  // the error word is set; no store of this tile happens
+      if (!ok) break;
       int img, y0, x0, n0;
       coord(t, img, y0, x0, n0);
 #pragma unroll
       for (int mt = 0; mt < MT; ++mt) {
-        const size_t pix = ((size_t)img * H + y0 + mt * TH + m / TW) * W + x0 + m % TW;
+        const int py = y0 + 16 * mt + m / 8, px = x0 + m % 8;
+        const bool inside = py < H;
+        const size_t pix = ((size_t)img * H + py) * W + px;
 #pragma unroll 1
-        for (int c0 = 0; c0 < BN; c0 += 32) {
+        for (int c0 = half * (BN / 2); c0 < (half + 1) * (BN / 2); c0 += 32) {
           uint32_t r[32];
           tmem_ld32(tmem + ((uint32_t)(qw * 32) << 16) + (uint32_t)(a * ACC_COLS + mt * BN + c0), r);
-          epilogue_store32<EPI>(r, bias, mask, addend, y, pix * Cout + n0 + c0, n0 + c0);
+          if (inside) epilogue_store32<EPI>(r, bias, mask, addend, y, pix * Cout + n0 + c0, n0 + c0);
         }
       }
       fence_before();
@@ -264,7 +304,6 @@ conv3x3_tc_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_const
   fence_before();
   __syncthreads();
   if (warp == 1) {
-    // every MMA must be complete before TMEM is released (bounded wait for the final commit)
     uint32_t it = 0;
     while (!mbar_try(smem_u32(&done_bar), 0u) && ++it < kSpin) {
     }
@@ -292,20 +331,19 @@ int get_tensor_map_encoder(PFN_cuTensorMapEncodeTiled_v12000* out) {
 constexpr size_t kStageBudget = 200 * 1024;  // ring bytes per CTA (one CTA per SM)
 
 template <int BN, int MT>
-constexpr int conv_stages() {
-  return (int)(kStageBudget / (size_t)(MT * BM * BK * 2 + BN * BK * 2)) < 8
-             ? (int)(kStageBudget / (size_t)(MT * BM * BK * 2 + BN * BK * 2))
+constexpr int halo_bstages() {
+  return (int)((kStageBudget - 2 * (size_t)Halo<MT>::kABytes) / (size_t)(BN * BK * 2)) < 8
+             ? (int)((kStageBudget - 2 * (size_t)Halo<MT>::kABytes) / (size_t)(BN * BK * 2))
              : 8;
 }
 
 template <int BN, int MT, int EPI>
-static int launch(const CUtensorMap& mx, const CUtensorMap& mw, const float* bias, const void* mask,
-                  const void* addend, void* y, int n, int h, int w, int cin, int cout, int* err, cudaStream_t st) {
-  constexpr int STAGES = conv_stages<BN, MT>();
-  static_assert(STAGES >= 3, "ring too shallow");
-  auto kern = conv3x3_tc_kernel<BN, MT, STAGES, EPI>;
-  const size_t smem = (size_t)STAGES * (MT * BM * BK * 2 + BN * BK * 2) + 1024;
-  // cudaFuncSetAttribute applies to the current device only: remember it per device ordinal
+static int launch_halo(const CUtensorMap& mx, const CUtensorMap& mw, const float* bias, const void* mask,
+                       const void* addend, void* y, int n, int h, int w, int cin, int cout, int* err, cudaStream_t st) {
+  constexpr int BST = halo_bstages<BN, MT>();
+  static_assert(BST >= 3, "weight ring too shallow");
+  auto kern = conv3x3_halo_kernel<BN, MT, 2, BST, EPI>;
+  const size_t smem = (size_t)BST * BN * BK * 2 + 2 * (size_t)Halo<MT>::kABytes + 1024;
   static std::atomic<bool> attr[64];
   static std::atomic<int> sms[64];
   int dev = 0;
@@ -322,24 +360,24 @@ static int launch(const CUtensorMap& mx, const CUtensorMap& mw, const float* bia
       return fail(SVBRDF_ERR_CUDA, "conv3x3: no SM count");
     sms[dev].store(c);
   }
-  const long long tiles = (long long)n * (h / (TH * MT)) * (w / TW) * (cout / BN);
+  const long long tiles = (long long)n * ((h + 16 * MT - 1) / (16 * MT)) * (w / 8) * (cout / BN);
   if (tiles >= (1LL << 31)) return fail(SVBRDF_ERR_UNSUPPORTED, "conv3x3: too many tiles");
   const int grid = (int)(tiles < sms[dev].load() ? tiles : sms[dev].load());
   kern<<<grid, kThreads, smem, st>>>(mx, mw, bias, (const __nv_bfloat16*)mask, (const __nv_bfloat16*)addend,
                                      (__nv_bfloat16*)y, n, h, w, cin, cout, err);
-  return check_launch("conv3x3_tc_kernel");
+  return check_launch("conv3x3_halo_kernel");
 }
 
 template <int BN, int MT>
-static int dispatch_epi(int epi, const CUtensorMap& mx, const CUtensorMap& mw, const float* bias, const void* mask,
-                        const void* addend, void* y, int n, int h, int w, int cin, int cout, int* err,
-                        cudaStream_t st) {
+static int dispatch_halo(int epi, const CUtensorMap& mx, const CUtensorMap& mw, const float* bias, const void* mask,
+                         const void* addend, void* y, int n, int h, int w, int cin, int cout, int* err,
+                         cudaStream_t st) {
   switch (epi) {
-    case kEpiNone: return launch<BN, MT, kEpiNone>(mx, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st);
+    case kEpiNone: return launch_halo<BN, MT, kEpiNone>(mx, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st);
     case kEpiBiasRelu:
-      return launch<BN, MT, kEpiBiasRelu>(mx, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st);
-    case kEpiMask: return launch<BN, MT, kEpiMask>(mx, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st);
-    default: return launch<BN, MT, kEpiAddMask>(mx, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st);
+      return launch_halo<BN, MT, kEpiBiasRelu>(mx, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st);
+    case kEpiMask: return launch_halo<BN, MT, kEpiMask>(mx, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st);
+    default: return launch_halo<BN, MT, kEpiAddMask>(mx, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st);
   }
 }
 
@@ -369,17 +407,7 @@ extern "C" int svbrdf_conv3x3_bf16_ex(const void* x, const void* weight, const f
   int rc = get_tensor_map_encoder(&g_encode);
   if (rc) return rc;
   const int bn = (cout % 256 == 0) ? 256 : (cout % 128 == 0 ? 128 : 64);
-  CUtensorMap mx, mw;
-  {
-    const cuuint64_t dims[4] = {(cuuint64_t)cin, (cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)n};
-    const cuuint64_t strides[3] = {(cuuint64_t)cin * 2, (cuuint64_t)w * cin * 2, (cuuint64_t)h * w * cin * 2};
-    const cuuint32_t box[4] = {(cuuint32_t)BK, (cuuint32_t)TW, (cuuint32_t)TH, 1};
-    const cuuint32_t es[4] = {1, 1, 1, 1};
-    const CUresult r = g_encode(&mx, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(x), dims, strides, box, es,
-                                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
-                                CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) return fail(SVBRDF_ERR_CUDA, "cuTensorMapEncodeTiled(x) failed: %d", (int)r);
-  }
+  CUtensorMap mw;
   {
     const cuuint64_t dims[2] = {(cuuint64_t)9 * cin, (cuuint64_t)cout};
     const cuuint64_t strides[1] = {(cuuint64_t)9 * cin * 2};
@@ -391,17 +419,29 @@ extern "C" int svbrdf_conv3x3_bf16_ex(const void* x, const void* weight, const f
     if (r != CUDA_SUCCESS) return fail(SVBRDF_ERR_CUDA, "cuTensorMapEncodeTiled(weight) failed: %d", (int)r);
   }
   cudaStream_t st = (cudaStream_t)stream;
-  // two stacked 8 x 16 patches per tile (each weight slice feeds 256 pixels) where H allows and
-  // Cout fits two double-buffered pairs of accumulators in TMEM
-  const bool two = h % (2 * TH) == 0 && bn <= 128;
-  switch (bn) {
-    case 256: return dispatch_epi<256, 1>(epilogue, mx, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st);
-    case 128:
-      return two ? dispatch_epi<128, 2>(epilogue, mx, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st)
-                 : dispatch_epi<128, 1>(epilogue, mx, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st);
-    default:
-      return two ? dispatch_epi<64, 2>(epilogue, mx, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st)
-                 : dispatch_epi<64, 1>(epilogue, mx, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st);
+  {
+    // the (16 MT + 2) x 10 input patch of each 64-channel chunk, loaded once: 8 channels (16
+    // bytes) per pixel per channel group, no swizzle; two stacked patches per tile where the map
+    // has 32+ rows and Cout fits two double-buffered pairs of accumulators in TMEM
+    const int mt = (bn <= 128 && h >= 32) ? 2 : 1;
+    CUtensorMap mh;
+    const cuuint64_t dims[4] = {(cuuint64_t)cin, (cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)n};
+    const cuuint64_t strides[3] = {(cuuint64_t)cin * 2, (cuuint64_t)w * cin * 2, (cuuint64_t)h * w * cin * 2};
+    const cuuint32_t box[4] = {8u, 10u, (cuuint32_t)(16 * mt + 2), 1u};
+    const cuuint32_t es[4] = {1, 1, 1, 1};
+    const CUresult r = g_encode(&mh, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(x), dims, strides, box, es,
+                                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(SVBRDF_ERR_CUDA, "cuTensorMapEncodeTiled(halo x) failed: %d", (int)r);
+    switch (bn) {
+      case 256: return dispatch_halo<256, 1>(epilogue, mh, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st);
+      case 128:
+        return mt == 2 ? dispatch_halo<128, 2>(epilogue, mh, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st)
+                       : dispatch_halo<128, 1>(epilogue, mh, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st);
+      default:
+        return mt == 2 ? dispatch_halo<64, 2>(epilogue, mh, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st)
+                       : dispatch_halo<64, 1>(epilogue, mh, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st);
+    }
   }
 }
 

@@ -66,6 +66,7 @@ struct Geom {
   int TH, TW, NB;  // one M-tile: NB images x TH rows x TW columns = 128 output pixels
   int pad, taps;
   int tiles_x, tiles_y, tiles_b, tiles_n;  // CTA tiles along x, y (TH * MT rows), images, Cout / BN
+  int splits, kper;  // K split into `splits` ranges of kper (tap, chunk) steps; 1 = no split
 };
 
 // One CTA tile: MT M-tiles stacked along y (MT * TH rows) x BN output channels.
@@ -91,7 +92,7 @@ __device__ __forceinline__ TileCoord tile_coord(const Geom& g, int t) {
 template <int BN, int MT, int STAGES>
 __global__ void __launch_bounds__(kThreads, 1)
 conv_tf32_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_constant__ CUtensorMap tmap_w,
-                 float* __restrict__ y, Geom g, int* err) {
+                 float* __restrict__ y, float* __restrict__ ws, Geom g, int* err) {
   constexpr int A_BYTES = BM * BK * 4;
   constexpr int B_BYTES = BN * BK * 4;
   constexpr int STAGE = MT * A_BYTES + B_BYTES;
@@ -108,7 +109,8 @@ conv_tf32_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_consta
 
   const uint32_t base = (smem_u32(dsmem) + 1023u) & ~1023u;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int n_tiles = g.tiles_b * g.tiles_y * g.tiles_x * g.tiles_n;
+  // work items: (tile, K range); with splits > 1 each writes an FP32 partial plane of ws
+  const int n_items = g.tiles_b * g.tiles_y * g.tiles_x * g.tiles_n * g.splits;
   const int kchunks = g.Cin / BK;
   const int total = g.taps * kchunks;
   const int ks = g.taps == 9 ? 3 : 1;
@@ -140,9 +142,10 @@ conv_tf32_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_consta
     if (lane == 0) {
       int q = 0;  // stages issued by this CTA
       bool bad = false;
-      for (int t = blockIdx.x; t < n_tiles && !bad; t += gridDim.x) {
-        const TileCoord c = tile_coord<BN, MT>(g, t);
-        for (int i = 0; i < total; ++i) {
+      for (int w = blockIdx.x; w < n_items && !bad; w += gridDim.x) {
+        const TileCoord c = tile_coord<BN, MT>(g, w / g.splits);
+        const int k_lo = (w % g.splits) * g.kper, k_hi = min(total, k_lo + g.kper);
+        for (int i = k_lo; i < k_hi; ++i) {
           const int s = q % STAGES;
           const uint32_t ph = (uint32_t)(q / STAGES) & 1u;
           if (q >= STAGES && !mbar_wait(smem_u32(&empty_bar[s]), ph ^ 1u, err, kErrTma)) {
@@ -174,13 +177,14 @@ conv_tf32_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_consta
       constexpr uint32_t id = idesc_tf32(BM, BN);
       int q = 0, j = 0;
       bool bad = false;
-      for (int t = blockIdx.x; t < n_tiles && !bad; t += gridDim.x, ++j) {
+      for (int w = blockIdx.x; w < n_items && !bad; w += gridDim.x, ++j) {
+        const int k_lo = (w % g.splits) * g.kper, k_hi = min(total, k_lo + g.kper);
         const int a = j & 1;
         // the epilogue must have drained this buffer's previous tile (j - 2)
         if (j >= 2 && !mbar_wait(smem_u32(&tempty_bar[a]), ((uint32_t)(j >> 1) & 1u) ^ 1u, err, kErrMma)) break;
         fence_after();
         const uint32_t acc = tmem + (uint32_t)a * ACC_COLS;
-        for (int i = 0; i < total; ++i, ++q) {
+        for (int i = k_lo; i < k_hi; ++i, ++q) {
           const int s = q % STAGES;
           const uint32_t ph = (uint32_t)(q / STAGES) & 1u;
           if (!mbar_wait(smem_u32(&full_bar[s]), ph, err, kErrMma)) {
@@ -195,7 +199,7 @@ conv_tf32_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_consta
 #pragma unroll
             for (int mt = 0; mt < MT; ++mt)
               mma_tf32(acc + (uint32_t)(mt * BN), sw128_desc(sa + (uint32_t)(mt * A_BYTES) + 32u * k),
-                       sw128_desc(sb + 32u * k), id, (i > 0 || k > 0) ? 1u : 0u);
+                       sw128_desc(sb + 32u * k), id, (i > k_lo || k > 0) ? 1u : 0u);
           }
           mma_commit(smem_u32(&empty_bar[s]));
         }
@@ -207,14 +211,15 @@ conv_tf32_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_consta
     const int qw = warp & 3;  // TMEM lanes 32 qw .. 32 qw + 31
     const int m = qw * 32 + lane;
     int j = 0;
-    for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, ++j) {
+    for (int w = blockIdx.x; w < n_items; w += gridDim.x, ++j) {
       const int a = j & 1;
       const bool ok = __all_sync(0xffffffffu, mbar_wait(smem_u32(&tfull_bar[a]), (uint32_t)(j >> 1) & 1u, err,
                                                         kErrEpi)) &&
                       *(volatile int*)err == 0;
       fence_after();
       if (!ok) break;
-      const TileCoord c = tile_coord<BN, MT>(g, t);
+      const TileCoord c = tile_coord<BN, MT>(g, w / g.splits);
+      float* dst = g.splits > 1 ? ws + (size_t)(w % g.splits) * ((size_t)g.B * g.Ho * g.Wo * g.Cout) : y;
       const int pb = c.b0 + m / (g.TH * g.TW);
       const int rem = m % (g.TH * g.TW);
       const int px = c.x0 + rem % g.TW;
@@ -222,9 +227,233 @@ conv_tf32_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_consta
       for (int mt = 0; mt < MT; ++mt) {
         const int py = c.y0 + mt * g.TH + rem / g.TW;
         const bool inside = pb < g.B && py < g.Ho && px < g.Wo;
-        float* out = y + (((size_t)pb * g.Ho + py) * g.Wo + px) * g.Cout + c.n0;
+        float* out = dst + (((size_t)pb * g.Ho + py) * g.Wo + px) * g.Cout + c.n0;
 #pragma unroll 1
         for (int c0 = 0; c0 < BN; c0 += 32) {
+          uint32_t r[32];
+          tmem_ld32(tmem + ((uint32_t)(qw * 32) << 16) + (uint32_t)(a * ACC_COLS + mt * BN + c0), r);
+          if (inside) {
+            float4* o4 = reinterpret_cast<float4*>(out + c0);
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+              o4[u] = make_float4(__uint_as_float(r[4 * u]), __uint_as_float(r[4 * u + 1]),
+                                  __uint_as_float(r[4 * u + 2]), __uint_as_float(r[4 * u + 3]));
+          }
+        }
+      }
+      fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(smem_u32(&tempty_bar[a]));
+    }
+  }
+  fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    uint32_t it = 0;
+    while (!mbar_try(smem_u32(&done_bar), 0u) && ++it < kSpin) {
+    }
+    fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+  }
+}
+
+// ---------------------------------------------------------------- halo form
+// Maps of 16+ rows and 8+ columns load each input patch once per 32-channel chunk, halo
+// included, and share it between the taps. A tile is MT stacked 16-row x 8-column output
+// patches of one image; its input is the (16 MT + KS - 1) x (8 + KS - 1) patch starting at
+// (y0 - pad, x0 - pad). Shared memory holds it K-major without swizzle: for each 4-channel
+// (16-byte) group g, the patch's pixels row-major at 16 bytes each, groups kKg bytes apart
+// (128-byte aligned). Accumulator row r of M-tile mt is output pixel (16 mt + r / 8, r % 8), so
+// tap (ky, kx) reads the descriptor started at patch pixel ky kCols + kx, with 8-row groups
+// kCols x 16 bytes apart (SBO) and K-adjacent core matrices one channel group apart (LBO). The
+// taps' BN x 32 weight slices stream through their own ring (128-byte swizzle). Per chunk a
+// tile loads about 1.4 x MT x 16 KB of input instead of taps x MT x 16 KB. A work item is (tile,
+// range of chunks); with splits > 1 its partial goes to plane `split` of ws.
+template <int MT, int KS>
+struct HaloT {
+  static constexpr int kRows = 16 * MT + KS - 1, kCols = 8 + KS - 1;
+  static constexpr int kKg = ((kRows * kCols * 16 + 127) / 128) * 128;
+  static constexpr int kABytes = 8 * kKg;  // 32 channels
+};
+
+constexpr int kHaloThreads = 320;  // warp 0 TMA, warp 1 MMA + TMEM owner, warps 2..9 epilogue (two per
+                                   // TMEM lane quadrant, each draining half the columns)
+
+template <int BN, int MT, int KS, int AST, int BST>
+__global__ void __launch_bounds__(kHaloThreads, 1)
+conv_tf32_halo_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_constant__ CUtensorMap tmap_w,
+                      float* __restrict__ y, float* __restrict__ ws, Geom g, int* err) {
+  using HP = HaloT<MT, KS>;
+  constexpr int B_BYTES = BN * BK * 4;
+  constexpr int TAPS = KS * KS;
+  constexpr uint32_t ACC_COLS = MT * BN;
+  constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;
+  static_assert(TMEM_COLS >= 32 && TMEM_COLS <= 512 && (TMEM_COLS & (TMEM_COLS - 1)) == 0, "TMEM columns");
+  static_assert(B_BYTES % 1024 == 0, "weight slices keep the 1024-byte swizzle alignment");
+  extern __shared__ uint8_t dsmem[];
+  __shared__ __align__(8) uint64_t afull[AST], aempty[AST], bfull[BST], bempty[BST];
+  __shared__ __align__(8) uint64_t tfull_bar[2], tempty_bar[2], done_bar;
+  __shared__ uint32_t tmem_slot;
+
+  const uint32_t bbase = (smem_u32(dsmem) + 1023u) & ~1023u;
+  const uint32_t abase = bbase + (uint32_t)(BST * B_BYTES);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int n_items = g.tiles_b * g.tiles_y * g.tiles_x * g.tiles_n * g.splits;
+  const int kchunks = g.Cin / BK;
+  auto coord = [&](int t, int& img, int& y0, int& x0, int& n0) {
+    n0 = (t % g.tiles_n) * BN;
+    int r = t / g.tiles_n;
+    x0 = (r % g.tiles_x) * 8;
+    r /= g.tiles_x;
+    y0 = (r % g.tiles_y) * (16 * MT);
+    img = r / g.tiles_y;
+  };
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < AST; ++s) {
+      mbar_init(smem_u32(&afull[s]), 1);
+      mbar_init(smem_u32(&aempty[s]), 1);
+    }
+    for (int s = 0; s < BST; ++s) {
+      mbar_init(smem_u32(&bfull[s]), 1);
+      mbar_init(smem_u32(&bempty[s]), 1);
+    }
+    for (int a = 0; a < 2; ++a) {
+      mbar_init(smem_u32(&tfull_bar[a]), 1);
+      mbar_init(smem_u32(&tempty_bar[a]), 8);
+    }
+    mbar_init(smem_u32(&done_bar), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  fence_before();
+  __syncthreads();
+  fence_after();
+  const uint32_t tmem = tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int qa = 0, qb = 0;
+      bool bad = false;
+      for (int w = blockIdx.x; w < n_items && !bad; w += gridDim.x) {
+        int img, y0, x0, n0;
+        coord(w / g.splits, img, y0, x0, n0);
+        const int c_lo = (w % g.splits) * g.kper, c_hi = min(kchunks, c_lo + g.kper);
+        for (int cc = c_lo; cc < c_hi && !bad; ++cc) {
+          const int sa = qa % AST;
+          if (qa >= AST && !mbar_wait(smem_u32(&aempty[sa]), ((uint32_t)(qa / AST) & 1u) ^ 1u, err, kErrTma)) {
+            bad = true;
+            break;
+          }
+          const uint32_t fa = smem_u32(&afull[sa]);
+          mbar_expect_tx(fa, (uint32_t)(8 * HP::kRows * HP::kCols * 16));
+#pragma unroll 1
+          for (int q = 0; q < 8; ++q)
+            tma_4d(abase + (uint32_t)(sa * HP::kABytes + q * HP::kKg), &tmap_x, cc * BK + 4 * q, x0 - g.pad,
+                   y0 - g.pad, img, fa);
+          ++qa;
+          for (int tap = 0; tap < TAPS; ++tap) {
+            const int sb = qb % BST;
+            if (qb >= BST && !mbar_wait(smem_u32(&bempty[sb]), ((uint32_t)(qb / BST) & 1u) ^ 1u, err, kErrTma)) {
+              bad = true;
+              break;
+            }
+            const uint32_t fb = smem_u32(&bfull[sb]);
+            mbar_expect_tx(fb, (uint32_t)B_BYTES);
+            tma_2d(bbase + (uint32_t)(sb * B_BYTES), &tmap_w, tap * g.Cin + cc * BK, n0, fb);
+            ++qb;
+          }
+        }
+      }
+      if (bad) {  // let the copies in flight land before the CTA can exit
+        for (int i = qa > AST ? qa - AST : 0; i < qa; ++i) {
+          uint32_t it = 0;
+          while (!mbar_try(smem_u32(&afull[i % AST]), (uint32_t)(i / AST) & 1u) && ++it < kSpin) {
+          }
+        }
+        for (int i = qb > BST ? qb - BST : 0; i < qb; ++i) {
+          uint32_t it = 0;
+          while (!mbar_try(smem_u32(&bfull[i % BST]), (uint32_t)(i / BST) & 1u) && ++it < kSpin) {
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      constexpr uint32_t id = idesc_tf32(BM, BN);
+      int qa = 0, qb = 0, j = 0;
+      bool bad = false;
+      for (int w = blockIdx.x; w < n_items && !bad; w += gridDim.x, ++j) {
+        const int a = j & 1;
+        if (j >= 2 && !mbar_wait(smem_u32(&tempty_bar[a]), ((uint32_t)(j >> 1) & 1u) ^ 1u, err, kErrMma)) break;
+        fence_after();
+        const uint32_t acc = tmem + (uint32_t)a * ACC_COLS;
+        const int c_lo = (w % g.splits) * g.kper, c_hi = min(kchunks, c_lo + g.kper);
+        for (int cc = c_lo; cc < c_hi && !bad; ++cc) {
+          const int sa = qa % AST;
+          if (!mbar_wait(smem_u32(&afull[sa]), (uint32_t)(qa / AST) & 1u, err, kErrMma)) {
+            bad = true;
+            break;
+          }
+          const uint32_t achunk = abase + (uint32_t)(sa * HP::kABytes);
+          for (int tap = 0; tap < TAPS; ++tap) {
+            const int sb = qb % BST;
+            if (!mbar_wait(smem_u32(&bfull[sb]), (uint32_t)(qb / BST) & 1u, err, kErrMma)) {
+              bad = true;
+              break;
+            }
+            fence_after();
+            const uint32_t atap = achunk + (uint32_t)(((tap / KS) * HP::kCols + tap % KS) * 16);
+            const uint32_t bs = bbase + (uint32_t)(sb * B_BYTES);
+#pragma unroll
+            for (int k = 0; k < BK / 8; ++k) {  // 8 TF32 channels = two channel groups per MMA
+#pragma unroll
+              for (int mt = 0; mt < MT; ++mt)
+                mma_tf32(acc + (uint32_t)(mt * BN),
+                         noswz_desc(atap + (uint32_t)(2 * k * HP::kKg + mt * 16 * HP::kCols * 16), (uint32_t)HP::kKg,
+                                    (uint32_t)(HP::kCols * 16)),
+                         sw128_desc(bs + 32u * k), id, (cc > c_lo || tap > 0 || k > 0) ? 1u : 0u);
+            }
+            mma_commit(smem_u32(&bempty[sb]));
+            ++qb;
+          }
+          if (bad) break;
+          mma_commit(smem_u32(&aempty[sa]));
+          ++qa;
+        }
+        if (!bad) mma_commit(smem_u32(&tfull_bar[a]));
+      }
+      mma_commit(smem_u32(&done_bar));  // also on abort, so TMEM is idle before it is freed
+    }
+  } else {
+    const int qw = warp & 3;        // the TMEM lane quadrant this warp may read
+    const int half = (warp - 2) >> 2;  // which half of the columns it drains (BN = 32: half 0 only)
+    constexpr int HCOLS = BN >= 64 ? BN / 2 : BN;
+    const int m = qw * 32 + lane;  // accumulator row: patch row m / 8, column m % 8
+    int j = 0;
+    for (int w = blockIdx.x; w < n_items; w += gridDim.x, ++j) {
+      const int a = j & 1;
+      const bool ok = __all_sync(0xffffffffu, mbar_wait(smem_u32(&tfull_bar[a]), (uint32_t)(j >> 1) & 1u, err,
+                                                        kErrEpi)) &&
+                      *(volatile int*)err == 0;
+      fence_after();
+      if (!ok) break;
+      int img, y0, x0, n0;
+      coord(w / g.splits, img, y0, x0, n0);
+      float* dst = g.splits > 1 ? ws + (size_t)(w % g.splits) * ((size_t)g.B * g.Ho * g.Wo * g.Cout) : y;
+      const int px = x0 + m % 8;
+#pragma unroll
+      for (int mt = 0; mt < MT; ++mt) {
+        const int py = y0 + 16 * mt + m / 8;
+        const bool inside = py < g.Ho && px < g.Wo;
+        float* out = dst + (((size_t)img * g.Ho + py) * g.Wo + px) * g.Cout + n0;
+#pragma unroll 1
+        for (int c0 = half * HCOLS; c0 < BN && c0 < (half + 1) * HCOLS; c0 += 32) {
           uint32_t r[32];
           tmem_ld32(tmem + ((uint32_t)(qw * 32) << 16) + (uint32_t)(a * ACC_COLS + mt * BN + c0), r);
           if (inside) {
@@ -261,54 +490,52 @@ constexpr int stages_for() {
              : 8;
 }
 
-template <int BN, int MT>
-static int launch(const CUtensorMap& mx, const CUtensorMap& mw, float* y, Geom g, int* err, cudaStream_t st) {
-  constexpr int STAGES = stages_for<BN, MT>();
-  static_assert(STAGES >= 3, "ring too shallow");
-  static std::atomic<size_t> have[64];
+// K-split partial planes summed in split order: y[i] = sum_s ws[s][i] (float4 over i).
+__global__ void __launch_bounds__(256) conv_tf32_split_sum_kernel(const float4* __restrict__ ws, float4* __restrict__ y,
+                                                                   long long n4, int splits) {
+  for (long long i = blockIdx.x * 256LL + threadIdx.x; i < n4; i += (long long)gridDim.x * 256) {
+    float4 a = __ldg(ws + i);
+    for (int s = 1; s < splits; ++s) {
+      const float4 b = __ldg(ws + (long long)s * n4 + i);
+      a.x += b.x;
+      a.y += b.y;
+      a.z += b.z;
+      a.w += b.w;
+    }
+    y[i] = a;
+  }
+}
+
+static int sm_count(int* out) {
   static std::atomic<int> sms[64];
-  const size_t smem = (size_t)STAGES * (MT * BM * BK * 4 + BN * BK * 4) + 1024;
-  auto kern = conv_tf32_kernel<BN, MT, STAGES>;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return fail(SVBRDF_ERR_CUDA, "no usable device");
-  if (have[dev].load() < smem) {
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-      return fail(SVBRDF_ERR_CUDA, "cudaFuncSetAttribute: %s", cudaGetErrorString(cudaGetLastError()));
-    have[dev].store(smem);
-  }
   if (sms[dev].load() == 0) {
     int n = 0;
     if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1)
       return fail(SVBRDF_ERR_CUDA, "no SM count");
     sms[dev].store(n);
   }
-  g.tiles_x = (g.Wo + g.TW - 1) / g.TW;
-  g.tiles_y = (g.Ho + g.TH * MT - 1) / (g.TH * MT);
-  g.tiles_b = (g.B + g.NB - 1) / g.NB;
-  g.tiles_n = g.Cout / BN;
-  const long long tiles = (long long)g.tiles_b * g.tiles_y * g.tiles_x * g.tiles_n;
-  if (tiles >= (1LL << 31)) return fail(SVBRDF_ERR_UNSUPPORTED, "conv_tf32: too many tiles");
-  const int grid = (int)(tiles < sms[dev].load() ? tiles : sms[dev].load());
-  kern<<<grid, kThreads, smem, st>>>(mx, mw, y, g, err);
-  return check_launch("conv_tf32_kernel");
+  *out = sms[dev].load();
+  return SVBRDF_OK;
 }
 
-}  // namespace tf32
-}  // namespace svb
-
-using namespace svb;
-
-extern "C" int svbrdf_gen_conv_tf32(const float* x, const float* weight, float* y, int b, int hin, int win, int cin,
-                                    int cout, int ksize, int pad, int* err, void* stream) {
-  using namespace svb::tf32;
-  if (!x || !weight || !y || !err) return fail(SVBRDF_ERR_INVALID, "conv_tf32: null x/weight/y/err");
+// The convolution's shape, patch, CTA tiling and K split. Maps with fewer CTA tiles than half
+// the SMs split K (taps x channel chunks, at least 4 steps a split) so that about one CTA per
+// SM has work; the splits then need a workspace of splits x B x Ho x Wo x Cout floats.
+struct Plan {
+  Geom g;
+  int bn, mt;
+  int halo, ks;  // the halo form (maps of 16+ rows, 8+ columns) and the kernel size
+};
+static int plan_conv(int b, int hin, int win, int cin, int cout, int ksize, int pad, int sms, Plan* pl) {
   if (ksize != 1 && ksize != 3) return fail(SVBRDF_ERR_INVALID, "conv_tf32: ksize must be 1 or 3");
   if (pad < 0 || pad > (ksize == 3 ? 2 : 0)) return fail(SVBRDF_ERR_INVALID, "conv_tf32: bad pad %d", pad);
   if (b < 1 || hin < 1 || win < 1 || cin < BK || cin % BK || cin > 8192)
     return fail(SVBRDF_ERR_UNSUPPORTED, "conv_tf32: Cin must be a multiple of %d (got %d)", BK, cin);
   if (cout < 32 || !(cout % 256 == 0 || cout == 128 || cout == 64 || cout == 32))
     return fail(SVBRDF_ERR_UNSUPPORTED, "conv_tf32: Cout must be 32, 64, 128 or a multiple of 256 (got %d)", cout);
-  Geom g;
+  Geom& g = pl->g;
   g.B = b; g.Hin = hin; g.Win = win; g.Cin = cin; g.Cout = cout; g.pad = pad; g.taps = ksize * ksize;
   g.Ho = hin + 2 * pad - (ksize - 1);
   g.Wo = win + 2 * pad - (ksize - 1);
@@ -320,11 +547,167 @@ extern "C" int svbrdf_gen_conv_tf32(const float* x, const float* weight, float* 
   else return fail(SVBRDF_ERR_UNSUPPORTED, "conv_tf32: output narrower than 4");
   if ((long long)b * hin * win * cin >= (1LL << 40) || (long long)b * g.Ho * g.Wo >= (1LL << 31))
     return fail(SVBRDF_ERR_UNSUPPORTED, "conv_tf32: tensor too large");
-  if (((uintptr_t)x | (uintptr_t)weight | (uintptr_t)y) % 16) return fail(SVBRDF_ERR_INVALID, "conv_tf32: 16-byte alignment");
-  PFN_cuTensorMapEncodeTiled_v12000 enc = nullptr;
-  int rc = get_tensor_map_encoder(&enc);
+  pl->bn = cout >= 256 ? 256 : cout;
+  pl->ks = ksize;
+  pl->halo = (g.Wo >= 8 && g.Ho >= 16) ? 1 : 0;
+  if (pl->halo) {
+    // 16-row x 8-column patches, two stacked where the map has 32+ rows and Cout fits two
+    // double-buffered accumulators in TMEM; K splits count 32-channel chunks (all taps each)
+    g.TW = 8; g.TH = 16; g.NB = 1;
+    pl->mt = (pl->bn <= 128 && g.Ho >= 32) ? 2 : 1;
+    g.tiles_x = (g.Wo + 7) / 8;
+    g.tiles_y = (g.Ho + 16 * pl->mt - 1) / (16 * pl->mt);
+    g.tiles_b = g.B;
+    g.tiles_n = g.Cout / pl->bn;
+    const long long tiles = (long long)g.tiles_b * g.tiles_y * g.tiles_x * g.tiles_n;
+    if (tiles >= (1LL << 30)) return fail(SVBRDF_ERR_UNSUPPORTED, "conv_tf32: too many tiles");
+    const int chunks = cin / BK;
+    int splits = 1;
+    if (2 * tiles < sms) {
+      splits = (int)(sms / tiles);
+      if (splits > chunks / 2) splits = chunks / 2;
+      if (splits < 1) splits = 1;
+    }
+    g.kper = (chunks + splits - 1) / splits;
+    g.splits = (chunks + g.kper - 1) / g.kper;
+    return SVBRDF_OK;
+  }
+  // two M-tiles per CTA tile (one weight slice feeds 256 output pixels) where the map has 16+
+  // rows and Cout fits two double-buffered accumulators in TMEM
+  pl->mt = (g.NB == 1 && g.Ho >= 16 && pl->bn <= 128) ? 2 : 1;
+  g.tiles_x = (g.Wo + g.TW - 1) / g.TW;
+  g.tiles_y = (g.Ho + g.TH * pl->mt - 1) / (g.TH * pl->mt);
+  g.tiles_b = (g.B + g.NB - 1) / g.NB;
+  g.tiles_n = g.Cout / pl->bn;
+  const long long tiles = (long long)g.tiles_b * g.tiles_y * g.tiles_x * g.tiles_n;
+  if (tiles >= (1LL << 30)) return fail(SVBRDF_ERR_UNSUPPORTED, "conv_tf32: too many tiles");
+  const int total = g.taps * (cin / BK);
+  int splits = 1;
+  if (2 * tiles < sms) {
+    splits = (int)(sms / tiles);
+    if (splits > total / 4) splits = total / 4;
+    if (splits < 1) splits = 1;
+  }
+  g.kper = (total + splits - 1) / splits;
+  g.splits = (total + g.kper - 1) / g.kper;  // no empty split
+  return SVBRDF_OK;
+}
+
+static long long split_ws_floats(const Geom& g) {
+  return g.splits > 1 ? (long long)g.splits * g.B * g.Ho * g.Wo * g.Cout : 0;
+}
+
+template <int BN, int MT>
+static int launch(const CUtensorMap& mx, const CUtensorMap& mw, float* y, float* ws, const Geom& g, int sms, int* err,
+                  cudaStream_t st) {
+  constexpr int STAGES = stages_for<BN, MT>();
+  static_assert(STAGES >= 3, "ring too shallow");
+  static std::atomic<size_t> have[64];
+  const size_t smem = (size_t)STAGES * (MT * BM * BK * 4 + BN * BK * 4) + 1024;
+  auto kern = conv_tf32_kernel<BN, MT, STAGES>;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return fail(SVBRDF_ERR_CUDA, "no usable device");
+  if (have[dev].load() < smem) {
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+      return fail(SVBRDF_ERR_CUDA, "cudaFuncSetAttribute: %s", cudaGetErrorString(cudaGetLastError()));
+    have[dev].store(smem);
+  }
+  const long long items = (long long)g.tiles_b * g.tiles_y * g.tiles_x * g.tiles_n * g.splits;
+  const int grid = (int)(items < sms ? items : sms);
+  kern<<<grid, kThreads, smem, st>>>(mx, mw, y, ws, g, err);
+  int rc = check_launch("conv_tf32_kernel");
+  if (rc || g.splits == 1) return rc;
+  const long long n4 = (long long)g.B * g.Ho * g.Wo * g.Cout / 4;
+  const long long blocks = (n4 + 255) / 256;
+  conv_tf32_split_sum_kernel<<<(unsigned)(blocks < 4 * sms ? blocks : 4 * sms), 256, 0, st>>>(
+      reinterpret_cast<const float4*>(ws), reinterpret_cast<float4*>(y), n4, g.splits);
+  return check_launch("conv_tf32_split_sum_kernel");
+}
+
+template <int BN, int MT, int KS>
+constexpr int halo_bstages() {
+  return (int)((kStageBudget - 2 * (size_t)HaloT<MT, KS>::kABytes) / (size_t)(BN * BK * 4)) < 8
+             ? (int)((kStageBudget - 2 * (size_t)HaloT<MT, KS>::kABytes) / (size_t)(BN * BK * 4))
+             : 8;
+}
+
+template <int BN, int MT, int KS>
+static int launch_halo(const CUtensorMap& mx, const CUtensorMap& mw, float* y, float* ws, const Geom& g, int sms,
+                       int* err, cudaStream_t st) {
+  constexpr int BST = halo_bstages<BN, MT, KS>();
+  static_assert(BST >= 3, "weight ring too shallow");
+  static std::atomic<size_t> have[64];
+  const size_t smem = (size_t)BST * BN * BK * 4 + 2 * (size_t)HaloT<MT, KS>::kABytes + 1024;
+  auto kern = conv_tf32_halo_kernel<BN, MT, KS, 2, BST>;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return fail(SVBRDF_ERR_CUDA, "no usable device");
+  if (have[dev].load() < smem) {
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+      return fail(SVBRDF_ERR_CUDA, "cudaFuncSetAttribute: %s", cudaGetErrorString(cudaGetLastError()));
+    have[dev].store(smem);
+  }
+  const long long items = (long long)g.tiles_b * g.tiles_y * g.tiles_x * g.tiles_n * g.splits;
+  const int grid = (int)(items < sms ? items : sms);
+  kern<<<grid, kHaloThreads, smem, st>>>(mx, mw, y, ws, g, err);
+  int rc = check_launch("conv_tf32_halo_kernel");
+  if (rc || g.splits == 1) return rc;
+  const long long n4 = (long long)g.B * g.Ho * g.Wo * g.Cout / 4;
+  const long long blocks = (n4 + 255) / 256;
+  conv_tf32_split_sum_kernel<<<(unsigned)(blocks < 4 * sms ? blocks : 4 * sms), 256, 0, st>>>(
+      reinterpret_cast<const float4*>(ws), reinterpret_cast<float4*>(y), n4, g.splits);
+  return check_launch("conv_tf32_split_sum_kernel");
+}
+
+template <int KS>
+static int dispatch_halo(int bn, int mt, const CUtensorMap& mx, const CUtensorMap& mw, float* y, float* ws,
+                         const Geom& g, int sms, int* err, cudaStream_t st) {
+  switch (bn) {
+    case 256: return launch_halo<256, 1, KS>(mx, mw, y, ws, g, sms, err, st);
+    case 128: return mt == 2 ? launch_halo<128, 2, KS>(mx, mw, y, ws, g, sms, err, st)
+                             : launch_halo<128, 1, KS>(mx, mw, y, ws, g, sms, err, st);
+    case 64: return mt == 2 ? launch_halo<64, 2, KS>(mx, mw, y, ws, g, sms, err, st)
+                            : launch_halo<64, 1, KS>(mx, mw, y, ws, g, sms, err, st);
+    default: return mt == 2 ? launch_halo<32, 2, KS>(mx, mw, y, ws, g, sms, err, st)
+                            : launch_halo<32, 1, KS>(mx, mw, y, ws, g, sms, err, st);
+  }
+}
+
+}  // namespace tf32
+}  // namespace svb
+
+using namespace svb;
+
+extern "C" long long svbrdf_gen_conv_tf32_ws_bytes(int b, int hin, int win, int cin, int cout, int ksize, int pad) {
+  using namespace svb::tf32;
+  int sms = 0;
+  tf32::Plan pl;
+  if (sm_count(&sms) || plan_conv(b, hin, win, cin, cout, ksize, pad, sms, &pl)) return -1;
+  return 4 * split_ws_floats(pl.g);
+}
+
+extern "C" int svbrdf_gen_conv_tf32_ex(const float* x, const float* weight, float* y, void* ws, long long ws_bytes,
+                                       int b, int hin, int win, int cin, int cout, int ksize, int pad, int* err,
+                                       void* stream) {
+  using namespace svb::tf32;
+  if (!x || !weight || !y || !err) return fail(SVBRDF_ERR_INVALID, "conv_tf32: null x/weight/y/err");
+  int sms = 0;
+  int rc = sm_count(&sms);
   if (rc) return rc;
-  const int bn = cout >= 256 ? 256 : cout;
+  tf32::Plan pl;
+  rc = plan_conv(b, hin, win, cin, cout, ksize, pad, sms, &pl);
+  if (rc) return rc;
+  Geom& g = pl.g;
+  if (g.splits > 1 && (!ws || ws_bytes < 4 * split_ws_floats(g))) {  // no room: one K range per tile
+    const int total = g.taps * (cin / BK);
+    g.splits = 1;
+    g.kper = total;
+  }
+  if (((uintptr_t)x | (uintptr_t)weight | (uintptr_t)y | (uintptr_t)(g.splits > 1 ? ws : nullptr)) % 16)
+    return fail(SVBRDF_ERR_INVALID, "conv_tf32: 16-byte alignment");
+  PFN_cuTensorMapEncodeTiled_v12000 enc = nullptr;
+  rc = get_tensor_map_encoder(&enc);
+  if (rc) return rc;
+  const int bn = pl.bn;
   CUtensorMap mx, mw;
   {
     const cuuint64_t dims[4] = {(cuuint64_t)cin, (cuuint64_t)win, (cuuint64_t)hin, (cuuint64_t)b};
@@ -347,13 +730,32 @@ extern "C" int svbrdf_gen_conv_tf32(const float* x, const float* weight, float* 
     if (r != CUDA_SUCCESS) return fail(SVBRDF_ERR_CUDA, "cuTensorMapEncodeTiled(weight) failed: %d", (int)r);
   }
   cudaStream_t st = (cudaStream_t)stream;
-  // two M-tiles per CTA tile (one weight slice feeds 256 output pixels) where the map has 16+
-  // rows and Cout fits two double-buffered accumulators in TMEM
-  const bool two = g.NB == 1 && g.Ho >= 16 && bn <= 128;
-  switch (bn) {
-    case 256: return launch<256, 1>(mx, mw, y, g, err, st);
-    case 128: return two ? launch<128, 2>(mx, mw, y, g, err, st) : launch<128, 1>(mx, mw, y, g, err, st);
-    case 64: return two ? launch<64, 2>(mx, mw, y, g, err, st) : launch<64, 1>(mx, mw, y, g, err, st);
-    default: return two ? launch<32, 2>(mx, mw, y, g, err, st) : launch<32, 1>(mx, mw, y, g, err, st);
+  float* wsf = g.splits > 1 ? static_cast<float*>(ws) : nullptr;
+  if (pl.halo) {
+    // the (16 MT + k - 1) x (8 + k - 1) input patch, 4 channels (16 bytes) per pixel per group
+    CUtensorMap mh;
+    const int rows = 16 * pl.mt + ksize - 1, cols = 8 + ksize - 1;
+    const cuuint64_t dims[4] = {(cuuint64_t)cin, (cuuint64_t)win, (cuuint64_t)hin, (cuuint64_t)b};
+    const cuuint64_t strides[3] = {(cuuint64_t)cin * 4, (cuuint64_t)win * cin * 4, (cuuint64_t)hin * win * cin * 4};
+    const cuuint32_t box[4] = {4u, (cuuint32_t)cols, (cuuint32_t)rows, 1u};
+    const cuuint32_t es[4] = {1, 1, 1, 1};
+    const CUresult r = enc(&mh, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<float*>(x), dims, strides, box, es,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(SVBRDF_ERR_CUDA, "cuTensorMapEncodeTiled(halo x) failed: %d", (int)r);
+    return ksize == 3 ? dispatch_halo<3>(bn, pl.mt, mh, mw, y, wsf, g, sms, err, st)
+                      : dispatch_halo<1>(bn, pl.mt, mh, mw, y, wsf, g, sms, err, st);
   }
+  const bool two = pl.mt == 2;
+  switch (bn) {
+    case 256: return launch<256, 1>(mx, mw, y, wsf, g, sms, err, st);
+    case 128: return two ? launch<128, 2>(mx, mw, y, wsf, g, sms, err, st) : launch<128, 1>(mx, mw, y, wsf, g, sms, err, st);
+    case 64: return two ? launch<64, 2>(mx, mw, y, wsf, g, sms, err, st) : launch<64, 1>(mx, mw, y, wsf, g, sms, err, st);
+    default: return two ? launch<32, 2>(mx, mw, y, wsf, g, sms, err, st) : launch<32, 1>(mx, mw, y, wsf, g, sms, err, st);
+  }
+}
+
+extern "C" int svbrdf_gen_conv_tf32(const float* x, const float* weight, float* y, int b, int hin, int win, int cin,
+                                    int cout, int ksize, int pad, int* err, void* stream) {
+  return svbrdf_gen_conv_tf32_ex(x, weight, y, nullptr, 0, b, hin, win, cin, cout, ksize, pad, err, stream);
 }

@@ -52,7 +52,7 @@ __global__ void __launch_bounds__(kRenderThreads)
 render_fwd_kernel(const float* __restrict__ tex, const float* __restrict__ cam, const float* __restrict__ lit,
                   const float* __restrict__ lpow, int V, int H, int W, float size, float* __restrict__ out,
                   const float* __restrict__ targets, float4* partials, unsigned* counter, float* loss_out,
-                  double inv_n) {
+                  double inv_n, int B) {
   __shared__ View s_views[kMaxViews];
   __shared__ float s_pow[3];
   __shared__ float s_red[kRenderThreads / 32];
@@ -65,20 +65,25 @@ render_fwd_kernel(const float* __restrict__ tex, const float* __restrict__ cam, 
   const long long T = (long long)H * W;
   float loss = 0.f;
   Adj dummy;
-  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < T;
-       idx += (long long)gridDim.x * blockDim.x) {
+  // texel gi of the batch: material b = gi / T, texel idx = gi % T; material b's maps start at
+  // 9 T b, its renders (and targets) at 3 V T b
+  for (long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x; gi < T * B;
+       gi += (long long)gridDim.x * blockDim.x) {
+    const long long b = gi / T, idx = gi - b * T;
+    const float* texb = tex + 9 * T * b;
     float t[9];
 #pragma unroll
-    for (int c = 0; c < 9; ++c) t[c] = tex[c * T + idx];
+    for (int c = 0; c < 9; ++c) t[c] = texb[c * T + idx];
     Maps m;
     decode(t, m);
     float px, py;
     texel_pos((int)(idx / W), (int)(idx % W), W, H, size, px, py);
+    const long long vb = 3LL * V * T * b;
     for (int v = 0; v < V; ++v) {
       float io[3];
       if (LOSS >= 0) {
 #pragma unroll
-        for (int c = 0; c < 3; ++c) io[c] = targets[(3LL * v + c) * T + idx];
+        for (int c = 0; c < 3; ++c) io[c] = targets[vb + (3LL * v + c) * T + idx];
       }
       if (s_views[v].coloc != 0.f)
         texel_view<kModeFwd, LOSS, false, true>(m, px, py, s_views[v], s_pow, io, loss, dummy);
@@ -86,7 +91,7 @@ render_fwd_kernel(const float* __restrict__ tex, const float* __restrict__ cam, 
         texel_view<kModeFwd, LOSS, false, false>(m, px, py, s_views[v], s_pow, io, loss, dummy);
       if (out) {
 #pragma unroll
-        for (int c = 0; c < 3; ++c) out[(3LL * v + c) * T + idx] = io[c];
+        for (int c = 0; c < 3; ++c) out[vb + (3LL * v + c) * T + idx] = io[c];
       }
     }
   }
@@ -108,7 +113,7 @@ __global__ void __launch_bounds__(kRenderThreads)
 render_bwd_kernel(const float* __restrict__ tex, const float* __restrict__ cam, const float* __restrict__ lit,
                   const float* __restrict__ lpow, int V, int H, int W, float size,
                   const float* __restrict__ gout, float* __restrict__ gtex, float* __restrict__ gpow,
-                  float4* partials, unsigned* counter) {
+                  float4* partials, unsigned* counter, int B) {
   __shared__ View s_views[kMaxViews];
   __shared__ float s_pow[3];
   __shared__ float s_red[kRenderThreads / 32];
@@ -120,21 +125,24 @@ render_bwd_kernel(const float* __restrict__ tex, const float* __restrict__ cam, 
 
   const long long T = (long long)H * W;
   float gp0 = 0.f, gp1 = 0.f, gp2 = 0.f, unused = 0.f;
-  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < T;
-       idx += (long long)gridDim.x * blockDim.x) {
+  for (long long gi = (long long)blockIdx.x * blockDim.x + threadIdx.x; gi < T * B;
+       gi += (long long)gridDim.x * blockDim.x) {
+    const long long b = gi / T, idx = gi - b * T;
+    const float* texb = tex + 9 * T * b;
     float t[9];
 #pragma unroll
-    for (int c = 0; c < 9; ++c) t[c] = tex[c * T + idx];
+    for (int c = 0; c < 9; ++c) t[c] = texb[c * T + idx];
     Maps m;
     decode(t, m);
     float px, py;
     texel_pos((int)(idx / W), (int)(idx % W), W, H, size, px, py);
     Adj a;
     adj_zero(a);
+    const long long vb = 3LL * V * T * b;
     for (int v = 0; v < V; ++v) {
       float io[3];
 #pragma unroll
-      for (int c = 0; c < 3; ++c) io[c] = gout[(3LL * v + c) * T + idx];
+      for (int c = 0; c < 3; ++c) io[c] = gout[vb + (3LL * v + c) * T + idx];
       if (s_views[v].coloc != 0.f)
         texel_view<kModeBwd, kLossMSE, GRAD_POW, true>(m, px, py, s_views[v], s_pow, io, unused, a);
       else
@@ -143,7 +151,7 @@ render_bwd_kernel(const float* __restrict__ tex, const float* __restrict__ cam, 
     float g[9];
     adj_to_params(t, m, a, 1.0f, g);
 #pragma unroll
-    for (int c = 0; c < 9; ++c) gtex[c * T + idx] = g[c];
+    for (int c = 0; c < 9; ++c) gtex[9 * T * b + c * T + idx] = g[c];
     if (GRAD_POW) { gp0 += a.gp[0]; gp1 += a.gp[1]; gp2 += a.gp[2]; }
   }
   if (GRAD_POW) {
@@ -205,12 +213,14 @@ int svbrdf_abi_version(void) { return SVBRDF_ABI_VERSION; }
 int svbrdf_max_views(void) { return kMaxViews; }
 size_t svbrdf_workspace_bytes(void) { return kWorkspaceBytes; }
 
-int svbrdf_render_fwd(const float* textures, const float* camera_pos, const float* light_pos,
-                      const float* light_pow, int n_views, int height, int width, float size, float* out,
-                      const float* targets, int loss_kind, float* loss_out, void* workspace,
-                      size_t workspace_bytes, void* stream) {
+int svbrdf_render_fwd_batch(const float* textures, const float* camera_pos, const float* light_pos,
+                            const float* light_pow, int n_views, int height, int width, float size, int batch,
+                            float* out, const float* targets, int loss_kind, float* loss_out, void* workspace,
+                            size_t workspace_bytes, void* stream) {
   int rc = check_common(textures, camera_pos, light_pos, light_pow, n_views, height, width, size);
   if (rc) return rc;
+  if (batch < 1 || (long long)batch * height * width >= (1LL << 40))
+    return fail(SVBRDF_ERR_INVALID, "bad batch %d", batch);
   if (loss_kind < SVBRDF_LOSS_NONE || loss_kind > SVBRDF_LOSS_LOG1P_PRE)
     return fail(SVBRDF_ERR_INVALID, "bad loss_kind %d", loss_kind);
   if (loss_kind == SVBRDF_LOSS_NONE && !out) return fail(SVBRDF_ERR_INVALID, "out is NULL and no loss requested");
@@ -220,7 +230,7 @@ int svbrdf_render_fwd(const float* textures, const float* camera_pos, const floa
       return fail(SVBRDF_ERR_WORKSPACE, "workspace of %zu bytes needed", kWorkspaceBytes);
   }
   const long long T = (long long)height * width;
-  const double inv_n = 1.0 / (3.0 * n_views * (double)T);
+  const double inv_n = 1.0 / (3.0 * n_views * (double)T * batch);
   unsigned* counter = (unsigned*)workspace;
   float4* partials = workspace ? (float4*)((char*)workspace + 16) : nullptr;
   cudaStream_t st = (cudaStream_t)stream;
@@ -228,10 +238,10 @@ int svbrdf_render_fwd(const float* textures, const float* camera_pos, const floa
 #define SVB_FWD(L)                                                                                          \
   {                                                                                                         \
     static int occ = occupancy(render_fwd_kernel<L>, kRenderThreads);                                       \
-    const int grid = grid_for(T, kRenderThreads, occ);                                                      \
+    const int grid = grid_for(T * batch, kRenderThreads, occ);                                              \
     render_fwd_kernel<L><<<grid, kRenderThreads, 0, st>>>(textures, camera_pos, light_pos, light_pow,      \
                                                           n_views, height, width, size, out, targets,       \
-                                                          partials, counter, loss_out, inv_n);              \
+                                                          partials, counter, loss_out, inv_n, batch);       \
     break;                                                                                                  \
   }
     case SVBRDF_LOSS_NONE: SVB_FWD(-1)
@@ -243,12 +253,22 @@ int svbrdf_render_fwd(const float* textures, const float* camera_pos, const floa
   return check_launch("render_fwd_kernel");
 }
 
-int svbrdf_render_bwd(const float* textures, const float* camera_pos, const float* light_pos,
-                      const float* light_pow, int n_views, int height, int width, float size,
-                      const float* grad_out, float* grad_textures, float* grad_light_pow, void* workspace,
+int svbrdf_render_fwd(const float* textures, const float* camera_pos, const float* light_pos,
+                      const float* light_pow, int n_views, int height, int width, float size, float* out,
+                      const float* targets, int loss_kind, float* loss_out, void* workspace,
                       size_t workspace_bytes, void* stream) {
+  return svbrdf_render_fwd_batch(textures, camera_pos, light_pos, light_pow, n_views, height, width, size, 1, out,
+                                 targets, loss_kind, loss_out, workspace, workspace_bytes, stream);
+}
+
+int svbrdf_render_bwd_batch(const float* textures, const float* camera_pos, const float* light_pos,
+                            const float* light_pow, int n_views, int height, int width, float size, int batch,
+                            const float* grad_out, float* grad_textures, float* grad_light_pow, void* workspace,
+                            size_t workspace_bytes, void* stream) {
   int rc = check_common(textures, camera_pos, light_pos, light_pow, n_views, height, width, size);
   if (rc) return rc;
+  if (batch < 1 || (long long)batch * height * width >= (1LL << 40))
+    return fail(SVBRDF_ERR_INVALID, "bad batch %d", batch);
   if (!grad_out || !grad_textures) return fail(SVBRDF_ERR_INVALID, "null grad_out/grad_textures");
   if (grad_light_pow && (!workspace || workspace_bytes < kWorkspaceBytes))
     return fail(SVBRDF_ERR_WORKSPACE, "workspace of %zu bytes needed", kWorkspaceBytes);
@@ -258,18 +278,26 @@ int svbrdf_render_bwd(const float* textures, const float* camera_pos, const floa
   cudaStream_t st = (cudaStream_t)stream;
   if (grad_light_pow) {
     static int occ = occupancy(render_bwd_kernel<true>, kRenderThreads);
-    const int grid = grid_for(T, kRenderThreads, occ);
+    const int grid = grid_for(T * batch, kRenderThreads, occ);
     render_bwd_kernel<true><<<grid, kRenderThreads, 0, st>>>(textures, camera_pos, light_pos, light_pow, n_views,
                                                              height, width, size, grad_out, grad_textures,
-                                                             grad_light_pow, partials, counter);
+                                                             grad_light_pow, partials, counter, batch);
   } else {
     static int occ = occupancy(render_bwd_kernel<false>, kRenderThreads);
-    const int grid = grid_for(T, kRenderThreads, occ);
+    const int grid = grid_for(T * batch, kRenderThreads, occ);
     render_bwd_kernel<false><<<grid, kRenderThreads, 0, st>>>(textures, camera_pos, light_pos, light_pow, n_views,
                                                               height, width, size, grad_out, grad_textures,
-                                                              nullptr, partials, counter);
+                                                              nullptr, partials, counter, batch);
   }
   return check_launch("render_bwd_kernel");
+}
+
+int svbrdf_render_bwd(const float* textures, const float* camera_pos, const float* light_pos,
+                      const float* light_pow, int n_views, int height, int width, float size,
+                      const float* grad_out, float* grad_textures, float* grad_light_pow, void* workspace,
+                      size_t workspace_bytes, void* stream) {
+  return svbrdf_render_bwd_batch(textures, camera_pos, light_pos, light_pow, n_views, height, width, size, 1, grad_out,
+                                 grad_textures, grad_light_pow, workspace, workspace_bytes, stream);
 }
 
 }  // extern "C"

@@ -113,6 +113,17 @@ __device__ __forceinline__ uint64_t sw128_desc_mn(uint32_t addr, uint32_t lbo, u
   return d;
 }
 
+// Shared-memory matrix descriptor without swizzle, K-major: core matrices of 8 rows x 16 bytes,
+// each stored as 128 contiguous bytes (row i at +16 i); `lbo` = bytes between core matrices
+// adjacent in K, `sbo` = bytes between 8-row groups adjacent in M (or N). Layout type 0.
+__device__ __forceinline__ uint64_t noswz_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = (uint64_t)((addr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+
 // cuTensorMapEncodeTiled, looked up once through the runtime.
 int get_tensor_map_encoder(PFN_cuTensorMapEncodeTiled_v12000* out);
 

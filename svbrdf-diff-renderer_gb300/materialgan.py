@@ -224,9 +224,20 @@ def generator_device_error(device="cuda") -> int:
     return int(_tf32_err(torch.device(device)).item())
 
 
+def _conv_tf32(x, w, y, b, h, wd, cin, cout, k, pad):
+    """One svbrdf_gen_conv_tf32_ex call; maps with few tiles split K over a workspace."""
+    from . import _native as N
+
+    L = N.lib()
+    nb = int(L.svbrdf_gen_conv_tf32_ws_bytes(b, h, wd, cin, cout, k, pad))
+    ws = torch.empty(nb, device=x.device, dtype=torch.uint8) if nb > 0 else None
+    N.check(L.svbrdf_gen_conv_tf32_ex(x.data_ptr(), w.data_ptr(), y.data_ptr(), N.ptr(ws), max(nb, 0), b, h, wd, cin,
+                                      cout, k, pad, _tf32_err(x.device).data_ptr(), N.stream_handle(x.device)))
+
+
 class _ConvTF32(torch.autograd.Function):
     """A k x k convolution (k = 3 or 1) of a channels-last FP32 map on the tensor cores in TF32
-    (svbrdf_gen_conv_tf32): ``pad`` 1 for a same-padded 3x3 convolution, 0 for a valid one (the
+    (svbrdf_gen_conv_tf32_ex): ``pad`` 1 for a same-padded 3x3 convolution, 0 for a valid one (the
     up-sampling layers) or a 1x1. The weights come prepared: ``w_fwd`` [Cout_p][k*k][Cin] and
     ``w_dg`` [Cin][k*k][Cout_p] (transposed, taps flipped), Cout_p = Cout padded to the
     kernel's minimum of 32 with zero rows. The data gradient is the same kernel on w_dg with pad
@@ -241,8 +252,7 @@ class _ConvTF32(torch.autograd.Function):
         coutp = w_fwd.shape[0]
         ho, wo = h + 2 * pad - (k - 1), wd + 2 * pad - (k - 1)
         y = torch.empty(b, coutp, ho, wo, device=x.device, dtype=torch.float32, memory_format=CL)
-        N.check(N.lib().svbrdf_gen_conv_tf32(x.data_ptr(), w_fwd.data_ptr(), y.data_ptr(), b, h, wd, c, coutp, k, pad,
-                                             _tf32_err(x.device).data_ptr(), N.stream_handle(x.device)))
+        _conv_tf32(x, w_fwd, y, b, h, wd, c, coutp, k, pad)
         ctx.save_for_backward(w_dg)
         ctx.geom = (b, c, h, wd, coutp, cout, k, pad, ho, wo)
         return y if coutp == cout else y[:, :cout]
@@ -260,8 +270,7 @@ class _ConvTF32(torch.autograd.Function):
             gy = gp
         gy = _cl(gy)
         gx = torch.empty(b, c, h, wd, device=gy.device, dtype=torch.float32, memory_format=CL)
-        N.check(N.lib().svbrdf_gen_conv_tf32(gy.data_ptr(), w_dg.data_ptr(), gx.data_ptr(), b, ho, wo, coutp, c, k,
-                                             k - 1 - pad, _tf32_err(gy.device).data_ptr(), N.stream_handle(gy.device)))
+        _conv_tf32(gy, w_dg, gx, b, ho, wo, coutp, c, k, k - 1 - pad)
         return gx, None, None, None, None, None
 
 

@@ -30,11 +30,10 @@ class _RenderFn(torch.autograd.Function):
         B, _, H, W = tex.shape
         out = torch.empty(B * r.n_of_imgs, 3, H, W, device=tex.device, dtype=torch.float32)
         s = N.stream_handle(tex.device)
-        per = r.n_of_imgs * 3 * H * W
-        for b in range(B):
-            N.check(L.svbrdf_render_fwd(tex[b].data_ptr(), r._cam.data_ptr(), r._lit.data_ptr(), lp.data_ptr(),
-                                        r.n_of_imgs, H, W, float(r.size), out.data_ptr() + 4 * per * b, None,
-                                        -1, None, None, 0, s))
+        # the whole batch in one launch
+        N.check(L.svbrdf_render_fwd_batch(tex.data_ptr(), r._cam.data_ptr(), r._lit.data_ptr(), lp.data_ptr(),
+                                          r.n_of_imgs, H, W, float(r.size), B, out.data_ptr(), None, -1, None, None,
+                                          0, s))
         ctx.save_for_backward(tex, lp)
         ctx.r = r
         return out
@@ -50,15 +49,10 @@ class _RenderFn(torch.autograd.Function):
         want_pow = ctx.needs_input_grad[1]
         gpow = torch.zeros(3, device=tex.device, dtype=torch.float32) if want_pow else None
         s = N.stream_handle(tex.device)
-        per = r.n_of_imgs * 3 * H * W
-        for b in range(B):
-            gp_b = torch.empty(3, device=tex.device, dtype=torch.float32) if want_pow else None
-            N.check(L.svbrdf_render_bwd(tex[b].data_ptr(), r._cam.data_ptr(), r._lit.data_ptr(), lp.data_ptr(),
-                                        r.n_of_imgs, H, W, float(r.size), gout.data_ptr() + 4 * per * b,
-                                        gtex[b].data_ptr(), N.ptr(gp_b), r._workspace.data_ptr(),
-                                        r._workspace.numel(), s))
-            if want_pow:
-                gpow += gp_b
+        # the whole batch in one launch; the light-power gradient sums over all of it
+        N.check(L.svbrdf_render_bwd_batch(tex.data_ptr(), r._cam.data_ptr(), r._lit.data_ptr(), lp.data_ptr(),
+                                          r.n_of_imgs, H, W, float(r.size), B, gout.data_ptr(), gtex.data_ptr(),
+                                          N.ptr(gpow), r._workspace.data_ptr(), r._workspace.numel(), s))
         return gtex, gpow, None
 
 

@@ -403,6 +403,44 @@ def _tf32_generator_errors(svb, cuda, gen, d, wp_np, noises_np, R_np):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("b,h,cin,cout,k,pad", [(16, 4, 512, 512, 3, 1), (16, 8, 512, 512, 3, 1),
+                                                 (16, 16, 512, 512, 3, 1), (16, 6, 512, 512, 3, 2),
+                                                 (16, 8, 512, 32, 1, 0)])
+def test_conv_tf32_split_k_matches_unsplit(svb, cuda, b, h, cin, cout, k, pad):
+    """The generator's small maps (4^2 to 16^2, 512 channels) split K over a workspace
+    (svbrdf_gen_conv_tf32_ex): the summed partials equal the unsplit kernel's result up to FP32
+    summation order, and torch's FP32 convolution within TF32 accuracy."""
+    N = svb._native
+    L = N.lib()
+    g = torch.Generator().manual_seed(b * h + cout)
+    x = torch.randn(b, h, h, cin, generator=g).to(cuda)
+    w = (torch.randn(cout, k * k, cin, generator=g) / (cin * k * k) ** 0.5).to(cuda)
+    ho = h + 2 * pad - (k - 1)
+    nb = int(L.svbrdf_gen_conv_tf32_ws_bytes(b, h, h, cin, cout, k, pad))
+    assert nb > 0  # these maps have fewer tiles than half the SMs
+    ws = torch.empty(nb, device=cuda, dtype=torch.uint8)
+    err = torch.zeros(1, dtype=torch.int32, device=cuda)
+    st = N.stream_handle(cuda)
+    y_split = torch.empty(b, ho, ho, cout, device=cuda)
+    y_one = torch.empty_like(y_split)
+    for _ in range(2):  # the workspace is reused
+        N.check(L.svbrdf_gen_conv_tf32_ex(x.data_ptr(), w.data_ptr(), y_split.data_ptr(), ws.data_ptr(), nb, b, h, h,
+                                          cin, cout, k, pad, err.data_ptr(), st))
+    N.check(L.svbrdf_gen_conv_tf32(x.data_ptr(), w.data_ptr(), y_one.data_ptr(), b, h, h, cin, cout, k, pad,
+                                   err.data_ptr(), st))
+    torch.backends.cudnn.allow_tf32 = False
+    try:
+        ref = torch.nn.functional.conv2d(x.permute(0, 3, 1, 2), w.reshape(cout, k, k, cin).permute(0, 3, 1, 2),
+                                         padding=pad).permute(0, 2, 3, 1)
+    finally:
+        torch.backends.cudnn.allow_tf32 = True
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    assert rel_l2(y_split, y_one) <= 1e-5
+    assert rel_l2(y_split, ref) <= 2e-3
+
+
+@pytest.mark.gpu
 def test_gpu_generator_tf32_matches_reference_network(svb, cuda):
     """The generator as it runs by default on the GPU (channels-last maps, the TF32 tensor-core
     convolutions, the NHWC kernels) on the reference network's fixture

@@ -116,3 +116,35 @@ def test_many_views_and_non_square_budget(svb, cuda):
     from oracle import microfacet_ref as R
     ref = R.render(tex, cam, cam, torch.full((3,), 1500.0), 17.0, torch.float64)
     assert rel_l2(out, ref) <= 1e-5
+
+
+def test_batched_eval_matches_per_material(svb, golden, cuda):
+    """A leading batch of materials (the reference's eval on [B, 9, H, W] -> [B * n, 3, H, W])
+    renders and differentiates in one launch each (svbrdf_render_fwd_batch / _bwd_batch): the
+    same renders and texture gradients as one call per material, and a light-power gradient
+    equal to their sum (one fixed-order reduction over the batch, so equal up to summation
+    order)."""
+    d = golden("render_general_24.npz")
+    res = d["textures"].shape[-1]
+    r = _renderer(svb, d, res, cuda)
+    g = torch.Generator().manual_seed(5)
+    tex = (d["textures"].float() + 0.3 * torch.randn(3, 9, res, res, generator=g)).clamp(-1, 1).to(cuda)
+    n = r.n_of_imgs
+    wts = torch.randn(3 * n, 3, res, res, generator=g).to(cuda)
+    lp = r.light_pow.detach().clone().requires_grad_(True)
+    r.update_light(lp)
+    tb = tex.clone().requires_grad_(True)
+    out = r.eval(tb)
+    assert out.shape == (3 * n, 3, res, res)
+    (out * wts).sum().backward()
+    g_batch = lp.grad.clone()
+    g_sum = torch.zeros_like(g_batch)
+    for b in range(3):
+        lp.grad = None
+        t1 = tex[b:b + 1].clone().requires_grad_(True)
+        o1 = r.eval(t1)
+        (o1 * wts[b * n:(b + 1) * n]).sum().backward()
+        assert torch.equal(out[b * n:(b + 1) * n].detach(), o1.detach())
+        assert torch.equal(tb.grad[b:b + 1], t1.grad)
+        g_sum += lp.grad
+    assert rel_l2(g_batch, g_sum) <= 1e-6

@@ -249,6 +249,16 @@ int svbrdf_conv3x3_bf16_ex(const void* x, const void* weight, const float* bias,
 /* Number of per-block partial sums svbrdf_desc_feat_loss writes. */
 int svbrdf_desc_partials(void);
 
+/* The loss scalars from their partial sums in one launch: out[j] = sum over the segments k with
+ * groups[k] == j (j = 0, 1) of weights[k] x (sum of the lengths[k] floats at buf + offsets[k]),
+ * added in a fixed order (FP32 within a thread's share of a segment, double across them; 1 to 16
+ * segments; host arrays). For the
+ * descriptor: group 0 the feature terms' partials (weights w_k^2 / n_features), group 1 the
+ * Gram terms' loss rows (weights w_k^2 / n_gram), as VGGLoss.forward weights them
+ * (src/descriptor.py:77-79). */
+int svbrdf_desc_loss_sums(const float* buf, int n_segs, const long long* offsets, const long long* lengths,
+                          const double* weights, const int* groups, float* out, void* stream);
+
 /* 2x2 box downsample (if `downsample`) of renders [v][3][2h][2w] FP32, ImageNet normalisation
  * with the reference's statistics (src/descriptor.py:65-75), conv1_1 (weight [64][3][3][3],
  * bias [64], FP32, zero padding 1) and ReLU. Writes NHWC [v][h][w][64] in FP32 (out_f32) and

@@ -146,6 +146,8 @@ def _declare(L):
     L.svbrdf_desc_avgpool_bwd.argtypes = [P, P, P, P, I, I, I, I, P]
     L.svbrdf_desc_feat_loss.restype = I
     L.svbrdf_desc_feat_loss.argtypes = [P, I, P, P, F, I, P, P, ctypes.c_longlong, P]
+    L.svbrdf_desc_loss_sums.restype = I
+    L.svbrdf_desc_loss_sums.argtypes = [P, I, P, P, P, P, P, P]
     L.svbrdf_desc_gram_splits.restype = I
     L.svbrdf_desc_gram_splits.argtypes = [I, I, I]
     L.svbrdf_desc_gram.restype = I
@@ -218,7 +220,7 @@ EXPORTS = [
     "svbrdf_batched_plan", "svbrdf_batched_workspace_bytes", "svbrdf_batched_step", "svbrdf_batched_steps", "svbrdf_conv3x3_bf16",
     "svbrdf_conv3x3_bf16_ex", "svbrdf_desc_partials", "svbrdf_desc_conv1_fwd", "svbrdf_desc_conv1_bwd",
     "svbrdf_desc_pool_fwd", "svbrdf_desc_pool_bwd", "svbrdf_desc_avgpool_fwd", "svbrdf_desc_avgpool_bwd",
-    "svbrdf_desc_feat_loss", "svbrdf_desc_gram_splits", "svbrdf_desc_gram", "svbrdf_desc_gram_finish",
+    "svbrdf_desc_feat_loss", "svbrdf_desc_loss_sums", "svbrdf_desc_gram_splits", "svbrdf_desc_gram", "svbrdf_desc_gram_finish",
     "svbrdf_desc_gemm_nt", "svbrdf_desc_gemm_nt_feat_partials", "svbrdf_desc_gemm_nt_feat",
     "svbrdf_gen_upsample2",
     "svbrdf_gen_upsample2_bwd", "svbrdf_gen_upsample2_scaled", "svbrdf_gen_scale", "svbrdf_gen_scale_bwd", "svbrdf_gen_act", "svbrdf_gen_act_bwd",

@@ -279,7 +279,7 @@ struct HaloT {
 constexpr int kHaloThreads = 320;  // warp 0 TMA, warp 1 MMA + TMEM owner, warps 2..9 epilogue (two per
                                    // TMEM lane quadrant, each draining half the columns)
 
-template <int BN, int MT, int KS, int AST, int BST>
+template <int BN, int MT, int KS, int AST, int BST, int NBUF>
 __global__ void __launch_bounds__(kHaloThreads, 1)
 conv_tf32_halo_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_constant__ CUtensorMap tmap_w,
                       float* __restrict__ y, float* __restrict__ ws, Geom g, int* err) {
@@ -287,7 +287,7 @@ conv_tf32_halo_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_c
   constexpr int B_BYTES = BN * BK * 4;
   constexpr int TAPS = KS * KS;
   constexpr uint32_t ACC_COLS = MT * BN;
-  constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;
+  constexpr uint32_t TMEM_COLS = NBUF * ACC_COLS;  // NBUF = 2: double-buffered accumulators
   static_assert(TMEM_COLS >= 32 && TMEM_COLS <= 512 && (TMEM_COLS & (TMEM_COLS - 1)) == 0, "TMEM columns");
   static_assert(B_BYTES % 1024 == 0, "weight slices keep the 1024-byte swizzle alignment");
   extern __shared__ uint8_t dsmem[];
@@ -389,8 +389,9 @@ conv_tf32_halo_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_c
       int qa = 0, qb = 0, j = 0;
       bool bad = false;
       for (int w = blockIdx.x; w < n_items && !bad; w += gridDim.x, ++j) {
-        const int a = j & 1;
-        if (j >= 2 && !mbar_wait(smem_u32(&tempty_bar[a]), ((uint32_t)(j >> 1) & 1u) ^ 1u, err, kErrMma)) break;
+        const int a = j % NBUF;
+        // the epilogue must have drained this buffer's previous tile (j - NBUF)
+        if (j >= NBUF && !mbar_wait(smem_u32(&tempty_bar[a]), ((uint32_t)(j / NBUF) & 1u) ^ 1u, err, kErrMma)) break;
         fence_after();
         const uint32_t acc = tmem + (uint32_t)a * ACC_COLS;
         const int c_lo = (w % g.splits) * g.kper, c_hi = min(kchunks, c_lo + g.kper);
@@ -437,8 +438,8 @@ conv_tf32_halo_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_c
     const int m = qw * 32 + lane;  // accumulator row: patch row m / 8, column m % 8
     int j = 0;
     for (int w = blockIdx.x; w < n_items; w += gridDim.x, ++j) {
-      const int a = j & 1;
-      const bool ok = __all_sync(0xffffffffu, mbar_wait(smem_u32(&tfull_bar[a]), (uint32_t)(j >> 1) & 1u, err,
+      const int a = j % NBUF;
+      const bool ok = __all_sync(0xffffffffu, mbar_wait(smem_u32(&tfull_bar[a]), (uint32_t)(j / NBUF) & 1u, err,
                                                         kErrEpi)) &&
                       *(volatile int*)err == 0;
       fence_after();
@@ -552,9 +553,12 @@ static int plan_conv(int b, int hin, int win, int cin, int cout, int ksize, int 
   pl->halo = (g.Wo >= 8 && g.Ho >= 16) ? 1 : 0;
   if (pl->halo) {
     // 16-row x 8-column patches, two stacked where the map has 32+ rows and Cout fits two
-    // double-buffered accumulators in TMEM; K splits count 32-channel chunks (all taps each)
+    // double-buffered accumulators in TMEM (BN <= 128; a 256 x 256 tile would fill TMEM with
+    // one accumulator, and the exposed epilogue then costs more than the halved weight
+    // traffic saves: measured 5-35 % slower on the generator's 32^2-128^2 layers). K splits
+    // count 32-channel chunks (all taps each).
     g.TW = 8; g.TH = 16; g.NB = 1;
-    pl->mt = (pl->bn <= 128 && g.Ho >= 32) ? 2 : 1;
+    pl->mt = (g.Ho >= 32 && pl->bn <= 128) ? 2 : 1;
     g.tiles_x = (g.Wo + 7) / 8;
     g.tiles_y = (g.Ho + 16 * pl->mt - 1) / (16 * pl->mt);
     g.tiles_b = g.B;
@@ -636,9 +640,11 @@ static int launch_halo(const CUtensorMap& mx, const CUtensorMap& mw, float* y, f
                        int* err, cudaStream_t st) {
   constexpr int BST = halo_bstages<BN, MT, KS>();
   static_assert(BST >= 3, "weight ring too shallow");
+  // 512 TMEM columns hold two MT x BN accumulators up to MT x BN = 256, else one
+  constexpr int NBUF = MT * BN <= 256 ? 2 : 1;
   static std::atomic<size_t> have[64];
   const size_t smem = (size_t)BST * BN * BK * 4 + 2 * (size_t)HaloT<MT, KS>::kABytes + 1024;
-  auto kern = conv_tf32_halo_kernel<BN, MT, KS, 2, BST>;
+  auto kern = conv_tf32_halo_kernel<BN, MT, KS, 2, BST, NBUF>;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return fail(SVBRDF_ERR_CUDA, "no usable device");
   if (have[dev].load() < smem) {

@@ -13,6 +13,7 @@
 //                          hook gradient + ReLU mask
 //   desc_feat_loss_kernel  sum of (f - t)^2 as per-block partials (a fixed-order sum), and
 //                          optionally g = coef (f - t) + gram_grad, masked by f > 0
+//   desc_loss_sums_kernel  weighted sums of loss partials (fixed order)
 //   desc_conv1_bwd_kernel  conv1_1 data gradient, back through the normalisation and the
 //                          downsample to d/d render
 //
@@ -107,20 +108,23 @@ __global__ void __launch_bounds__(256) desc_conv1_fwd_kernel(const float* __rest
   }
 }
 
-// ---------------------------------------------------------------- conv1_1 data gradient
-// d in(y, x, ci) = sum_{co, ky, kx} w[co][ci][ky][kx] gz(y + 1 - ky, x + 1 - kx, co); then
-// d render = d in / std, spread over the 2x2 block with weight 1/4 when downsampling.
+// ---------------------------------------------------------------- conv1_1 backward
+// d render = conv1_1's data gradient (3 x 3, 64 -> 3 channels), through the normalisation
+// and the 2x2 box downsample. A block takes a 16 x 16 tile of the 256-pixel side; each of its
+// 128 threads computes 2 adjacent pixels of one row, so every weight pair and every input
+// column read from shared memory serves up to 2 pixels (per channel pair and kernel row: 4
+// input values and 9 weight pairs for 36 FMAs).
 template <bool DOWN>
-__global__ void __launch_bounds__(256) desc_conv1_bwd_kernel(const __nv_bfloat16* __restrict__ gz,
-                                                             const float* __restrict__ w, float* __restrict__ gr,
-                                                             int H, int W) {
+__global__ void __launch_bounds__(128) desc_conv1_bwd_kernel(const __nv_bfloat16* __restrict__ gz,
+                                                            const float* __restrict__ w, float* __restrict__ gr,
+                                                            int H, int W) {
   __shared__ __nv_bfloat162 s_g[32][kTile + 2][kTile + 2];  // gz tile, channel pairs outermost
   __shared__ __align__(8) float s_w[27][64];                 // [ci*9 + ky*3 + kx][co]
-  const int tid = threadIdx.y * kTile + threadIdx.x;
+  const int tid = threadIdx.x;
   const int v = blockIdx.z, y0 = blockIdx.y * kTile, x0 = blockIdx.x * kTile;
-  for (int i = tid; i < 64 * 27; i += 256) s_w[i % 27][i / 27] = w[i];
+  for (int i = tid; i < 64 * 27; i += 128) s_w[i % 27][i / 27] = w[i];
   // rows y0-1 .. y0+16 and columns x0-1 .. x0+16 of gz, 8 channels per step
-  for (int i = tid; i < (kTile + 2) * (kTile + 2) * 8; i += 256) {
+  for (int i = tid; i < (kTile + 2) * (kTile + 2) * 8; i += 128) {
     const int p = i / 8, c8 = i % 8;
     const int ty = p / (kTile + 2), tx = p % (kTile + 2);
     const int gy = y0 + ty - 1, gx = x0 + tx - 1;
@@ -132,37 +136,57 @@ __global__ void __launch_bounds__(256) desc_conv1_bwd_kernel(const __nv_bfloat16
     for (int j = 0; j < 4; ++j) s_g[c8 * 4 + j][ty][tx] = e[j];
   }
   __syncthreads();
-  const int ty = threadIdx.y, tx = threadIdx.x;
-  const int y = y0 + ty, x = x0 + tx;
-  if (y >= H || x >= W) return;
-  float d[3] = {0.f, 0.f, 0.f};
+  const int ty = tid / 8, tx0 = 2 * (tid % 8);  // pixels (ty, tx0 .. tx0 + 1) of the tile
+  float d[2][3];
 #pragma unroll
-  for (int ky = 0; ky < 3; ++ky)
+  for (int q = 0; q < 2; ++q) d[q][0] = d[q][1] = d[q][2] = 0.f;
+#pragma unroll 2
+  for (int c2 = 0; c2 < 32; ++c2) {
 #pragma unroll
-    for (int kx = 0; kx < 3; ++kx) {
-      // gz at output (y + 1 - ky, x + 1 - kx) = tile (ty + 2 - ky, tx + 2 - kx)
-      const int sy = ty + 2 - ky, sx = tx + 2 - kx;
-#pragma unroll 4
-      for (int c2 = 0; c2 < 32; ++c2) {
-        const float2 g = __bfloat1622float2(s_g[c2][sy][sx]);
+    for (int ky = 0; ky < 3; ++ky) {
+      // gz at output (y + 1 - ky, x + 1 - kx) = tile (ty + 2 - ky, tx + 2 - kx): columns tx0 .. tx0 + 3
+      float2 g[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) g[j] = __bfloat1622float2(s_g[c2][ty + 2 - ky][tx0 + j]);
+#pragma unroll
+      for (int kx = 0; kx < 3; ++kx) {
 #pragma unroll
         for (int ci = 0; ci < 3; ++ci) {
           const float2 wv = reinterpret_cast<const float2*>(s_w[ci * 9 + ky * 3 + kx])[c2];
-          d[ci] = fmaf(wv.y, g.y, fmaf(wv.x, g.x, d[ci]));
+#pragma unroll
+          for (int q = 0; q < 2; ++q) d[q][ci] = fmaf(wv.y, g[q + 2 - kx].y, fmaf(wv.x, g[q + 2 - kx].x, d[q][ci]));
         }
       }
     }
+  }
+  const int y = y0 + ty, x = x0 + tx0;
+  if (y >= H) return;
   const int RH = DOWN ? 2 * H : H, RW = DOWN ? 2 * W : W;
 #pragma unroll
   for (int ci = 0; ci < 3; ++ci) {
     float* rp = gr + ((size_t)v * 3 + ci) * RH * RW;
-    const float g = d[ci] / c_std[ci];
+    const float is = 1.0f / c_std[ci];
+    float gq[2];
+#pragma unroll
+    for (int q = 0; q < 2; ++q) gq[q] = d[q][ci] * is;
     if (DOWN) {
-      const float q = 0.25f * g;
-      *reinterpret_cast<float2*>(rp + (size_t)(2 * y) * RW + 2 * x) = make_float2(q, q);
-      *reinterpret_cast<float2*>(rp + (size_t)(2 * y + 1) * RW + 2 * x) = make_float2(q, q);
+      if (x + 1 < W && RW % 4 == 0 && ((uintptr_t)rp & 15u) == 0) {  // 16-byte aligned rows
+        const float4 a = make_float4(0.25f * gq[0], 0.25f * gq[0], 0.25f * gq[1], 0.25f * gq[1]);
+        *reinterpret_cast<float4*>(rp + (size_t)(2 * y) * RW + 2 * x) = a;
+        *reinterpret_cast<float4*>(rp + (size_t)(2 * y + 1) * RW + 2 * x) = a;
+      } else {
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          if (x + q >= W) break;
+          const float qv = 0.25f * gq[q];
+          *reinterpret_cast<float2*>(rp + (size_t)(2 * y) * RW + 2 * (x + q)) = make_float2(qv, qv);
+          *reinterpret_cast<float2*>(rp + (size_t)(2 * y + 1) * RW + 2 * (x + q)) = make_float2(qv, qv);
+        }
+      }
     } else {
-      rp[(size_t)y * RW + x] = g;
+#pragma unroll
+      for (int q = 0; q < 2; ++q)
+        if (x + q < W) rp[(size_t)y * RW + x + q] = gq[q];
     }
   }
 }
@@ -311,6 +335,45 @@ __global__ void __launch_bounds__(kLossThreads) desc_feat_loss_kernel(const TF* 
   }
 }
 
+// ---------------------------------------------------------------- loss sums
+// out[j] = sum over segments s of group j of w_s x (sum of the segment's floats), added in a
+// fixed order by one block: thread t adds elements t, t + 1024, ... of each segment in FP32
+// (a few dozen terms), the weighted per-segment totals are kept in double, and the block's
+// partials are added in thread order.
+constexpr int kMaxLossSegs = 16;
+constexpr int kLossSumThreads = 1024;
+struct LossSegs {
+  long long off[kMaxLossSegs];
+  long long len[kMaxLossSegs];
+  double w[kMaxLossSegs];
+  int group[kMaxLossSegs];
+  int n;
+};
+__global__ void __launch_bounds__(kLossSumThreads) desc_loss_sums_kernel(const float* __restrict__ buf, LossSegs segs,
+                                                                          float* __restrict__ out) {
+  __shared__ double red[2][kLossSumThreads / 32];
+  double acc[2] = {0.0, 0.0};
+  for (int k = 0; k < segs.n; ++k) {
+    float sk = 0.0f;
+    const float* p = buf + segs.off[k];
+    for (long long i = threadIdx.x; i < segs.len[k]; i += kLossSumThreads) sk += __ldg(p + i);
+    acc[segs.group[k]] += segs.w[k] * (double)sk;
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    double v = acc[j];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[j][warp] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 2) {
+    double t = 0.0;
+    for (int w = 0; w < kLossSumThreads / 32; ++w) t += red[threadIdx.x][w];
+    out[threadIdx.x] = (float)t;
+  }
+}
+
 }  // namespace desc
 }  // namespace svb
 
@@ -373,7 +436,7 @@ int svbrdf_desc_conv1_bwd(const void* gz, const float* weight, float* grad_rende
   if (v < 1 || h < 1 || w < 1) return fail(SVBRDF_ERR_INVALID, "bad shape");
   if ((uintptr_t)gz % 16 || (downsample && (uintptr_t)grad_renders % 8))
     return fail(SVBRDF_ERR_INVALID, "misaligned gz/grad_renders");
-  dim3 grid((w + kTile - 1) / kTile, (h + kTile - 1) / kTile, v), block(kTile, kTile);
+  dim3 grid((w + kTile - 1) / kTile, (h + kTile - 1) / kTile, v), block(128);
   cudaStream_t st = (cudaStream_t)stream;
   if (downsample)
     desc_conv1_bwd_kernel<true><<<grid, block, 0, st>>>((const __nv_bfloat16*)gz, weight, grad_renders, h, w);
@@ -411,6 +474,25 @@ int svbrdf_desc_feat_loss(const void* f, int f_is_bf16, const float* t, const fl
     desc_feat_loss_kernel<float><<<kLossBlocks, kLossThreads, 0, st>>>((const float*)f, t, gram_grad, coef, mask,
                                                                       (__nv_bfloat16*)g, partial, n);
   return check_launch("desc_feat_loss_kernel");
+}
+
+int svbrdf_desc_loss_sums(const float* buf, int n_segs, const long long* offsets, const long long* lengths,
+                          const double* weights, const int* groups, float* out, void* stream) {
+  if (!buf || !out || !offsets || !lengths || !weights || !groups) return fail(SVBRDF_ERR_INVALID, "null pointer");
+  if (n_segs < 1 || n_segs > kMaxLossSegs)
+    return fail(SVBRDF_ERR_UNSUPPORTED, "loss sums: 1 to %d segments (got %d)", kMaxLossSegs, n_segs);
+  LossSegs segs;
+  segs.n = n_segs;
+  for (int k = 0; k < n_segs; ++k) {
+    if (offsets[k] < 0 || lengths[k] < 0 || (groups[k] != 0 && groups[k] != 1))
+      return fail(SVBRDF_ERR_INVALID, "loss sums: bad segment %d", k);
+    segs.off[k] = offsets[k];
+    segs.len[k] = lengths[k];
+    segs.w[k] = weights[k];
+    segs.group[k] = groups[k];
+  }
+  desc_loss_sums_kernel<<<1, kLossSumThreads, 0, (cudaStream_t)stream>>>(buf, segs, out);
+  return check_launch("desc_loss_sums_kernel");
 }
 
 }  // extern "C"

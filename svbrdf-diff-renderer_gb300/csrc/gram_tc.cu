@@ -229,6 +229,7 @@ gemm_nt_kernel(const __grid_constant__ CUtensorMap tmap_a, const __grid_constant
   __shared__ __align__(8) uint64_t empty_bar[STAGES];
   __shared__ __align__(8) uint64_t acc_bar;
   __shared__ uint32_t tmem_slot;
+  __shared__ __align__(16) float s_tr[FUSE ? 4 : 1][32][36];  // per epilogue warp: a 32 x 32 chunk, rows padded
 
   const uint32_t base = (smem_u32(dsmem) + 1023u) & ~1023u;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -296,61 +297,63 @@ gemm_nt_kernel(const __grid_constant__ CUtensorMap tmap_a, const __grid_constant
                     *(volatile int*)err == 0;
     fence_after();
     if (FUSE) {
-      const size_t off = ((size_t)b * M + m) * Nn + n0;
+      // This warp's 32 rows: each 32-column chunk of F dG goes through a shared-memory tile so
+      // that f, t and g are read and written a row at a time (8 lanes x 4 channels per row,
+      // four rows per instruction) instead of one row per lane.
+      float(*tr)[36] = s_tr[q];
+      const size_t row0 = (size_t)b * M + m0 + q * 32;
+      const int rg = lane >> 3, qd = lane & 7;
       float acc = 0.0f;
       if (ok) {
 #pragma unroll 1
         for (int c0 = 0; c0 < BN; c0 += 32) {
           uint32_t r[32];
           tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)c0, r);
-          float fv[32];
-          if (fe.f_bf16) {
-            const uint4* fp = reinterpret_cast<const uint4*>(reinterpret_cast<const __nv_bfloat16*>(fe.f) + off + c0);
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-              const uint4 v4 = __ldg(fp + u);
-              const __nv_bfloat162* h2 = reinterpret_cast<const __nv_bfloat162*>(&v4);
+          for (int k = 0; k < 8; ++k)
+            *reinterpret_cast<float4*>(&tr[lane][4 * k]) =
+                make_float4(__uint_as_float(r[4 * k]), __uint_as_float(r[4 * k + 1]), __uint_as_float(r[4 * k + 2]),
+                            __uint_as_float(r[4 * k + 3]));
+          __syncwarp();
+          // four rows' f and t first (8 loads in flight per lane), then their arithmetic
+#pragma unroll 1
+          for (int h = 0; h < 8; h += 4) {
+          float fv[4][4], tv[4][4];
 #pragma unroll
-              for (int e = 0; e < 4; ++e) {
-                const float2 f2 = __bfloat1622float2(h2[e]);
-                fv[8 * u + 2 * e] = f2.x;
-                fv[8 * u + 2 * e + 1] = f2.y;
-              }
+          for (int i = 0; i < 4; ++i) {
+            const size_t off = (row0 + 4 * (h + i) + rg) * Nn + n0 + c0 + 4 * qd;
+            if (fe.f_bf16) {
+              const uint2 raw = __ldg(reinterpret_cast<const uint2*>(reinterpret_cast<const __nv_bfloat16*>(fe.f) + off));
+              const float2 a = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&raw.x));
+              const float2 c = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&raw.y));
+              fv[i][0] = a.x; fv[i][1] = a.y; fv[i][2] = c.x; fv[i][3] = c.y;
+            } else {
+              const float4 v4 = __ldg(reinterpret_cast<const float4*>(reinterpret_cast<const float*>(fe.f) + off));
+              fv[i][0] = v4.x; fv[i][1] = v4.y; fv[i][2] = v4.z; fv[i][3] = v4.w;
             }
-          } else {
-            const float4* fp = reinterpret_cast<const float4*>(reinterpret_cast<const float*>(fe.f) + off + c0);
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-              const float4 v4 = __ldg(fp + u);
-              fv[4 * u] = v4.x;
-              fv[4 * u + 1] = v4.y;
-              fv[4 * u + 2] = v4.z;
-              fv[4 * u + 3] = v4.w;
-            }
+            const float4 t4 = __ldg(reinterpret_cast<const float4*>(fe.t + off));
+            tv[i][0] = t4.x; tv[i][1] = t4.y; tv[i][2] = t4.z; tv[i][3] = t4.w;
           }
-          const float4* tp = reinterpret_cast<const float4*>(fe.t + off + c0);
-          uint32_t packed[16];
 #pragma unroll
-          for (int u = 0; u < 8; ++u) {
-            const float4 t4 = __ldg(tp + u);
-            const float tv[4] = {t4.x, t4.y, t4.z, t4.w};
+          for (int i = 0; i < 4; ++i) {
+            const int rr = 4 * (h + i) + rg;
+            const size_t off = (row0 + rr) * Nn + n0 + c0 + 4 * qd;
+            const float4 gd = *reinterpret_cast<const float4*>(&tr[rr][4 * qd]);
+            const float gg[4] = {gd.x, gd.y, gd.z, gd.w};
             float gv[4];
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
-              const int j = 4 * u + e;
-              const float d = fv[j] - tv[e];
+              const float d = fv[i][e] - tv[i][e];
               acc = fmaf(d, d, acc);
-              gv[e] = fe.mask && !(fv[j] > 0.0f) ? 0.0f : fmaf(fe.coef, d, __uint_as_float(r[j]));
+              gv[e] = fe.mask && !(fv[i][e] > 0.0f) ? 0.0f : fmaf(fe.coef, d, gg[e]);
             }
             __nv_bfloat162 h0 = __floats2bfloat162_rn(gv[0], gv[1]);
             __nv_bfloat162 h1 = __floats2bfloat162_rn(gv[2], gv[3]);
-            packed[2 * u] = *reinterpret_cast<uint32_t*>(&h0);
-            packed[2 * u + 1] = *reinterpret_cast<uint32_t*>(&h1);
+            *reinterpret_cast<uint2*>(fe.g + off) = make_uint2(*reinterpret_cast<uint32_t*>(&h0),
+                                                               *reinterpret_cast<uint32_t*>(&h1));
           }
-          uint4* gp = reinterpret_cast<uint4*>(fe.g + off + c0);
-#pragma unroll
-          for (int u = 0; u < 4; ++u)
-            gp[u] = make_uint4(packed[4 * u], packed[4 * u + 1], packed[4 * u + 2], packed[4 * u + 3]);
+          }
+          __syncwarp();  // the tile is rewritten by the next chunk
         }
       }
 #pragma unroll

@@ -38,6 +38,7 @@ gradient F dG as a K-major BF16 GEMM; BF16 operands, FP32 accumulation.
 """
 from __future__ import annotations
 
+import ctypes
 import math
 from typing import List, Optional, Sequence
 
@@ -74,11 +75,12 @@ def conv3x3_bf16(x: torch.Tensor, w: torch.Tensor, bias: Optional[torch.Tensor],
 
 
 def gram_bf16(f: torch.Tensor, err: torch.Tensor, target: Optional[torch.Tensor] = None, coef: float = 0.0,
-              want_dgram: bool = False):
+              want_dgram: bool = False, rows_out: Optional[torch.Tensor] = None):
     """The Gram term of NHWC BF16 features f [V, H, W, C] on the tensor cores
     (svbrdf_desc_gram + svbrdf_desc_gram_finish): G = F^T F / S per view (FP32 [V, C, C]). With
     ``target``: (None, loss rows [V, C] = sum_j (G - target)^2, BF16 coef (G - target) if
-    ``want_dgram``); without: (G, None, None)."""
+    ``want_dgram``), the rows written into ``rows_out`` when given (a contiguous FP32 [V, C]
+    view); without: (G, None, None)."""
     L = N.lib()
     st = N.stream_handle(f.device)
     v, h, w, c = f.shape
@@ -93,7 +95,7 @@ def gram_bf16(f: torch.Tensor, err: torch.Tensor, target: Optional[torch.Tensor]
         g = torch.empty(v, c, c, device=f.device, dtype=torch.float32)
         N.check(L.svbrdf_desc_gram_finish(part.data_ptr(), splits, v, c, s, None, 0.0, g.data_ptr(), None, None, st))
         return g, None, None
-    rows = torch.empty(v, c, device=f.device, dtype=torch.float32)
+    rows = rows_out if rows_out is not None else torch.empty(v, c, device=f.device, dtype=torch.float32)
     dg = torch.empty(v, c, c, device=f.device, dtype=torch.bfloat16) if want_dgram else None
     N.check(L.svbrdf_desc_gram_finish(part.data_ptr(), splits, v, c, s, target.data_ptr(), float(coef), None,
                                       N.ptr(dg), rows.data_ptr(), st))
@@ -157,7 +159,6 @@ class VGGDescriptor:
                 entry["w_fwd"] = wb.permute(0, 2, 3, 1).reshape(cout, 9, cin).contiguous().to(self.device)
                 entry["w_dg"] = wb.flip(2, 3).permute(1, 2, 3, 0).reshape(cin, 9, cout).contiguous().to(self.device)
             self.params[name] = entry
-        self._w2 = torch.tensor([wt * wt for wt in self.hook_weights], device=self.device, dtype=torch.float64)
         self.target = None
 
     def bf16_weights(self):
@@ -201,7 +202,9 @@ class VGGDescriptor:
     def _terms(self, hooks, cf: Optional[float], cg: Optional[float], hooks16=None):
         """Feature and Gram losses (0-d FP32 tensors). With cf/cg given, also the loss
         gradient at each hooked activation, cf d(feature)/df + cg d(gram)/df, as BF16 NHWC; the
-        last layer's gradient is masked by its ReLU (it starts the backward chain)."""
+        last layer's gradient is masked by its ReLU (it starts the backward chain). Every term's
+        partial sums land in one buffer, and one launch (svbrdf_desc_loss_sums) adds them with
+        the hook weights in a fixed order."""
         L = N.lib()
         st = N.stream_handle(self.device)
         tf, tg = self.target
@@ -210,40 +213,64 @@ class VGGDescriptor:
         nf = sum(f.numel() for f in hooks.values())
         ng = sum(g.numel() for g in tg)
         nparts = L.svbrdf_desc_partials()
-        feat_sums, gram_terms, grads = [], [], {}
+        fused = cf is not None and self.gram
+        # segments: each hook's feature partials, then each hook's Gram loss rows
+        lens, weights, groups = [], [], []
+        for name, wt in zip(self.hooks, self.hook_weights):
+            v, h, w, c = hooks[name].shape
+            lens.append(int(L.svbrdf_desc_gemm_nt_feat_partials(v, h * w, c)) if fused else nparts)
+            weights.append(wt * wt / nf)
+            groups.append(0)
+        if self.gram:
+            for name, wt in zip(self.hooks, self.hook_weights):
+                v, h, w, c = hooks[name].shape
+                lens.append(v * c)
+                weights.append(wt * wt / ng)
+                groups.append(1)
+        offs = [0]
+        for n in lens[:-1]:
+            offs.append(offs[-1] + n)
+        buf = torch.empty(offs[-1] + lens[-1], device=self.device, dtype=torch.float32)
+        nh = len(self.hooks)
+        grads = {}
         last = [it for it in self.layers if it != "pool"][-1][0]
         for k, (name, wt) in enumerate(zip(self.hooks, self.hook_weights)):
             f = hooks[name]
             v, h, w, c = f.shape
             s = h * w
+            part = buf[offs[k]:offs[k] + lens[k]]
             g = None
             if self.gram:
                 # the BF16 feature map (relu1_1's hook is FP32; its BF16 copy feeds conv1_2)
                 ff = hooks16[name]
                 # d/dF of w^2 sum (G - Gt)^2 / ng with G = F^T F / s: F (2 dG) / s, dG = 2 w^2 (G - Gt) / ng
                 coef_g = (4.0 * wt * wt * cg / (ng * s)) if cf is not None else 0.0
-                _, rows, dgram = gram_bf16(ff, self.err, tg[k], coef_g, want_dgram=cf is not None)
-                gram_terms.append((wt * wt) * rows.sum())
+                rows = buf[offs[nh + k]:offs[nh + k] + lens[nh + k]].view(v, c)
+                _, _, dgram = gram_bf16(ff, self.err, tg[k], coef_g, want_dgram=cf is not None, rows_out=rows)
             coef = (2.0 * wt * wt * cf / nf) if cf is not None else 0.0
             if cf is not None:
                 g = torch.empty(v, h, w, c, device=self.device, dtype=torch.bfloat16)
                 grads[name] = g
-            if cf is not None and self.gram:
+            if fused:
                 # the Gram gradient F dG with this hook's feature term in its epilogue
-                part = torch.empty(int(L.svbrdf_desc_gemm_nt_feat_partials(v, s, c)), device=self.device,
-                                   dtype=torch.float32)
                 N.check(L.svbrdf_desc_gemm_nt_feat(ff.data_ptr(), dgram.data_ptr(), f.data_ptr(),
                                                    int(f.dtype == torch.bfloat16), tf[k].data_ptr(), coef,
                                                    int(name == last), g.data_ptr(), part.data_ptr(), v, s, c, c,
                                                    self.err.data_ptr(), st))
             else:
-                part = torch.empty(nparts, device=self.device, dtype=torch.float32)
                 N.check(L.svbrdf_desc_feat_loss(f.data_ptr(), int(f.dtype == torch.bfloat16), tf[k].data_ptr(),
                                                 None, coef, int(name == last), N.ptr(g), part.data_ptr(),
                                                 f.numel(), st))
-            feat_sums.append(part.double().sum())
-        fl = ((torch.stack(feat_sums) * self._w2).sum() / nf).float()
-        gl = torch.stack(gram_terms).sum() / ng if self.gram else torch.zeros((), device=self.device)
+        out = torch.empty(2, device=self.device, dtype=torch.float32)
+        ns = len(lens)
+        a_off = (ctypes.c_longlong * ns)(*offs)
+        a_len = (ctypes.c_longlong * ns)(*lens)
+        a_w = (ctypes.c_double * ns)(*weights)
+        a_g = (ctypes.c_int * ns)(*groups)
+        N.check(L.svbrdf_desc_loss_sums(buf.data_ptr(), ns, ctypes.addressof(a_off), ctypes.addressof(a_len),
+                                        ctypes.addressof(a_w), ctypes.addressof(a_g), out.data_ptr(), st))
+        fl = out[0]
+        gl = out[1] if self.gram else torch.zeros((), device=self.device)
         return fl, gl, grads
 
     # ---- backward chain ----------------------------------------------------------------

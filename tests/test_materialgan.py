@@ -350,14 +350,17 @@ def test_gpu_generator_matches_reference_network(svb, cuda):
                                                  (2, 18, 256, 128, 3, 0), (1, 32, 128, 128, 3, 1),
                                                  (2, 16, 128, 9, 1, 0), (2, 20, 128, 64, 3, 1),
                                                  (16, 64, 64, 64, 3, 1), (24, 64, 64, 256, 3, 1),
-                                                 (16, 66, 128, 128, 3, 0)])
+                                                 (16, 66, 128, 128, 3, 0), (2, 32, 256, 256, 3, 1),
+                                                 (4, 40, 512, 256, 3, 0), (3, 64, 256, 512, 3, 1),
+                                                 (16, 64, 256, 256, 3, 1)])
 def test_conv_tf32_matches_torch(svb, cuda, b, h, cin, cout, k, pad):
     """The TF32 tensor-core convolution (forward and data gradient through _ConvTF32) against
     torch's FP32 convolution of the same channels-last maps: relative L2 <= 2e-3 (TF32 rounds
     both operands to 10 mantissa bits; FP32 accumulation). The shapes cover the 4^2 and 8^2
-    patches, two M-tiles per CTA tile (with a partial second one at 20 rows), and maps with
-    more tiles than SMs, where each persistent CTA runs several tiles through both TMEM
-    accumulator buffers."""
+    patches, two M-tiles per CTA tile (with a partial second one at 20 rows), maps with more
+    tiles than SMs, where each persistent CTA runs several tiles through both TMEM accumulator
+    buffers, and deep 256- and 512-channel maps (a partial tile at 38 rows, several tiles per
+    CTA)."""
     MG = svb.materialgan
     g = torch.Generator().manual_seed(b * h + cin)
     x = torch.randn(b, cin, h, h, generator=g).to(cuda).contiguous(memory_format=torch.channels_last)

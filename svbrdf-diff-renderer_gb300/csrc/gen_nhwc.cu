@@ -65,9 +65,9 @@ __device__ __forceinline__ void taps(int o, int n, int& lo, int& hi, float& wlo,
 
 __device__ __forceinline__ float act_pre(float y, float dv, float nz, float bias) { return fmaf(y, dv, nz) + bias; }
 
-// grid (ceil(W2 cv / 256), B H2), W2 = 2w + 2 halo: block row (b, Y); thread t of the row is
-// output vector (X, c) = (t / cv, t % cv), at up-sampled index X - halo. 32-bit index math
-// within a row.
+// grid (min(ceil(W2 cv / 256), 8), B H2), W2 = 2w + 2 halo: block row (b, Y); thread t of the
+// row is output vector (X, c) = (t / cv, t % cv), at up-sampled index X - halo, for t stepping
+// by the row's threads. 32-bit index math within a row.
 template <int VEC>
 __global__ void __launch_bounds__(256) nhwc_up_fwd_kernel(const float* __restrict__ x, const float* __restrict__ s,
                                                           float* __restrict__ y, int h, int w, int C, int halo) {
@@ -80,6 +80,7 @@ __global__ void __launch_bounds__(256) nhwc_up_fwd_kernel(const float* __restric
   const float* r1 = x + ((long long)b * h + y1) * w * C;
   const float* sb = s ? s + (long long)b * C : nullptr;
   float* out = y + (long long)blockIdx.y * W2 * C;
+#pragma unroll 2
   for (int t = blockIdx.x * 256 + threadIdx.x; t < W2 * cv; t += gridDim.x * 256) {
     const int c = t % cv, X = t / cv;
     int x0, x1;
@@ -416,7 +417,10 @@ int svbrdf_gen_upsample2_nhwc(const float* x, const float* s, float* y, int b, i
     return fail(SVBRDF_ERR_UNSUPPORTED, "upsample2_nhwc: too large");
   const bool v4 = c % 4 == 0 && a16(x) && a16(y) && a16(s);
   const int row = (2 * w + 2 * halo) * (v4 ? c / 4 : c);
-  dim3 grid((unsigned)((row + 255) / 256), (unsigned)(b * (2 * h + 2 * halo)));
+  // at most 8 blocks per output row: each thread loops over several vectors of the row, so
+  // the launch is a few tens of thousands of blocks rather than one per 256 vectors
+  const int per_row = (row + 255) / 256;
+  dim3 grid((unsigned)(per_row < 8 ? per_row : 8), (unsigned)(b * (2 * h + 2 * halo)));
   cudaStream_t st = (cudaStream_t)stream;
   if (v4) gen_nhwc::nhwc_up_fwd_kernel<4><<<grid, 256, 0, st>>>(x, s, y, h, w, c, halo);
   else gen_nhwc::nhwc_up_fwd_kernel<1><<<grid, 256, 0, st>>>(x, s, y, h, w, c, halo);

@@ -697,11 +697,11 @@ extern "C" int svbrdf_gen_conv_tf32_ex(const float* x, const float* weight, floa
   using namespace svb::tf32;
   if (!x || !weight || !y || !err) return fail(SVBRDF_ERR_INVALID, "conv_tf32: null x/weight/y/err");
   int sms = 0;
-  int rc = sm_count(&sms);
-  if (rc) return rc;
+  const int src = sm_count(&sms);
   tf32::Plan pl;
-  rc = plan_conv(b, hin, win, cin, cout, ksize, pad, sms, &pl);
+  int rc = plan_conv(b, hin, win, cin, cout, ksize, pad, src == SVBRDF_OK ? sms : 0, &pl);  // shape errors first
   if (rc) return rc;
+  if (src) return src;
   Geom& g = pl.g;
   if (g.splits > 1 && (!ws || ws_bytes < 4 * split_ws_floats(g))) {  // no room: one K range per tile
     const int total = g.taps * (cin / BK);

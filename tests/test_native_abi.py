@@ -299,3 +299,38 @@ def test_texel_count_limit_rejected_on_host(lib):
         args = [fake] * 8 + [9, h, w, 17.0, 0, 1, 0.01, 0.9, 0.999, 1e-8, fake, fake, 1 << 20, None]
         assert lib.svbrdf_fused_step(*args) == -2
         assert lib.svbrdf_fused_step_noalloc(*(args[:19] + [None])) == -2
+
+
+def test_new_entry_points_reject_bad_arguments_on_host(lib):
+    """The batched render, the loss sums, the fused Gram-gradient GEMM and the TF32 convolution
+    with a workspace refuse bad arguments before touching the device (nothing is launched)."""
+    fake = ctypes.c_void_p(16)
+    # batched render: batch must be >= 1; the per-material shape checks still apply
+    assert lib.svbrdf_render_fwd_batch(fake, fake, fake, fake, 9, 8, 8, 17.0, 0, fake, None, -1, None, None, 0,
+                                       None) == -1
+    assert lib.svbrdf_render_bwd_batch(fake, fake, fake, fake, 9, 8, 8, 17.0, -1, fake, fake, None, None, 0,
+                                       None) == -1
+    assert lib.svbrdf_render_fwd_batch(fake, fake, fake, fake, 9, 46341, 46341, 17.0, 2, fake, None, -1, None,
+                                       None, 0, None) == -2
+    # loss sums: 1 to 16 segments, groups 0 or 1
+    off = (ctypes.c_longlong * 2)(0, 4)
+    ln = (ctypes.c_longlong * 2)(4, 4)
+    w = (ctypes.c_double * 2)(1.0, 1.0)
+    g_ok = (ctypes.c_int * 2)(0, 1)
+    g_bad = (ctypes.c_int * 2)(0, 2)
+    a = [ctypes.addressof(x) for x in (off, ln, w)]
+    assert lib.svbrdf_desc_loss_sums(fake, 0, *a, ctypes.addressof(g_ok), fake, None) == -2
+    assert lib.svbrdf_desc_loss_sums(fake, 17, *a, ctypes.addressof(g_ok), fake, None) == -2
+    assert lib.svbrdf_desc_loss_sums(fake, 2, *a, ctypes.addressof(g_bad), fake, None) == -1
+    assert lib.svbrdf_desc_loss_sums(None, 2, *a, ctypes.addressof(g_ok), fake, None) == -1
+    # fused Gram gradient: m a multiple of 128, k of 64, the feature pointers present
+    err = fake
+    assert lib.svbrdf_desc_gemm_nt_feat(fake, fake, fake, 1, fake, 0.1, 0, fake, fake, 1, 100, 64, 64, err,
+                                        None) == -2
+    assert lib.svbrdf_desc_gemm_nt_feat(fake, fake, None, 1, fake, 0.1, 0, fake, fake, 1, 128, 64, 64, err,
+                                        None) == -1
+    assert lib.svbrdf_desc_gemm_nt_feat_partials(0, 128, 64) == 0
+    assert lib.svbrdf_desc_gemm_nt_feat_partials(2, 256, 64) == 2 * 2 * 1 * 4
+    # TF32 convolution with a workspace: the same shape rules as without
+    assert lib.svbrdf_gen_conv_tf32_ex(fake, fake, fake, None, 0, 1, 8, 8, 48, 64, 3, 1, err, None) == -2
+    assert lib.svbrdf_gen_conv_tf32_ex(fake, fake, fake, None, 0, 1, 8, 8, 64, 64, 5, 1, err, None) == -1

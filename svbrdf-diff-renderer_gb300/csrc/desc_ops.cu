@@ -219,12 +219,12 @@ __device__ __forceinline__ void bf8_store(__nv_bfloat16* p, const float f[8]) {
 template <bool AVG>
 __global__ void desc_pool_fwd_kernel(const __nv_bfloat16* __restrict__ x, __nv_bfloat16* __restrict__ y, int V, int H,
                                      int W, int C) {
+  // grid (ceil(Wo C8 / 256), V Ho): block row (v, yo); thread q of the row is (xo, c8)
   const int Ho = H / 2, Wo = W / 2, C8 = C / 8;
-  const long long n = (long long)V * Ho * Wo * C8;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const int c8 = (int)(i % C8);
-    const long long p = i / C8;
-    const int xo = (int)(p % Wo), yo = (int)((p / Wo) % Ho), v = (int)(p / ((long long)Wo * Ho));
+  const int v = blockIdx.y / Ho, yo = blockIdx.y % Ho;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < Wo * C8; q += gridDim.x * blockDim.x) {
+    const int c8 = q % C8, xo = q / C8;
+    const size_t p = ((size_t)v * Ho + yo) * Wo + xo;
     const __nv_bfloat16* base = x + (((size_t)v * H + 2 * yo) * W + 2 * xo) * C + c8 * 8;
     float m[8], t[8];
     bf8_load(base, m);
@@ -250,12 +250,12 @@ template <bool AVG>
 __global__ void desc_pool_bwd_kernel(const __nv_bfloat16* __restrict__ gy, const __nv_bfloat16* __restrict__ x,
                                      const __nv_bfloat16* __restrict__ addend, __nv_bfloat16* __restrict__ gx, int V,
                                      int H, int W, int C) {
+  // grid (ceil(Wo C8 / 256), V Ho): block row (v, yo); thread t of the row is (xo, c8)
   const int Ho = H / 2, Wo = W / 2, C8 = C / 8;
-  const long long n = (long long)V * Ho * Wo * C8;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    const int c8 = (int)(i % C8);
-    const long long p = i / C8;
-    const int xo = (int)(p % Wo), yo = (int)((p / Wo) % Ho), v = (int)(p / ((long long)Wo * Ho));
+  const int v = blockIdx.y / Ho, yo = blockIdx.y % Ho;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < Wo * C8; t += gridDim.x * blockDim.x) {
+    const int c8 = t % C8, xo = t / C8;
+    const size_t p = ((size_t)v * Ho + yo) * Wo + xo;
     const size_t b0 = (((size_t)v * H + 2 * yo) * W + 2 * xo) * C + c8 * 8;
     const size_t offs[4] = {0, (size_t)C, (size_t)W * C, (size_t)W * C + C};
     float xv[4][8], g[8];
@@ -380,19 +380,16 @@ __global__ void __launch_bounds__(kLossSumThreads) desc_loss_sums_kernel(const f
 using namespace svb;
 using namespace svb::desc;
 
-static int grid_for_elems(long long n) {
-  const long long b = (n + 255) / 256;
-  return (int)(b < 4096 ? (b < 1 ? 1 : b) : 4096);
-}
-
 template <bool AVG>
 static int pool_fwd(const void* x, void* y, int v, int h, int w, int c, void* stream) {
   if (!x || !y) return fail(SVBRDF_ERR_INVALID, "null pointer");
   if (v < 1 || h < 2 || w < 2 || h % 2 || w % 2 || c < 8 || c % 8)
     return fail(SVBRDF_ERR_UNSUPPORTED, "pool: even H, W and C a multiple of 8 needed");
   if (((uintptr_t)x | (uintptr_t)y) % 16) return fail(SVBRDF_ERR_INVALID, "pool: 16-byte alignment needed");
-  const long long n = (long long)v * (h / 2) * (w / 2) * (c / 8);
-  desc_pool_fwd_kernel<AVG><<<grid_for_elems(n), 256, 0, (cudaStream_t)stream>>>(
+  if ((long long)v * (h / 2) > 65535 || (long long)(w / 2) * (c / 8) >= (1LL << 30))
+    return fail(SVBRDF_ERR_UNSUPPORTED, "pool: too large");
+  const dim3 grid((unsigned)(((w / 2) * (c / 8) + 255) / 256), (unsigned)(v * (h / 2)));
+  desc_pool_fwd_kernel<AVG><<<grid, 256, 0, (cudaStream_t)stream>>>(
       (const __nv_bfloat16*)x, (__nv_bfloat16*)y, v, h, w, c);
   return check_launch("desc_pool_fwd_kernel");
 }
@@ -405,8 +402,10 @@ static int pool_bwd(const void* gy, const void* x, const void* addend, void* gx,
     return fail(SVBRDF_ERR_UNSUPPORTED, "pool: even H, W and C a multiple of 8 needed");
   if (((uintptr_t)gy | (uintptr_t)x | (uintptr_t)addend | (uintptr_t)gx) % 16)
     return fail(SVBRDF_ERR_INVALID, "pool: 16-byte alignment needed");
-  const long long n = (long long)v * (h / 2) * (w / 2) * (c / 8);
-  desc_pool_bwd_kernel<AVG><<<grid_for_elems(n), 256, 0, (cudaStream_t)stream>>>(
+  if ((long long)v * (h / 2) > 65535 || (long long)(w / 2) * (c / 8) >= (1LL << 30))
+    return fail(SVBRDF_ERR_UNSUPPORTED, "pool: too large");
+  const dim3 grid((unsigned)(((w / 2) * (c / 8) + 255) / 256), (unsigned)(v * (h / 2)));
+  desc_pool_bwd_kernel<AVG><<<grid, 256, 0, (cudaStream_t)stream>>>(
       (const __nv_bfloat16*)gy, (const __nv_bfloat16*)x, (const __nv_bfloat16*)addend, (__nv_bfloat16*)gx, v, h, w,
       c);
   return check_launch("desc_pool_bwd_kernel");

@@ -172,7 +172,7 @@ gram_kernel(const __grid_constant__ CUtensorMap tmap_f, float* __restrict__ part
   if (warp == 1) release_tmem(&acc_bar, tmem, (uint32_t)BN);
 }
 
-// grid (C, V), min(C, 256) threads (whole warps): row i of view v.
+// grid (C, V), 256 threads: row i of view v.
 __global__ void __launch_bounds__(256)
 gram_finish_kernel(const float* __restrict__ partial, int splits, int C, float inv_s, const float* __restrict__ gt,
                    float coef, float* __restrict__ gram_out, __nv_bfloat16* __restrict__ dgram,
@@ -180,9 +180,8 @@ gram_finish_kernel(const float* __restrict__ partial, int splits, int C, float i
   const int i = blockIdx.x, v = blockIdx.y;
   __shared__ double red[8];
   double acc = 0.0;
-  for (int j = threadIdx.x; j < C; j += blockDim.x) {
+  for (int j = threadIdx.x; j < C; j += 256) {
     float g = 0.f;
-#pragma unroll 8
     for (int s = 0; s < splits; ++s) g += __ldg(partial + (((size_t)v * splits + s) * C + i) * C + j);
     g *= inv_s;
     const size_t o = ((size_t)v * C + i) * C + j;
@@ -197,7 +196,8 @@ gram_finish_kernel(const float* __restrict__ partial, int splits, int C, float i
   __syncthreads();
   if (threadIdx.x == 0 && loss_part) {
     double t = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+#pragma unroll
+    for (int w = 0; w < 8; ++w) t += red[w];
     loss_part[(size_t)v * C + i] = (float)t;
   }
 }
@@ -512,9 +512,7 @@ int svbrdf_desc_gram_finish(const float* partial, int splits, int v, int c, int 
   if (!partial || splits < 1 || v < 1 || v > 65535 || c < 1 || c > 65535 || s < 1)
     return fail(SVBRDF_ERR_INVALID, "gram_finish: bad arguments");
   dim3 grid((unsigned)c, (unsigned)v);
-  // one block per row of G, one thread per column up to 256 (C = 64: 64-thread blocks)
-  const int threads = c < 256 ? ((c + 31) / 32) * 32 : 256;
-  gram::gram_finish_kernel<<<grid, threads, 0, (cudaStream_t)stream>>>(partial, splits, c, 1.0f / (float)s, gram_target,
+  gram::gram_finish_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(partial, splits, c, 1.0f / (float)s, gram_target,
                                                                    coef, gram_out, (__nv_bfloat16*)dgram, loss_part);
   return check_launch("gram_finish_kernel");
 }

@@ -51,7 +51,17 @@ class _Dense(torch.nn.Module):
         self.act = act
 
     def forward(self, x):
-        y = Fn.linear(x, self.weight * self.scale, self.bias * self.lr_mul)
+        if self.weight.requires_grad or self.bias.requires_grad:
+            w, b = self.weight * self.scale, self.bias * self.lr_mul
+        else:  # frozen: the scaled pair once, while the parameters are unchanged
+            key = (self.weight.data_ptr(), self.weight._version, self.bias.data_ptr(), self.bias._version,
+                   self.weight.dtype)
+            if getattr(self, "_scaled_key", None) != key:
+                with torch.no_grad():
+                    self._w_scaled, self._b_scaled = self.weight * self.scale, self.bias * self.lr_mul
+                self._scaled_key = key
+            w, b = self._w_scaled, self._b_scaled
+        y = Fn.linear(x, w, b)
         return Fn.leaky_relu(y, 0.2) * LRELU_GAIN if self.act else y
 
 
@@ -463,7 +473,7 @@ class _ModConv(torch.nn.Module):
         """The shared-weight convolution of the style-scaled input, and the demodulation
         d [B, cout] (None without demodulation) still to be applied to its output."""
         s = self.affine(w)  # [B, cin]
-        wsc = self.weight * self.scale
+        wsc, w2t = self._scaled_weight()
         # an up-sampling layer convolves the up-sampled map with its one-sample halo, unpadded
         # (_upsample2_halo): the reference's transposed convolution + filter on the border too
         pad = 0 if self.up else self.k // 2
@@ -482,9 +492,24 @@ class _ModConv(torch.nn.Module):
             y = Fn.conv2d(x, wsc, padding=pad)
         d = None
         if self.demod:
-            w2 = wsc.pow(2).sum(dim=(2, 3))  # [cout, cin]
-            d = torch.rsqrt(s.pow(2) @ w2.t() + 1e-8)  # [B, cout]
+            d = torch.rsqrt(s.pow(2) @ w2t + 1e-8)  # [B, cout]
         return y, d
+
+    def _scaled_weight(self):
+        """(scale * weight, its squared sums over the taps transposed, [cin, cout]). A frozen
+        weight's pair is computed once and cached while the weight is unchanged; a trainable
+        one is recomputed on every call, inside autograd."""
+        if self.weight.requires_grad:
+            wsc = self.weight * self.scale
+            return wsc, wsc.pow(2).sum(dim=(2, 3)).t()
+        key = (self.weight.data_ptr(), self.weight._version, str(self.weight.device), self.weight.dtype)
+        if getattr(self, "_wsc_key", None) != key:
+            with torch.no_grad():
+                wsc = self.weight * self.scale
+                self._wsc = wsc
+                self._w2t = wsc.pow(2).sum(dim=(2, 3)).t().contiguous()
+            self._wsc_key = key
+        return self._wsc, self._w2t
 
 
 class _StyleLayer(torch.nn.Module):

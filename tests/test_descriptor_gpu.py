@@ -199,6 +199,36 @@ def test_descriptor_reference_mode_vs_fp64_oracle(svb, cuda):
     assert rel_l2(gdr, r.grad) <= 1e-6
 
 
+@pytest.mark.parametrize("v,h,w,c", [(2, 8, 12, 16), (9, 64, 64, 64), (3, 32, 16, 256)])
+def test_maxpool_kernels_match_torch(svb, cuda, v, h, w, c):
+    """svbrdf_desc_pool_fwd/_bwd against torch's max pool on the same BF16 values: the pooled
+    maxima exactly; the backward (the gradient routed to the window's maximum, plus the
+    addend, masked by x > 0) exactly on every window whose maximum is unique."""
+    N = svb._native
+    L = N.lib()
+    st = N.stream_handle(cuda)
+    g = torch.Generator().manual_seed(v * h + c)
+    x = torch.randn(v, h, w, c, generator=g).to(cuda, torch.bfloat16)
+    y = torch.empty(v, h // 2, w // 2, c, device=cuda, dtype=torch.bfloat16)
+    N.check(L.svbrdf_desc_pool_fwd(x.data_ptr(), y.data_ptr(), v, h, w, c, st))
+    xf = x.float().permute(0, 3, 1, 2)
+    ref, idx = torch.nn.functional.max_pool2d(xf, 2, return_indices=True)
+    assert torch.equal(y.float(), ref.permute(0, 2, 3, 1))
+    gy = torch.randn(v, h // 2, w // 2, c, generator=g).to(cuda, torch.bfloat16)
+    add = torch.randn(v, h, w, c, generator=g).to(cuda, torch.bfloat16)
+    gx = torch.empty_like(x)
+    N.check(L.svbrdf_desc_pool_bwd(gy.data_ptr(), x.data_ptr(), add.data_ptr(), gx.data_ptr(), v, h, w, c, st))
+    routed = torch.nn.functional.max_unpool2d(gy.float().permute(0, 3, 1, 2), idx, 2, output_size=xf.shape[-2:])
+    want = ((routed + add.float().permute(0, 3, 1, 2)) * (xf > 0)).permute(0, 2, 3, 1)
+    win = xf.reshape(v, c, h // 2, 2, w // 2, 2)
+    top = win.amax(dim=(3, 5), keepdim=True)
+    unique = ((win == top).sum(dim=(3, 5)) == 1)  # [v, c, h/2, w/2]
+    keep = unique.repeat_interleave(2, 2).repeat_interleave(2, 3).permute(0, 2, 3, 1)
+    torch.cuda.synchronize()
+    assert bool(keep.float().mean() > 0.9)
+    assert torch.equal(gx.float()[keep], want.to(torch.bfloat16).float()[keep])
+
+
 def test_avgpool_kernels_match_torch(svb, cuda):
     """svbrdf_desc_avgpool_fwd/_bwd against torch's average pool on the same BF16 values, the
     backward with its hook gradient and ReLU mask."""

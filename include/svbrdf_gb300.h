@@ -390,6 +390,16 @@ int svbrdf_gen_upsample2_nhwc(const float* x, const float* s, float* y, int b, i
 /* Adjoint of the up-sampling: gx [b][h][w][c] from g [b][2h+2 halo][2w+2 halo][c]. */
 int svbrdf_gen_upsample2_nhwc_bwd(const float* g, float* gx, int b, int h, int w, int c, int halo, void* stream);
 
+/* The toRGB layer's epilogue (the reference's ToRGB output plus the up-sampled skip image,
+ * src/higan_models/stylegan2_generator_network.py): img [b][c][h][w] (NCHW) = yp[b][y][x][ch]
+ * (channels-last, cp >= c channels per pixel: the 1x1 convolution's padded output) + bias[ch]
+ * + up2(prev) (prev NCHW [b][c][h/2][w/2], nullable; the 2x up-sampling of
+ * svbrdf_gen_upsample2). The adjoint writes gyp = g for ch < c and 0 for the padding channels;
+ * prev's gradient is svbrdf_gen_upsample2_bwd of g. */
+int svbrdf_gen_rgb_nhwc(const float* yp, int cp, const float* bias, const float* prev, float* img, int b, int c, int h,
+                        int w, void* stream);
+int svbrdf_gen_rgb_nhwc_bwd(const float* g, float* gyp, int cp, int b, int c, int h, int w, void* stream);
+
 /* y[b][p][c] = x[b][p][c] s[b][c], hw pixels. */
 int svbrdf_gen_scale_nhwc(const float* x, const float* s, float* y, int b, int hw, int c, void* stream);
 

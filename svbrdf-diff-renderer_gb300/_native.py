@@ -186,6 +186,10 @@ def _declare(L):
     L.svbrdf_gen_upsample2_nhwc.argtypes = [P, P, P, I, I, I, I, I, P]
     L.svbrdf_gen_upsample2_nhwc_bwd.restype = I
     L.svbrdf_gen_upsample2_nhwc_bwd.argtypes = [P, P, I, I, I, I, I, P]
+    L.svbrdf_gen_rgb_nhwc.restype = I
+    L.svbrdf_gen_rgb_nhwc.argtypes = [P, I, P, P, P, I, I, I, I, P]
+    L.svbrdf_gen_rgb_nhwc_bwd.restype = I
+    L.svbrdf_gen_rgb_nhwc_bwd.argtypes = [P, P, I, I, I, I, I, P]
     L.svbrdf_gen_scale_nhwc.restype = I
     L.svbrdf_gen_scale_nhwc.argtypes = [P, P, P, I, I, I, P]
     L.svbrdf_gen_scale_nhwc_bwd.restype = I
@@ -225,6 +229,7 @@ EXPORTS = [
     "svbrdf_gen_upsample2",
     "svbrdf_gen_upsample2_bwd", "svbrdf_gen_upsample2_scaled", "svbrdf_gen_scale", "svbrdf_gen_scale_bwd", "svbrdf_gen_act", "svbrdf_gen_act_bwd",
     "svbrdf_gen_nhwc_partial_floats", "svbrdf_gen_upsample2_nhwc", "svbrdf_gen_upsample2_nhwc_bwd",
+    "svbrdf_gen_rgb_nhwc", "svbrdf_gen_rgb_nhwc_bwd",
     "svbrdf_gen_scale_nhwc", "svbrdf_gen_scale_nhwc_bwd", "svbrdf_gen_act_nhwc", "svbrdf_gen_act_nhwc_bwd",
     "svbrdf_gen_conv_tf32", "svbrdf_gen_conv_tf32_ws_bytes", "svbrdf_gen_conv_tf32_ex",
     "svbrdf_envmap_render", "svbrdf_selftest_wait_timeout",

@@ -328,13 +328,15 @@ int get_tensor_map_encoder(PFN_cuTensorMapEncodeTiled_v12000* out) {
   return SVBRDF_OK;
 }
 
-constexpr size_t kStageBudget = 200 * 1024;  // ring bytes per CTA (one CTA per SM)
+constexpr size_t kStageBudget = 216 * 1024;  // ring bytes per CTA (one CTA per SM)
 
+// Weight-ring depth: as many slices as fit beside two input slots, up to 16 (a 64-channel
+// tile's 9 taps then stream a whole tile ahead).
 template <int BN, int MT>
 constexpr int halo_bstages() {
-  return (int)((kStageBudget - 2 * (size_t)Halo<MT>::kABytes) / (size_t)(BN * BK * 2)) < 8
+  return (int)((kStageBudget - 2 * (size_t)Halo<MT>::kABytes) / (size_t)(BN * BK * 2)) < 16
              ? (int)((kStageBudget - 2 * (size_t)Halo<MT>::kABytes) / (size_t)(BN * BK * 2))
-             : 8;
+             : 16;
 }
 
 template <int BN, int MT, int EPI>

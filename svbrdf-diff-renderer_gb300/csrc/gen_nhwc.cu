@@ -388,6 +388,56 @@ __global__ void nhwc_colsum_kernel(const float* __restrict__ part, float* __rest
   out[i] = sum;
 }
 
+// The toRGB layer's epilogue: its 1x1 convolution leaves a channels-last map with cp (>= c)
+// channels per pixel; the image is written in NCHW (the layout of the textures the renderer
+// reads) as img[b][ch][y][x] = yp[b][y][x][ch] + bias[ch] + up2(prev)[b][ch][y][x], prev the
+// previous resolution's image (NCHW, nullable; up2 the [1, 3, 3, 1] up-sampling as
+// nhwc_up_fwd_kernel computes it). grid (ceil(W / 256), B H): block row (b, y), thread x.
+__global__ void __launch_bounds__(256) rgb_fwd_kernel(const float* __restrict__ yp, int cp,
+                                                      const float* __restrict__ bias, const float* __restrict__ prev,
+                                                      float* __restrict__ img, int C, int H, int W) {
+  const int b = blockIdx.y / H, yy = blockIdx.y % H;
+  const int x = blockIdx.x * 256 + threadIdx.x;
+  if (x >= W) return;
+  const float* row = yp + (((long long)b * H + yy) * W + x) * cp;
+  int y0 = 0, y1 = 0, x0 = 0, x1 = 0;
+  float wy0 = 0.f, wy1 = 0.f, wx0 = 0.f, wx1 = 0.f;
+  if (prev) {
+    taps(yy, H / 2, y0, y1, wy0, wy1);
+    taps(x, W / 2, x0, x1, wx0, wx1);
+  }
+  const long long hw = (long long)H * W, hw2 = (long long)(H / 2) * (W / 2);
+  for (int ch = 0; ch < C; ++ch) {
+    float v = __ldg(row + ch) + __ldg(bias + ch);
+    if (prev) {
+      const float* pp = prev + ((long long)b * C + ch) * hw2;
+      const int w2 = W / 2;
+      v += wy0 * (wx0 * __ldg(pp + y0 * w2 + x0) + wx1 * __ldg(pp + y0 * w2 + x1)) +
+           wy1 * (wx0 * __ldg(pp + y1 * w2 + x0) + wx1 * __ldg(pp + y1 * w2 + x1));
+    }
+    img[((long long)b * C + ch) * hw + (long long)yy * W + x] = v;
+  }
+}
+
+// Its adjoint for the convolution: gyp[b][y][x][ch] = g[b][ch][y][x] for ch < C, 0 for the
+// padding channels C .. cp - 1 (the skip image's gradient is the NCHW up-sampling adjoint of g).
+template <int VEC>
+__global__ void __launch_bounds__(256) rgb_bwd_kernel(const float* __restrict__ g, float* __restrict__ gyp, int cp,
+                                                      int C, int H, int W) {
+  const int b = blockIdx.y / H, yy = blockIdx.y % H;
+  const int x = blockIdx.x * 256 + threadIdx.x;
+  if (x >= W) return;
+  float* row = gyp + (((long long)b * H + yy) * W + x) * cp;
+  const long long hw = (long long)H * W;
+  const float* gp = g + (long long)b * C * hw + (long long)yy * W + x;
+  for (int ch = 0; ch < cp; ch += VEC) {  // VEC = 4: the pixel's row as 16-byte stores
+    float v[VEC];
+#pragma unroll
+    for (int j = 0; j < VEC; ++j) v[j] = ch + j < C ? __ldg(gp + (long long)(ch + j) * hw) : 0.0f;
+    stv<VEC>(row + ch, v);
+  }
+}
+
 }  // namespace gen_nhwc
 }  // namespace svb
 
@@ -515,6 +565,29 @@ int svbrdf_gen_act_nhwc_bwd(const float* gout, const float* y, const float* d, c
   if (rc || !gd) return rc;
   gen_nhwc::nhwc_colsum_kernel<<<(unsigned)((b * c + 255) / 256), 256, 0, st>>>(part, gd, b, c, nc);
   return check_launch("nhwc_colsum_kernel");
+}
+
+
+int svbrdf_gen_rgb_nhwc(const float* yp, int cp, const float* bias, const float* prev, float* img, int b, int c, int h,
+                        int w, void* stream) {
+  if (!yp || !bias || !img || b < 1 || c < 1 || cp < c || h < 1 || w < 1)
+    return fail(SVBRDF_ERR_INVALID, "rgb_nhwc: bad arguments");
+  if (prev && (h % 2 || w % 2)) return fail(SVBRDF_ERR_INVALID, "rgb_nhwc: a skip image needs even H and W");
+  if ((long long)b * h > 65535) return fail(SVBRDF_ERR_UNSUPPORTED, "rgb_nhwc: too large");
+  dim3 grid((unsigned)((w + 255) / 256), (unsigned)(b * h));
+  gen_nhwc::rgb_fwd_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(yp, cp, bias, prev, img, c, h, w);
+  return check_launch("rgb_fwd_kernel");
+}
+
+int svbrdf_gen_rgb_nhwc_bwd(const float* g, float* gyp, int cp, int b, int c, int h, int w, void* stream) {
+  if (!g || !gyp || b < 1 || c < 1 || cp < c || h < 1 || w < 1) return fail(SVBRDF_ERR_INVALID, "rgb_nhwc_bwd: bad arguments");
+  if ((long long)b * h > 65535) return fail(SVBRDF_ERR_UNSUPPORTED, "rgb_nhwc_bwd: too large");
+  dim3 grid((unsigned)((w + 255) / 256), (unsigned)(b * h));
+  if (cp % 4 == 0 && a16(gyp))
+    gen_nhwc::rgb_bwd_kernel<4><<<grid, 256, 0, (cudaStream_t)stream>>>(g, gyp, cp, c, h, w);
+  else
+    gen_nhwc::rgb_bwd_kernel<1><<<grid, 256, 0, (cudaStream_t)stream>>>(g, gyp, cp, c, h, w);
+  return check_launch("rgb_bwd_kernel");
 }
 
 }  // extern "C"

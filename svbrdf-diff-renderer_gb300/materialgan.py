@@ -254,7 +254,7 @@ class _ConvTF32(torch.autograd.Function):
     k - 1 - pad; the weights are frozen (no weight gradient)."""
 
     @staticmethod
-    def forward(ctx, x, w_fwd, w_dg, cout, k, pad):
+    def forward(ctx, x, w_fwd, w_dg, cout, k, pad, keep_pad=False):
         from . import _native as N
 
         x = _cl(x)
@@ -265,7 +265,8 @@ class _ConvTF32(torch.autograd.Function):
         _conv_tf32(x, w_fwd, y, b, h, wd, c, coutp, k, pad)
         ctx.save_for_backward(w_dg)
         ctx.geom = (b, c, h, wd, coutp, cout, k, pad, ho, wo)
-        return y if coutp == cout else y[:, :cout]
+        ctx.keep_pad = keep_pad
+        return y if (coutp == cout or keep_pad) else y[:, :cout]
 
     @staticmethod
     def backward(ctx, gy):
@@ -273,7 +274,7 @@ class _ConvTF32(torch.autograd.Function):
 
         (w_dg,) = ctx.saved_tensors
         b, c, h, wd, coutp, cout, k, pad, ho, wo = ctx.geom
-        if coutp != cout:
+        if coutp != cout and not ctx.keep_pad:
             gp = torch.empty(b, coutp, ho, wo, device=gy.device, dtype=torch.float32, memory_format=CL)
             gp[:, cout:].zero_()
             gp[:, :cout] = gy
@@ -281,7 +282,40 @@ class _ConvTF32(torch.autograd.Function):
         gy = _cl(gy)
         gx = torch.empty(b, c, h, wd, device=gy.device, dtype=torch.float32, memory_format=CL)
         _conv_tf32(gy, w_dg, gx, b, ho, wo, coutp, c, k, k - 1 - pad)
-        return gx, None, None, None, None, None
+        return gx, None, None, None, None, None, None
+
+
+class _RgbNHWC(torch.autograd.Function):
+    """The toRGB epilogue (svbrdf_gen_rgb_nhwc[_bwd]): the 1x1 convolution's padded
+    channels-last output yp [B, cp, H, W] plus the bias plus the up-sampled previous image
+    ``prev`` (NCHW, or None), written as one NCHW image [B, c, H, W]. The bias is frozen."""
+
+    @staticmethod
+    def forward(ctx, yp, bias, prev, c):
+        from . import _native as N
+
+        b, cp, h, w = yp.shape
+        img = torch.empty(b, c, h, w, device=yp.device, dtype=torch.float32)
+        N.check(N.lib().svbrdf_gen_rgb_nhwc(yp.data_ptr(), cp, bias.data_ptr(), N.ptr(prev), img.data_ptr(), b, c, h, w,
+                                            N.stream_handle(yp.device)))
+        ctx.geom = (b, cp, c, h, w, prev is not None)
+        return img
+
+    @staticmethod
+    def backward(ctx, g):
+        from . import _native as N
+
+        b, cp, c, h, w, has_prev = ctx.geom
+        L = N.lib()
+        st = N.stream_handle(g.device)
+        g = g.contiguous()
+        gyp = torch.empty(b, cp, h, w, device=g.device, dtype=torch.float32, memory_format=CL)
+        N.check(L.svbrdf_gen_rgb_nhwc_bwd(g.data_ptr(), gyp.data_ptr(), cp, b, c, h, w, st))
+        gprev = None
+        if has_prev and ctx.needs_input_grad[2]:
+            gprev = torch.empty(b, c, h // 2, w // 2, device=g.device, dtype=torch.float32)
+            N.check(L.svbrdf_gen_upsample2_bwd(g.data_ptr(), gprev.data_ptr(), b * c, h // 2, w // 2, st))
+        return gyp, None, gprev, None
 
 
 class _ScaleNHWC(torch.autograd.Function):
@@ -469,9 +503,10 @@ class _ModConv(torch.nn.Module):
             self._tf32_key = key
         return self._w_fwd, self._w_dg
 
-    def parts(self, x, w):
+    def parts(self, x, w, keep_pad=False):
         """The shared-weight convolution of the style-scaled input, and the demodulation
-        d [B, cout] (None without demodulation) still to be applied to its output."""
+        d [B, cout] (None without demodulation) still to be applied to its output. With
+        ``keep_pad`` the TF32 path returns its output with the channels padded to 32."""
         s = self.affine(w)  # [B, cin]
         wsc, w2t = self._scaled_weight()
         # an up-sampling layer convolves the up-sampled map with its one-sample halo, unpadded
@@ -482,7 +517,7 @@ class _ModConv(torch.nn.Module):
             x = _UpsampleNHWC.apply(x, s, 1) if self.up else _ScaleNHWC.apply(x, s)
             if self._tf32_ok(x):
                 w_fwd, w_dg = self._tf32_weights(wsc)
-                y = _ConvTF32.apply(x, w_fwd, w_dg, self.weight.shape[0], self.k, pad)
+                y = _ConvTF32.apply(x, w_fwd, w_dg, self.weight.shape[0], self.k, pad, keep_pad)
             else:
                 y = Fn.conv2d(x, _cl(wsc), padding=pad)
         else:
@@ -538,6 +573,15 @@ class _ToRGB(torch.nn.Module):
         self.bias = torch.nn.Parameter(torch.zeros(cout))
 
     def forward(self, x, w, skip):
+        cout = self.bias.shape[0]
+        if (_use_kernels(x) and _is_nhwc(x) and not self.bias.requires_grad and self.conv._tf32_ok(x) and
+                x.shape[-1] % 2 == 0 and x.shape[-2] % 2 == 0 and
+                (skip is None or (skip.is_contiguous() and skip.dtype == torch.float32 and
+                                  tuple(skip.shape) == (x.shape[0], cout, x.shape[-2] // 2, x.shape[-1] // 2)))):
+            # the TF32 convolution's padded channels-last output, bias and the up-sampled skip
+            # image in one pass that writes the image in NCHW
+            yp, _ = self.conv.parts(x, w, keep_pad=True)
+            return _RgbNHWC.apply(_cl(yp), self.bias, skip, cout)
         y = self.conv(x, w) + self.bias.view(1, -1, 1, 1)
         return y if skip is None else y + _upsample2(skip)
 

@@ -444,6 +444,36 @@ def test_conv_tf32_split_k_matches_unsplit(svb, cuda, b, h, cin, cout, k, pad):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("b,h,cp,c,skip", [(3, 16, 32, 9, True), (2, 4, 32, 9, False), (16, 64, 32, 9, True)])
+def test_rgb_epilogue_matches_torch(svb, cuda, b, h, cp, c, skip):
+    """The toRGB epilogue kernel (padded channels-last conv output + bias + up-sampled skip
+    image, written NCHW) and its adjoint against the same composition in torch ops."""
+    MG = svb.materialgan
+    g = torch.Generator().manual_seed(b * h + cp)
+    yp = torch.randn(b, cp, h, h, generator=g).to(cuda).contiguous(memory_format=torch.channels_last)
+    bias = torch.randn(c, generator=g).to(cuda)
+    prev = torch.randn(b, c, h // 2, h // 2, generator=g).to(cuda) if skip else None
+    y1 = yp.clone().requires_grad_(True)
+    p1 = prev.clone().requires_grad_(True) if skip else None
+    out = MG._RgbNHWC.apply(y1, bias, p1, c)
+    assert out.is_contiguous() and out.shape == (b, c, h, h)
+    y2 = yp.clone().requires_grad_(True)
+    p2 = prev.clone().requires_grad_(True) if skip else None
+    ref = y2[:, :c] + bias.view(1, -1, 1, 1)
+    if skip:
+        ref = ref + MG._up1d(MG._up1d(p2, -1), -2)
+    gout = torch.randn(out.shape, generator=g).to(cuda)
+    (out * gout).sum().backward()
+    (ref * gout).sum().backward()
+    torch.cuda.synchronize()
+    assert rel_l2(out, ref) <= 1e-6
+    assert rel_l2(y1.grad, y2.grad) <= 1e-6
+    assert float(y1.grad[:, c:].abs().max()) == 0.0
+    if skip:
+        assert rel_l2(p1.grad, p2.grad) <= 1e-6
+
+
+@pytest.mark.gpu
 def test_gpu_generator_tf32_matches_reference_network(svb, cuda):
     """The generator as it runs by default on the GPU (channels-last maps, the TF32 tensor-core
     convolutions, the NHWC kernels) on the reference network's fixture

@@ -417,6 +417,18 @@ int svbrdf_gen_act_nhwc_bwd(const float* gout, const float* y, const float* d, c
                             const float* bias, float gain, float* gy, float* gd, float* gnoise, float* part, int b,
                             int hw, int c, void* stream);
 
+/* A style layer's epilogue fused with the next layer's input scaling, for an output whose only
+ * consumer is that layer (the generator's up-sampling layers feed only the convolution after
+ * them): out = lrelu(y d + ns noise + bias, 0.2) gain s2[b][c] is written, the unscaled map is
+ * not. The adjoint takes dL/d out and gives gy, gd, gnoise as svbrdf_gen_act_nhwc_bwd and
+ * gs2[b][c] = sum over the pixels of dL/d out x (the unscaled output), with a second scratch of
+ * svbrdf_gen_nhwc_partial_floats(b, c) floats for its column sums. */
+int svbrdf_gen_act_scale_nhwc(const float* y, const float* d, const float* noise, const float* ns, const float* bias,
+                              float gain, const float* s2, float* out, int b, int hw, int c, void* stream);
+int svbrdf_gen_act_scale_nhwc_bwd(const float* gout, const float* y, const float* d, const float* noise, const float* ns,
+                                  const float* bias, float gain, const float* s2, float* gy, float* gd, float* gs2,
+                                  float* gnoise, float* part, float* part2, int b, int hw, int c, void* stream);
+
 /* ---- MaterialGAN generator: its convolutions in TF32 on the tensor cores (the reference's
  * modulated convolutions, src/higan_models/stylegan2_generator_network.py:585-759, computed as a
  * shared-weight convolution between the modulation and demodulation kernels above) ---- */

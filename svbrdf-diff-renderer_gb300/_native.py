@@ -198,6 +198,10 @@ def _declare(L):
     L.svbrdf_gen_act_nhwc.argtypes = [P, P, P, P, P, F, P, I, I, I, P]
     L.svbrdf_gen_act_nhwc_bwd.restype = I
     L.svbrdf_gen_act_nhwc_bwd.argtypes = [P, P, P, P, P, P, F, P, P, P, P, I, I, I, P]
+    L.svbrdf_gen_act_scale_nhwc.restype = I
+    L.svbrdf_gen_act_scale_nhwc.argtypes = [P, P, P, P, P, F, P, P, I, I, I, P]
+    L.svbrdf_gen_act_scale_nhwc_bwd.restype = I
+    L.svbrdf_gen_act_scale_nhwc_bwd.argtypes = [P, P, P, P, P, P, F, P, P, P, P, P, P, P, I, I, I, P]
     L.svbrdf_selftest_wait_timeout.restype = I
     L.svbrdf_selftest_wait_timeout.argtypes = [P, S, I, P]
     L.svbrdf_envmap_render.restype = I
@@ -231,6 +235,7 @@ EXPORTS = [
     "svbrdf_gen_nhwc_partial_floats", "svbrdf_gen_upsample2_nhwc", "svbrdf_gen_upsample2_nhwc_bwd",
     "svbrdf_gen_rgb_nhwc", "svbrdf_gen_rgb_nhwc_bwd",
     "svbrdf_gen_scale_nhwc", "svbrdf_gen_scale_nhwc_bwd", "svbrdf_gen_act_nhwc", "svbrdf_gen_act_nhwc_bwd",
+    "svbrdf_gen_act_scale_nhwc", "svbrdf_gen_act_scale_nhwc_bwd",
     "svbrdf_gen_conv_tf32", "svbrdf_gen_conv_tf32_ws_bytes", "svbrdf_gen_conv_tf32_ex",
     "svbrdf_envmap_render", "svbrdf_selftest_wait_timeout",
 ]

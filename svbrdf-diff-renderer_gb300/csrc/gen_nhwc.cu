@@ -248,7 +248,8 @@ __global__ void __launch_bounds__(256) nhwc_act_fwd_kernel(const float* __restri
                                                            const float* __restrict__ noise,
                                                            const float* __restrict__ ns,
                                                            const float* __restrict__ bias, float gain,
-                                                           float* __restrict__ out, int HW, int C) {
+                                                           const float* __restrict__ s2, float* __restrict__ out,
+                                                           int HW, int C) {
   const int cv = C / VEC, n = HW * cv, b = blockIdx.y;
   const float nsv = noise ? __ldg(ns) : 0.0f;
   const float* yb = y + (long long)b * HW * C;
@@ -274,10 +275,17 @@ __global__ void __launch_bounds__(256) nhwc_act_fwd_kernel(const float* __restri
           for (int j = 0; j < VEC; ++j) dv[j] = 1.0f;
         }
         const float nz = nb ? nsv * __ldg(nb + p) : 0.0f;
+        float sv[VEC];
+        if (s2) {
+          ldv<VEC>(s2 + (long long)b * C + c * VEC, sv);
+        } else {
+#pragma unroll
+          for (int j = 0; j < VEC; ++j) sv[j] = 1.0f;
+        }
 #pragma unroll
         for (int j = 0; j < VEC; ++j) {
           const float pre = act_pre(v[u][j], dv[j], nz, bv[j]);
-          v[u][j] = (pre > 0.0f ? pre : 0.2f * pre) * gain;
+          v[u][j] = (pre > 0.0f ? pre : 0.2f * pre) * gain * sv[j];
         }
         stv<VEC>(ob + t * VEC, v[u]);
       }
@@ -289,13 +297,14 @@ __global__ void __launch_bounds__(256) nhwc_act_fwd_kernel(const float* __restri
 // gradient of pixel p is the sum of its gpre over the cv threads of its row: a shuffle
 // butterfly within the row's lanes when cv is a power of two up to 32, else through shared
 // memory.
-template <int VEC>
-__global__ void __launch_bounds__(256) nhwc_act_bwd_kernel(const float* __restrict__ gout,
+template <int VEC, bool SCALE>
+__global__ void __launch_bounds__(256, 3) nhwc_act_bwd_kernel(const float* __restrict__ gout,
                                                            const float* __restrict__ y, const float* __restrict__ d,
                                                            const float* __restrict__ noise,
                                                            const float* __restrict__ ns,
                                                            const float* __restrict__ bias, float gain,
-                                                           float* __restrict__ gy, float* __restrict__ part,
+                                                           const float* __restrict__ s2, float* __restrict__ gy,
+                                                           float* __restrict__ part, float* __restrict__ part2,
                                                            float* __restrict__ gnoise, int HW, int C, int nchunk) {
   __shared__ float red[256 * VEC];
   __shared__ float rowbuf[kU][256];
@@ -310,11 +319,12 @@ __global__ void __launch_bounds__(256) nhwc_act_bwd_kernel(const float* __restri
   const float* yb = y + (long long)b * HW * C + c * VEC;
   float* ob = gy + (long long)b * HW * C + c * VEC;
   const float* nb = noise ? noise + (long long)b * HW : nullptr;
-  float dv[VEC], bv[VEC], acc[VEC];
+  float dv[VEC], bv[VEC], sv[VEC], acc[VEC], acc2[VEC];
 #pragma unroll
-  for (int j = 0; j < VEC; ++j) acc[j] = 0.0f, dv[j] = 1.0f, bv[j] = 0.0f;
+  for (int j = 0; j < VEC; ++j) acc[j] = 0.0f, acc2[j] = 0.0f, dv[j] = 1.0f, bv[j] = 0.0f, sv[j] = 1.0f;
   if (r < rows) {
     if (d) ldv<VEC>(d + (long long)b * C + c * VEC, dv);
+    if (SCALE) ldv<VEC>(s2 + (long long)b * C + c * VEC, sv);
     ldv<VEC>(bias + c * VEC, bv);
   }
   // every thread runs the same number of steps (the shuffles and barriers are uniform)
@@ -338,7 +348,11 @@ __global__ void __launch_bounds__(256) nhwc_act_bwd_kernel(const float* __restri
         float o[VEC];
 #pragma unroll
         for (int j = 0; j < VEC; ++j) {
-          const float gp = go[u][j] * gain * (act_pre(yv[u][j], dv[j], nz[u], bv[j]) > 0.0f ? 1.0f : 0.2f);
+          const float pre = act_pre(yv[u][j], dv[j], nz[u], bv[j]);
+          const float slope = pre > 0.0f ? 1.0f : 0.2f;
+          // with s2 the output was scaled by the next layer's style: gout is dL/d(out s2)
+          if (SCALE) acc2[j] = fmaf(go[u][j], pre * slope * gain, acc2[j]);
+          const float gp = (SCALE ? go[u][j] * sv[j] : go[u][j]) * gain * slope;
           acc[j] = fmaf(gp, yv[u][j], acc[j]);
           rs[u] += gp;
           o[j] = gp * dv[j];
@@ -375,6 +389,10 @@ __global__ void __launch_bounds__(256) nhwc_act_bwd_kernel(const float* __restri
     }
   }
   if (part) column_partials<VEC>(acc, red, cv, rows, part, C, nchunk);
+  if (SCALE && part2) {
+    __syncthreads();  // the first column pass has read red
+    column_partials<VEC>(acc2, red, cv, rows, part2, C, nchunk);
+  }
 }
 
 // out[b][c] = sum over chunks k (in order) of part[b][k][c].
@@ -535,9 +553,28 @@ int svbrdf_gen_act_nhwc(const float* y, const float* d, const float* noise, cons
   const int cv = v4 ? c / 4 : c;
   cudaStream_t st = (cudaStream_t)stream;
   if (v4)
-    gen_nhwc::nhwc_act_fwd_kernel<4><<<entry_grid(hw, cv, b), 256, 0, st>>>(y, d, noise, ns, bias, gain, out, hw, c);
+    gen_nhwc::nhwc_act_fwd_kernel<4><<<entry_grid(hw, cv, b), 256, 0, st>>>(y, d, noise, ns, bias, gain, nullptr, out,
+                                                                         hw, c);
   else
-    gen_nhwc::nhwc_act_fwd_kernel<1><<<entry_grid(hw, cv, b), 256, 0, st>>>(y, d, noise, ns, bias, gain, out, hw, c);
+    gen_nhwc::nhwc_act_fwd_kernel<1><<<entry_grid(hw, cv, b), 256, 0, st>>>(y, d, noise, ns, bias, gain, nullptr, out,
+                                                                         hw, c);
+  return check_launch("nhwc_act_fwd_kernel");
+}
+
+int svbrdf_gen_act_scale_nhwc(const float* y, const float* d, const float* noise, const float* ns, const float* bias,
+                              float gain, const float* s2, float* out, int b, int hw, int c, void* stream) {
+  if (!y || !bias || !s2 || !out || (noise && !ns) || b < 1 || b > 65535 || hw < 1 || c < 1)
+    return fail(SVBRDF_ERR_INVALID, "act_scale_nhwc: bad arguments");
+  if ((long long)hw * c > (1LL << 30)) return fail(SVBRDF_ERR_UNSUPPORTED, "act_scale_nhwc: too large");
+  const bool v4 = c % 4 == 0 && a16(y) && a16(d) && a16(bias) && a16(s2) && a16(out);
+  const int cv = v4 ? c / 4 : c;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (v4)
+    gen_nhwc::nhwc_act_fwd_kernel<4><<<entry_grid(hw, cv, b), 256, 0, st>>>(y, d, noise, ns, bias, gain, s2, out, hw,
+                                                                         c);
+  else
+    gen_nhwc::nhwc_act_fwd_kernel<1><<<entry_grid(hw, cv, b), 256, 0, st>>>(y, d, noise, ns, bias, gain, s2, out, hw,
+                                                                         c);
   return check_launch("nhwc_act_fwd_kernel");
 }
 
@@ -556,15 +593,50 @@ int svbrdf_gen_act_nhwc_bwd(const float* gout, const float* y, const float* d, c
   dim3 grid((unsigned)nc, (unsigned)b);
   float* pp = gd ? part : nullptr;
   if (v4)
-    gen_nhwc::nhwc_act_bwd_kernel<4><<<grid, 256, 0, st>>>(gout, y, d, noise, ns, bias, gain, gy, pp, gnoise, hw, c,
-                                                           nc);
+    gen_nhwc::nhwc_act_bwd_kernel<4, false><<<grid, 256, 0, st>>>(gout, y, d, noise, ns, bias, gain, nullptr, gy, pp, nullptr,
+                                                           gnoise, hw, c, nc);
   else
-    gen_nhwc::nhwc_act_bwd_kernel<1><<<grid, 256, 0, st>>>(gout, y, d, noise, ns, bias, gain, gy, pp, gnoise, hw, c,
-                                                           nc);
+    gen_nhwc::nhwc_act_bwd_kernel<1, false><<<grid, 256, 0, st>>>(gout, y, d, noise, ns, bias, gain, nullptr, gy, pp, nullptr,
+                                                           gnoise, hw, c, nc);
   int rc = check_launch("nhwc_act_bwd_kernel");
   if (rc || !gd) return rc;
   gen_nhwc::nhwc_colsum_kernel<<<(unsigned)((b * c + 255) / 256), 256, 0, st>>>(part, gd, b, c, nc);
   return check_launch("nhwc_colsum_kernel");
+}
+
+int svbrdf_gen_act_scale_nhwc_bwd(const float* gout, const float* y, const float* d, const float* noise, const float* ns,
+                                  const float* bias, float gain, const float* s2, float* gy, float* gd, float* gs2,
+                                  float* gnoise, float* part, float* part2, int b, int hw, int c, void* stream) {
+  if (!gout || !y || !bias || !s2 || !gy || (noise && !ns) || (gnoise && !noise) || (gd && !part) ||
+      (gs2 && !part2) || b < 1 || b > 65535 || hw < 1 || c < 1)
+    return fail(SVBRDF_ERR_INVALID, "act_scale_nhwc_bwd: bad arguments");
+  if ((long long)hw * c > (1LL << 30)) return fail(SVBRDF_ERR_UNSUPPORTED, "act_scale_nhwc_bwd: too large");
+  const bool v4 = c % 4 == 0 && a16(gout) && a16(y) && a16(d) && a16(bias) && a16(s2) && a16(gy);
+  const int cv = v4 ? c / 4 : c;
+  if (cv > 256) return fail(SVBRDF_ERR_UNSUPPORTED, "act_scale_nhwc_bwd: %d channels are more than one block's row", c);
+  const int nc = nchunks(hw, 256 / cv);
+  cudaStream_t st = (cudaStream_t)stream;
+  dim3 grid((unsigned)nc, (unsigned)b);
+  float* pp = gd ? part : nullptr;
+  float* pp2 = gs2 ? part2 : nullptr;
+  if (v4)
+    gen_nhwc::nhwc_act_bwd_kernel<4, true><<<grid, 256, 0, st>>>(gout, y, d, noise, ns, bias, gain, s2, gy, pp, pp2, gnoise,
+                                                           hw, c, nc);
+  else
+    gen_nhwc::nhwc_act_bwd_kernel<1, true><<<grid, 256, 0, st>>>(gout, y, d, noise, ns, bias, gain, s2, gy, pp, pp2, gnoise,
+                                                           hw, c, nc);
+  int rc = check_launch("nhwc_act_bwd_kernel");
+  if (rc) return rc;
+  if (gd) {
+    gen_nhwc::nhwc_colsum_kernel<<<(unsigned)((b * c + 255) / 256), 256, 0, st>>>(part, gd, b, c, nc);
+    rc = check_launch("nhwc_colsum_kernel");
+    if (rc) return rc;
+  }
+  if (gs2) {
+    gen_nhwc::nhwc_colsum_kernel<<<(unsigned)((b * c + 255) / 256), 256, 0, st>>>(part2, gs2, b, c, nc);
+    rc = check_launch("nhwc_colsum_kernel");
+  }
+  return rc;
 }
 
 

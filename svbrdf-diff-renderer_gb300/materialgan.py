@@ -285,6 +285,51 @@ class _ConvTF32(torch.autograd.Function):
         return gx, None, None, None, None, None, None
 
 
+class _ActScaleNHWC(torch.autograd.Function):
+    """_ActNHWC followed by the next layer's input scaling (x s2[b, c]) in one pass each way
+    (svbrdf_gen_act_scale_nhwc[_bwd]), for an output whose only consumer is that layer: the
+    unscaled activation is never stored, the backward recomputes it from y."""
+
+    @staticmethod
+    def forward(ctx, y, d, noise, ns, bias, gain, s2):
+        from . import _native as N
+
+        y, d, bias, s2 = _cl(y), d.contiguous(), bias.contiguous(), s2.contiguous()
+        noise = noise.contiguous() if noise is not None else None
+        b, c, h, w = y.shape
+        out = torch.empty_like(y)
+        N.check(N.lib().svbrdf_gen_act_scale_nhwc(y.data_ptr(), d.data_ptr(), N.ptr(noise),
+                                                  ns.data_ptr() if noise is not None else None, bias.data_ptr(), gain,
+                                                  s2.data_ptr(), out.data_ptr(), b, h * w, c,
+                                                  N.stream_handle(y.device)))
+        ctx.save_for_backward(y, d, noise, ns, bias, s2)
+        ctx.gain = gain
+        return out
+
+    @staticmethod
+    def backward(ctx, g):
+        from . import _native as N
+
+        y, d, noise, ns, bias, s2 = ctx.saved_tensors
+        b, c, h, w = y.shape
+        L = N.lib()
+        g = _cl(g)
+        gy = torch.empty_like(y)
+        gd = torch.empty(b, c, device=y.device, dtype=torch.float32)
+        gs2 = torch.empty(b, c, device=y.device, dtype=torch.float32)
+        want_noise = noise is not None and ctx.needs_input_grad[2]
+        gn = torch.empty_like(noise) if want_noise else None
+        nparts = L.svbrdf_gen_nhwc_partial_floats(b, c)
+        part = torch.empty(nparts, device=y.device, dtype=torch.float32)
+        part2 = torch.empty(nparts, device=y.device, dtype=torch.float32)
+        N.check(L.svbrdf_gen_act_scale_nhwc_bwd(g.data_ptr(), y.data_ptr(), d.data_ptr(), N.ptr(noise),
+                                                ns.data_ptr() if noise is not None else None, bias.data_ptr(), ctx.gain,
+                                                s2.data_ptr(), gy.data_ptr(), gd.data_ptr(), gs2.data_ptr(), N.ptr(gn),
+                                                part.data_ptr(), part2.data_ptr(), b, h * w, c,
+                                                N.stream_handle(y.device)))
+        return gy, gd, gn, None, None, None, gs2
+
+
 class _RgbNHWC(torch.autograd.Function):
     """The toRGB epilogue (svbrdf_gen_rgb_nhwc[_bwd]): the 1x1 convolution's padded
     channels-last output yp [B, cp, H, W] plus the bias plus the up-sampled previous image
@@ -503,18 +548,24 @@ class _ModConv(torch.nn.Module):
             self._tf32_key = key
         return self._w_fwd, self._w_dg
 
-    def parts(self, x, w, keep_pad=False):
+    def parts(self, x, w, keep_pad=False, sd=None, prescaled=False):
         """The shared-weight convolution of the style-scaled input, and the demodulation
         d [B, cout] (None without demodulation) still to be applied to its output. With
-        ``keep_pad`` the TF32 path returns its output with the channels padded to 32."""
-        s = self.affine(w)  # [B, cin]
+        ``keep_pad`` the TF32 path returns its output with the channels padded to 32; ``sd``
+        is this layer's (style, demodulation) pair when the generator computed them for all
+        layers at once (StyleGAN2Generator._styles); ``prescaled`` says that the
+        channels-last input already carries this layer's style scaling (_ActScaleNHWC)."""
+        s = self.affine(w) if sd is None else sd[0]  # [B, cin]
         wsc, w2t = self._scaled_weight()
         # an up-sampling layer convolves the up-sampled map with its one-sample halo, unpadded
         # (_upsample2_halo): the reference's transposed convolution + filter on the border too
         pad = 0 if self.up else self.k // 2
         if _use_kernels(x) and _is_nhwc(x):
             # channels-last: the layout of the TF32 tensor-core convolutions (and of cuDNN's)
-            x = _UpsampleNHWC.apply(x, s, 1) if self.up else _ScaleNHWC.apply(x, s)
+            if self.up:
+                x = _UpsampleNHWC.apply(x, s, 1)
+            elif not prescaled:
+                x = _ScaleNHWC.apply(x, s)
             if self._tf32_ok(x):
                 w_fwd, w_dg = self._tf32_weights(wsc)
                 y = _ConvTF32.apply(x, w_fwd, w_dg, self.weight.shape[0], self.k, pad, keep_pad)
@@ -527,7 +578,7 @@ class _ModConv(torch.nn.Module):
             y = Fn.conv2d(x, wsc, padding=pad)
         d = None
         if self.demod:
-            d = torch.rsqrt(s.pow(2) @ w2t + 1e-8)  # [B, cout]
+            d = torch.rsqrt(s.pow(2) @ w2t + 1e-8) if sd is None else sd[1]  # [B, cout]
         return y, d
 
     def _scaled_weight(self):
@@ -554,10 +605,18 @@ class _StyleLayer(torch.nn.Module):
         self.noise_strength = torch.nn.Parameter(torch.zeros(()))
         self.bias = torch.nn.Parameter(torch.zeros(cout))
 
-    def forward(self, x, w, noise):
-        if _use_kernels(x) and not (self.bias.requires_grad or self.noise_strength.requires_grad) and (
-                noise is None or (noise.shape[0] == x.shape[0] and noise.shape[1] == 1)):
-            y, d = self.conv.parts(x, w)
+    def kernel_ok(self, x, noise) -> bool:
+        """Whether forward takes the CUDA-kernel path for this input and noise map."""
+        return _use_kernels(x) and not (self.bias.requires_grad or self.noise_strength.requires_grad) and (
+            noise is None or (noise.shape[0] == x.shape[0] and noise.shape[1] == 1))
+
+    def forward(self, x, w, noise, sd=None, s_next=None, prescaled=False):
+        """``s_next``: the next layer's style, to scale this layer's output by in the same pass
+        (channels-last kernel path only; the caller then passes ``prescaled`` to that layer)."""
+        if self.kernel_ok(x, noise):
+            y, d = self.conv.parts(x, w, sd=sd, prescaled=prescaled)
+            if s_next is not None and _is_nhwc(y):
+                return _ActScaleNHWC.apply(y, d, noise, self.noise_strength, self.bias, LRELU_GAIN, s_next)
             act = _ActNHWC if _is_nhwc(y) else _ActCuda
             return act.apply(y, d, noise, self.noise_strength, self.bias, LRELU_GAIN)
         y = self.conv(x, w)
@@ -572,7 +631,7 @@ class _ToRGB(torch.nn.Module):
         self.conv = _ModConv(cin, cout, 1, w_dim, g, demod=False)
         self.bias = torch.nn.Parameter(torch.zeros(cout))
 
-    def forward(self, x, w, skip):
+    def forward(self, x, w, skip, sd=None):
         cout = self.bias.shape[0]
         if (_use_kernels(x) and _is_nhwc(x) and not self.bias.requires_grad and self.conv._tf32_ok(x) and
                 x.shape[-1] % 2 == 0 and x.shape[-2] % 2 == 0 and
@@ -580,7 +639,7 @@ class _ToRGB(torch.nn.Module):
                                   tuple(skip.shape) == (x.shape[0], cout, x.shape[-2] // 2, x.shape[-1] // 2)))):
             # the TF32 convolution's padded channels-last output, bias and the up-sampled skip
             # image in one pass that writes the image in NCHW
-            yp, _ = self.conv.parts(x, w, keep_pad=True)
+            yp, _ = self.conv.parts(x, w, keep_pad=True, sd=sd)
             return _RgbNHWC.apply(_cl(yp), self.bias, skip, cout)
         y = self.conv(x, w) + self.bias.view(1, -1, 1, 1)
         return y if skip is None else y + _upsample2(skip)
@@ -693,6 +752,49 @@ class StyleGAN2Generator(torch.nn.Module):
             out.append(n.to(device))
         return out
 
+    def _layers(self):
+        """Every modulated convolution in the order synthesis runs them, with its W+ row."""
+        out = [(self.conv4.conv, 0), (self.rgb4.conv, 1)]
+        for i, (up, conv, rgb) in enumerate(zip(self.ups, self.convs, self.rgbs)):
+            out += [(up.conv, 1 + 2 * i), (conv.conv, 2 + 2 * i), (rgb.conv, 3 + 2 * i)]
+        return out
+
+    def _styles(self, wp: torch.Tensor):
+        """The styles s = affine(w) and demodulations d = rsqrt(s^2 sum_taps (scale w)^2 + 1e-8)
+        of every layer, for frozen weights: layers of one shape (input and output channels,
+        demodulated or not) share one batched product each (torch.baddbmm / bmm), in place of
+        two small GEMMs and a few elementwise ops per layer. Returns {layer: (s, d)}; {} when
+        a weight is trainable (each layer then computes its own, inside autograd)."""
+        layers = self._layers()
+        if any(m.weight.requires_grad or m.affine.weight.requires_grad or m.affine.bias.requires_grad
+               for m, _ in layers):
+            return {}
+        key = tuple((m.weight.data_ptr(), m.weight._version, m.affine.weight._version, m.affine.bias._version)
+                    for m, _ in layers) + (wp.device, wp.dtype)
+        if getattr(self, "_style_key", None) != key:
+            groups = {}
+            for m, widx in layers:
+                groups.setdefault((m.weight.shape[1], m.weight.shape[0], m.demod), []).append((m, widx))
+            packed = []
+            with torch.no_grad():
+                for (cin, cout, demod), ms in groups.items():
+                    a = torch.stack([(m.affine.weight * m.affine.scale).t() for m, _ in ms]).to(wp.device, wp.dtype)
+                    b = torch.stack([(m.affine.bias * m.affine.lr_mul) for m, _ in ms]).unsqueeze(1).to(wp.device, wp.dtype)
+                    w2 = (torch.stack([m._scaled_weight()[1] for m, _ in ms]).to(wp.device, wp.dtype).contiguous()
+                          if demod else None)
+                    idx = torch.tensor([wi for _, wi in ms], device=wp.device)
+                    packed.append(([m for m, _ in ms], idx, a.contiguous(), b.contiguous(), w2))
+            self._style_packed, self._style_key = packed, key
+        sd = {}
+        for mods, idx, a, b, w2 in self._style_packed:
+            st = torch.baddbmm(b, wp.index_select(1, idx).transpose(0, 1), a)  # [L, B, cin]
+            dm = torch.rsqrt(torch.bmm(st * st, w2) + 1e-8) if w2 is not None else None  # [L, B, cout]
+            ss = torch.unbind(st, 0)
+            ds = torch.unbind(dm, 0) if dm is not None else [None] * len(mods)
+            for m, si, di in zip(mods, ss, ds):
+                sd[m] = (si, di)
+        return sd
+
     def synthesis(self, wp: torch.Tensor, noises: Optional[List[torch.Tensor]] = None) -> torch.Tensor:
         """W+ [B, num_ws, w_dim] -> [B, out_channels, res, res]."""
         b = wp.shape[0]
@@ -700,12 +802,23 @@ class StyleGAN2Generator(torch.nn.Module):
         x = self.const.expand(b, -1, -1, -1)
         if self.channels_last and _use_kernels(x):
             x = _cl(x)
-        x = self.conv4(x, wp[:, 0], noises[0])
-        img = self.rgb4(x, wp[:, 1], None)
+        # all layers' styles and demodulations at once on the GPU path with frozen weights
+        sd = self._styles(wp) if _use_kernels(x) else {}
+        x = self.conv4(x, wp[:, 0], noises[0], sd.get(self.conv4.conv))
+        img = self.rgb4(x, wp[:, 1], None, sd.get(self.rgb4.conv))
         for i, (up, conv, rgb) in enumerate(zip(self.ups, self.convs, self.rgbs)):
-            x = up(x, wp[:, 1 + 2 * i], noises[1 + 2 * i])
-            x = conv(x, wp[:, 2 + 2 * i], noises[2 + 2 * i])
-            img = rgb(x, wp[:, 3 + 2 * i], img)
+            n_up, n_conv = noises[1 + 2 * i], noises[2 + 2 * i]
+            # an up-sampling layer's output feeds only the next convolution: on the
+            # channels-last kernel path its epilogue also applies that layer's style scaling
+            fuse = (bool(sd) and _is_nhwc(x) and up.kernel_ok(x, n_up) and conv.kernel_ok(x, n_conv)
+                    and conv.conv in sd)
+            if fuse:
+                x = up(x, wp[:, 1 + 2 * i], n_up, sd.get(up.conv), s_next=sd[conv.conv][0])
+                x = conv(x, wp[:, 2 + 2 * i], n_conv, sd.get(conv.conv), prescaled=True)
+            else:
+                x = up(x, wp[:, 1 + 2 * i], n_up, sd.get(up.conv))
+                x = conv(x, wp[:, 2 + 2 * i], n_conv, sd.get(conv.conv))
+            img = rgb(x, wp[:, 3 + 2 * i], img, sd.get(rgb.conv))
         return img
 
 

@@ -444,6 +444,39 @@ def test_conv_tf32_split_k_matches_unsplit(svb, cuda, b, h, cin, cout, k, pad):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("b,h,c,noise", [(4, 16, 128, True), (2, 8, 512, False), (16, 64, 256, True), (3, 8, 6, True)])
+def test_act_scale_matches_composition(svb, cuda, b, h, c, noise):
+    """The style layer's epilogue fused with the next layer's input scaling (_ActScaleNHWC)
+    against _ActNHWC followed by the scaling, forward and all four gradients (y, d, noise,
+    the next style)."""
+    MG = svb.materialgan
+    g = torch.Generator().manual_seed(b * c + h)
+    y = torch.randn(b, c, h, h, generator=g).to(cuda).contiguous(memory_format=torch.channels_last)
+    d = (torch.rand(b, c, generator=g) + 0.5).to(cuda)
+    nz = torch.randn(b, 1, h, h, generator=g).to(cuda) if noise else None
+    ns = torch.tensor(0.3, device=cuda)
+    bias = torch.randn(c, generator=g).to(cuda)
+    s2 = (torch.randn(b, c, generator=g) * 0.5 + 1.0).to(cuda)
+    gout = torch.randn(b, c, h, h, generator=g).to(cuda).contiguous(memory_format=torch.channels_last)
+
+    def run(fused):
+        yy, dd, s22 = y.clone().requires_grad_(True), d.clone().requires_grad_(True), s2.clone().requires_grad_(True)
+        nn_ = nz.clone().requires_grad_(True) if noise else None
+        if fused:
+            out = MG._ActScaleNHWC.apply(yy, dd, nn_, ns, bias, MG.LRELU_GAIN, s22)
+        else:
+            out = MG._ActNHWC.apply(yy, dd, nn_, ns, bias, MG.LRELU_GAIN) * s22[:, :, None, None]
+        (out * gout).sum().backward()
+        return out.detach(), yy.grad, dd.grad, s22.grad, (nn_.grad if noise else None)
+
+    a, r = run(True), run(False)
+    torch.cuda.synchronize()
+    for x1, x2 in zip(a, r):
+        if x1 is not None:
+            assert rel_l2(x1, x2) <= 1e-5
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("b,h,cp,c,skip", [(3, 16, 32, 9, True), (2, 4, 32, 9, False), (16, 64, 32, 9, True)])
 def test_rgb_epilogue_matches_torch(svb, cuda, b, h, cp, c, skip):
     """The toRGB epilogue kernel (padded channels-last conv output + bias + up-sampled skip

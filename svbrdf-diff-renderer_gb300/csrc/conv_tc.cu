@@ -9,11 +9,13 @@
 // The kernel is persistent: one CTA per SM walks the tiles i, i + grid, ... For each 64-channel
 // chunk the producer warp TMA-loads the tile's input patch once, with its one-pixel halo
 // (out-of-image pixels read the TMA zero fill, which is exactly the padding), and the 9 taps'
-// BN x 64 weight slices, 128-byte swizzled, into two rings of shared-memory stages that run on
-// across tiles; the 9 taps read the one patch through shifted descriptors (the halo form
+// BN x 64 weight slices, all 128-byte swizzled, into two rings of shared-memory stages that run
+// on across tiles; the 9 taps read the one patch through shifted descriptors (the halo form
 // below). One thread issues tcgen05.mma (kind::f16, BF16 in, FP32 accumulate) into MT
 // 128 x BN TMEM accumulators, double-buffered; tcgen05.commit frees each stage and signals the
-// epilogue per tile. Eight epilogue warps (two per TMEM lane quadrant, each with half the
+// epilogue per tile. A commit group of MMAs costs at least about 560 cycles on this part (an
+// M=128, N=64, K=16 MMA issues every 48 cycles, N=128 every 64), so where BN <= 128 a weight
+// stage holds a whole kernel row (3 taps, 24 MMAs per commit) instead of one tap. Eight epilogue warps (two per TMEM lane quadrant, each with half the
 // columns) read TMEM with tcgen05.ld, apply the epilogue (bias + ReLU, or a ReLU-mask multiply
 // for the backward pass) and store BF16 NHWC while the MMAs of the next tile run.
 // The data gradient of a convolution is the same kernel run on dL/dY with the weights
@@ -98,31 +100,32 @@ __device__ __forceinline__ void epilogue_store32(const uint32_t (&r)[32], const 
 }
 
 // ---------------------------------------------------------------- halo form
-// The same convolution with each input patch loaded once per 64-channel chunk, halo included,
-// and shared by the 9 taps. A tile is MT stacked 16-row x 8-column patches of one image; its
-// input is the (16 MT + 2) x 10 halo patch. Shared memory holds that patch K-major without
-// swizzle: for each 8-channel group g, the halo pixels (row-major, 10 per row) at 16 bytes each,
-// groups kHaloKg bytes apart. The 128 accumulator rows of M-tile mt are the patch's 16 rows of
-// 8 pixels: row group r (8 pixels) of tap (ky, kx) starts at halo pixel (16 mt + r + ky) x 10 +
-// kx, so a tap is the same descriptor shifted by (10 ky + kx) x 16 bytes, with 8-row groups 160
-// bytes apart (SBO) and K-adjacent core matrices one channel group apart (LBO). The weight
-// slices [BN][64] of the 9 taps stream through their own ring (128-byte swizzle, as above).
-// Per chunk the tile loads (16 MT + 2) x 10 x 128 bytes of input instead of 9 x MT x 16 KB.
+// Each input patch is loaded once per 64-channel chunk, halo included, and shared by the 9
+// taps. A tile is MT stacked 16-row x 8-column patches of one image; its input is the
+// (16 MT + 2) x 10 halo patch, one TMA box of 128-byte pixel rows (64 BF16 channels), 128-byte
+// swizzled, pixels row-major (10 per patch row) from a 1024-byte boundary. The 128 accumulator
+// rows of M-tile mt are the patch's 16 rows of 8 pixels: 8-row group r of tap (ky, kx) starts at
+// patch pixel (16 mt + r + ky) x 10 + kx, so a tap is the patch's descriptor moved by
+// (10 ky + kx) pixels, with 8-row groups 10 pixels (1280 bytes) apart (SBO). The weight slices
+// [BN][64] stream through their own ring, TPS taps per stage. Per chunk the tile loads
+// (16 MT + 2) x 10 x 128 bytes of input instead of 9 x MT x 16 KB.
 template <int MT>
 struct Halo {
   static constexpr int kRows = 16 * MT + 2, kCols = 10;
-  static constexpr int kKg = ((kRows * kCols * 16 + 127) / 128) * 128;  // one channel group, 128-byte aligned
-  static constexpr int kABytes = 8 * kKg;                               // one 64-channel chunk
+  static constexpr int kABytes = ((kRows * kCols * 128 + 1023) / 1024) * 1024;  // one 64-channel chunk
 };
 
-template <int BN, int MT, int AST, int BST, int EPI>
+template <int BN, int MT, int AST, int BST, int EPI, int TPS>
 __global__ void __launch_bounds__(kThreads, 1)
 conv3x3_halo_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_constant__ CUtensorMap tmap_w,
                     const float* __restrict__ bias, const __nv_bfloat16* __restrict__ mask,
                     const __nv_bfloat16* __restrict__ addend, __nv_bfloat16* __restrict__ y, int N, int H, int W,
                     int Cin, int Cout, int* err) {
   using HP = Halo<MT>;
-  constexpr int B_BYTES = BN * BK * 2;
+  constexpr int B_BYTES = BN * BK * 2;  // one tap's weight slice
+  constexpr int S_BYTES = TPS * B_BYTES;  // one weight stage
+  constexpr int GROUPS = 9 / TPS;
+  static_assert(TPS == 1 || TPS == 3, "a weight stage holds one tap or one kernel row");
   constexpr uint32_t ACC_COLS = MT * BN;
   constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;
   static_assert(TMEM_COLS >= 32 && TMEM_COLS <= 512 && (TMEM_COLS & (TMEM_COLS - 1)) == 0, "TMEM columns");
@@ -133,7 +136,7 @@ conv3x3_halo_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_con
   __shared__ uint32_t tmem_slot;
 
   const uint32_t bbase = (smem_u32(dsmem) + 1023u) & ~1023u;  // weight ring, then the halo ring
-  const uint32_t abase = bbase + (uint32_t)(BST * B_BYTES);
+  const uint32_t abase = bbase + (uint32_t)(BST * S_BYTES);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int tiles_x = W / 8, tiles_y = (H + 16 * MT - 1) / (16 * MT), tiles_n = Cout / BN;
   const int n_tiles = N * tiles_y * tiles_x * tiles_n;
@@ -189,21 +192,19 @@ conv3x3_halo_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_con
             break;
           }
           const uint32_t fa = smem_u32(&afull[sa]);
-          mbar_expect_tx(fa, (uint32_t)(8 * HP::kRows * HP::kCols * 16));
-#pragma unroll 1
-          for (int g = 0; g < 8; ++g)
-            tma_4d(abase + (uint32_t)(sa * HP::kABytes + g * HP::kKg), &tmap_x, cc * BK + 8 * g, x0 - 1, y0 - 1, img,
-                   fa);
+          mbar_expect_tx(fa, (uint32_t)(HP::kRows * HP::kCols * 128));
+          tma_4d(abase + (uint32_t)(sa * HP::kABytes), &tmap_x, cc * BK, x0 - 1, y0 - 1, img, fa);
           ++qa;
-          for (int tap = 0; tap < 9; ++tap) {
+          for (int grp = 0; grp < GROUPS; ++grp) {
             const int sb = qb % BST;
             if (qb >= BST && !mbar_wait(smem_u32(&bempty[sb]), ((uint32_t)(qb / BST) & 1u) ^ 1u, err, kErrTma)) {
               bad = true;
               break;
             }
             const uint32_t fb = smem_u32(&bfull[sb]);
-            mbar_expect_tx(fb, (uint32_t)B_BYTES);
-            tma_2d(bbase + (uint32_t)(sb * B_BYTES), &tmap_w, tap * Cin + cc * BK, n0, fb);
+            mbar_expect_tx(fb, (uint32_t)S_BYTES);
+            for (int u = 0; u < TPS; ++u)
+              tma_2d(bbase + (uint32_t)(sb * S_BYTES + u * B_BYTES), &tmap_w, (grp * TPS + u) * Cin + cc * BK, n0, fb);
             ++qb;
           }
         }
@@ -240,23 +241,27 @@ conv3x3_halo_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_con
             break;
           }
           const uint32_t achunk = abase + (uint32_t)(sa * HP::kABytes);
-          for (int tap = 0; tap < 9; ++tap) {
+          for (int grp = 0; grp < GROUPS; ++grp) {
             const int sb = qb % BST;
             if (!mbar_wait(smem_u32(&bfull[sb]), (uint32_t)(qb / BST) & 1u, err, kErrMma)) {
               bad = true;
               break;
             }
             fence_after();
-            const uint32_t atap = achunk + (uint32_t)(((tap / 3) * HP::kCols + tap % 3) * 16);
-            const uint32_t bs = bbase + (uint32_t)(sb * B_BYTES);
 #pragma unroll
-            for (int k = 0; k < BK / 16; ++k) {  // 16 channels = two channel groups per MMA
+            for (int u = 0; u < TPS; ++u) {
+              const int tap = grp * TPS + u;
+              const uint32_t atap = achunk + (uint32_t)(((tap / 3) * HP::kCols + tap % 3) * 128);
+              const uint32_t bs = bbase + (uint32_t)(sb * S_BYTES + u * B_BYTES);
 #pragma unroll
-              for (int mt = 0; mt < MT; ++mt)
-                mma_bf16(acc + (uint32_t)(mt * BN),
-                         noswz_desc(atap + (uint32_t)(2 * k * HP::kKg + mt * 16 * HP::kCols * 16), (uint32_t)HP::kKg,
-                                    (uint32_t)(HP::kCols * 16)),
-                         sw128_desc(bs + 32u * k), idesc, (cc > 0 || tap > 0 || k > 0) ? 1u : 0u);
+              for (int k = 0; k < BK / 16; ++k) {  // 16 channels (32 bytes) per MMA
+#pragma unroll
+                for (int mt = 0; mt < MT; ++mt)
+                  mma_bf16(acc + (uint32_t)(mt * BN),
+                           sw128_desc_sbo(atap + (uint32_t)(mt * 16 * HP::kCols * 128 + 32 * k),
+                                          (uint32_t)(HP::kCols * 128)),
+                           sw128_desc(bs + 32u * k), idesc, (cc > 0 || tap > 0 || k > 0) ? 1u : 0u);
+              }
             }
             mma_commit(smem_u32(&bempty[sb]));
             ++qb;
@@ -330,22 +335,28 @@ int get_tensor_map_encoder(PFN_cuTensorMapEncodeTiled_v12000* out) {
 
 constexpr size_t kStageBudget = 216 * 1024;  // ring bytes per CTA (one CTA per SM)
 
-// Weight-ring depth: as many slices as fit beside two input slots, up to 16 (a 64-channel
-// tile's 9 taps then stream a whole tile ahead).
+// Taps per weight stage: a kernel row where the MMAs are narrow (BN <= 128), else one tap.
+template <int BN>
+constexpr int halo_tps() {
+  return BN <= 128 ? 3 : 1;
+}
+// Weight-ring depth: as many stages as fit beside two input slots, up to 16 taps in flight.
 template <int BN, int MT>
 constexpr int halo_bstages() {
-  return (int)((kStageBudget - 2 * (size_t)Halo<MT>::kABytes) / (size_t)(BN * BK * 2)) < 16
-             ? (int)((kStageBudget - 2 * (size_t)Halo<MT>::kABytes) / (size_t)(BN * BK * 2))
-             : 16;
+  constexpr size_t stage = (size_t)halo_tps<BN>() * BN * BK * 2;
+  constexpr int fit = (int)((kStageBudget - 2 * (size_t)Halo<MT>::kABytes) / stage);
+  constexpr int cap = 16 / halo_tps<BN>();
+  return fit < cap ? fit : cap;
 }
 
 template <int BN, int MT, int EPI>
 static int launch_halo(const CUtensorMap& mx, const CUtensorMap& mw, const float* bias, const void* mask,
                        const void* addend, void* y, int n, int h, int w, int cin, int cout, int* err, cudaStream_t st) {
+  constexpr int TPS = halo_tps<BN>();
   constexpr int BST = halo_bstages<BN, MT>();
-  static_assert(BST >= 3, "weight ring too shallow");
-  auto kern = conv3x3_halo_kernel<BN, MT, 2, BST, EPI>;
-  const size_t smem = (size_t)BST * BN * BK * 2 + 2 * (size_t)Halo<MT>::kABytes + 1024;
+  static_assert(BST >= 2 && BST * TPS >= 5, "weight ring too shallow");
+  auto kern = conv3x3_halo_kernel<BN, MT, 2, BST, EPI, TPS>;
+  const size_t smem = (size_t)BST * TPS * BN * BK * 2 + 2 * (size_t)Halo<MT>::kABytes + 1024;
   static std::atomic<bool> attr[64];
   static std::atomic<int> sms[64];
   int dev = 0;
@@ -422,17 +433,17 @@ extern "C" int svbrdf_conv3x3_bf16_ex(const void* x, const void* weight, const f
   }
   cudaStream_t st = (cudaStream_t)stream;
   {
-    // the (16 MT + 2) x 10 input patch of each 64-channel chunk, loaded once: 8 channels (16
-    // bytes) per pixel per channel group, no swizzle; two stacked patches per tile where the map
-    // has 32+ rows and Cout fits two double-buffered pairs of accumulators in TMEM
+    // the (16 MT + 2) x 10 input patch of each 64-channel chunk, loaded once: one 128-byte
+    // swizzled row per pixel; two stacked patches per tile where the map has 32+ rows and Cout
+    // fits two double-buffered pairs of accumulators in TMEM
     const int mt = (bn <= 128 && h >= 32) ? 2 : 1;
     CUtensorMap mh;
     const cuuint64_t dims[4] = {(cuuint64_t)cin, (cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)n};
     const cuuint64_t strides[3] = {(cuuint64_t)cin * 2, (cuuint64_t)w * cin * 2, (cuuint64_t)h * w * cin * 2};
-    const cuuint32_t box[4] = {8u, 10u, (cuuint32_t)(16 * mt + 2), 1u};
+    const cuuint32_t box[4] = {(cuuint32_t)BK, 10u, (cuuint32_t)(16 * mt + 2), 1u};
     const cuuint32_t es[4] = {1, 1, 1, 1};
     const CUresult r = g_encode(&mh, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(x), dims, strides, box, es,
-                                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                                 CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(SVBRDF_ERR_CUDA, "cuTensorMapEncodeTiled(halo x) failed: %d", (int)r);
     switch (bn) {

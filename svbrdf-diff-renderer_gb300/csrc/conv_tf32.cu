@@ -261,31 +261,34 @@ conv_tf32_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_consta
 // Maps of 16+ rows and 8+ columns load each input patch once per 32-channel chunk, halo
 // included, and share it between the taps. A tile is MT stacked 16-row x 8-column output
 // patches of one image; its input is the (16 MT + KS - 1) x (8 + KS - 1) patch starting at
-// (y0 - pad, x0 - pad). Shared memory holds it K-major without swizzle: for each 4-channel
-// (16-byte) group g, the patch's pixels row-major at 16 bytes each, groups kKg bytes apart
-// (128-byte aligned). Accumulator row r of M-tile mt is output pixel (16 mt + r / 8, r % 8), so
-// tap (ky, kx) reads the descriptor started at patch pixel ky kCols + kx, with 8-row groups
-// kCols x 16 bytes apart (SBO) and K-adjacent core matrices one channel group apart (LBO). The
-// taps' BN x 32 weight slices stream through their own ring (128-byte swizzle). Per chunk a
-// tile loads about 1.4 x MT x 16 KB of input instead of taps x MT x 16 KB. A work item is (tile,
-// range of chunks); with splits > 1 its partial goes to plane `split` of ws.
+// (y0 - pad, x0 - pad), one TMA box of 128-byte pixel rows (32 TF32 channels), 128-byte
+// swizzled, row-major from a 1024-byte boundary. Accumulator row r of M-tile mt is output pixel
+// (16 mt + r / 8, r % 8), so tap (ky, kx) reads the patch's descriptor moved by ky kCols + kx
+// pixels, with 8-row groups kCols pixels (kCols x 128 bytes) apart (SBO); the swizzle follows
+// the address, so any pixel offset is a valid start. The taps' BN x 32 weight slices stream
+// through their own ring (128-byte swizzle), TPS taps per stage: a whole kernel row where the
+// MMAs are narrow (BN <= 128), as a group of MMAs between two commits costs at least about 560
+// cycles. Per chunk a tile loads about 1.4 x MT x 16 KB of input instead of taps x MT x 16 KB.
+// A work item is (tile, range of chunks); with splits > 1 its partial goes to plane `split` of ws.
 template <int MT, int KS>
 struct HaloT {
   static constexpr int kRows = 16 * MT + KS - 1, kCols = 8 + KS - 1;
-  static constexpr int kKg = ((kRows * kCols * 16 + 127) / 128) * 128;
-  static constexpr int kABytes = 8 * kKg;  // 32 channels
+  static constexpr int kABytes = ((kRows * kCols * 128 + 1023) / 1024) * 1024;  // 32 channels
 };
 
 constexpr int kHaloThreads = 320;  // warp 0 TMA, warp 1 MMA + TMEM owner, warps 2..9 epilogue (two per
                                    // TMEM lane quadrant, each draining half the columns)
 
-template <int BN, int MT, int KS, int AST, int BST, int NBUF>
+template <int BN, int MT, int KS, int AST, int BST, int NBUF, int TPS>
 __global__ void __launch_bounds__(kHaloThreads, 1)
 conv_tf32_halo_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_constant__ CUtensorMap tmap_w,
                       float* __restrict__ y, float* __restrict__ ws, Geom g, int* err) {
   using HP = HaloT<MT, KS>;
-  constexpr int B_BYTES = BN * BK * 4;
+  constexpr int B_BYTES = BN * BK * 4;  // one tap's weight slice
   constexpr int TAPS = KS * KS;
+  constexpr int S_BYTES = TPS * B_BYTES;  // one weight stage
+  constexpr int GROUPS = TAPS / TPS;
+  static_assert(TAPS % TPS == 0, "a weight stage holds whole taps of one chunk");
   constexpr uint32_t ACC_COLS = MT * BN;
   constexpr uint32_t TMEM_COLS = NBUF * ACC_COLS;  // NBUF = 2: double-buffered accumulators
   static_assert(TMEM_COLS >= 32 && TMEM_COLS <= 512 && (TMEM_COLS & (TMEM_COLS - 1)) == 0, "TMEM columns");
@@ -296,7 +299,7 @@ conv_tf32_halo_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_c
   __shared__ uint32_t tmem_slot;
 
   const uint32_t bbase = (smem_u32(dsmem) + 1023u) & ~1023u;
-  const uint32_t abase = bbase + (uint32_t)(BST * B_BYTES);
+  const uint32_t abase = bbase + (uint32_t)(BST * S_BYTES);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int n_items = g.tiles_b * g.tiles_y * g.tiles_x * g.tiles_n * g.splits;
   const int kchunks = g.Cin / BK;
@@ -351,21 +354,20 @@ conv_tf32_halo_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_c
             break;
           }
           const uint32_t fa = smem_u32(&afull[sa]);
-          mbar_expect_tx(fa, (uint32_t)(8 * HP::kRows * HP::kCols * 16));
-#pragma unroll 1
-          for (int q = 0; q < 8; ++q)
-            tma_4d(abase + (uint32_t)(sa * HP::kABytes + q * HP::kKg), &tmap_x, cc * BK + 4 * q, x0 - g.pad,
-                   y0 - g.pad, img, fa);
+          mbar_expect_tx(fa, (uint32_t)(HP::kRows * HP::kCols * 128));
+          tma_4d(abase + (uint32_t)(sa * HP::kABytes), &tmap_x, cc * BK, x0 - g.pad, y0 - g.pad, img, fa);
           ++qa;
-          for (int tap = 0; tap < TAPS; ++tap) {
+          for (int grp = 0; grp < GROUPS; ++grp) {
             const int sb = qb % BST;
             if (qb >= BST && !mbar_wait(smem_u32(&bempty[sb]), ((uint32_t)(qb / BST) & 1u) ^ 1u, err, kErrTma)) {
               bad = true;
               break;
             }
             const uint32_t fb = smem_u32(&bfull[sb]);
-            mbar_expect_tx(fb, (uint32_t)B_BYTES);
-            tma_2d(bbase + (uint32_t)(sb * B_BYTES), &tmap_w, tap * g.Cin + cc * BK, n0, fb);
+            mbar_expect_tx(fb, (uint32_t)S_BYTES);
+            for (int u = 0; u < TPS; ++u)
+              tma_2d(bbase + (uint32_t)(sb * S_BYTES + u * B_BYTES), &tmap_w, (grp * TPS + u) * g.Cin + cc * BK, n0,
+                     fb);
             ++qb;
           }
         }
@@ -402,23 +404,27 @@ conv_tf32_halo_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_c
             break;
           }
           const uint32_t achunk = abase + (uint32_t)(sa * HP::kABytes);
-          for (int tap = 0; tap < TAPS; ++tap) {
+          for (int grp = 0; grp < GROUPS; ++grp) {
             const int sb = qb % BST;
             if (!mbar_wait(smem_u32(&bfull[sb]), (uint32_t)(qb / BST) & 1u, err, kErrMma)) {
               bad = true;
               break;
             }
             fence_after();
-            const uint32_t atap = achunk + (uint32_t)(((tap / KS) * HP::kCols + tap % KS) * 16);
-            const uint32_t bs = bbase + (uint32_t)(sb * B_BYTES);
 #pragma unroll
-            for (int k = 0; k < BK / 8; ++k) {  // 8 TF32 channels = two channel groups per MMA
+            for (int u = 0; u < TPS; ++u) {
+              const int tap = grp * TPS + u;
+              const uint32_t atap = achunk + (uint32_t)(((tap / KS) * HP::kCols + tap % KS) * 128);
+              const uint32_t bs = bbase + (uint32_t)(sb * S_BYTES + u * B_BYTES);
 #pragma unroll
-              for (int mt = 0; mt < MT; ++mt)
-                mma_tf32(acc + (uint32_t)(mt * BN),
-                         noswz_desc(atap + (uint32_t)(2 * k * HP::kKg + mt * 16 * HP::kCols * 16), (uint32_t)HP::kKg,
-                                    (uint32_t)(HP::kCols * 16)),
-                         sw128_desc(bs + 32u * k), id, (cc > c_lo || tap > 0 || k > 0) ? 1u : 0u);
+              for (int k = 0; k < BK / 8; ++k) {  // 8 TF32 channels (32 bytes) per MMA
+#pragma unroll
+                for (int mt = 0; mt < MT; ++mt)
+                  mma_tf32(acc + (uint32_t)(mt * BN),
+                           sw128_desc_sbo(atap + (uint32_t)(mt * 16 * HP::kCols * 128 + 32 * k),
+                                          (uint32_t)(HP::kCols * 128)),
+                           sw128_desc(bs + 32u * k), id, (cc > c_lo || tap > 0 || k > 0) ? 1u : 0u);
+              }
             }
             mma_commit(smem_u32(&bempty[sb]));
             ++qb;
@@ -628,23 +634,31 @@ static int launch(const CUtensorMap& mx, const CUtensorMap& mw, float* y, float*
   return check_launch("conv_tf32_split_sum_kernel");
 }
 
+// Taps per weight stage: a kernel row of a 3x3 convolution where the MMAs are narrow.
+template <int BN, int KS>
+constexpr int halo_tps() {
+  return (KS == 3 && BN <= 128) ? 3 : 1;
+}
+// Weight-ring depth: as many stages as fit beside two input slots, up to 16 taps in flight.
 template <int BN, int MT, int KS>
 constexpr int halo_bstages() {
-  return (int)((kStageBudget - 2 * (size_t)HaloT<MT, KS>::kABytes) / (size_t)(BN * BK * 4)) < 8
-             ? (int)((kStageBudget - 2 * (size_t)HaloT<MT, KS>::kABytes) / (size_t)(BN * BK * 4))
-             : 8;
+  constexpr size_t stage = (size_t)halo_tps<BN, KS>() * BN * BK * 4;
+  constexpr int fit = (int)((kStageBudget - 2 * (size_t)HaloT<MT, KS>::kABytes) / stage);
+  constexpr int cap = 16 / halo_tps<BN, KS>();
+  return fit < cap ? fit : cap;
 }
 
 template <int BN, int MT, int KS>
 static int launch_halo(const CUtensorMap& mx, const CUtensorMap& mw, float* y, float* ws, const Geom& g, int sms,
                        int* err, cudaStream_t st) {
+  constexpr int TPS = halo_tps<BN, KS>();
   constexpr int BST = halo_bstages<BN, MT, KS>();
-  static_assert(BST >= 3, "weight ring too shallow");
+  static_assert(BST >= 2 && BST * TPS >= 4, "weight ring too shallow");
   // 512 TMEM columns hold two MT x BN accumulators up to MT x BN = 256, else one
   constexpr int NBUF = MT * BN <= 256 ? 2 : 1;
   static std::atomic<size_t> have[64];
-  const size_t smem = (size_t)BST * BN * BK * 4 + 2 * (size_t)HaloT<MT, KS>::kABytes + 1024;
-  auto kern = conv_tf32_halo_kernel<BN, MT, KS, 2, BST, NBUF>;
+  const size_t smem = (size_t)BST * TPS * BN * BK * 4 + 2 * (size_t)HaloT<MT, KS>::kABytes + 1024;
+  auto kern = conv_tf32_halo_kernel<BN, MT, KS, 2, BST, NBUF, TPS>;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return fail(SVBRDF_ERR_CUDA, "no usable device");
   if (have[dev].load() < smem) {
@@ -738,15 +752,16 @@ extern "C" int svbrdf_gen_conv_tf32_ex(const float* x, const float* weight, floa
   cudaStream_t st = (cudaStream_t)stream;
   float* wsf = g.splits > 1 ? static_cast<float*>(ws) : nullptr;
   if (pl.halo) {
-    // the (16 MT + k - 1) x (8 + k - 1) input patch, 4 channels (16 bytes) per pixel per group
+    // the (16 MT + k - 1) x (8 + k - 1) input patch of a 32-channel chunk, one 128-byte
+    // swizzled row per pixel
     CUtensorMap mh;
     const int rows = 16 * pl.mt + ksize - 1, cols = 8 + ksize - 1;
     const cuuint64_t dims[4] = {(cuuint64_t)cin, (cuuint64_t)win, (cuuint64_t)hin, (cuuint64_t)b};
     const cuuint64_t strides[3] = {(cuuint64_t)cin * 4, (cuuint64_t)win * cin * 4, (cuuint64_t)hin * win * cin * 4};
-    const cuuint32_t box[4] = {4u, (cuuint32_t)cols, (cuuint32_t)rows, 1u};
+    const cuuint32_t box[4] = {(cuuint32_t)BK, (cuuint32_t)cols, (cuuint32_t)rows, 1u};
     const cuuint32_t es[4] = {1, 1, 1, 1};
     const CUresult r = enc(&mh, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<float*>(x), dims, strides, box, es,
-                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(SVBRDF_ERR_CUDA, "cuTensorMapEncodeTiled(halo x) failed: %d", (int)r);
     return ksize == 3 ? dispatch_halo<3>(bn, pl.mt, mh, mw, y, wsf, g, sms, err, st)

@@ -71,6 +71,19 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
   d |= (uint64_t)2 << 61;                             // 128-byte swizzle
   return d;
 }
+// The same K-major 128-byte-swizzle descriptor with 8-row groups `sbo` bytes apart. The
+// swizzle is a function of the shared-memory address (bits 4-6 XOR bits 7-9), so a matrix may
+// start at any 128-byte row of a region that the TMA wrote swizzled from a 1024-byte boundary,
+// and its row groups may be any multiple of 128 bytes apart: a 3x3 tap's window into an input
+// patch of 128-byte pixels is the patch's descriptor moved by whole pixels.
+__device__ __forceinline__ uint64_t sw128_desc_sbo(uint32_t addr, uint32_t sbo) {
+  uint64_t d = (uint64_t)((addr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)1 << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
 // Instruction descriptor, kind::f16: FP32 accumulator, BF16 A and B, both K-major.
 __host__ __device__ constexpr uint32_t idesc_bf16(int m, int n) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
@@ -110,17 +123,6 @@ __device__ __forceinline__ uint64_t sw128_desc_mn(uint32_t addr, uint32_t lbo, u
   d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
   d |= (uint64_t)1 << 46;
   d |= (uint64_t)2 << 61;
-  return d;
-}
-
-// Shared-memory matrix descriptor without swizzle, K-major: core matrices of 8 rows x 16 bytes,
-// each stored as 128 contiguous bytes (row i at +16 i); `lbo` = bytes between core matrices
-// adjacent in K, `sbo` = bytes between 8-row groups adjacent in M (or N). Layout type 0.
-__device__ __forceinline__ uint64_t noswz_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
-  uint64_t d = (uint64_t)((addr & 0x3FFFFu) >> 4);
-  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
-  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
-  d |= (uint64_t)1 << 46;
   return d;
 }
 

@@ -238,7 +238,14 @@ int svbrdf_conv3x3_bf16(const void* x, const void* weight, const float* bias, co
  * y. In the descriptor's backward pass this adds a hooked layer's loss gradient to the data
  * gradient arriving from the layer above and applies that hooked ReLU's mask, in one pass
  * (the autograd graph of src/descriptor.py:77-79 does the add, the mask and the next
- * convolution as separate kernels). */
+ * convolution as separate kernels).
+ * Epilogues 4 and 5 fold the backward pass of a 2x2 pool (stride 2) that precedes this
+ * convolution in the forward pass: the result (the gradient at the pool's output, h x w) is
+ * routed to the pool's input, mask BF16 NHWC [n][2h][2w][cout] -- to the first maximum of each
+ * window in row-major order (4, a max-pool, as ATen routes it) or a quarter to each element
+ * (5, an average pool) -- plus addend (BF16 like mask, or null) there, times (mask > 0) (the
+ * ReLU below the pool), written to y [n][2h][2w][cout]. One pass replaces the pool's backward
+ * kernel and the round trip of the pooled gradient through memory. */
 int svbrdf_conv3x3_bf16_ex(const void* x, const void* weight, const float* bias, const void* mask,
                            const void* addend, void* y, int n, int h, int w, int cin, int cout, int epilogue,
                            int* err, void* stream);
@@ -271,6 +278,16 @@ int svbrdf_desc_conv1_fwd(const float* renders, const float* weight, const float
  * without `downsample`), overwritten. */
 int svbrdf_desc_conv1_bwd(const void* gz, const float* weight, float* grad_renders, int v, int h, int w,
                           int downsample, void* stream);
+
+/* The same data gradient on the tensor cores: the 64 -> 3 channel 3x3 convolution as a BF16
+ * tcgen05 implicit GEMM (N = 16: weight rows 3..15 zero), FP32 accumulation. w16: BF16
+ * [16][9][64], row c, tap 3 ky + kx, channel k = conv1_1's weight[k][c][2 - ky][2 - kx] for
+ * c < 3. scale[c] (FP32, 3 values) multiplies channel c: 1 / std[c] of the normalisation, times
+ * 1/4 with `downsample` (the box filter's adjoint gives each of the window's 4 render pixels
+ * the scaled value). h % 8 == 0, w % 16 == 0; gz and w16 16-byte aligned, grad_renders
+ * 8-byte aligned. `err` as in svbrdf_conv3x3_bf16. */
+int svbrdf_desc_conv1_bwd_tc(const void* gz, const void* w16, const float* scale, float* grad_renders, int v, int h,
+                             int w, int downsample, int* err, void* stream);
 
 /* 2x2 max-pool, BF16 NHWC [v][h][w][c] -> [v][h/2][w/2][c]; h, w even, c % 8 == 0. */
 int svbrdf_desc_pool_fwd(const void* x, void* y, int v, int h, int w, int c, void* stream);

@@ -136,6 +136,8 @@ def _declare(L):
     L.svbrdf_desc_conv1_fwd.argtypes = [P, P, P, P, P, I, I, I, I, P]
     L.svbrdf_desc_conv1_bwd.restype = I
     L.svbrdf_desc_conv1_bwd.argtypes = [P, P, P, I, I, I, I, P]
+    L.svbrdf_desc_conv1_bwd_tc.restype = I
+    L.svbrdf_desc_conv1_bwd_tc.argtypes = [P, P, P, P, I, I, I, I, P, P]
     L.svbrdf_desc_pool_fwd.restype = I
     L.svbrdf_desc_pool_fwd.argtypes = [P, P, I, I, I, I, P]
     L.svbrdf_desc_pool_bwd.restype = I
@@ -226,7 +228,7 @@ EXPORTS = [
     "svbrdf_fused_step", "svbrdf_fused_step_noalloc",
     "svbrdf_batched_plan_bytes",
     "svbrdf_batched_plan", "svbrdf_batched_workspace_bytes", "svbrdf_batched_step", "svbrdf_batched_steps", "svbrdf_conv3x3_bf16",
-    "svbrdf_conv3x3_bf16_ex", "svbrdf_desc_partials", "svbrdf_desc_conv1_fwd", "svbrdf_desc_conv1_bwd",
+    "svbrdf_conv3x3_bf16_ex", "svbrdf_desc_partials", "svbrdf_desc_conv1_fwd", "svbrdf_desc_conv1_bwd", "svbrdf_desc_conv1_bwd_tc",
     "svbrdf_desc_pool_fwd", "svbrdf_desc_pool_bwd", "svbrdf_desc_avgpool_fwd", "svbrdf_desc_avgpool_bwd",
     "svbrdf_desc_feat_loss", "svbrdf_desc_loss_sums", "svbrdf_desc_gram_splits", "svbrdf_desc_gram", "svbrdf_desc_gram_finish",
     "svbrdf_desc_gemm_nt", "svbrdf_desc_gemm_nt_feat_partials", "svbrdf_desc_gemm_nt_feat",

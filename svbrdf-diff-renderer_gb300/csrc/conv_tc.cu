@@ -40,14 +40,24 @@ constexpr int BK = 64;   // input channels per chunk (one 128-byte weight row)
 constexpr int kThreads = 320;  // warp 0 TMA, warp 1 MMA + TMEM owner, warps 2..9 epilogue
 constexpr int kEpiWarps = 8;  // two per TMEM lane quadrant, each draining half the columns
 
-enum Epilogue : int { kEpiNone = 0, kEpiBiasRelu = 1, kEpiMask = 2, kEpiAddMask = 3 };
+// kEpiUnpoolMax / kEpiUnpoolAvg: the convolution's output is the gradient at a 2x2 pool's
+// output; the epilogue routes it back to the pool's input (the window's first maximum, or a
+// quarter to each element), adds the addend there and applies the ReLU mask of the pool's input.
+// `mask` is the pool's input and `y` the gradient at it, both [N, 2H, 2W, Cout].
+// kEpiRenderDown / kEpiRender (BN = 16, the data gradient of the descriptor's first layer,
+// 64 -> 3 channels padded to 16): channel c < 3 of the accumulator times scale[c] (`bias`) is the
+// gradient at the normalised render, written FP32 NCHW to `y` [N][3][2H][2W] through the 2x2
+// box downsample's adjoint (each of the window's 4 pixels takes the value; the 1/4 is in scale)
+// or [N][3][H][W] without it.
+enum Epilogue : int { kEpiNone = 0, kEpiBiasRelu = 1, kEpiMask = 2, kEpiAddMask = 3, kEpiUnpoolMax = 4,
+                      kEpiUnpoolAvg = 5, kEpiRenderDown = 6, kEpiRender = 7 };
 enum ConvError : int { kErrTma = 11, kErrMma = 12, kErrEpi = 13 };
 
-// One accumulator row (an output pixel) of 32 channels through the epilogue, stored as BF16.
+// One accumulator row (an output pixel) of 32 channels through the epilogue, stored as BF16;
+// `mv` and `av` hold the row's 32 mask and addend values (BF16, 4 x 16 bytes each).
 template <int EPI>
-__device__ __forceinline__ void epilogue_store32(const uint32_t (&r)[32], const float* __restrict__ bias,
-                                                 const __nv_bfloat16* __restrict__ mask,
-                                                 const __nv_bfloat16* __restrict__ addend, __nv_bfloat16* out,
+__device__ __forceinline__ void epilogue_apply32(const uint32_t (&r)[32], const float* __restrict__ bias,
+                                                 const uint4 (&mv)[4], const uint4 (&av)[4], __nv_bfloat16* out,
                                                  size_t off, int nc) {
   float v[32];
 #pragma unroll
@@ -57,11 +67,9 @@ __device__ __forceinline__ void epilogue_store32(const uint32_t (&r)[32], const 
     for (int j = 0; j < 32; ++j) v[j] = fmaxf(v[j] + __ldg(bias + nc + j), 0.0f);
   } else if (EPI == kEpiMask || EPI == kEpiAddMask) {
     if (EPI == kEpiAddMask) {  // + the hook's loss gradient at this activation
-      const uint4* ap = reinterpret_cast<const uint4*>(addend + off);
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
-        const uint4 av = __ldg(ap + u);
-        const __nv_bfloat162* a2 = reinterpret_cast<const __nv_bfloat162*>(&av);
+        const __nv_bfloat162* a2 = reinterpret_cast<const __nv_bfloat162*>(&av[u]);
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
           const float2 f = __bfloat1622float2(a2[e]);
@@ -70,11 +78,9 @@ __device__ __forceinline__ void epilogue_store32(const uint32_t (&r)[32], const 
         }
       }
     }
-    const uint4* mp = reinterpret_cast<const uint4*>(mask + off);
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
-      const uint4 mv = __ldg(mp + u);
-      const __nv_bfloat162* m2 = reinterpret_cast<const __nv_bfloat162*>(&mv);
+      const __nv_bfloat162* m2 = reinterpret_cast<const __nv_bfloat162*>(&mv[u]);
 #pragma unroll
       for (int e = 0; e < 4; ++e) {
         const float2 f = __bfloat1622float2(m2[e]);
@@ -96,6 +102,94 @@ __device__ __forceinline__ void epilogue_store32(const uint32_t (&r)[32], const 
     pk.z = *reinterpret_cast<uint32_t*>(&h2);
     pk.w = *reinterpret_cast<uint32_t*>(&h3);
     op[u] = pk;
+  }
+}
+
+// The row's mask (and addend) values, 4 x 16 bytes each, for epilogue_apply32.
+template <int EPI>
+__device__ __forceinline__ void epilogue_load32(const __nv_bfloat16* __restrict__ mask,
+                                                const __nv_bfloat16* __restrict__ addend, size_t off, uint4 (&mv)[4],
+                                                uint4 (&av)[4]) {
+  if (EPI == kEpiMask || EPI == kEpiAddMask) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) mv[u] = __ldg(reinterpret_cast<const uint4*>(mask + off) + u);
+  }
+  if (EPI == kEpiAddMask) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) av[u] = __ldg(reinterpret_cast<const uint4*>(addend + off) + u);
+  }
+}
+
+// One accumulator row (the gradient at pool-output pixel (py, px), 32 channels) routed back
+// through a 2x2 pool: `base` is element (2 py, 2 px, channel) of the [.., 2H, 2W, Cout] maps,
+// `rs` their row stride in elements. Window order (0,0), (0,1), (1,0), (1,1); a max-pool's
+// gradient goes to the first maximum (strictly greater replaces).
+template <bool AVG>
+__device__ __forceinline__ void epilogue_unpool32(const uint32_t (&r)[32], const __nv_bfloat16* __restrict__ x,
+                                                  const __nv_bfloat16* __restrict__ addend, __nv_bfloat16* out,
+                                                  size_t base, size_t rs, int cout) {
+  const size_t offs[4] = {base, base + cout, base + rs, base + rs + cout};
+#pragma unroll
+  for (int u = 0; u < 4; ++u) {  // 8 channels at a time
+    uint4 xv[4], av[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) xv[k] = __ldg(reinterpret_cast<const uint4*>(x + offs[k]) + u);
+    if (addend) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) av[k] = __ldg(reinterpret_cast<const uint4*>(addend + offs[k]) + u);
+    }
+    float xf[4][8], o[4][8];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&xv[k]);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const float2 f = __bfloat1622float2(h[e]);
+        xf[k][2 * e] = f.x;
+        xf[k][2 * e + 1] = f.y;
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      const float g = __uint_as_float(r[u * 8 + c]);
+      int am = 0;
+      if (!AVG) {
+        float m = xf[0][c];
+#pragma unroll
+        for (int k = 1; k < 4; ++k)
+          if (xf[k][c] > m) {
+            m = xf[k][c];
+            am = k;
+          }
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k) o[k][c] = AVG ? 0.25f * g : (am == k ? g : 0.0f);
+    }
+    if (addend) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const __nv_bfloat162* h = reinterpret_cast<const __nv_bfloat162*>(&av[k]);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const float2 f = __bfloat1622float2(h[e]);
+          o[k][2 * e] += f.x;
+          o[k][2 * e + 1] += f.y;
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      uint4 pk;
+      uint32_t* pw = reinterpret_cast<uint32_t*>(&pk);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const float a0 = xf[k][2 * e] > 0.0f ? o[k][2 * e] : 0.0f;
+        const float a1 = xf[k][2 * e + 1] > 0.0f ? o[k][2 * e + 1] : 0.0f;
+        __nv_bfloat162 hh = __floats2bfloat162_rn(a0, a1);
+        pw[e] = *reinterpret_cast<uint32_t*>(&hh);
+      }
+      reinterpret_cast<uint4*>(out + offs[k])[u] = pk;
+    }
   }
 }
 
@@ -275,30 +369,81 @@ conv3x3_halo_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_con
       mma_commit(smem_u32(&done_bar));  // also on abort, so TMEM is idle before it is freed
     }
   } else {
-    // ---------------------------------------------------------------- epilogue (warps 2..5)
+    // ---------------------------------------------------------------- epilogue (warps 2..9)
+    // Each thread owns accumulator row m (one output pixel) and drains NCH 32-column chunks: of
+    // every M-tile, its half of the columns; or, where BN = 64 and MT = 2, all 64 columns of
+    // M-tile `half`, so that each thread moves its pixel's whole 128-byte row. The mask / addend
+    // values of the first PF chunks depend only on the tile's coordinates, so they are loaded
+    // before the wait for the accumulator.
+    constexpr bool BYTILE = BN == 64 && MT == 2;
+    constexpr int CPH = BYTILE ? 2 : (BN >= 64 ? BN / 64 : 1);  // 32-column chunks per M-tile drained
+    constexpr int NCH = BN >= 64 ? (BYTILE ? 1 : MT) * CPH : 0;  // BN = 16 (the render epilogues) drains below
+    constexpr int PF = EPI == kEpiMask ? (NCH < 4 ? NCH : 4) : EPI == kEpiAddMask ? (NCH < 2 ? NCH : 2) : 0;
     const int qw = warp & 3;        // the TMEM lane quadrant this warp may read
-    const int half = (warp - 2) >> 2;  // which half of the columns it drains
+    const int half = (warp - 2) >> 2;  // which half of the columns (or which M-tile) it drains
     const int m = qw * 32 + lane;  // accumulator row: patch row m / 8, column m % 8
+    const int mt0 = BYTILE ? half : 0, cbase = BYTILE ? 0 : half * (BN / 2);
     int j = 0;
     for (int t = blockIdx.x; t < n_tiles; t += gridDim.x, ++j) {
       const int a = j & 1;
+      int img, y0, x0, n0;
+      coord(t, img, y0, x0, n0);
+      uint4 pm[PF > 0 ? PF : 1][4], pa[PF > 0 ? PF : 1][4];
+#pragma unroll
+      for (int q = 0; q < PF; ++q) {
+        const int mt = mt0 + q / CPH, c0 = cbase + (q % CPH) * 32;
+        const int py = y0 + 16 * mt + m / 8, px = x0 + m % 8;
+        if (py < H) epilogue_load32<EPI>(mask, addend, (((size_t)img * H + py) * W + px) * Cout + n0 + c0, pm[q], pa[q]);
+      }
       const bool ok = __all_sync(0xffffffffu, mbar_wait(smem_u32(&tfull_bar[a]), (uint32_t)(j >> 1) & 1u, err,
                                                         kErrEpi)) &&
                       *(volatile int*)err == 0;
       fence_after();
       if (!ok) break;
-      int img, y0, x0, n0;
-      coord(t, img, y0, x0, n0);
 #pragma unroll
-      for (int mt = 0; mt < MT; ++mt) {
+      for (int q = 0; q < NCH; ++q) {
+        const int mt = mt0 + q / CPH, c0 = cbase + (q % CPH) * 32;
         const int py = y0 + 16 * mt + m / 8, px = x0 + m % 8;
-        const bool inside = py < H;
-        const size_t pix = ((size_t)img * H + py) * W + px;
-#pragma unroll 1
-        for (int c0 = half * (BN / 2); c0 < (half + 1) * (BN / 2); c0 += 32) {
-          uint32_t r[32];
-          tmem_ld32(tmem + ((uint32_t)(qw * 32) << 16) + (uint32_t)(a * ACC_COLS + mt * BN + c0), r);
-          if (inside) epilogue_store32<EPI>(r, bias, mask, addend, y, pix * Cout + n0 + c0, n0 + c0);
+        const size_t off = (((size_t)img * H + py) * W + px) * Cout + n0 + c0;
+        uint32_t r[32];
+        tmem_ld32(tmem + ((uint32_t)(qw * 32) << 16) + (uint32_t)(a * ACC_COLS + mt * BN + c0), r);
+        if (EPI == kEpiUnpoolMax || EPI == kEpiUnpoolAvg) {
+          if (py < H) {
+            const size_t rs = (size_t)2 * W * Cout;
+            const size_t base = ((size_t)img * 2 * H + 2 * py) * rs + (size_t)2 * px * Cout + n0 + c0;
+            epilogue_unpool32<EPI == kEpiUnpoolAvg>(r, mask, addend, y, base, rs, Cout);
+          }
+        } else if (py < H) {
+          if (q < PF) {
+            epilogue_apply32<EPI>(r, bias, pm[q < PF ? q : 0], pa[q < PF ? q : 0], y, off, n0 + c0);
+          } else {
+            uint4 mv[4], av[4];
+            epilogue_load32<EPI>(mask, addend, off, mv, av);
+            epilogue_apply32<EPI>(r, bias, mv, av, y, off, n0 + c0);
+          }
+        }
+      }
+      if ((EPI == kEpiRenderDown || EPI == kEpiRender) && half == 0) {
+        float* dr = reinterpret_cast<float*>(y);
+        const int px = x0 + m % 8;
+#pragma unroll
+        for (int mt = 0; mt < MT; ++mt) {
+          const int py = y0 + 16 * mt + m / 8;
+          uint32_t r[4];
+          tmem_ld4(tmem + ((uint32_t)(qw * 32) << 16) + (uint32_t)(a * ACC_COLS + mt * BN), r);
+          if (py < H) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              const float val = __uint_as_float(r[c]) * __ldg(bias + c);
+              if (EPI == kEpiRenderDown) {
+                float* row = dr + (((size_t)img * 3 + c) * 2 * H + 2 * py) * (size_t)(2 * W) + 2 * px;
+                *reinterpret_cast<float2*>(row) = make_float2(val, val);
+                *reinterpret_cast<float2*>(row + 2 * W) = make_float2(val, val);
+              } else {
+                dr[(((size_t)img * 3 + c) * H + py) * (size_t)W + px] = val;
+              }
+            }
+          }
         }
       }
       fence_before();
@@ -390,7 +535,11 @@ static int dispatch_halo(int epi, const CUtensorMap& mx, const CUtensorMap& mw, 
     case kEpiBiasRelu:
       return launch_halo<BN, MT, kEpiBiasRelu>(mx, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st);
     case kEpiMask: return launch_halo<BN, MT, kEpiMask>(mx, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st);
-    default: return launch_halo<BN, MT, kEpiAddMask>(mx, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st);
+    case kEpiAddMask:
+      return launch_halo<BN, MT, kEpiAddMask>(mx, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st);
+    case kEpiUnpoolMax:
+      return launch_halo<BN, MT, kEpiUnpoolMax>(mx, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st);
+    default: return launch_halo<BN, MT, kEpiUnpoolAvg>(mx, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st);
   }
 }
 
@@ -408,9 +557,9 @@ extern "C" int svbrdf_conv3x3_bf16_ex(const void* x, const void* weight, const f
     return fail(SVBRDF_ERR_UNSUPPORTED, "conv3x3: H must be a multiple of %d and W of %d (got %dx%d)", TH, TW, h, w);
   if (cin < BK || cin % BK || cout < 64 || cout % 64 || cin > 4096 || cout > 4096)
     return fail(SVBRDF_ERR_UNSUPPORTED, "conv3x3: channels must be multiples of 64 (got %d -> %d)", cin, cout);
-  if (epilogue < kEpiNone || epilogue > kEpiAddMask) return fail(SVBRDF_ERR_INVALID, "bad epilogue %d", epilogue);
+  if (epilogue < kEpiNone || epilogue > kEpiUnpoolAvg) return fail(SVBRDF_ERR_INVALID, "bad epilogue %d", epilogue);
   if (epilogue == kEpiBiasRelu && !bias) return fail(SVBRDF_ERR_INVALID, "bias+relu epilogue needs bias");
-  if ((epilogue == kEpiMask || epilogue == kEpiAddMask) && !mask)
+  if ((epilogue == kEpiMask || epilogue == kEpiAddMask || epilogue >= kEpiUnpoolMax) && !mask)
     return fail(SVBRDF_ERR_INVALID, "mask epilogue needs mask");
   if (epilogue == kEpiAddMask && !addend) return fail(SVBRDF_ERR_INVALID, "add+mask epilogue needs addend");
   if (((uintptr_t)x | (uintptr_t)weight | (uintptr_t)y | (uintptr_t)mask | (uintptr_t)addend) % 16)
@@ -456,6 +605,50 @@ extern "C" int svbrdf_conv3x3_bf16_ex(const void* x, const void* weight, const f
                        : dispatch_halo<64, 1>(epilogue, mh, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st);
     }
   }
+}
+
+extern "C" int svbrdf_desc_conv1_bwd_tc(const void* gz, const void* w16, const float* scale, float* dr, int n, int h,
+                                        int w, int down, int* err, void* stream) {
+  using namespace svb::tc;
+  if (!gz || !w16 || !scale || !dr || !err) return fail(SVBRDF_ERR_INVALID, "conv1_bwd_tc: null argument");
+  if (n < 1 || n > 65535 || h < TH || w < TW || h % TH || w % TW)
+    return fail(SVBRDF_ERR_UNSUPPORTED, "conv1_bwd_tc: H must be a multiple of %d and W of %d (got %dx%d)", TH, TW, h,
+                w);
+  if (((uintptr_t)gz | (uintptr_t)w16) % 16 || (uintptr_t)dr % 8)
+    return fail(SVBRDF_ERR_INVALID, "conv1_bwd_tc: gz / w16 must be 16-byte aligned, dr 8-byte aligned");
+  if ((long long)n * h * w * 64 >= (1LL << 40)) return fail(SVBRDF_ERR_UNSUPPORTED, "conv1_bwd_tc: tensor too large");
+  PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+  int rc = get_tensor_map_encoder(&g_encode);
+  if (rc) return rc;
+  CUtensorMap mw, mh;
+  {
+    const cuuint64_t dims[2] = {(cuuint64_t)9 * 64, 16};
+    const cuuint64_t strides[1] = {(cuuint64_t)9 * 64 * 2};
+    const cuuint32_t box[2] = {(cuuint32_t)BK, 16u};
+    const cuuint32_t es[2] = {1, 1};
+    const CUresult r = g_encode(&mw, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(w16), dims, strides, box,
+                                es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(SVBRDF_ERR_CUDA, "cuTensorMapEncodeTiled(w16) failed: %d", (int)r);
+  }
+  const int mt = h >= 32 ? 2 : 1;
+  {
+    const cuuint64_t dims[4] = {64, (cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)n};
+    const cuuint64_t strides[3] = {64 * 2, (cuuint64_t)w * 64 * 2, (cuuint64_t)h * w * 64 * 2};
+    const cuuint32_t box[4] = {(cuuint32_t)BK, 10u, (cuuint32_t)(16 * mt + 2), 1u};
+    const cuuint32_t es[4] = {1, 1, 1, 1};
+    const CUresult r = g_encode(&mh, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void*>(gz), dims, strides, box,
+                                es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(SVBRDF_ERR_CUDA, "cuTensorMapEncodeTiled(gz) failed: %d", (int)r);
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  void* y = dr;
+  if (down)
+    return mt == 2 ? launch_halo<16, 2, kEpiRenderDown>(mh, mw, scale, nullptr, nullptr, y, n, h, w, 64, 16, err, st)
+                   : launch_halo<16, 1, kEpiRenderDown>(mh, mw, scale, nullptr, nullptr, y, n, h, w, 64, 16, err, st);
+  return mt == 2 ? launch_halo<16, 2, kEpiRender>(mh, mw, scale, nullptr, nullptr, y, n, h, w, 64, 16, err, st)
+                 : launch_halo<16, 1, kEpiRender>(mh, mw, scale, nullptr, nullptr, y, n, h, w, 64, 16, err, st);
 }
 
 extern "C" int svbrdf_conv3x3_bf16(const void* x, const void* weight, const float* bias, const void* mask, void* y,

@@ -33,47 +33,52 @@ __constant__ float c_std[3] = {0.229f, 0.224f, 0.255f};  // the reference's blue
 constexpr int kTile = 16;
 
 // ---------------------------------------------------------------- conv1_1 forward
-// A block computes a 16 x 16 pixel tile, all 64 channels. Thread t owns channels
-// 4 (t % 16) .. +3 of the 16 pixels of tile row t / 16, so the 16 threads of a half-warp store
-// one pixel's 64 channels as one contiguous 256-byte run (128 bytes in BF16).
+// A block computes an 8-row x 16-column pixel tile, all 64 channels, with 128 threads. Thread t
+// owns channels 4 (t % 16) .. +3 of the 16 pixels of tile row t / 16, so the 16 threads of a
+// half-warp store one pixel's 64 channels as one contiguous 256-byte run (128 bytes in BF16).
+// The products run as packed FP32 pair FMAs (channels 4k, 4k+1 and 4k+2, 4k+3), each lane
+// rounded as a scalar FMA. Small blocks (several per SM) let one block's input staging overlap
+// another's arithmetic and stores.
+constexpr int kTileY = 8;
 template <bool DOWN>
-__global__ void __launch_bounds__(256) desc_conv1_fwd_kernel(const float* __restrict__ r, const float* __restrict__ w,
+__global__ void __launch_bounds__(128) desc_conv1_fwd_kernel(const float* __restrict__ r, const float* __restrict__ w,
                                                              const float* __restrict__ b, float* __restrict__ out32,
                                                              __nv_bfloat16* __restrict__ out16, int H, int W) {
-  __shared__ float s_in[3][kTile + 2][kTile + 2];
+  __shared__ float s_in[3][kTileY + 2][kTile + 2];
   __shared__ __align__(16) float s_w[27][64];  // [ci*9 + ky*3 + kx][co]
   __shared__ __align__(16) float s_b[64];
   const int tid = threadIdx.x;
-  const int v = blockIdx.z, y0 = blockIdx.y * kTile, x0 = blockIdx.x * kTile;
-  for (int i = tid; i < 64 * 27; i += 256) s_w[i % 27][i / 27] = w[i];  // w is [co][ci][ky][kx]
+  const int v = blockIdx.z, y0 = blockIdx.y * kTileY, x0 = blockIdx.x * kTile;
+  for (int i = tid; i < 64 * 27; i += 128) s_w[i % 27][i / 27] = w[i];  // w is [co][ci][ky][kx]
   if (tid < 64) s_b[tid] = b[tid];
   const int RH = DOWN ? 2 * H : H, RW = DOWN ? 2 * W : W;
-  for (int i = tid; i < 3 * (kTile + 2) * (kTile + 2); i += 256) {
-    const int ci = i / ((kTile + 2) * (kTile + 2)), rem = i % ((kTile + 2) * (kTile + 2));
+  for (int i = tid; i < 3 * (kTileY + 2) * (kTile + 2); i += 128) {
+    const int ci = i / ((kTileY + 2) * (kTile + 2)), rem = i % ((kTileY + 2) * (kTile + 2));
     const int ty = rem / (kTile + 2), tx = rem % (kTile + 2);
     const int gy = y0 + ty - 1, gx = x0 + tx - 1;
     float val = 0.0f;  // zero padding of the normalised image
     if (gy >= 0 && gy < H && gx >= 0 && gx < W) {
       const float* rp = r + ((size_t)v * 3 + ci) * RH * RW;
-      float s;
+      float sv;
       if (DOWN) {
         const float* q = rp + (size_t)(2 * gy) * RW + 2 * gx;
-        s = (q[0] + q[1] + q[RW] + q[RW + 1]) * 0.25f;
+        sv = (q[0] + q[1] + q[RW] + q[RW + 1]) * 0.25f;
       } else {
-        s = rp[(size_t)gy * RW + gx];
+        sv = rp[(size_t)gy * RW + gx];
       }
-      val = (s - c_mean[ci]) / c_std[ci];
+      val = (sv - c_mean[ci]) / c_std[ci];
     }
     s_in[ci][ty][tx] = val;
   }
   __syncthreads();
   const int cg = tid & 15, row = tid >> 4;
   const int y = y0 + row;
-  float acc[kTile][4];
+  float2 acc[kTile][2];
   const float4 bias4 = reinterpret_cast<const float4*>(s_b)[cg];
 #pragma unroll
   for (int px = 0; px < kTile; ++px) {
-    acc[px][0] = bias4.x; acc[px][1] = bias4.y; acc[px][2] = bias4.z; acc[px][3] = bias4.w;
+    acc[px][0] = make_float2(bias4.x, bias4.y);
+    acc[px][1] = make_float2(bias4.z, bias4.w);
   }
 #pragma unroll
   for (int ci = 0; ci < 3; ++ci)
@@ -82,13 +87,13 @@ __global__ void __launch_bounds__(256) desc_conv1_fwd_kernel(const float* __rest
 #pragma unroll
       for (int kx = 0; kx < 3; ++kx) {
         const float4 w4 = reinterpret_cast<const float4*>(s_w[ci * 9 + ky * 3 + kx])[cg];
+        const float2 w01 = make_float2(w4.x, w4.y), w23 = make_float2(w4.z, w4.w);
 #pragma unroll
         for (int px = 0; px < kTile; ++px) {
           const float xv = s_in[ci][row + ky][px + kx];
-          acc[px][0] = fmaf(w4.x, xv, acc[px][0]);
-          acc[px][1] = fmaf(w4.y, xv, acc[px][1]);
-          acc[px][2] = fmaf(w4.z, xv, acc[px][2]);
-          acc[px][3] = fmaf(w4.w, xv, acc[px][3]);
+          const float2 x2 = make_float2(xv, xv);
+          acc[px][0] = __ffma2_rn(w01, x2, acc[px][0]);
+          acc[px][1] = __ffma2_rn(w23, x2, acc[px][1]);
         }
       }
   if (y >= H) return;
@@ -96,8 +101,8 @@ __global__ void __launch_bounds__(256) desc_conv1_fwd_kernel(const float* __rest
   for (int px = 0; px < kTile; ++px) {
     const int x = x0 + px;
     if (x >= W) break;
-    const float a0 = fmaxf(acc[px][0], 0.f), a1 = fmaxf(acc[px][1], 0.f), a2 = fmaxf(acc[px][2], 0.f),
-                a3 = fmaxf(acc[px][3], 0.f);
+    const float a0 = fmaxf(acc[px][0].x, 0.f), a1 = fmaxf(acc[px][0].y, 0.f), a2 = fmaxf(acc[px][1].x, 0.f),
+                a3 = fmaxf(acc[px][1].y, 0.f);
     const size_t pix = ((size_t)v * H + y) * W + x;
     reinterpret_cast<float4*>(out32 + pix * 64)[cg] = make_float4(a0, a1, a2, a3);
     __nv_bfloat162 h0 = __floats2bfloat162_rn(a0, a1), h1 = __floats2bfloat162_rn(a2, a3);
@@ -245,11 +250,18 @@ __global__ void desc_pool_fwd_kernel(const __nv_bfloat16* __restrict__ x, __nv_b
 
 // gx = (pool-route(gy) + addend) * (x > 0). x is the pool's input, a ReLU output, so x > 0 is
 // that ReLU's mask. Max-pool: the window's first maximum in row-major order takes the
-// gradient. AVG: every element of the window takes gy / 4.
+// gradient. AVG: every element of the window takes gy / 4. Each thread issues all of its loads
+// (the window's x, gy, the window's addend: nine 16-byte loads) before any arithmetic, keeping
+// them as raw BF16 until use.
+__device__ __forceinline__ float2 bf2f(const uint4& u, int e) {
+  return __bfloat1622float2(reinterpret_cast<const __nv_bfloat162*>(&u)[e]);
+}
 template <bool AVG>
-__global__ void desc_pool_bwd_kernel(const __nv_bfloat16* __restrict__ gy, const __nv_bfloat16* __restrict__ x,
-                                     const __nv_bfloat16* __restrict__ addend, __nv_bfloat16* __restrict__ gx, int V,
-                                     int H, int W, int C) {
+__global__ void __launch_bounds__(256) desc_pool_bwd_kernel(const __nv_bfloat16* __restrict__ gy,
+                                                            const __nv_bfloat16* __restrict__ x,
+                                                            const __nv_bfloat16* __restrict__ addend,
+                                                            __nv_bfloat16* __restrict__ gx, int V, int H, int W,
+                                                            int C) {
   // grid (ceil(Wo C8 / 256), V Ho): block row (v, yo); thread t of the row is (xo, c8)
   const int Ho = H / 2, Wo = W / 2, C8 = C / 8;
   const int v = blockIdx.y / Ho, yo = blockIdx.y % Ho;
@@ -258,31 +270,46 @@ __global__ void desc_pool_bwd_kernel(const __nv_bfloat16* __restrict__ gy, const
     const size_t p = ((size_t)v * Ho + yo) * Wo + xo;
     const size_t b0 = (((size_t)v * H + 2 * yo) * W + 2 * xo) * C + c8 * 8;
     const size_t offs[4] = {0, (size_t)C, (size_t)W * C, (size_t)W * C + C};
-    float xv[4][8], g[8];
+    uint4 xr[4], ar[4];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) bf8_load(x + b0 + offs[k], xv[k]);
-    bf8_load(gy + p * C + c8 * 8, g);
-    int am[8];
+    for (int k = 0; k < 4; ++k) xr[k] = __ldg(reinterpret_cast<const uint4*>(x + b0 + offs[k]));
+    const uint4 gr = __ldg(reinterpret_cast<const uint4*>(gy + p * C + c8 * 8));
+    if (addend) {
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      float m = xv[0][j];
-      am[j] = 0;
+      for (int k = 0; k < 4; ++k) ar[k] = __ldg(reinterpret_cast<const uint4*>(addend + b0 + offs[k]));
+    } else {
 #pragma unroll
-      for (int k = 1; k < 4; ++k)
-        if (xv[k][j] > m) { m = xv[k][j]; am[j] = k; }
+      for (int k = 0; k < 4; ++k) ar[k] = make_uint4(0u, 0u, 0u, 0u);  // BF16 zeros
     }
+    uint4 o[4];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      float o[8], ad[8];
-      if (addend) bf8_load(addend + b0 + offs[k], ad);
+    for (int e = 0; e < 4; ++e) {  // channel pairs 2e, 2e + 1
+      const float2 g = bf2f(gr, e);
+      float2 xv[4];
 #pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        float val = AVG ? 0.25f * g[j] : ((am[j] == k) ? g[j] : 0.0f);
-        if (addend) val += ad[j];
-        o[j] = xv[k][j] > 0.0f ? val : 0.0f;
+      for (int k = 0; k < 4; ++k) xv[k] = bf2f(xr[k], e);
+      int amx = 0, amy = 0;
+      if (!AVG) {
+        float mx = xv[0].x, my = xv[0].y;
+#pragma unroll
+        for (int k = 1; k < 4; ++k) {
+          if (xv[k].x > mx) { mx = xv[k].x; amx = k; }
+          if (xv[k].y > my) { my = xv[k].y; amy = k; }
+        }
       }
-      bf8_store(gx + b0 + offs[k], o);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const float2 ad = bf2f(ar[k], e);
+        float vx = AVG ? 0.25f * g.x : (amx == k ? g.x : 0.0f);
+        float vy = AVG ? 0.25f * g.y : (amy == k ? g.y : 0.0f);
+        vx += ad.x;
+        vy += ad.y;
+        const __nv_bfloat162 h = __floats2bfloat162_rn(xv[k].x > 0.0f ? vx : 0.0f, xv[k].y > 0.0f ? vy : 0.0f);
+        reinterpret_cast<uint32_t*>(&o[k])[e] = *reinterpret_cast<const uint32_t*>(&h);
+      }
     }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) *reinterpret_cast<uint4*>(gx + b0 + offs[k]) = o[k];
   }
 }
 
@@ -356,7 +383,19 @@ __global__ void __launch_bounds__(kLossSumThreads) desc_loss_sums_kernel(const f
   for (int k = 0; k < segs.n; ++k) {
     float sk = 0.0f;
     const float* p = buf + segs.off[k];
-    for (long long i = threadIdx.x; i < segs.len[k]; i += kLossSumThreads) sk += __ldg(p + i);
+    const long long len = segs.len[k];
+    // the thread's elements i, i + T, i + 2T, ... added in that order, eight loads in flight
+    for (long long i = threadIdx.x; i < len; i += 8LL * kLossSumThreads) {
+      float q[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const long long e = i + (long long)u * kLossSumThreads;
+        q[u] = e < len ? __ldg(p + e) : 0.0f;
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        if (i + (long long)u * kLossSumThreads < len) sk += q[u];
+    }
     acc[segs.group[k]] += segs.w[k] * (double)sk;
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -420,7 +459,8 @@ int svbrdf_desc_conv1_fwd(const float* renders, const float* weight, const float
   if (!renders || !weight || !bias || !out_f32 || !out_bf16) return fail(SVBRDF_ERR_INVALID, "null pointer");
   if (v < 1 || h < 1 || w < 1) return fail(SVBRDF_ERR_INVALID, "bad shape");
   if (((uintptr_t)out_f32 | (uintptr_t)out_bf16) % 16) return fail(SVBRDF_ERR_INVALID, "outputs must be 16-byte aligned");
-  dim3 grid((w + kTile - 1) / kTile, (h + kTile - 1) / kTile, v), block(256);
+  if (v > 65535 || (h + kTileY - 1) / kTileY > 65535) return fail(SVBRDF_ERR_UNSUPPORTED, "conv1_fwd: too large");
+  dim3 grid((w + kTile - 1) / kTile, (h + kTileY - 1) / kTileY, v), block(128);
   cudaStream_t st = (cudaStream_t)stream;
   if (downsample)
     desc_conv1_fwd_kernel<true><<<grid, block, 0, st>>>(renders, weight, bias, out_f32, (__nv_bfloat16*)out_bf16, h, w);

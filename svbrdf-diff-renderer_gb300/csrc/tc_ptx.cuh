@@ -114,6 +114,14 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+// Columns 0..3 of this warp's 32 TMEM lanes starting at `taddr`.
+__device__ __forceinline__ void tmem_ld4(uint32_t taddr, uint32_t (&r)[4]) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%4];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
 // Shared-memory matrix descriptor, 128-byte swizzle, for an MN-major operand: atoms of 64
 // (BF16) MN elements x 8 K rows, 128 bytes per K row; `lbo` = bytes between MN atoms, `sbo` =
 // bytes between 8-row K groups.

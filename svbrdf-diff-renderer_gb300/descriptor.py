@@ -59,7 +59,7 @@ HOOKS = ("conv1_1", "conv1_2", "conv3_2", "conv4_1")  # their ReLU outputs
 VGG19_TO_CONV4_2 = VGG19_TO_CONV4_1 + [("conv4_2", 512, 512)]
 REF_HOOKS = ("conv1_1", "conv1_2", "conv3_2", "conv4_2")
 
-EPI_NONE, EPI_BIAS_RELU, EPI_MASK, EPI_ADD_MASK = 0, 1, 2, 3
+EPI_NONE, EPI_BIAS_RELU, EPI_MASK, EPI_ADD_MASK, EPI_UNPOOL_MAX, EPI_UNPOOL_AVG = 0, 1, 2, 3, 4, 5
 
 
 def conv3x3_bf16(x: torch.Tensor, w: torch.Tensor, bias: Optional[torch.Tensor], epilogue: int,
@@ -132,6 +132,11 @@ class VGGDescriptor:
     ``load(targets)`` caches the target features (like ``VGGLoss.load``, src/descriptor.py:62-63);
     ``loss(renders)`` returns (feature_loss, gram_loss) as 0-d tensors, differentiable w.r.t.
     ``renders [V, 3, H, W]`` (H, W multiples of 16 after the 2x2 downsample).
+    ``fuse_pool`` (default False): True runs each pool's backward pass in the epilogue of the
+    data gradient of the convolution above it instead of its own kernel. The fused epilogue
+    reads the pool's input and the hook gradient at four window positions per lane (16 bytes
+    each, 256 bytes apart) and measured slower than the separate kernels at the descriptor's
+    sizes.
     """
 
     def __init__(self, device="cuda", seed: int = 0, weights: Sequence[float] = (0.25, 0.25, 0.25, 0.25),
@@ -147,6 +152,7 @@ class VGGDescriptor:
         self.gram = not ref
         self.hook_weights = list(weights)
         self.downsample = (not ref) if downsample is None else downsample
+        self.fuse_pool = False
         self.err = torch.zeros(1, dtype=torch.int32, device=self.device)
         raw = he_normal_weights(seed, self.layers)
         self.params = {}
@@ -158,6 +164,13 @@ class VGGDescriptor:
                 # forward: [Cout, tap, Cin]; data gradient: [Cin, tap, Cout] with the taps flipped
                 entry["w_fwd"] = wb.permute(0, 2, 3, 1).reshape(cout, 9, cin).contiguous().to(self.device)
                 entry["w_dg"] = wb.flip(2, 3).permute(1, 2, 3, 0).reshape(cin, 9, cout).contiguous().to(self.device)
+            else:
+                # conv1_1's data gradient on the tensor cores: [16, tap, 64], rows 3..15 zero
+                w16 = torch.zeros(16, 9, cout, dtype=torch.bfloat16)
+                w16[:cin] = wb.flip(2, 3).permute(1, 2, 3, 0).reshape(cin, 9, cout)
+                entry["w_dg16"] = w16.contiguous().to(self.device)
+                sc = torch.tensor([1.0 / s for s in STD], dtype=torch.float32)
+                entry["dg_scale"] = (sc * (0.25 if self.downsample else 1.0)).to(self.device)
             self.params[name] = entry
         self.target = None
 
@@ -277,14 +290,18 @@ class VGGDescriptor:
     def _backward(self, acts, grads, render_shape):
         """d(loss)/d renders from the hook gradients, layer by layer in reverse:
         data-gradient convolutions whose epilogue adds the next hook's gradient and applies
-        the ReLU mask below, max-pool backward fused the same way, and conv1_1's data
-        gradient back through the normalisation and the downsample."""
+        the ReLU mask below; each pool's backward (routing, the hook gradient of the convolution
+        under it, that ReLU's mask) as its own kernel, or with ``fuse_pool`` in the epilogue of
+        the data gradient of the convolution above it, which then writes the gradient at the
+        pool's input; then conv1_1's data gradient (tensor cores) back through the
+        normalisation and the downsample."""
         L = N.lib()
         st = N.stream_handle(self.device)
         items = self.layers
         pool_bwd = L.svbrdf_desc_avgpool_bwd if self.avg_pool else L.svbrdf_desc_pool_bwd
         g = grads[items[-1][0]]  # masked gradient at the last ReLU
-        for i in range(len(items) - 1, 0, -1):
+        i = len(items) - 1
+        while i > 0:
             item, below = items[i], items[i - 1]
             x = acts[i - 1]  # the input of layer i: a ReLU output, or a pool output
             n_, h, w, c = x.shape
@@ -294,22 +311,32 @@ class VGGDescriptor:
                 add = grads.get(below[0])
                 N.check(pool_bwd(g.data_ptr(), x.data_ptr(), N.ptr(add), gx.data_ptr(), n_, h, w, c, st))
                 g = gx
+                i -= 1
                 continue
             q = self.params[item[0]]
-            gx = torch.empty(n_, h, w, c, device=self.device, dtype=torch.bfloat16)
-            if below == "pool":
+            step = 1
+            if below == "pool" and self.fuse_pool:
+                xp = acts[i - 2]  # the pool's input, a ReLU output
+                gx = torch.empty_like(xp)
+                add = grads.get(items[i - 2][0])
+                epi, mask = (EPI_UNPOOL_AVG if self.avg_pool else EPI_UNPOOL_MAX), xp
+                step = 2
+            elif below == "pool":
+                gx = torch.empty(n_, h, w, c, device=self.device, dtype=torch.bfloat16)
                 epi, mask, add = EPI_NONE, None, None
             else:
+                gx = torch.empty(n_, h, w, c, device=self.device, dtype=torch.bfloat16)
                 add = grads.get(below[0])
                 epi, mask = (EPI_ADD_MASK if add is not None else EPI_MASK), x
             N.check(L.svbrdf_conv3x3_bf16_ex(g.data_ptr(), q["w_dg"].data_ptr(), None, N.ptr(mask), N.ptr(add),
                                              gx.data_ptr(), n_, h, w, item[2], item[1], epi, self.err.data_ptr(), st))
             g = gx
+            i -= step
         v, h, w, _ = g.shape
         dr = torch.empty(render_shape, device=self.device, dtype=torch.float32)
         p = self.params["conv1_1"]
-        N.check(L.svbrdf_desc_conv1_bwd(g.data_ptr(), p["w32"].data_ptr(), dr.data_ptr(), v, h, w,
-                                        int(self.downsample), st))
+        N.check(L.svbrdf_desc_conv1_bwd_tc(g.data_ptr(), p["w_dg16"].data_ptr(), p["dg_scale"].data_ptr(),
+                                           dr.data_ptr(), v, h, w, int(self.downsample), self.err.data_ptr(), st))
         return dr
 
     def features(self, renders: torch.Tensor) -> List[torch.Tensor]:

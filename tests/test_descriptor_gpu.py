@@ -85,6 +85,96 @@ def test_conv3x3_tc_add_mask_epilogue(svb, cuda, n, h, w, c):
     assert rel_l2(out.float(), ref) <= 1e-2
 
 
+@pytest.mark.parametrize("avg,with_add", [(False, True), (False, False), (True, True)])
+def test_conv3x3_unpool_epilogue(svb, cuda, avg, with_add):
+    """The pool-backward epilogues: the data gradient at a 2x2 pool's output (h x w) routed to
+    the pool's input (the window's first maximum, or a quarter each), plus the hook gradient
+    there, times the ReLU mask, against torch on the same BF16 operands."""
+    D = svb.descriptor
+    L = svb._native.lib()
+    n, h, w, cin, cout = 3, 32, 16, 128, 64
+    g = torch.Generator().manual_seed(7 + 2 * int(avg) + int(with_add))
+    gy = torch.randn(n, h, w, cin, generator=g).to(cuda, torch.bfloat16)
+    wt = (torch.randn(cout, 9, cin, generator=g) * (2.0 / (9 * cin)) ** 0.5).to(cuda, torch.bfloat16)
+    x = torch.randn(n, 2 * h, 2 * w, cout, generator=g).to(cuda, torch.bfloat16)  # the pool's input
+    add = torch.randn(n, 2 * h, 2 * w, cout, generator=g).to(cuda, torch.bfloat16) if with_add else None
+    out = torch.full((n, 2 * h, 2 * w, cout), float("nan"), device=cuda, dtype=torch.bfloat16)
+    err = torch.zeros(1, dtype=torch.int32, device=cuda)
+    epi = D.EPI_UNPOOL_AVG if avg else D.EPI_UNPOOL_MAX
+    svb._native.check(L.svbrdf_conv3x3_bf16_ex(gy.data_ptr(), wt.data_ptr(), None, x.data_ptr(),
+                                               svb._native.ptr(add), out.data_ptr(), n, h, w, cin, cout, epi,
+                                               err.data_ptr(), svb._native.stream_handle(cuda)))
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    gp = _ref_conv(gy, wt).permute(0, 3, 1, 2)  # [n, cout, h, w], FP32
+    xf = x.float().permute(0, 3, 1, 2)
+    if avg:
+        routed = gp.repeat_interleave(2, 2).repeat_interleave(2, 3) * 0.25
+    else:
+        _, idx = torch.nn.functional.max_pool2d(xf, 2, return_indices=True)
+        routed = torch.nn.functional.max_unpool2d(gp, idx, 2, output_size=xf.shape[-2:])
+    if add is not None:
+        routed = routed + add.float().permute(0, 3, 1, 2)
+    want = (routed * (xf > 0)).permute(0, 2, 3, 1)
+    assert not torch.isnan(out.float()).any()
+    assert rel_l2(out.float(), want) <= 1e-2
+
+
+def test_descriptor_fused_pool_backward_matches_separate(svb, cuda):
+    """The descriptor's render gradient with each pool's backward in the epilogue of the
+    convolution above it equals the chain with separate pool kernels (up to the BF16 rounding
+    of the pooled gradient, which the fused form skips), in both modes."""
+    from oracle import microfacet_ref as R
+
+    sc = svb.scenes.single_scene(res=256, seed=1012)
+    tgt = R.render(sc.gt, sc.camera_pos[:2], sc.light_pos[:2], sc.light_pow, sc.size, torch.float32).to(cuda)
+    cur = R.render(0.5 * sc.gt + 0.5 * sc.init, sc.camera_pos[:2], sc.light_pos[:2], sc.light_pow, sc.size,
+                   torch.float32).to(cuda)
+    for mode in ("config", "reference"):
+        d = svb.descriptor.VGGDescriptor(cuda, seed=5, mode=mode)
+        d.load(tgt)
+        out = []
+        for fuse in (True, False):
+            d.fuse_pool = fuse
+            r = cur.clone().requires_grad_(True)
+            fl, gl = d.loss(r)
+            (fl + gl).backward()
+            out.append((float(fl.detach()), r.grad.clone()))
+        torch.cuda.synchronize()
+        assert d.device_error() == 0
+        assert out[0][0] == out[1][0]  # the forward pass is the same
+        assert rel_l2(out[0][1], out[1][1]) <= 2e-2, mode
+
+
+@pytest.mark.parametrize("v,h,w,down", [(2, 64, 48, 1), (3, 32, 16, 0), (1, 24, 32, 1)])
+def test_conv1_bwd_tc_matches_torch(svb, cuda, v, h, w, down):
+    """conv1_1's data gradient on the tensor cores (64 -> 3 channels, N = 16) through the
+    normalisation and the downsample's adjoint, against torch's conv2d_input on the same BF16
+    weights and gradient, and against the CUDA-core kernel."""
+    N = svb._native
+    L = N.lib()
+    st = N.stream_handle(cuda)
+    d = svb.descriptor.VGGDescriptor(cuda, seed=9, downsample=bool(down))
+    p = d.params["conv1_1"]
+    g = torch.Generator().manual_seed(h + w + down)
+    gz = torch.randn(v, h, w, 64, generator=g).to(cuda, torch.bfloat16)
+    rh, rw = (2 * h, 2 * w) if down else (h, w)
+    dr = torch.full((v, 3, rh, rw), float("nan"), device=cuda)
+    dr_cc = torch.empty_like(dr)
+    err = torch.zeros(1, dtype=torch.int32, device=cuda)
+    N.check(L.svbrdf_desc_conv1_bwd_tc(gz.data_ptr(), p["w_dg16"].data_ptr(), p["dg_scale"].data_ptr(),
+                                       dr.data_ptr(), v, h, w, down, err.data_ptr(), st))
+    N.check(L.svbrdf_desc_conv1_bwd(gz.data_ptr(), p["w32"].data_ptr(), dr_cc.data_ptr(), v, h, w, down, st))
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    gn = torch.nn.grad.conv2d_input((v, 3, h, w), p["w32"], gz.float().permute(0, 3, 1, 2), padding=1)
+    gn = gn / torch.tensor(svb.descriptor.STD, device=cuda).view(1, 3, 1, 1)
+    want = (0.25 * gn).repeat_interleave(2, 2).repeat_interleave(2, 3) if down else gn
+    assert not torch.isnan(dr).any()
+    assert rel_l2(dr, want) <= 1e-5
+    assert rel_l2(dr, dr_cc) <= 1e-5
+
+
 def test_conv3x3_rejects_bad_shapes(svb, cuda):
     D = svb.descriptor
     err = torch.zeros(1, dtype=torch.int32, device=cuda)

@@ -301,9 +301,11 @@ def test_texel_count_limit_rejected_on_host(lib):
         assert lib.svbrdf_fused_step_noalloc(*(args[:19] + [None])) == -2
 
 
-def test_new_entry_points_reject_bad_arguments_on_host(lib):
-    """The batched render, the loss sums, the fused Gram-gradient GEMM and the TF32 convolution
-    with a workspace refuse bad arguments before touching the device (nothing is launched)."""
+def test_batched_render_loss_sums_and_conv_entries_reject_bad_arguments_on_host(lib):
+    """The batched render, the loss sums, the fused Gram-gradient GEMM, the TF32 convolution
+    with a workspace, the pool-backward and render epilogues of the BF16 convolution and
+    conv1_1's tensor-core data gradient refuse bad arguments before touching the device
+    (nothing is launched)."""
     fake = ctypes.c_void_p(16)
     # batched render: batch must be >= 1; the per-material shape checks still apply
     assert lib.svbrdf_render_fwd_batch(fake, fake, fake, fake, 9, 8, 8, 17.0, 0, fake, None, -1, None, None, 0,
@@ -334,3 +336,10 @@ def test_new_entry_points_reject_bad_arguments_on_host(lib):
     # TF32 convolution with a workspace: the same shape rules as without
     assert lib.svbrdf_gen_conv_tf32_ex(fake, fake, fake, None, 0, 1, 8, 8, 48, 64, 3, 1, err, None) == -2
     assert lib.svbrdf_gen_conv_tf32_ex(fake, fake, fake, None, 0, 1, 8, 8, 64, 64, 5, 1, err, None) == -1
+    # BF16 convolution: epilogues 4 and 5 (pool backward) need the pool's input as mask; 6 and
+    # up are not epilogues of this entry
+    assert lib.svbrdf_conv3x3_bf16_ex(fake, fake, None, None, None, fake, 1, 16, 16, 64, 64, 4, err, None) == -1
+    assert lib.svbrdf_conv3x3_bf16_ex(fake, fake, None, fake, None, fake, 1, 16, 16, 64, 64, 6, err, None) == -1
+    # conv1_1's tensor-core data gradient: shape granularity and null pointers
+    assert lib.svbrdf_desc_conv1_bwd_tc(fake, fake, fake, fake, 1, 12, 16, 1, err, None) == -2
+    assert lib.svbrdf_desc_conv1_bwd_tc(fake, None, fake, fake, 1, 16, 16, 1, err, None) == -1

@@ -568,7 +568,10 @@ extern "C" int svbrdf_conv3x3_bf16_ex(const void* x, const void* weight, const f
   PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
   int rc = get_tensor_map_encoder(&g_encode);
   if (rc) return rc;
-  const int bn = (cout % 256 == 0) ? 256 : (cout % 128 == 0 ? 128 : 64);
+  // BN = 256 (one M-tile) only on maps under 32 rows: elsewhere BN = 128 with two M-tiles has
+  // the same MMA time per tap (N = 128 issues at 98 % of the N = 256 rate) and streams half the
+  // weight bytes per output, which is what limits a 128 x 256 tile
+  const int bn = (cout % 256 == 0 && h < 32) ? 256 : (cout % 128 == 0 ? 128 : 64);
   CUtensorMap mw;
   {
     const cuuint64_t dims[2] = {(cuuint64_t)9 * cin, (cuuint64_t)cout};

@@ -561,9 +561,13 @@ static int plan_conv(int b, int hin, int win, int cin, int cout, int ksize, int 
     // 16-row x 8-column patches, two stacked where the map has 32+ rows and Cout fits two
     // double-buffered accumulators in TMEM (BN <= 128; a 256 x 256 tile would fill TMEM with
     // one accumulator, and the exposed epilogue then costs more than the halved weight
-    // traffic saves: measured 5-35 % slower on the generator's 32^2-128^2 layers). K splits
-    // count 32-channel chunks (all taps each).
+    // traffic saves: measured 5-35 % slower on the generator's 32^2-128^2 layers). Wide
+    // layers (Cout >= 256) on such maps take BN = 128 with two M-tiles rather than BN = 256
+    // with one: the same MMA time per tap (an N = 128 MMA issues at 98 % of the N = 256 rate)
+    // for half the weight bytes per output, which a 128 x 256 tile streams from L2 at about
+    // 90 GB/s per SM, its limit. K splits count 32-channel chunks (all taps each).
     g.TW = 8; g.TH = 16; g.NB = 1;
+    if (pl->bn == 256 && g.Ho >= 32) pl->bn = 128;
     pl->mt = (g.Ho >= 32 && pl->bn <= 128) ? 2 : 1;
     g.tiles_x = (g.Wo + 7) / 8;
     g.tiles_y = (g.Ho + 16 * pl->mt - 1) / (16 * pl->mt);

@@ -56,9 +56,8 @@ enum ConvError : int { kErrTma = 11, kErrMma = 12, kErrEpi = 13 };
 // One accumulator row (an output pixel) of 32 channels through the epilogue, stored as BF16;
 // `mv` and `av` hold the row's 32 mask and addend values (BF16, 4 x 16 bytes each).
 template <int EPI>
-__device__ __forceinline__ void epilogue_apply32(const uint32_t (&r)[32], const float* __restrict__ bias,
-                                                 const uint4 (&mv)[4], const uint4 (&av)[4], __nv_bfloat16* out,
-                                                 size_t off, int nc) {
+__device__ __forceinline__ void epilogue_values32(const uint32_t (&r)[32], const float* __restrict__ bias,
+                                                  const uint4 (&mv)[4], const uint4 (&av)[4], int nc, uint4 (&pk)[4]) {
   float v[32];
 #pragma unroll
   for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
@@ -89,20 +88,27 @@ __device__ __forceinline__ void epilogue_apply32(const uint32_t (&r)[32], const 
       }
     }
   }
-  uint4* op = reinterpret_cast<uint4*>(out + off);
 #pragma unroll
   for (int u = 0; u < 4; ++u) {
-    uint4 pk;
     __nv_bfloat162 h0 = __floats2bfloat162_rn(v[u * 8 + 0], v[u * 8 + 1]);
     __nv_bfloat162 h1 = __floats2bfloat162_rn(v[u * 8 + 2], v[u * 8 + 3]);
     __nv_bfloat162 h2 = __floats2bfloat162_rn(v[u * 8 + 4], v[u * 8 + 5]);
     __nv_bfloat162 h3 = __floats2bfloat162_rn(v[u * 8 + 6], v[u * 8 + 7]);
-    pk.x = *reinterpret_cast<uint32_t*>(&h0);
-    pk.y = *reinterpret_cast<uint32_t*>(&h1);
-    pk.z = *reinterpret_cast<uint32_t*>(&h2);
-    pk.w = *reinterpret_cast<uint32_t*>(&h3);
-    op[u] = pk;
+    pk[u].x = *reinterpret_cast<uint32_t*>(&h0);
+    pk[u].y = *reinterpret_cast<uint32_t*>(&h1);
+    pk[u].z = *reinterpret_cast<uint32_t*>(&h2);
+    pk[u].w = *reinterpret_cast<uint32_t*>(&h3);
   }
+}
+template <int EPI>
+__device__ __forceinline__ void epilogue_apply32(const uint32_t (&r)[32], const float* __restrict__ bias,
+                                                 const uint4 (&mv)[4], const uint4 (&av)[4], __nv_bfloat16* out,
+                                                 size_t off, int nc) {
+  uint4 pk[4];
+  epilogue_values32<EPI>(r, bias, mv, av, nc, pk);
+  uint4* op = reinterpret_cast<uint4*>(out + off);
+#pragma unroll
+  for (int u = 0; u < 4; ++u) op[u] = pk[u];
 }
 
 // The row's mask (and addend) values, 4 x 16 bytes each, for epilogue_apply32.
@@ -201,25 +207,33 @@ __device__ __forceinline__ void epilogue_unpool32(const uint32_t (&r)[32], const
 // rows of M-tile mt are the patch's 16 rows of 8 pixels: 8-row group r of tap (ky, kx) starts at
 // patch pixel (16 mt + r + ky) x 10 + kx, so a tap is the patch's descriptor moved by
 // (10 ky + kx) pixels, with 8-row groups 10 pixels (1280 bytes) apart (SBO). The weight slices
-// [BN][64] stream through their own ring, TPS taps per stage. Per chunk the tile loads
-// (16 MT + 2) x 10 x 128 bytes of input instead of 9 x MT x 16 KB.
+// [BN][64] stream through their own ring, TPS taps per stage; with RESB (one 64-channel chunk,
+// one Cout block: conv1_2 and its data gradient) all 9 slices are one stage, loaded once per
+// CTA and never released. Per chunk the tile loads (16 MT + 2) x 10 x 128 bytes of input instead
+// of 9 x MT x 16 KB.
+// TST (BN = 64, MT = 2, epilogues 0..3): each epilogue warp writes its 32 pixels x 64 channels,
+// BF16, into its own 4 KB block of shared memory (128-byte rows, 128-byte swizzled) and one lane
+// stores the block with a TMA tensor store (`tmap_y`, box 64 x 8 x 4), instead of 2048 16-byte
+// stores per tile spread over 128-byte strides.
 template <int MT>
 struct Halo {
   static constexpr int kRows = 16 * MT + 2, kCols = 10;
   static constexpr int kABytes = ((kRows * kCols * 128 + 1023) / 1024) * 1024;  // one 64-channel chunk
 };
 
-template <int BN, int MT, int AST, int BST, int EPI, int TPS>
+template <int BN, int MT, int AST, int BST, int EPI, int TPS, bool RESB, bool TST>
 __global__ void __launch_bounds__(kThreads, 1)
 conv3x3_halo_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_constant__ CUtensorMap tmap_w,
-                    const float* __restrict__ bias, const __nv_bfloat16* __restrict__ mask,
-                    const __nv_bfloat16* __restrict__ addend, __nv_bfloat16* __restrict__ y, int N, int H, int W,
-                    int Cin, int Cout, int* err) {
+                    const __grid_constant__ CUtensorMap tmap_y, const float* __restrict__ bias,
+                    const __nv_bfloat16* __restrict__ mask, const __nv_bfloat16* __restrict__ addend,
+                    __nv_bfloat16* __restrict__ y, int N, int H, int W, int Cin, int Cout, int* err) {
   using HP = Halo<MT>;
   constexpr int B_BYTES = BN * BK * 2;  // one tap's weight slice
   constexpr int S_BYTES = TPS * B_BYTES;  // one weight stage
   constexpr int GROUPS = 9 / TPS;
-  static_assert(TPS == 1 || TPS == 3, "a weight stage holds one tap or one kernel row");
+  static_assert(TPS == 1 || TPS == 3 || TPS == 9, "a weight stage holds one tap, a kernel row or all 9");
+  static_assert(!RESB || (TPS == 9 && BST == 1), "resident weights: one stage of all 9 taps");
+  static_assert(!TST || (BN == 64 && MT == 2 && EPI <= kEpiAddMask), "TMA-store epilogue: BN 64, MT 2, epilogues 0..3");
   constexpr uint32_t ACC_COLS = MT * BN;
   constexpr uint32_t TMEM_COLS = 2 * ACC_COLS;
   static_assert(TMEM_COLS >= 32 && TMEM_COLS <= 512 && (TMEM_COLS & (TMEM_COLS - 1)) == 0, "TMEM columns");
@@ -231,6 +245,7 @@ conv3x3_halo_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_con
 
   const uint32_t bbase = (smem_u32(dsmem) + 1023u) & ~1023u;  // weight ring, then the halo ring
   const uint32_t abase = bbase + (uint32_t)(BST * S_BYTES);
+  const uint32_t sbase = abase + (uint32_t)(AST * HP::kABytes);  // TST: 8 x 4 KB output blocks
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int tiles_x = W / 8, tiles_y = (H + 16 * MT - 1) / (16 * MT), tiles_n = Cout / BN;
   const int n_tiles = N * tiles_y * tiles_x * tiles_n;
@@ -289,7 +304,7 @@ conv3x3_halo_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_con
           mbar_expect_tx(fa, (uint32_t)(HP::kRows * HP::kCols * 128));
           tma_4d(abase + (uint32_t)(sa * HP::kABytes), &tmap_x, cc * BK, x0 - 1, y0 - 1, img, fa);
           ++qa;
-          for (int grp = 0; grp < GROUPS; ++grp) {
+          for (int grp = 0; grp < GROUPS && (!RESB || qb == 0); ++grp) {
             const int sb = qb % BST;
             if (qb >= BST && !mbar_wait(smem_u32(&bempty[sb]), ((uint32_t)(qb / BST) & 1u) ^ 1u, err, kErrTma)) {
               bad = true;
@@ -337,7 +352,7 @@ conv3x3_halo_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_con
           const uint32_t achunk = abase + (uint32_t)(sa * HP::kABytes);
           for (int grp = 0; grp < GROUPS; ++grp) {
             const int sb = qb % BST;
-            if (!mbar_wait(smem_u32(&bfull[sb]), (uint32_t)(qb / BST) & 1u, err, kErrMma)) {
+            if ((!RESB || qb == 0) && !mbar_wait(smem_u32(&bfull[sb]), (uint32_t)(qb / BST) & 1u, err, kErrMma)) {
               bad = true;
               break;
             }
@@ -357,8 +372,12 @@ conv3x3_halo_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_con
                            sw128_desc(bs + 32u * k), idesc, (cc > 0 || tap > 0 || k > 0) ? 1u : 0u);
               }
             }
-            mma_commit(smem_u32(&bempty[sb]));
-            ++qb;
+            if (!RESB) {
+              mma_commit(smem_u32(&bempty[sb]));
+              ++qb;
+            } else {
+              qb = 1;
+            }
           }
           if (bad) break;
           mma_commit(smem_u32(&aempty[sa]));
@@ -393,6 +412,8 @@ conv3x3_halo_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_con
       for (int q = 0; q < PF; ++q) {
         const int mt = mt0 + q / CPH, c0 = cbase + (q % CPH) * 32;
         const int py = y0 + 16 * mt + m / 8, px = x0 + m % 8;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) pm[q][u] = pa[q][u] = make_uint4(0u, 0u, 0u, 0u);
         if (py < H) epilogue_load32<EPI>(mask, addend, (((size_t)img * H + py) * W + px) * Cout + n0 + c0, pm[q], pa[q]);
       }
       const bool ok = __all_sync(0xffffffffu, mbar_wait(smem_u32(&tfull_bar[a]), (uint32_t)(j >> 1) & 1u, err,
@@ -400,6 +421,10 @@ conv3x3_halo_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_con
                       *(volatile int*)err == 0;
       fence_after();
       if (!ok) break;
+      if (TST && j > 0) {  // the previous tile's store has read this warp's block
+        if (lane == 0) bulk_wait_read0();
+        __syncwarp();
+      }
 #pragma unroll
       for (int q = 0; q < NCH; ++q) {
         const int mt = mt0 + q / CPH, c0 = cbase + (q % CPH) * 32;
@@ -407,7 +432,26 @@ conv3x3_halo_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_con
         const size_t off = (((size_t)img * H + py) * W + px) * Cout + n0 + c0;
         uint32_t r[32];
         tmem_ld32(tmem + ((uint32_t)(qw * 32) << 16) + (uint32_t)(a * ACC_COLS + mt * BN + c0), r);
-        if (EPI == kEpiUnpoolMax || EPI == kEpiUnpoolAvg) {
+        if (TST) {
+          // row `lane` of this warp's block, 16-byte chunk c0 / 8 + u at its swizzled position
+          uint4 pk[4], mv[4], av[4];
+          if (q < PF) {
+            epilogue_values32<EPI>(r, bias, pm[q < PF ? q : 0], pa[q < PF ? q : 0], n0 + c0, pk);
+          } else {
+#pragma unroll
+            for (int u = 0; u < 4; ++u) mv[u] = av[u] = make_uint4(0u, 0u, 0u, 0u);
+            if (py < H) epilogue_load32<EPI>(mask, addend, off, mv, av);
+            epilogue_values32<EPI>(r, bias, mv, av, n0 + c0, pk);
+          }
+          const uint32_t row = sbase + (uint32_t)((warp - 2) * 4096 + lane * 128);
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const uint32_t a16 = row + (uint32_t)((((c0 >> 3) + u) ^ (lane & 7)) * 16);
+            asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(a16), "r"(pk[u].x), "r"(pk[u].y),
+                         "r"(pk[u].z), "r"(pk[u].w)
+                         : "memory");
+          }
+        } else if (EPI == kEpiUnpoolMax || EPI == kEpiUnpoolAvg) {
           if (py < H) {
             const size_t rs = (size_t)2 * W * Cout;
             const size_t base = ((size_t)img * 2 * H + 2 * py) * rs + (size_t)2 * px * Cout + n0 + c0;
@@ -421,6 +465,14 @@ conv3x3_halo_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_con
             epilogue_load32<EPI>(mask, addend, off, mv, av);
             epilogue_apply32<EPI>(r, bias, mv, av, y, off, n0 + c0);
           }
+        }
+      }
+      if (TST) {  // the warp's 4 patch rows x 8 pixels x 64 channels, one tensor store
+        fence_async_smem();
+        __syncwarp();
+        if (lane == 0) {
+          tma_store_4d(&tmap_y, sbase + (uint32_t)((warp - 2) * 4096), n0, x0, y0 + 16 * mt0 + 4 * qw, img);
+          bulk_commit();
         }
       }
       if ((EPI == kEpiRenderDown || EPI == kEpiRender) && half == 0) {
@@ -450,6 +502,7 @@ conv3x3_halo_kernel(const __grid_constant__ CUtensorMap tmap_x, const __grid_con
       __syncwarp();
       if (lane == 0) mbar_arrive(smem_u32(&tempty_bar[a]));
     }
+    if (TST && lane == 0) bulk_wait0();  // the stores have finished with shared memory
   }
   fence_before();
   __syncthreads();
@@ -485,23 +538,30 @@ template <int BN>
 constexpr int halo_tps() {
   return BN <= 128 ? 3 : 1;
 }
-// Weight-ring depth: as many stages as fit beside two input slots, up to 16 taps in flight.
-template <int BN, int MT>
+constexpr size_t kStagingBytes = (size_t)kEpiWarps * 4096;  // TST: one 4 KB output block per epilogue warp
+// Weight-ring depth: as many stages as fit beside two input slots (and the TST output blocks),
+// up to 16 taps in flight.
+template <int BN, int MT, bool TST>
 constexpr int halo_bstages() {
   constexpr size_t stage = (size_t)halo_tps<BN>() * BN * BK * 2;
-  constexpr int fit = (int)((kStageBudget - 2 * (size_t)Halo<MT>::kABytes) / stage);
+  constexpr int fit = (int)((kStageBudget - 2 * (size_t)Halo<MT>::kABytes - (TST ? kStagingBytes : 0)) / stage);
   constexpr int cap = 16 / halo_tps<BN>();
   return fit < cap ? fit : cap;
 }
 
-template <int BN, int MT, int EPI>
-static int launch_halo(const CUtensorMap& mx, const CUtensorMap& mw, const float* bias, const void* mask,
-                       const void* addend, void* y, int n, int h, int w, int cin, int cout, int* err, cudaStream_t st) {
-  constexpr int TPS = halo_tps<BN>();
-  constexpr int BST = halo_bstages<BN, MT>();
-  static_assert(BST >= 2 && BST * TPS >= 5, "weight ring too shallow");
-  auto kern = conv3x3_halo_kernel<BN, MT, 2, BST, EPI, TPS>;
-  const size_t smem = (size_t)BST * TPS * BN * BK * 2 + 2 * (size_t)Halo<MT>::kABytes + 1024;
+template <int BN, int MT, int EPI, bool RESB, bool TST>
+static int launch_variant(const CUtensorMap& mx, const CUtensorMap& mw, const CUtensorMap& my, const float* bias,
+                          const void* mask, const void* addend, void* y, int n, int h, int w, int cin, int cout,
+                          int* err, cudaStream_t st) {
+  constexpr int TPS = RESB ? 9 : halo_tps<BN>();
+  constexpr int BST = RESB ? 1 : halo_bstages<BN, MT, TST>();
+  static_assert(RESB || (BST >= 2 && BST * TPS >= 5), "weight ring too shallow");
+  auto kern = conv3x3_halo_kernel<BN, MT, 2, BST, EPI, TPS, RESB, TST>;
+  const size_t smem = (size_t)BST * TPS * BN * BK * 2 + 2 * (size_t)Halo<MT>::kABytes + (TST ? kStagingBytes : 0) +
+                      1024;
+  static_assert((size_t)BST * TPS * BN * BK * 2 + 2 * (size_t)Halo<MT>::kABytes + (TST ? kStagingBytes : 0) + 1024 <=
+                    227 * 1024,
+                "shared memory");
   static std::atomic<bool> attr[64];
   static std::atomic<int> sms[64];
   int dev = 0;
@@ -521,25 +581,41 @@ static int launch_halo(const CUtensorMap& mx, const CUtensorMap& mw, const float
   const long long tiles = (long long)n * ((h + 16 * MT - 1) / (16 * MT)) * (w / 8) * (cout / BN);
   if (tiles >= (1LL << 31)) return fail(SVBRDF_ERR_UNSUPPORTED, "conv3x3: too many tiles");
   const int grid = (int)(tiles < sms[dev].load() ? tiles : sms[dev].load());
-  kern<<<grid, kThreads, smem, st>>>(mx, mw, bias, (const __nv_bfloat16*)mask, (const __nv_bfloat16*)addend,
+  kern<<<grid, kThreads, smem, st>>>(mx, mw, my, bias, (const __nv_bfloat16*)mask, (const __nv_bfloat16*)addend,
                                      (__nv_bfloat16*)y, n, h, w, cin, cout, err);
   return check_launch("conv3x3_halo_kernel");
 }
 
+// `my`: the output's tensor map for the TMA-store epilogue (BN = 64, MT = 2, epilogues 0..3), or
+// null; weights stay resident where the layer is one 64-channel chunk and one Cout block.
+template <int BN, int MT, int EPI>
+static int launch_halo(const CUtensorMap& mx, const CUtensorMap& mw, const CUtensorMap* my, const float* bias,
+                       const void* mask, const void* addend, void* y, int n, int h, int w, int cin, int cout, int* err,
+                       cudaStream_t st) {
+  if constexpr (BN == 64 && MT == 2 && EPI <= kEpiAddMask) {
+    if (my) {
+      if (cin == BK && cout == BN)
+        return launch_variant<BN, MT, EPI, true, true>(mx, mw, *my, bias, mask, addend, y, n, h, w, cin, cout, err, st);
+      return launch_variant<BN, MT, EPI, false, true>(mx, mw, *my, bias, mask, addend, y, n, h, w, cin, cout, err, st);
+    }
+  }
+  return launch_variant<BN, MT, EPI, false, false>(mx, mw, mx, bias, mask, addend, y, n, h, w, cin, cout, err, st);
+}
+
 template <int BN, int MT>
-static int dispatch_halo(int epi, const CUtensorMap& mx, const CUtensorMap& mw, const float* bias, const void* mask,
-                         const void* addend, void* y, int n, int h, int w, int cin, int cout, int* err,
-                         cudaStream_t st) {
+static int dispatch_halo(int epi, const CUtensorMap& mx, const CUtensorMap& mw, const CUtensorMap* my,
+                         const float* bias, const void* mask, const void* addend, void* y, int n, int h, int w, int cin,
+                         int cout, int* err, cudaStream_t st) {
   switch (epi) {
-    case kEpiNone: return launch_halo<BN, MT, kEpiNone>(mx, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st);
+    case kEpiNone: return launch_halo<BN, MT, kEpiNone>(mx, mw, my, bias, mask, addend, y, n, h, w, cin, cout, err, st);
     case kEpiBiasRelu:
-      return launch_halo<BN, MT, kEpiBiasRelu>(mx, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st);
-    case kEpiMask: return launch_halo<BN, MT, kEpiMask>(mx, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st);
+      return launch_halo<BN, MT, kEpiBiasRelu>(mx, mw, my, bias, mask, addend, y, n, h, w, cin, cout, err, st);
+    case kEpiMask: return launch_halo<BN, MT, kEpiMask>(mx, mw, my, bias, mask, addend, y, n, h, w, cin, cout, err, st);
     case kEpiAddMask:
-      return launch_halo<BN, MT, kEpiAddMask>(mx, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st);
+      return launch_halo<BN, MT, kEpiAddMask>(mx, mw, my, bias, mask, addend, y, n, h, w, cin, cout, err, st);
     case kEpiUnpoolMax:
-      return launch_halo<BN, MT, kEpiUnpoolMax>(mx, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st);
-    default: return launch_halo<BN, MT, kEpiUnpoolAvg>(mx, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st);
+      return launch_halo<BN, MT, kEpiUnpoolMax>(mx, mw, my, bias, mask, addend, y, n, h, w, cin, cout, err, st);
+    default: return launch_halo<BN, MT, kEpiUnpoolAvg>(mx, mw, my, bias, mask, addend, y, n, h, w, cin, cout, err, st);
   }
 }
 
@@ -598,14 +674,27 @@ extern "C" int svbrdf_conv3x3_bf16_ex(const void* x, const void* weight, const f
                                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                                 CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(SVBRDF_ERR_CUDA, "cuTensorMapEncodeTiled(halo x) failed: %d", (int)r);
+    // the output as 64-channel x 8 x 4 boxes for the TMA-store epilogue (BN 64, MT 2)
+    CUtensorMap my;
+    const CUtensorMap* pmy = nullptr;
+    if (bn == 64 && mt == 2 && epilogue <= kEpiAddMask) {
+      const cuuint64_t ydims[4] = {(cuuint64_t)cout, (cuuint64_t)w, (cuuint64_t)h, (cuuint64_t)n};
+      const cuuint64_t ystrides[3] = {(cuuint64_t)cout * 2, (cuuint64_t)w * cout * 2, (cuuint64_t)h * w * cout * 2};
+      const cuuint32_t ybox[4] = {64u, 8u, 4u, 1u};
+      const CUresult ry = g_encode(&my, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, y, ydims, ystrides, ybox, es,
+                                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                   CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+      if (ry != CUDA_SUCCESS) return fail(SVBRDF_ERR_CUDA, "cuTensorMapEncodeTiled(y) failed: %d", (int)ry);
+      pmy = &my;
+    }
     switch (bn) {
-      case 256: return dispatch_halo<256, 1>(epilogue, mh, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st);
+      case 256: return dispatch_halo<256, 1>(epilogue, mh, mw, pmy, bias, mask, addend, y, n, h, w, cin, cout, err, st);
       case 128:
-        return mt == 2 ? dispatch_halo<128, 2>(epilogue, mh, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st)
-                       : dispatch_halo<128, 1>(epilogue, mh, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st);
+        return mt == 2 ? dispatch_halo<128, 2>(epilogue, mh, mw, pmy, bias, mask, addend, y, n, h, w, cin, cout, err, st)
+                       : dispatch_halo<128, 1>(epilogue, mh, mw, pmy, bias, mask, addend, y, n, h, w, cin, cout, err, st);
       default:
-        return mt == 2 ? dispatch_halo<64, 2>(epilogue, mh, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st)
-                       : dispatch_halo<64, 1>(epilogue, mh, mw, bias, mask, addend, y, n, h, w, cin, cout, err, st);
+        return mt == 2 ? dispatch_halo<64, 2>(epilogue, mh, mw, pmy, bias, mask, addend, y, n, h, w, cin, cout, err, st)
+                       : dispatch_halo<64, 1>(epilogue, mh, mw, pmy, bias, mask, addend, y, n, h, w, cin, cout, err, st);
     }
   }
 }
@@ -648,10 +737,10 @@ extern "C" int svbrdf_desc_conv1_bwd_tc(const void* gz, const void* w16, const f
   cudaStream_t st = (cudaStream_t)stream;
   void* y = dr;
   if (down)
-    return mt == 2 ? launch_halo<16, 2, kEpiRenderDown>(mh, mw, scale, nullptr, nullptr, y, n, h, w, 64, 16, err, st)
-                   : launch_halo<16, 1, kEpiRenderDown>(mh, mw, scale, nullptr, nullptr, y, n, h, w, 64, 16, err, st);
-  return mt == 2 ? launch_halo<16, 2, kEpiRender>(mh, mw, scale, nullptr, nullptr, y, n, h, w, 64, 16, err, st)
-                 : launch_halo<16, 1, kEpiRender>(mh, mw, scale, nullptr, nullptr, y, n, h, w, 64, 16, err, st);
+    return mt == 2 ? launch_halo<16, 2, kEpiRenderDown>(mh, mw, nullptr, scale, nullptr, nullptr, y, n, h, w, 64, 16, err, st)
+                   : launch_halo<16, 1, kEpiRenderDown>(mh, mw, nullptr, scale, nullptr, nullptr, y, n, h, w, 64, 16, err, st);
+  return mt == 2 ? launch_halo<16, 2, kEpiRender>(mh, mw, nullptr, scale, nullptr, nullptr, y, n, h, w, 64, 16, err, st)
+                 : launch_halo<16, 1, kEpiRender>(mh, mw, nullptr, scale, nullptr, nullptr, y, n, h, w, 64, 16, err, st);
 }
 
 extern "C" int svbrdf_conv3x3_bf16(const void* x, const void* weight, const float* bias, const void* mask, void* y,

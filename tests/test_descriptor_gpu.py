@@ -25,12 +25,14 @@ def _ref_conv(x_nhwc, w_cout_tap_cin, bias=None):
 
 @pytest.mark.parametrize("n,h,w,cin,cout", [(1, 8, 16, 64, 64), (2, 16, 32, 64, 128), (1, 24, 48, 128, 256),
                                             (2, 32, 32, 256, 512), (1, 8, 16, 192, 64), (4, 128, 128, 64, 64),
-                                            (3, 40, 96, 64, 128), (6, 64, 64, 64, 256)])
+                                            (3, 40, 96, 64, 128), (6, 64, 64, 64, 256), (2, 48, 32, 64, 64),
+                                            (3, 40, 32, 128, 64)])
 def test_conv3x3_tc_matches_torch(svb, cuda, n, h, w, cin, cout):
     """Every epilogue against torch's FP32 convolution of the same BF16 operands. The shapes
     cover one and two stacked patches per tile (H a multiple of 16 or not), 64/128/256-channel
-    accumulators, and maps with more tiles than SMs (several tiles per persistent CTA, both
-    TMEM accumulator buffers)."""
+    accumulators, maps with more tiles than SMs (several tiles per persistent CTA, both TMEM
+    accumulator buffers), and the TMA-store epilogue of 64-channel outputs with resident weights
+    (Cin 64) or a weight ring (Cin 128), with tiles that the store clips at the map's last row."""
     D = svb.descriptor
     g = torch.Generator().manual_seed(n * 1000 + cin)
     x = torch.randn(n, h, w, cin, generator=g).to(cuda, torch.bfloat16)
@@ -63,7 +65,7 @@ def test_conv3x3_tc_data_gradient(svb, cuda):
     assert rel_l2(gx.float(), ref.permute(0, 2, 3, 1)) <= 1e-2
 
 
-@pytest.mark.parametrize("n,h,w,c", [(4, 128, 128, 64), (9, 24, 32, 128)])
+@pytest.mark.parametrize("n,h,w,c", [(4, 128, 128, 64), (9, 24, 32, 128), (2, 48, 16, 64)])
 def test_conv3x3_tc_add_mask_epilogue(svb, cuda, n, h, w, c):
     """The backward pass's add+mask epilogue (data gradient + the hook's loss gradient, times
     the ReLU mask) against torch on the same BF16 operands."""

@@ -90,7 +90,8 @@ def test_adjoint_vs_fp64_finite_differences_1024(svb, oracle, cuda):
     loss.backward()
     g = torch.Generator().manual_seed(5)
     cand = torch.randint(0, 1024, (256, 2), generator=g).tolist()
-    ok = [(i, j) for i, j in cand if 2e-3 < float(out[:, :, i, j].min()) and float(out[:, :, i, j].max()) < 0.999][:64]
+    od = out.detach()
+    ok = [(i, j) for i, j in cand if 2e-3 < float(od[:, :, i, j].min()) and float(od[:, :, i, j].max()) < 0.999][:64]
     assert len(ok) == 64
     fd = oracle.fd_gradient(state.cpu(), sc.targets.cpu(), sc.camera_pos.cpu(), sc.light_pos.cpu(),
                             sc.light_pow.cpu(), sc.size, ok, "log1p", h=1e-6)

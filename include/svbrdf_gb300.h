@@ -342,9 +342,11 @@ int svbrdf_desc_gemm_nt(const void* a, const void* b, float* out, int batch, int
  * stored BF16 (as svbrdf_desc_feat_loss with gram_grad = dF, which then never reaches memory);
  * partial[i] (i < svbrdf_desc_gemm_nt_feat_partials(batch, m, n)) = a fixed-order share of
  * sum d^2. a = the hook's BF16 features [batch][m][k = n], b = dG BF16 [batch][n][n]; f is the
- * same map as a (f_is_bf16) or its FP32 original; t FP32. Shapes as svbrdf_desc_gemm_nt. */
+ * same map as a or its FP32 original, t BF16 or FP32: `dtypes` bit 0 set = f is BF16, bit 1 set
+ * = t is BF16 (a BF16 hook's target features lose nothing in BF16 and cost 2 bytes fewer per
+ * element). Shapes as svbrdf_desc_gemm_nt. */
 long long svbrdf_desc_gemm_nt_feat_partials(int batch, int m, int n);
-int svbrdf_desc_gemm_nt_feat(const void* a, const void* b, const void* f, int f_is_bf16, const float* t, float coef,
+int svbrdf_desc_gemm_nt_feat(const void* a, const void* b, const void* f, int dtypes, const void* t, float coef,
                              int mask, void* g, float* partial, int batch, int m, int n, int k, int* err,
                              void* stream);
 

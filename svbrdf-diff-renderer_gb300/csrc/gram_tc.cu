@@ -224,7 +224,8 @@ gram_finish_kernel(const float* __restrict__ partial, int splits, int C, int cw,
 struct FeatEpi {
   const void* f;  // the hook's features, BF16 or FP32
   int f_bf16;
-  const float* t;  // target features
+  const void* t;  // target features, BF16 or FP32
+  int t_bf16;
   float coef;
   int mask;
   __nv_bfloat16* g;  // the loss gradient at the hook
@@ -347,8 +348,15 @@ gemm_nt_kernel(const __grid_constant__ CUtensorMap tmap_a, const __grid_constant
               const float4 v4 = __ldg(reinterpret_cast<const float4*>(reinterpret_cast<const float*>(fe.f) + off));
               fv[i][0] = v4.x; fv[i][1] = v4.y; fv[i][2] = v4.z; fv[i][3] = v4.w;
             }
-            const float4 t4 = __ldg(reinterpret_cast<const float4*>(fe.t + off));
-            tv[i][0] = t4.x; tv[i][1] = t4.y; tv[i][2] = t4.z; tv[i][3] = t4.w;
+            if (fe.t_bf16) {
+              const uint2 raw = __ldg(reinterpret_cast<const uint2*>(reinterpret_cast<const __nv_bfloat16*>(fe.t) + off));
+              const float2 a = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&raw.x));
+              const float2 c = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162*>(&raw.y));
+              tv[i][0] = a.x; tv[i][1] = a.y; tv[i][2] = c.x; tv[i][3] = c.y;
+            } else {
+              const float4 t4 = __ldg(reinterpret_cast<const float4*>(reinterpret_cast<const float*>(fe.t) + off));
+              tv[i][0] = t4.x; tv[i][1] = t4.y; tv[i][2] = t4.z; tv[i][3] = t4.w;
+            }
           }
 #pragma unroll
           for (int i = 0; i < 4; ++i) {
@@ -551,10 +559,11 @@ long long svbrdf_desc_gemm_nt_feat_partials(int batch, int m, int n) {
   return (long long)batch * (m / 128) * (n / (n >= 256 ? 256 : n)) * 4;
 }
 
-int svbrdf_desc_gemm_nt_feat(const void* a, const void* b, const void* f, int f_is_bf16, const float* t, float coef,
+int svbrdf_desc_gemm_nt_feat(const void* a, const void* b, const void* f, int dtypes, const void* t, float coef,
                              int mask, void* g, float* partial, int batch, int m, int n, int k, int* err,
                              void* stream) {
-  const gram::FeatEpi fe{f, f_is_bf16 ? 1 : 0, t, coef, mask ? 1 : 0, (__nv_bfloat16*)g, partial};
+  if (dtypes < 0 || dtypes > 3) return fail(SVBRDF_ERR_INVALID, "gemm_nt_feat: dtypes must be 0..3");
+  const gram::FeatEpi fe{f, dtypes & 1, t, (dtypes >> 1) & 1, coef, mask ? 1 : 0, (__nv_bfloat16*)g, partial};
   return gram::gemm_nt_entry<true>(a, b, nullptr, batch, m, n, k, err, fe, stream);
 }
 

@@ -173,6 +173,7 @@ class VGGDescriptor:
                 entry["dg_scale"] = (sc * (0.25 if self.downsample else 1.0)).to(self.device)
             self.params[name] = entry
         self.target = None
+        self.target16 = None  # BF16 copies of the BF16 hooks' targets (load)
 
     def bf16_weights(self):
         """{name: (weight [Cout, Cin, 3, 3] as the kernels use it, bias)} in FP32."""
@@ -265,9 +266,12 @@ class VGGDescriptor:
                 g = torch.empty(v, h, w, c, device=self.device, dtype=torch.bfloat16)
                 grads[name] = g
             if fused:
-                # the Gram gradient F dG with this hook's feature term in its epilogue
-                N.check(L.svbrdf_desc_gemm_nt_feat(ff.data_ptr(), dgram.data_ptr(), f.data_ptr(),
-                                                   int(f.dtype == torch.bfloat16), tf[k].data_ptr(), coef,
+                # the Gram gradient F dG with this hook's feature term in its epilogue; a BF16
+                # hook's targets are read in BF16 (exact: they are BF16 values)
+                t16 = self.target16[k] if getattr(self, "target16", None) else None
+                dtypes = int(f.dtype == torch.bfloat16) | (2 if t16 is not None else 0)
+                N.check(L.svbrdf_desc_gemm_nt_feat(ff.data_ptr(), dgram.data_ptr(), f.data_ptr(), dtypes,
+                                                   (t16 if t16 is not None else tf[k]).data_ptr(), coef,
                                                    int(name == last), g.data_ptr(), part.data_ptr(), v, s, c, c,
                                                    self.err.data_ptr(), st))
             else:
@@ -352,6 +356,7 @@ class VGGDescriptor:
             grams = ([gram_bf16(self._bf16_hooks(acts, hooks)[n], self.err)[0] for n in self.hooks]
                      if self.gram else [])
             self.target = ([f.float().contiguous() for f in feats], grams)
+            self.target16 = [f.contiguous() if f.dtype == torch.bfloat16 else None for f in feats]
 
     @staticmethod
     def _bf16_hooks(acts, hooks):

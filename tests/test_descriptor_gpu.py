@@ -379,13 +379,15 @@ def test_gemm_nt_tc_matches_torch(svb, cuda, b, m, n, k):
     assert rel_l2(out, ref) <= 1e-5
 
 
-@pytest.mark.parametrize("v,s,c,f32,mask", [(2, 4096, 64, True, False), (3, 1024, 128, False, True),
-                                            (2, 256, 256, False, False), (9, 1024, 512, False, True)])
-def test_gemm_nt_feat_matches_separate_kernels(svb, cuda, v, s, c, f32, mask):
+@pytest.mark.parametrize("v,s,c,f32,mask,t16", [(2, 4096, 64, True, False, False), (3, 1024, 128, False, True, False),
+                                                (2, 256, 256, False, False, True), (9, 1024, 512, False, True, False),
+                                                (9, 4096, 64, False, True, True)])
+def test_gemm_nt_feat_matches_separate_kernels(svb, cuda, v, s, c, f32, mask, t16):
     """The Gram gradient with the feature term in its epilogue (svbrdf_desc_gemm_nt_feat)
     against the two kernels it replaces: F dG in FP32 (svbrdf_desc_gemm_nt), then the feature
     term on it (svbrdf_desc_feat_loss). The BF16 gradient within one BF16 rounding, the sum of
-    squared feature differences within FP32 summation order."""
+    squared feature differences within FP32 summation order. With t16 the targets are BF16
+    values, passed to the fused kernel in BF16 and to the reference in FP32."""
     D = svb.descriptor
     L = svb._native.lib()
     st = svb._native.stream_handle(cuda)
@@ -394,6 +396,9 @@ def test_gemm_nt_feat_matches_separate_kernels(svb, cuda, v, s, c, f32, mask):
     f16 = f32v.to(torch.bfloat16)
     f = f32v if f32 else f16
     t = (f.float() + 0.3 * torch.randn(v, s, c, generator=g).to(cuda)).contiguous()
+    if t16:
+        t = t.to(torch.bfloat16).float().contiguous()  # BF16 values, held in FP32 for the reference
+    t_fused = t.to(torch.bfloat16).contiguous() if t16 else t
     dg = (torch.randn(v, c, c, generator=g) * 0.01).to(cuda, torch.bfloat16)
     dg = ((dg.float() + dg.float().transpose(1, 2)) * 0.5).to(torch.bfloat16).contiguous()
     coef = 0.013
@@ -405,8 +410,9 @@ def test_gemm_nt_feat_matches_separate_kernels(svb, cuda, v, s, c, f32, mask):
                                               g_ref.data_ptr(), p_ref.data_ptr(), f.numel(), st))
     g_out = torch.empty(v, s, c, device=cuda, dtype=torch.bfloat16)
     p_out = torch.full((int(L.svbrdf_desc_gemm_nt_feat_partials(v, s, c)),), float("nan"), device=cuda)
-    svb._native.check(L.svbrdf_desc_gemm_nt_feat(f16.data_ptr(), dg.data_ptr(), f.data_ptr(), int(not f32),
-                                                 t.data_ptr(), coef, int(mask), g_out.data_ptr(), p_out.data_ptr(), v,
+    svb._native.check(L.svbrdf_desc_gemm_nt_feat(f16.data_ptr(), dg.data_ptr(), f.data_ptr(),
+                                                 int(not f32) | (2 if t16 else 0), t_fused.data_ptr(), coef,
+                                                 int(mask), g_out.data_ptr(), p_out.data_ptr(), v,
                                                  s, c, c, err.data_ptr(), st))
     torch.cuda.synchronize()
     assert int(err.item()) == 0

@@ -331,6 +331,8 @@ def test_batched_render_loss_sums_and_conv_entries_reject_bad_arguments_on_host(
                                         None) == -2
     assert lib.svbrdf_desc_gemm_nt_feat(fake, fake, None, 1, fake, 0.1, 0, fake, fake, 1, 128, 64, 64, err,
                                         None) == -1
+    assert lib.svbrdf_desc_gemm_nt_feat(fake, fake, fake, 4, fake, 0.1, 0, fake, fake, 1, 128, 64, 64, err,
+                                        None) == -1  # dtypes 0..3
     assert lib.svbrdf_desc_gemm_nt_feat_partials(0, 128, 64) == 0
     assert lib.svbrdf_desc_gemm_nt_feat_partials(2, 256, 64) == 2 * 2 * 1 * 4
     # TF32 convolution with a workspace: the same shape rules as without

@@ -83,19 +83,23 @@ __global__ void __launch_bounds__(128) desc_conv1_fwd_kernel(const float* __rest
 #pragma unroll
   for (int ci = 0; ci < 3; ++ci)
 #pragma unroll
-    for (int ky = 0; ky < 3; ++ky)
+    for (int ky = 0; ky < 3; ++ky) {
+      // the 18 inputs of this channel and kernel row, read once for the three kx taps
+      float xr[kTile + 2];
+#pragma unroll
+      for (int i = 0; i < kTile + 2; ++i) xr[i] = s_in[ci][row + ky][i];
 #pragma unroll
       for (int kx = 0; kx < 3; ++kx) {
         const float4 w4 = reinterpret_cast<const float4*>(s_w[ci * 9 + ky * 3 + kx])[cg];
         const float2 w01 = make_float2(w4.x, w4.y), w23 = make_float2(w4.z, w4.w);
 #pragma unroll
         for (int px = 0; px < kTile; ++px) {
-          const float xv = s_in[ci][row + ky][px + kx];
-          const float2 x2 = make_float2(xv, xv);
+          const float2 x2 = make_float2(xr[px + kx], xr[px + kx]);
           acc[px][0] = __ffma2_rn(w01, x2, acc[px][0]);
           acc[px][1] = __ffma2_rn(w23, x2, acc[px][1]);
         }
       }
+    }
   if (y >= H) return;
 #pragma unroll
   for (int px = 0; px < kTile; ++px) {

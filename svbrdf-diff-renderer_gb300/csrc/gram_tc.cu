@@ -63,11 +63,15 @@ __device__ __forceinline__ void drain_loads(uint64_t* full_bar, int issued, int 
 }
 
 // grid (tiles_i * tiles_j, splits, V). Rows of the partial at or beyond C are not stored.
-template <int BN, int STAGES>
-__global__ void __launch_bounds__(kThreads, 1)
+// Z64 (C = 64): a stage is the one 64-channel box, which is B and A's first atom; A's second
+// atom (rows 64..127, never stored) is a zero atom written once per CTA, reached through A's
+// leading byte offset. One 8 KB load per 64-pixel step instead of three.
+template <int BN, int STAGES, bool Z64>
+__global__ void __launch_bounds__(kThreads)
 gram_kernel(const __grid_constant__ CUtensorMap tmap_f, float* __restrict__ partial, int S, int C, int splits,
             int pix_per_split, int* err) {
-  constexpr int A_BYTES = 2 * kAtom;  // M = 128 channels: two 64-channel atoms
+  static_assert(!Z64 || BN == 64, "Z64 is the 64-channel form");
+  constexpr int A_BYTES = Z64 ? 0 : 2 * kAtom;  // M = 128 channels: two 64-channel atoms
   constexpr int B_BYTES = (BN / 64) * kAtom;
   constexpr int STAGE = A_BYTES + B_BYTES;
   extern __shared__ uint8_t dsmem[];
@@ -85,6 +89,12 @@ gram_kernel(const __grid_constant__ CUtensorMap tmap_f, float* __restrict__ part
   const int p1 = min(S, p0 + pix_per_split);
   const int steps = p1 > p0 ? (p1 - p0) / KP : 0;
   const int row0 = v * S + p0;
+  const uint32_t zbase = base + (uint32_t)(STAGES * STAGE);  // Z64: the zero atom
+  if (Z64) {
+    for (int i = threadIdx.x; i < kAtom / 16; i += blockDim.x)
+      asm volatile("st.shared.v4.b32 [%0], {%1, %1, %1, %1};" ::"r"(zbase + 16u * i), "r"(0u) : "memory");
+    fence_async_smem();  // the zeros are read by the MMAs (async proxy); the barrier below orders them
+  }
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -116,8 +126,10 @@ gram_kernel(const __grid_constant__ CUtensorMap tmap_f, float* __restrict__ part
         const uint32_t fb = smem_u32(&full_bar[s]);
         const int row = row0 + i * KP;
         mbar_expect_tx(fb, (uint32_t)STAGE);
-        tma_2d(st, &tmap_f, i0, row, fb);
-        tma_2d(st + kAtom, &tmap_f, i0 + 64, row, fb);  // past C: zero fill
+        if (!Z64) {
+          tma_2d(st, &tmap_f, i0, row, fb);
+          tma_2d(st + kAtom, &tmap_f, i0 + 64, row, fb);  // past C: zero fill
+        }
 #pragma unroll
         for (int b = 0; b < BN / 64; ++b) tma_2d(st + A_BYTES + b * kAtom, &tmap_f, j0 + 64 * b, row, fb);
         ++issued;
@@ -134,9 +146,11 @@ gram_kernel(const __grid_constant__ CUtensorMap tmap_f, float* __restrict__ part
         fence_after();
         const uint32_t a = base + (uint32_t)(s * STAGE);
         const uint32_t b = a + A_BYTES;
+        // Z64: A's atoms are the stage's box and the zero atom (zbase - a bytes on)
+        const uint32_t a_lbo = Z64 ? zbase - a : (uint32_t)kAtom;
 #pragma unroll
         for (int k = 0; k < KP / 16; ++k)  // 16 pixels = two 8-row groups per MMA
-          mma_bf16(tmem, sw128_desc_mn(a + 2048u * k, kAtom, 1024), sw128_desc_mn(b + 2048u * k, kAtom, 1024), id,
+          mma_bf16(tmem, sw128_desc_mn(a + 2048u * k, a_lbo, 1024), sw128_desc_mn(b + 2048u * k, kAtom, 1024), id,
                    (i > 0 || k > 0) ? 1u : 0u);
         mma_commit(smem_u32(&empty_bar[s]));
       }
@@ -432,12 +446,12 @@ static int allow(K kern, size_t need, std::atomic<size_t>* have) {
   return SVBRDF_OK;
 }
 
-template <int BN, int STAGES>
+template <int BN, int STAGES, bool Z64>
 static int launch_gram(const CUtensorMap& m, float* partial, int v, int s, int c, int splits, int pps, int* err,
                        cudaStream_t st) {
   static std::atomic<size_t> have[64];
-  const size_t smem = (size_t)STAGES * (2 * kAtom + (BN / 64) * kAtom) + 1024;
-  auto kern = gram_kernel<BN, STAGES>;
+  const size_t smem = (size_t)STAGES * ((Z64 ? 0 : 2 * kAtom) + (BN / 64) * kAtom) + (Z64 ? kAtom : 0) + 1024;
+  auto kern = gram_kernel<BN, STAGES, Z64>;
   int rc = allow(kern, smem, have);
   if (rc) return rc;
   dim3 grid((unsigned)(((c + 127) / 128) * (c / BN)), (unsigned)splits, (unsigned)v);
@@ -530,9 +544,9 @@ int svbrdf_desc_gram(const void* features, float* partial, int v, int s, int c, 
   int rc = encode_2d(&m, features, (uint64_t)c, (uint64_t)v * s, 64, 64);
   if (rc) return rc;
   cudaStream_t st = (cudaStream_t)stream;
-  if (c == 64) return launch_gram<64, 6>(m, partial, v, s, c, splits, pps, err, st);
-  if (c == 128) return launch_gram<128, 5>(m, partial, v, s, c, splits, pps, err, st);
-  return launch_gram<256, 4>(m, partial, v, s, c, splits, pps, err, st);
+  if (c == 64) return launch_gram<64, 8, true>(m, partial, v, s, c, splits, pps, err, st);  // 73 KB: 3 CTAs per SM
+  if (c == 128) return launch_gram<128, 5, false>(m, partial, v, s, c, splits, pps, err, st);
+  return launch_gram<256, 4, false>(m, partial, v, s, c, splits, pps, err, st);
 }
 
 int svbrdf_desc_gram_finish(const float* partial, int splits, int v, int c, int s, const float* gram_target,

@@ -188,7 +188,7 @@ gram_kernel(const __grid_constant__ CUtensorMap tmap_f, float* __restrict__ part
 
 // grid (ceil(C / rows), V), 256 threads: `rows` = 256 / cw rows of view v per block, cw threads
 // per row (cw = C rounded up to a power of two, 32 to 256). The splits' partials of an element
-// are loaded up to eight at a time (all of them for the usual 4 to 8 splits) and added in split
+// are loaded up to eight at a time (all of them for the usual 2 to 8 splits) and added in split
 // order.
 __global__ void __launch_bounds__(256)
 gram_finish_kernel(const float* __restrict__ partial, int splits, int C, int cw, float inv_s,
@@ -522,7 +522,7 @@ int svbrdf_desc_gram_splits(int v, int s, int c) {
   const int tiles = ((c + 127) / 128) * (c / (c >= 256 ? 256 : c));
   const int steps = s / gram::KP;
   const int target = c <= 64 ? 304 : 152;
-  int splits = (target + tiles * v - 1) / (tiles * v);
+  int splits = target / (tiles * v);  // rounded down: all CTAs in the intended waves
   if (splits < 1) splits = 1;
   if (splits > steps) splits = steps;
   const int per = (steps + splits - 1) / splits;

@@ -493,6 +493,11 @@ static int gemm_nt_entry(const void* a, const void* b, float* out, int batch, in
   rc = encode_2d(&mb, b, (uint64_t)k, (uint64_t)batch * n, 64, (uint32_t)bn);
   if (rc) return rc;
   cudaStream_t st = (cudaStream_t)stream;
+  if (k <= 64 && bn == 64) {
+    // one k-step per tile: a single stage keeps the CTA at about 42 KB, five to an SM, so that
+    // more tiles' epilogues (the fused feature term, memory-latency bound) run at once
+    return launch_gemm<64, 1, FUSE>(ma, mb, out, batch, m, n, k, err, fe, st);
+  }
   if (k <= 128) {
     // one or two k-steps per tile: a 2-stage ring keeps the CTA small (49-97 KB), so several
     // CTAs share an SM and one's set-up and epilogue overlap another's loads and MMAs

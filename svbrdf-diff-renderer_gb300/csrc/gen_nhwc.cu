@@ -470,6 +470,17 @@ int nchunks(int hw, int rows) {
   const long long n = ((long long)hw + 8LL * rows - 1) / (8LL * rows);
   return (int)(n < 1 ? 1 : n > gen_nhwc::kMaxChunks ? gen_nhwc::kMaxChunks : n);
 }
+// The same, reduced so that b x chunks blocks fill whole waves of a kernel that keeps
+// `per_sm` blocks on each SM (the activation adjoint: 3), where they exceed one wave: on a
+// 256^2 map of 16 entries, 57 chunks (2 full waves) instead of 64 (2.25).
+int nchunks_waves(int hw, int rows, int b, int per_sm) {
+  const int n0 = nchunks(hw, rows);
+  const long long slots = (long long)(device_sm_count() > 0 ? device_sm_count() : 1) * per_sm;
+  const long long waves = (long long)b * n0 / slots;
+  if (waves < 1) return n0;
+  const long long n = waves * slots / b;
+  return (int)(n < 1 ? 1 : n < n0 ? n : n0);
+}
 
 }  // namespace
 
@@ -588,7 +599,7 @@ int svbrdf_gen_act_nhwc_bwd(const float* gout, const float* y, const float* d, c
   const bool v4 = c % 4 == 0 && a16(gout) && a16(y) && a16(d) && a16(bias) && a16(gy);
   const int cv = v4 ? c / 4 : c;
   if (cv > 256) return fail(SVBRDF_ERR_UNSUPPORTED, "act_nhwc_bwd: %d channels are more than one block's row", c);
-  const int nc = nchunks(hw, 256 / cv);
+  const int nc = nchunks_waves(hw, 256 / cv, b, 3);
   cudaStream_t st = (cudaStream_t)stream;
   dim3 grid((unsigned)nc, (unsigned)b);
   float* pp = gd ? part : nullptr;
@@ -614,7 +625,7 @@ int svbrdf_gen_act_scale_nhwc_bwd(const float* gout, const float* y, const float
   const bool v4 = c % 4 == 0 && a16(gout) && a16(y) && a16(d) && a16(bias) && a16(s2) && a16(gy);
   const int cv = v4 ? c / 4 : c;
   if (cv > 256) return fail(SVBRDF_ERR_UNSUPPORTED, "act_scale_nhwc_bwd: %d channels are more than one block's row", c);
-  const int nc = nchunks(hw, 256 / cv);
+  const int nc = nchunks_waves(hw, 256 / cv, b, 3);
   cudaStream_t st = (cudaStream_t)stream;
   dim3 grid((unsigned)nc, (unsigned)b);
   float* pp = gd ? part : nullptr;

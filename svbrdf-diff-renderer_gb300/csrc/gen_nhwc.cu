@@ -471,8 +471,9 @@ int nchunks(int hw, int rows) {
   return (int)(n < 1 ? 1 : n > gen_nhwc::kMaxChunks ? gen_nhwc::kMaxChunks : n);
 }
 // The same, reduced so that b x chunks blocks fill whole waves of a kernel that keeps
-// `per_sm` blocks on each SM (the activation adjoint: 3), where they exceed one wave: on a
-// 256^2 map of 16 entries, 57 chunks (2 full waves) instead of 64 (2.25).
+// `per_sm` blocks on each SM (the activation adjoint: 3, the scaling adjoint: 4), where they
+// exceed one wave: on a 256^2 map of 16 entries, 57 chunks (2 full waves of the activation
+// adjoint) instead of 64 (2.25).
 int nchunks_waves(int hw, int rows, int b, int per_sm) {
   const int n0 = nchunks(hw, rows);
   const long long slots = (long long)(device_sm_count() > 0 ? device_sm_count() : 1) * per_sm;
@@ -544,7 +545,7 @@ int svbrdf_gen_scale_nhwc_bwd(const float* g, const float* x, const float* s, fl
   const bool v4 = c % 4 == 0 && a16(g) && a16(x) && a16(gx) && a16(s);
   const int cv = v4 ? c / 4 : c;
   if (cv > 256) return fail(SVBRDF_ERR_UNSUPPORTED, "scale_nhwc_bwd: %d channels are more than one block's row", c);
-  const int nc = nchunks(hw, 256 / cv);
+  const int nc = nchunks_waves(hw, 256 / cv, b, 4);  // 64 registers: 4 blocks per SM
   cudaStream_t st = (cudaStream_t)stream;
   dim3 grid((unsigned)nc, (unsigned)b);
   if (v4) gen_nhwc::nhwc_scale_bwd_kernel<4><<<grid, 256, 0, st>>>(g, x, s, gx, part, hw, c, nc);
